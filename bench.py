@@ -1,0 +1,328 @@
+"""Benchmark: 3D Cahn-Hilliard at 256^3, FP32 device state, semi-implicit Euler.
+
+Workload (the configuration the headline metric is quoted on): periodic
+256x256x256 grid, dx = 1, c0 = U(-0.1, 0.1) i.i.d. from seed 1 (SplitMix64,
+synthetic), M = 1, gamma = 0.5, dt = 0.05, the plain splitting of
+examples/cahnHilliard/main.go:33:
+    dconc/dt = M*LAP conc^3 + m1*LAP conc + m1*gamma*LAP^2 conc,  m1 = -M.
+
+One step = one Euler step of the whole grid (pf/euler.go:16-47).
+  value : steps/s with the field resident in HBM (CUDA events on the stepping stream)
+  e2e   : steps/s through the C ABI with host buffers: every step uploads the
+          []complex128 field from pinned memory, steps once and downloads it
+  roofline : dominant kernel's algorithmic bytes / its average duration
+  cpu_baseline : the FP64 CPU oracle (a restatement of the reference's Euler
+                 step, OpenMP over all host cores) on a bounded sample
+
+--impl reference times the CPU oracle alone (the reference itself is Go +
+FFTW and cannot be built on these machines).
+Multi-GPU: the path does not shard (one grid per step); N > 1 runs N
+independent replicas, one per rank, and reports the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = ("CH steps/s at 256³ FP32 vs GPU FP64 (rel-L2≤1e-4); FFT % of HBM peak; sweep steps/s")
+UNIT = "steps/s"
+DIMS = [256, 256, 256]
+GAMMA, M, DT, SEED = 0.5, 1.0, 0.05, 1
+CH_EQ = "dconc/dt = M*LAP conc^3 + m1*LAP conc + m1*gamma*LAP^2 conc"
+FALLBACK_HBM_GBS = 6800.0
+WORKLOAD = "cahn_hilliard_3d_256cube_fp32_euler"
+
+
+def peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            d = json.load(open(p))
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def config(extra=None):
+    c = {
+        "workload": WORKLOAD,
+        "grid": "256x256x256",
+        "gamma": GAMMA,
+        "M": M,
+        "dt": DT,
+        "splitting": "examples/cahnHilliard plain (c^3 explicit, k^2 and gamma k^4 implicit)",
+        "init": "c0 = U(-0.1, 0.1), seed 1 (SplitMix64)",
+        "l2": "inputs larger than L2: state 67.6 MB + work 67.6 MB = 135 MB > 129 MB",
+    }
+    if extra:
+        c.update(extra)
+    return c
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.device)], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_oracle_step_rate(dims, max_seconds: float, max_steps: int, warmup: int = 0):
+    """Steps/s of the FP64 CPU oracle's Euler step (all host threads)."""
+    from gopf_gb300.synthetic import uniform_field
+    from oracle import oracle as O
+
+    n = int(np.prod(dims))
+    O.build()
+    threads = O.num_threads()
+    m = O.cahn_hilliard(dims, gamma=GAMMA, M=M)
+    m.set_field(0, uniform_field(SEED, n, 0.0, 0.1))
+    for _ in range(warmup):
+        m.step_euler(DT, 1)
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < max_steps:
+        m.step_euler(DT, 1)
+        steps += 1
+        if time.perf_counter() - t0 > max_seconds:
+            break
+    el = time.perf_counter() - t0
+    return steps / el, steps, el, threads
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return 0
+    budget = float(os.environ.get("GOPF_REF_SECONDS", "120"))
+    per_step = max(budget / max(args.steps + args.warmup, 1), 1.0)
+    rate, steps, el, threads = cpu_oracle_step_rate(DIMS, max_seconds=budget, max_steps=args.steps,
+                                                    warmup=min(args.warmup, 1))
+    sample = (f"{steps} Euler steps of the 256^3 grid in FP64 (complex128 fields, Z2Z FFTs, as the reference), "
+              f"{el:.1f} s; steps capped by a {budget:.0f} s budget")
+    out = {
+        "metric": METRIC, "value": rate, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+        "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": 1000.0 / rate, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config({"backend": "CPU oracle (C restatement of pf/euler.go; Go reference unbuildable here)"}),
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    del per_step
+    print(json.dumps(out))
+    return 0
+
+
+def run_gpu(args):
+    import torch
+
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    n = int(np.prod(DIMS))
+    c0 = uniform_field(SEED, n, 0.0, 0.1)
+
+    m = G.Model(DIMS, "fp32", device=local)
+    m.add_field("conc")
+    m.add_scalar("gamma", GAMMA)
+    m.add_scalar("M", M)
+    m.add_scalar("m1", -M)
+    m.add_equation(CH_EQ)
+    m.init()
+    m.set_stepper("euler", DT)
+    stream = torch.cuda.Stream()
+    m.set_stream(stream.cuda_stream)
+    m.set_option(G._lib.OPT_CHECK_FINITE, 0)
+    m.upload(0, c0)
+    mass0 = m.mass(0)
+    m.step(max(args.warmup, 3))  # warm-up (also captures the CUDA graphs)
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region ----
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        m.step(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    clocks = clk.summary()
+    per_step_ms = ms / args.steps
+    value = world * args.steps / (ms / 1000.0)
+    mass1 = m.mass(0)
+    finite = m.reduce(0, G.RED_NONFINITE) == 0
+
+    # ---- per-kernel roofline (launch by launch, events on the same stream) ----
+    prof = m.profile_step(20)
+    dom = max(prof, key=lambda p: p["ms"])
+    hbm, peak_kind = peaks()
+    achieved = dom["bytes"] / (dom["ms"] * 1e-3) / 1e9
+    step_bytes = sum(p["bytes"] for p in prof)
+
+    # ---- end to end through the C ABI with pinned host buffers ----
+    host = torch.empty(2 * n, dtype=torch.float64, pin_memory=True)
+    host.numpy()[0::2] = c0
+    host.numpy()[1::2] = 0.0
+    ptr = host.data_ptr()
+    import ctypes
+
+    L = G.load()
+    dp = ctypes.cast(ptr, ctypes.POINTER(ctypes.c_double))
+    k_e2e = max(3, min(args.steps, 50))
+    for _ in range(2):
+        m._ck(L.gopf_field_upload(m.handle, 0, dp, n))
+        m.step(1)
+        m._ck(L.gopf_field_download(m.handle, 0, dp, n))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(k_e2e):
+        m._ck(L.gopf_field_upload(m.handle, 0, dp, n))
+        m.step(1)
+        m._ck(L.gopf_field_download(m.handle, 0, dp, n))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1000.0)
+    if dist:
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e = {"value": world * k_e2e / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": 16 * n,
+           "d2h_bytes_per_step": 16 * n, "steps": k_e2e,
+           "path": "gopf_field_upload ([]complex128, pinned) + gopf_step(1) + gopf_field_download per step"}
+
+    out = None
+    if rank == 0:
+        cpu = None
+        if world == 1 and not args.no_cpu_baseline:
+            rate, steps, el, threads = cpu_oracle_step_rate(DIMS, max_seconds=args.cpu_seconds, max_steps=50)
+            cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": f"{steps} FP64 Euler steps of the 256^3 grid ({el:.1f} s) on the host cores"}
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": per_step_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config({"parallelism": "replicas" if world > 1 else "single GPU",
+                              "cell_updates_per_s": value * n,
+                              "step_bytes_algorithmic": step_bytes,
+                              "step_fraction_of_hbm": (step_bytes * value / world / 1e9) / hbm,
+                              "mass_drift_per_cell": abs(mass1 - mass0) / n, "finite": bool(finite)}),
+            "e2e": e2e,
+            "roofline": {"bound": "hbm", "kernel": dom["name"], "achieved": achieved, "peak": hbm,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                         "per_kernel": [{"name": p["name"], "ms": p["ms"], "GBps": p["bytes"] / p["ms"] / 1e6,
+                                         "bytes": p["bytes"]} for p in prof]},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": m.kernels_per_step * args.steps,
+        }
+        print(json.dumps(out))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

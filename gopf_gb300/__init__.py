@@ -1,0 +1,270 @@
+"""gopf_gb300 -- GB300-native spectral time stepping for gopf models.
+
+The product is libgopf_gpu.so (CUDA kernels for sm_103a behind the C ABI of
+include/gopf_gpu.h).  This package is the Python front end used by the tests,
+the benchmark and the adjoint harness: `Model` mirrors how a Go program
+drives pf.Model + pf.Solver (pf/model.go, pf/solver.go), one call per C-ABI
+entry point.  There is no CPU fallback: every compute call goes to the
+device library and raises GopfError when it fails.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import (  # noqa: F401
+    DER_INDICATOR,
+    DER_INDICATOR_D,
+    DER_INDICATOR_HD,
+    DER_POLY,
+    DER_PRODUCT,
+    GOPF_FP32,
+    GOPF_FP64,
+    RED_MAX,
+    RED_MIN,
+    RED_NONFINITE,
+    RED_SUM,
+    RED_SUMSQ,
+    SRC_DERIVED,
+    SRC_FIELD,
+    SRC_NONE,
+    GopfDerived,
+    GopfTerm,
+)
+
+__all__ = ["Model", "GopfError", "load", "build"]
+
+_STEPPERS = {"euler": _lib.GOPF_STEPPER_EULER, "rk4": _lib.GOPF_STEPPER_RK4}
+
+
+class GopfError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{_lib.STATUS.get(status, status)}: {message}")
+        self.status = status
+        self.message = message
+
+
+def load():
+    return _lib.load()
+
+
+def build(force: bool = False) -> str:
+    from . import build as _b
+
+    return _b.build(force=force)
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Model:
+    """A device-resident gopf model: fields, equations, stepper.
+
+    Mirrors pf.NewModel / AddField / AddScalar / RegisterFunction /
+    AddEquation / NewSolver / Solve on top of the C ABI.
+    """
+
+    def __init__(self, domain_size, precision: str = "fp32", device: int = 0):
+        self._L = _lib.load()
+        self.domain_size = [int(d) for d in domain_size]
+        self.N = int(np.prod(self.domain_size))
+        prec = {"fp32": _lib.GOPF_FP32, "fp64": _lib.GOPF_FP64}[precision]
+        self.precision = precision
+        h = ctypes.c_void_p()
+        dims = (ctypes.c_int * len(self.domain_size))(*self.domain_size)
+        rc = self._L.gopf_ctx_create(len(self.domain_size), dims, prec, device, ctypes.byref(h))
+        self._h = h
+        if rc != 0:
+            msg = self._L.gopf_last_error(h).decode() if h.value else _lib.STATUS.get(rc, "")
+            self.close()
+            raise GopfError(rc, msg)
+        self.field_names: list[str] = []
+
+    # ---- plumbing ----
+    def _ck(self, rc: int) -> None:
+        if rc != 0:
+            raise GopfError(rc, self._L.gopf_last_error(self._h).decode())
+
+    def close(self) -> None:
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._L.gopf_ctx_destroy(h)
+        self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        self._ck(self._L.gopf_set_stream(self._h, ctypes.c_void_p(stream_handle or 0)))
+
+    def set_option(self, option: int, value: int) -> None:
+        self._ck(self._L.gopf_set_option(self._h, option, value))
+
+    # ---- pf.Model mirror ----
+    def add_field(self, name: str) -> int:
+        fid = ctypes.c_int()
+        self._ck(self._L.gopf_add_field(self._h, name.encode(), ctypes.byref(fid)))
+        self.field_names.append(name)
+        return fid.value
+
+    def add_scalar(self, name: str, value) -> None:
+        v = complex(value)
+        self._ck(self._L.gopf_add_scalar(self._h, name.encode(), v.real, v.imag))
+
+    def register_function(self, name: str, kind: int, field: str, coefs=None, powers=None) -> None:
+        n = 0 if coefs is None else len(coefs)
+        c = (ctypes.c_double * max(n, 1))(*(coefs or [0.0]))
+        p = (ctypes.c_int * max(n, 1))(*(powers or [0]))
+        self._ck(self._L.gopf_register_function(self._h, name.encode(), kind, field.encode(), c, p, n))
+
+    def register_elastic(self, name: str, field: str, C, misfit) -> None:
+        c = np.ascontiguousarray(C, dtype=np.float64).reshape(81)
+        m = np.ascontiguousarray(misfit, dtype=np.float64).reshape(9)
+        self._ck(self._L.gopf_register_elastic(self._h, name.encode(), field.encode(), _dptr(c), _dptr(m)))
+
+    def register_volcons(self, name: str, field: str, indicator: str, dt: float) -> None:
+        self._ck(self._L.gopf_register_volcons(self._h, name.encode(), field.encode(), indicator.encode(), dt))
+
+    def add_equation(self, eq: str) -> None:
+        self._ck(self._L.gopf_add_equation(self._h, eq.encode()))
+
+    def init(self) -> None:
+        self._ck(self._L.gopf_init(self._h))
+
+    def summary(self, eq: int = 0):
+        ne, ni = ctypes.c_int(), ctypes.c_int()
+        self._ck(self._L.gopf_equation_summary(self._h, eq, ctypes.byref(ne), ctypes.byref(ni)))
+        return ne.value, ni.value
+
+    def terms(self):
+        n = ctypes.c_int()
+        self._ck(self._L.gopf_get_terms(self._h, None, 0, ctypes.byref(n)))
+        arr = (GopfTerm * max(n.value, 1))()
+        self._ck(self._L.gopf_get_terms(self._h, arr, n.value, ctypes.byref(n)))
+        return [dict(eq=t.eq, implicit=t.implicit, coef=t.coef, lap=t.lap, source=t.source, src_index=t.src_index)
+                for t in arr[: n.value]]
+
+    def derived(self):
+        n = ctypes.c_int()
+        self._ck(self._L.gopf_get_derived(self._h, None, 0, ctypes.byref(n)))
+        arr = (GopfDerived * max(n.value, 1))()
+        self._ck(self._L.gopf_get_derived(self._h, arr, n.value, ctypes.byref(n)))
+        return [dict(kind=d.kind, field=list(d.field[: d.nfac]), power=list(d.power[: d.nfac]),
+                     coef=list(d.coef[: d.nfac])) for d in arr[: n.value]]
+
+    def set_terms(self, nfields: int, derived, terms) -> None:
+        """Install a pre-compiled term table (dicts with the GopfDerived/GopfTerm fields)."""
+        D = (GopfDerived * max(len(derived), 1))()
+        for i, d in enumerate(derived):
+            D[i].kind = d["kind"]
+            D[i].nfac = len(d["field"])
+            for j, f in enumerate(d["field"]):
+                D[i].field[j] = f
+                D[i].power[j] = d.get("power", [1] * len(d["field"]))[j]
+                D[i].coef[j] = d.get("coef", [1.0] * len(d["field"]))[j]
+        T = (GopfTerm * max(len(terms), 1))()
+        for i, t in enumerate(terms):
+            T[i].eq = t.get("eq", 0)
+            T[i].implicit = int(t.get("implicit", 0))
+            T[i].coef = t["coef"]
+            T[i].lap = t.get("lap", 0)
+            T[i].source = t.get("source", SRC_NONE)
+            T[i].src_index = t.get("src_index", 0)
+        self._ck(self._L.gopf_set_terms(self._h, nfields, D, len(derived), T, len(terms)))
+
+    # ---- pf.TimeStepper mirror ----
+    def set_stepper(self, name: str, dt: float) -> None:
+        self._ck(self._L.gopf_set_stepper(self._h, _STEPPERS[name], dt))
+
+    def upload(self, field: int, data) -> None:
+        a = np.ascontiguousarray(np.asarray(data).reshape(-1).astype(np.complex128))
+        self._ck(self._L.gopf_field_upload(self._h, field, _dptr(a.view(np.float64)), a.size))
+
+    def upload_real(self, field: int, data) -> None:
+        a = np.ascontiguousarray(np.asarray(data, dtype=np.float64).reshape(-1))
+        self._ck(self._L.gopf_field_upload_real(self._h, field, _dptr(a), a.size))
+
+    def download(self, field: int = 0) -> np.ndarray:
+        out = np.empty(self.N, dtype=np.complex128)
+        self._ck(self._L.gopf_field_download(self._h, field, _dptr(out.view(np.float64)), self.N))
+        return out
+
+    def download_real(self, field: int = 0) -> np.ndarray:
+        out = np.empty(self.N, dtype=np.float64)
+        self._ck(self._L.gopf_field_download_real(self._h, field, _dptr(out), self.N))
+        return out
+
+    def step(self, nsteps: int) -> None:
+        self._ck(self._L.gopf_step(self._h, int(nsteps)))
+
+    def synchronize(self) -> None:
+        self._ck(self._L.gopf_synchronize(self._h))
+
+    @property
+    def time(self) -> float:
+        t = ctypes.c_double()
+        self._ck(self._L.gopf_get_time(self._h, ctypes.byref(t)))
+        return t.value
+
+    @property
+    def current_step(self) -> int:
+        s = ctypes.c_longlong()
+        self._ck(self._L.gopf_get_step(self._h, ctypes.byref(s)))
+        return s.value
+
+    def reduce(self, field: int, what: int) -> float:
+        out = ctypes.c_double()
+        self._ck(self._L.gopf_reduce(self._h, field, what, ctypes.byref(out)))
+        return out.value
+
+    def mass(self, field: int = 0) -> float:
+        return self.reduce(field, RED_SUM)
+
+    # ---- pfutil.FourierTransform mirror ----
+    def fft(self, data, sign: int = -1) -> np.ndarray:
+        a = np.ascontiguousarray(np.asarray(data, dtype=np.complex128).reshape(-1)).copy()
+        self._ck(self._L.gopf_fft(self._h, sign, _dptr(a.view(np.float64)), a.size))
+        return a
+
+    def freq(self, i: int) -> np.ndarray:
+        out = (ctypes.c_double * 3)()
+        self._ck(self._L.gopf_freq(self._h, i, out))
+        return np.array(out[: len(self.domain_size)])
+
+    def conjugate_node(self, i: int) -> int:
+        return int(self._L.gopf_conjugate_node(self._h, i))
+
+    @property
+    def device_bytes(self) -> int:
+        b = ctypes.c_size_t()
+        self._ck(self._L.gopf_device_bytes(self._h, ctypes.byref(b)))
+        return b.value
+
+    def profile_step(self, nsteps: int):
+        """Per-kernel average device time (ms) and algorithmic bytes of one Euler step."""
+        ms = (ctypes.c_double * 16)()
+        by = (ctypes.c_double * 16)()
+        n = ctypes.c_int()
+        self._ck(self._L.gopf_profile_step(self._h, int(nsteps), ms, by, 16, ctypes.byref(n)))
+        out = []
+        buf = ctypes.create_string_buffer(64)
+        for k in range(n.value):
+            self._ck(self._L.gopf_profile_slot_name(self._h, k, buf, 64))
+            out.append(dict(name=buf.value.decode(), ms=ms[k], bytes=by[k]))
+        return out
+
+    @property
+    def kernels_per_step(self) -> int:
+        n = ctypes.c_int()
+        self._ck(self._L.gopf_kernels_per_step(self._h, ctypes.byref(n)))
+        return n.value

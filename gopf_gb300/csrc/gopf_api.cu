@@ -1,0 +1,985 @@
+// gopf_api.cu -- C ABI of the GB300 spectral stepper: contexts, device
+// buffers, plans, the step sequence and its CUDA-graph replay.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gopf_ctx.h"
+#include "gopf_kernels.cuh"
+
+using namespace gopf;
+
+// ------------------------------------------------------------------
+// errors
+// ------------------------------------------------------------------
+
+int gopf_fail(gopf_ctx *ctx, int code, const std::string &msg)
+{
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+static int cuda_fail(gopf_ctx *ctx, cudaError_t e, const char *where)
+{
+    std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+    return gopf_fail(ctx, e == cudaErrorMemoryAllocation ? GOPF_ERR_OOM : GOPF_ERR_CUDA, m);
+}
+
+#define CK(call)                                                                                                       \
+    do {                                                                                                               \
+        cudaError_t e_ = (call);                                                                                       \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);                                                       \
+    } while (0)
+
+extern "C" const char *gopf_status_string(int s)
+{
+    switch (s) {
+    case GOPF_OK: return "ok";
+    case GOPF_ERR_ARG: return "bad argument";
+    case GOPF_ERR_CUDA: return "CUDA error";
+    case GOPF_ERR_OOM: return "out of device memory";
+    case GOPF_ERR_NAN: return "non-finite value in field";
+    case GOPF_ERR_TIMEOUT: return "device wait timed out";
+    case GOPF_ERR_UNSUPPORTED: return "unsupported on the device";
+    case GOPF_ERR_STATE: return "call out of order";
+    case GOPF_ERR_PARSE: return "equation parse error";
+    default: return "unknown status";
+    }
+}
+
+extern "C" const char *gopf_last_error(const gopf_ctx *ctx)
+{
+    return ctx ? ctx->err.c_str() : "null context";
+}
+
+// ------------------------------------------------------------------
+// plans and twiddle tables
+// ------------------------------------------------------------------
+
+static bool make_plan(int n, int tws, LinePlan &pl)
+{
+    memset(&pl, 0, sizeof(pl));
+    pl.n = n;
+    if (n < 1) return false;
+    int m = n, a = 0, b = 0;
+    while (m % 2 == 0) { m /= 2; ++a; }
+    while (m % 3 == 0) { m /= 3; ++b; }
+    if (m != 1) return false;
+    std::vector<int> rad;
+    for (int i = 0; i < b; ++i) rad.push_back(3);
+    if (a % 4) rad.push_back(1 << (a % 4));
+    for (int i = 0; i < a / 4; ++i) rad.push_back(16);
+    if ((int)rad.size() > GOPF_MAX_STAGES) return false;
+    pl.nst = (int)rad.size();
+    int ns = 1;
+    for (int s = 0; s < pl.nst; ++s) {
+        pl.rad[s] = rad[s];
+        pl.ns[s] = ns;
+        pl.nsmask[s] = ((ns & (ns - 1)) == 0) ? ns - 1 : -1;
+        pl.twmul[s] = (int)((long long)n * tws / ((long long)ns * rad[s]));
+        ns *= rad[s];
+    }
+    return true;
+}
+
+template <typename R> static int upload_table(gopf_ctx *ctx, int n, void **dptr)
+{
+    typedef typename VecOf<R>::type V;
+    std::vector<V> h(n);
+    for (int t = 0; t < n; ++t) {
+        long double ang = -2.0L * 3.141592653589793238462643383279502884L * (long double)t / (long double)n;
+        h[t].x = (R)cosl(ang);
+        h[t].y = (R)sinl(ang);
+    }
+    CK(cudaMalloc(dptr, sizeof(V) * n));
+    ctx->dev_bytes += sizeof(V) * n;
+    CK(cudaMemcpy(*dptr, h.data(), sizeof(V) * n, cudaMemcpyHostToDevice));
+    return GOPF_OK;
+}
+
+// ------------------------------------------------------------------
+// small elementwise kernels
+// ------------------------------------------------------------------
+
+template <typename R>
+__global__ void k_c128_to_real(const double2 *__restrict__ in, R *__restrict__ out, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = (R)in[i].x;
+}
+
+template <typename R>
+__global__ void k_real_to_c128(const R *__restrict__ in, double2 *__restrict__ out, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = make_double2((double)in[i], 0.0);
+}
+
+template <typename R>
+__global__ void k_double_to_real(const double *__restrict__ in, R *__restrict__ out, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = (R)in[i];
+}
+
+template <typename R>
+__global__ void k_real_to_double(const R *__restrict__ in, double *__restrict__ out, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
+}
+
+// Final cross-block reduction with Neumaier compensation (one block).
+__global__ void k_finish_reduce(const double *__restrict__ part, int nblocks, double *__restrict__ out)
+{
+    __shared__ double s_sum[256], s_c[256], s_min[256], s_max[256], s_sq[256], s_sqc[256], s_nf[256];
+    double sum = 0, c = 0, sq = 0, sqc = 0, mn = INFINITY, mx = -INFINITY, nf = 0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+        const double *p = part + (long long)b * RED_SLOTS;
+        double v = p[RED_SUM];
+        double t = sum + v;
+        c += (fabs(sum) >= fabs(v)) ? (sum - t) + v : (v - t) + sum;
+        sum = t;
+        v = p[RED_SUMSQ];
+        t = sq + v;
+        sqc += (fabs(sq) >= fabs(v)) ? (sq - t) + v : (v - t) + sq;
+        sq = t;
+        mn = fmin(mn, p[RED_MIN]);
+        mx = fmax(mx, p[RED_MAX]);
+        nf += p[RED_NONFINITE];
+    }
+    s_sum[threadIdx.x] = sum;
+    s_c[threadIdx.x] = c;
+    s_sq[threadIdx.x] = sq;
+    s_sqc[threadIdx.x] = sqc;
+    s_min[threadIdx.x] = mn;
+    s_max[threadIdx.x] = mx;
+    s_nf[threadIdx.x] = nf;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double S = 0, Cc = 0, Q = 0, Qc = 0, MN = INFINITY, MX = -INFINITY, NF = 0;
+        for (int i = 0; i < (int)blockDim.x; ++i) {
+            double v = s_sum[i], t = S + v;
+            Cc += (fabs(S) >= fabs(v)) ? (S - t) + v : (v - t) + S;
+            S = t;
+            Cc += s_c[i];
+            v = s_sq[i];
+            t = Q + v;
+            Qc += (fabs(Q) >= fabs(v)) ? (Q - t) + v : (v - t) + Q;
+            Q = t;
+            Qc += s_sqc[i];
+            MN = fmin(MN, s_min[i]);
+            MX = fmax(MX, s_max[i]);
+            NF += s_nf[i];
+        }
+        out[RED_SUM] = S + Cc;
+        out[RED_SUMSQ] = Q + Qc;
+        out[RED_MIN] = MN;
+        out[RED_MAX] = MX;
+        out[RED_NONFINITE] = NF;
+    }
+}
+
+static unsigned ew_blocks(long long n)
+{
+    long long b = (n + 255) / 256;
+    return (unsigned)std::min<long long>(b, 152 * 16);
+}
+
+// ------------------------------------------------------------------
+// context
+// ------------------------------------------------------------------
+
+static int set_device(gopf_ctx *ctx)
+{
+    if (ctx->device < 0)
+        return gopf_fail(ctx, GOPF_ERR_STATE, "host-only context (device < 0): model definition only");
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
+    return GOPF_OK;
+}
+
+static int check_len(int n, const char *what, gopf_ctx *ctx)
+{
+    LinePlan p;
+    if (!make_plan(n, 1, p))
+        return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED,
+                         std::string(what) + " length " + std::to_string(n) + " must be 2^a*3^b");
+    return GOPF_OK;
+}
+
+template <typename R> static int ctx_alloc(gopf_ctx *ctx)
+{
+    typedef typename VecOf<R>::type V;
+    const Geom &g = ctx->g;
+    CK(cudaMalloc(&ctx->d_state, sizeof(V) * g.C));
+    CK(cudaMalloc(&ctx->d_T, sizeof(V) * g.C));
+    CK(cudaMalloc(&ctx->d_real, sizeof(R) * g.N));
+    CK(cudaMalloc(&ctx->d_c128, sizeof(double2) * g.N));
+    ctx->dev_bytes += 2 * sizeof(V) * g.C + sizeof(R) * g.N + sizeof(double2) * g.N;
+    ctx->nred_blocks = ((g.Y + ctx->LBx - 1) / ctx->LBx) * g.Z;
+    CK(cudaMalloc(&ctx->d_red, sizeof(double) * RED_SLOTS * ctx->nred_blocks));
+    CK(cudaMalloc(&ctx->d_redout, sizeof(double) * RED_SLOTS));
+    ctx->dev_bytes += sizeof(double) * RED_SLOTS * (ctx->nred_blocks + 1);
+    CK(cudaMemset(ctx->d_state, 0, sizeof(V) * g.C));
+    CK(cudaMemset(ctx->d_T, 0, sizeof(V) * g.C));
+    int rc;
+    if ((rc = upload_table<R>(ctx, g.X, &ctx->d_twX))) return rc;
+    if ((rc = upload_table<R>(ctx, g.Y, &ctx->d_twY))) return rc;
+    if (g.Z > 1 && (rc = upload_table<R>(ctx, g.Z, &ctx->d_twZ))) return rc;
+    return GOPF_OK;
+}
+
+static void ctx_free(gopf_ctx *ctx)
+{
+    if (ctx->gexec1) cudaGraphExecDestroy(ctx->gexec1);
+    if (ctx->gexecK) cudaGraphExecDestroy(ctx->gexecK);
+    void *ptrs[] = {ctx->d_state, ctx->d_T, ctx->d_real, ctx->d_c128, ctx->d_red, ctx->d_redout,
+                    ctx->d_twX,   ctx->d_twY, ctx->d_twZ};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    for (int i = 1; i < GOPF_MAX_GROUPS; ++i)
+        if (ctx->d_U[i]) cudaFree(ctx->d_U[i]);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+}
+
+extern "C" int gopf_ctx_create(int ndim, const int *domain_size, int precision, int device, gopf_ctx **out)
+{
+    if (!out) return GOPF_ERR_ARG;
+    *out = nullptr;
+    if ((ndim != 2 && ndim != 3) || !domain_size) return GOPF_ERR_ARG;
+    if (precision != GOPF_FP32 && precision != GOPF_FP64) return GOPF_ERR_ARG;
+    gopf_ctx *ctx = new gopf_ctx();
+    ctx->device = device;
+    ctx->ndim = ndim;
+    ctx->prec = precision;
+    for (int d = 0; d < ndim; ++d) {
+        if (domain_size[d] < 1) { delete ctx; return GOPF_ERR_ARG; }
+        ctx->dims[d] = domain_size[d];
+    }
+    if (ndim == 3 && !(domain_size[0] == domain_size[1] && domain_size[1] == domain_size[2])) {
+        // pfutil/fftWrap.go plans FFTW over [n0][n1][n2] while Freq/Pos use depth-major
+        // node order; the two agree only for cubes, so only cubes are accepted in 3D.
+        ctx->err = "3D domains must be cubic (the reference's FFT and Freq conventions agree only for cubes)";
+        *out = ctx;
+        return GOPF_ERR_UNSUPPORTED;
+    }
+    Geom &g = ctx->g;
+    g.X = ctx->dims[1];
+    g.Y = ctx->dims[0];
+    g.Z = (ndim == 3) ? ctx->dims[2] : 1;
+    *out = ctx;
+    if (g.X % 2 != 0) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "the column count (domainSize[1]) must be even");
+    int rc;
+    if ((rc = check_len(g.X / 2, "half column", ctx))) return rc;
+    if ((rc = check_len(g.Y, "row", ctx))) return rc;
+    if ((rc = check_len(g.Z, "depth", ctx))) return rc;
+    g.H = g.X / 2;
+    g.KX = g.H + 1;
+    g.S = (long long)g.KX * g.Y;
+    g.C = g.S * g.Z;
+    g.N = (long long)g.X * g.Y * g.Z;
+    const int vb = (precision == GOPF_FP32) ? 8 : 16;
+    ctx->LBx = lb_for(g.H, vb);
+    ctx->LBy = lb_for(g.Y, vb);
+    ctx->LBz = lb_for(g.Z, vb);
+    if ((long long)ctx->LBx * g.H > 4096 || (long long)ctx->LBy * g.Y > 4096 || (long long)ctx->LBz * g.Z > 4096)
+        return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "axis longer than 1024 (2048 columns) is not supported");
+    make_plan(g.H, 2, ctx->planH);
+    make_plan(g.Y, 1, ctx->planY);
+    make_plan(g.Z, 1, ctx->planZ);
+    if (device < 0) return GOPF_OK; // host-only: equations can be defined and compiled, nothing runs
+    if ((rc = set_device(ctx))) return rc;
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamCreate");
+    ctx->stream = ctx->own_stream;
+    rc = (precision == GOPF_FP32) ? ctx_alloc<float>(ctx) : ctx_alloc<double>(ctx);
+    return rc;
+}
+
+extern "C" int gopf_ctx_destroy(gopf_ctx *ctx)
+{
+    if (!ctx) return GOPF_ERR_ARG;
+    if (ctx->device >= 0) {
+        cudaSetDevice(ctx->device);
+        if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+        ctx_free(ctx);
+    }
+    delete ctx;
+    return GOPF_OK;
+}
+
+static void invalidate_graphs(gopf_ctx *ctx)
+{
+    if (ctx->gexec1) cudaGraphExecDestroy(ctx->gexec1);
+    if (ctx->gexecK) cudaGraphExecDestroy(ctx->gexecK);
+    ctx->gexec1 = ctx->gexecK = nullptr;
+    ctx->graphs_dirty = true;
+}
+
+extern "C" int gopf_set_stream(gopf_ctx *ctx, void *s)
+{
+    if (!ctx) return GOPF_ERR_ARG;
+    int rc;
+    if ((rc = set_device(ctx))) return rc;
+    ctx->stream = s ? (cudaStream_t)s : ctx->own_stream;
+    return GOPF_OK;
+}
+
+extern "C" int gopf_set_option(gopf_ctx *ctx, int opt, long long v)
+{
+    if (!ctx) return GOPF_ERR_ARG;
+    if (opt == GOPF_OPT_CHECK_FINITE) ctx->check_finite = (int)(v != 0);
+    else if (opt == GOPF_OPT_USE_GRAPHS) ctx->use_graphs = (int)(v != 0);
+    else return gopf_fail(ctx, GOPF_ERR_ARG, "unknown option");
+    return GOPF_OK;
+}
+
+// ------------------------------------------------------------------
+// model compilation: term table -> device tables
+// ------------------------------------------------------------------
+
+// Expand a derived field of field 0 into polynomial terms (coef, power).
+static int derived_poly(gopf_ctx *ctx, const gopf_derived &d, std::vector<std::pair<double, int>> &out)
+{
+    out.clear();
+    switch (d.kind) {
+    case GOPF_DER_PRODUCT: {
+        int p = 0;
+        for (int j = 0; j < d.nfac; ++j) {
+            if (d.field[j] != 0)
+                return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "derived fields of several fields are not on the device yet");
+            if (d.power[j] < 0) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "negative powers are not on the device");
+            p += d.power[j];
+        }
+        out.push_back({1.0, p});
+        break;
+    }
+    case GOPF_DER_POLY:
+        for (int j = 0; j < d.nfac; ++j) {
+            if (d.field[j] != 0)
+                return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "derived fields of several fields are not on the device yet");
+            if (d.power[j] < 0) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "negative powers are not on the device");
+            out.push_back({d.coef[j], d.power[j]});
+        }
+        break;
+    case GOPF_DER_INDICATOR: out = {{3.0, 2}, {-2.0, 3}}; break;
+    case GOPF_DER_INDICATOR_D: out = {{6.0, 1}, {-6.0, 2}}; break;
+    case GOPF_DER_INDICATOR_HD: out = {{18.0, 3}, {-30.0, 4}, {12.0, 5}}; break;
+    default: return gopf_fail(ctx, GOPF_ERR_ARG, "unknown derived-field kind");
+    }
+    return GOPF_OK;
+}
+
+int gopf_compile_model(gopf_ctx *ctx)
+{
+    if (ctx->nfields != 1)
+        return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "the device stepper supports single-field models");
+    if (!ctx->specials.empty())
+        return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "user-defined terms are not on the device yet");
+    PwTable pw;
+    memset(&pw, 0, sizeof(pw));
+    UpdTable u;
+    memset(&u, 0, sizeof(u));
+    int maxp = 0;
+    for (const gopf_term &t : ctx->terms) {
+        if (t.eq != 0) return gopf_fail(ctx, GOPF_ERR_ARG, "term refers to an equation that does not exist");
+        if (t.lap < 0 || t.lap >= GOPF_MAX_IMP) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "LAP power out of range");
+        if (t.implicit) {
+            u.imp[t.lap] += t.coef;
+            maxp = std::max(maxp, t.lap + 1);
+            continue;
+        }
+        std::vector<std::pair<double, int>> poly;
+        if (t.source == GOPF_SRC_FIELD) {
+            if (t.src_index != 0) return gopf_fail(ctx, GOPF_ERR_ARG, "bad field index");
+            poly = {{1.0, 1}};
+        } else if (t.source == GOPF_SRC_DERIVED) {
+            if (t.src_index < 0 || t.src_index >= (int)ctx->der.size())
+                return gopf_fail(ctx, GOPF_ERR_ARG, "bad derived-field index");
+            int rc = derived_poly(ctx, ctx->der[t.src_index], poly);
+            if (rc) return rc;
+        } else {
+            return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED,
+                             "a term without a field (constant in k space) has no device implementation");
+        }
+        int grp = -1;
+        for (int b = 0; b < u.ngrp; ++b)
+            if (u.glap[b] == t.lap) grp = b;
+        if (grp < 0) {
+            if (u.ngrp >= GOPF_MAX_GROUPS) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "too many distinct LAP powers");
+            grp = u.ngrp++;
+            u.glap[grp] = t.lap;
+        }
+        for (auto &pc : poly) {
+            // merge equal powers
+            int at = -1;
+            for (int q = 0; q < pw.nterm[grp]; ++q)
+                if (pw.pw[grp][q] == pc.second) at = q;
+            if (at < 0) {
+                if (pw.nterm[grp] >= GOPF_MAX_POLY) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "polynomial too long");
+                at = pw.nterm[grp]++;
+                pw.pw[grp][at] = pc.second;
+                pw.coef[grp][at] = 0.0;
+            }
+            pw.coef[grp][at] += t.coef * pc.first;
+        }
+    }
+    pw.ngrp = u.ngrp;
+    u.nimp = maxp;
+    ctx->pw = pw;
+    ctx->upd = u;
+    ctx->ngroups = u.ngrp;
+    // work arrays for groups beyond the first
+    const size_t vb = (ctx->prec == GOPF_FP32) ? sizeof(float2) : sizeof(double2);
+    for (int b = 1; b < std::max(1, u.ngrp); ++b) {
+        if (ctx->device >= 0 && !ctx->d_U[b]) {
+            cudaError_t e = cudaMalloc(&ctx->d_U[b], vb * ctx->g.C);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(group buffer)");
+            ctx->dev_bytes += vb * ctx->g.C;
+        }
+    }
+    ctx->initialised = true;
+    invalidate_graphs(ctx);
+    return GOPF_OK;
+}
+
+extern "C" int gopf_set_terms(gopf_ctx *ctx, int nfields, const gopf_derived *derived, int nderived,
+                              const gopf_term *terms, int nterms)
+{
+    if (!ctx || nfields < 1 || nderived < 0 || nterms < 0 || (nderived && !derived) || (nterms && !terms))
+        return gopf_fail(ctx, GOPF_ERR_ARG, "bad term table");
+    int rc;
+    if (ctx->device >= 0 && (rc = set_device(ctx))) return rc;
+    ctx->nfields = nfields;
+    ctx->der.assign(derived, derived + nderived);
+    ctx->terms.assign(terms, terms + nterms);
+    ctx->specials.clear();
+    return gopf_compile_model(ctx);
+}
+
+extern "C" int gopf_get_terms(gopf_ctx *ctx, gopf_term *terms, int capacity, int *nterms)
+{
+    if (!ctx || !nterms) return GOPF_ERR_ARG;
+    *nterms = (int)ctx->terms.size();
+    for (int i = 0; i < *nterms && i < capacity; ++i) terms[i] = ctx->terms[i];
+    return GOPF_OK;
+}
+
+extern "C" int gopf_get_derived(gopf_ctx *ctx, gopf_derived *der, int capacity, int *nder)
+{
+    if (!ctx || !nder) return GOPF_ERR_ARG;
+    *nder = (int)ctx->der.size();
+    for (int i = 0; i < *nder && i < capacity; ++i) der[i] = ctx->der[i];
+    return GOPF_OK;
+}
+
+extern "C" int gopf_equation_summary(gopf_ctx *ctx, int eq, int *ne, int *ni)
+{
+    if (!ctx || !ne || !ni) return GOPF_ERR_ARG;
+    *ne = *ni = 0;
+    for (const gopf_term &t : ctx->terms)
+        if (t.eq == eq) (t.implicit ? *ni : *ne) += 1;
+    for (const gopf_special &s : ctx->specials)
+        if (s.eq == eq) *ne += 1;
+    return GOPF_OK;
+}
+
+extern "C" int gopf_set_stepper(gopf_ctx *ctx, int stepper, double dt)
+{
+    if (!ctx) return GOPF_ERR_ARG;
+    if (stepper != GOPF_STEPPER_EULER && stepper != GOPF_STEPPER_RK4)
+        return gopf_fail(ctx, GOPF_ERR_ARG, "unknown stepper");
+    if (!(dt > 0.0) || !std::isfinite(dt)) return gopf_fail(ctx, GOPF_ERR_ARG, "dt must be positive");
+    ctx->stepper = stepper;
+    ctx->dt = dt;
+    invalidate_graphs(ctx);
+    return GOPF_OK;
+}
+
+// ------------------------------------------------------------------
+// pass helpers
+// ------------------------------------------------------------------
+
+template <typename R> static XPassArgs<R> xargs(gopf_ctx *ctx)
+{
+    typedef typename VecOf<R>::type V;
+    XPassArgs<R> a;
+    memset(&a, 0, sizeof(a));
+    a.g = ctx->g;
+    a.planH = ctx->planH;
+    a.twX = (const V *)ctx->d_twX;
+    return a;
+}
+
+template <typename R> static PassArgs<R> pargs(gopf_ctx *ctx, bool zaxis)
+{
+    typedef typename VecOf<R>::type V;
+    PassArgs<R> a;
+    memset(&a, 0, sizeof(a));
+    a.g = ctx->g;
+    a.plan = zaxis ? ctx->planZ : ctx->planY;
+    a.tw = (const V *)(zaxis ? ctx->d_twZ : ctx->d_twY);
+    return a;
+}
+
+static void prof_mark(gopf_ctx *ctx)
+{
+    if (ctx->prof_events && ctx->prof_next < ctx->prof_events->size())
+        cudaEventRecord((*ctx->prof_events)[ctx->prof_next++], ctx->stream);
+}
+
+#define LK(call)                                                                                                       \
+    do {                                                                                                               \
+        cudaError_t e_ = (call);                                                                                       \
+        if (e_ != cudaSuccess) return e_;                                                                              \
+        prof_mark(ctx);                                                                                                \
+    } while (0)
+
+// From T (after the inverse y/z passes) produce real rows and/or reductions.
+template <typename R> static cudaError_t enqueue_xpass_out(gopf_ctx *ctx, R *rout, double *red)
+{
+    XPassArgs<R> xa = xargs<R>(ctx);
+    xa.in_mode = XIN_SPECTRAL;
+    xa.in = (const typename VecOf<R>::type *)ctx->d_T;
+    xa.rout = rout;
+    xa.red = red;
+    xa.ngrp_out = 0;
+    return launch_xpass<R>(xa, ctx->LBx, ctx->stream);
+}
+
+// Load real field d_real into the state: c-hat = FFT(c), T = partial inverse of c-hat/N.
+template <typename R> static cudaError_t enqueue_load_state(gopf_ctx *ctx)
+{
+    typedef typename VecOf<R>::type V;
+    XPassArgs<R> xa = xargs<R>(ctx);
+    xa.in_mode = XIN_REAL;
+    xa.rin = (const R *)ctx->d_real;
+    xa.out[0] = (V *)ctx->d_T;
+    xa.ngrp_out = 1;
+    xa.identity = 1;
+    LK(launch_xpass<R>(xa, ctx->LBx, ctx->stream));
+    UpdTable u;
+    memset(&u, 0, sizeof(u));
+    u.invN = 1.0 / (double)ctx->g.N;
+    if (ctx->g.Z > 1) {
+        PassArgs<R> pa = pargs<R>(ctx, false);
+        pa.mode = PM_FWD;
+        pa.buf[0] = (V *)ctx->d_T;
+        pa.nbuf = 1;
+        LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+        PassArgs<R> sa = pargs<R>(ctx, true);
+        sa.mode = PM_INIT;
+        sa.buf[0] = (V *)ctx->d_T;
+        sa.nbuf = 1;
+        sa.state = (V *)ctx->d_state;
+        sa.tout = (V *)ctx->d_T;
+        sa.upd = u;
+        LK(launch_spass<R>(sa, ctx->LBz, ctx->stream));
+        pa.mode = PM_INV;
+        LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+    } else {
+        PassArgs<R> pa = pargs<R>(ctx, false);
+        pa.mode = PM_INIT;
+        pa.buf[0] = (V *)ctx->d_T;
+        pa.nbuf = 1;
+        pa.state = (V *)ctx->d_state;
+        pa.tout = (V *)ctx->d_T;
+        pa.upd = u;
+        LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+    }
+    return cudaSuccess;
+}
+
+// One Euler step (pf/euler.go:16-47) of a single-field model.
+template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx)
+{
+    typedef typename VecOf<R>::type V;
+    const int G = ctx->ngroups;
+    V *U[GOPF_MAX_GROUPS];
+    U[0] = (V *)ctx->d_T;
+    for (int b = 1; b < GOPF_MAX_GROUPS; ++b) U[b] = (V *)ctx->d_U[b];
+    UpdTable u = ctx->upd;
+    u.dt = ctx->dt;
+    u.invN = 1.0 / (double)ctx->g.N;
+    if (G > 0) {
+        XPassArgs<R> xa = xargs<R>(ctx);
+        xa.in_mode = XIN_SPECTRAL;
+        xa.in = (const V *)ctx->d_T;
+        for (int b = 0; b < G; ++b) xa.out[b] = U[b];
+        xa.ngrp_out = G;
+        xa.pw = ctx->pw;
+        LK(launch_xpass<R>(xa, ctx->LBx, ctx->stream));
+    }
+    // with no explicit term the last pass still needs T = partial transform of c-hat/N;
+    // it reads c-hat through the update (identity contribution when ngrp == 0)
+    const int nb = std::max(G, 1);
+    if (ctx->g.Z > 1) {
+        PassArgs<R> pa = pargs<R>(ctx, false);
+        if (G > 0) {
+            pa.mode = PM_FWD;
+            for (int b = 0; b < G; ++b) pa.buf[b] = U[b];
+            pa.nbuf = G;
+            LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+        }
+        PassArgs<R> sa = pargs<R>(ctx, true);
+        sa.mode = PM_FUSED;
+        for (int b = 0; b < nb; ++b) sa.buf[b] = U[b];
+        sa.nbuf = nb;
+        sa.state = (V *)ctx->d_state;
+        sa.tout = (V *)ctx->d_T;
+        sa.upd = u;
+        LK(launch_spass<R>(sa, ctx->LBz, ctx->stream));
+        PassArgs<R> ia = pargs<R>(ctx, false);
+        ia.mode = PM_INV;
+        ia.buf[0] = (V *)ctx->d_T;
+        ia.nbuf = 1;
+        LK(launch_cpass<R>(ia, ctx->LBy, ctx->stream));
+    } else {
+        PassArgs<R> pa = pargs<R>(ctx, false);
+        pa.mode = PM_FUSED;
+        for (int b = 0; b < nb; ++b) pa.buf[b] = U[b];
+        pa.nbuf = nb;
+        pa.state = (V *)ctx->d_state;
+        pa.tout = (V *)ctx->d_T;
+        pa.upd = u;
+        LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+    }
+    return cudaSuccess;
+}
+
+template <typename R> static cudaError_t enqueue_steps(gopf_ctx *ctx, int n)
+{
+    for (int i = 0; i < n; ++i) LK(enqueue_euler<R>(ctx));
+    return cudaSuccess;
+}
+
+static cudaError_t enqueue_steps_any(gopf_ctx *ctx, int n)
+{
+    return (ctx->prec == GOPF_FP32) ? enqueue_steps<float>(ctx, n) : enqueue_steps<double>(ctx, n);
+}
+
+static int capture_graph(gopf_ctx *ctx, int nsteps, cudaGraphExec_t *exec)
+{
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = enqueue_steps_any(ctx, nsteps);
+    cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &graph);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "capture");
+    if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
+    return GOPF_OK;
+}
+
+// ------------------------------------------------------------------
+// field transfer
+// ------------------------------------------------------------------
+
+static int require_ready(gopf_ctx *ctx, int field)
+{
+    if (field < 0 || (ctx->nfields > 0 && field >= ctx->nfields) || (ctx->nfields == 0 && field != 0))
+        return gopf_fail(ctx, GOPF_ERR_ARG, "bad field id");
+    return GOPF_OK;
+}
+
+template <typename R> static int upload_impl(gopf_ctx *ctx, const double *data, bool complex_in)
+{
+    const long long N = ctx->g.N;
+    if (complex_in) {
+        CK(cudaMemcpyAsync(ctx->d_c128, data, sizeof(double2) * N, cudaMemcpyHostToDevice, ctx->stream));
+        k_c128_to_real<R><<<ew_blocks(N), 256, 0, ctx->stream>>>(ctx->d_c128, (R *)ctx->d_real, N);
+    } else {
+        CK(cudaMemcpyAsync(ctx->d_c128, data, sizeof(double) * N, cudaMemcpyHostToDevice, ctx->stream));
+        k_double_to_real<R><<<ew_blocks(N), 256, 0, ctx->stream>>>((const double *)ctx->d_c128, (R *)ctx->d_real, N);
+    }
+    CK(cudaGetLastError());
+    CK(enqueue_load_state<R>(ctx));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return GOPF_OK;
+}
+
+template <typename R> static int download_impl(gopf_ctx *ctx, double *data, bool complex_out)
+{
+    const long long N = ctx->g.N;
+    CK(enqueue_xpass_out<R>(ctx, (R *)ctx->d_real, nullptr));
+    if (complex_out) {
+        k_real_to_c128<R><<<ew_blocks(N), 256, 0, ctx->stream>>>((const R *)ctx->d_real, ctx->d_c128, N);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(data, ctx->d_c128, sizeof(double2) * N, cudaMemcpyDeviceToHost, ctx->stream));
+    } else {
+        k_real_to_double<R><<<ew_blocks(N), 256, 0, ctx->stream>>>((const R *)ctx->d_real, (double *)ctx->d_c128, N);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(data, ctx->d_c128, sizeof(double) * N, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return GOPF_OK;
+}
+
+static int transfer(gopf_ctx *ctx, int field, double *data, size_t n, bool up, bool cplx)
+{
+    if (!ctx || !data) return gopf_fail(ctx, GOPF_ERR_ARG, "null argument");
+    int rc;
+    if ((rc = require_ready(ctx, field))) return rc;
+    if ((long long)n != ctx->g.N)
+        return gopf_fail(ctx, GOPF_ERR_ARG, "Inconsistent domain size and number of grid points");
+    if ((rc = set_device(ctx))) return rc;
+    if (up) {
+        rc = (ctx->prec == GOPF_FP32) ? upload_impl<float>(ctx, data, cplx) : upload_impl<double>(ctx, data, cplx);
+        if (!rc) ctx->state_valid = true;
+        return rc;
+    }
+    if (!ctx->state_valid) return gopf_fail(ctx, GOPF_ERR_STATE, "field has not been uploaded");
+    return (ctx->prec == GOPF_FP32) ? download_impl<float>(ctx, data, cplx) : download_impl<double>(ctx, data, cplx);
+}
+
+extern "C" int gopf_field_upload(gopf_ctx *ctx, int f, const double *d, size_t n)
+{
+    return transfer(ctx, f, const_cast<double *>(d), n, true, true);
+}
+extern "C" int gopf_field_download(gopf_ctx *ctx, int f, double *d, size_t n) { return transfer(ctx, f, d, n, false, true); }
+extern "C" int gopf_field_upload_real(gopf_ctx *ctx, int f, const double *d, size_t n)
+{
+    return transfer(ctx, f, const_cast<double *>(d), n, true, false);
+}
+extern "C" int gopf_field_download_real(gopf_ctx *ctx, int f, double *d, size_t n)
+{
+    return transfer(ctx, f, d, n, false, false);
+}
+
+// ------------------------------------------------------------------
+// reductions
+// ------------------------------------------------------------------
+
+static int reduce_all(gopf_ctx *ctx, double *host5)
+{
+    cudaError_t e = (ctx->prec == GOPF_FP32) ? enqueue_xpass_out<float>(ctx, nullptr, ctx->d_red)
+                                             : enqueue_xpass_out<double>(ctx, nullptr, ctx->d_red);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "reduction pass");
+    k_finish_reduce<<<1, 256, 0, ctx->stream>>>(ctx->d_red, ctx->nred_blocks, ctx->d_redout);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(host5, ctx->d_redout, sizeof(double) * 5, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return GOPF_OK;
+}
+
+extern "C" int gopf_reduce(gopf_ctx *ctx, int field, int what, double *out)
+{
+    if (!ctx || !out) return gopf_fail(ctx, GOPF_ERR_ARG, "null argument");
+    int rc;
+    if ((rc = require_ready(ctx, field))) return rc;
+    if (what < 0 || what > GOPF_RED_NONFINITE) return gopf_fail(ctx, GOPF_ERR_ARG, "unknown reduction");
+    if (!ctx->state_valid) return gopf_fail(ctx, GOPF_ERR_STATE, "field has not been uploaded");
+    if ((rc = set_device(ctx))) return rc;
+    double r[5];
+    if ((rc = reduce_all(ctx, r))) return rc;
+    *out = r[what];
+    return GOPF_OK;
+}
+
+// ------------------------------------------------------------------
+// stepping
+// ------------------------------------------------------------------
+
+extern "C" int gopf_step(gopf_ctx *ctx, long long nsteps)
+{
+    if (!ctx) return GOPF_ERR_ARG;
+    if (nsteps < 0) return gopf_fail(ctx, GOPF_ERR_ARG, "negative step count");
+    if (!ctx->initialised) return gopf_fail(ctx, GOPF_ERR_STATE, "model not initialised (gopf_init/gopf_set_terms)");
+    if (!(ctx->dt > 0.0)) return gopf_fail(ctx, GOPF_ERR_STATE, "no stepper set (gopf_set_stepper)");
+    if (!ctx->state_valid) return gopf_fail(ctx, GOPF_ERR_STATE, "field has not been uploaded");
+    if (ctx->stepper != GOPF_STEPPER_EULER) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "stepper not available yet");
+    int rc;
+    if ((rc = set_device(ctx))) return rc;
+    long long left = nsteps;
+    if (ctx->use_graphs) {
+        if (!ctx->gexec1 && (rc = capture_graph(ctx, 1, &ctx->gexec1))) return rc;
+        if (left >= ctx->graphK && !ctx->gexecK && (rc = capture_graph(ctx, ctx->graphK, &ctx->gexecK))) return rc;
+        while (left >= ctx->graphK) {
+            CK(cudaGraphLaunch(ctx->gexecK, ctx->stream));
+            left -= ctx->graphK;
+        }
+        while (left > 0) {
+            CK(cudaGraphLaunch(ctx->gexec1, ctx->stream));
+            --left;
+        }
+    } else {
+        cudaError_t e = enqueue_steps_any(ctx, (int)std::min<long long>(left, 1 << 30));
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "step");
+    }
+    ctx->step += nsteps;
+    if (ctx->check_finite) {
+        double r[5];
+        if ((rc = reduce_all(ctx, r))) return rc;
+        if (r[RED_NONFINITE] > 0)
+            return gopf_fail(ctx, GOPF_ERR_NAN, "field contains " + std::to_string((long long)r[RED_NONFINITE]) +
+                                                    " non-finite values after step " + std::to_string(ctx->step));
+    }
+    return GOPF_OK;
+}
+
+extern "C" int gopf_synchronize(gopf_ctx *ctx)
+{
+    if (!ctx) return GOPF_ERR_ARG;
+    int rc;
+    if ((rc = set_device(ctx))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return GOPF_OK;
+}
+
+extern "C" int gopf_get_time(gopf_ctx *ctx, double *t)
+{
+    if (!ctx || !t) return GOPF_ERR_ARG;
+    *t = (double)ctx->step * ctx->dt; // Euler.GetTime (pf/euler.go:50-52)
+    return GOPF_OK;
+}
+
+extern "C" int gopf_get_step(gopf_ctx *ctx, long long *s)
+{
+    if (!ctx || !s) return GOPF_ERR_ARG;
+    *s = ctx->step;
+    return GOPF_OK;
+}
+
+// ------------------------------------------------------------------
+// Freq / ConjugateNode (pfutil/fftWrap.go:41-95)
+// ------------------------------------------------------------------
+
+extern "C" int gopf_freq(gopf_ctx *ctx, long long i, double *out)
+{
+    if (!ctx || !out) return GOPF_ERR_ARG;
+    const long long n0 = ctx->dims[0], n1 = ctx->dims[1];
+    if (i < 0 || i >= ctx->g.N) return gopf_fail(ctx, GOPF_ERR_ARG, "node index out of range");
+    const long long col = i % n1, row = (i / n1) % n0;
+    out[0] = (double)row / (double)n0;
+    out[1] = (double)col / (double)n1;
+    if (ctx->ndim == 3) out[2] = (double)(i / (n0 * n1)) / (double)ctx->dims[2];
+    for (int d = 0; d < ctx->ndim; ++d)
+        if (out[d] > 0.5) out[d] -= 1.0;
+    return GOPF_OK;
+}
+
+extern "C" long long gopf_conjugate_node(gopf_ctx *ctx, long long i)
+{
+    if (!ctx || i < 0 || i >= ctx->g.N) return -1;
+    const long long n0 = ctx->dims[0], n1 = ctx->dims[1];
+    const long long c = i % n1, r = (i / n1) % n0;
+    long long cd = 0;
+    if (ctx->ndim == 3) {
+        const long long d = i / (n0 * n1);
+        cd = (ctx->dims[2] - d) % ctx->dims[2];
+    }
+    return cd * n0 * n1 + ((n0 - r) % n0) * n1 + (n1 - c) % n1;
+}
+
+extern "C" int gopf_device_bytes(gopf_ctx *ctx, size_t *bytes)
+{
+    if (!ctx || !bytes) return GOPF_ERR_ARG;
+    *bytes = ctx->dev_bytes;
+    return GOPF_OK;
+}
+
+static void step_slots(gopf_ctx *ctx, std::vector<std::string> &names, std::vector<double> &bytes);
+
+extern "C" int gopf_kernels_per_step(gopf_ctx *ctx, int *n)
+{
+    if (!ctx || !n) return GOPF_ERR_ARG;
+    std::vector<std::string> names;
+    std::vector<double> bytes;
+    step_slots(ctx, names, bytes);
+    *n = (int)names.size();
+    return GOPF_OK;
+}
+
+// ------------------------------------------------------------------
+// per-kernel profiling of one step
+// ------------------------------------------------------------------
+
+// Kernel slots of one step with their algorithmic HBM bytes (each pass reads
+// and writes its arrays once).
+static void step_slots(gopf_ctx *ctx, std::vector<std::string> &names, std::vector<double> &bytes)
+{
+    const double vb = (ctx->prec == GOPF_FP32) ? 8.0 : 16.0;
+    const double C = (double)ctx->g.C * vb;
+    const int G = ctx->ngroups;
+    const int nb = std::max(G, 1);
+    names.clear();
+    bytes.clear();
+    if (G > 0) {
+        names.push_back("xpass_pointwise");
+        bytes.push_back((1.0 + G) * C);
+    }
+    if (ctx->g.Z > 1) {
+        if (G > 0) {
+            names.push_back("ypass_forward");
+            bytes.push_back(2.0 * G * C);
+        }
+        names.push_back("zpass_update");
+        bytes.push_back((nb + 3.0) * C);
+        names.push_back("ypass_inverse");
+        bytes.push_back(2.0 * C);
+    } else {
+        names.push_back("ypass_update");
+        bytes.push_back((nb + 3.0) * C);
+    }
+}
+
+extern "C" int gopf_profile_step(gopf_ctx *ctx, int nsteps, double *avg_ms, double *alg_bytes, int capacity, int *nslots)
+{
+    if (!ctx || !nslots || nsteps < 1) return gopf_fail(ctx, GOPF_ERR_ARG, "bad argument");
+    if (!ctx->initialised || !ctx->state_valid || !(ctx->dt > 0.0))
+        return gopf_fail(ctx, GOPF_ERR_STATE, "model, stepper and field must be set before profiling");
+    if (ctx->stepper != GOPF_STEPPER_EULER) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "profiling covers the Euler step");
+    int rc;
+    if ((rc = set_device(ctx))) return rc;
+    std::vector<std::string> names;
+    std::vector<double> bytes;
+    step_slots(ctx, names, bytes);
+    const size_t ns = names.size();
+    *nslots = (int)ns;
+    std::vector<cudaEvent_t> ev(1 + ns * nsteps);
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    std::vector<double> acc(ns, 0.0);
+    CK(cudaEventRecord(ev[0], ctx->stream));
+    ctx->prof_events = &ev;
+    ctx->prof_next = 1;
+    cudaError_t e = cudaSuccess;
+    for (int s = 0; s < nsteps && e == cudaSuccess; ++s)
+        e = (ctx->prec == GOPF_FP32) ? enqueue_euler<float>(ctx) : enqueue_euler<double>(ctx);
+    ctx->prof_events = nullptr;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess && ctx->prof_next != ev.size()) e = cudaErrorInvalidValue;
+    if (e == cudaSuccess) {
+        for (int s = 0; s < nsteps; ++s)
+            for (size_t k = 0; k < ns; ++k) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, ev[s * ns + k], ev[s * ns + k + 1]);
+                acc[k] += ms;
+            }
+        ctx->step += nsteps;
+    }
+    for (auto &x : ev) cudaEventDestroy(x);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "profile");
+    for (size_t k = 0; k < ns && (int)k < capacity; ++k) {
+        if (avg_ms) avg_ms[k] = acc[k] / nsteps;
+        if (alg_bytes) alg_bytes[k] = bytes[k];
+    }
+    return GOPF_OK;
+}
+
+extern "C" int gopf_profile_slot_name(gopf_ctx *ctx, int slot, char *buf, int buflen)
+{
+    if (!ctx || !buf || buflen < 1) return GOPF_ERR_ARG;
+    std::vector<std::string> names;
+    std::vector<double> bytes;
+    step_slots(ctx, names, bytes);
+    if (slot < 0 || slot >= (int)names.size()) return gopf_fail(ctx, GOPF_ERR_ARG, "bad slot");
+    snprintf(buf, buflen, "%s", names[slot].c_str());
+    return GOPF_OK;
+}
+
+// FourierTransform.FFT/IFFT on host []complex128 is provided by gopf_fft.cu.

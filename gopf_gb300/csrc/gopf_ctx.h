@@ -1,0 +1,109 @@
+// gopf_ctx.h -- internal definition of gopf_ctx shared by the C-ABI translation units.
+#pragma once
+#include <complex>
+#include <map>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/gopf_gpu.h"
+#include "gopf_types.h"
+
+// Host-side mirror of the parts of pf.Model that the equation strings refer to.
+struct gopf_modeldef {
+    std::vector<std::string> fields;                             // Model.Fields names, in AddField order
+    std::map<std::string, std::complex<double>> scalars;         // Scalar bricks
+    struct Func {
+        std::string name;
+        int kind;
+        int field;
+        std::vector<double> coefs;
+        std::vector<int> powers;
+    };
+    std::vector<Func> funcs;                                     // RegisterFunction (device kinds only)
+    struct Elastic {
+        std::string name;
+        int field;
+        double C[81];
+        double misfit[9];
+    };
+    std::vector<Elastic> elastic;                                // HomogeneousModulusLinElast terms
+    struct Volcons {
+        std::string name;
+        int field;
+        std::string indicator;
+        double dt;
+    };
+    std::vector<Volcons> volcons;                                // VolumeConservingLP terms
+    std::vector<std::string> equations;                          // AddEquation (spaces removed)
+    std::vector<std::string> derived_names;                      // derived fields, in registration order
+    std::vector<gopf_derived> derived;
+};
+
+// A special (non-polynomial) explicit term attached to an equation.
+struct gopf_special {
+    int kind; // 1 elastic, 2 volcons
+    int index;
+    int eq;
+    double coef;
+    int lap;
+};
+
+struct gopf_ctx {
+    int device = 0;
+    int ndim = 0;
+    int dims[3] = {1, 1, 1};
+    int prec = GOPF_FP32;
+    gopf::Geom g{};
+    int LBx = 16, LBy = 16, LBz = 16; // tile widths of the x, y and z passes
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+
+    // device buffers (element type float2/double2 for spectral, float/double for real)
+    void *d_state = nullptr;
+    void *d_T = nullptr;
+    void *d_U[GOPF_MAX_GROUPS] = {nullptr, nullptr, nullptr, nullptr};
+    void *d_real = nullptr;
+    double2 *d_c128 = nullptr;
+    double *d_red = nullptr;
+    double *d_redout = nullptr;
+    int nred_blocks = 0;
+    void *d_twX = nullptr, *d_twY = nullptr, *d_twZ = nullptr;
+    gopf::LinePlan planH{}, planY{}, planZ{};
+    size_t dev_bytes = 0;
+
+    // model
+    gopf_modeldef def;
+    bool initialised = false;  // gopf_init / gopf_set_terms done
+    int nfields = 0;
+    std::vector<gopf_derived> der;
+    std::vector<gopf_term> terms;
+    std::vector<gopf_special> specials;
+    gopf::PwTable pw{};
+    gopf::UpdTable upd{};
+    int ngroups = 0;
+
+    // stepping
+    int stepper = GOPF_STEPPER_EULER;
+    double dt = 0.0;
+    long long step = 0;
+    bool state_valid = false;
+
+    // graphs
+    cudaGraphExec_t gexec1 = nullptr;
+    cudaGraphExec_t gexecK = nullptr;
+    int graphK = 16;
+    bool graphs_dirty = true;
+
+    // per-kernel profiling (gopf_profile_step): events recorded after each launch
+    std::vector<cudaEvent_t> *prof_events = nullptr;
+    size_t prof_next = 0;
+
+    int check_finite = 1;
+    int use_graphs = 1;
+    std::string err;
+};
+
+int gopf_fail(gopf_ctx *ctx, int code, const std::string &msg);
+int gopf_compile_model(gopf_ctx *ctx);

@@ -1,0 +1,439 @@
+// gopf_kernels.cu -- spectral semi-implicit step kernels (sm_103a).
+//
+// Per Euler step of a single-field model (pf/euler.go:16-47) the device runs
+//   3D: x-pass (c2r -> pointwise terms -> r2c), y-pass forward,
+//       z-pass (forward -> k-space update -> inverse), y-pass inverse;
+//   2D: x-pass, y-pass (forward -> update -> inverse).
+// The state is kept as c-hat; the real field only exists in shared memory
+// inside the x-pass.  The pointwise derived fields of pf/util.go:57-64 and
+// the explicit/implicit term algebra of pf/rhsBuilder.go:125-190 are applied
+// in registers: explicit terms with the same LAP power are summed in real
+// space before their common forward transform, and the implicit symbol
+// sum_p a_p (-k^2)^p (pf/model.go:306-314, pf/diffOp.go:25-30) is evaluated
+// per frequency in the last-axis pass.
+#pragma once
+#include "gopf_kernels.cuh"
+#include <math.h>
+
+namespace gopf {
+
+template <int LB> struct Log2 { static constexpr int v = (LB == 1) ? 0 : 1 + Log2<LB / 2>::v; };
+template <> struct Log2<1> { static constexpr int v = 0; };
+
+template <typename R> __device__ __forceinline__ R poly_eval(const PwTable &pw, int grp, R c)
+{
+    R acc = (R)0;
+    const int nt = pw.nterm[grp];
+    for (int t = 0; t < nt; ++t) {
+        const int p = pw.pw[grp][t];
+        R x = (R)1;
+        for (int i = 0; i < p; ++i) x *= c;
+        acc += (R)pw.coef[grp][t] * x;
+    }
+    return acc;
+}
+
+// block-wide reduction of RED_SLOTS doubles into red[block]
+__device__ __forceinline__ void block_reduce_store(double *vals, double *red, double *sh)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int s = 0; s < RED_SLOTS; ++s) {
+        double v = vals[s];
+        for (int o = 16; o > 0; o >>= 1) {
+            double w = __shfl_xor_sync(0xffffffffu, v, o);
+            if (s == RED_MIN) v = fmin(v, w);
+            else if (s == RED_MAX) v = fmax(v, w);
+            else v += w;
+        }
+        if (lane == 0) sh[warp * RED_SLOTS + s] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < RED_SLOTS) {
+        const int s = threadIdx.x;
+        double v = sh[s];
+        for (int w = 1; w < nw; ++w) {
+            double u = sh[w * RED_SLOTS + s];
+            if (s == RED_MIN) v = fmin(v, u);
+            else if (s == RED_MAX) v = fmax(v, u);
+            else v += u;
+        }
+        red[(long long)(blockIdx.y * gridDim.x + blockIdx.x) * RED_SLOTS + s] = v;
+    }
+    __syncthreads();
+}
+
+// ------------------------------------------------------------------
+// x-pass: c2r (or real load) -> pointwise -> r2c
+// ------------------------------------------------------------------
+
+template <typename R, int LB, int PERB>
+__global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_xpass(const XPassArgs<R> a)
+{
+    typedef typename VecOf<R>::type V;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int LBSH = Log2<LB>::v;
+    const Geom &g = a.g;
+    const int H = g.H, KX = g.KX, Y = g.Y;
+    V *A = reinterpret_cast<V *>(smem_raw);
+    V *B = A + KX * LB;
+    const int y0 = blockIdx.x * LB;
+    const int z = blockIdx.y;
+    const int nl = min(LB, Y - y0);
+    const long long sbase = (long long)z * g.S + y0;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const V zero = cmk<V>((R)0, (R)0);
+    const V *__restrict__ twX = a.twX;
+
+    if (a.in_mode == XIN_SPECTRAL) {
+        const V *__restrict__ in = a.in;
+        for (int e = tid; e < KX * LB; e += nt) {
+            const int kx = e >> LBSH, l = e & (LB - 1);
+            A[e] = (l < nl) ? in[sbase + (long long)kx * Y + l] : zero;
+        }
+        __syncthreads();
+        const int npair = H / 2 + 1;
+        for (int e = tid; e < npair * LB; e += nt) {
+            const int k = e >> LBSH, l = e & (LB - 1);
+            if (k == 0) {
+                const V a0 = A[l], b0 = A[H * LB + l];
+                const V s = cadd(a0, cconj(b0)), d = csub(a0, cconj(b0));
+                A[l] = cmk<V>(s.x - d.y, s.y + d.x);
+            } else {
+                const int k2 = H - k;
+                const V av = A[k * LB + l], bv = A[k2 * LB + l];
+                const V s = cadd(av, cconj(bv)), d = csub(av, cconj(bv));
+                const V t = cmulc(d, __ldg(&twX[k]));
+                const V zk = cmk<V>(s.x - t.y, s.y + t.x);
+                if (k2 != k) {
+                    const V s2 = cadd(bv, cconj(av)), d2 = csub(bv, cconj(av));
+                    const V t2 = cmulc(d2, __ldg(&twX[k2]));
+                    A[k2 * LB + l] = cmk<V>(s2.x - t2.y, s2.y + t2.x);
+                }
+                A[k * LB + l] = zk;
+            }
+        }
+        __syncthreads();
+        fft_tile<true, LB, PERB>(A, LB, a.planH, twX);
+    } else {
+        const V *rin2 = reinterpret_cast<const V *>(a.rin) + ((long long)z * Y + y0) * H;
+        for (int e = tid; e < LB * H; e += nt) {
+            const int l = e / H, m = e - l * H;
+            A[m * LB + l] = (l < nl) ? rin2[(long long)l * H + m] : zero;
+        }
+        __syncthreads();
+    }
+
+    // A[m*LB + l] = (c[2m], c[2m+1]) of row y0 + l
+    if (a.rout) {
+        V *rout2 = reinterpret_cast<V *>(a.rout) + ((long long)z * Y + y0) * H;
+        for (int e = tid; e < LB * H; e += nt) {
+            const int l = e / H, m = e - l * H;
+            if (l < nl) rout2[(long long)l * H + m] = A[m * LB + l];
+        }
+    }
+    if (a.red) {
+        double vals[RED_SLOTS];
+#pragma unroll
+        for (int s = 0; s < RED_SLOTS; ++s) vals[s] = 0.0;
+        vals[RED_MIN] = INFINITY;
+        vals[RED_MAX] = -INFINITY;
+        for (int e = tid; e < H * LB; e += nt) {
+            const int l = e & (LB - 1);
+            if (l < nl) {
+                const V c = A[e];
+                const double c0 = (double)c.x, c1 = (double)c.y;
+                vals[RED_SUM] += c0 + c1;
+                vals[RED_SUMSQ] += c0 * c0 + c1 * c1;
+                vals[RED_MIN] = fmin(vals[RED_MIN], fmin(c0, c1));
+                vals[RED_MAX] = fmax(vals[RED_MAX], fmax(c0, c1));
+                vals[RED_NONFINITE] += (isfinite(c0) ? 0.0 : 1.0) + (isfinite(c1) ? 0.0 : 1.0);
+            }
+        }
+        __shared__ double shred[32 * RED_SLOTS];
+        block_reduce_store(vals, a.red, shred);
+    }
+
+    for (int grp = 0; grp < a.ngrp_out; ++grp) {
+        for (int e = tid; e < H * LB; e += nt) {
+            const V c = A[e];
+            B[e] = a.identity ? c : cmk<V>(poly_eval<R>(a.pw, grp, c.x), poly_eval<R>(a.pw, grp, c.y));
+        }
+        __syncthreads();
+        fft_tile<false, LB, PERB>(B, LB, a.planH, twX);
+        const int npair = H / 2 + 1;
+        const R half = (R)0.5;
+        for (int e = tid; e < npair * LB; e += nt) {
+            const int k = e >> LBSH, l = e & (LB - 1);
+            if (k == 0) {
+                const V z0 = B[l];
+                B[l] = cmk<V>(z0.x + z0.y, (R)0);
+                B[H * LB + l] = cmk<V>(z0.x - z0.y, (R)0);
+            } else {
+                const int k2 = H - k;
+                const V av = B[k * LB + l], bv = B[k2 * LB + l];
+                const V s = cadd(av, cconj(bv)), d = csub(av, cconj(bv));
+                const V t = cmul(__ldg(&twX[k]), d);
+                const V xk = cmk<V>(half * (s.x + t.y), half * (s.y - t.x));
+                if (k2 != k) {
+                    const V s2 = cadd(bv, cconj(av)), d2 = csub(bv, cconj(av));
+                    const V t2 = cmul(__ldg(&twX[k2]), d2);
+                    B[k2 * LB + l] = cmk<V>(half * (s2.x + t2.y), half * (s2.y - t2.x));
+                }
+                B[k * LB + l] = xk;
+            }
+        }
+        __syncthreads();
+        V *__restrict__ out = a.out[grp];
+        for (int e = tid; e < KX * LB; e += nt) {
+            const int kx = e >> LBSH, l = e & (LB - 1);
+            if (l < nl) out[sbase + (long long)kx * Y + l] = B[e];
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------
+// y (contiguous) and z (strided) passes
+// ------------------------------------------------------------------
+
+template <typename R> __device__ __forceinline__ R fsq_index(int i, int n)
+{
+    const int j = (2 * i > n) ? (n - i) : i;
+    const R f = (R)j / (R)n;
+    return f * f;
+}
+
+// Tile element mapping:
+//   CONTIG : tile = LB consecutive lines q0.. of length n; global (q, p) = q*n + p
+//            smem pitch LB+1, iteration order line-major (coalesced global)
+//   STRIDED: tile = LB consecutive inner indices i0.. of a pos-stride S array;
+//            global (p, i) = p*S + i; smem pitch LB; iteration order pos-major
+template <typename R, int LB, int PERB, bool CONTIG>
+__global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_pass(const PassArgs<R> a)
+{
+    typedef typename VecOf<R>::type V;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int LBSH = Log2<LB>::v;
+    constexpr int pitch = CONTIG ? LB + 1 : LB;
+    const Geom &g = a.g;
+    const int n = a.plan.n;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const long long nlines = CONTIG ? (long long)g.Z * g.KX : g.S;
+    const long long l0 = (long long)blockIdx.x * LB;
+    const int nl = (int)min((long long)LB, nlines - l0);
+    const long long pstride = CONTIG ? 1 : g.S;
+    const long long lstride = CONTIG ? n : 1;
+    const long long gbase = l0 * lstride;
+    const int tile = n * pitch;
+    V *sm = reinterpret_cast<V *>(smem_raw);
+    const V zero = cmk<V>((R)0, (R)0);
+    const int total = n * LB;
+
+    // element e of the iteration space -> (p, l)
+    auto decode = [&](int e, int &p, int &l) {
+        if (CONTIG) {
+            l = e / n;
+            p = e - l * n;
+        } else {
+            p = e >> LBSH;
+            l = e & (LB - 1);
+        }
+    };
+
+    if (a.mode == PM_FWD || a.mode == PM_INV) {
+        V *__restrict__ buf = a.buf[blockIdx.y];
+        for (int e = tid; e < total; e += nt) {
+            int p, l;
+            decode(e, p, l);
+            sm[p * pitch + l] = (l < nl) ? buf[gbase + p * pstride + l * lstride] : zero;
+        }
+        __syncthreads();
+        if (a.mode == PM_FWD) fft_tile<false, LB, PERB>(sm, pitch, a.plan, a.tw);
+        else fft_tile<true, LB, PERB>(sm, pitch, a.plan, a.tw);
+        for (int e = tid; e < total; e += nt) {
+            int p, l;
+            decode(e, p, l);
+            if (l < nl) buf[gbase + p * pstride + l * lstride] = sm[p * pitch + l];
+        }
+        return;
+    }
+
+    // FUSED / INIT: all groups are loaded and forward transformed
+    const int nb = a.nbuf;
+    for (int b = 0; b < nb; ++b) {
+        const V *__restrict__ buf = a.buf[b];
+        V *s = sm + b * tile;
+        for (int e = tid; e < total; e += nt) {
+            int p, l;
+            decode(e, p, l);
+            s[p * pitch + l] = (l < nl) ? buf[gbase + p * pstride + l * lstride] : zero;
+        }
+    }
+    __syncthreads();
+    for (int b = 0; b < nb; ++b) fft_tile<false, LB, PERB>(sm + b * tile, pitch, a.plan, a.tw);
+
+    const UpdTable &u = a.upd;
+    const R dt = (R)u.dt, invN = (R)u.invN;
+    const R fourpi2 = (R)39.478417604357434475337963999504; // 4 pi^2
+    V *__restrict__ state = a.state;
+    for (int e = tid; e < total; e += nt) {
+        int p, l;
+        decode(e, p, l);
+        if (l >= nl) continue;
+        const long long gi = gbase + p * pstride + l * lstride;
+        V cn;
+        if (a.mode == PM_INIT) {
+            cn = sm[p * pitch + l];
+        } else {
+            // frequency of this element
+            int kx, y, zz;
+            if (CONTIG) {
+                const long long q = l0 + l;
+                zz = (int)(q / g.KX);
+                kx = (int)(q - (long long)zz * g.KX);
+                y = p;
+            } else {
+                const long long i = l0 + l;
+                kx = (int)(i / g.Y);
+                y = (int)(i - (long long)kx * g.Y);
+                zz = p;
+            }
+            const R fx = (R)kx / (R)g.X;
+            const R ksq = fourpi2 * (fx * fx + fsq_index<R>(y, g.Y) + fsq_index<R>(zz, g.Z));
+            const R mk = -ksq;
+            // explicit part
+            V nhat = zero;
+            for (int b = 0; b < u.ngrp; ++b) {
+                R f = (R)1;
+                for (int q = 0; q < u.glap[b]; ++q) f *= mk;
+                const V tv = sm[b * tile + p * pitch + l];
+                nhat.x += f * tv.x;
+                nhat.y += f * tv.y;
+            }
+            // implicit symbol
+            R L = (R)0;
+            for (int q = u.nimp - 1; q >= 0; --q) L = L * mk + (R)u.imp[q];
+            const R den = (R)1 - dt * L;
+            const V c0 = state[gi];
+            cn = cmk<V>((c0.x + dt * nhat.x) / den, (c0.y + dt * nhat.y) / den);
+        }
+        state[gi] = cn;
+        sm[p * pitch + l] = cmk<V>(cn.x * invN, cn.y * invN);
+    }
+    __syncthreads();
+    fft_tile<true, LB, PERB>(sm, pitch, a.plan, a.tw);
+    V *__restrict__ tout = a.tout;
+    for (int e = tid; e < total; e += nt) {
+        int p, l;
+        decode(e, p, l);
+        if (l < nl) tout[gbase + p * pstride + l * lstride] = sm[p * pitch + l];
+    }
+}
+
+// ------------------------------------------------------------------
+// launchers
+// ------------------------------------------------------------------
+
+template <typename R> constexpr int perb() { return 16; }
+
+// Threads per block: enough for the per-thread register budget of the
+// Stockham stages (blockDim >= LB*n/PERB), at most the 256 of __launch_bounds__.
+static int pick_threads(long long work_items, int perb_)
+{
+    long long need = (work_items + perb_ - 1) / perb_;
+    int nt = 128;
+    while (nt < need && nt < 256) nt *= 2;
+    return nt;
+}
+static bool threads_ok(long long work_items, int perb_) { return (work_items + perb_ - 1) / perb_ <= 256; }
+
+// Raise a kernel's dynamic shared-memory limit only when a launch needs more
+// than before, so launches recorded into a CUDA graph set no attributes.
+// (Per device; the library drives one device per process in practice.)
+template <typename K> static cudaError_t ensure_smem(K kern, int smem, int &have)
+{
+    if (smem <= have) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) have = smem;
+    return e;
+}
+
+inline int xpass_smem_bytes(const Geom &g, int LB, int vbytes) { return 2 * g.KX * LB * vbytes; }
+inline int cpass_smem_bytes(const Geom &g, int n, int LB, int nbuf, int vbytes) { return nbuf * n * (LB + 1) * vbytes; }
+inline int spass_smem_bytes(const Geom &g, int n, int LB, int nbuf, int vbytes) { return nbuf * n * LB * vbytes; }
+
+template <typename R, int LB> static cudaError_t launch_xpass_lb(const XPassArgs<R> &a, cudaStream_t st)
+{
+    typedef typename VecOf<R>::type V;
+    const int smem = xpass_smem_bytes(a.g, LB, sizeof(V));
+    auto kern = k_xpass<R, LB, perb<R>()>;
+    static int have = 48 * 1024; // one per kernel instantiation
+    cudaError_t e = ensure_smem(kern, smem, have);
+    if (e != cudaSuccess) return e;
+    if (!threads_ok((long long)LB * a.g.H, perb<R>())) return cudaErrorInvalidConfiguration;
+    const int nt = pick_threads((long long)LB * a.g.H, perb<R>());
+    dim3 grid((a.g.Y + LB - 1) / LB, a.g.Z);
+    kern<<<grid, nt, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename R> cudaError_t launch_xpass(const XPassArgs<R> &a, int LB, cudaStream_t st)
+{
+    if constexpr (sizeof(R) == 4) {
+        if (LB == 16) return launch_xpass_lb<R, 16>(a, st);
+        if (LB == 8) return launch_xpass_lb<R, 8>(a, st);
+        if (LB == 4) return launch_xpass_lb<R, 4>(a, st);
+    } else {
+        if (LB == 8) return launch_xpass_lb<R, 8>(a, st);
+        if (LB == 4) return launch_xpass_lb<R, 4>(a, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+template <typename R, int LB, bool CONTIG> static cudaError_t launch_pass_lb(const PassArgs<R> &a, cudaStream_t st)
+{
+    typedef typename VecOf<R>::type V;
+    const int n = a.plan.n;
+    const bool fused = (a.mode == PM_FUSED || a.mode == PM_INIT);
+    const int nsm = fused ? a.nbuf : 1;
+    const int smem = CONTIG ? cpass_smem_bytes(a.g, n, LB, nsm, sizeof(V)) : spass_smem_bytes(a.g, n, LB, nsm, sizeof(V));
+    auto kern = k_pass<R, LB, perb<R>(), CONTIG>;
+    static int have = 48 * 1024; // one per kernel instantiation
+    cudaError_t e = ensure_smem(kern, smem, have);
+    if (e != cudaSuccess) return e;
+    if (!threads_ok((long long)LB * n, perb<R>())) return cudaErrorInvalidConfiguration;
+    const int nt = pick_threads((long long)LB * n, perb<R>());
+    const long long nlines = CONTIG ? (long long)a.g.Z * a.g.KX : a.g.S;
+    dim3 grid((unsigned)((nlines + LB - 1) / LB), fused ? 1 : a.nbuf);
+    kern<<<grid, nt, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename R> cudaError_t launch_cpass(const PassArgs<R> &a, int LB, cudaStream_t st)
+{
+    if constexpr (sizeof(R) == 4) {
+        if (LB == 16) return launch_pass_lb<R, 16, true>(a, st);
+        if (LB == 8) return launch_pass_lb<R, 8, true>(a, st);
+        if (LB == 4) return launch_pass_lb<R, 4, true>(a, st);
+    } else {
+        if (LB == 8) return launch_pass_lb<R, 8, true>(a, st);
+        if (LB == 4) return launch_pass_lb<R, 4, true>(a, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+template <typename R> cudaError_t launch_spass(const PassArgs<R> &a, int LB, cudaStream_t st)
+{
+    if constexpr (sizeof(R) == 4) {
+        if (LB == 16) return launch_pass_lb<R, 16, false>(a, st);
+        if (LB == 8) return launch_pass_lb<R, 8, false>(a, st);
+        if (LB == 4) return launch_pass_lb<R, 4, false>(a, st);
+    } else {
+        if (LB == 8) return launch_pass_lb<R, 8, false>(a, st);
+        if (LB == 4) return launch_pass_lb<R, 4, false>(a, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+} // namespace gopf

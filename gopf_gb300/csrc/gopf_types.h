@@ -1,0 +1,99 @@
+// gopf_types.h -- plain data structures shared by host code and kernels.
+//
+// Spectral layout in HBM (ours, not the reference's): a real field of the
+// reference's domainSize [n0 rows, n1 cols, n2 depth] (node index
+// depth*n0*n1 + row*n1 + col, pfutil/indexPositionConversion.go:23-34) is kept
+// as its half spectrum S[z][kx][y] with kx in [0, n1/2] slowest inside a
+// depth plane and the row frequency y fastest.  Every pass then reads either
+// whole contiguous lines (the y axis) or 128-byte segments of LB consecutive
+// y values (the kx and z axes).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gopf {
+
+#define GOPF_MAX_STAGES 12
+
+struct LinePlan {
+    int n;       // complex line length
+    int nst;     // number of stages
+    int rad[GOPF_MAX_STAGES];
+    int ns[GOPF_MAX_STAGES];     // product of the radices of earlier stages
+    int nsmask[GOPF_MAX_STAGES]; // ns-1 when ns is a power of two, else -1
+    int twmul[GOPF_MAX_STAGES];  // table index multiplier: W_{ns*R}^{q} = tw[q * twmul]
+};
+
+
+#define GOPF_MAX_GROUPS 4
+#define GOPF_MAX_POLY 8
+#define GOPF_MAX_IMP 9
+
+struct Geom {
+    int X, Y, Z; // cols (fastest real axis), rows, depth (1 in 2D)
+    int H;       // X/2
+    int KX;      // X/2 + 1
+    long long S; // KX * Y
+    long long C; // S * Z spectral elements
+    long long N; // X * Y * Z cells
+};
+
+// Real-space pointwise polynomials g_g(c) = sum_t coef[g][t] * c^pw[g][t]
+struct PwTable {
+    int ngrp;
+    int nterm[GOPF_MAX_GROUPS];
+    int pw[GOPF_MAX_GROUPS][GOPF_MAX_POLY];
+    double coef[GOPF_MAX_GROUPS][GOPF_MAX_POLY];
+};
+
+// k-space update: c_new = (c + dt * sum_g m^glap[g] U_g) / (1 - dt * sum_p imp[p] m^p),  m = -k^2
+struct UpdTable {
+    double dt;
+    double invN;
+    int nimp;                    // number of coefficients in imp (degree + 1)
+    double imp[GOPF_MAX_IMP];
+    int ngrp;
+    int glap[GOPF_MAX_GROUPS];
+};
+
+// Reduction slots written by the x-pass (FP64, compensated per block)
+enum { RED_SUM = 0, RED_SUMSQ = 1, RED_MIN = 2, RED_MAX = 3, RED_NONFINITE = 4, RED_SLOTS = 8 };
+
+enum XInMode { XIN_SPECTRAL = 0, XIN_REAL = 1 };
+
+template <typename R> struct VecOf;
+template <> struct VecOf<float> { typedef float2 type; };
+template <> struct VecOf<double> { typedef double2 type; };
+
+template <typename R> struct XPassArgs {
+    typedef typename VecOf<R>::type V;
+    Geom g;
+    LinePlan planH;       // complex FFT of length X/2 (table twX, stride 2)
+    const V *twX;         // W_X^t, t < X
+    int in_mode;          // XIN_SPECTRAL: read spectral tile from in; XIN_REAL: read real rows from rin
+    const V *in;
+    const R *rin;
+    R *rout;              // optional: write real rows of c
+    V *out[GOPF_MAX_GROUPS];
+    int ngrp_out;         // number of spectral outputs (0 = none)
+    int identity;         // 1: output group 0 is r2c(c) itself
+    PwTable pw;
+    double *red;          // optional: per-block partial sums [gridDim.x*gridDim.y][RED_SLOTS]
+};
+
+enum PassMode { PM_FWD = 0, PM_INV = 1, PM_FUSED = 2, PM_INIT = 3 };
+
+template <typename R> struct PassArgs {
+    typedef typename VecOf<R>::type V;
+    Geom g;
+    LinePlan plan;        // transform along this pass's axis
+    const V *tw;          // table for plan
+    int mode;
+    V *buf[GOPF_MAX_GROUPS]; // input groups (transformed in place for FWD/INV)
+    int nbuf;
+    V *state;             // c-hat (FUSED reads+writes, INIT writes)
+    V *tout;              // FUSED/INIT: inverse-transformed c_new/N goes here
+    UpdTable upd;
+};
+
+} // namespace gopf

@@ -1,0 +1,181 @@
+/*
+ * gopf_gpu.h -- C ABI of the GB300 spectral time stepper.
+ *
+ * This is the drop-in boundary for gopf's hot path.  A Go program binds it
+ * with cgo and gets a pf.TimeStepper whose fields stay
+ * resident in device memory between steps.  Every entry point returns an
+ * int status (GOPF_OK == 0); nothing throws or aborts across the ABI.  Host
+ * pointers are borrowed for the duration of the call only.  A context is not
+ * thread-safe: calls on one context must be serialised by the caller.  Each
+ * call makes the context's device current, so calls may come from any OS
+ * thread.
+ *
+ * Reference interfaces replaced (github.com/davidkleiven/gopf):
+ *   pf.TimeStepper   pf/solver.go:15-19   -> gopf_set_stepper / gopf_step / gopf_get_time
+ *   pf.Euler.Step    pf/euler.go:16-47    -> gopf_step (GOPF_STEPPER_EULER)
+ *   pf.RK4.Step      pf/rk4.go:29-74      -> gopf_step (GOPF_STEPPER_RK4)
+ *   pf.FourierTransform pf/solver.go:22-26, pfutil/fftWrap.go:26-95
+ *                                         -> gopf_fft / gopf_freq / gopf_conjugate_node
+ *   pf.Model.AddField/AddScalar/AddEquation/RegisterFunction/Init
+ *                    pf/model.go:133-162,244-260,400-412 -> gopf_add_field ... gopf_init
+ *   pf.Build / ConcreteTerm  pf/rhsBuilder.go:26-190 -> gopf_init (equation strings) or
+ *                                                      gopf_set_terms (pre-compiled table)
+ *   pf.HomogeneousModulusLinElast pf/homoLinElast.go:33-150 -> gopf_register_elastic
+ *   pf.VolumeConservingLP pf/volumeConserving.go:8-61 -> gopf_register_volcons
+ *   Field.Data access (host <-> device)   -> gopf_field_upload / gopf_field_download
+ *   mass check pf/solver_test.go:20-27, PointMonitor pf/monitor.go:27-30 -> gopf_reduce
+ */
+#ifndef GOPF_GPU_H
+#define GOPF_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gopf_ctx gopf_ctx;
+
+/* status codes */
+enum {
+    GOPF_OK = 0,
+    GOPF_ERR_ARG = 1,         /* bad argument (size mismatch: the reference panics, pf/solver.go:55-60) */
+    GOPF_ERR_CUDA = 2,        /* CUDA runtime error */
+    GOPF_ERR_OOM = 3,         /* device allocation failed */
+    GOPF_ERR_NAN = 4,         /* non-finite value detected in a field after stepping */
+    GOPF_ERR_TIMEOUT = 5,     /* a bounded device wait gave up */
+    GOPF_ERR_UNSUPPORTED = 6, /* model feature with no device implementation (no CPU fallback) */
+    GOPF_ERR_STATE = 7,       /* call out of order (e.g. step before init) */
+    GOPF_ERR_PARSE = 8        /* equation string could not be parsed (pf/rhsBuilder.go panics) */
+};
+
+/* precision of the device state */
+enum { GOPF_FP32 = 0, GOPF_FP64 = 1 };
+
+/* time steppers */
+enum { GOPF_STEPPER_EULER = 0, GOPF_STEPPER_RK4 = 1 };
+
+/* derived-field kinds (real-space pointwise functions of one field) */
+enum {
+    GOPF_DER_PRODUCT = 0,     /* prod_j field_j^power_j; names like "conc^3" (pf/util.go:38-65) */
+    GOPF_DER_POLY = 1,        /* sum_t coef_t * field^power_t (a RegisterFunction polynomial) */
+    GOPF_DER_INDICATOR = 2,   /* 3x^2 - 2x^3 (pf/homoLinElast.go:10-12) */
+    GOPF_DER_INDICATOR_D = 3, /* 6x - 6x^2 (pf/homoLinElast.go:15-17) */
+    GOPF_DER_INDICATOR_HD = 4 /* Indicator(x) * IndicatorDeriv(x) */
+};
+
+/* term sources */
+enum { GOPF_SRC_NONE = 0, GOPF_SRC_FIELD = 1, GOPF_SRC_DERIVED = 2 };
+
+/* reductions over the real field (FP64) */
+enum {
+    GOPF_RED_SUM = 0,   /* sum of c over cells (total mass) */
+    GOPF_RED_SUMSQ = 1, /* sum of c^2 */
+    GOPF_RED_MIN = 2,
+    GOPF_RED_MAX = 3,
+    GOPF_RED_NONFINITE = 4 /* number of NaN/Inf cells */
+};
+
+/* options for gopf_set_option */
+enum {
+    GOPF_OPT_CHECK_FINITE = 0, /* 1 (default): gopf_step synchronises and checks the field for NaN/Inf */
+    GOPF_OPT_USE_GRAPHS = 1    /* 1 (default): steps are replayed from captured CUDA graphs */
+};
+
+#define GOPF_MAX_FACTORS 8
+
+/* A real-space derived field (what pf.Model.UpdateDerivedFields / RegisterFunction register). */
+typedef struct {
+    int kind;                      /* GOPF_DER_* */
+    int nfac;                      /* number of factors / polynomial terms */
+    int field[GOPF_MAX_FACTORS];   /* field ids */
+    int power[GOPF_MAX_FACTORS];   /* integer powers */
+    double coef[GOPF_MAX_FACTORS]; /* polynomial coefficients (GOPF_DER_POLY) */
+} gopf_derived;
+
+/* One term of an equation, as pf.Build produces it (pf/rhsBuilder.go:125-242):
+ * value(k) = coef * (-(2 pi |f|)^2)^lap * source(k). */
+typedef struct {
+    int eq;        /* equation index == index of the field it evolves */
+    int implicit;  /* 1: bilinear in the field -> enters the denominator (Denum) */
+    double coef;   /* sign * prod(scalar^power) */
+    int lap;       /* power of the Laplacian symbol */
+    int source;    /* GOPF_SRC_* (ignored for implicit terms) */
+    int src_index; /* field id or derived id */
+} gopf_term;
+
+/* ---- context ---- */
+int gopf_ctx_create(int ndim, const int *domain_size, int precision, int device, gopf_ctx **out);
+int gopf_ctx_destroy(gopf_ctx *ctx);
+const char *gopf_last_error(const gopf_ctx *ctx);
+const char *gopf_status_string(int status);
+/* Enqueue all work on this CUDA stream (a cudaStream_t); NULL restores the context's own stream. */
+int gopf_set_stream(gopf_ctx *ctx, void *cuda_stream);
+int gopf_set_option(gopf_ctx *ctx, int option, long long value);
+
+/* ---- model definition, pf.Model mirror (pf/model.go) ---- */
+int gopf_add_field(gopf_ctx *ctx, const char *name, int *field_id);               /* Model.AddField */
+int gopf_add_scalar(gopf_ctx *ctx, const char *name, double re, double im);       /* Model.AddScalar */
+/* Model.RegisterFunction restricted to device pointwise kinds (GOPF_DER_*). */
+int gopf_register_function(gopf_ctx *ctx, const char *name, int kind, const char *field,
+                           const double *coefs, const int *powers, int nterms);
+/* NewHomogeneousModolus + RegisterExplicitTerm(term_name, ...): C is the 3x3x3x3 stiffness
+ * (index i*27+j*9+k*3+l, elasticity/rank4.go:19-21), misfit the 3x3 misfit strain. */
+int gopf_register_elastic(gopf_ctx *ctx, const char *term_name, const char *field, const double *C81,
+                          const double *misfit9);
+/* NewVolumeConservingLP + RegisterExplicitTerm(term_name, ...) */
+int gopf_register_volcons(gopf_ctx *ctx, const char *term_name, const char *field, const char *indicator,
+                          double dt);
+int gopf_add_equation(gopf_ctx *ctx, const char *equation);                       /* Model.AddEquation */
+/* Model.Init + pf.Build: compile every equation into the device term table. */
+int gopf_init(gopf_ctx *ctx);
+/* Number of explicit/implicit terms of equation eq after gopf_init (Model.Summarize's NE/NI). */
+int gopf_equation_summary(gopf_ctx *ctx, int eq, int *n_explicit, int *n_implicit);
+/* Copy out the compiled term table (for inspection and tests). */
+int gopf_get_terms(gopf_ctx *ctx, gopf_term *terms, int capacity, int *nterms);
+int gopf_get_derived(gopf_ctx *ctx, gopf_derived *der, int capacity, int *nder);
+
+/* ---- model definition, pre-compiled (what a Go shim builds from pf.Model.RHS) ---- */
+int gopf_set_terms(gopf_ctx *ctx, int nfields, const gopf_derived *derived, int nderived, const gopf_term *terms,
+                   int nterms);
+
+/* ---- stepping (pf.TimeStepper) ---- */
+int gopf_set_stepper(gopf_ctx *ctx, int stepper, double dt);
+/* Field.Data <-> device. data is a []complex128 (interleaved re, im; n complex values).
+ * Upload takes the real part; the stepped fields are real. */
+int gopf_field_upload(gopf_ctx *ctx, int field_id, const double *data, size_t n);
+int gopf_field_download(gopf_ctx *ctx, int field_id, double *data, size_t n);
+/* Real-valued variants (n doubles) */
+int gopf_field_upload_real(gopf_ctx *ctx, int field_id, const double *data, size_t n);
+int gopf_field_download_real(gopf_ctx *ctx, int field_id, double *data, size_t n);
+/* Solver.Propagate(nsteps): nsteps steps plus the per-step OnStepFinished hooks of device terms. */
+int gopf_step(gopf_ctx *ctx, long long nsteps);
+int gopf_get_time(gopf_ctx *ctx, double *t);
+int gopf_get_step(gopf_ctx *ctx, long long *step);
+int gopf_synchronize(gopf_ctx *ctx);
+
+/* ---- monitors ---- */
+int gopf_reduce(gopf_ctx *ctx, int field_id, int what, double *out);
+
+/* ---- FourierTransform (pfutil/fftWrap.go) on host data, not a hot path ---- */
+/* sign -1: forward FFT, +1: unnormalised backward, of a []complex128 of length N. */
+int gopf_fft(gopf_ctx *ctx, int sign, double *data, size_t n);
+/* Freq(i): writes ndim frequencies (cycles/sample, (-0.5, 0.5]) */
+int gopf_freq(gopf_ctx *ctx, long long i, double *out);
+long long gopf_conjugate_node(gopf_ctx *ctx, long long i);
+
+/* ---- introspection ---- */
+/* Bytes of device memory held by the context. */
+int gopf_device_bytes(gopf_ctx *ctx, size_t *bytes);
+/* Number of kernel launches enqueued by one step of the current stepper. */
+int gopf_kernels_per_step(gopf_ctx *ctx, int *n);
+/* Run nsteps Euler steps launch by launch with CUDA events between kernels on the
+ * context's stream; per kernel slot of one step write the average device time (ms)
+ * and the algorithmic HBM bytes (each array read and written once).  Advances the state. */
+int gopf_profile_step(gopf_ctx *ctx, int nsteps, double *avg_ms, double *alg_bytes, int capacity, int *nslots);
+int gopf_profile_slot_name(gopf_ctx *ctx, int slot, char *buf, int buflen);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GOPF_GPU_H */

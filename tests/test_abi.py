@@ -1,0 +1,207 @@
+"""CPU-only checks of the C ABI: the library loads, exports every entry point
+of include/gopf_gpu.h, and its equation front end makes the same term split
+as pf.Build (pf/rhsBuilder.go).  Host-only contexts (device = -1) compile
+models without touching a GPU."""
+import math
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _header_symbols():
+    txt = open(os.path.join(ROOT, "include", "gopf_gpu.h")).read()
+    return sorted(set(re.findall(r"\b(gopf_[a-z_0-9]+)\s*\(", txt)))
+
+
+def test_library_exports_every_header_symbol(gpulib):
+    syms = _header_symbols()
+    assert len(syms) >= 30
+    for s in syms:
+        assert hasattr(gpulib, s), s
+
+
+def test_status_strings(gpulib):
+    assert gpulib.gopf_status_string(0) == b"ok"
+    assert gpulib.gopf_status_string(4) == b"non-finite value in field"
+
+
+def _host_model(dims=(16, 16)):
+    import gopf_gb300 as G
+
+    return G.Model(list(dims), "fp32", device=-1)
+
+
+def test_cahn_hilliard_string_split():
+    """examples/cahnHilliard/main.go:33 -> 1 explicit (LAP conc^3) + 2 implicit terms."""
+    m = _host_model()
+    m.add_field("conc")
+    m.add_scalar("gamma", 2.0)
+    m.add_scalar("m1", -1.0)
+    m.add_equation("dconc/dt = LAP conc^3 + m1*LAP conc + m1*gamma*LAP^2 conc")
+    m.init()
+    assert m.summary(0) == (1, 2)
+    terms = m.terms()
+    expl = [t for t in terms if not t["implicit"]]
+    impl = sorted([t for t in terms if t["implicit"]], key=lambda t: t["lap"])
+    assert expl[0]["coef"] == 1.0 and expl[0]["lap"] == 1 and expl[0]["source"] == 2
+    assert impl[0]["coef"] == -1.0 and impl[0]["lap"] == 1
+    assert impl[1]["coef"] == -2.0 and impl[1]["lap"] == 2
+    der = m.derived()
+    assert der == [dict(kind=0, field=[0], power=[3], coef=[1.0])]
+
+
+def test_term_diffusion_is_implicit():
+    """TestTermDiffusion (pf/model_test.go:17-43): 'dconc/dt = LAP conc' -> 0 terms, 1 denominator."""
+    m = _host_model((2, 2))
+    m.add_field("conc")
+    m.add_equation("dconc/dt = LAP conc")
+    m.init()
+    assert m.summary(0) == (0, 1)
+    t = m.terms()[0]
+    assert t["implicit"] == 1 and t["coef"] == 1.0 and t["lap"] == 1
+
+
+def test_decay_strings():
+    """pf/euler_test.go: 'rate*field' is bilinear (implicit); 'rate*field^2' is explicit with a derived field."""
+    m = _host_model((8, 8))
+    m.add_field("field")
+    m.add_scalar("rate", -1.0)
+    m.add_equation("dfield/dt = rate*field")
+    m.init()
+    assert m.summary(0) == (0, 1)
+    assert m.terms()[0]["coef"] == -1.0
+    m2 = _host_model((8, 8))
+    m2.add_field("field")
+    m2.add_scalar("rate", -1.0)
+    m2.add_equation("dfield/dt = rate*field^2")
+    m2.init()
+    assert m2.summary(0) == (1, 0)
+    assert m2.derived()[0]["power"] == [2]
+
+
+def test_logistic_string():
+    """pf/rk4_test.go:79 'field + rate*field^2' -> 1 implicit (+1) and 1 explicit (-field^2)."""
+    m = _host_model((8, 8))
+    m.add_field("field")
+    m.add_scalar("rate", -1.0)
+    m.add_equation("dfield/dt = field + rate*field^2")
+    m.init()
+    assert m.summary(0) == (1, 1)
+    t = {bool(t["implicit"]): t for t in m.terms()}
+    assert t[True]["coef"] == 1.0 and t[True]["lap"] == 0
+    assert t[False]["coef"] == -1.0
+
+
+def test_negative_sign_and_prefixes():
+    """Signs from the preceding delimiter (pf/rhsBuilder.go:126-130) and LAP^2 powers."""
+    m = _host_model()
+    m.add_field("c")
+    m.add_scalar("k", 0.5)
+    m.add_equation("dc/dt = -k*LAP^2 c - LAP c^3")
+    m.init()
+    terms = m.terms()
+    imp = [t for t in terms if t["implicit"]][0]
+    exp_ = [t for t in terms if not t["implicit"]][0]
+    assert imp["coef"] == -0.5 and imp["lap"] == 2
+    assert exp_["coef"] == -1.0 and exp_["lap"] == 1
+
+
+def test_registered_function_as_brick():
+    """RegisterFunction (pf/model.go:400-412): 'LAP MU' uses the function as the term's field."""
+    import gopf_gb300 as G
+
+    m = _host_model()
+    m.add_field("conc")
+    m.add_scalar("mg", -0.5)
+    m.register_function("MU", G.DER_POLY, "conc", [1.0, -1.0], [3, 1])
+    m.add_equation("dconc/dt = LAP MU + mg*LAP^2 conc")
+    m.init()
+    terms = m.terms()
+    assert m.summary(0) == (1, 1)
+    e = [t for t in terms if not t["implicit"]][0]
+    assert e["source"] == G.SRC_DERIVED and e["lap"] == 1
+    assert m.derived()[0]["power"] == [3, 1]
+
+
+def test_unknown_name_is_a_parse_error():
+    """TestPanicOnUnknownName (pf/rhsBuilder_test.go:158): unknown names are rejected."""
+    import gopf_gb300 as G
+
+    m = _host_model()
+    m.add_field("conc")
+    m.add_equation("dconc/dt = foo*LAP conc^3")
+    with pytest.raises(G.GopfError) as e:
+        m.init()
+    assert e.value.status == 8
+
+
+def test_reserved_names_rejected():
+    """panicOnPrefixInName (pf/model.go:480-485)."""
+    import gopf_gb300 as G
+
+    m = _host_model()
+    with pytest.raises(G.GopfError):
+        m.add_field("LAPconc")
+
+
+def test_bad_leibniz():
+    import gopf_gb300 as G
+
+    m = _host_model()
+    m.add_field("conc")
+    with pytest.raises(G.GopfError):
+        m.add_equation("conc = LAP conc")
+
+
+def test_cubic_3d_only():
+    import gopf_gb300 as G
+
+    with pytest.raises(G.GopfError) as e:
+        G.Model([16, 16, 32], "fp32", device=-1)
+    assert e.value.status == 6
+
+
+def test_odd_columns_rejected():
+    import gopf_gb300 as G
+
+    with pytest.raises(G.GopfError):
+        G.Model([8, 9], "fp32", device=-1)
+
+
+def test_freq_and_conjugate_node_host_only():
+    m = _host_model((8, 8))
+    from oracle import oracle as O
+
+    for i in range(64):
+        assert np.allclose(m.freq(i), O.freq([8, 8], i))
+        assert m.conjugate_node(i) == O.conjugate_node([8, 8], i)
+
+
+def test_stepping_needs_a_device():
+    import gopf_gb300 as G
+
+    m = _host_model()
+    m.add_field("conc")
+    m.add_equation("dconc/dt = LAP conc")
+    m.init()
+    m.set_stepper("euler", 0.1)
+    with pytest.raises(G.GopfError) as e:
+        m.upload(0, np.zeros(256))
+    assert e.value.status == 7
+
+
+def test_size_mismatch_is_an_argument_error():
+    """NewSolver panics on inconsistent sizes (pf/solver.go:55-60); the ABI returns GOPF_ERR_ARG."""
+    import ctypes
+
+    import gopf_gb300 as G
+
+    m = _host_model()
+    m.add_field("conc")
+    a = np.zeros(2 * 100)
+    rc = m._L.gopf_field_upload(m.handle, 0, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 100)
+    assert rc == 1

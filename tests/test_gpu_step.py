@@ -1,0 +1,209 @@
+"""GPU parity of the semi-implicit spectral Euler step against the FP64 oracle.
+
+Cases follow the reference's known-answer tests (pf/euler_test.go,
+pf/solver_test.go) and the Cahn-Hilliard string of
+examples/cahnHilliard/main.go:33, at sizes the oracle runs in seconds.
+Tolerances: FP64 mode rel-L2 <= 1e-11 against the oracle; FP32 mode
+rel-L2 <= 1e-4 (short trajectories) -- both written per test.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+CH_EQ = "dconc/dt = LAP conc^3 + m1*LAP conc + m1*gamma*LAP^2 conc"
+
+
+def ch_gpu(dims, prec, gamma, dt, c0, M=1.0):
+    import gopf_gb300 as G
+
+    m = G.Model(dims, prec, device=0)
+    m.add_field("conc")
+    m.add_scalar("gamma", gamma)
+    m.add_scalar("m1", -M)
+    m.add_scalar("M", M)
+    m.add_equation("dconc/dt = M*LAP conc^3 + m1*LAP conc + m1*gamma*LAP^2 conc")
+    m.init()
+    m.set_stepper("euler", dt)
+    m.upload(0, c0)
+    return m
+
+
+def ch_oracle(O, dims, gamma, c0, M=1.0):
+    m = O.cahn_hilliard(dims, gamma=gamma, M=M)
+    m.set_field(0, c0)
+    return m
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def test_exponential_decay_gpu():
+    """TestExponentialDecay (pf/euler_test.go:10-49) on the device, FP64."""
+    import gopf_gb300 as G
+
+    m = G.Model([8, 8], "fp64", device=0)
+    m.add_field("field")
+    m.add_scalar("rate", -1.0)
+    m.add_equation("dfield/dt = rate*field")
+    m.init()
+    m.set_stepper("euler", 0.001)
+    m.upload(0, np.ones(64))
+    m.step(1000)
+    f = m.download(0)
+    assert np.all(np.abs(f.real - math.exp(-1.0)) < 1e-3)
+    assert abs(m.time - 1.0) < 1e-10
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_square_decay_gpu(prec):
+    """TestEulerSquareDecary (pf/euler_test.go:51-85): 1/(1+t) within 1e-3."""
+    import gopf_gb300 as G
+
+    m = G.Model([8, 8], prec, device=0)
+    m.add_field("field")
+    m.add_scalar("rate", -1.0)
+    m.add_equation("dfield/dt = rate*field^2")
+    m.init()
+    m.set_stepper("euler", 0.001)
+    m.upload(0, np.ones(64))
+    m.step(1000)
+    assert np.all(np.abs(m.download(0).real - 0.5) < 1e-3)
+
+
+def test_solver_diffusion_gpu():
+    """TestSolverDiffusion (pf/solver_test.go:9-34): mass 1 to 1e-4, values in [0, 1)."""
+    import gopf_gb300 as G
+
+    m = G.Model([16, 16], "fp64", device=0)
+    m.add_field("conc")
+    m.add_equation("dconc/dt = LAP conc")
+    m.init()
+    m.set_stepper("euler", 0.1)
+    c = np.zeros(256)
+    c[128] = 1.0
+    m.upload(0, c)
+    for _ in range(10):
+        m.step(10)
+    d = m.download(0).real
+    assert abs(d.sum() - 1.0) < 1e-4
+    assert np.all(d < 1.0) and np.all(d >= 0.0)
+
+
+@pytest.mark.parametrize("dims,steps", [([64, 64], 50), ([128, 128], 1000), ([48, 96], 100)])
+def test_cahn_hilliard_2d_fp64_parity(oracle, dims, steps):
+    """2D CH, the plain splitting of examples/cahnHilliard, FP64 mode vs oracle: rel-L2 <= 1e-11."""
+    from gopf_gb300.synthetic import uniform_field
+
+    n = int(np.prod(dims))
+    c0 = uniform_field(0, n, 0.5, 0.05)
+    g = ch_gpu(dims, "fp64", 1.0, 0.1, c0)
+    g.step(steps)
+    o = ch_oracle(oracle, dims, 1.0, c0)
+    o.step_euler(0.1, steps)
+    err = rel_l2(g.download(0).real, o.field(0).real)
+    assert err <= 1e-11, err
+    assert abs(g.mass(0) - o.field(0).real.sum()) <= 1e-9 * n
+
+
+@pytest.mark.parametrize("dims,steps", [([16, 16, 16], 20), ([32, 32, 32], 50), ([24, 24, 24], 10)])
+def test_cahn_hilliard_3d_fp64_parity(oracle, dims, steps):
+    """3D CH (gamma 0.5, dt 0.05 as in the 256^3 configuration), FP64 mode vs oracle: rel-L2 <= 1e-11."""
+    from gopf_gb300.synthetic import uniform_field
+
+    n = int(np.prod(dims))
+    c0 = uniform_field(1, n, 0.0, 0.1)
+    g = ch_gpu(dims, "fp64", 0.5, 0.05, c0)
+    g.step(steps)
+    o = ch_oracle(oracle, dims, 0.5, c0)
+    o.step_euler(0.05, steps)
+    err = rel_l2(g.download(0).real, o.field(0).real)
+    assert err <= 1e-11, err
+
+
+@pytest.mark.parametrize("dims,steps,gamma,dt,center,hw", [([128, 128], 100, 1.0, 0.1, 0.5, 0.05),
+                                                            ([32, 32, 32], 50, 0.5, 0.05, 0.0, 0.1)])
+def test_cahn_hilliard_fp32_parity(oracle, dims, steps, gamma, dt, center, hw):
+    """FP32 mode vs the FP64 oracle on short trajectories: rel-L2 <= 1e-4."""
+    from gopf_gb300.synthetic import uniform_field
+
+    n = int(np.prod(dims))
+    c0 = uniform_field(2, n, center, hw)
+    g = ch_gpu(dims, "fp32", gamma, dt, c0)
+    g.step(steps)
+    o = ch_oracle(oracle, dims, gamma, c0)
+    o.step_euler(dt, steps)
+    err = rel_l2(g.download(0).real, o.field(0).real)
+    assert err <= 1e-4, err
+
+
+def test_explicit_linear_splitting_matches_oracle(oracle):
+    """The spec splitting mu = c^3 - c explicit, -gamma k^4 implicit, via a registered polynomial."""
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+
+    dims = [64, 64]
+    c0 = uniform_field(5, 64 * 64, 0.5, 0.05)
+    m = G.Model(dims, "fp64", device=0)
+    m.add_field("conc")
+    m.add_scalar("mg", -1.3)
+    m.add_scalar("M", 0.8)
+    m.register_function("MU", G.DER_POLY, "conc", [1.0, -1.0], [3, 1])
+    m.add_equation("dconc/dt = M*LAP MU + mg*M*LAP^2 conc")
+    m.init()
+    m.set_stepper("euler", 0.05)
+    m.upload(0, c0)
+    m.step(200)
+    o = oracle.cahn_hilliard(dims, gamma=1.3, M=0.8, splitting="explicit_linear")
+    o.set_field(0, c0)
+    o.step_euler(0.05, 200)
+    assert rel_l2(m.download(0).real, o.field(0).real) <= 1e-11
+
+
+def test_graph_and_eager_paths_agree():
+    """Steps replayed from CUDA graphs equal steps launched one by one (bitwise)."""
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+
+    dims = [64, 64, 64]
+    c0 = uniform_field(9, 64 ** 3, 0.0, 0.1)
+    a = ch_gpu(dims, "fp32", 0.5, 0.05, c0)
+    b = ch_gpu(dims, "fp32", 0.5, 0.05, c0)
+    b.set_option(G._lib.OPT_USE_GRAPHS, 0)
+    a.step(37)
+    b.step(37)
+    assert np.array_equal(a.download(0), b.download(0))
+
+
+def test_nan_is_reported_not_trapped():
+    """A blow-up is reported as GOPF_ERR_NAN by the host check (no device trap)."""
+    import gopf_gb300 as G
+
+    m = G.Model([8, 8], "fp32", device=0)
+    m.add_field("f")
+    m.add_equation("df/dt = f^4")
+    m.init()
+    m.set_stepper("euler", 1.0)
+    m.upload(0, np.full(64, 10.0))
+    with pytest.raises(G.GopfError) as e:
+        m.step(10)
+    assert e.value.status == 4
+
+
+def test_mass_conserved_3d_256_fp32():
+    """3D CH at 256^3 FP32 (the configuration of the benchmark): mass drift after 200 steps <= 1e-6 (absolute per cell)."""
+    from gopf_gb300.synthetic import uniform_field
+
+    n = 256 ** 3
+    c0 = uniform_field(1, n, 0.0, 0.1)
+    g = ch_gpu([256, 256, 256], "fp32", 0.5, 0.05, c0)
+    m0 = g.mass(0)
+    g.step(200)
+    m1 = g.mass(0)
+    assert abs(m1 - m0) / n <= 1e-6
+    d = g.download(0).real
+    assert np.all(np.isfinite(d))
+    assert abs(d.sum() - c0.sum()) / n <= 1e-6
