@@ -51,9 +51,9 @@ def load():
 
 
 def build(force: bool = False) -> str:
-    from . import build as _b
+    import importlib
 
-    return _b.build(force=force)
+    return importlib.import_module(__name__ + ".build").build(force=force)
 
 
 def _dptr(a: np.ndarray):
