@@ -300,3 +300,71 @@ def test_seeded_generator_matches_python():
     b = O.uniform_field(3, 5000, 0.3, 0.02)
     assert np.array_equal(a, b)
     assert a.min() >= 0.28 and a.max() < 0.32
+
+
+# ---------------------------------------------------------------- elastic symbol
+
+def _cubic(c11, c12, c44):
+    """elasticity.CubicMaterial (elasticity/rank4.go:113-128)."""
+    C = np.zeros((3, 3, 3, 3))
+    for i in range(3):
+        C[i, i, i, i] = c11
+    for i in range(3):
+        for j in range(i + 1, 3):
+            C[i, i, j, j] = c12
+            C[j, j, i, i] = c12
+            C[i, j, i, j] = c44
+            C[j, i, j, i] = c44
+    return C
+
+
+def _bsym(dims, C, mis):
+    """The device's elastic symbol: b(k) = sum_{i<D} (A f~)_i (Gamma(f)^-1 A f)_i, symmetrised over k, -k."""
+    D = len(dims)
+    N = int(np.prod(dims))
+    A = np.einsum("ijkl,kl->ij", C, mis)
+
+    def bval(f):
+        if np.all(np.abs(f) < 1e-10):
+            return 0.0
+        ft = f.copy()
+        ft[np.abs(np.abs(ft) - 0.5) < 1e-10] = 0.0
+        G = np.einsum("mjnl,j,l->mn", C, f, f)
+        return float(np.dot((A @ ft)[:D], np.linalg.solve(G, A @ f)[:D]))
+
+    b = np.zeros(N)
+    for i in range(N):
+        f = np.zeros(3)
+        f[:D] = O.freq(dims, i)
+        fm = np.zeros(3)
+        fm[:D] = O.freq(dims, O.conjugate_node(dims, i))
+        b[i] = 0.5 * (bval(f) + bval(fm))
+    return b
+
+
+@pytest.mark.parametrize("dims", [[16, 16], [8, 8, 8], [12, 12, 12]])
+def test_elastic_symbol_is_hermitian_part_of_reference_term(dims):
+    """The Khachaturyan term of pf/homoLinElast.go:47-99 (14 FFTs + per-k 3x3 solves in 3D) equals,
+    in its Hermitian part, FFT[H'(h) (IFFT(b Hhat)/N - 2 e0 H(h))] with the symmetrised symbol b.
+    The reference's anti-Hermitian remainder comes from f = +0.5 at both k and -k on Nyquist planes."""
+    rng = np.random.default_rng(0)
+    N = int(np.prod(dims))
+    h = 0.3 + 0.2 * rng.random(N)
+    C = _cubic(1.0, 0.6, 0.5)
+    mis = np.eye(3) * 0.01
+    mis[0, 1] = mis[1, 0] = 0.003
+    m = O.Model(dims, 1)
+    e = m.add_elastic(0, 0, C, mis)
+    m.elastic_hfield(e)[:] = h
+    m.set_field(0, h)
+    ref = m.eval_rhs(0)
+    conj = np.array([O.conjugate_node(dims, i) for i in range(N)])
+    herm = 0.5 * (ref + np.conj(ref[conj]))
+    A = np.einsum("ijkl,kl->ij", C, mis)
+    e0 = 0.5 * np.einsum("ijkl,ij,kl->", C, mis, mis)
+    H = 3 * h * h - 2 * h ** 3
+    Hd = 6 * h - 6 * h * h
+    w = (O.fftn(_bsym(dims, C, mis) * O.fftn(H.astype(complex), dims, -1), dims, +1) / N).real
+    mine = O.fftn((Hd * (w - 2 * e0 * H)).astype(complex), dims, -1)
+    assert np.abs(herm - mine).max() <= 1e-12 * np.abs(ref).max()
+    del A
