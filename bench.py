@@ -58,7 +58,7 @@ def peaks():
 def config(extra=None):
     c = {
         "workload": WORKLOAD,
-        "grid": "256x256x256",
+        "grid": "x".join(str(d) for d in DIMS),
         "gamma": GAMMA,
         "M": M,
         "dt": DT,
@@ -185,6 +185,11 @@ def run_reference(args):
 def run_gpu(args):
     import torch
 
+    global DIMS, WORKLOAD
+    if args.grid != 256:
+        DIMS = [args.grid] * 3
+        WORKLOAD = f"cahn_hilliard_3d_{args.grid}cube_fp32_euler"
+
     import gopf_gb300 as G
     from gopf_gb300.synthetic import uniform_field
 
@@ -245,6 +250,19 @@ def run_gpu(args):
     step_bytes = sum(p["bytes"] for p in prof)
 
     # ---- end to end through the C ABI with pinned host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, m, stream, c0, n, world, dist, torch, G)
+    out = emit(args, m, world, rank, value, per_step_ms, mass0, mass1, finite, prof, dom, hbm, peak_kind, achieved,
+               step_bytes, e2e, clocks, n)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def run_e2e(args, m, stream, c0, n, world, dist, torch, G):
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     host = torch.empty(2 * n, dtype=torch.float64, pin_memory=True)
     host.numpy()[0::2] = c0
     host.numpy()[1::2] = 0.0
@@ -274,10 +292,13 @@ def run_gpu(args):
         t = torch.tensor([e2e_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
-    e2e = {"value": world * k_e2e / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": 16 * n,
-           "d2h_bytes_per_step": 16 * n, "steps": k_e2e,
-           "path": "gopf_field_upload ([]complex128, pinned) + gopf_step(1) + gopf_field_download per step"}
+    return {"value": world * k_e2e / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": 16 * n,
+            "d2h_bytes_per_step": 16 * n, "steps": k_e2e,
+            "path": "gopf_field_upload ([]complex128, pinned) + gopf_step(1) + gopf_field_download per step"}
 
+
+def emit(args, m, world, rank, value, per_step_ms, mass0, mass1, finite, prof, dom, hbm, peak_kind, achieved,
+         step_bytes, e2e, clocks, n):
     out = None
     if rank == 0:
         cpu = None
@@ -304,10 +325,7 @@ def run_gpu(args):
             "gpu_launches": m.kernels_per_step * args.steps,
         }
         print(json.dumps(out))
-    if dist:
-        dist.barrier()
-        dist.destroy_process_group()
-    return 0
+    return out
 
 
 def main():
@@ -318,6 +336,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--grid", type=int, default=256, help="cube side (256 is the benchmark workload)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

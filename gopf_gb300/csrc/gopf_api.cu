@@ -243,6 +243,9 @@ static void ctx_free(gopf_ctx *ctx)
         if (p) cudaFree(p);
     for (int i = 1; i < GOPF_MAX_GROUPS; ++i)
         if (ctx->d_U[i]) cudaFree(ctx->d_U[i]);
+    void *more[] = {ctx->d_bsym, ctx->d_U0, ctx->d_UH, ctx->d_vc, ctx->d_red2};
+    for (void *p : more)
+        if (p) cudaFree(p);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
 }
 
@@ -374,12 +377,38 @@ static int derived_poly(gopf_ctx *ctx, const gopf_derived &d, std::vector<std::p
     return GOPF_OK;
 }
 
+static int add_poly_to_group(gopf_ctx *ctx, PwTable &pw, int grp, const std::vector<std::pair<double, int>> &poly,
+                             double coef)
+{
+    for (auto &pc : poly) {
+        int at = -1; // merge equal powers
+        for (int q = 0; q < pw.nterm[grp]; ++q)
+            if (pw.pw[grp][q] == pc.second) at = q;
+        if (at < 0) {
+            if (pw.nterm[grp] >= GOPF_MAX_POLY) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "polynomial too long");
+            at = pw.nterm[grp]++;
+            pw.pw[grp][at] = pc.second;
+            pw.coef[grp][at] = 0.0;
+        }
+        pw.coef[grp][at] += coef * pc.first;
+    }
+    return GOPF_OK;
+}
+
+static int alloc_spectral(gopf_ctx *ctx, void **p)
+{
+    if (ctx->device < 0 || *p) return GOPF_OK;
+    const size_t vb = (ctx->prec == GOPF_FP32) ? sizeof(float2) : sizeof(double2);
+    cudaError_t e = cudaMalloc(p, vb * ctx->g.C);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(work buffer)");
+    ctx->dev_bytes += vb * ctx->g.C;
+    return GOPF_OK;
+}
+
 int gopf_compile_model(gopf_ctx *ctx)
 {
     if (ctx->nfields != 1)
         return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "the device stepper supports single-field models");
-    if (!ctx->specials.empty())
-        return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "user-defined terms are not on the device yet");
     PwTable pw;
     memset(&pw, 0, sizeof(pw));
     UpdTable u;
@@ -414,34 +443,99 @@ int gopf_compile_model(gopf_ctx *ctx)
             grp = u.ngrp++;
             u.glap[grp] = t.lap;
         }
-        for (auto &pc : poly) {
-            // merge equal powers
-            int at = -1;
-            for (int q = 0; q < pw.nterm[grp]; ++q)
-                if (pw.pw[grp][q] == pc.second) at = q;
-            if (at < 0) {
-                if (pw.nterm[grp] >= GOPF_MAX_POLY) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "polynomial too long");
-                at = pw.nterm[grp]++;
-                pw.pw[grp][at] = pc.second;
-                pw.coef[grp][at] = 0.0;
-            }
-            pw.coef[grp][at] += t.coef * pc.first;
+        int rc = add_poly_to_group(ctx, pw, grp, poly, t.coef);
+        if (rc) return rc;
+    }
+    // user-defined terms that run on the device
+    ctx->has_elastic = false;
+    ctx->has_volcons = false;
+    ctx->vc_group = -1;
+    for (const gopf_special &sp : ctx->specials) {
+        if (sp.eq != 0) return gopf_fail(ctx, GOPF_ERR_ARG, "term refers to an equation that does not exist");
+        if (sp.kind == 1) {
+            if (ctx->has_elastic) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "one elastic term per model");
+            const gopf_modeldef::Elastic &e = ctx->def.elastic[sp.index];
+            if (e.field != 0) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "elastic term must act on field 0");
+            ctx->has_elastic = true;
+            memcpy(ctx->el_C, e.C, sizeof(ctx->el_C));
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) {
+                    double a = 0.0;
+                    for (int k = 0; k < 3; ++k)
+                        for (int l = 0; l < 3; ++l) a += e.C[i * 27 + j * 9 + k * 3 + l] * e.misfit[k * 3 + l];
+                    ctx->el_A[i * 3 + j] = a;
+                }
+            double e0 = 0.0;
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j)
+                    for (int k = 0; k < 3; ++k)
+                        for (int l = 0; l < 3; ++l)
+                            e0 += e.C[i * 27 + j * 9 + k * 3 + l] * e.misfit[i * 3 + j] * e.misfit[k * 3 + l];
+            ctx->el_e0 = 0.5 * e0;
+            ctx->el_coef = sp.coef;
+            ctx->el_lap = sp.lap;
+        } else if (sp.kind == 2) {
+            if (ctx->has_volcons) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "one volume-conserving term per model");
+            const gopf_modeldef::Volcons &v = ctx->def.volcons[sp.index];
+            if (v.field != 0) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "volume-conserving term must act on field 0");
+            int did = -1;
+            for (size_t i = 0; i < ctx->def.derived_names.size(); ++i)
+                if (ctx->def.derived_names[i] == v.indicator) did = (int)i;
+            if (did < 0) return gopf_fail(ctx, GOPF_ERR_ARG, "VolumeConservingLP: Indicator is not a derived field");
+            std::vector<std::pair<double, int>> poly;
+            int rc = derived_poly(ctx, ctx->def.derived[did], poly);
+            if (rc) return rc;
+            if (u.ngrp >= GOPF_MAX_GROUPS) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "too many term groups");
+            const int grp = u.ngrp++;
+            u.glap[grp] = sp.lap;
+            if ((rc = add_poly_to_group(ctx, pw, grp, poly, 1.0))) return rc;
+            ctx->has_volcons = true;
+            ctx->vc_group = grp;
+            ctx->vc_dt = v.dt;
+            ctx->vc_coef = sp.coef;
+        } else {
+            return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "user-defined term kind has no device implementation");
         }
     }
+    if (ctx->has_elastic && u.ngrp + 1 > GOPF_MAX_GROUPS)
+        return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "too many term groups with the elastic term");
     pw.ngrp = u.ngrp;
     u.nimp = maxp;
     ctx->pw = pw;
     ctx->upd = u;
     ctx->ngroups = u.ngrp;
-    // work arrays for groups beyond the first
-    const size_t vb = (ctx->prec == GOPF_FP32) ? sizeof(float2) : sizeof(double2);
-    for (int b = 1; b < std::max(1, u.ngrp); ++b) {
-        if (ctx->device >= 0 && !ctx->d_U[b]) {
-            cudaError_t e = cudaMalloc(&ctx->d_U[b], vb * ctx->g.C);
-            if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(group buffer)");
-            ctx->dev_bytes += vb * ctx->g.C;
+    // the elastic step's x-pass also emits H(c) = 3c^2 - 2c^3 as an extra group
+    ctx->pw_el = pw;
+    if (ctx->has_elastic) {
+        const int gH = pw.ngrp;
+        ctx->pw_el.ngrp = gH + 1;
+        ctx->pw_el.nterm[gH] = 2;
+        ctx->pw_el.pw[gH][0] = 2;
+        ctx->pw_el.coef[gH][0] = 3.0;
+        ctx->pw_el.pw[gH][1] = 3;
+        ctx->pw_el.coef[gH][1] = -2.0;
+    }
+    if (ctx->device >= 0) {
+        int rc;
+        for (int b = 1; b < std::max(1, u.ngrp); ++b)
+            if ((rc = alloc_spectral(ctx, &ctx->d_U[b]))) return rc;
+        if (ctx->has_elastic) {
+            if ((rc = alloc_spectral(ctx, &ctx->d_U0))) return rc;
+            if ((rc = alloc_spectral(ctx, &ctx->d_UH))) return rc;
+            if ((rc = set_device(ctx))) return rc;
+            if ((rc = gopf_elastic_table(ctx))) return rc;
+        }
+        if (ctx->has_volcons) {
+            if (!ctx->d_vc) {
+                CK(cudaMalloc(&ctx->d_vc, sizeof(double) * 8));
+                CK(cudaMalloc(&ctx->d_red2, sizeof(double) * RED_SLOTS * ctx->nred_blocks));
+                ctx->dev_bytes += sizeof(double) * (8 + RED_SLOTS * ctx->nred_blocks);
+            }
+            CK(cudaMemset(ctx->d_vc, 0, sizeof(double) * 8));
+            ctx->upd.gscale[ctx->vc_group] = ctx->d_vc + 4;
         }
     }
+    ctx->el_primed = false;
     ctx->initialised = true;
     invalidate_graphs(ctx);
     return GOPF_OK;
@@ -579,6 +673,7 @@ template <typename R> static cudaError_t enqueue_load_state(gopf_ctx *ctx)
         sa.tout = (V *)ctx->d_T;
         sa.upd = u;
         LK(launch_spass<R>(sa, ctx->LBz, ctx->stream));
+        LK(gopf_launch_hermitian_planes(ctx, ctx->d_state));
         pa.mode = PM_INV;
         LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
     } else {
@@ -590,63 +685,117 @@ template <typename R> static cudaError_t enqueue_load_state(gopf_ctx *ctx)
         pa.tout = (V *)ctx->d_T;
         pa.upd = u;
         LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+        LK(gopf_launch_hermitian_planes(ctx, ctx->d_state));
     }
     return cudaSuccess;
 }
 
 // One Euler step (pf/euler.go:16-47) of a single-field model.
+//   x-pass      : c2r(T) -> polynomial groups g_b(c) (+ H(c) for elasticity) -> r2c
+//   [volcons]   : Lagrange-multiplier update from the x-pass's FP64 block sums
+//   [elastic]   : H-hat -> b(k) H-hat / N -> w(x); x-pass q = s H'(c)(w - 2 e0 H(c)) -> r2c
+//   last axis   : forward, c-hat <- (c-hat + dt sum_b m^lap_b U_b)/(1 - dt L(m)), T <- inverse(c-hat/N)
+// The elastic part runs from the second step on: the reference's h-field is
+// zero until the first OnStepFinished (pf/homoLinElast.go:130-145).
 template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx)
 {
     typedef typename VecOf<R>::type V;
+    const bool el = ctx->has_elastic && ctx->el_primed;
     const int G = ctx->ngroups;
+    const int GE = G + (el ? 1 : 0); // groups entering the update
+    V *T = (V *)ctx->d_T;
+    V *UH = (V *)ctx->d_UH;
     V *U[GOPF_MAX_GROUPS];
-    U[0] = (V *)ctx->d_T;
+    U[0] = el ? (V *)ctx->d_U0 : T;
     for (int b = 1; b < GOPF_MAX_GROUPS; ++b) U[b] = (V *)ctx->d_U[b];
+    if (el) U[G] = UH;
     UpdTable u = ctx->upd;
     u.dt = ctx->dt;
     u.invN = 1.0 / (double)ctx->g.N;
-    if (G > 0) {
+    if (el) {
+        u.ngrp = GE;
+        u.glap[G] = ctx->el_lap;
+        u.gscale[G] = nullptr;
+    }
+    const bool is3d = ctx->g.Z > 1;
+    if (GE > 0) {
         XPassArgs<R> xa = xargs<R>(ctx);
         xa.in_mode = XIN_SPECTRAL;
-        xa.in = (const V *)ctx->d_T;
-        for (int b = 0; b < G; ++b) xa.out[b] = U[b];
-        xa.ngrp_out = G;
-        xa.pw = ctx->pw;
+        xa.in = T;
+        for (int b = 0; b < GE; ++b) xa.out[b] = U[b];
+        xa.ngrp_out = GE;
+        xa.pw = el ? ctx->pw_el : ctx->pw;
+        if (ctx->has_volcons) {
+            xa.red = ctx->d_red;
+            xa.red2 = ctx->d_red2;
+            xa.redgrp = ctx->vc_group;
+        }
         LK(launch_xpass<R>(xa, ctx->LBx, ctx->stream));
     }
-    // with no explicit term the last pass still needs T = partial transform of c-hat/N;
-    // it reads c-hat through the update (identity contribution when ngrp == 0)
-    const int nb = std::max(G, 1);
-    if (ctx->g.Z > 1) {
-        PassArgs<R> pa = pargs<R>(ctx, false);
-        if (G > 0) {
+    if (ctx->has_volcons) LK(gopf_launch_volcons_finalize(ctx));
+    if (el) {
+        if (is3d) {
+            PassArgs<R> pa = pargs<R>(ctx, false);
             pa.mode = PM_FWD;
-            for (int b = 0; b < G; ++b) pa.buf[b] = U[b];
-            pa.nbuf = G;
+            for (int b = 0; b < GE; ++b) pa.buf[b] = U[b];
+            pa.nbuf = GE;
             LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
         }
-        PassArgs<R> sa = pargs<R>(ctx, true);
-        sa.mode = PM_FUSED;
-        for (int b = 0; b < nb; ++b) sa.buf[b] = U[b];
-        sa.nbuf = nb;
-        sa.state = (V *)ctx->d_state;
-        sa.tout = (V *)ctx->d_T;
-        sa.upd = u;
-        LK(launch_spass<R>(sa, ctx->LBz, ctx->stream));
+        PassArgs<R> ka = pargs<R>(ctx, is3d);
+        ka.mode = PM_ELASTIC_K;
+        ka.buf[0] = UH;
+        ka.nbuf = 1;
+        ka.upd = u;
+        ka.bsym = (const R *)ctx->d_bsym;
+        LK(is3d ? launch_spass<R>(ka, ctx->LBz, ctx->stream) : launch_cpass<R>(ka, ctx->LBy, ctx->stream));
+        if (is3d) {
+            PassArgs<R> ia = pargs<R>(ctx, false);
+            ia.mode = PM_INV;
+            ia.buf[0] = UH;
+            ia.nbuf = 1;
+            LK(launch_cpass<R>(ia, ctx->LBy, ctx->stream));
+        }
+        XPassArgs<R> xc = xargs<R>(ctx);
+        xc.in_mode = XIN_SPECTRAL;
+        xc.in = T;
+        xc.program = XP_ELASTIC_Q;
+        xc.in2 = UH;
+        xc.out[0] = UH;
+        xc.ngrp_out = 1;
+        xc.e0 = ctx->el_e0;
+        xc.escale = ctx->el_coef;
+        LK(launch_xpass<R>(xc, ctx->LBx, ctx->stream));
+        if (is3d) {
+            PassArgs<R> pa = pargs<R>(ctx, false);
+            pa.mode = PM_FWD;
+            pa.buf[0] = UH;
+            pa.nbuf = 1;
+            LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+        }
+    } else if (is3d && GE > 0) {
+        PassArgs<R> pa = pargs<R>(ctx, false);
+        pa.mode = PM_FWD;
+        for (int b = 0; b < GE; ++b) pa.buf[b] = U[b];
+        pa.nbuf = GE;
+        LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+    }
+    // with no explicit term the last pass reads c-hat only (identity contribution when ngrp == 0)
+    const int nb = std::max(GE, 1);
+    PassArgs<R> fa = pargs<R>(ctx, is3d);
+    fa.mode = PM_FUSED;
+    for (int b = 0; b < nb; ++b) fa.buf[b] = U[b];
+    fa.nbuf = nb;
+    fa.state = (V *)ctx->d_state;
+    fa.tout = T;
+    fa.upd = u;
+    LK(is3d ? launch_spass<R>(fa, ctx->LBz, ctx->stream) : launch_cpass<R>(fa, ctx->LBy, ctx->stream));
+    LK(gopf_launch_hermitian_planes(ctx, ctx->d_state));
+    if (is3d) {
         PassArgs<R> ia = pargs<R>(ctx, false);
         ia.mode = PM_INV;
-        ia.buf[0] = (V *)ctx->d_T;
+        ia.buf[0] = T;
         ia.nbuf = 1;
         LK(launch_cpass<R>(ia, ctx->LBy, ctx->stream));
-    } else {
-        PassArgs<R> pa = pargs<R>(ctx, false);
-        pa.mode = PM_FUSED;
-        for (int b = 0; b < nb; ++b) pa.buf[b] = U[b];
-        pa.nbuf = nb;
-        pa.state = (V *)ctx->d_state;
-        pa.tout = (V *)ctx->d_T;
-        pa.upd = u;
-        LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
     }
     return cudaSuccess;
 }
@@ -796,6 +945,14 @@ extern "C" int gopf_step(gopf_ctx *ctx, long long nsteps)
     int rc;
     if ((rc = set_device(ctx))) return rc;
     long long left = nsteps;
+    if (ctx->has_elastic && !ctx->el_primed && left > 0) {
+        // first step ever: the elastic term sees the reference's zero h-field
+        cudaError_t e = enqueue_steps_any(ctx, 1);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "step");
+        ctx->el_primed = true;
+        invalidate_graphs(ctx);
+        --left;
+    }
     if (ctx->use_graphs) {
         if (!ctx->gexec1 && (rc = capture_graph(ctx, 1, &ctx->gexec1))) return rc;
         if (left >= ctx->graphK && !ctx->gexecK && (rc = capture_graph(ctx, ctx->graphK, &ctx->gexecK))) return rc;
@@ -905,27 +1062,31 @@ static void step_slots(gopf_ctx *ctx, std::vector<std::string> &names, std::vect
 {
     const double vb = (ctx->prec == GOPF_FP32) ? 8.0 : 16.0;
     const double C = (double)ctx->g.C * vb;
+    const bool el = ctx->has_elastic && ctx->el_primed;
     const int G = ctx->ngroups;
-    const int nb = std::max(G, 1);
+    const int GE = G + (el ? 1 : 0);
+    const int nb = std::max(GE, 1);
+    const bool is3d = ctx->g.Z > 1;
     names.clear();
     bytes.clear();
-    if (G > 0) {
-        names.push_back("xpass_pointwise");
-        bytes.push_back((1.0 + G) * C);
+    auto add = [&](const char *n, double b) {
+        names.push_back(n);
+        bytes.push_back(b);
+    };
+    if (GE > 0) add("xpass_pointwise", (1.0 + GE) * C);
+    if (ctx->has_volcons) add("volcons_multiplier", 0.0);
+    if (el) {
+        if (is3d) add("ypass_forward", 2.0 * GE * C);
+        add(is3d ? "zpass_elastic_symbol" : "ypass_elastic_symbol", 2.0 * C + C / 2.0);
+        if (is3d) add("ypass_inverse", 2.0 * C);
+        add("xpass_elastic", 3.0 * C);
+        if (is3d) add("ypass_forward", 2.0 * C);
+    } else if (is3d && GE > 0) {
+        add("ypass_forward", 2.0 * GE * C);
     }
-    if (ctx->g.Z > 1) {
-        if (G > 0) {
-            names.push_back("ypass_forward");
-            bytes.push_back(2.0 * G * C);
-        }
-        names.push_back("zpass_update");
-        bytes.push_back((nb + 3.0) * C);
-        names.push_back("ypass_inverse");
-        bytes.push_back(2.0 * C);
-    } else {
-        names.push_back("ypass_update");
-        bytes.push_back((nb + 3.0) * C);
-    }
+    add(is3d ? "zpass_update" : "ypass_update", (nb + 3.0) * C);
+    add("hermitian_planes", 4.0 * C / ctx->g.KX);
+    if (is3d) add("ypass_inverse", 2.0 * C);
 }
 
 extern "C" int gopf_profile_step(gopf_ctx *ctx, int nsteps, double *avg_ms, double *alg_bytes, int capacity, int *nslots)
@@ -934,6 +1095,7 @@ extern "C" int gopf_profile_step(gopf_ctx *ctx, int nsteps, double *avg_ms, doub
     if (!ctx->initialised || !ctx->state_valid || !(ctx->dt > 0.0))
         return gopf_fail(ctx, GOPF_ERR_STATE, "model, stepper and field must be set before profiling");
     if (ctx->stepper != GOPF_STEPPER_EULER) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "profiling covers the Euler step");
+    if (ctx->has_elastic && !ctx->el_primed) return gopf_fail(ctx, GOPF_ERR_STATE, "take one step before profiling");
     int rc;
     if ((rc = set_device(ctx))) return rc;
     std::vector<std::string> names;

@@ -96,6 +96,25 @@ struct gopf_ctx {
     int graphK = 16;
     bool graphs_dirty = true;
 
+    // Khachaturyan term (at most one per context)
+    bool has_elastic = false;
+    double el_C[81] = {0};
+    double el_A[9] = {0};
+    double el_e0 = 0.0, el_coef = 1.0;
+    int el_lap = 0;
+    bool el_primed = false; // false until the first step: the reference's h-field starts at zero
+    void *d_bsym = nullptr;
+    void *d_U0 = nullptr; // group-0 buffer separate from T (T must survive the elastic step)
+    void *d_UH = nullptr; // H-hat, then the elastic term
+    gopf::PwTable pw_el{}; // polynomial groups + the indicator H(c)
+
+    // VolumeConservingLP (at most one per context)
+    bool has_volcons = false;
+    int vc_group = -1;
+    double vc_dt = 0.0, vc_coef = 1.0;
+    double *d_vc = nullptr;   // [lambda, current integral, previous indicator integral, count, coef*lambda]
+    double *d_red2 = nullptr; // block sums of the indicator
+
     // per-kernel profiling (gopf_profile_step): events recorded after each launch
     std::vector<cudaEvent_t> *prof_events = nullptr;
     size_t prof_next = 0;
@@ -107,3 +126,6 @@ struct gopf_ctx {
 
 int gopf_fail(gopf_ctx *ctx, int code, const std::string &msg);
 int gopf_compile_model(gopf_ctx *ctx);
+int gopf_elastic_table(gopf_ctx *ctx);
+cudaError_t gopf_launch_volcons_finalize(gopf_ctx *ctx);
+cudaError_t gopf_launch_hermitian_planes(gopf_ctx *ctx, void *state);

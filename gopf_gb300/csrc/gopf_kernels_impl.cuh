@@ -63,6 +63,100 @@ __device__ __forceinline__ void block_reduce_store(double *vals, double *red, do
     __syncthreads();
 }
 
+// Load the spectral tile (z, all kx, LB rows from y0) of `in`, undo the r2c
+// packing and inverse transform along x: on return A[m*LB + l] = (c[2m],
+// c[2m+1]) of row y0 + l (times the transform's normalisation).
+template <typename R, int LB, int PERB>
+__device__ __forceinline__ void xload_c2r(typename VecOf<R>::type *A, const typename VecOf<R>::type *__restrict__ in,
+                                          long long sbase, int nl, const Geom &g, const LinePlan &planH,
+                                          const typename VecOf<R>::type *__restrict__ twX)
+{
+    typedef typename VecOf<R>::type V;
+    constexpr int LBSH = Log2<LB>::v;
+    const int H = g.H, KX = g.KX, Y = g.Y;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const V zero = cmk<V>((R)0, (R)0);
+    for (int e = tid; e < KX * LB; e += nt) {
+        const int kx = e >> LBSH, l = e & (LB - 1);
+        A[e] = (l < nl) ? in[sbase + (long long)kx * Y + l] : zero;
+    }
+    __syncthreads();
+    const int npair = H / 2 + 1;
+    for (int e = tid; e < npair * LB; e += nt) {
+        const int k = e >> LBSH, l = e & (LB - 1);
+        if (k == 0) {
+            const V a0 = A[l], b0 = A[H * LB + l];
+            const V s = cadd(a0, cconj(b0)), d = csub(a0, cconj(b0));
+            A[l] = cmk<V>(s.x - d.y, s.y + d.x);
+        } else {
+            const int k2 = H - k;
+            const V av = A[k * LB + l], bv = A[k2 * LB + l];
+            const V s = cadd(av, cconj(bv)), d = csub(av, cconj(bv));
+            const V t = cmulc(d, __ldg(&twX[k]));
+            const V zk = cmk<V>(s.x - t.y, s.y + t.x);
+            if (k2 != k) {
+                const V s2 = cadd(bv, cconj(av)), d2 = csub(bv, cconj(av));
+                const V t2 = cmulc(d2, __ldg(&twX[k2]));
+                A[k2 * LB + l] = cmk<V>(s2.x - t2.y, s2.y + t2.x);
+            }
+            A[k * LB + l] = zk;
+        }
+    }
+    __syncthreads();
+    fft_tile<true, LB, PERB>(A, LB, planH, twX);
+}
+
+// r2c along x of the packed real rows in B (B[m*LB+l] = (g[2m], g[2m+1])) and
+// store the half spectrum of the tile into out.
+template <typename R, int LB, int PERB>
+__device__ __forceinline__ void xr2c_store(typename VecOf<R>::type *B, typename VecOf<R>::type *__restrict__ out,
+                                           long long sbase, int nl, const Geom &g, const LinePlan &planH,
+                                           const typename VecOf<R>::type *__restrict__ twX)
+{
+    typedef typename VecOf<R>::type V;
+    constexpr int LBSH = Log2<LB>::v;
+    const int H = g.H, KX = g.KX, Y = g.Y;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    fft_tile<false, LB, PERB>(B, LB, planH, twX);
+    const int npair = H / 2 + 1;
+    const R half = (R)0.5;
+    for (int e = tid; e < npair * LB; e += nt) {
+        const int k = e >> LBSH, l = e & (LB - 1);
+        if (k == 0) {
+            const V z0 = B[l];
+            B[l] = cmk<V>(z0.x + z0.y, (R)0);
+            B[H * LB + l] = cmk<V>(z0.x - z0.y, (R)0);
+        } else {
+            const int k2 = H - k;
+            const V av = B[k * LB + l], bv = B[k2 * LB + l];
+            const V s = cadd(av, cconj(bv)), d = csub(av, cconj(bv));
+            const V t = cmul(__ldg(&twX[k]), d);
+            const V xk = cmk<V>(half * (s.x + t.y), half * (s.y - t.x));
+            if (k2 != k) {
+                const V s2 = cadd(bv, cconj(av)), d2 = csub(bv, cconj(av));
+                const V t2 = cmul(__ldg(&twX[k2]), d2);
+                B[k2 * LB + l] = cmk<V>(half * (s2.x + t2.y), half * (s2.y - t2.x));
+            }
+            B[k * LB + l] = xk;
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < KX * LB; e += nt) {
+        const int kx = e >> LBSH, l = e & (LB - 1);
+        if (l < nl) out[sbase + (long long)kx * Y + l] = B[e];
+    }
+    __syncthreads();
+}
+
+// The Khachaturyan pointwise factor (pf/homoLinElast.go:10-17, 69-97):
+// s * H'(c) * (w - 2 e0 H(c)) with H = 3c^2 - 2c^3, H' = 6c - 6c^2.
+template <typename R> __device__ __forceinline__ R elastic_q(R c, R w, R e0, R s)
+{
+    const R Hc = (R)3 * c * c - (R)2 * c * c * c;
+    const R dH = (R)6 * c - (R)6 * c * c;
+    return s * (dH * (w - (R)2 * e0 * Hc));
+}
+
 // ------------------------------------------------------------------
 // x-pass: c2r (or real load) -> pointwise -> r2c
 // ------------------------------------------------------------------
@@ -86,35 +180,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_xpass(const X
     const V *__restrict__ twX = a.twX;
 
     if (a.in_mode == XIN_SPECTRAL) {
-        const V *__restrict__ in = a.in;
-        for (int e = tid; e < KX * LB; e += nt) {
-            const int kx = e >> LBSH, l = e & (LB - 1);
-            A[e] = (l < nl) ? in[sbase + (long long)kx * Y + l] : zero;
-        }
-        __syncthreads();
-        const int npair = H / 2 + 1;
-        for (int e = tid; e < npair * LB; e += nt) {
-            const int k = e >> LBSH, l = e & (LB - 1);
-            if (k == 0) {
-                const V a0 = A[l], b0 = A[H * LB + l];
-                const V s = cadd(a0, cconj(b0)), d = csub(a0, cconj(b0));
-                A[l] = cmk<V>(s.x - d.y, s.y + d.x);
-            } else {
-                const int k2 = H - k;
-                const V av = A[k * LB + l], bv = A[k2 * LB + l];
-                const V s = cadd(av, cconj(bv)), d = csub(av, cconj(bv));
-                const V t = cmulc(d, __ldg(&twX[k]));
-                const V zk = cmk<V>(s.x - t.y, s.y + t.x);
-                if (k2 != k) {
-                    const V s2 = cadd(bv, cconj(av)), d2 = csub(bv, cconj(av));
-                    const V t2 = cmulc(d2, __ldg(&twX[k2]));
-                    A[k2 * LB + l] = cmk<V>(s2.x - t2.y, s2.y + t2.x);
-                }
-                A[k * LB + l] = zk;
-            }
-        }
-        __syncthreads();
-        fft_tile<true, LB, PERB>(A, LB, a.planH, twX);
+        xload_c2r<R, LB, PERB>(A, a.in, sbase, nl, g, a.planH, twX);
     } else {
         const V *rin2 = reinterpret_cast<const V *>(a.rin) + ((long long)z * Y + y0) * H;
         for (int e = tid; e < LB * H; e += nt) {
@@ -154,42 +220,39 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_xpass(const X
         block_reduce_store(vals, a.red, shred);
     }
 
+    if (a.program == XP_ELASTIC_Q) {
+        // w = c2r(in2) into B, then q into B, then r2c into out[0]
+        xload_c2r<R, LB, PERB>(B, a.in2, sbase, nl, g, a.planH, twX);
+        const R e0 = (R)a.e0, es = (R)a.escale;
+        for (int e = tid; e < H * LB; e += nt) {
+            const V c = A[e], w = B[e];
+            B[e] = cmk<V>(elastic_q<R>(c.x, w.x, e0, es), elastic_q<R>(c.y, w.y, e0, es));
+        }
+        __syncthreads();
+        xr2c_store<R, LB, PERB>(B, a.out[0], sbase, nl, g, a.planH, twX);
+        return;
+    }
+
     for (int grp = 0; grp < a.ngrp_out; ++grp) {
+        double gsum = 0.0;
         for (int e = tid; e < H * LB; e += nt) {
             const V c = A[e];
-            B[e] = a.identity ? c : cmk<V>(poly_eval<R>(a.pw, grp, c.x), poly_eval<R>(a.pw, grp, c.y));
+            const V r = a.identity ? c : cmk<V>(poly_eval<R>(a.pw, grp, c.x), poly_eval<R>(a.pw, grp, c.y));
+            B[e] = r;
+            if (a.red2 && grp == a.redgrp && (e & (LB - 1)) < nl) gsum += (double)r.x + (double)r.y;
+        }
+        if (a.red2 && grp == a.redgrp) {
+            double vals[RED_SLOTS];
+#pragma unroll
+            for (int s2 = 0; s2 < RED_SLOTS; ++s2) vals[s2] = 0.0;
+            vals[RED_SUM] = gsum;
+            vals[RED_MIN] = INFINITY;
+            vals[RED_MAX] = -INFINITY;
+            __shared__ double shred2[32 * RED_SLOTS];
+            block_reduce_store(vals, a.red2, shred2);
         }
         __syncthreads();
-        fft_tile<false, LB, PERB>(B, LB, a.planH, twX);
-        const int npair = H / 2 + 1;
-        const R half = (R)0.5;
-        for (int e = tid; e < npair * LB; e += nt) {
-            const int k = e >> LBSH, l = e & (LB - 1);
-            if (k == 0) {
-                const V z0 = B[l];
-                B[l] = cmk<V>(z0.x + z0.y, (R)0);
-                B[H * LB + l] = cmk<V>(z0.x - z0.y, (R)0);
-            } else {
-                const int k2 = H - k;
-                const V av = B[k * LB + l], bv = B[k2 * LB + l];
-                const V s = cadd(av, cconj(bv)), d = csub(av, cconj(bv));
-                const V t = cmul(__ldg(&twX[k]), d);
-                const V xk = cmk<V>(half * (s.x + t.y), half * (s.y - t.x));
-                if (k2 != k) {
-                    const V s2 = cadd(bv, cconj(av)), d2 = csub(bv, cconj(av));
-                    const V t2 = cmul(__ldg(&twX[k2]), d2);
-                    B[k2 * LB + l] = cmk<V>(half * (s2.x + t2.y), half * (s2.y - t2.x));
-                }
-                B[k * LB + l] = xk;
-            }
-        }
-        __syncthreads();
-        V *__restrict__ out = a.out[grp];
-        for (int e = tid; e < KX * LB; e += nt) {
-            const int kx = e >> LBSH, l = e & (LB - 1);
-            if (l < nl) out[sbase + (long long)kx * Y + l] = B[e];
-        }
-        __syncthreads();
+        xr2c_store<R, LB, PERB>(B, a.out[grp], sbase, nl, g, a.planH, twX);
     }
 }
 
@@ -241,6 +304,35 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_pass(const Pa
         }
     };
 
+    if (a.mode == PM_ELASTIC_K) {
+        // w-hat = b(k) * H-hat / N along the last axis, then back (pf/homoLinElast.go:53-75)
+        V *__restrict__ buf = a.buf[0];
+        for (int e = tid; e < total; e += nt) {
+            int p, l;
+            decode(e, p, l);
+            sm[p * pitch + l] = (l < nl) ? buf[gbase + p * pstride + l * lstride] : zero;
+        }
+        __syncthreads();
+        fft_tile<false, LB, PERB>(sm, pitch, a.plan, a.tw);
+        const R invN = (R)a.upd.invN;
+        for (int e = tid; e < total; e += nt) {
+            int p, l;
+            decode(e, p, l);
+            if (l >= nl) continue;
+            const R b = a.bsym[gbase + p * pstride + l * lstride] * invN;
+            const V v = sm[p * pitch + l];
+            sm[p * pitch + l] = cmk<V>(v.x * b, v.y * b);
+        }
+        __syncthreads();
+        fft_tile<true, LB, PERB>(sm, pitch, a.plan, a.tw);
+        for (int e = tid; e < total; e += nt) {
+            int p, l;
+            decode(e, p, l);
+            if (l < nl) buf[gbase + p * pstride + l * lstride] = sm[p * pitch + l];
+        }
+        return;
+    }
+
     if (a.mode == PM_FWD || a.mode == PM_INV) {
         V *__restrict__ buf = a.buf[blockIdx.y];
         for (int e = tid; e < total; e += nt) {
@@ -275,6 +367,9 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_pass(const Pa
 
     const UpdTable &u = a.upd;
     const R dt = (R)u.dt, invN = (R)u.invN;
+    R gsc[GOPF_MAX_GROUPS];
+#pragma unroll
+    for (int b = 0; b < GOPF_MAX_GROUPS; ++b) gsc[b] = (b < u.ngrp && u.gscale[b]) ? (R)(*u.gscale[b]) : (R)1;
     const R fourpi2 = (R)39.478417604357434475337963999504; // 4 pi^2
     V *__restrict__ state = a.state;
     for (int e = tid; e < total; e += nt) {
@@ -305,7 +400,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_pass(const Pa
             // explicit part
             V nhat = zero;
             for (int b = 0; b < u.ngrp; ++b) {
-                R f = (R)1;
+                R f = gsc[b];
                 for (int q = 0; q < u.glap[b]; ++q) f *= mk;
                 const V tv = sm[b * tile + p * pitch + l];
                 nhat.x += f * tv.x;

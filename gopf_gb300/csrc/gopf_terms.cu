@@ -1,0 +1,207 @@
+// gopf_terms.cu -- device pieces of gopf's user-defined hot terms.
+//
+// Khachaturyan elasticity (pf/homoLinElast.go:47-99).  The reference
+// evaluates, per step, FFT(H), the effective force (elasticity/effectiveForce.go:26-35),
+// a 3x3 LU solve per frequency for the displacement
+// (elasticity/linearElasticity.go:33-63), the strains (67-83) and one
+// inverse + one forward transform per strain component.  All of that is
+// linear in H-hat, so it collapses to a scalar symbol
+//     b(k) = sum_{i<D} (A f~)_i (Gamma(f)^-1 A f)_i ,
+//     Gamma_mn(f) = sum_jl C_mjnl f_j f_l ,   A = C : eps*  (elasticity/rank4.go:62-75),
+// where f~ is f with Nyquist components zeroed, as Strain does.  The term is
+// then FFT[ H'(c) (IFFT(b H-hat)/N - 2 e0 H(c)) ].  b is tabulated once per
+// context in FP64 (this kernel) and stored in the state precision.  Because
+// the reference keeps f = +0.5 for both k and -k on Nyquist planes, its b is
+// not even there and its term has a small anti-Hermitian part; a real field
+// can only carry the Hermitian part, which is b symmetrised over (k, -k).
+//
+// VolumeConservingLP (pf/volumeConserving.go:31-50): the Lagrange multiplier
+// update after every step, done on the device from FP64 block sums of the
+// field and of the indicator so that the step stays capturable in a graph.
+#include <cmath>
+
+#include "gopf_ctx.h"
+#include "gopf_kernels.cuh"
+
+namespace gopf {
+
+struct ElasticParams {
+    double C[81];
+    double A[9];
+    int ndim;
+};
+
+__device__ __forceinline__ double fold_freq(long long i, long long n)
+{
+    double f = (double)i / (double)n;
+    return (f > 0.5) ? f - 1.0 : f;
+}
+
+__device__ double elastic_b(const ElasticParams &p, const double f[3])
+{
+    const double tol = 1e-10;
+    if (fabs(f[0]) < tol && fabs(f[1]) < tol && fabs(f[2]) < tol) return 0.0;
+    double ft[3];
+    for (int d = 0; d < 3; ++d) ft[d] = (fabs(fabs(f[d]) - 0.5) < tol) ? 0.0 : f[d];
+    double G[3][3], v[3];
+    for (int m = 0; m < 3; ++m) {
+        for (int n = 0; n < 3; ++n) {
+            double e = 0.0;
+            for (int j = 0; j < 3; ++j)
+                for (int l = 0; l < 3; ++l) e += p.C[m * 27 + j * 9 + n * 3 + l] * f[j] * f[l];
+            G[m][n] = e;
+        }
+        v[m] = p.A[m * 3 + 0] * f[0] + p.A[m * 3 + 1] * f[1] + p.A[m * 3 + 2] * f[2];
+    }
+    // Gaussian elimination with partial pivoting
+    for (int c = 0; c < 3; ++c) {
+        int best = c;
+        for (int r = c + 1; r < 3; ++r)
+            if (fabs(G[r][c]) > fabs(G[best][c])) best = r;
+        if (best != c) {
+            for (int k = 0; k < 3; ++k) {
+                double t = G[c][k];
+                G[c][k] = G[best][k];
+                G[best][k] = t;
+            }
+            double t = v[c];
+            v[c] = v[best];
+            v[best] = t;
+        }
+        for (int r = c + 1; r < 3; ++r) {
+            const double fct = G[r][c] / G[c][c];
+            for (int k = c; k < 3; ++k) G[r][k] -= fct * G[c][k];
+            v[r] -= fct * v[c];
+        }
+    }
+    double u[3];
+    for (int r = 2; r >= 0; --r) {
+        double s = v[r];
+        for (int q = r + 1; q < 3; ++q) s -= G[r][q] * u[q];
+        u[r] = s / G[r][r];
+    }
+    double b = 0.0;
+    for (int i = 0; i < p.ndim; ++i) {
+        const double af = p.A[i * 3 + 0] * ft[0] + p.A[i * 3 + 1] * ft[1] + p.A[i * 3 + 2] * ft[2];
+        b += af * u[i];
+    }
+    return b;
+}
+
+// out[z][kx][y] = (b(f) + b(f(-k))) / 2
+template <typename R> __global__ void k_elastic_symbol(Geom g, ElasticParams p, R *__restrict__ out)
+{
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < g.C;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long z = idx / g.S;
+        const long long rem = idx - z * g.S;
+        const long long kx = rem / g.Y;
+        const long long y = rem - kx * g.Y;
+        // reference order: f[0] row (y), f[1] col (kx), f[2] depth (z)
+        double f[3] = {fold_freq(y, g.Y), fold_freq(kx, g.X), (p.ndim == 3) ? fold_freq(z, g.Z) : 0.0};
+        double fm[3] = {fold_freq((g.Y - y) % g.Y, g.Y), fold_freq((g.X - kx) % g.X, g.X),
+                        (p.ndim == 3) ? fold_freq((g.Z - z) % g.Z, g.Z) : 0.0};
+        out[idx] = (R)(0.5 * (elastic_b(p, f) + elastic_b(p, fm)));
+    }
+}
+
+// Neumaier sum of slot `slot` over the block partials (single thread).
+__device__ double sum_partials(const double *part, int nblocks, int slot)
+{
+    double s = 0.0, c = 0.0;
+    for (int b = 0; b < nblocks; ++b) {
+        const double v = part[(long long)b * RED_SLOTS + slot];
+        const double t = s + v;
+        c += (fabs(s) >= fabs(v)) ? (s - t) + v : (v - t) + s;
+        s = t;
+    }
+    return s + c;
+}
+
+// vc = [lambda, current_integral, indicator_integral_prev, count, coef*lambda]
+__global__ void k_volcons_finalize(const double *__restrict__ red_field, const double *__restrict__ red_ind, int nblocks,
+                                   double dt, double coef, double *__restrict__ vc)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const double I = sum_partials(red_field, nblocks, RED_SUM);
+    const double S = sum_partials(red_ind, nblocks, RED_SUM);
+    const double count = vc[3];
+    if (count == 1.0) {
+        vc[1] = I; // IsFirstUpdate: remember the integral, keep the multiplier
+    } else if (count >= 2.0) {
+        vc[0] = vc[0] - (I - vc[1]) / (dt * vc[2]);
+        vc[1] = I;
+    }
+    vc[2] = S;
+    vc[3] = count + 1.0;
+    vc[4] = coef * vc[0];
+}
+
+// Hermitian projection of the self-conjugate planes kx = 0 and kx = X/2 of the
+// half spectrum: c(k) <- (c(k) + conj c(-k)) / 2 for the pairs (ky, kz) <-> (-ky, -kz).
+// A real field cannot feed back into the anti-Hermitian part of these planes,
+// so without the projection FFT round-off there grows like 1/(1 - dt L(k)) per
+// step in the unstable band of L (the complex-field reference carries that
+// part in its imaginary component, where the nonlinearity damps it).
+template <typename V> __global__ void k_hermitian_planes(V *__restrict__ c, Geom g)
+{
+    const long long per = (long long)g.Y * g.Z;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < 2 * per;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int plane = (int)(idx / per);
+        const long long r = idx - plane * per;
+        const long long z = r / g.Y, y = r - z * g.Y;
+        const long long zp = (g.Z - z) % g.Z, yp = (g.Y - y) % g.Y;
+        if (z * g.Y + y > zp * g.Y + yp) continue; // the partner's thread does the pair
+        const long long kx = plane ? g.H : 0;
+        const long long ia = z * g.S + kx * g.Y + y, ib = zp * g.S + kx * g.Y + yp;
+        const V a = c[ia], b = c[ib];
+        V m;
+        m.x = (a.x + b.x) * 0.5f;
+        m.y = (a.y - b.y) * 0.5f;
+        c[ia] = m;
+        m.y = -m.y;
+        c[ib] = m;
+    }
+}
+
+} // namespace gopf
+
+using namespace gopf;
+
+cudaError_t gopf_launch_hermitian_planes(gopf_ctx *ctx, void *state)
+{
+    const long long n = 2LL * ctx->g.Y * ctx->g.Z;
+    const unsigned blocks = (unsigned)std::min<long long>((n + 255) / 256, 152 * 8);
+    if (ctx->prec == GOPF_FP32) k_hermitian_planes<float2><<<blocks, 256, 0, ctx->stream>>>((float2 *)state, ctx->g);
+    else k_hermitian_planes<double2><<<blocks, 256, 0, ctx->stream>>>((double2 *)state, ctx->g);
+    return cudaGetLastError();
+}
+
+int gopf_elastic_table(gopf_ctx *ctx)
+{
+    ElasticParams p;
+    memcpy(p.C, ctx->el_C, sizeof(p.C));
+    memcpy(p.A, ctx->el_A, sizeof(p.A));
+    p.ndim = ctx->ndim;
+    const size_t eb = (ctx->prec == GOPF_FP32) ? sizeof(float) : sizeof(double);
+    if (!ctx->d_bsym) {
+        cudaError_t e = cudaMalloc(&ctx->d_bsym, eb * ctx->g.C);
+        if (e != cudaSuccess) return gopf_fail(ctx, GOPF_ERR_OOM, "cudaMalloc(elastic symbol)");
+        ctx->dev_bytes += eb * ctx->g.C;
+    }
+    const unsigned blocks = (unsigned)std::min<long long>((ctx->g.C + 255) / 256, 152 * 32);
+    if (ctx->prec == GOPF_FP32) k_elastic_symbol<float><<<blocks, 256, 0, ctx->stream>>>(ctx->g, p, (float *)ctx->d_bsym);
+    else k_elastic_symbol<double><<<blocks, 256, 0, ctx->stream>>>(ctx->g, p, (double *)ctx->d_bsym);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return gopf_fail(ctx, GOPF_ERR_CUDA, std::string("elastic symbol: ") + cudaGetErrorString(e));
+    return GOPF_OK;
+}
+
+cudaError_t gopf_launch_volcons_finalize(gopf_ctx *ctx)
+{
+    k_volcons_finalize<<<1, 32, 0, ctx->stream>>>(ctx->d_red, ctx->d_red2, ctx->nred_blocks, ctx->vc_dt, ctx->vc_coef,
+                                                  ctx->d_vc);
+    return cudaGetLastError();
+}

@@ -54,6 +54,9 @@ struct UpdTable {
     double imp[GOPF_MAX_IMP];
     int ngrp;
     int glap[GOPF_MAX_GROUPS];
+    // optional device-resident scale of a group (the volume-conserving Lagrange
+    // multiplier, updated on the device every step); nullptr = 1
+    const double *gscale[GOPF_MAX_GROUPS];
 };
 
 // Reduction slots written by the x-pass (FP64, compensated per block)
@@ -79,9 +82,20 @@ template <typename R> struct XPassArgs {
     int identity;         // 1: output group 0 is r2c(c) itself
     PwTable pw;
     double *red;          // optional: per-block partial sums [gridDim.x*gridDim.y][RED_SLOTS]
+    // program XP_ELASTIC_Q: out[0] = r2c(escale * H'(c) * (w - 2 e0 H(c))), c = c2r(in), w = c2r(in2)
+    int program;
+    const V *in2;
+    double e0;
+    double escale;
+    // optional: per-block FP64 sums of group `redgrp`'s real-space values into red2[block]
+    int redgrp;
+    double *red2;
 };
 
-enum PassMode { PM_FWD = 0, PM_INV = 1, PM_FUSED = 2, PM_INIT = 3 };
+enum XProgram { XP_POLY = 0, XP_ELASTIC_Q = 1 };
+
+// PM_ELASTIC_K: forward transform buf[0], multiply by bsym(k)/N, inverse transform in place
+enum PassMode { PM_FWD = 0, PM_INV = 1, PM_FUSED = 2, PM_INIT = 3, PM_ELASTIC_K = 4 };
 
 template <typename R> struct PassArgs {
     typedef typename VecOf<R>::type V;
@@ -94,6 +108,7 @@ template <typename R> struct PassArgs {
     V *state;             // c-hat (FUSED reads+writes, INIT writes)
     V *tout;              // FUSED/INIT: inverse-transformed c_new/N goes here
     UpdTable upd;
+    const R *bsym;        // PM_ELASTIC_K: elastic symbol in the spectral layout
 };
 
 } // namespace gopf

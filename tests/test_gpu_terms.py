@@ -1,0 +1,183 @@
+"""GPU parity of gopf's user-defined hot terms against the FP64 oracle.
+
+- HomogeneousModulusLinElast (pf/homoLinElast.go) entering a Cahn-Hilliard
+  equation as "- LAP LIN_ELAST", cubic stiffness (elasticity/rank4.go:113-128),
+  including the reference's first step, where the term sees a zero field.
+- VolumeConservingLP (pf/volumeConserving.go) with its per-step multiplier update.
+Tolerances: FP64 mode rel-L2 <= 1e-11, FP32 mode rel-L2 <= 1e-4.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+CH_EL = "dconc/dt = LAP conc^3 + m1*LAP conc + m1*gamma*LAP^2 conc - LAP LIN_ELAST"
+
+
+def cubic(c11, c12, c44):
+    C = np.zeros((3, 3, 3, 3))
+    for i in range(3):
+        C[i, i, i, i] = c11
+    for i in range(3):
+        for j in range(i + 1, 3):
+            C[i, i, j, j] = c12
+            C[j, j, i, i] = c12
+            C[i, j, i, j] = c44
+            C[j, i, j, i] = c44
+    return C
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def elastic_gpu(dims, prec, c0, dt, gamma=1.0, misfit=None, C=None):
+    import gopf_gb300 as G
+
+    m = G.Model(dims, prec, device=0)
+    m.add_field("conc")
+    m.add_scalar("gamma", gamma)
+    m.add_scalar("m1", -1.0)
+    m.register_elastic("LIN_ELAST", "conc", cubic(1.0, 0.6, 0.5) if C is None else C,
+                       np.eye(3) * 0.01 if misfit is None else misfit)
+    m.add_equation(CH_EL)
+    m.init()
+    m.set_stepper("euler", dt)
+    m.upload(0, c0)
+    return m
+
+
+def elastic_oracle(O, dims, c0, gamma=1.0, misfit=None, C=None):
+    m = O.cahn_hilliard(dims, gamma=gamma)
+    m.add_elastic(0, 0, cubic(1.0, 0.6, 0.5) if C is None else C, np.eye(3) * 0.01 if misfit is None else misfit,
+                  coef=-1.0, lap=1)
+    m.set_field(0, c0)
+    return m
+
+
+def test_elastic_summary_counts_user_term():
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+
+    m = elastic_gpu([16, 16], "fp64", uniform_field(3, 256, 0.3, 0.02), 0.02)
+    assert m.summary(0) == (2, 2)
+
+
+@pytest.mark.parametrize("dims,steps", [([32, 32], 50), ([16, 16, 16], 20), ([12, 12, 12], 10)])
+def test_ch_elastic_fp64_parity(oracle, dims, steps):
+    """CH + Khachaturyan elasticity (the 256^3 elastic configuration's physics at small size)."""
+    from gopf_gb300.synthetic import uniform_field
+
+    n = int(np.prod(dims))
+    c0 = uniform_field(3, n, 0.3, 0.02)
+    g = elastic_gpu(dims, "fp64", c0, 0.02)
+    g.step(steps)
+    o = elastic_oracle(oracle, dims, c0)
+    o.step_euler(0.02, steps)
+    assert rel_l2(g.download(0).real, o.field(0).real) <= 1e-11
+
+
+def test_ch_elastic_large_misfit_fp64(oracle):
+    """A misfit large enough for the elastic term to dominate (shear misfit, 2D)."""
+    from gopf_gb300.synthetic import uniform_field
+
+    dims = [32, 32]
+    mis = np.array([[0.2, 0.05, 0.0], [0.05, -0.1, 0.0], [0.0, 0.0, 0.0]])
+    C = cubic(110.0, 60.0, 30.0)
+    c0 = uniform_field(4, 32 * 32, 0.5, 0.3)
+    g = elastic_gpu(dims, "fp64", c0, 0.001, misfit=mis, C=C)
+    g.step(30)
+    o = elastic_oracle(oracle, dims, c0, misfit=mis, C=C)
+    o.step_euler(0.001, 30)
+    assert rel_l2(g.download(0).real, o.field(0).real) <= 1e-11
+
+
+def test_elastic_first_step_sees_zero_field():
+    """Step 0 of the reference evaluates the elastic term at h = 0 (pf/homoLinElast.go:145), i.e. not at all."""
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+
+    dims = [32, 32]
+    c0 = uniform_field(3, 32 * 32, 0.3, 0.02)
+    g = elastic_gpu(dims, "fp64", c0, 0.02)
+    g.step(1)
+    p = G.Model(dims, "fp64", device=0)
+    p.add_field("conc")
+    p.add_scalar("gamma", 1.0)
+    p.add_scalar("m1", -1.0)
+    p.add_equation("dconc/dt = LAP conc^3 + m1*LAP conc + m1*gamma*LAP^2 conc")
+    p.init()
+    p.set_stepper("euler", 0.02)
+    p.upload(0, c0)
+    p.step(1)
+    assert np.array_equal(g.download(0), p.download(0))
+    g.step(1)
+    p.step(1)
+    assert not np.array_equal(g.download(0), p.download(0))
+
+
+def test_ch_elastic_fp32_parity(oracle):
+    from gopf_gb300.synthetic import uniform_field
+
+    dims = [32, 32, 32]
+    c0 = uniform_field(3, 32 ** 3, 0.3, 0.02)
+    g = elastic_gpu(dims, "fp32", c0, 0.02)
+    g.step(30)
+    o = elastic_oracle(oracle, dims, c0)
+    o.step_euler(0.02, 30)
+    assert rel_l2(g.download(0).real, o.field(0).real) <= 1e-4
+
+
+def test_elastic_graph_equals_eager():
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+
+    dims = [64, 64, 64]
+    c0 = uniform_field(3, 64 ** 3, 0.3, 0.02)
+    a = elastic_gpu(dims, "fp32", c0, 0.02)
+    b = elastic_gpu(dims, "fp32", c0, 0.02)
+    b.set_option(G._lib.OPT_USE_GRAPHS, 0)
+    a.step(21)
+    b.step(21)
+    assert np.array_equal(a.download(0), b.download(0))
+
+
+def _volcons_models(O, dims, c0, dt):
+    import gopf_gb300 as G
+
+    g = G.Model(dims, "fp64", device=0)
+    g.add_field("phi")
+    g.add_scalar("m1", -1.0)
+    g.register_function("IND", G.DER_INDICATOR_D, "phi")
+    g.register_volcons("CONSERVE", "phi", "IND", dt)
+    g.add_equation("dphi/dt = m1*phi + CONSERVE + phi^2")
+    g.init()
+    g.set_stepper("euler", dt)
+    g.upload(0, c0)
+    o = O.Model(dims, 1)
+    o.set_field(0, c0)
+    ind = o.add_indicator(0, O.DER_INDICATOR_D)
+    sq = o.add_product([0], [2])
+    o.add_term(0, -1.0, implicit=True)
+    o.add_volcons(0, 0, ind, dt)
+    o.add_term(0, 1.0, src_kind=O.SRC_DERIVED, src=sq)
+    return g, o
+
+
+@pytest.mark.parametrize("dims", [[16, 16], [8, 8, 8]])
+def test_volume_conserving_fp64_parity(oracle, dims):
+    """Non-conserved dynamics held at constant volume by the Lagrange multiplier (pf/volumeConserving.go)."""
+    from gopf_gb300.synthetic import uniform_field
+
+    n = int(np.prod(dims))
+    c0 = uniform_field(7, n, 0.5, 0.3)
+    dt = 0.01
+    g, o = _volcons_models(oracle, dims, c0, dt)
+    g.step(40)
+    o.step_euler(dt, 40)
+    assert rel_l2(g.download(0).real, o.field(0).real) <= 1e-11
+    # volume held near the value after the first step
+    g1, o1 = _volcons_models(oracle, dims, c0, dt)
+    o1.step_euler(dt, 1)
+    v1 = o1.field(0).real.sum()
+    assert abs(g.mass(0) - v1) < 0.02 * abs(v1)
