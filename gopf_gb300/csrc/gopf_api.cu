@@ -243,7 +243,7 @@ static void ctx_free(gopf_ctx *ctx)
         if (p) cudaFree(p);
     for (int i = 1; i < GOPF_MAX_GROUPS; ++i)
         if (ctx->d_U[i]) cudaFree(ctx->d_U[i]);
-    void *more[] = {ctx->d_bsym, ctx->d_U0, ctx->d_UH, ctx->d_vc, ctx->d_red2};
+    void *more[] = {ctx->d_bsym, ctx->d_U0, ctx->d_UH, ctx->d_vc, ctx->d_red2, ctx->d_rkF};
     for (void *p : more)
         if (p) cudaFree(p);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -800,9 +800,71 @@ template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx)
     return cudaSuccess;
 }
 
+// One RK4 step (pf/rk4.go:29-127): four explicit-RHS evaluations, each an
+// x-pass + forward y + a fused last-axis pass that accumulates
+// F = c + dt(k1 + 2k2 + 2k3 + k4)/6 and forms the next stage's input
+// (c + a k)/(1 - a L); the last stage sets c = F/(1 - dt L).
+template <typename R> static cudaError_t enqueue_rk4(gopf_ctx *ctx)
+{
+    typedef typename VecOf<R>::type V;
+    const int G = ctx->ngroups;
+    V *T = (V *)ctx->d_T;
+    V *U[GOPF_MAX_GROUPS];
+    U[0] = T;
+    for (int b = 1; b < GOPF_MAX_GROUPS; ++b) U[b] = (V *)ctx->d_U[b];
+    const bool is3d = ctx->g.Z > 1;
+    const double dt = ctx->dt;
+    const double afin[4] = {dt / 6.0, dt / 3.0, dt / 3.0, dt / 6.0};
+    const double ay[3] = {0.5 * dt, 0.5 * dt, dt};
+    for (int stage = 1; stage <= 4; ++stage) {
+        if (G > 0) {
+            XPassArgs<R> xa = xargs<R>(ctx);
+            xa.in_mode = XIN_SPECTRAL;
+            xa.in = T;
+            for (int b = 0; b < G; ++b) xa.out[b] = U[b];
+            xa.ngrp_out = G;
+            xa.pw = ctx->pw;
+            LK(launch_xpass<R>(xa, ctx->LBx, ctx->stream));
+            if (is3d) {
+                PassArgs<R> pa = pargs<R>(ctx, false);
+                pa.mode = PM_FWD;
+                for (int b = 0; b < G; ++b) pa.buf[b] = U[b];
+                pa.nbuf = G;
+                LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+            }
+        }
+        UpdTable u = ctx->upd;
+        u.dt = dt;
+        u.invN = 1.0 / (double)ctx->g.N;
+        u.rk_stage = stage;
+        u.rk_afin = afin[stage - 1];
+        u.rk_ay = (stage < 4) ? ay[stage - 1] : 0.0;
+        u.rk_fden = (stage < 4) ? ay[stage - 1] : dt;
+        const int nb = std::max(G, 1);
+        PassArgs<R> fa = pargs<R>(ctx, is3d);
+        fa.mode = PM_FUSED;
+        for (int b = 0; b < nb; ++b) fa.buf[b] = U[b];
+        fa.nbuf = nb;
+        fa.state = (V *)ctx->d_state;
+        fa.tout = T;
+        fa.upd = u;
+        fa.rkF = (V *)ctx->d_rkF;
+        LK(is3d ? launch_spass<R>(fa, ctx->LBz, ctx->stream) : launch_cpass<R>(fa, ctx->LBy, ctx->stream));
+        if (stage == 4) LK(gopf_launch_hermitian_planes(ctx, ctx->d_state));
+        if (is3d) {
+            PassArgs<R> ia = pargs<R>(ctx, false);
+            ia.mode = PM_INV;
+            ia.buf[0] = T;
+            ia.nbuf = 1;
+            LK(launch_cpass<R>(ia, ctx->LBy, ctx->stream));
+        }
+    }
+    return cudaSuccess;
+}
+
 template <typename R> static cudaError_t enqueue_steps(gopf_ctx *ctx, int n)
 {
-    for (int i = 0; i < n; ++i) LK(enqueue_euler<R>(ctx));
+    for (int i = 0; i < n; ++i) LK(ctx->stepper == GOPF_STEPPER_RK4 ? enqueue_rk4<R>(ctx) : enqueue_euler<R>(ctx));
     return cudaSuccess;
 }
 
@@ -941,9 +1003,13 @@ extern "C" int gopf_step(gopf_ctx *ctx, long long nsteps)
     if (!ctx->initialised) return gopf_fail(ctx, GOPF_ERR_STATE, "model not initialised (gopf_init/gopf_set_terms)");
     if (!(ctx->dt > 0.0)) return gopf_fail(ctx, GOPF_ERR_STATE, "no stepper set (gopf_set_stepper)");
     if (!ctx->state_valid) return gopf_fail(ctx, GOPF_ERR_STATE, "field has not been uploaded");
-    if (ctx->stepper != GOPF_STEPPER_EULER) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "stepper not available yet");
     int rc;
     if ((rc = set_device(ctx))) return rc;
+    if (ctx->stepper == GOPF_STEPPER_RK4) {
+        if (ctx->has_elastic || ctx->has_volcons)
+            return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "user-defined terms are stepped with Euler only");
+        if ((rc = alloc_spectral(ctx, &ctx->d_rkF))) return rc;
+    }
     long long left = nsteps;
     if (ctx->has_elastic && !ctx->el_primed && left > 0) {
         // first step ever: the elastic term sees the reference's zero h-field

@@ -115,6 +115,8 @@ struct gopf_ctx {
     double *d_vc = nullptr;   // [lambda, current integral, previous indicator integral, count, coef*lambda]
     double *d_red2 = nullptr; // block sums of the indicator
 
+    void *d_rkF = nullptr; // RK4 accumulator
+
     // per-kernel profiling (gopf_profile_step): events recorded after each launch
     std::vector<cudaEvent_t> *prof_events = nullptr;
     size_t prof_next = 0;

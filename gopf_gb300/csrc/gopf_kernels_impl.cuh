@@ -269,15 +269,36 @@ template <typename R> __device__ __forceinline__ R fsq_index(int i, int n)
 
 // Tile element mapping:
 //   CONTIG : tile = LB consecutive lines q0.. of length n; global (q, p) = q*n + p
-//            smem pitch LB+1, iteration order line-major (coalesced global)
+//            smem pitch LB+1, iteration line-major (a warp reads 32 consecutive p)
 //   STRIDED: tile = LB consecutive inner indices i0.. of a pos-stride S array;
-//            global (p, i) = p*S + i; smem pitch LB; iteration order pos-major
+//            global (p, i) = p*S + i; smem pitch LB; iteration pos-major (LB
+//            consecutive i form one 128-byte segment)
+template <int LB, bool CONTIG, typename F> __device__ __forceinline__ void tile_foreach(int n, F &&f)
+{
+    constexpr int LBSH = Log2<LB>::v;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    if (CONTIG) {
+        if (n >= nt) {
+            for (int l = 0; l < LB; ++l)
+#pragma unroll 4
+                for (int p = tid; p < n; p += nt) f(p, l);
+        } else {
+            for (int e = tid; e < n * LB; e += nt) {
+                const int l = e / n;
+                f(e - l * n, l);
+            }
+        }
+    } else {
+#pragma unroll 4
+        for (int e = tid; e < n * LB; e += nt) f(e >> LBSH, e & (LB - 1));
+    }
+}
+
 template <typename R, int LB, int PERB, bool CONTIG>
 __global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_pass(const PassArgs<R> a)
 {
     typedef typename VecOf<R>::type V;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int LBSH = Log2<LB>::v;
     constexpr int pitch = CONTIG ? LB + 1 : LB;
     const Geom &g = a.g;
     const int n = a.plan.n;
@@ -291,77 +312,69 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_pass(const Pa
     const int tile = n * pitch;
     V *sm = reinterpret_cast<V *>(smem_raw);
     const V zero = cmk<V>((R)0, (R)0);
-    const int total = n * LB;
-
-    // element e of the iteration space -> (p, l)
-    auto decode = [&](int e, int &p, int &l) {
-        if (CONTIG) {
-            l = e / n;
-            p = e - l * n;
-        } else {
-            p = e >> LBSH;
-            l = e & (LB - 1);
-        }
+    auto gidx = [&](int p, int l) -> long long { return gbase + p * pstride + l * lstride; };
+    auto load = [&](V *dst, const V *__restrict__ src) {
+        tile_foreach<LB, CONTIG>(n, [&](int p, int l) { dst[p * pitch + l] = (l < nl) ? src[gidx(p, l)] : zero; });
     };
+    auto store = [&](V *__restrict__ dst, const V *s) {
+        tile_foreach<LB, CONTIG>(n, [&](int p, int l) {
+            if (l < nl) dst[gidx(p, l)] = s[p * pitch + l];
+        });
+    };
+
+    if (a.mode == PM_FWD || a.mode == PM_INV) {
+        V *__restrict__ buf = a.buf[blockIdx.y];
+        load(sm, buf);
+        __syncthreads();
+        if (a.mode == PM_FWD) fft_tile<false, LB, PERB>(sm, pitch, a.plan, a.tw);
+        else fft_tile<true, LB, PERB>(sm, pitch, a.plan, a.tw);
+        store(buf, sm);
+        return;
+    }
 
     if (a.mode == PM_ELASTIC_K) {
         // w-hat = b(k) * H-hat / N along the last axis, then back (pf/homoLinElast.go:53-75)
         V *__restrict__ buf = a.buf[0];
-        for (int e = tid; e < total; e += nt) {
-            int p, l;
-            decode(e, p, l);
-            sm[p * pitch + l] = (l < nl) ? buf[gbase + p * pstride + l * lstride] : zero;
-        }
+        load(sm, buf);
         __syncthreads();
         fft_tile<false, LB, PERB>(sm, pitch, a.plan, a.tw);
         const R invN = (R)a.upd.invN;
-        for (int e = tid; e < total; e += nt) {
-            int p, l;
-            decode(e, p, l);
-            if (l >= nl) continue;
-            const R b = a.bsym[gbase + p * pstride + l * lstride] * invN;
+        tile_foreach<LB, CONTIG>(n, [&](int p, int l) {
+            if (l >= nl) return;
+            const R b = a.bsym[gidx(p, l)] * invN;
             const V v = sm[p * pitch + l];
             sm[p * pitch + l] = cmk<V>(v.x * b, v.y * b);
-        }
+        });
         __syncthreads();
         fft_tile<true, LB, PERB>(sm, pitch, a.plan, a.tw);
-        for (int e = tid; e < total; e += nt) {
-            int p, l;
-            decode(e, p, l);
-            if (l < nl) buf[gbase + p * pstride + l * lstride] = sm[p * pitch + l];
-        }
-        return;
-    }
-
-    if (a.mode == PM_FWD || a.mode == PM_INV) {
-        V *__restrict__ buf = a.buf[blockIdx.y];
-        for (int e = tid; e < total; e += nt) {
-            int p, l;
-            decode(e, p, l);
-            sm[p * pitch + l] = (l < nl) ? buf[gbase + p * pstride + l * lstride] : zero;
-        }
-        __syncthreads();
-        if (a.mode == PM_FWD) fft_tile<false, LB, PERB>(sm, pitch, a.plan, a.tw);
-        else fft_tile<true, LB, PERB>(sm, pitch, a.plan, a.tw);
-        for (int e = tid; e < total; e += nt) {
-            int p, l;
-            decode(e, p, l);
-            if (l < nl) buf[gbase + p * pstride + l * lstride] = sm[p * pitch + l];
-        }
+        store(buf, sm);
         return;
     }
 
     // FUSED / INIT: all groups are loaded and forward transformed
     const int nb = a.nbuf;
-    for (int b = 0; b < nb; ++b) {
-        const V *__restrict__ buf = a.buf[b];
-        V *s = sm + b * tile;
-        for (int e = tid; e < total; e += nt) {
-            int p, l;
-            decode(e, p, l);
-            s[p * pitch + l] = (l < nl) ? buf[gbase + p * pstride + l * lstride] : zero;
+    // squared frequencies: per line (the two axes the line does not run along)
+    // and per position (the axis it runs along), in cycles/sample
+    R *fline = reinterpret_cast<R *>(sm + nb * tile);
+    R *fpos = fline + LB;
+    for (int b = 0; b < nb; ++b) load(sm + b * tile, a.buf[b]);
+    for (int l = tid; l < LB; l += nt) {
+        const long long q = l0 + l;
+        R f2 = (R)0;
+        if (q < nlines) {
+            if (CONTIG) { // line = (z, kx), position = y
+                const int zz = (int)(q / g.KX), kx = (int)(q - (long long)zz * g.KX);
+                const R fx = (R)kx / (R)g.X;
+                f2 = fx * fx + fsq_index<R>(zz, g.Z);
+            } else { // line = (kx, y), position = z
+                const int kx = (int)(q / g.Y), y = (int)(q - (long long)kx * g.Y);
+                const R fx = (R)kx / (R)g.X;
+                f2 = fx * fx + fsq_index<R>(y, g.Y);
+            }
         }
+        fline[l] = f2;
     }
+    for (int p = tid; p < n; p += nt) fpos[p] = CONTIG ? fsq_index<R>(p, g.Y) : fsq_index<R>(p, g.Z);
     __syncthreads();
     for (int b = 0; b < nb; ++b) fft_tile<false, LB, PERB>(sm + b * tile, pitch, a.plan, a.tw);
 
@@ -372,32 +385,14 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_pass(const Pa
     for (int b = 0; b < GOPF_MAX_GROUPS; ++b) gsc[b] = (b < u.ngrp && u.gscale[b]) ? (R)(*u.gscale[b]) : (R)1;
     const R fourpi2 = (R)39.478417604357434475337963999504; // 4 pi^2
     V *__restrict__ state = a.state;
-    for (int e = tid; e < total; e += nt) {
-        int p, l;
-        decode(e, p, l);
-        if (l >= nl) continue;
-        const long long gi = gbase + p * pstride + l * lstride;
+    tile_foreach<LB, CONTIG>(n, [&](int p, int l) {
+        if (l >= nl) return;
+        const long long gi = gidx(p, l);
         V cn;
         if (a.mode == PM_INIT) {
             cn = sm[p * pitch + l];
         } else {
-            // frequency of this element
-            int kx, y, zz;
-            if (CONTIG) {
-                const long long q = l0 + l;
-                zz = (int)(q / g.KX);
-                kx = (int)(q - (long long)zz * g.KX);
-                y = p;
-            } else {
-                const long long i = l0 + l;
-                kx = (int)(i / g.Y);
-                y = (int)(i - (long long)kx * g.Y);
-                zz = p;
-            }
-            const R fx = (R)kx / (R)g.X;
-            const R ksq = fourpi2 * (fx * fx + fsq_index<R>(y, g.Y) + fsq_index<R>(zz, g.Z));
-            const R mk = -ksq;
-            // explicit part
+            const R mk = -fourpi2 * (fline[l] + fpos[p]); // -k^2
             V nhat = zero;
             for (int b = 0; b < u.ngrp; ++b) {
                 R f = gsc[b];
@@ -406,24 +401,35 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_pass(const Pa
                 nhat.x += f * tv.x;
                 nhat.y += f * tv.y;
             }
-            // implicit symbol
+            // implicit symbol L = sum_p imp[p] (-k^2)^p
             R L = (R)0;
             for (int q = u.nimp - 1; q >= 0; --q) L = L * mk + (R)u.imp[q];
-            const R den = (R)1 - dt * L;
             const V c0 = state[gi];
-            cn = cmk<V>((c0.x + dt * nhat.x) / den, (c0.y + dt * nhat.y) / den);
+            if (u.rk_stage > 0) {
+                const R af = (R)u.rk_afin;
+                V F = (u.rk_stage == 1) ? c0 : a.rkF[gi];
+                F = cmk<V>(F.x + af * nhat.x, F.y + af * nhat.y);
+                if (u.rk_stage < 4) {
+                    a.rkF[gi] = F;
+                    const R ay = (R)u.rk_ay;
+                    const R d = (R)1 - (R)u.rk_fden * L;
+                    const V nx = cmk<V>((c0.x + ay * nhat.x) / d, (c0.y + ay * nhat.y) / d);
+                    sm[p * pitch + l] = cmk<V>(nx.x * invN, nx.y * invN);
+                    return; // the state changes only in the last stage
+                }
+                const R d = (R)1 - dt * L;
+                cn = cmk<V>(F.x / d, F.y / d);
+            } else {
+                const R den = (R)1 - dt * L;
+                cn = cmk<V>((c0.x + dt * nhat.x) / den, (c0.y + dt * nhat.y) / den);
+            }
         }
         state[gi] = cn;
         sm[p * pitch + l] = cmk<V>(cn.x * invN, cn.y * invN);
-    }
+    });
     __syncthreads();
     fft_tile<true, LB, PERB>(sm, pitch, a.plan, a.tw);
-    V *__restrict__ tout = a.tout;
-    for (int e = tid; e < total; e += nt) {
-        int p, l;
-        decode(e, p, l);
-        if (l < nl) tout[gbase + p * pstride + l * lstride] = sm[p * pitch + l];
-    }
+    store(a.tout, sm);
 }
 
 // ------------------------------------------------------------------
@@ -492,7 +498,8 @@ template <typename R, int LB, bool CONTIG> static cudaError_t launch_pass_lb(con
     const int n = a.plan.n;
     const bool fused = (a.mode == PM_FUSED || a.mode == PM_INIT);
     const int nsm = fused ? a.nbuf : 1;
-    const int smem = CONTIG ? cpass_smem_bytes(a.g, n, LB, nsm, sizeof(V)) : spass_smem_bytes(a.g, n, LB, nsm, sizeof(V));
+    int smem = CONTIG ? cpass_smem_bytes(a.g, n, LB, nsm, sizeof(V)) : spass_smem_bytes(a.g, n, LB, nsm, sizeof(V));
+    if (fused) smem += (LB + n) * (int)sizeof(R); // frequency tables
     auto kern = k_pass<R, LB, perb<R>(), CONTIG>;
     static int have = 48 * 1024; // one per kernel instantiation
     cudaError_t e = ensure_smem(kern, smem, have);

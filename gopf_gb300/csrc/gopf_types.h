@@ -57,6 +57,11 @@ struct UpdTable {
     // optional device-resident scale of a group (the volume-conserving Lagrange
     // multiplier, updated on the device every step); nullptr = 1
     const double *gscale[GOPF_MAX_GROUPS];
+    // RK4 stage (pf/rk4.go:29-127); 0 = Euler.  With k the explicit RHS of this stage:
+    //   stage 1: F = c + afin k          else F += afin k
+    //   stage < 4: next = (c + ay k) / (1 - fden L)      stage 4: c = F / (1 - dt L)
+    int rk_stage;
+    double rk_afin, rk_ay, rk_fden;
 };
 
 // Reduction slots written by the x-pass (FP64, compensated per block)
@@ -109,6 +114,7 @@ template <typename R> struct PassArgs {
     V *tout;              // FUSED/INIT: inverse-transformed c_new/N goes here
     UpdTable upd;
     const R *bsym;        // PM_ELASTIC_K: elastic symbol in the spectral layout
+    V *rkF;               // RK4 accumulator (FUSED with upd.rk_stage > 0)
 };
 
 } // namespace gopf

@@ -207,3 +207,51 @@ def test_mass_conserved_3d_256_fp32():
     d = g.download(0).real
     assert np.all(np.isfinite(d))
     assert abs(d.sum() - c0.sum()) / n <= 1e-6
+
+
+# ---------------------------------------------------------------- RK4 (pf/rk4.go)
+
+def test_rk4_simple_model_gpu():
+    """TestSimpleModel (pf/rk4_test.go:14-54): dfield/dt = rate*field^2, RK4 dt 0.1, 10 steps, 1e-6."""
+    import gopf_gb300 as G
+
+    m = G.Model([8, 8], "fp64", device=0)
+    m.add_field("field")
+    m.add_scalar("rate", -1.0)
+    m.add_equation("dfield/dt = rate*field^2")
+    m.init()
+    m.set_stepper("rk4", 0.1)
+    m.upload(0, np.ones(64))
+    m.step(10)
+    assert np.all(np.abs(m.download(0).real - 0.5) < 1e-6)
+
+
+def test_rk4_with_implicit_gpu():
+    """TestWithImplicit (pf/rk4_test.go:61-99): logistic growth, RK4 dt 0.01, 100 steps, 1e-3."""
+    import gopf_gb300 as G
+
+    m = G.Model([8, 8], "fp64", device=0)
+    m.add_field("field")
+    m.add_scalar("rate", -1.0)
+    m.add_equation("dfield/dt = field + rate*field^2")
+    m.init()
+    m.set_stepper("rk4", 0.01)
+    m.upload(0, np.full(64, 0.5))
+    m.step(100)
+    exp = math.exp(1.0) / (1.0 + math.exp(1.0))
+    assert np.all(np.abs(m.download(0).real - exp) < 1e-3)
+
+
+@pytest.mark.parametrize("dims,steps,prec,tol", [([64, 64], 100, "fp64", 1e-11), ([16, 16, 16], 20, "fp64", 1e-11),
+                                                  ([32, 32, 32], 30, "fp32", 1e-4)])
+def test_rk4_cahn_hilliard_parity(oracle, dims, steps, prec, tol):
+    from gopf_gb300.synthetic import uniform_field
+
+    n = int(np.prod(dims))
+    c0 = uniform_field(6, n, 0.5 if len(dims) == 2 else 0.0, 0.05 if len(dims) == 2 else 0.1)
+    g = ch_gpu(dims, prec, 1.0, 0.1, c0)
+    g.set_stepper("rk4", 0.1)
+    g.step(steps)
+    o = ch_oracle(oracle, dims, 1.0, c0)
+    o.step_rk4(0.1, steps)
+    assert rel_l2(g.download(0).real, o.field(0).real) <= tol

@@ -78,7 +78,12 @@ def test_ch_elastic_fp64_parity(oracle, dims, steps):
 
 
 def test_ch_elastic_large_misfit_fp64(oracle):
-    """A misfit large enough for the elastic term to dominate (shear misfit, 2D)."""
+    """A misfit large enough for the elastic term to dominate (shear misfit, 2D).
+
+    Here the reference's anti-Hermitian Nyquist remainder (f = +0.5 at k and -k) gives its
+    complex field imaginary parts of ~1e-4 that feed back through c^3; a real field has the
+    semantics of the oracle with the field projected onto its real part after every step,
+    which is what the device must match to 1e-11."""
     from gopf_gb300.synthetic import uniform_field
 
     dims = [32, 32]
@@ -88,7 +93,10 @@ def test_ch_elastic_large_misfit_fp64(oracle):
     g = elastic_gpu(dims, "fp64", c0, 0.001, misfit=mis, C=C)
     g.step(30)
     o = elastic_oracle(oracle, dims, c0, misfit=mis, C=C)
-    o.step_euler(0.001, 30)
+    for _ in range(30):
+        o.step_euler(0.001, 1)
+        f = o.field(0)
+        f[:] = f.real
     assert rel_l2(g.download(0).real, o.field(0).real) <= 1e-11
 
 
