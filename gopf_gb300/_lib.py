@@ -24,7 +24,7 @@ GOPF_STEPPER_EULER, GOPF_STEPPER_RK4 = 0, 1
 DER_PRODUCT, DER_POLY, DER_INDICATOR, DER_INDICATOR_D, DER_INDICATOR_HD = range(5)
 SRC_NONE, SRC_FIELD, SRC_DERIVED = range(3)
 RED_SUM, RED_SUMSQ, RED_MIN, RED_MAX, RED_NONFINITE = range(5)
-OPT_CHECK_FINITE, OPT_USE_GRAPHS = 0, 1
+OPT_CHECK_FINITE, OPT_USE_GRAPHS, OPT_FAST_KERNELS = 0, 1, 2
 MAX_FACTORS = 8
 
 

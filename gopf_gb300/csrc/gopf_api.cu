@@ -337,6 +337,7 @@ extern "C" int gopf_set_option(gopf_ctx *ctx, int opt, long long v)
     if (!ctx) return GOPF_ERR_ARG;
     if (opt == GOPF_OPT_CHECK_FINITE) ctx->check_finite = (int)(v != 0);
     else if (opt == GOPF_OPT_USE_GRAPHS) ctx->use_graphs = (int)(v != 0);
+    else if (opt == GOPF_OPT_FAST_KERNELS) ctx->use_fast = (int)(v != 0);
     else return gopf_fail(ctx, GOPF_ERR_ARG, "unknown option");
     return GOPF_OK;
 }
@@ -606,6 +607,7 @@ template <typename R> static XPassArgs<R> xargs(gopf_ctx *ctx)
     a.g = ctx->g;
     a.planH = ctx->planH;
     a.twX = (const V *)ctx->d_twX;
+    a.allow_fast = ctx->use_fast;
     return a;
 }
 

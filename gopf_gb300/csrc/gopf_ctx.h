@@ -123,6 +123,7 @@ struct gopf_ctx {
 
     int check_finite = 1;
     int use_graphs = 1;
+    int use_fast = 1;
     std::string err;
 };
 

@@ -479,7 +479,7 @@ template <typename R, int LB> static cudaError_t launch_xpass_lb(const XPassArgs
     return cudaGetLastError();
 }
 
-template <typename R> cudaError_t launch_xpass(const XPassArgs<R> &a, int LB, cudaStream_t st)
+template <typename R> static cudaError_t launch_xpass_generic(const XPassArgs<R> &a, int LB, cudaStream_t st)
 {
     if constexpr (sizeof(R) == 4) {
         if (LB == 16) return launch_xpass_lb<R, 16>(a, st);
@@ -512,7 +512,7 @@ template <typename R, int LB, bool CONTIG> static cudaError_t launch_pass_lb(con
     return cudaGetLastError();
 }
 
-template <typename R> cudaError_t launch_cpass(const PassArgs<R> &a, int LB, cudaStream_t st)
+template <typename R> static cudaError_t launch_cpass_generic(const PassArgs<R> &a, int LB, cudaStream_t st)
 {
     if constexpr (sizeof(R) == 4) {
         if (LB == 16) return launch_pass_lb<R, 16, true>(a, st);
@@ -525,7 +525,7 @@ template <typename R> cudaError_t launch_cpass(const PassArgs<R> &a, int LB, cud
     return cudaErrorInvalidValue;
 }
 
-template <typename R> cudaError_t launch_spass(const PassArgs<R> &a, int LB, cudaStream_t st)
+template <typename R> static cudaError_t launch_spass_generic(const PassArgs<R> &a, int LB, cudaStream_t st)
 {
     if constexpr (sizeof(R) == 4) {
         if (LB == 16) return launch_pass_lb<R, 16, false>(a, st);

@@ -95,6 +95,7 @@ template <typename R> struct XPassArgs {
     // optional: per-block FP64 sums of group `redgrp`'s real-space values into red2[block]
     int redgrp;
     double *red2;
+    int allow_fast; // 1: a specialised kernel may serve this launch
 };
 
 enum XProgram { XP_POLY = 0, XP_ELASTIC_Q = 1 };
@@ -115,6 +116,7 @@ template <typename R> struct PassArgs {
     UpdTable upd;
     const R *bsym;        // PM_ELASTIC_K: elastic symbol in the spectral layout
     V *rkF;               // RK4 accumulator (FUSED with upd.rk_stage > 0)
+    int allow_fast;       // 1: a specialised kernel may serve this launch
 };
 
 } // namespace gopf

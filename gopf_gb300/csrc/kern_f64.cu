@@ -2,7 +2,16 @@
 #include "gopf_kernels_impl.cuh"
 
 namespace gopf {
-template cudaError_t launch_xpass<double>(const XPassArgs<double> &, int, cudaStream_t);
-template cudaError_t launch_cpass<double>(const PassArgs<double> &, int, cudaStream_t);
-template cudaError_t launch_spass<double>(const PassArgs<double> &, int, cudaStream_t);
+template <> cudaError_t launch_xpass<double>(const XPassArgs<double> &a, int LB, cudaStream_t st)
+{
+    return launch_xpass_generic<double>(a, LB, st);
+}
+template <> cudaError_t launch_cpass<double>(const PassArgs<double> &a, int LB, cudaStream_t st)
+{
+    return launch_cpass_generic<double>(a, LB, st);
+}
+template <> cudaError_t launch_spass<double>(const PassArgs<double> &a, int LB, cudaStream_t st)
+{
+    return launch_spass_generic<double>(a, LB, st);
+}
 } // namespace gopf

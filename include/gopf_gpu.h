@@ -79,7 +79,8 @@ enum {
 /* options for gopf_set_option */
 enum {
     GOPF_OPT_CHECK_FINITE = 0, /* 1 (default): gopf_step synchronises and checks the field for NaN/Inf */
-    GOPF_OPT_USE_GRAPHS = 1    /* 1 (default): steps are replayed from captured CUDA graphs */
+    GOPF_OPT_USE_GRAPHS = 1,   /* 1 (default): steps are replayed from captured CUDA graphs */
+    GOPF_OPT_FAST_KERNELS = 2  /* 1 (default): register-resident kernels serve the lengths they cover */
 };
 
 #define GOPF_MAX_FACTORS 8

@@ -255,3 +255,56 @@ def test_rk4_cahn_hilliard_parity(oracle, dims, steps, prec, tol):
     o = ch_oracle(oracle, dims, 1.0, c0)
     o.step_rk4(0.1, steps)
     assert rel_l2(g.download(0).real, o.field(0).real) <= tol
+
+
+# ---------------------------------------------------------------- register-resident 256-point kernels
+
+def _two_group_model(dims, prec, c0, fast):
+    """Two explicit groups (LAP^1 and LAP^0) so that the fused passes carry two arrays."""
+    import gopf_gb300 as G
+
+    m = G.Model(dims, prec, device=0)
+    m.set_option(G._lib.OPT_FAST_KERNELS, int(fast))
+    m.add_field("conc")
+    m.add_scalar("gamma", 0.5)
+    m.add_scalar("m1", -1.0)
+    m.add_scalar("eps", 0.05)
+    m.add_equation("dconc/dt = LAP conc^3 + m1*LAP conc + m1*gamma*LAP^2 conc - eps*conc^2")
+    m.init()
+    m.set_stepper("euler", 0.05)
+    m.upload(0, c0)
+    return m
+
+
+@pytest.mark.parametrize("dims", [[256, 256, 256], [256, 256]])
+@pytest.mark.parametrize("two_groups", [False, True])
+def test_fast_kernels_match_generic(dims, two_groups):
+    """The 256-point register kernels and the generic Stockham kernels agree (FP32, 20 steps)."""
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+
+    n = int(np.prod(dims))
+    c0 = uniform_field(1, n, 0.0, 0.1)
+    if two_groups:
+        a = _two_group_model(dims, "fp32", c0, True)
+        b = _two_group_model(dims, "fp32", c0, False)
+    else:
+        a = ch_gpu(dims, "fp32", 0.5, 0.05, c0)
+        b = ch_gpu(dims, "fp32", 0.5, 0.05, c0)
+        b.set_option(G._lib.OPT_FAST_KERNELS, 0)
+    a.step(20)
+    b.step(20)
+    assert rel_l2(a.download(0).real, b.download(0).real) <= 2e-6
+
+
+def test_fast_kernels_2d_256_vs_oracle(oracle):
+    """FP32 fast path on 256^2 against the FP64 oracle, 100 steps: rel-L2 <= 1e-4."""
+    from gopf_gb300.synthetic import uniform_field
+
+    dims = [256, 256]
+    c0 = uniform_field(0, 256 * 256, 0.5, 0.05)
+    g = ch_gpu(dims, "fp32", 1.0, 0.1, c0)
+    g.step(100)
+    o = ch_oracle(oracle, dims, 1.0, c0)
+    o.step_euler(0.1, 100)
+    assert rel_l2(g.download(0).real, o.field(0).real) <= 1e-4
