@@ -34,7 +34,7 @@ from ._lib import (  # noqa: F401
     GopfTerm,
 )
 
-__all__ = ["Model", "GopfError", "load", "build"]
+__all__ = ["Model", "Batch", "GopfError", "load", "build"]
 
 _STEPPERS = {"euler": _lib.GOPF_STEPPER_EULER, "rk4": _lib.GOPF_STEPPER_RK4}
 
@@ -268,3 +268,41 @@ class Model:
         n = ctypes.c_int()
         self._ck(self._L.gopf_kernels_per_step(self._h, ctypes.byref(n)))
         return n.value
+
+
+class Batch:
+    """Several 2D Models stepped together by shared launches (gopf_batch_*)."""
+
+    def __init__(self, models):
+        self._L = _lib.load()
+        self.models = list(models)
+        arr = (ctypes.c_void_p * len(self.models))(*[m.handle.value for m in self.models])
+        h = ctypes.c_void_p()
+        rc = self._L.gopf_batch_create(arr, len(self.models), ctypes.byref(h))
+        self._h = h
+        if rc != 0:
+            msg = self._L.gopf_batch_last_error(h).decode() if h.value else ""
+            self.close()
+            raise GopfError(rc, msg)
+
+    def _ck(self, rc: int) -> None:
+        if rc != 0:
+            raise GopfError(rc, self._L.gopf_batch_last_error(self._h).decode())
+
+    def step(self, nsteps: int) -> None:
+        self._ck(self._L.gopf_batch_step(self._h, int(nsteps)))
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        self._ck(self._L.gopf_batch_set_stream(self._h, ctypes.c_void_p(stream_handle or 0)))
+
+    def close(self) -> None:
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._L.gopf_batch_destroy(h)
+        self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

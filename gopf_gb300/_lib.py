@@ -92,6 +92,12 @@ SIGNATURES = {
     "gopf_kernels_per_step": ([_vp, _ip], _i),
     "gopf_profile_step": ([_vp, _i, _dp, _dp, _i, _ip], _i),
     "gopf_profile_slot_name": ([_vp, _i, ctypes.c_char_p, _i], _i),
+    "gopf_batch_create": ([ctypes.POINTER(_vp), _i, ctypes.POINTER(_vp)], _i),
+    "gopf_batch_destroy": ([_vp], _i),
+    "gopf_batch_last_error": ([_vp], _cp),
+    "gopf_batch_set_stream": ([_vp, _vp], _i),
+    "gopf_batch_step": ([_vp, _ll], _i),
+    "gopf_batch_kernels_per_step": ([_vp, _ip], _i),
 }
 
 _lib = None

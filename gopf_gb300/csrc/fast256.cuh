@@ -78,7 +78,8 @@ __device__ __forceinline__ float2 euler_update(float2 c0, const float2 *U, int n
 // z axis (strided), fused forward -> update -> inverse.  Lines are 16
 // consecutive inner indices i0 + l of the S = KX*Y plane; thread t = r*16 + l.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(NT, 2) k_z256_fused(const PassArgs<float> a)
+template <int NG>
+__global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_z256_fused(const PassArgs<float> a)
 {
     __shared__ __align__(16) float2 s_x[N * 16];
     __shared__ float2 s_tw[N];
@@ -88,7 +89,7 @@ __global__ void __launch_bounds__(NT, 2) k_z256_fused(const PassArgs<float> a)
     const long long i0 = (long long)blockIdx.x * 16;
     const long long S = g.S;
     const float2 *__restrict__ U0 = a.buf[0];
-    const int ngrp = a.upd.ngrp;
+    const int ngrp = (NG == 1) ? (a.upd.ngrp > 0 ? 1 : 0) : a.upd.ngrp;
     const bool init = (a.mode == PM_INIT);
 
     float2 v[16];
@@ -106,12 +107,12 @@ __global__ void __launch_bounds__(NT, 2) k_z256_fused(const PassArgs<float> a)
     auto at = [&](int x, int y) -> float2 & { return s_x[(x * 16 + y) * 16 + l]; };
     fft256<false>(v, r, s_tw, at);
 
-    float2 w[16];
-    if (ngrp > 1) {
+    float2 w[NG == 1 ? 1 : 16];
+    if (NG > 1 && ngrp > 1) {
         const float2 *__restrict__ U1 = a.buf[1];
 #pragma unroll
         for (int i = 0; i < 16; ++i) w[i] = U1[i0 + l + (long long)(r + 16 * i) * S];
-        fft256<false>(w, r, s_tw, at);
+        fft256<false>(reinterpret_cast<float2(&)[16]>(w), r, s_tw, at);
     }
 
     const UpdTable &u = a.upd;
@@ -130,7 +131,7 @@ __global__ void __launch_bounds__(NT, 2) k_z256_fused(const PassArgs<float> a)
             cn = v[i];
         } else {
             const float mk = -fourpi2 * (s_fl[l] + s_fz[k]);
-            float2 U[2] = {v[i], w[i]};
+            float2 U[2] = {v[i], (NG > 1) ? w[NG > 1 ? i : 0] : v[i]};
             float L;
             cn = euler_update(state[gi], U, ngrp, u, mk, gsc, dt, &L);
         }
@@ -148,7 +149,8 @@ __global__ void __launch_bounds__(NT, 2) k_z256_fused(const PassArgs<float> a)
 // fused update.  Thread t = l*16 + r: a half-warp reads 128 contiguous bytes.
 // Shared slots are swizzled so both exchange directions are conflict free.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(NT, 2) k_y256(const PassArgs<float> a)
+template <int NG>
+__global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_y256(const PassArgs<float> a)
 {
     __shared__ __align__(16) float2 s_x[N * 16];
     __shared__ float2 s_tw[N];
@@ -190,13 +192,13 @@ __global__ void __launch_bounds__(NT, 2) k_y256(const PassArgs<float> a)
         return;
     }
     fft256<false>(v, r, s_tw, at);
-    const int ngrp = a.upd.ngrp;
-    float2 w[16];
-    if (ngrp > 1) {
+    const int ngrp = (NG == 1) ? (a.upd.ngrp > 0 ? 1 : 0) : a.upd.ngrp;
+    float2 w[NG == 1 ? 1 : 16];
+    if (NG > 1 && ngrp > 1) {
         const float2 *__restrict__ U1 = a.buf[1];
 #pragma unroll
         for (int i = 0; i < 16; ++i) w[i] = valid ? U1[q * N + r + 16 * i] : zero;
-        fft256<false>(w, r, s_tw, at);
+        fft256<false>(reinterpret_cast<float2(&)[16]>(w), r, s_tw, at);
     }
     const UpdTable &u = a.upd;
     const float dt = (float)u.dt, invN = (float)u.invN;
@@ -215,7 +217,7 @@ __global__ void __launch_bounds__(NT, 2) k_y256(const PassArgs<float> a)
                 cn = v[i];
             } else {
                 const float mk = -fourpi2 * (s_fl[l] + s_fy[k]);
-                float2 U[2] = {v[i], w[i]};
+                float2 U[2] = {v[i], (NG > 1) ? w[NG > 1 ? i : 0] : v[i]};
                 float L;
                 cn = euler_update(state[gi], U, ngrp, u, mk, gsc, dt, &L);
             }
@@ -238,6 +240,12 @@ constexpr int XROWS = 32;
 
 template <typename F> __device__ __forceinline__ float polyf(const PwTable &pw, int grp, float c)
 {
+    const int d = pw.deg[grp];
+    if (d >= 0) {
+        float acc = (float)pw.dense[grp][d];
+        for (int q = d - 1; q >= 0; --q) acc = acc * c + (float)pw.dense[grp][q];
+        return acc;
+    }
     float acc = 0.f;
     const int nt = pw.nterm[grp];
     for (int t = 0; t < nt; ++t) {
@@ -249,7 +257,9 @@ template <typename F> __device__ __forceinline__ float polyf(const PwTable &pw, 
     return acc;
 }
 
-__global__ void __launch_bounds__(NT, 2) k_x256(const XPassArgs<float> a)
+// NG == 1: one output group, transformed in place; NG == 0: any number of groups
+template <int NG>
+__global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_x256(const XPassArgs<float> a)
 {
     // spectral tile [129][32] during c2r input, then exchange slots [256][16]
     __shared__ __align__(16) float2 s_x[N * 16 + 64];
@@ -285,8 +295,10 @@ __global__ void __launch_bounds__(NT, 2) k_x256(const XPassArgs<float> a)
     auto at = [&](int x, int y) -> float2 & { return s_x[(x * 16 + y) * 16 + j]; };
     fft256<true>(v, r, s_tw, at);
     // v[i] = c(row 2j, col r + 16 i) + i c(row 2j+1, col r + 16 i)
-    for (int grp = 0; grp < a.ngrp_out; ++grp) {
-        float2 w[16];
+    const int ng = (NG == 1) ? 1 : a.ngrp_out;
+    for (int grp = 0; grp < ng; ++grp) {
+        float2 wbuf[NG == 1 ? 1 : 16];
+        float2(&w)[16] = (NG == 1) ? v : reinterpret_cast<float2(&)[16]>(wbuf);
 #pragma unroll
         for (int i = 0; i < 16; ++i)
             w[i] = a.identity ? v[i] : make_float2(polyf<float>(a.pw, grp, v[i].x), polyf<float>(a.pw, grp, v[i].y));

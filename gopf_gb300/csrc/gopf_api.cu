@@ -501,6 +501,7 @@ int gopf_compile_model(gopf_ctx *ctx)
     if (ctx->has_elastic && u.ngrp + 1 > GOPF_MAX_GROUPS)
         return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "too many term groups with the elastic term");
     pw.ngrp = u.ngrp;
+    pw_densify(pw);
     u.nimp = maxp;
     ctx->pw = pw;
     ctx->upd = u;
@@ -515,6 +516,7 @@ int gopf_compile_model(gopf_ctx *ctx)
         ctx->pw_el.coef[gH][0] = 3.0;
         ctx->pw_el.pw[gH][1] = 3;
         ctx->pw_el.coef[gH][1] = -2.0;
+        pw_densify(ctx->pw_el);
     }
     if (ctx->device >= 0) {
         int rc;
@@ -619,6 +621,7 @@ template <typename R> static PassArgs<R> pargs(gopf_ctx *ctx, bool zaxis)
     a.g = ctx->g;
     a.plan = zaxis ? ctx->planZ : ctx->planY;
     a.tw = (const V *)(zaxis ? ctx->d_twZ : ctx->d_twY);
+    a.allow_fast = ctx->use_fast;
     return a;
 }
 

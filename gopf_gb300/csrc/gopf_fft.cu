@@ -38,6 +38,7 @@ template <typename R> XPassArgs<R> xbase(gopf_ctx *ctx)
     a.g = ctx->g;
     a.planH = ctx->planH;
     a.twX = (const V *)ctx->d_twX;
+    a.allow_fast = ctx->use_fast;
     return a;
 }
 
@@ -52,6 +53,7 @@ template <typename R> PassArgs<R> pbase(gopf_ctx *ctx, bool zaxis, int mode, voi
     a.mode = mode;
     a.buf[0] = (V *)buf;
     a.nbuf = 1;
+    a.allow_fast = ctx->use_fast;
     return a;
 }
 

@@ -22,6 +22,12 @@ template <> struct Log2<1> { static constexpr int v = 0; };
 
 template <typename R> __device__ __forceinline__ R poly_eval(const PwTable &pw, int grp, R c)
 {
+    const int d = pw.deg[grp];
+    if (d >= 0) { // Horner; for a monomial c^p this is exactly the repeated product
+        R acc = (R)pw.dense[grp][d];
+        for (int q = d - 1; q >= 0; --q) acc = acc * c + (R)pw.dense[grp][q];
+        return acc;
+    }
     R acc = (R)0;
     const int nt = pw.nterm[grp];
     for (int t = 0; t < nt; ++t) {
@@ -161,8 +167,9 @@ template <typename R> __device__ __forceinline__ R elastic_q(R c, R w, R e0, R s
 // x-pass: c2r (or real load) -> pointwise -> r2c
 // ------------------------------------------------------------------
 
+// One x-pass tile: LB rows starting at row ty*LB of depth plane z.
 template <typename R, int LB, int PERB>
-__global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_xpass(const XPassArgs<R> a)
+__device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
 {
     typedef typename VecOf<R>::type V;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -171,8 +178,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_xpass(const X
     const int H = g.H, KX = g.KX, Y = g.Y;
     V *A = reinterpret_cast<V *>(smem_raw);
     V *B = A + KX * LB;
-    const int y0 = blockIdx.x * LB;
-    const int z = blockIdx.y;
+    const int y0 = ty * LB;
     const int nl = min(LB, Y - y0);
     const long long sbase = (long long)z * g.S + y0;
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -294,8 +300,10 @@ template <int LB, bool CONTIG, typename F> __device__ __forceinline__ void tile_
     }
 }
 
+// One tile of a y (CONTIG) or z pass: LB lines starting at line tile*LB;
+// bsel selects the buffer in the FWD/INV modes.
 template <typename R, int LB, int PERB, bool CONTIG>
-__global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_pass(const PassArgs<R> a)
+__device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, int bsel)
 {
     typedef typename VecOf<R>::type V;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -304,7 +312,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_pass(const Pa
     const int n = a.plan.n;
     const int tid = threadIdx.x, nt = blockDim.x;
     const long long nlines = CONTIG ? (long long)g.Z * g.KX : g.S;
-    const long long l0 = (long long)blockIdx.x * LB;
+    const long long l0 = tix * LB;
     const int nl = (int)min((long long)LB, nlines - l0);
     const long long pstride = CONTIG ? 1 : g.S;
     const long long lstride = CONTIG ? n : 1;
@@ -323,7 +331,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_pass(const Pa
     };
 
     if (a.mode == PM_FWD || a.mode == PM_INV) {
-        V *__restrict__ buf = a.buf[blockIdx.y];
+        V *__restrict__ buf = a.buf[bsel];
         load(sm, buf);
         __syncthreads();
         if (a.mode == PM_FWD) fft_tile<false, LB, PERB>(sm, pitch, a.plan, a.tw);
@@ -430,6 +438,18 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_pass(const Pa
     __syncthreads();
     fft_tile<true, LB, PERB>(sm, pitch, a.plan, a.tw);
     store(a.tout, sm);
+}
+
+template <typename R, int LB, int PERB>
+__global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_xpass(const XPassArgs<R> a)
+{
+    xpass_tile<R, LB, PERB>(a, blockIdx.x, blockIdx.y);
+}
+
+template <typename R, int LB, int PERB, bool CONTIG>
+__global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_pass(const PassArgs<R> a)
+{
+    pass_tile<R, LB, PERB, CONTIG>(a, blockIdx.x, blockIdx.y);
 }
 
 // ------------------------------------------------------------------

@@ -39,12 +39,34 @@ struct Geom {
 };
 
 // Real-space pointwise polynomials g_g(c) = sum_t coef[g][t] * c^pw[g][t]
+#define GOPF_MAX_DEG 12
 struct PwTable {
     int ngrp;
     int nterm[GOPF_MAX_GROUPS];
     int pw[GOPF_MAX_GROUPS][GOPF_MAX_POLY];
     double coef[GOPF_MAX_GROUPS][GOPF_MAX_POLY];
+    // the same polynomials in dense form for Horner evaluation (deg < 0: not representable)
+    int deg[GOPF_MAX_GROUPS];
+    double dense[GOPF_MAX_GROUPS][GOPF_MAX_DEG + 1];
 };
+
+// Fill deg/dense from the sparse terms.
+inline void pw_densify(PwTable &pw)
+{
+    for (int g = 0; g < GOPF_MAX_GROUPS; ++g) {
+        for (int q = 0; q <= GOPF_MAX_DEG; ++q) pw.dense[g][q] = 0.0;
+        int d = 0;
+        bool ok = true;
+        for (int t = 0; t < pw.nterm[g]; ++t) {
+            if (pw.pw[g][t] < 0 || pw.pw[g][t] > GOPF_MAX_DEG) ok = false;
+            else {
+                pw.dense[g][pw.pw[g][t]] += pw.coef[g][t];
+                if (pw.pw[g][t] > d) d = pw.pw[g][t];
+            }
+        }
+        pw.deg[g] = ok ? d : -1;
+    }
+}
 
 // k-space update: c_new = (c + dt * sum_g m^glap[g] U_g) / (1 - dt * sum_p imp[p] m^p),  m = -k^2
 struct UpdTable {

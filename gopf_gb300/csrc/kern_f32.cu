@@ -28,7 +28,8 @@ template <> cudaError_t launch_xpass<float>(const XPassArgs<float> &a, int LB, c
 {
     if (fast_x(a)) {
         dim3 grid(a.g.Y / f256::XROWS, a.g.Z);
-        f256::k_x256<<<grid, f256::NT, 0, st>>>(a);
+        if (a.ngrp_out == 1) f256::k_x256<1><<<grid, f256::NT, 0, st>>>(a);
+        else f256::k_x256<0><<<grid, f256::NT, 0, st>>>(a);
         return cudaGetLastError();
     }
     return launch_xpass_generic<float>(a, LB, st);
@@ -40,7 +41,8 @@ template <> cudaError_t launch_cpass<float>(const PassArgs<float> &a, int LB, cu
         const long long nlines = (long long)a.g.Z * a.g.KX;
         const bool fused = (a.mode == PM_FUSED || a.mode == PM_INIT);
         dim3 grid((unsigned)((nlines + 15) / 16), fused ? 1 : a.nbuf);
-        f256::k_y256<<<grid, f256::NT, 0, st>>>(a);
+        if (fused && a.nbuf > 1) f256::k_y256<2><<<grid, f256::NT, 0, st>>>(a);
+        else f256::k_y256<1><<<grid, f256::NT, 0, st>>>(a);
         return cudaGetLastError();
     }
     return launch_cpass_generic<float>(a, LB, st);
@@ -49,7 +51,8 @@ template <> cudaError_t launch_cpass<float>(const PassArgs<float> &a, int LB, cu
 template <> cudaError_t launch_spass<float>(const PassArgs<float> &a, int LB, cudaStream_t st)
 {
     if (fast_z(a)) {
-        f256::k_z256_fused<<<(unsigned)(a.g.S / 16), f256::NT, 0, st>>>(a);
+        if (a.nbuf > 1) f256::k_z256_fused<2><<<(unsigned)(a.g.S / 16), f256::NT, 0, st>>>(a);
+        else f256::k_z256_fused<1><<<(unsigned)(a.g.S / 16), f256::NT, 0, st>>>(a);
         return cudaGetLastError();
     }
     return launch_spass_generic<float>(a, LB, st);

@@ -165,6 +165,22 @@ int gopf_fft(gopf_ctx *ctx, int sign, double *data, size_t n);
 int gopf_freq(gopf_ctx *ctx, long long i, double *out);
 long long gopf_conjugate_node(gopf_ctx *ctx, long long i);
 
+/* ---- batches: many independent 2D instances stepped by shared launches ----
+ * Replaces running one pf.Solver per swept parameter set (the workflow the
+ * sweep database serves, README.md:21-33, pf/database.go:67-80); it has no
+ * single counterpart in the reference.  Every context keeps its own model,
+ * dt and device state; gopf_batch_step(nsteps) advances all of them by
+ * nsteps Euler steps with three launches per step (captured in a CUDA graph).
+ * Contexts must be 2D, single-field, Euler, without user-defined terms, on one
+ * device and precision, and stay alive while the batch exists. */
+typedef struct gopf_batch gopf_batch;
+int gopf_batch_create(gopf_ctx *const *ctxs, int n, gopf_batch **out);
+int gopf_batch_destroy(gopf_batch *batch);
+const char *gopf_batch_last_error(const gopf_batch *batch);
+int gopf_batch_set_stream(gopf_batch *batch, void *cuda_stream);
+int gopf_batch_step(gopf_batch *batch, long long nsteps);
+int gopf_batch_kernels_per_step(gopf_batch *batch, int *n);
+
 /* ---- introspection ---- */
 /* Bytes of device memory held by the context. */
 int gopf_device_bytes(gopf_ctx *ctx, size_t *bytes);
