@@ -328,6 +328,100 @@ def emit(args, m, world, rank, value, per_step_ms, mass0, mass1, finite, prof, d
     return out
 
 
+SWEEP_SIDES = [128, 256, 384, 512, 768, 1024]
+
+
+def sweep_params(n=64, seed=2):
+    """64 instances: side uniform over SWEEP_SIDES, gamma ~ U(0.2, 2), M ~ U(0.5, 2) (SplitMix64, seed 2)."""
+    from gopf_gb300.synthetic import splitmix64_uniform
+
+    u = splitmix64_uniform(seed, 3 * n)
+    return [(SWEEP_SIDES[min(int(u[3 * i] * 6), 5)], 0.2 + 1.8 * u[3 * i + 1], 0.5 + 1.5 * u[3 * i + 2])
+            for i in range(n)]
+
+
+def sweep_models(prec, params, fast=True):
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+
+    models = []
+    for i, (side, gamma, Mv) in enumerate(params):
+        m = G.Model([side, side], prec, device=0)
+        m.set_option(G._lib.OPT_FAST_KERNELS, int(fast))
+        m.set_option(G._lib.OPT_CHECK_FINITE, 0)
+        m.add_field("conc")
+        m.add_scalar("gamma", gamma)
+        m.add_scalar("M", Mv)
+        m.add_scalar("mM", -Mv)
+        m.add_equation("dconc/dt = M*LAP conc^3 + mM*LAP conc + mM*gamma*LAP^2 conc")
+        m.init()
+        m.set_stepper("euler", 0.05)
+        m.upload(0, uniform_field(1000 + i, side * side, 0.5, 0.05))
+        models.append(m)
+    return models
+
+
+def run_sweep(args):
+    """Batched parameter sweep: 64 independent 2D CH instances of uneven size, FP32, dt 0.05."""
+    import torch
+
+    import gopf_gb300 as G
+
+    params = sweep_params()
+    cells = sum(s * s for s, _, _ in params)
+    models = sweep_models("fp32", params)
+    batch = G.Batch(models)
+    stream = torch.cuda.Stream()
+    batch.set_stream(stream.cuda_stream)
+    batch.step(max(args.warmup, 3))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        e0.record(stream)
+        batch.step(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    batched = args.steps / (ms / 1000.0)
+    # sequential: every instance stepped by its own launches (own CUDA graphs)
+    seq_models = sweep_models("fp32", params)
+    for m in seq_models:
+        m.set_stream(stream.cuda_stream)
+        m.step(3)
+    torch.cuda.synchronize()
+    kseq = max(3, min(args.steps, 200))
+    e0.record(stream)
+    for _ in range(kseq):
+        for m in seq_models:
+            m.step(1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    seq = kseq / (e0.elapsed_time(e1) / 1000.0)
+    out = {"metric": "sweep steps/s (64 uneven 2D CH instances, one step of all instances)", "value": batched,
+           "unit": "sweep-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
+           "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "sweep_64_ch2d_uneven_fp32", "sides": [p[0] for p in params], "cells": cells,
+                      "dt": 0.05, "params_seed": 2, "init": "c0 = 0.5 + U(-0.05, 0.05), seed 1000 + i"},
+           "sequential_value": seq, "speedup_vs_sequential": batched / seq,
+           "cell_updates_per_s": batched * cells, "clocks": clk.summary(), "gpu_launches": 3 * args.steps}
+    if args.check_steps > 0:
+        # per-instance rel-L2 of the FP32 batch against sequential FP64 runs after check_steps steps
+        a = sweep_models("fp32", params)
+        G.Batch(a).step(args.check_steps)
+        errs = []
+        for i, m in enumerate(a):
+            r = sweep_models("fp64", [params[i]])[0]
+            r.step(args.check_steps)
+            ref = r.download_real(0)
+            errs.append(float(np.linalg.norm(m.download_real(0) - ref) / np.linalg.norm(ref)))
+            r.close()
+        out["check"] = {"steps": args.check_steps, "rel_l2_max": max(errs), "rel_l2_median": float(np.median(errs)),
+                        "rel_l2": errs}
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -338,9 +432,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--grid", type=int, default=256, help="cube side (256 is the benchmark workload)")
+    ap.add_argument("--workload", default="ch3d", choices=["ch3d", "sweep"])
+    ap.add_argument("--check-steps", type=int, default=0, help="sweep: compare against FP64 after this many steps")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "sweep":
+        return run_sweep(args)
     return run_gpu(args)
 
 
