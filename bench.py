@@ -340,7 +340,7 @@ def sweep_params(n=64, seed=2):
             for i in range(n)]
 
 
-def sweep_models(prec, params, fast=True):
+def sweep_models(prec, params, fast=True, first=0):
     import gopf_gb300 as G
     from gopf_gb300.synthetic import uniform_field
 
@@ -356,7 +356,7 @@ def sweep_models(prec, params, fast=True):
         m.add_equation("dconc/dt = M*LAP conc^3 + mM*LAP conc + mM*gamma*LAP^2 conc")
         m.init()
         m.set_stepper("euler", 0.05)
-        m.upload(0, uniform_field(1000 + i, side * side, 0.5, 0.05))
+        m.upload(0, uniform_field(1000 + first + i, side * side, 0.5, 0.05))
         models.append(m)
     return models
 
@@ -411,13 +411,63 @@ def run_sweep(args):
         G.Batch(a).step(args.check_steps)
         errs = []
         for i, m in enumerate(a):
-            r = sweep_models("fp64", [params[i]])[0]
+            r = sweep_models("fp64", [params[i]], first=i)[0]
             r.step(args.check_steps)
             ref = r.download_real(0)
             errs.append(float(np.linalg.norm(m.download_real(0) - ref) / np.linalg.norm(ref)))
             r.close()
         out["check"] = {"steps": args.check_steps, "rel_l2_max": max(errs), "rel_l2_median": float(np.median(errs)),
                         "rel_l2": errs}
+    print(json.dumps(out))
+    return 0
+
+
+def run_adjoint(args):
+    """Adjoint parameter fit workload: 2D CH 512^2, 200 steps, dt 0.05, checkpoints every 20 (FP32 adjoint)."""
+    import torch
+
+    from gopf_gb300.adjoint import AdjointCH
+    from gopf_gb300.synthetic import uniform_field
+    from oracle import adjoint_ref as A
+
+    dims, T, dt, every = [512, 512], 200, 0.05, 20
+    c0 = uniform_field(4, 512 * 512, 0.5, 0.05)
+    ref64 = AdjointCH(dims, "fp64", dt=dt, nsteps=T, every=every)
+    target = ref64.forward(c0, 1.3, 0.8)  # target microstructure from the FP64 forward at gamma*=1.3, M*=0.8
+    run = AdjointCH(dims, "fp32", dt=dt, nsteps=T, every=every)
+    run.loss_and_grad(c0, 1.0, 1.0, target)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = max(1, min(args.steps, 5))
+    for _ in range(reps):
+        loss, dg, dm, dc0 = run.loss_and_grad(c0, 1.0, 1.0, target)
+    el = (time.perf_counter() - t0) / reps
+    l64, g64, m64, c64 = ref64.loss_and_grad(c0, 1.0, 1.0, target)
+
+    def L(g, m):
+        r = ref64.forward(c0, g, m) - target
+        return 0.5 * float(r @ r)
+
+    h = 1e-4
+    fdg = (L(1.0 + h, 1.0) - L(1.0 - h, 1.0)) / (2 * h)
+    fdm = (L(1.0, 1.0 + h) - L(1.0, 1.0 - h)) / (2 * h)
+    out = {"metric": "adjoint gradient (gamma, M, c0) of CH 512^2 x 200 steps, FP32, checkpoints every 20",
+           "value": 1.0 / el, "unit": "forward+adjoint/s", "n_gpus": 1, "steps": reps, "warmup": 1,
+           "ms_per_step": el * 1000.0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "adjoint_ch2d_512_200steps", "target": "FP64 forward at gamma*=1.3, M*=0.8",
+                      "at": "gamma=1.0, M=1.0", "checkpoint_every": every},
+           "loss": loss, "grad": {"gamma": dg, "M": dm},
+           "fd_fp64": {"gamma": fdg, "M": fdm, "h": h},
+           "rel_err_vs_fd": {"gamma": abs(dg - fdg) / abs(fdg), "M": abs(dm - fdm) / abs(fdm)},
+           "rel_err_vs_fp64_adjoint": {"gamma": abs(dg - g64) / abs(g64), "M": abs(dm - m64) / abs(m64),
+                                       "c0": float(np.linalg.norm(dc0 - c64) / np.linalg.norm(c64))},
+           "fp64_adjoint_vs_fd": {"gamma": abs(g64 - fdg) / abs(fdg), "M": abs(m64 - fdm) / abs(fdm)}}
+    if args.check_steps > 0:
+        cT = ref64.forward(c0, 1.0, 1.0)
+        rg, rm, rc0 = A.adjoint(c0, dims, 1.0, 1.0, dt, T, cT - target)
+        out["fp64_adjoint_vs_numpy"] = {"gamma": abs(g64 - rg) / abs(rg), "M": abs(m64 - rm) / abs(rm),
+                                        "c0": float(np.linalg.norm(c64 - rc0) / np.linalg.norm(rc0))}
     print(json.dumps(out))
     return 0
 
@@ -432,13 +482,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--grid", type=int, default=256, help="cube side (256 is the benchmark workload)")
-    ap.add_argument("--workload", default="ch3d", choices=["ch3d", "sweep"])
+    ap.add_argument("--workload", default="ch3d", choices=["ch3d", "sweep", "adjoint"])
     ap.add_argument("--check-steps", type=int, default=0, help="sweep: compare against FP64 after this many steps")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "sweep":
         return run_sweep(args)
+    if args.workload == "adjoint":
+        return run_adjoint(args)
     return run_gpu(args)
 
 

@@ -92,6 +92,9 @@ SIGNATURES = {
     "gopf_kernels_per_step": ([_vp, _ip], _i),
     "gopf_profile_step": ([_vp, _i, _dp, _dp, _i, _ip], _i),
     "gopf_profile_slot_name": ([_vp, _i, ctypes.c_char_p, _i], _i),
+    "gopf_adjoint_forward": ([_vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, _i, _i, _dp, _dp], _i),
+    "gopf_adjoint_backward": ([_vp, _dp, _dp, _dp, _dp], _i),
+    "gopf_adjoint_release": ([_vp], _i),
     "gopf_batch_create": ([ctypes.POINTER(_vp), _i, ctypes.POINTER(_vp)], _i),
     "gopf_batch_destroy": ([_vp], _i),
     "gopf_batch_last_error": ([_vp], _cp),

@@ -32,7 +32,7 @@ __device__ __forceinline__ void fft256(float2 (&v)[16], int r, const float2 *__r
     dft16<INV>(v);
 #pragma unroll
     for (int k1 = 1; k1 < 16; ++k1) {
-        const float2 w = tw[r * k1];
+        const float2 w = tw[k1 * 16 + r]; // W256^(r k1), laid out [k1][r]: conflict free
         v[k1] = INV ? cmulc(v[k1], w) : cmul(v[k1], w);
     }
 #pragma unroll
@@ -44,9 +44,10 @@ __device__ __forceinline__ void fft256(float2 (&v)[16], int r, const float2 *__r
     __syncthreads(); // slots may be reused after return
 }
 
+// s_tw[k1*16 + r] = W256^(r*k1)
 __device__ __forceinline__ void load_twiddles(float2 *s_tw, const float2 *__restrict__ tw)
 {
-    for (int t = threadIdx.x; t < N; t += blockDim.x) s_tw[t] = tw[t];
+    for (int t = threadIdx.x; t < N; t += blockDim.x) s_tw[t] = tw[(t & 15) * (t >> 4)];
 }
 
 __device__ __forceinline__ float fsqf(int i, int n)
@@ -70,8 +71,8 @@ __device__ __forceinline__ float2 euler_update(float2 c0, const float2 *U, int n
     float L = 0.f;
     for (int q = u.nimp - 1; q >= 0; --q) L = L * mk + (float)u.imp[q];
     *Lout = L;
-    const float den = 1.f - dt * L;
-    return make_float2((c0.x + dt * nhat.x) / den, (c0.y + dt * nhat.y) / den);
+    const float rden = 1.f / (1.f - dt * L);
+    return make_float2((c0.x + dt * nhat.x) * rden, (c0.y + dt * nhat.y) * rden);
 }
 
 // ---------------------------------------------------------------------------
@@ -79,7 +80,7 @@ __device__ __forceinline__ float2 euler_update(float2 c0, const float2 *U, int n
 // consecutive inner indices i0 + l of the S = KX*Y plane; thread t = r*16 + l.
 // ---------------------------------------------------------------------------
 template <int NG>
-__global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_z256_fused(const PassArgs<float> a)
+__global__ void __launch_bounds__(NT, 2) k_z256_fused(const PassArgs<float> a)
 {
     __shared__ __align__(16) float2 s_x[N * 16];
     __shared__ float2 s_tw[N];
@@ -92,9 +93,13 @@ __global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_z256_fused(const PassAr
     const int ngrp = (NG == 1) ? (a.upd.ngrp > 0 ? 1 : 0) : a.upd.ngrp;
     const bool init = (a.mode == PM_INIT);
 
-    float2 v[16];
+    float2 v[16], sv[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = U0[i0 + l + (long long)(r + 16 * i) * S];
+    if (!init) { // the state's loads overlap the forward transform
+#pragma unroll
+        for (int i = 0; i < 16; ++i) sv[i] = a.state[i0 + l + (long long)(r + 16 * i) * S];
+    }
     load_twiddles(s_tw, a.tw);
     if (threadIdx.x < 16) {
         const long long q = i0 + threadIdx.x;
@@ -133,7 +138,7 @@ __global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_z256_fused(const PassAr
             const float mk = -fourpi2 * (s_fl[l] + s_fz[k]);
             float2 U[2] = {v[i], (NG > 1) ? w[NG > 1 ? i : 0] : v[i]};
             float L;
-            cn = euler_update(state[gi], U, ngrp, u, mk, gsc, dt, &L);
+            cn = euler_update(sv[i], U, ngrp, u, mk, gsc, dt, &L);
         }
         state[gi] = cn;
         v[i] = make_float2(cn.x * invN, cn.y * invN);
@@ -259,7 +264,7 @@ template <typename F> __device__ __forceinline__ float polyf(const PwTable &pw, 
 
 // NG == 1: one output group, transformed in place; NG == 0: any number of groups
 template <int NG>
-__global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_x256(const XPassArgs<float> a)
+__global__ void __launch_bounds__(NT, 2) k_x256(const XPassArgs<float> a)
 {
     // spectral tile [129][32] during c2r input, then exchange slots [256][16]
     __shared__ __align__(16) float2 s_x[N * 16 + 64];

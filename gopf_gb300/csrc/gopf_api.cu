@@ -303,9 +303,12 @@ extern "C" int gopf_ctx_create(int ndim, const int *domain_size, int precision, 
     return rc;
 }
 
+extern "C" int gopf_adjoint_release(gopf_ctx *ctx);
+
 extern "C" int gopf_ctx_destroy(gopf_ctx *ctx)
 {
     if (!ctx) return GOPF_ERR_ARG;
+    if (ctx->device >= 0) gopf_adjoint_release(ctx);
     if (ctx->device >= 0) {
         cudaSetDevice(ctx->device);
         if (ctx->stream) cudaStreamSynchronize(ctx->stream);
@@ -1047,6 +1050,33 @@ extern "C" int gopf_step(gopf_ctx *ctx, long long nsteps)
             return gopf_fail(ctx, GOPF_ERR_NAN, "field contains " + std::to_string((long long)r[RED_NONFINITE]) +
                                                     " non-finite values after step " + std::to_string(ctx->step));
     }
+    return GOPF_OK;
+}
+
+// ---- device-side helpers for the adjoint (stream-ordered, no synchronisation) ----
+
+int gopf_state_to_real(gopf_ctx *ctx, void *dst)
+{
+    cudaError_t e = (ctx->prec == GOPF_FP32) ? enqueue_xpass_out<float>(ctx, (float *)dst, nullptr)
+                                             : enqueue_xpass_out<double>(ctx, (double *)dst, nullptr);
+    return (e == cudaSuccess) ? GOPF_OK : cuda_fail(ctx, e, "state to real");
+}
+
+int gopf_real_to_state(gopf_ctx *ctx, const void *src)
+{
+    const size_t rb = (ctx->prec == GOPF_FP32 ? sizeof(float) : sizeof(double)) * ctx->g.N;
+    CK(cudaMemcpyAsync(ctx->d_real, src, rb, cudaMemcpyDeviceToDevice, ctx->stream));
+    cudaError_t e = (ctx->prec == GOPF_FP32) ? enqueue_load_state<float>(ctx) : enqueue_load_state<double>(ctx);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "real to state");
+    ctx->state_valid = true;
+    return GOPF_OK;
+}
+
+int gopf_step_device(gopf_ctx *ctx, long long n)
+{
+    cudaError_t e = enqueue_steps_any(ctx, (int)n);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "step");
+    ctx->step += n;
     return GOPF_OK;
 }
 

@@ -165,6 +165,18 @@ int gopf_fft(gopf_ctx *ctx, int sign, double *data, size_t n);
 int gopf_freq(gopf_ctx *ctx, long long i, double *out);
 long long gopf_conjugate_node(gopf_ctx *ctx, long long i);
 
+/* ---- adjoint of the semi-implicit Cahn-Hilliard step (no counterpart in the reference) ----
+ * Model: dconc/dt = M*LAP MU - M*gamma*LAP^2 conc with MU = conc^3 - conc, Euler
+ * (pf/euler.go:16-47).  gopf_adjoint_forward installs that model on the context,
+ * runs nsteps steps from the real field c0 (N doubles), keeps the field every
+ * `every` steps on the device and writes c_T (N doubles, may be NULL).
+ * gopf_adjoint_backward takes lambda_T = dL/dc_T (N doubles) and returns dL/dgamma,
+ * dL/dM and dL/dc0 (N doubles, may be NULL), recomputing each checkpoint segment. */
+int gopf_adjoint_forward(gopf_ctx *ctx, double gamma, double M, double dt, int nsteps, int every, const double *c0,
+                         double *cT);
+int gopf_adjoint_backward(gopf_ctx *ctx, const double *lambda_T, double *dgamma, double *dM, double *dc0);
+int gopf_adjoint_release(gopf_ctx *ctx);
+
 /* ---- batches: many independent 2D instances stepped by shared launches ----
  * Replaces running one pf.Solver per swept parameter set (the workflow the
  * sweep database serves, README.md:21-33, pf/database.go:67-80); it has no

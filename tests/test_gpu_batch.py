@@ -31,7 +31,7 @@ def _params(n):
     from gopf_gb300.synthetic import splitmix64_uniform
 
     u = splitmix64_uniform(2, 3 * n)
-    sides = [16, 32, 48, 64, 96, 128, 24, 40]
+    sides = [16, 32, 48, 64, 96, 128, 24, 72]
     return [(sides[int(u[3 * i] * len(sides))], 0.2 + 1.8 * u[3 * i + 1], 0.5 + 1.5 * u[3 * i + 2]) for i in range(n)]
 
 
