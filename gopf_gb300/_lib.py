@@ -95,6 +95,8 @@ SIGNATURES = {
     "gopf_adjoint_forward": ([_vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, _i, _i, _dp, _dp], _i),
     "gopf_adjoint_backward": ([_vp, _dp, _dp, _dp, _dp], _i),
     "gopf_adjoint_release": ([_vp], _i),
+    "gopf_reduce_noalloc": ([_vp, _sz, _dp, _vp], _i),
+    "gopf_noalloc_last_error": ([], _cp),
     "gopf_batch_create": ([ctypes.POINTER(_vp), _i, ctypes.POINTER(_vp)], _i),
     "gopf_batch_destroy": ([_vp], _i),
     "gopf_batch_last_error": ([_vp], _cp),

@@ -193,6 +193,22 @@ int gopf_batch_set_stream(gopf_batch *batch, void *cuda_stream);
 int gopf_batch_step(gopf_batch *batch, long long nsteps);
 int gopf_batch_kernels_per_step(gopf_batch *batch, int *n);
 
+/* ---- reduction without device allocation (no counterpart in the reference) ----
+ * For callers that cannot allocate device memory at the point of the call (a host
+ * that manages all device memory itself, an allocator budget enforced outside CUDA,
+ * a pool that must not be touched).  Reduces a real FP64 field the caller holds in
+ * device memory; out receives, on the host, {sum, sum of squares, min, max,
+ * non-finite count} as gopf_reduce reports them.  Its only scratch is a static
+ * device array of GOPF_NOALLOC_MAX_BLOCKS + 1 rows of 8 doubles (about 1 MiB per GPU
+ * that loads the library, held until exit), so n is limited to
+ * GOPF_NOALLOC_MAX_BLOCKS * 4096 elements; larger n returns GOPF_ERR_ARG.  The first
+ * call on a device looks the scratch address up and should come before any stream
+ * capture.  Calls share the scratch: calls that overlap on the GPU race and must be
+ * serialised by the caller.  stream may be NULL (the default stream). */
+#define GOPF_NOALLOC_MAX_BLOCKS 16384
+int gopf_reduce_noalloc(const double *field, size_t n, double *out, void *cuda_stream);
+const char *gopf_noalloc_last_error(void);
+
 /* ---- introspection ---- */
 /* Bytes of device memory held by the context. */
 int gopf_device_bytes(gopf_ctx *ctx, size_t *bytes);
