@@ -472,6 +472,131 @@ def run_adjoint(args):
     return 0
 
 
+def _cubic(c11, c12, c44):
+    C = np.zeros((3, 3, 3, 3))
+    for i in range(3):
+        C[i, i, i, i] = c11
+    for i in range(3):
+        for j in range(i + 1, 3):
+            C[i, i, j, j] = c12
+            C[j, j, i, i] = c12
+            C[i, j, i, j] = c44
+            C[j, i, j, i] = c44
+    return C
+
+
+def run_elastic(args):
+    """CH + Khachaturyan elasticity, 256^3, FP32: C11=1.0, C12=0.6, C44=0.5, misfit 0.01*I coupled through H(c),
+    c0 = 0.3 + U(-0.02, 0.02) (seed 3), M=1, gamma=1, dt=0.02, "- LAP LIN_ELAST" in the CH string."""
+    import torch
+
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+
+    n = 256 ** 3
+    c0 = uniform_field(3, n, 0.3, 0.02)
+    m = G.Model([256] * 3, "fp32", device=0)
+    m.set_option(G._lib.OPT_CHECK_FINITE, 0)
+    m.add_field("conc")
+    m.add_scalar("gamma", 1.0)
+    m.add_scalar("m1", -1.0)
+    m.register_elastic("LIN_ELAST", "conc", _cubic(1.0, 0.6, 0.5), np.eye(3) * 0.01)
+    m.add_equation("dconc/dt = LAP conc^3 + m1*LAP conc + m1*gamma*LAP^2 conc - LAP LIN_ELAST")
+    m.init()
+    m.set_stepper("euler", 0.02)
+    stream = torch.cuda.Stream()
+    m.set_stream(stream.cuda_stream)
+    m.upload(0, c0)
+    mass0 = m.mass(0)
+    m.step(max(args.warmup, 3))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        e0.record(stream)
+        m.step(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    prof = m.profile_step(10)
+    step_bytes = sum(p["bytes"] for p in prof)
+    hbm, kind = peaks()
+    value = args.steps / (ms / 1000.0)
+    out = {"metric": "CH + Khachaturyan elasticity steps/s at 256^3 FP32", "value": value, "unit": "steps/s",
+           "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "ch_elastic_3d_256cube_fp32", "C11": 1.0, "C12": 0.6, "C44": 0.5, "misfit": 0.01,
+                      "dt": 0.02, "init": "c0 = 0.3 + U(-0.02, 0.02), seed 3"},
+           "step_bytes_algorithmic": step_bytes, "step_fraction_of_hbm": step_bytes * value / 1e9 / hbm,
+           "mass_drift_per_cell": abs(m.mass(0) - mass0) / n,
+           "per_kernel": [{"name": p["name"], "ms": p["ms"], "GBps": p["bytes"] / p["ms"] / 1e6 if p["ms"] > 0 else 0}
+                          for p in prof], "clocks": clk.summary(), "gpu_launches": m.kernels_per_step * args.steps}
+    print(json.dumps(out))
+    return 0
+
+
+def run_precision(args):
+    """3D CH 256^3: FP64 device mode steps/s, FP64 device vs the FP64 oracle at full size (few steps),
+    FP32 vs FP64 device rel-L2 and mass drift after --check-steps steps."""
+    import torch
+
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+    from oracle import oracle as O
+
+    n = 256 ** 3
+    c0 = uniform_field(SEED, n, 0.0, 0.1)
+
+    def mk(prec):
+        m = G.Model(DIMS, prec, device=0)
+        m.set_option(G._lib.OPT_CHECK_FINITE, 0)
+        m.add_field("conc")
+        m.add_scalar("gamma", GAMMA)
+        m.add_scalar("M", M)
+        m.add_scalar("m1", -M)
+        m.add_equation(CH_EQ)
+        m.init()
+        m.set_stepper("euler", DT)
+        m.upload(0, c0)
+        return m
+
+    m64 = mk("fp64")
+    m64.step(3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    m64.step(args.steps)
+    m64.synchronize()
+    fp64_rate = args.steps / (time.perf_counter() - t0)
+    # FP64 device against the FP64 oracle at full size
+    k = 5
+    a = mk("fp64")
+    a.step(k)
+    o = O.cahn_hilliard(DIMS, gamma=GAMMA, M=M)
+    o.set_field(0, c0)
+    o.step_euler(DT, k)
+    ref = o.field(0).real
+    fp64_vs_oracle = float(np.linalg.norm(a.download_real(0) - ref) / np.linalg.norm(ref))
+    del o
+    # FP32 vs FP64 device after check_steps
+    S = args.check_steps if args.check_steps > 0 else 1000
+    a32, a64 = mk("fp32"), mk("fp64")
+    hist = []
+    done = 0
+    for s in sorted(set([10, 50, 100, 200, 500, S])):
+        if s > S:
+            continue
+        a32.step(s - done)
+        a64.step(s - done)
+        done = s
+        d32, d64 = a32.download_real(0), a64.download_real(0)
+        hist.append({"step": s, "rel_l2_fp32_vs_fp64": float(np.linalg.norm(d32 - d64) / np.linalg.norm(d64))})
+    out = {"metric": "CH 256^3: FP64 device steps/s and FP32-vs-FP64 accuracy", "fp64_steps_per_s": fp64_rate,
+           "fp64_vs_oracle": {"steps": k, "rel_l2": fp64_vs_oracle},
+           "fp32_vs_fp64": hist, "mass_drift_per_cell": {"fp32": abs(a32.mass(0) - c0.sum()) / n,
+                                                         "fp64": abs(a64.mass(0) - c0.sum()) / n}}
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -482,7 +607,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--grid", type=int, default=256, help="cube side (256 is the benchmark workload)")
-    ap.add_argument("--workload", default="ch3d", choices=["ch3d", "sweep", "adjoint"])
+    ap.add_argument("--workload", default="ch3d", choices=["ch3d", "sweep", "adjoint", "elastic", "precision"])
     ap.add_argument("--check-steps", type=int, default=0, help="sweep: compare against FP64 after this many steps")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -491,6 +616,10 @@ def main():
         return run_sweep(args)
     if args.workload == "adjoint":
         return run_adjoint(args)
+    if args.workload == "elastic":
+        return run_elastic(args)
+    if args.workload == "precision":
+        return run_precision(args)
     return run_gpu(args)
 
 

@@ -36,7 +36,8 @@ from ._lib import (  # noqa: F401
 
 __all__ = ["Model", "Batch", "GopfError", "load", "build"]
 
-_STEPPERS = {"euler": _lib.GOPF_STEPPER_EULER, "rk4": _lib.GOPF_STEPPER_RK4}
+_STEPPERS = {"euler": _lib.GOPF_STEPPER_EULER, "rk4": _lib.GOPF_STEPPER_RK4,
+             "implicit_euler": _lib.GOPF_STEPPER_IMPLICIT_EULER}
 
 
 class GopfError(RuntimeError):
@@ -135,6 +136,11 @@ class Model:
     def register_volcons(self, name: str, field: str, indicator: str, dt: float) -> None:
         self._ck(self._L.gopf_register_volcons(self._h, name.encode(), field.encode(), indicator.encode(), dt))
 
+    def register_noise(self, name: str, kind: str, field: str, strength: float, seed: int = 0) -> None:
+        """WhiteNoise as a function ("white") or ConservativeNoise as a term ("conservative")."""
+        k = {"white": _lib.NOISE_WHITE, "conservative": _lib.NOISE_CONSERVATIVE}[kind]
+        self._ck(self._L.gopf_register_noise(self._h, name.encode(), k, field.encode(), float(strength), int(seed)))
+
     def add_equation(self, eq: str) -> None:
         self._ck(self._L.gopf_add_equation(self._h, eq.encode()))
 
@@ -185,6 +191,18 @@ class Model:
     # ---- pf.TimeStepper mirror ----
     def set_stepper(self, name: str, dt: float) -> None:
         self._ck(self._L.gopf_set_stepper(self._h, _STEPPERS[name], dt))
+
+    def set_newton_krylov(self, maxiter: int = 50, step_size: float = 1e-3, tol: float = 1e-7, stencil: int = 6,
+                          restart: int = 50) -> None:
+        """ImplicitEuler's solver controls (pf/implicitEuler.go:221-228 defaults)."""
+        self._ck(self._L.gopf_set_newton_krylov(self._h, maxiter, step_size, tol, stencil, restart))
+
+    def newton_stats(self):
+        """(Newton iterations, GMRES iterations, max|F|, converged) of the last ImplicitEuler step."""
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        r = ctypes.c_double()
+        self._ck(self._L.gopf_newton_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(r), ctypes.byref(c)))
+        return a.value, b.value, r.value, bool(c.value)
 
     def upload(self, field: int, data) -> None:
         a = np.ascontiguousarray(np.asarray(data).reshape(-1).astype(np.complex128))

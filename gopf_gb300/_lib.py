@@ -20,11 +20,12 @@ STATUS = {
     8: "GOPF_ERR_PARSE",
 }
 GOPF_FP32, GOPF_FP64 = 0, 1
-GOPF_STEPPER_EULER, GOPF_STEPPER_RK4 = 0, 1
-DER_PRODUCT, DER_POLY, DER_INDICATOR, DER_INDICATOR_D, DER_INDICATOR_HD = range(5)
+GOPF_STEPPER_EULER, GOPF_STEPPER_RK4, GOPF_STEPPER_IMPLICIT_EULER = 0, 1, 2
+DER_PRODUCT, DER_POLY, DER_INDICATOR, DER_INDICATOR_D, DER_INDICATOR_HD, DER_WHITE_NOISE = range(6)
+NOISE_WHITE, NOISE_CONSERVATIVE = 1, 2
 SRC_NONE, SRC_FIELD, SRC_DERIVED = range(3)
 RED_SUM, RED_SUMSQ, RED_MIN, RED_MAX, RED_NONFINITE = range(5)
-OPT_CHECK_FINITE, OPT_USE_GRAPHS, OPT_FAST_KERNELS = 0, 1, 2
+OPT_CHECK_FINITE, OPT_USE_GRAPHS, OPT_FAST_KERNELS, OPT_TMA = 0, 1, 2, 3
 MAX_FACTORS = 8
 
 
@@ -70,6 +71,7 @@ SIGNATURES = {
     "gopf_register_elastic": ([_vp, _cp, _cp, _dp, _dp], _i),
     "gopf_register_volcons": ([_vp, _cp, _cp, _cp, ctypes.c_double], _i),
     "gopf_add_equation": ([_vp, _cp], _i),
+    "gopf_register_noise": ([_vp, _cp, _i, _cp, ctypes.c_double, ctypes.c_ulonglong], _i),
     "gopf_init": ([_vp], _i),
     "gopf_equation_summary": ([_vp, _i, _ip, _ip], _i),
     "gopf_get_terms": ([_vp, ctypes.POINTER(GopfTerm), _i, _ip], _i),
@@ -97,6 +99,8 @@ SIGNATURES = {
     "gopf_adjoint_release": ([_vp], _i),
     "gopf_reduce_noalloc": ([_vp, _sz, _dp, _vp], _i),
     "gopf_noalloc_last_error": ([], _cp),
+    "gopf_set_newton_krylov": ([_vp, _i, ctypes.c_double, ctypes.c_double, _i, _i], _i),
+    "gopf_newton_stats": ([_vp, _ip, _ip, _dp, _ip], _i),
     "gopf_batch_create": ([ctypes.POINTER(_vp), _i, ctypes.POINTER(_vp)], _i),
     "gopf_batch_destroy": ([_vp], _i),
     "gopf_batch_last_error": ([_vp], _cp),

@@ -16,6 +16,8 @@
 // X_b(k) = (Z(k) - conj Z(-k))/(2i).
 #pragma once
 #include "gopf_kernels.cuh"
+#include "noise.cuh"
+#include "tma.cuh"
 
 namespace gopf {
 namespace f256 {
@@ -57,30 +59,81 @@ __device__ __forceinline__ float fsqf(int i, int n)
     return f * f;
 }
 
-// k-space update of one element (pf/euler.go:32-34 with the term algebra of pf/rhsBuilder.go)
-__device__ __forceinline__ float2 euler_update(float2 c0, const float2 *U, int ngrp, const UpdTable &u, float mk,
-                                               const float *gsc, float dt, float *Lout)
+// Kernels with the update take NZ: true only for models with a noise term, so
+// the Philox/Box-Muller code is not carried by the noise-free instantiations.
+
+// k-space update coefficients staged in registers once per thread
+struct UpdRegs {
+    float dt, invN;
+    int ng;
+    float gs[2];
+    int gl[2];
+    int nimp;
+    float imp[4];
+};
+
+__device__ __forceinline__ UpdRegs load_upd(const UpdTable &u, int ng)
 {
-    float2 nhat = make_float2(0.f, 0.f);
-    for (int b = 0; b < ngrp; ++b) {
-        float f = gsc[b];
-        for (int q = 0; q < u.glap[b]; ++q) f *= mk;
-        nhat.x += f * U[b].x;
-        nhat.y += f * U[b].y;
+    UpdRegs R;
+    R.dt = (float)u.dt;
+    R.invN = (float)u.invN;
+    R.ng = ng;
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+        R.gs[b] = (b < ng && u.gscale[b]) ? (float)(*u.gscale[b]) : 1.f;
+        R.gl[b] = (b < ng) ? u.glap[b] : 0;
     }
-    float L = 0.f;
-    for (int q = u.nimp - 1; q >= 0; --q) L = L * mk + (float)u.imp[q];
-    *Lout = L;
-    const float rden = 1.f / (1.f - dt * L);
-    return make_float2((c0.x + dt * nhat.x) * rden, (c0.y + dt * nhat.y) * rden);
+    R.nimp = u.nimp;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) R.imp[q] = (q < u.nimp) ? (float)u.imp[q] : 0.f;
+    return R;
+}
+
+__device__ __forceinline__ float mkpow(float mk, int p)
+{
+    switch (p) {
+    case 0: return 1.f;
+    case 1: return mk;
+    case 2: return mk * mk;
+    case 3: return mk * mk * mk;
+    default: {
+        float f = 1.f;
+        for (int q = 0; q < p; ++q) f *= mk;
+        return f;
+    }
+    }
+}
+
+// k-space update of one element (pf/euler.go:32-34 with the term algebra of pf/rhsBuilder.go):
+// c <- (c + dt sum_b s_b m^p_b U_b) / (1 - dt L(m)),  m = -k^2
+__device__ __forceinline__ float2 euler_update(const UpdRegs &R, const UpdTable &u, float2 c0, float2 U0, float2 U1,
+                                               float mk)
+{
+    const float f0 = R.gs[0] * mkpow(mk, R.gl[0]);
+    float2 nh = make_float2(f0 * U0.x, f0 * U0.y);
+    if (R.ng > 1) {
+        const float f1 = R.gs[1] * mkpow(mk, R.gl[1]);
+        nh.x += f1 * U1.x;
+        nh.y += f1 * U1.y;
+    }
+    if (R.ng == 0) nh = make_float2(0.f, 0.f);
+    float L;
+    if (R.nimp <= 4) {
+        L = ((R.imp[3] * mk + R.imp[2]) * mk + R.imp[1]) * mk + R.imp[0];
+    } else {
+        L = 0.f;
+        for (int q = u.nimp - 1; q >= 0; --q) L = L * mk + (float)u.imp[q];
+    }
+    const float rden = 1.f / (1.f - R.dt * L);
+    return make_float2((c0.x + R.dt * nh.x) * rden, (c0.y + R.dt * nh.y) * rden);
 }
 
 // ---------------------------------------------------------------------------
 // z axis (strided), fused forward -> update -> inverse.  Lines are 16
 // consecutive inner indices i0 + l of the S = KX*Y plane; thread t = r*16 + l.
 // ---------------------------------------------------------------------------
-template <int NG>
-__global__ void __launch_bounds__(NT, 2) k_z256_fused(const PassArgs<float> a)
+template <int NG, bool NZ>
+__global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_z256_fused(const PassArgs<float> a)
 {
     __shared__ __align__(16) float2 s_x[N * 16];
     __shared__ float2 s_tw[N];
@@ -93,13 +146,9 @@ __global__ void __launch_bounds__(NT, 2) k_z256_fused(const PassArgs<float> a)
     const int ngrp = (NG == 1) ? (a.upd.ngrp > 0 ? 1 : 0) : a.upd.ngrp;
     const bool init = (a.mode == PM_INIT);
 
-    float2 v[16], sv[16];
+    float2 v[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = U0[i0 + l + (long long)(r + 16 * i) * S];
-    if (!init) { // the state's loads overlap the forward transform
-#pragma unroll
-        for (int i = 0; i < 16; ++i) sv[i] = a.state[i0 + l + (long long)(r + 16 * i) * S];
-    }
     load_twiddles(s_tw, a.tw);
     if (threadIdx.x < 16) {
         const long long q = i0 + threadIdx.x;
@@ -121,11 +170,9 @@ __global__ void __launch_bounds__(NT, 2) k_z256_fused(const PassArgs<float> a)
     }
 
     const UpdTable &u = a.upd;
-    const float dt = (float)u.dt, invN = (float)u.invN;
-    float gsc[2];
-    gsc[0] = (u.gscale[0]) ? (float)(*u.gscale[0]) : 1.f;
-    gsc[1] = (ngrp > 1 && u.gscale[1]) ? (float)(*u.gscale[1]) : 1.f;
+    const UpdRegs R = load_upd(u, ngrp);
     const float fourpi2 = 39.478417604357434f;
+    const float fl = s_fl[l];
     float2 *__restrict__ state = a.state;
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
@@ -135,13 +182,19 @@ __global__ void __launch_bounds__(NT, 2) k_z256_fused(const PassArgs<float> a)
         if (init) {
             cn = v[i];
         } else {
-            const float mk = -fourpi2 * (s_fl[l] + s_fz[k]);
-            float2 U[2] = {v[i], (NG > 1) ? w[NG > 1 ? i : 0] : v[i]};
-            float L;
-            cn = euler_update(sv[i], U, ngrp, u, mk, gsc, dt, &L);
+            const float mk = -fourpi2 * (fl + s_fz[k]);
+            float2 c0 = state[gi];
+            if (NZ && u.noise.kind) { // noise enters as dt * N_noise, folded into c0 before the division
+                const long long q = i0 + l, kx = q / g.Y, yy = q - kx * g.Y;
+                double nr, ni;
+                noise_term(u.noise, g.X, g.Y, g.Z, kx, yy, k, (double)mk, nr, ni);
+                c0.x += R.dt * (float)nr;
+                c0.y += R.dt * (float)ni;
+            }
+            cn = euler_update(R, u, c0, v[i], (NG > 1) ? w[NG > 1 ? i : 0] : v[i], mk);
         }
         state[gi] = cn;
-        v[i] = make_float2(cn.x * invN, cn.y * invN);
+        v[i] = make_float2(cn.x * R.invN, cn.y * R.invN);
     }
     fft256<true>(v, r, s_tw, at);
     float2 *__restrict__ T = a.tout;
@@ -150,11 +203,132 @@ __global__ void __launch_bounds__(NT, 2) k_z256_fused(const PassArgs<float> a)
 }
 
 // ---------------------------------------------------------------------------
+// z axis with TMA tiles.  The same transform and update as k_z256_fused, but
+// the block's input tiles (group 0, group 1, c-hat: 16 inner indices x 256 z
+// = 32 KB each) arrive in shared memory through one tensor copy apiece, and
+// the c-hat and T tiles leave the same way.  The threads never wait on
+// individual global loads: three blocks per SM overlap one block's copies
+// with the others' transforms.  Tensor maps: [Z][S] of 8-byte elements, box
+// {16, 256}.
+// ---------------------------------------------------------------------------
+constexpr int ZT_TILE_BYTES = 16 * N * 8;
+
+__host__ __device__ constexpr int z256_tma_smem_bytes(int ng)
+{
+    return 128 /* alignment slack */ + ZT_TILE_BYTES * (ng + 1) + N * 8 /* twiddles */ + N * 4 /* fz */ +
+           16 * 4 /* fl */ + 16 /* barrier, flag */;
+}
+
+template <int NG, bool NZ>
+__global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2)
+    k_z256_tma(const PassArgs<float> a, const __grid_constant__ CUtensorMap mU0, const __grid_constant__ CUtensorMap mU1,
+               const __grid_constant__ CUtensorMap mS, const __grid_constant__ CUtensorMap mT)
+{
+    extern __shared__ unsigned char z_dsm[];
+    unsigned char *base = z_dsm + ((128u - (smem_u32(z_dsm) & 127u)) & 127u);
+    float2 *tU0 = reinterpret_cast<float2 *>(base);
+    float2 *tU1 = reinterpret_cast<float2 *>(base + ZT_TILE_BYTES);
+    float2 *tS = reinterpret_cast<float2 *>(base + ZT_TILE_BYTES * NG);
+    float2 *s_tw = reinterpret_cast<float2 *>(base + ZT_TILE_BYTES * (NG + 1));
+    float *s_fz = reinterpret_cast<float *>(s_tw + N);
+    float *s_fl = s_fz + N;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(s_fl + 16);
+    int *s_ok = reinterpret_cast<int *>(bar + 1);
+
+    const Geom &g = a.g;
+    const int l = threadIdx.x & 15, r = threadIdx.x >> 4;
+    const int i0 = blockIdx.x * 16;
+    const bool init = (a.mode == PM_INIT);
+    const int ngrp = (NG == 1) ? (a.upd.ngrp > 0 ? 1 : 0) : a.upd.ngrp;
+    const bool two = (NG > 1 && ngrp > 1);
+
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t bytes = (uint32_t)ZT_TILE_BYTES * (1u + (two ? 1u : 0u) + (init ? 0u : 1u));
+        mbar_arrive_expect_tx(bar, bytes);
+        tma_load_2d(tU0, &mU0, i0, 0, bar);
+        if (two) tma_load_2d(tU1, &mU1, i0, 0, bar);
+        if (!init) tma_load_2d(tS, &mS, i0, 0, bar);
+    }
+    load_twiddles(s_tw, a.tw);
+    if (threadIdx.x < 16) {
+        const int q = i0 + threadIdx.x;
+        const int kx = q / g.Y, y = q - kx * g.Y;
+        const float fx = (float)kx / (float)g.X;
+        s_fl[threadIdx.x] = fx * fx + fsqf(y, g.Y);
+    }
+    s_fz[threadIdx.x] = fsqf(threadIdx.x, g.Z);
+    if (threadIdx.x == 0) *s_ok = tma_wait_or_flag(bar, 0, a.status) ? 1 : 0;
+    __syncthreads();
+    if (!*s_ok) return;
+
+    float2 v[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = tU0[(r + 16 * i) * 16 + l];
+    __syncthreads(); // the group-0 tile becomes the exchange buffer
+    auto at = [&](int x, int y) -> float2 & { return tU0[(x * 16 + y) * 16 + l]; };
+    fft256<false>(v, r, s_tw, at);
+
+    float2 w[NG == 1 ? 1 : 16];
+    if (two) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) w[i] = tU1[(r + 16 * i) * 16 + l];
+        fft256<false>(reinterpret_cast<float2(&)[16]>(w), r, s_tw, at);
+    }
+
+    const UpdTable &u = a.upd;
+    const UpdRegs R = load_upd(u, ngrp);
+    const float fourpi2 = 39.478417604357434f;
+    const float fl = s_fl[l];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int k = r + 16 * i;
+        float2 cn;
+        if (init) {
+            cn = v[i];
+        } else {
+            const float mk = -fourpi2 * (fl + s_fz[k]);
+            float2 c0 = tS[k * 16 + l];
+            if (NZ && u.noise.kind) {
+                const long long q = i0 + l, kx = q / g.Y, yy = q - kx * g.Y;
+                double nr, ni;
+                noise_term(u.noise, g.X, g.Y, g.Z, kx, yy, k, (double)mk, nr, ni);
+                c0.x += R.dt * (float)nr;
+                c0.y += R.dt * (float)ni;
+            }
+            cn = euler_update(R, u, c0, v[i], (NG > 1) ? w[NG > 1 ? i : 0] : v[i], mk);
+        }
+        tS[k * 16 + l] = cn; // each thread rewrites exactly the elements it read
+        v[i] = make_float2(cn.x * R.invN, cn.y * R.invN);
+    }
+    fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        tma_store_2d(&mS, i0, 0, tS);
+        bulk_commit();
+    }
+    fft256<true>(v, r, s_tw, at);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) tU0[(r + 16 * i) * 16 + l] = v[i];
+    fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        tma_store_2d(&mT, i0, 0, tU0);
+        bulk_commit();
+        bulk_wait_read_all(); // the tiles stay allocated until both stores have read them
+    }
+}
+
+// ---------------------------------------------------------------------------
 // y axis (contiguous lines of 256), forward or inverse in place, or the 2D
 // fused update.  Thread t = l*16 + r: a half-warp reads 128 contiguous bytes.
 // Shared slots are swizzled so both exchange directions are conflict free.
 // ---------------------------------------------------------------------------
-template <int NG>
+template <int NG, bool NZ>
 __global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_y256(const PassArgs<float> a)
 {
     __shared__ __align__(16) float2 s_x[N * 16];
@@ -206,11 +380,9 @@ __global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_y256(const PassArgs<flo
         fft256<false>(reinterpret_cast<float2(&)[16]>(w), r, s_tw, at);
     }
     const UpdTable &u = a.upd;
-    const float dt = (float)u.dt, invN = (float)u.invN;
-    float gsc[2];
-    gsc[0] = (u.gscale[0]) ? (float)(*u.gscale[0]) : 1.f;
-    gsc[1] = (ngrp > 1 && u.gscale[1]) ? (float)(*u.gscale[1]) : 1.f;
+    const UpdRegs R = load_upd(u, ngrp);
     const float fourpi2 = 39.478417604357434f;
+    const float fl = s_fl[l];
     float2 *__restrict__ state = a.state;
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
@@ -221,14 +393,20 @@ __global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_y256(const PassArgs<flo
             if (a.mode == PM_INIT) {
                 cn = v[i];
             } else {
-                const float mk = -fourpi2 * (s_fl[l] + s_fy[k]);
-                float2 U[2] = {v[i], (NG > 1) ? w[NG > 1 ? i : 0] : v[i]};
-                float L;
-                cn = euler_update(state[gi], U, ngrp, u, mk, gsc, dt, &L);
+                const float mk = -fourpi2 * (fl + s_fy[k]);
+                float2 c0 = state[gi];
+                if (NZ && u.noise.kind) {
+                    const long long zz = q / g.KX, kx = q - zz * g.KX;
+                    double nr, ni;
+                    noise_term(u.noise, g.X, g.Y, g.Z, kx, k, zz, (double)mk, nr, ni);
+                    c0.x += R.dt * (float)nr;
+                    c0.y += R.dt * (float)ni;
+                }
+                cn = euler_update(R, u, c0, v[i], (NG > 1) ? w[NG > 1 ? i : 0] : v[i], mk);
             }
             state[gi] = cn;
         }
-        v[i] = make_float2(cn.x * invN, cn.y * invN);
+        v[i] = make_float2(cn.x * R.invN, cn.y * R.invN);
     }
     fft256<true>(v, r, s_tw, at);
     float2 *__restrict__ T = a.tout;
@@ -262,6 +440,50 @@ template <typename F> __device__ __forceinline__ float polyf(const PwTable &pw, 
     return acc;
 }
 
+// Pointwise polynomial of the packed row pair, forward transform and separation
+// of the two rows' half spectra into out[grp] (v is overwritten).
+template <typename AT>
+__device__ __forceinline__ void xpoint_fwd_store(float2 (&v)[16], const XPassArgs<float> &a, int grp,
+                                                 const float *s_poly, int r, int j, const float2 *s_tw, AT &&at,
+                                                 float2 *s_x, long long sbase, int KX, int Y)
+{
+    if (!a.identity) {
+        const int d = a.pw.deg[grp];
+        const float *cf = s_poly + grp * (GOPF_MAX_DEG + 1);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            float px, py;
+            if (d >= 0) {
+                px = cf[d];
+                py = cf[d];
+                for (int q = d - 1; q >= 0; --q) {
+                    px = px * v[i].x + cf[q];
+                    py = py * v[i].y + cf[q];
+                }
+            } else {
+                px = polyf<float>(a.pw, grp, v[i].x);
+                py = polyf<float>(a.pw, grp, v[i].y);
+            }
+            v[i] = make_float2(px, py);
+        }
+    }
+    fft256<false>(v, r, s_tw, at);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) s_x[(r + 16 * i) * 16 + j] = v[i];
+    __syncthreads();
+    float2 *__restrict__ out = a.out[grp];
+    for (int e = threadIdx.x; e < KX * XROWS; e += NT) {
+        const int kx = e >> 5, y = e & 31, jj = y >> 1;
+        const float2 P = s_x[kx * 16 + jj];
+        const float2 Q = s_x[((N - kx) & (N - 1)) * 16 + jj];
+        float2 o;
+        if ((y & 1) == 0) o = make_float2(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y));
+        else o = make_float2(0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
+        out[sbase + (long long)kx * Y + y] = o;
+    }
+    __syncthreads();
+}
+
 // NG == 1: one output group, transformed in place; NG == 0: any number of groups
 template <int NG>
 __global__ void __launch_bounds__(NT, 2) k_x256(const XPassArgs<float> a)
@@ -269,8 +491,11 @@ __global__ void __launch_bounds__(NT, 2) k_x256(const XPassArgs<float> a)
     // spectral tile [129][32] during c2r input, then exchange slots [256][16]
     __shared__ __align__(16) float2 s_x[N * 16 + 64];
     __shared__ float2 s_tw[N];
+    __shared__ float s_poly[GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1)];
     const Geom &g = a.g;
     const int j = threadIdx.x & 15, r = threadIdx.x >> 4;
+    for (int t = threadIdx.x; t < GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1); t += NT)
+        s_poly[t] = (float)a.pw.dense[t / (GOPF_MAX_DEG + 1)][t % (GOPF_MAX_DEG + 1)];
     const int y0 = blockIdx.x * XROWS;
     const int z = blockIdx.y;
     const long long sbase = (long long)z * g.S + y0;
@@ -300,30 +525,305 @@ __global__ void __launch_bounds__(NT, 2) k_x256(const XPassArgs<float> a)
     auto at = [&](int x, int y) -> float2 & { return s_x[(x * 16 + y) * 16 + j]; };
     fft256<true>(v, r, s_tw, at);
     // v[i] = c(row 2j, col r + 16 i) + i c(row 2j+1, col r + 16 i)
-    const int ng = (NG == 1) ? 1 : a.ngrp_out;
-    for (int grp = 0; grp < ng; ++grp) {
-        float2 wbuf[NG == 1 ? 1 : 16];
-        float2(&w)[16] = (NG == 1) ? v : reinterpret_cast<float2(&)[16]>(wbuf);
+    if (NG == 1) {
+        xpoint_fwd_store(v, a, 0, s_poly, r, j, s_tw, at, s_x, sbase, KX, Y);
+    } else {
+        for (int grp = 0; grp < a.ngrp_out; ++grp) {
+            float2 w[16];
 #pragma unroll
-        for (int i = 0; i < 16; ++i)
-            w[i] = a.identity ? v[i] : make_float2(polyf<float>(a.pw, grp, v[i].x), polyf<float>(a.pw, grp, v[i].y));
+            for (int i = 0; i < 16; ++i) w[i] = v[i];
+            xpoint_fwd_store(w, a, grp, s_poly, r, j, s_tw, at, s_x, sbase, KX, Y);
+        }
+    }
+}
+
+
+// ---------------------------------------------------------------------------
+// z axis, persistent and double-buffered (one explicit group).  Two blocks per
+// SM walk the tiles blockIdx.x, blockIdx.x + gridDim.x, ...; the group tile of
+// the next tile is requested a whole iteration ahead and the c-hat tile as soon
+// as the previous one has been read out, so HBM traffic overlaps the
+// transforms instead of waiting on them.  Shared memory: two group tiles (the
+// current one doubles as the exchange buffer and then as the T tile), one
+// c-hat tile, twiddles and frequency tables.
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int z256_pipe_smem_bytes()
+{
+    return 128 + ZT_TILE_BYTES * 3 + N * 8 + N * 4 + 16 * 4 + 32;
+}
+
+template <bool NZ>
+__global__ void __launch_bounds__(NT, 2)
+    k_z256_pipe(const PassArgs<float> a, const __grid_constant__ CUtensorMap mU0, const __grid_constant__ CUtensorMap mS,
+                const __grid_constant__ CUtensorMap mT, int ntiles)
+{
+    extern __shared__ unsigned char p_dsm[];
+    unsigned char *base = p_dsm + ((128u - (smem_u32(p_dsm) & 127u)) & 127u);
+    float2 *bufU[2] = {reinterpret_cast<float2 *>(base), reinterpret_cast<float2 *>(base + ZT_TILE_BYTES)};
+    float2 *tS = reinterpret_cast<float2 *>(base + 2 * ZT_TILE_BYTES);
+    float2 *s_tw = reinterpret_cast<float2 *>(base + 3 * ZT_TILE_BYTES);
+    float *s_fz = reinterpret_cast<float *>(s_tw + N);
+    float *s_fl = s_fz + N;
+    uint64_t *barU = reinterpret_cast<uint64_t *>(s_fl + 16); // [2]
+    uint64_t *barS = barU + 2;
+    int *s_ok = reinterpret_cast<int *>(barS + 1);
+
+    const Geom &g = a.g;
+    const int tid = threadIdx.x;
+    const int l = tid & 15, r = tid >> 4;
+    const bool init = (a.mode == PM_INIT);
+    const int ngrp = (a.upd.ngrp > 0) ? 1 : 0;
+    int tile = blockIdx.x;
+    if (tile >= ntiles) return;
+
+    if (tid == 0) {
+        mbar_init(&barU[0], 1);
+        mbar_init(&barU[1], 1);
+        mbar_init(barS, 1);
+        fence_mbar_init();
+        mbar_arrive_expect_tx(&barU[0], (uint32_t)ZT_TILE_BYTES);
+        tma_load_2d(bufU[0], &mU0, tile * 16, 0, &barU[0]);
+        if (!init) {
+            mbar_arrive_expect_tx(barS, (uint32_t)ZT_TILE_BYTES);
+            tma_load_2d(tS, &mS, tile * 16, 0, barS);
+        }
+        *s_ok = 1;
+    }
+    load_twiddles(s_tw, a.tw);
+    s_fz[tid] = fsqf(tid, g.Z);
+    const UpdTable &u = a.upd;
+    const UpdRegs R = load_upd(u, ngrp);
+    const float fourpi2 = 39.478417604357434f;
+    auto wait_flag = [&](uint64_t *bar, uint32_t parity) {
+        if (tid == 0 && !tma_wait_or_flag(bar, parity, a.status)) *s_ok = 0;
+        __syncthreads();
+        return *s_ok != 0;
+    };
+
+    for (int it = 0; tile < ntiles; ++it, tile += gridDim.x) {
+        const int cur = it & 1;
+        const int next = tile + gridDim.x;
+        const int i0 = tile * 16;
+        float2 *tU = bufU[cur];
+        if (tid == 0 && next < ntiles) {
+            bulk_wait_read_all(); // the previous tile's stores have read bufU[cur ^ 1]
+            mbar_arrive_expect_tx(&barU[cur ^ 1], (uint32_t)ZT_TILE_BYTES);
+            tma_load_2d(bufU[cur ^ 1], &mU0, next * 16, 0, &barU[cur ^ 1]);
+        }
+        if (tid < 16) {
+            const int q = i0 + tid;
+            const int kx = q / g.Y, y = q - kx * g.Y;
+            const float fx = (float)kx / (float)g.X;
+            s_fl[tid] = fx * fx + fsqf(y, g.Y);
+        }
+        if (!wait_flag(&barU[cur], (uint32_t)((it >> 1) & 1))) return;
+
+        float2 v[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = tU[(r + 16 * i) * 16 + l];
+        __syncthreads(); // the group tile becomes the exchange buffer
+        auto at = [&](int x, int y) -> float2 & { return tU[(x * 16 + y) * 16 + l]; };
+        fft256<false>(v, r, s_tw, at);
+
+        if (!init && !wait_flag(barS, (uint32_t)(it & 1))) return;
+        const float fl = s_fl[l];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const int k = r + 16 * i;
+            float2 cn;
+            if (init) {
+                cn = v[i];
+            } else {
+                const float mk = -fourpi2 * (fl + s_fz[k]);
+                float2 c0 = tS[k * 16 + l];
+                if (NZ && u.noise.kind) {
+                    const long long q = i0 + l, kx = q / g.Y, yy = q - kx * g.Y;
+                    double nr, ni;
+                    noise_term(u.noise, g.X, g.Y, g.Z, kx, yy, k, (double)mk, nr, ni);
+                    c0.x += R.dt * (float)nr;
+                    c0.y += R.dt * (float)ni;
+                }
+                cn = euler_update(R, u, c0, v[i], v[i], mk);
+            }
+            tS[k * 16 + l] = cn;
+            v[i] = make_float2(cn.x * R.invN, cn.y * R.invN);
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tma_store_2d(&mS, i0, 0, tS);
+            bulk_commit();
+        }
+        fft256<true>(v, r, s_tw, at);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) tU[(r + 16 * i) * 16 + l] = v[i];
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tma_store_2d(&mT, i0, 0, tU);
+            bulk_commit();
+            if (next < ntiles && !init) {
+                asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); // the c-hat store has read tS
+                mbar_arrive_expect_tx(barS, (uint32_t)ZT_TILE_BYTES);
+                tma_load_2d(tS, &mS, next * 16, 0, barS);
+            }
+        }
+    }
+    if (tid == 0) bulk_wait_read_all();
+}
+
+// ---------------------------------------------------------------------------
+// x axis with TMA tiles.  The block's input is the [129 kx][32 y] half
+// spectrum of 32 rows of one depth plane (one 3D tensor copy); each output
+// group's [129][32] tile is assembled in shared memory by the separation step
+// and leaves as one tensor store.  Per thread, the separation works on a fixed
+// row y = tid mod 32 and kx = tid/32 + 8 q, so no index arithmetic is 64-bit.
+// Tensor map: [Z][KX][Y] of 8-byte elements, box {32, KX, 1}.
+// ---------------------------------------------------------------------------
+constexpr int XT_TILE_BYTES = 129 * XROWS * 8;          // 33,024
+constexpr int XT_XCH_BYTES = (N * 16 + 64) * 8;         // exchange slots [256][16] (+ pad)
+
+__host__ __device__ constexpr int x256_tma_smem_bytes()
+{
+    return 128 + XT_XCH_BYTES + XT_TILE_BYTES + N * 8 + GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1) * 4 + 16;
+}
+
+template <int D> __device__ __forceinline__ float horner_f(const float (&c)[GOPF_MAX_DEG + 1], float x)
+{
+    float acc = c[D];
+#pragma unroll
+    for (int q = D - 1; q >= 0; --q) acc = acc * x + c[q];
+    return acc;
+}
+
+template <int D> __device__ __forceinline__ void poly_regs(float2 (&v)[16], const float *cf)
+{
+    float c[GOPF_MAX_DEG + 1];
+#pragma unroll
+    for (int q = 0; q <= D; ++q) c[q] = cf[q];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = make_float2(horner_f<D>(c, v[i].x), horner_f<D>(c, v[i].y));
+}
+
+// g(c) of group grp on both packed rows, with the degree resolved once per block
+__device__ __forceinline__ void apply_poly(float2 (&v)[16], const XPassArgs<float> &a, int grp, const float *cf)
+{
+    switch (a.pw.deg[grp]) {
+    case 0: poly_regs<0>(v, cf); return;
+    case 1: poly_regs<1>(v, cf); return;
+    case 2: poly_regs<2>(v, cf); return;
+    case 3: poly_regs<3>(v, cf); return;
+    case 4: poly_regs<4>(v, cf); return;
+    case 5: poly_regs<5>(v, cf); return;
+    case 6: poly_regs<6>(v, cf); return;
+    default: break;
+    }
+    const int d = a.pw.deg[grp];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        float px, py;
+        if (d >= 0) {
+            px = cf[d];
+            py = cf[d];
+            for (int q = d - 1; q >= 0; --q) {
+                px = px * v[i].x + cf[q];
+                py = py * v[i].y + cf[q];
+            }
+        } else {
+            px = polyf<float>(a.pw, grp, v[i].x);
+            py = polyf<float>(a.pw, grp, v[i].y);
+        }
+        v[i] = make_float2(px, py);
+    }
+}
+
+template <int NG>
+__global__ void __launch_bounds__(NT, 3)
+    k_x256_tma(const XPassArgs<float> a, const __grid_constant__ CUtensorMap mIn, const __grid_constant__ CUtensorMap mO0,
+               const __grid_constant__ CUtensorMap mO1, const __grid_constant__ CUtensorMap mO2,
+               const __grid_constant__ CUtensorMap mO3)
+{
+    extern __shared__ unsigned char x_dsm[];
+    unsigned char *base = x_dsm + ((128u - (smem_u32(x_dsm) & 127u)) & 127u);
+    float2 *s_x = reinterpret_cast<float2 *>(base);                        // input tile, then exchange slots
+    float2 *s_o = reinterpret_cast<float2 *>(base + XT_XCH_BYTES);         // output tile [129][32]
+    float2 *s_tw = reinterpret_cast<float2 *>(base + XT_XCH_BYTES + XT_TILE_BYTES);
+    float *s_poly = reinterpret_cast<float *>(s_tw + N);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(s_poly + GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1));
+    int *s_ok = reinterpret_cast<int *>(bar + 1);
+
+    const int tid = threadIdx.x;
+    const int j = tid & 15, r = tid >> 4;
+    const int y0 = blockIdx.x * XROWS;
+    const int z = blockIdx.y;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        mbar_arrive_expect_tx(bar, (uint32_t)XT_TILE_BYTES);
+        tma_load_3d(s_x, &mIn, y0, 0, z, bar);
+    }
+    for (int t = tid; t < GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1); t += NT)
+        s_poly[t] = (float)a.pw.dense[t / (GOPF_MAX_DEG + 1)][t % (GOPF_MAX_DEG + 1)];
+    load_twiddles(s_tw, a.twX);
+    if (tid == 0) *s_ok = tma_wait_or_flag(bar, 0, a.status) ? 1 : 0;
+    __syncthreads();
+    if (!*s_ok) return;
+
+    // Hermitian extension, rows (2j, 2j+1) packed as a + i b
+    float2 v[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int k = r + 16 * i;
+        if (k <= 128) {
+            const float4 ab = *reinterpret_cast<const float4 *>(&s_x[k * XROWS + 2 * j]);
+            v[i] = make_float2(ab.x - ab.w, ab.y + ab.z);
+        } else {
+            const float4 ab = *reinterpret_cast<const float4 *>(&s_x[(N - k) * XROWS + 2 * j]);
+            v[i] = make_float2(ab.x + ab.w, -ab.y + ab.z);
+        }
+    }
+    __syncthreads();
+    auto at = [&](int x, int y) -> float2 & { return s_x[(x * 16 + y) * 16 + j]; };
+    fft256<true>(v, r, s_tw, at);
+    // v[i] = c(row 2j, col r + 16 i) + i c(row 2j+1, col r + 16 i)
+
+    const int ng = (NG == 1) ? 1 : a.ngrp_out;
+    const int yy = tid & 31, jj = yy >> 1, odd = yy & 1, kx0 = tid >> 5;
+    for (int grp = 0; grp < ng; ++grp) {
+        float2 w[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) w[i] = v[i];
+        if (!a.identity) apply_poly(w, a, grp, s_poly + grp * (GOPF_MAX_DEG + 1));
         fft256<false>(w, r, s_tw, at);
-        // w[i] = G(k = r + 16 i); separate the two rows' half spectra
 #pragma unroll
         for (int i = 0; i < 16; ++i) s_x[(r + 16 * i) * 16 + j] = w[i];
+        if (grp > 0 && tid == 0) bulk_wait_read_all(); // the previous group's store has read s_o
         __syncthreads();
-        float2 *__restrict__ out = a.out[grp];
-        for (int e = threadIdx.x; e < KX * XROWS; e += NT) {
-            const int kx = e >> 5, y = e & 31, jj = y >> 1;
-            const float2 P = s_x[kx * 16 + jj];
-            const float2 Q = s_x[((N - kx) & (N - 1)) * 16 + jj];
-            float2 o;
-            if ((y & 1) == 0) o = make_float2(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y));
-            else o = make_float2(0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
-            out[sbase + (long long)kx * Y + y] = o;
+        // separation: X_a(k) = (Z(k) + conj Z(-k))/2 (even rows), X_b(k) = (Z(k) - conj Z(-k))/(2i) (odd rows)
+#pragma unroll 4
+        for (int q = 0; q < 17; ++q) {
+            const int kx = kx0 + 8 * q;
+            if (kx <= 128) {
+                const float2 P = s_x[kx * 16 + jj];
+                const float2 Q = s_x[((N - kx) & (N - 1)) * 16 + jj];
+                float2 o;
+                if (!odd) o = make_float2(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y));
+                else o = make_float2(0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
+                s_o[kx * XROWS + yy] = o;
+            }
         }
+        fence_async_smem();
         __syncthreads();
+        if (tid == 0) {
+            const CUtensorMap *m = (grp == 0) ? &mO0 : (grp == 1) ? &mO1 : (grp == 2) ? &mO2 : &mO3;
+            tma_store_3d(m, y0, 0, z, s_o);
+            bulk_commit();
+        }
     }
+    if (tid == 0) bulk_wait_read_all();
 }
 
 } // namespace f256

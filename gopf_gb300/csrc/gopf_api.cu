@@ -223,7 +223,9 @@ template <typename R> static int ctx_alloc(gopf_ctx *ctx)
     ctx->nred_blocks = ((g.Y + ctx->LBx - 1) / ctx->LBx) * g.Z;
     CK(cudaMalloc(&ctx->d_red, sizeof(double) * RED_SLOTS * ctx->nred_blocks));
     CK(cudaMalloc(&ctx->d_redout, sizeof(double) * RED_SLOTS));
-    ctx->dev_bytes += sizeof(double) * RED_SLOTS * (ctx->nred_blocks + 1);
+    CK(cudaMalloc(&ctx->d_status, sizeof(unsigned)));
+    CK(cudaMemset(ctx->d_status, 0, sizeof(unsigned)));
+    ctx->dev_bytes += sizeof(double) * RED_SLOTS * (ctx->nred_blocks + 1) + sizeof(unsigned);
     CK(cudaMemset(ctx->d_state, 0, sizeof(V) * g.C));
     CK(cudaMemset(ctx->d_T, 0, sizeof(V) * g.C));
     int rc;
@@ -233,8 +235,12 @@ template <typename R> static int ctx_alloc(gopf_ctx *ctx)
     return GOPF_OK;
 }
 
+void gopf_ie_free(gopf_ctx *ctx);
+int gopf_ie_step(gopf_ctx *ctx);
+
 static void ctx_free(gopf_ctx *ctx)
 {
+    gopf_ie_free(ctx);
     if (ctx->gexec1) cudaGraphExecDestroy(ctx->gexec1);
     if (ctx->gexecK) cudaGraphExecDestroy(ctx->gexecK);
     void *ptrs[] = {ctx->d_state, ctx->d_T, ctx->d_real, ctx->d_c128, ctx->d_red, ctx->d_redout,
@@ -243,7 +249,7 @@ static void ctx_free(gopf_ctx *ctx)
         if (p) cudaFree(p);
     for (int i = 1; i < GOPF_MAX_GROUPS; ++i)
         if (ctx->d_U[i]) cudaFree(ctx->d_U[i]);
-    void *more[] = {ctx->d_bsym, ctx->d_U0, ctx->d_UH, ctx->d_vc, ctx->d_red2, ctx->d_rkF};
+    void *more[] = {ctx->d_bsym, ctx->d_U0, ctx->d_UH, ctx->d_vc, ctx->d_red2, ctx->d_rkF, ctx->d_stepctr, ctx->d_status};
     for (void *p : more)
         if (p) cudaFree(p);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -341,7 +347,9 @@ extern "C" int gopf_set_option(gopf_ctx *ctx, int opt, long long v)
     if (opt == GOPF_OPT_CHECK_FINITE) ctx->check_finite = (int)(v != 0);
     else if (opt == GOPF_OPT_USE_GRAPHS) ctx->use_graphs = (int)(v != 0);
     else if (opt == GOPF_OPT_FAST_KERNELS) ctx->use_fast = (int)(v != 0);
+    else if (opt == GOPF_OPT_TMA) ctx->use_tma = (int)std::min<long long>(std::max<long long>(v, 0), 2);
     else return gopf_fail(ctx, GOPF_ERR_ARG, "unknown option");
+    invalidate_graphs(ctx); // captured launches carry the old choice
     return GOPF_OK;
 }
 
@@ -376,9 +384,21 @@ static int derived_poly(gopf_ctx *ctx, const gopf_derived &d, std::vector<std::p
     case GOPF_DER_INDICATOR: out = {{3.0, 2}, {-2.0, 3}}; break;
     case GOPF_DER_INDICATOR_D: out = {{6.0, 1}, {-6.0, 2}}; break;
     case GOPF_DER_INDICATOR_HD: out = {{18.0, 3}, {-30.0, 4}, {12.0, 5}}; break;
+    case GOPF_DER_WHITE_NOISE:
+        return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "white noise enters only as a term of its own");
     default: return gopf_fail(ctx, GOPF_ERR_ARG, "unknown derived-field kind");
     }
     return GOPF_OK;
+}
+
+static unsigned long long noise_seed_of(gopf_ctx *ctx, int derived_index)
+{
+    if (derived_index < (int)ctx->def.derived_names.size()) {
+        const std::string &nm = ctx->def.derived_names[derived_index];
+        for (auto &nz : ctx->def.noise)
+            if (nz.kind == 1 && nz.name == nm) return nz.seed;
+    }
+    return 0;
 }
 
 static int add_poly_to_group(gopf_ctx *ctx, PwTable &pw, int grp, const std::vector<std::pair<double, int>> &poly,
@@ -417,6 +437,10 @@ int gopf_compile_model(gopf_ctx *ctx)
     memset(&pw, 0, sizeof(pw));
     UpdTable u;
     memset(&u, 0, sizeof(u));
+    NoiseParams noise;
+    memset(&noise, 0, sizeof(noise));
+    double noise_strength = 0.0;
+    unsigned long long noise_seed = 0;
     int maxp = 0;
     for (const gopf_term &t : ctx->terms) {
         if (t.eq != 0) return gopf_fail(ctx, GOPF_ERR_ARG, "term refers to an equation that does not exist");
@@ -433,6 +457,15 @@ int gopf_compile_model(gopf_ctx *ctx)
         } else if (t.source == GOPF_SRC_DERIVED) {
             if (t.src_index < 0 || t.src_index >= (int)ctx->der.size())
                 return gopf_fail(ctx, GOPF_ERR_ARG, "bad derived-field index");
+            if (ctx->der[t.src_index].kind == GOPF_DER_WHITE_NOISE) {
+                if (noise.kind) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "one noise term per model");
+                noise.kind = 1;
+                noise.coef = t.coef;
+                noise.lap = t.lap;
+                noise_strength = ctx->der[t.src_index].coef[0];
+                noise_seed = noise_seed_of(ctx, t.src_index);
+                continue;
+            }
             int rc = derived_poly(ctx, ctx->der[t.src_index], poly);
             if (rc) return rc;
         } else {
@@ -497,15 +530,39 @@ int gopf_compile_model(gopf_ctx *ctx)
             ctx->vc_group = grp;
             ctx->vc_dt = v.dt;
             ctx->vc_coef = sp.coef;
+        } else if (sp.kind == 3) {
+            const gopf_modeldef::Noise &nz = ctx->def.noise[sp.index];
+            if (noise.kind) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "one noise term per model");
+            noise.kind = 2;
+            noise.coef = sp.coef;
+            noise.lap = sp.lap;
+            noise_strength = nz.strength;
+            noise_seed = nz.seed;
         } else {
             return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "user-defined term kind has no device implementation");
         }
+    }
+    if (noise.kind) {
+        noise.ndim = ctx->ndim;
+        noise.amp = sqrt((double)ctx->g.N * 2.0 * noise_strength);
+        noise.seed_lo = (uint32_t)(noise_seed & 0xffffffffu);
+        noise.seed_hi = (uint32_t)(noise_seed >> 32);
     }
     if (ctx->has_elastic && u.ngrp + 1 > GOPF_MAX_GROUPS)
         return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "too many term groups with the elastic term");
     pw.ngrp = u.ngrp;
     pw_densify(pw);
     u.nimp = maxp;
+    if (noise.kind && ctx->device >= 0) {
+        if (!ctx->d_stepctr) {
+            CK(cudaMalloc(&ctx->d_stepctr, sizeof(unsigned long long)));
+            ctx->dev_bytes += sizeof(unsigned long long);
+        }
+        CK(cudaMemset(ctx->d_stepctr, 0, sizeof(unsigned long long)));
+        noise.step = ctx->d_stepctr;
+    }
+    u.noise = noise;
+    ctx->noise = noise;
     ctx->pw = pw;
     ctx->upd = u;
     ctx->ngroups = u.ngrp;
@@ -591,7 +648,7 @@ extern "C" int gopf_equation_summary(gopf_ctx *ctx, int eq, int *ne, int *ni)
 extern "C" int gopf_set_stepper(gopf_ctx *ctx, int stepper, double dt)
 {
     if (!ctx) return GOPF_ERR_ARG;
-    if (stepper != GOPF_STEPPER_EULER && stepper != GOPF_STEPPER_RK4)
+    if (stepper != GOPF_STEPPER_EULER && stepper != GOPF_STEPPER_RK4 && stepper != GOPF_STEPPER_IMPLICIT_EULER)
         return gopf_fail(ctx, GOPF_ERR_ARG, "unknown stepper");
     if (!(dt > 0.0) || !std::isfinite(dt)) return gopf_fail(ctx, GOPF_ERR_ARG, "dt must be positive");
     ctx->stepper = stepper;
@@ -612,7 +669,8 @@ template <typename R> static XPassArgs<R> xargs(gopf_ctx *ctx)
     a.g = ctx->g;
     a.planH = ctx->planH;
     a.twX = (const V *)ctx->d_twX;
-    a.allow_fast = ctx->use_fast;
+    a.allow_fast = ctx->use_fast ? (ctx->use_tma >= 2 ? 7 : ctx->use_tma ? 3 : 1) : 0;
+    a.status = ctx->d_status;
     return a;
 }
 
@@ -624,7 +682,8 @@ template <typename R> static PassArgs<R> pargs(gopf_ctx *ctx, bool zaxis)
     a.g = ctx->g;
     a.plan = zaxis ? ctx->planZ : ctx->planY;
     a.tw = (const V *)(zaxis ? ctx->d_twZ : ctx->d_twY);
-    a.allow_fast = ctx->use_fast;
+    a.allow_fast = ctx->use_fast ? (ctx->use_tma >= 2 ? 7 : ctx->use_tma ? 3 : 1) : 0;
+    a.status = ctx->d_status;
     return a;
 }
 
@@ -974,6 +1033,20 @@ extern "C" int gopf_field_download_real(gopf_ctx *ctx, int f, double *d, size_t 
 // reductions
 // ------------------------------------------------------------------
 
+// Read and clear the device status word (stream-synchronising).  A set bit
+// means a bounded device wait ran out: the step's results are not valid.
+static int check_device_status(gopf_ctx *ctx)
+{
+    unsigned st = 0;
+    CK(cudaMemcpyAsync(&st, ctx->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (st) {
+        CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(unsigned), ctx->stream));
+        return gopf_fail(ctx, GOPF_ERR_TIMEOUT, "a device copy did not complete in time (status " + std::to_string(st) + ")");
+    }
+    return GOPF_OK;
+}
+
 static int reduce_all(gopf_ctx *ctx, double *host5)
 {
     cudaError_t e = (ctx->prec == GOPF_FP32) ? enqueue_xpass_out<float>(ctx, nullptr, ctx->d_red)
@@ -1014,9 +1087,29 @@ extern "C" int gopf_step(gopf_ctx *ctx, long long nsteps)
     int rc;
     if ((rc = set_device(ctx))) return rc;
     if (ctx->stepper == GOPF_STEPPER_RK4) {
-        if (ctx->has_elastic || ctx->has_volcons)
-            return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "user-defined terms are stepped with Euler only");
+        if (ctx->has_elastic || ctx->has_volcons || ctx->noise.kind)
+            return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "user-defined and noise terms are stepped with Euler only");
         if ((rc = alloc_spectral(ctx, &ctx->d_rkF))) return rc;
+    }
+    if (ctx->stepper == GOPF_STEPPER_IMPLICIT_EULER) {
+        if (ctx->has_elastic || ctx->has_volcons || ctx->noise.kind)
+            return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "user-defined and noise terms are stepped with Euler only");
+        if (ctx->ngroups + 1 > GOPF_MAX_GROUPS)
+            return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "implicit Euler supports at most 3 explicit groups");
+        // a host-driven Newton-Krylov solve per step: no graphs
+        for (long long s = 0; s < nsteps; ++s) {
+            if ((rc = gopf_ie_step(ctx))) return rc;
+            ++ctx->step;
+        }
+        if (ctx->check_finite) {
+            if ((rc = check_device_status(ctx))) return rc;
+            double r[5];
+            if ((rc = reduce_all(ctx, r))) return rc;
+            if (r[RED_NONFINITE] > 0)
+                return gopf_fail(ctx, GOPF_ERR_NAN, "field contains non-finite values after step " +
+                                                        std::to_string(ctx->step));
+        }
+        return GOPF_OK;
     }
     long long left = nsteps;
     if (ctx->has_elastic && !ctx->el_primed && left > 0) {
@@ -1044,6 +1137,7 @@ extern "C" int gopf_step(gopf_ctx *ctx, long long nsteps)
     }
     ctx->step += nsteps;
     if (ctx->check_finite) {
+        if ((rc = check_device_status(ctx))) return rc;
         double r[5];
         if ((rc = reduce_all(ctx, r))) return rc;
         if (r[RED_NONFINITE] > 0)
@@ -1080,13 +1174,161 @@ int gopf_step_device(gopf_ctx *ctx, long long n)
     return GOPF_OK;
 }
 
+// ---- device pieces of ImplicitEuler (pf/implicitEuler.go), stream-ordered ----
+
+// N_n = the explicit RHS of the current state (read from T) in k space, into nprev.
+// tmp0 is a spectral scratch buffer; T and the state are left unchanged.
+template <typename R> static cudaError_t enqueue_ie_rhs(gopf_ctx *ctx, void *nprev, void *tmp0)
+{
+    typedef typename VecOf<R>::type V;
+    const int G = ctx->ngroups;
+    const bool is3d = ctx->g.Z > 1;
+    if (G == 0) return cudaMemsetAsync(nprev, 0, sizeof(V) * ctx->g.C, ctx->stream);
+    V *U[GOPF_MAX_GROUPS];
+    U[0] = (V *)tmp0;
+    for (int b = 1; b < GOPF_MAX_GROUPS; ++b) U[b] = (V *)ctx->d_U[b];
+    XPassArgs<R> xa = xargs<R>(ctx);
+    xa.in_mode = XIN_SPECTRAL;
+    xa.in = (const V *)ctx->d_T;
+    for (int b = 0; b < G; ++b) xa.out[b] = U[b];
+    xa.ngrp_out = G;
+    xa.pw = ctx->pw;
+    LK(launch_xpass<R>(xa, ctx->LBx, ctx->stream));
+    if (is3d) {
+        PassArgs<R> pa = pargs<R>(ctx, false);
+        pa.mode = PM_FWD;
+        for (int b = 0; b < G; ++b) pa.buf[b] = U[b];
+        pa.nbuf = G;
+        LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+    }
+    PassArgs<R> fa = pargs<R>(ctx, is3d);
+    fa.mode = PM_FUSED;
+    for (int b = 0; b < G; ++b) fa.buf[b] = U[b];
+    fa.nbuf = G;
+    fa.state = (V *)ctx->d_state;
+    fa.tout = U[0];
+    fa.upd = ctx->upd;
+    fa.upd.dt = ctx->dt;
+    fa.upd.invN = 1.0 / (double)ctx->g.N;
+    fa.upd.etd = 1;
+    fa.rkF = (V *)nprev;
+    LK(is3d ? launch_spass<R>(fa, ctx->LBz, ctx->stream) : launch_cpass<R>(fa, ctx->LBy, ctx->stream));
+    return cudaSuccess;
+}
+
+// F(x) = x - IFFT(c_n e^(L dt) + I(L, N(x), N_n)) / N for a real field x (updateEquation,
+// pf/implicitEuler.go:68-94).  Uses T, the group buffers and tmp0 as work space.
+template <typename R>
+static cudaError_t enqueue_ie_residual(gopf_ctx *ctx, const R *x, R *F, const void *chat0, const void *nprev,
+                                       void *tmp0)
+{
+    typedef typename VecOf<R>::type V;
+    const int G = ctx->ngroups;
+    const bool is3d = ctx->g.Z > 1;
+    V *U[GOPF_MAX_GROUPS];
+    U[0] = (V *)ctx->d_T;
+    for (int b = 1; b < GOPF_MAX_GROUPS; ++b) U[b] = (V *)ctx->d_U[b];
+    U[G] = (V *)tmp0; // FFT(x)
+    PwTable pw = ctx->pw;
+    pw.ngrp = G + 1;
+    pw.nterm[G] = 1;
+    pw.pw[G][0] = 1;
+    pw.coef[G][0] = 1.0;
+    pw_densify(pw);
+    XPassArgs<R> xa = xargs<R>(ctx);
+    xa.in_mode = XIN_REAL;
+    xa.rin = x;
+    for (int b = 0; b <= G; ++b) xa.out[b] = U[b];
+    xa.ngrp_out = G + 1;
+    xa.pw = pw;
+    LK(launch_xpass<R>(xa, ctx->LBx, ctx->stream));
+    if (is3d) {
+        PassArgs<R> pa = pargs<R>(ctx, false);
+        pa.mode = PM_FWD;
+        for (int b = 0; b <= G; ++b) pa.buf[b] = U[b];
+        pa.nbuf = G + 1;
+        LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+    }
+    PassArgs<R> fa = pargs<R>(ctx, is3d);
+    fa.mode = PM_FUSED;
+    for (int b = 0; b <= G; ++b) fa.buf[b] = U[b];
+    fa.nbuf = G + 1;
+    fa.state = (V *)const_cast<void *>(chat0);
+    fa.tout = (V *)ctx->d_T;
+    fa.upd = ctx->upd;
+    fa.upd.dt = ctx->dt;
+    fa.upd.invN = 1.0 / (double)ctx->g.N;
+    fa.upd.etd = 2;
+    fa.rkF = (V *)const_cast<void *>(nprev);
+    LK(is3d ? launch_spass<R>(fa, ctx->LBz, ctx->stream) : launch_cpass<R>(fa, ctx->LBy, ctx->stream));
+    if (is3d) {
+        PassArgs<R> ia = pargs<R>(ctx, false);
+        ia.mode = PM_INV;
+        ia.buf[0] = (V *)ctx->d_T;
+        ia.nbuf = 1;
+        LK(launch_cpass<R>(ia, ctx->LBy, ctx->stream));
+    }
+    return enqueue_xpass_out<R>(ctx, F, nullptr);
+}
+
+int gopf_ie_rhs(gopf_ctx *ctx, void *nprev, void *tmp0)
+{
+    cudaError_t e = (ctx->prec == GOPF_FP32) ? enqueue_ie_rhs<float>(ctx, nprev, tmp0)
+                                             : enqueue_ie_rhs<double>(ctx, nprev, tmp0);
+    return (e == cudaSuccess) ? GOPF_OK : cuda_fail(ctx, e, "implicit Euler: RHS");
+}
+
+int gopf_ie_residual(gopf_ctx *ctx, const void *x, void *F, const void *chat0, const void *nprev, void *tmp0)
+{
+    cudaError_t e = (ctx->prec == GOPF_FP32)
+                        ? enqueue_ie_residual<float>(ctx, (const float *)x, (float *)F, chat0, nprev, tmp0)
+                        : enqueue_ie_residual<double>(ctx, (const double *)x, (double *)F, chat0, nprev, tmp0);
+    return (e == cudaSuccess) ? GOPF_OK : cuda_fail(ctx, e, "implicit Euler: residual");
+}
+
+// One explicit Euler step of the state (the Newton start, pf/implicitEuler.go:182-190); x0 <- real field.
+int gopf_ie_euler_guess(gopf_ctx *ctx, void *x0)
+{
+    cudaError_t e = (ctx->prec == GOPF_FP32) ? enqueue_euler<float>(ctx) : enqueue_euler<double>(ctx);
+    if (e == cudaSuccess)
+        e = (ctx->prec == GOPF_FP32) ? enqueue_xpass_out<float>(ctx, (float *)x0, nullptr)
+                                     : enqueue_xpass_out<double>(ctx, (double *)x0, nullptr);
+    return (e == cudaSuccess) ? GOPF_OK : cuda_fail(ctx, e, "implicit Euler: explicit guess");
+}
+
+extern "C" int gopf_set_newton_krylov(gopf_ctx *ctx, int maxiter, double step_size, double tol, int stencil,
+                                      int restart)
+{
+    if (!ctx) return GOPF_ERR_ARG;
+    if (maxiter < 0 || !(step_size > 0.0) || !(tol > 0.0) || restart < 1 || restart > 1000)
+        return gopf_fail(ctx, GOPF_ERR_ARG, "bad Newton-Krylov controls");
+    if (stencil != 2 && stencil != 4 && stencil != 6 && stencil != 8)
+        return gopf_fail(ctx, GOPF_ERR_ARG, "finite-difference stencil must have 2, 4, 6 or 8 points");
+    ctx->nk_maxiter = maxiter;
+    ctx->nk_step = step_size;
+    ctx->nk_tol = tol;
+    ctx->nk_stencil = stencil;
+    ctx->nk_restart = restart;
+    return GOPF_OK;
+}
+
+extern "C" int gopf_newton_stats(gopf_ctx *ctx, int *newton_iters, int *krylov_iters, double *residual, int *converged)
+{
+    if (!ctx) return GOPF_ERR_ARG;
+    if (newton_iters) *newton_iters = ctx->nk_last_newton;
+    if (krylov_iters) *krylov_iters = ctx->nk_last_krylov;
+    if (residual) *residual = ctx->nk_last_residual;
+    if (converged) *converged = ctx->nk_last_converged;
+    return GOPF_OK;
+}
+
 extern "C" int gopf_synchronize(gopf_ctx *ctx)
 {
     if (!ctx) return GOPF_ERR_ARG;
     int rc;
     if ((rc = set_device(ctx))) return rc;
     CK(cudaStreamSynchronize(ctx->stream));
-    return GOPF_OK;
+    return check_device_status(ctx);
 }
 
 extern "C" int gopf_get_time(gopf_ctx *ctx, double *t)

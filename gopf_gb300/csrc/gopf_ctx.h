@@ -36,6 +36,14 @@ struct gopf_modeldef {
         double dt;
     };
     std::vector<Volcons> volcons;                                // VolumeConservingLP terms
+    struct Noise {
+        std::string name;
+        int kind; // 1 white (a derived field), 2 conservative (a user term)
+        int field;
+        double strength;
+        unsigned long long seed;
+    };
+    std::vector<Noise> noise;                                    // WhiteNoise / ConservativeNoise
     std::vector<std::string> equations;                          // AddEquation (spaces removed)
     std::vector<std::string> derived_names;                      // derived fields, in registration order
     std::vector<gopf_derived> derived;
@@ -49,6 +57,8 @@ struct gopf_special {
     double coef;
     int lap;
 };
+
+struct gopf_ie_work;
 
 struct gopf_ctx {
     int device = 0;
@@ -117,6 +127,11 @@ struct gopf_ctx {
 
     void *d_rkF = nullptr; // RK4 accumulator
 
+    // Gaussian noise term (at most one per context) and the device step counter keying it
+    gopf::NoiseParams noise{};
+    unsigned long long *d_stepctr = nullptr;
+    unsigned *d_status = nullptr; // device status word of the bounded waits (0 = clean)
+
     // per-kernel profiling (gopf_profile_step): events recorded after each launch
     std::vector<cudaEvent_t> *prof_events = nullptr;
     size_t prof_next = 0;
@@ -124,6 +139,19 @@ struct gopf_ctx {
     int check_finite = 1;
     int use_graphs = 1;
     int use_fast = 1;
+    int use_tma = 1;
+
+    // ImplicitEuler's Newton-Krylov controls (DefaultNonLinSolver, pf/implicitEuler.go:221-228) and
+    // the outcome of the last step
+    int nk_maxiter = 50;
+    double nk_step = 1e-3;
+    double nk_tol = 1e-7;
+    int nk_stencil = 6;
+    int nk_restart = 50;
+    double nk_krylov_rtol = 1e-8;
+    int nk_last_newton = 0, nk_last_krylov = 0, nk_last_converged = 0;
+    double nk_last_residual = 0.0;
+    gopf_ie_work *ie = nullptr;
     std::string err;
 };
 

@@ -13,6 +13,7 @@
 // per frequency in the last-axis pass.
 #pragma once
 #include "gopf_kernels.cuh"
+#include "noise.cuh"
 #include <math.h>
 
 namespace gopf {
@@ -409,10 +410,55 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
                 nhat.x += f * tv.x;
                 nhat.y += f * tv.y;
             }
+            if (u.noise.kind) {
+                long long kx, yy, zz;
+                if (CONTIG) {
+                    const long long q = l0 + l;
+                    zz = q / g.KX;
+                    kx = q - zz * g.KX;
+                    yy = p;
+                } else {
+                    const long long i = l0 + l;
+                    kx = i / g.Y;
+                    yy = i - kx * g.Y;
+                    zz = p;
+                }
+                double nr, ni;
+                noise_term(u.noise, g.X, g.Y, g.Z, kx, yy, zz, (double)mk, nr, ni);
+                nhat.x += (R)nr;
+                nhat.y += (R)ni;
+            }
             // implicit symbol L = sum_p imp[p] (-k^2)^p
             R L = (R)0;
             for (int q = u.nimp - 1; q >= 0; --q) L = L * mk + (R)u.imp[q];
             const V c0 = state[gi];
+            if (u.etd == 1) { // ImplicitEuler: the explicit RHS at the step's start
+                a.rkF[gi] = nhat;
+                sm[p * pitch + l] = zero;
+                return;
+            }
+            if (u.etd == 2) {
+                // ImplicitEuler residual (pf/implicitEuler.go:68-94): c_n e^(L dt) + integral of the RHS
+                // interpolated linearly between N_n and N(x) (nonlinearIntegral, :151-162), in FP64
+                const double Ld = (double)L, dtd = u.dt;
+                const double f = exp(Ld * dtd);
+                const V np = a.rkF[gi];
+                double ir, ii;
+                if (fabs(Ld) < 1e-5) {
+                    ir = 0.5 * dtd * ((double)nhat.x + (double)np.x * f);
+                    ii = 0.5 * dtd * ((double)nhat.y + (double)np.y * f);
+                } else {
+                    const double c1 = (f - 1.0) / Ld, c2 = (f - Ld * dtd - 1.0) / (Ld * Ld);
+                    const double br = ((double)nhat.x - (double)np.x) / dtd, bi = ((double)nhat.y - (double)np.y) / dtd;
+                    ir = (double)np.x * c1 + br * c2;
+                    ii = (double)np.y * c1 + bi * c2;
+                }
+                const V xh = sm[u.ngrp * tile + p * pitch + l];
+                const double rr = (double)xh.x - ((double)c0.x * f + ir);
+                const double ri = (double)xh.y - ((double)c0.y * f + ii);
+                sm[p * pitch + l] = cmk<V>((R)(rr * u.invN), (R)(ri * u.invN));
+                return;
+            }
             if (u.rk_stage > 0) {
                 const R af = (R)u.rk_afin;
                 V F = (u.rk_stage == 1) ? c0 : a.rkF[gi];

@@ -299,6 +299,11 @@ struct Ctx {
     }
     int user_term(const std::string &name, int &kind) const
     {
+        for (size_t i = 0; i < d.noise.size(); ++i)
+            if (d.noise[i].kind == 2 && d.noise[i].name == name) {
+                kind = 3;
+                return (int)i;
+            }
         for (size_t i = 0; i < d.elastic.size(); ++i)
             if (d.elastic[i].name == name) {
                 kind = 1;
@@ -560,6 +565,31 @@ extern "C" int gopf_register_volcons(gopf_ctx *ctx, const char *term, const char
     v.indicator = indicator;
     v.dt = dt;
     ctx->def.volcons.push_back(v);
+    ctx->initialised = false;
+    return GOPF_OK;
+}
+
+extern "C" int gopf_register_noise(gopf_ctx *ctx, const char *name, int kind, const char *field, double strength,
+                                   unsigned long long seed)
+{
+    if (!ctx || !name || !*name) return gopf_fail(ctx, GOPF_ERR_ARG, "noise name required");
+    if (name_is_reserved(name))
+        return gopf_fail(ctx, GOPF_ERR_ARG, "names may not start with the reserved words -, LAP^4, LAP^2, LAP, *");
+    if (kind != GOPF_NOISE_WHITE && kind != GOPF_NOISE_CONSERVATIVE) return gopf_fail(ctx, GOPF_ERR_ARG, "unknown noise kind");
+    if (!(strength >= 0.0)) return gopf_fail(ctx, GOPF_ERR_ARG, "noise strength must be >= 0");
+    int fid = field_index(ctx, field);
+    if (fid < 0) return gopf_fail(ctx, GOPF_ERR_ARG, "unknown field");
+    ctx->def.noise.push_back({name, kind, fid, strength, seed});
+    if (kind == GOPF_NOISE_WHITE) { // a derived field brick, as RegisterFunction does
+        gopf_derived dv;
+        memset(&dv, 0, sizeof(dv));
+        dv.kind = GOPF_DER_WHITE_NOISE;
+        dv.nfac = 1;
+        dv.field[0] = fid;
+        dv.coef[0] = strength;
+        ctx->def.derived.push_back(dv);
+        ctx->def.derived_names.push_back(name);
+    }
     ctx->initialised = false;
     return GOPF_OK;
 }

@@ -143,8 +143,9 @@ __global__ void k_volcons_finalize(const double *__restrict__ red_field, const d
 // so without the projection FFT round-off there grows like 1/(1 - dt L(k)) per
 // step in the unstable band of L (the complex-field reference carries that
 // part in its imaginary component, where the nonlinearity damps it).
-template <typename V> __global__ void k_hermitian_planes(V *__restrict__ c, Geom g)
+template <typename V> __global__ void k_hermitian_planes(V *__restrict__ c, Geom g, unsigned long long *stepctr)
 {
+    if (stepctr && blockIdx.x == 0 && threadIdx.x == 0) *stepctr += 1; // after this step's noise draws
     const long long per = (long long)g.Y * g.Z;
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < 2 * per;
          idx += (long long)gridDim.x * blockDim.x) {
@@ -173,8 +174,9 @@ cudaError_t gopf_launch_hermitian_planes(gopf_ctx *ctx, void *state)
 {
     const long long n = 2LL * ctx->g.Y * ctx->g.Z;
     const unsigned blocks = (unsigned)std::min<long long>((n + 255) / 256, 152 * 8);
-    if (ctx->prec == GOPF_FP32) k_hermitian_planes<float2><<<blocks, 256, 0, ctx->stream>>>((float2 *)state, ctx->g);
-    else k_hermitian_planes<double2><<<blocks, 256, 0, ctx->stream>>>((double2 *)state, ctx->g);
+    unsigned long long *ctr = (state == ctx->d_state && ctx->noise.kind) ? ctx->d_stepctr : nullptr;
+    if (ctx->prec == GOPF_FP32) k_hermitian_planes<float2><<<blocks, 256, 0, ctx->stream>>>((float2 *)state, ctx->g, ctr);
+    else k_hermitian_planes<double2><<<blocks, 256, 0, ctx->stream>>>((double2 *)state, ctx->g, ctr);
     return cudaGetLastError();
 }
 

@@ -68,6 +68,17 @@ inline void pw_densify(PwTable &pw)
     }
 }
 
+// k-space Gaussian noise term (white or conservative), drawn per mode and step
+struct NoiseParams {
+    int kind;            // 0 none, 1 white (derived field), 2 conservative (D current components)
+    int ndim;
+    double coef;         // sign * scalars of the term
+    int lap;             // LAP power of the term
+    double amp;          // sqrt(N * 2S): standard deviation of |x(k)| of a complex mode
+    uint32_t seed_lo, seed_hi;
+    const unsigned long long *step; // device step counter
+};
+
 // k-space update: c_new = (c + dt * sum_g m^glap[g] U_g) / (1 - dt * sum_p imp[p] m^p),  m = -k^2
 struct UpdTable {
     double dt;
@@ -84,6 +95,12 @@ struct UpdTable {
     //   stage < 4: next = (c + ay k) / (1 - fden L)      stage 4: c = F / (1 - dt L)
     int rk_stage;
     double rk_afin, rk_ay, rk_fden;
+    NoiseParams noise;
+    // ImplicitEuler (pf/implicitEuler.go:68-162); 0 = off.  With N the explicit RHS of the groups:
+    //   etd == 1: rkF <- N (the RHS at the step's start), the state is not changed
+    //   etd == 2: buf[ngrp] holds FFT(x); tile <- (FFT(x) - c e^(L dt) - I(L, N, rkF)) / N for the
+    //             inverse pass (the Newton residual); the state is not changed
+    int etd;
 };
 
 // Reduction slots written by the x-pass (FP64, compensated per block)
@@ -118,6 +135,7 @@ template <typename R> struct XPassArgs {
     int redgrp;
     double *red2;
     int allow_fast; // 1: a specialised kernel may serve this launch
+    unsigned *status; // device status word (bounded waits that ran out set bits)
 };
 
 enum XProgram { XP_POLY = 0, XP_ELASTIC_Q = 1 };
@@ -139,6 +157,7 @@ template <typename R> struct PassArgs {
     const R *bsym;        // PM_ELASTIC_K: elastic symbol in the spectral layout
     V *rkF;               // RK4 accumulator (FUSED with upd.rk_stage > 0)
     int allow_fast;       // 1: a specialised kernel may serve this launch
+    unsigned *status;     // device status word (bounded waits that ran out set bits)
 };
 
 } // namespace gopf

@@ -1,9 +1,119 @@
 // kern_f32.cu -- FP32 instantiation of the spectral-step kernels, with the
 // register-resident 256-point kernels serving the launches they cover.
+#include <algorithm>
+#include <mutex>
+
 #include "fast256.cuh"
 #include "gopf_kernels_impl.cuh"
 
 namespace gopf {
+
+// [Z][S] view of a z-pass array with 16 x 256 boxes
+static bool z_map(CUtensorMap *m, const float2 *p, const Geom &g)
+{
+    const unsigned long long dims[2] = {(unsigned long long)g.S, (unsigned long long)g.Z};
+    const unsigned long long strides[1] = {(unsigned long long)g.S * sizeof(float2)};
+    const unsigned box[2] = {16, (unsigned)f256::N};
+    return encode_map_8b(m, p, 2, dims, strides, box);
+}
+
+// [Z][KX][Y] view of an x-pass array with {32, KX, 1} boxes
+static bool x_map(CUtensorMap *m, const float2 *p, const Geom &g)
+{
+    const unsigned long long dims[3] = {(unsigned long long)g.Y, (unsigned long long)g.KX, (unsigned long long)g.Z};
+    const unsigned long long strides[2] = {(unsigned long long)g.Y * sizeof(float2),
+                                           (unsigned long long)g.S * sizeof(float2)};
+    const unsigned box[3] = {(unsigned)f256::XROWS, (unsigned)g.KX, 1};
+    return encode_map_8b(m, p, 3, dims, strides, box);
+}
+
+static bool launch_x_tma(const XPassArgs<float> &a, cudaStream_t st, cudaError_t *err)
+{
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+        attr_err = cudaFuncSetAttribute(f256::k_x256_tma<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        f256::x256_tma_smem_bytes());
+        if (attr_err == cudaSuccess)
+            attr_err = cudaFuncSetAttribute(f256::k_x256_tma<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            f256::x256_tma_smem_bytes());
+    });
+    if (attr_err != cudaSuccess || a.g.KX != 129 || a.ngrp_out > GOPF_MAX_GROUPS) return false;
+    CUtensorMap mi, mo[GOPF_MAX_GROUPS];
+    if (!x_map(&mi, a.in, a.g)) return false;
+    for (int b = 0; b < GOPF_MAX_GROUPS; ++b) {
+        if (b < a.ngrp_out) {
+            if (!x_map(&mo[b], a.out[b], a.g)) return false;
+        } else {
+            mo[b] = mo[0];
+        }
+    }
+    dim3 grid(a.g.Y / f256::XROWS, a.g.Z);
+    if (a.ngrp_out == 1)
+        f256::k_x256_tma<1><<<grid, f256::NT, f256::x256_tma_smem_bytes(), st>>>(a, mi, mo[0], mo[1], mo[2], mo[3]);
+    else
+        f256::k_x256_tma<0><<<grid, f256::NT, f256::x256_tma_smem_bytes(), st>>>(a, mi, mo[0], mo[1], mo[2], mo[3]);
+    *err = cudaGetLastError();
+    return true;
+}
+
+// Launch the TMA z kernel; false when a tensor map cannot be made (the caller
+// then launches the plain-load kernel).
+static bool launch_z_tma(const PassArgs<float> &a, cudaStream_t st, cudaError_t *err)
+{
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+        const void *k[4] = {(const void *)f256::k_z256_tma<1, false>, (const void *)f256::k_z256_tma<2, false>,
+                            (const void *)f256::k_z256_tma<1, true>, (const void *)f256::k_z256_tma<2, true>};
+        for (int i = 0; i < 4 && attr_err == cudaSuccess; ++i)
+            attr_err = cudaFuncSetAttribute(k[i], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            f256::z256_tma_smem_bytes(1 + (i & 1)));
+        if (attr_err == cudaSuccess)
+            attr_err = cudaFuncSetAttribute(f256::k_z256_pipe<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            f256::z256_pipe_smem_bytes());
+        if (attr_err == cudaSuccess)
+            attr_err = cudaFuncSetAttribute(f256::k_z256_pipe<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            f256::z256_pipe_smem_bytes());
+    });
+    if (attr_err != cudaSuccess) return false;
+    CUtensorMap mU0, mU1, mS, mT;
+    if (!z_map(&mU0, a.buf[0], a.g) || !z_map(&mT, a.tout, a.g) || !z_map(&mS, a.state, a.g)) return false;
+    if (a.nbuf > 1) {
+        if (!z_map(&mU1, a.buf[1], a.g)) return false;
+    } else {
+        mU1 = mU0;
+    }
+    const unsigned grid = (unsigned)(a.g.S / 16);
+    const bool nz = a.upd.noise.kind != 0;
+    if (a.nbuf == 1 && (a.allow_fast & 4)) {
+        // persistent double-buffered variant: two blocks per SM
+        static int nsm = 0;
+        if (!nsm) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+            if (nsm <= 0) nsm = 1;
+        }
+        const int ntiles = (int)grid;
+        const unsigned pg = (unsigned)std::min(ntiles, 2 * nsm);
+        const int smp = f256::z256_pipe_smem_bytes();
+        if (nz) f256::k_z256_pipe<true><<<pg, f256::NT, smp, st>>>(a, mU0, mS, mT, ntiles);
+        else f256::k_z256_pipe<false><<<pg, f256::NT, smp, st>>>(a, mU0, mS, mT, ntiles);
+        *err = cudaGetLastError();
+        return true;
+    }
+    const int sm1 = f256::z256_tma_smem_bytes(1), sm2 = f256::z256_tma_smem_bytes(2);
+    if (a.nbuf > 1) {
+        if (nz) f256::k_z256_tma<2, true><<<grid, f256::NT, sm2, st>>>(a, mU0, mU1, mS, mT);
+        else f256::k_z256_tma<2, false><<<grid, f256::NT, sm2, st>>>(a, mU0, mU1, mS, mT);
+    } else {
+        if (nz) f256::k_z256_tma<1, true><<<grid, f256::NT, sm1, st>>>(a, mU0, mU1, mS, mT);
+        else f256::k_z256_tma<1, false><<<grid, f256::NT, sm1, st>>>(a, mU0, mU1, mS, mT);
+    }
+    *err = cudaGetLastError();
+    return true;
+}
 
 static bool fast_x(const XPassArgs<float> &a)
 {
@@ -15,18 +125,21 @@ static bool fast_y(const PassArgs<float> &a)
 {
     if (!a.allow_fast || a.plan.n != 256 || a.g.Y != 256) return false;
     if (a.mode == PM_FWD || a.mode == PM_INV) return true;
-    return (a.mode == PM_FUSED || a.mode == PM_INIT) && a.g.Z == 1 && a.nbuf <= 2 && a.upd.rk_stage == 0;
+    return (a.mode == PM_FUSED || a.mode == PM_INIT) && a.g.Z == 1 && a.nbuf <= 2 && a.upd.rk_stage == 0 &&
+           a.upd.etd == 0;
 }
 
 static bool fast_z(const PassArgs<float> &a)
 {
     return a.allow_fast && a.plan.n == 256 && a.g.Z == 256 && a.g.S % 16 == 0 &&
-           (a.mode == PM_FUSED || a.mode == PM_INIT) && a.nbuf <= 2 && a.upd.rk_stage == 0;
+           (a.mode == PM_FUSED || a.mode == PM_INIT) && a.nbuf <= 2 && a.upd.rk_stage == 0 && a.upd.etd == 0;
 }
 
 template <> cudaError_t launch_xpass<float>(const XPassArgs<float> &a, int LB, cudaStream_t st)
 {
     if (fast_x(a)) {
+        cudaError_t e;
+        if ((a.allow_fast & 2) && launch_x_tma(a, st, &e)) return e;
         dim3 grid(a.g.Y / f256::XROWS, a.g.Z);
         if (a.ngrp_out == 1) f256::k_x256<1><<<grid, f256::NT, 0, st>>>(a);
         else f256::k_x256<0><<<grid, f256::NT, 0, st>>>(a);
@@ -41,8 +154,14 @@ template <> cudaError_t launch_cpass<float>(const PassArgs<float> &a, int LB, cu
         const long long nlines = (long long)a.g.Z * a.g.KX;
         const bool fused = (a.mode == PM_FUSED || a.mode == PM_INIT);
         dim3 grid((unsigned)((nlines + 15) / 16), fused ? 1 : a.nbuf);
-        if (fused && a.nbuf > 1) f256::k_y256<2><<<grid, f256::NT, 0, st>>>(a);
-        else f256::k_y256<1><<<grid, f256::NT, 0, st>>>(a);
+        const bool nz = fused && a.upd.noise.kind != 0;
+        if (fused && a.nbuf > 1) {
+            if (nz) f256::k_y256<2, true><<<grid, f256::NT, 0, st>>>(a);
+            else f256::k_y256<2, false><<<grid, f256::NT, 0, st>>>(a);
+        } else {
+            if (nz) f256::k_y256<1, true><<<grid, f256::NT, 0, st>>>(a);
+            else f256::k_y256<1, false><<<grid, f256::NT, 0, st>>>(a);
+        }
         return cudaGetLastError();
     }
     return launch_cpass_generic<float>(a, LB, st);
@@ -51,8 +170,17 @@ template <> cudaError_t launch_cpass<float>(const PassArgs<float> &a, int LB, cu
 template <> cudaError_t launch_spass<float>(const PassArgs<float> &a, int LB, cudaStream_t st)
 {
     if (fast_z(a)) {
-        if (a.nbuf > 1) f256::k_z256_fused<2><<<(unsigned)(a.g.S / 16), f256::NT, 0, st>>>(a);
-        else f256::k_z256_fused<1><<<(unsigned)(a.g.S / 16), f256::NT, 0, st>>>(a);
+        cudaError_t e;
+        if ((a.allow_fast & 2) && launch_z_tma(a, st, &e)) return e;
+        const unsigned grid = (unsigned)(a.g.S / 16);
+        const bool nz = a.upd.noise.kind != 0;
+        if (a.nbuf > 1) {
+            if (nz) f256::k_z256_fused<2, true><<<grid, f256::NT, 0, st>>>(a);
+            else f256::k_z256_fused<2, false><<<grid, f256::NT, 0, st>>>(a);
+        } else {
+            if (nz) f256::k_z256_fused<1, true><<<grid, f256::NT, 0, st>>>(a);
+            else f256::k_z256_fused<1, false><<<grid, f256::NT, 0, st>>>(a);
+        }
         return cudaGetLastError();
     }
     return launch_spass_generic<float>(a, LB, st);

@@ -14,6 +14,7 @@
  *   pf.TimeStepper   pf/solver.go:15-19   -> gopf_set_stepper / gopf_step / gopf_get_time
  *   pf.Euler.Step    pf/euler.go:16-47    -> gopf_step (GOPF_STEPPER_EULER)
  *   pf.RK4.Step      pf/rk4.go:29-74      -> gopf_step (GOPF_STEPPER_RK4)
+ *   pf.ImplicitEuler.Step pf/implicitEuler.go:165-207 -> gopf_step (GOPF_STEPPER_IMPLICIT_EULER)
  *   pf.FourierTransform pf/solver.go:22-26, pfutil/fftWrap.go:26-95
  *                                         -> gopf_fft / gopf_freq / gopf_conjugate_node
  *   pf.Model.AddField/AddScalar/AddEquation/RegisterFunction/Init
@@ -53,7 +54,7 @@ enum {
 enum { GOPF_FP32 = 0, GOPF_FP64 = 1 };
 
 /* time steppers */
-enum { GOPF_STEPPER_EULER = 0, GOPF_STEPPER_RK4 = 1 };
+enum { GOPF_STEPPER_EULER = 0, GOPF_STEPPER_RK4 = 1, GOPF_STEPPER_IMPLICIT_EULER = 2 };
 
 /* derived-field kinds (real-space pointwise functions of one field) */
 enum {
@@ -61,7 +62,14 @@ enum {
     GOPF_DER_POLY = 1,        /* sum_t coef_t * field^power_t (a RegisterFunction polynomial) */
     GOPF_DER_INDICATOR = 2,   /* 3x^2 - 2x^3 (pf/homoLinElast.go:10-12) */
     GOPF_DER_INDICATOR_D = 3, /* 6x - 6x^2 (pf/homoLinElast.go:15-17) */
-    GOPF_DER_INDICATOR_HD = 4 /* Indicator(x) * IndicatorDeriv(x) */
+    GOPF_DER_INDICATOR_HD = 4, /* Indicator(x) * IndicatorDeriv(x) */
+    GOPF_DER_WHITE_NOISE = 5   /* N(0, 2S) per cell and step (WhiteNoise.Generate, pf/noise.go:20-23) */
+};
+
+/* noise kinds for gopf_register_noise */
+enum {
+    GOPF_NOISE_WHITE = 1,       /* a function (derived field) name, as RegisterFunction(name, WhiteNoise.Generate) */
+    GOPF_NOISE_CONSERVATIVE = 2 /* a user term name, as RegisterExplicitTerm(name, &ConservativeNoise, ...) */
 };
 
 /* term sources */
@@ -80,7 +88,9 @@ enum {
 enum {
     GOPF_OPT_CHECK_FINITE = 0, /* 1 (default): gopf_step synchronises and checks the field for NaN/Inf */
     GOPF_OPT_USE_GRAPHS = 1,   /* 1 (default): steps are replayed from captured CUDA graphs */
-    GOPF_OPT_FAST_KERNELS = 2  /* 1 (default): register-resident kernels serve the lengths they cover */
+    GOPF_OPT_FAST_KERNELS = 2, /* 1 (default): register-resident kernels serve the lengths they cover */
+    GOPF_OPT_TMA = 3           /* those kernels move their tiles with TMA tensor copies: 0 no, 1 one tile
+                                  per block (default), 2 also the persistent double-buffered z pass */
 };
 
 #define GOPF_MAX_FACTORS 8
@@ -127,6 +137,13 @@ int gopf_register_elastic(gopf_ctx *ctx, const char *term_name, const char *fiel
 /* NewVolumeConservingLP + RegisterExplicitTerm(term_name, ...) */
 int gopf_register_volcons(gopf_ctx *ctx, const char *term_name, const char *field, const char *indicator,
                           double dt);
+/* WhiteNoise (pf/noise.go:11-23) registered as a function, or ConservativeNoise
+ * (pf/noise.go:25-99) registered as an explicit term, with strength S and a seed for
+ * the device's counter-based generator.  The noise is drawn per mode in k space with
+ * the statistics of the FFT of real white noise N(0, 2S); it matches the reference
+ * statistically, not sample for sample (the reference uses Go's global math/rand). */
+int gopf_register_noise(gopf_ctx *ctx, const char *name, int kind, const char *field, double strength,
+                        unsigned long long seed);
 int gopf_add_equation(gopf_ctx *ctx, const char *equation);                       /* Model.AddEquation */
 /* Model.Init + pf.Build: compile every equation into the device term table. */
 int gopf_init(gopf_ctx *ctx);
@@ -142,6 +159,15 @@ int gopf_set_terms(gopf_ctx *ctx, int nfields, const gopf_derived *derived, int 
 
 /* ---- stepping (pf.TimeStepper) ---- */
 int gopf_set_stepper(gopf_ctx *ctx, int stepper, double dt);
+/* ImplicitEuler's Newton-Krylov controls: the fields of nonlin.NewtonKrylov that DefaultNonLinSolver
+ * sets (pf/implicitEuler.go:221-228; defaults maxiter 50, step 1e-3, tol 1e-7, stencil 6) plus the
+ * GMRES basis size (default 50; each vector is one real field on the device).  tol bounds
+ * max|F(x)| of the real-space residual of updateEquation (pf/implicitEuler.go:68-94). */
+int gopf_set_newton_krylov(gopf_ctx *ctx, int maxiter, double step_size, double tol, int stencil, int restart);
+/* Outcome of the last ImplicitEuler step: Newton iterations, GMRES iterations in total, max|F|,
+ * and whether tol was met (the reference logs a warning and keeps the iterate when it is not,
+ * pf/implicitEuler.go:199-201; so does gopf_step). */
+int gopf_newton_stats(gopf_ctx *ctx, int *newton_iters, int *krylov_iters, double *residual, int *converged);
 /* Field.Data <-> device. data is a []complex128 (interleaved re, im; n complex values).
  * Upload takes the real part; the stepped fields are real. */
 int gopf_field_upload(gopf_ctx *ctx, int field_id, const double *data, size_t n);
