@@ -37,6 +37,11 @@ sys.path.insert(0, HERE)
 
 METRIC = ("CH steps/s at 256³ FP32 vs GPU FP64 (rel-L2≤1e-4); FFT % of HBM peak; sweep steps/s")
 UNIT = "steps/s"
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of each step kernel, from
+# one ncu capture of `python bench.py --steps 10 --warmup 3 --no-cpu-baseline --no-e2e` on a GB300
+# (profiles/launches_ch3d_256_fp32.md).  Bytes that a launch leaves in L2 are not in these counts.
+NCU_TRAFFIC = {"zpass_update": 205.5e6, "xpass_pointwise": 72.8e6, "ypass_forward": 72.1e6,
+               "ypass_inverse": 72.1e6}
 DIMS = [256, 256, 256]
 GAMMA, M, DT, SEED = 0.5, 1.0, 0.05, 1
 CH_EQ = "dconc/dt = M*LAP conc^3 + m1*LAP conc + m1*gamma*LAP^2 conc"
@@ -214,9 +219,13 @@ def run_gpu(args):
     stream = torch.cuda.Stream()
     m.set_stream(stream.cuda_stream)
     m.set_option(G._lib.OPT_CHECK_FINITE, 0)
+    if args.tma is not None:
+        m.set_option(G._lib.OPT_TMA, args.tma)
+    if args.plane is not None:
+        m.set_option(G._lib.OPT_PLANE, args.plane)
     m.upload(0, c0)
     mass0 = m.mass(0)
-    m.step(max(args.warmup, 3))  # warm-up (also captures the CUDA graphs)
+    m.step(warmup_steps(args))  # warm-up: captures both CUDA graphs (1 and 16 steps) before timing
     torch.cuda.synchronize()
 
     # ---- device-resident timed region ----
@@ -259,6 +268,12 @@ def run_gpu(args):
         dist.barrier()
         dist.destroy_process_group()
     return 0
+
+
+def warmup_steps(args) -> int:
+    """At least 3 warm-up steps, and at least one full 16-step graph so that both CUDA graphs
+    (1 and 16 steps) are captured before the timed region."""
+    return max(args.warmup, 3, 17)
 
 
 def run_e2e(args, m, stream, c0, n, world, dist, torch, G):
@@ -308,7 +323,7 @@ def emit(args, m, world, rank, value, per_step_ms, mass0, mass1, finite, prof, d
                    "sample": f"{steps} FP64 Euler steps of the 256^3 grid ({el:.1f} s) on the host cores"}
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": max(args.warmup, 3), "ms_per_step": per_step_ms, "higher_is_better": True, "scaling": "weak",
+            "warmup": warmup_steps(args), "ms_per_step": per_step_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": config({"parallelism": "replicas" if world > 1 else "single GPU",
                               "cell_updates_per_s": value * n,
@@ -317,12 +332,13 @@ def emit(args, m, world, rank, value, per_step_ms, mass0, mass1, finite, prof, d
                               "mass_drift_per_cell": abs(mass1 - mass0) / n, "finite": bool(finite)}),
             "e2e": e2e,
             "roofline": {"bound": "hbm", "kernel": dom["name"], "achieved": achieved, "peak": hbm,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": NCU_TRAFFIC.get(dom["name"]),
                          "per_kernel": [{"name": p["name"], "ms": p["ms"], "GBps": p["bytes"] / p["ms"] / 1e6,
                                          "bytes": p["bytes"]} for p in prof]},
             "cpu_baseline": cpu,
             "clocks": clocks,
-            "gpu_launches": m.kernels_per_step * args.steps,
+            "gpu_launches": m.kernel_launches(args.steps),
         }
         print(json.dumps(out))
     return out
@@ -508,7 +524,7 @@ def run_elastic(args):
     m.set_stream(stream.cuda_stream)
     m.upload(0, c0)
     mass0 = m.mass(0)
-    m.step(max(args.warmup, 3))
+    m.step(warmup_steps(args))
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(0) as clk:
@@ -522,14 +538,14 @@ def run_elastic(args):
     hbm, kind = peaks()
     value = args.steps / (ms / 1000.0)
     out = {"metric": "CH + Khachaturyan elasticity steps/s at 256^3 FP32", "value": value, "unit": "steps/s",
-           "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps,
+           "n_gpus": 1, "steps": args.steps, "warmup": warmup_steps(args), "ms_per_step": ms / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": "ch_elastic_3d_256cube_fp32", "C11": 1.0, "C12": 0.6, "C44": 0.5, "misfit": 0.01,
                       "dt": 0.02, "init": "c0 = 0.3 + U(-0.02, 0.02), seed 3"},
            "step_bytes_algorithmic": step_bytes, "step_fraction_of_hbm": step_bytes * value / 1e9 / hbm,
            "mass_drift_per_cell": abs(m.mass(0) - mass0) / n,
            "per_kernel": [{"name": p["name"], "ms": p["ms"], "GBps": p["bytes"] / p["ms"] / 1e6 if p["ms"] > 0 else 0}
-                          for p in prof], "clocks": clk.summary(), "gpu_launches": m.kernels_per_step * args.steps}
+                          for p in prof], "clocks": clk.summary(), "gpu_launches": m.kernel_launches(args.steps)}
     print(json.dumps(out))
     return 0
 
@@ -608,6 +624,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--grid", type=int, default=256, help="cube side (256 is the benchmark workload)")
     ap.add_argument("--workload", default="ch3d", choices=["ch3d", "sweep", "adjoint", "elastic", "precision"])
+    ap.add_argument("--tma", type=int, default=None, choices=[0, 1, 2],
+                    help="tile movement of the 256-point kernels: 0 plain loads, 1 TMA, 2 TMA + persistent z pass")
+    ap.add_argument("--plane", type=int, default=None, choices=[0, 1],
+                    help="1: depth-plane cluster kernel between consecutive z passes")
     ap.add_argument("--check-steps", type=int, default=0, help="sweep: compare against FP64 after this many steps")
     args = ap.parse_args()
     if args.impl == "reference":

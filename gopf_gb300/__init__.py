@@ -197,6 +197,12 @@ class Model:
         """ImplicitEuler's solver controls (pf/implicitEuler.go:221-228 defaults)."""
         self._ck(self._L.gopf_set_newton_krylov(self._h, maxiter, step_size, tol, stencil, restart))
 
+    def kernel_launches(self, nsteps: int) -> int:
+        """Kernel launches gopf_step(nsteps) makes through the captured graphs."""
+        c = ctypes.c_longlong()
+        self._ck(self._L.gopf_kernel_launches(self._h, int(nsteps), ctypes.byref(c)))
+        return int(c.value)
+
     def newton_stats(self):
         """(Newton iterations, GMRES iterations, max|F|, converged) of the last ImplicitEuler step."""
         a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()

@@ -595,7 +595,10 @@ __global__ void __launch_bounds__(NT, 2)
     const UpdRegs R = load_upd(u, ngrp);
     const float fourpi2 = 39.478417604357434f;
     auto wait_flag = [&](uint64_t *bar, uint32_t parity) {
-        if (tid == 0 && !tma_wait_or_flag(bar, parity, a.status)) *s_ok = 0;
+        if (tid == 0 && !tma_wait_or_flag(bar, parity, a.status)) {
+            *s_ok = 0;
+            bulk_wait_read_all(); // stores in flight finish reading before the block leaves
+        }
         __syncthreads();
         return *s_ok != 0;
     };

@@ -132,7 +132,12 @@ __global__ void k_real_to_double(const R *__restrict__ in, double *__restrict__ 
         out[i] = (double)in[i];
 }
 
-// Final cross-block reduction with Neumaier compensation (one block).
+// Final cross-block reduction (one block of 256 threads, a power of two).
+// Each thread folds a strided share of the block partials with Neumaier
+// compensation; a fixed-order tree then combines the 256 (sum, error) pairs,
+// adding each combination's rounding error to the error terms.  The result
+// is deterministic and the FP64 dependency chain is short (GB300 runs FP64
+// at a small fraction of its FP32 rate).
 __global__ void k_finish_reduce(const double *__restrict__ part, int nblocks, double *__restrict__ out)
 {
     __shared__ double s_sum[256], s_c[256], s_min[256], s_max[256], s_sq[256], s_sqc[256], s_nf[256];
@@ -151,36 +156,51 @@ __global__ void k_finish_reduce(const double *__restrict__ part, int nblocks, do
         mx = fmax(mx, p[RED_MAX]);
         nf += p[RED_NONFINITE];
     }
-    s_sum[threadIdx.x] = sum;
-    s_c[threadIdx.x] = c;
-    s_sq[threadIdx.x] = sq;
-    s_sqc[threadIdx.x] = sqc;
-    s_min[threadIdx.x] = mn;
-    s_max[threadIdx.x] = mx;
-    s_nf[threadIdx.x] = nf;
+    const int t = threadIdx.x;
+    s_sum[t] = sum;
+    s_c[t] = c;
+    s_sq[t] = sq;
+    s_sqc[t] = sqc;
+    s_min[t] = mn;
+    s_max[t] = mx;
+    s_nf[t] = nf;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double S = 0, Cc = 0, Q = 0, Qc = 0, MN = INFINITY, MX = -INFINITY, NF = 0;
-        for (int i = 0; i < (int)blockDim.x; ++i) {
-            double v = s_sum[i], t = S + v;
-            Cc += (fabs(S) >= fabs(v)) ? (S - t) + v : (v - t) + S;
-            S = t;
-            Cc += s_c[i];
-            v = s_sq[i];
-            t = Q + v;
-            Qc += (fabs(Q) >= fabs(v)) ? (Q - t) + v : (v - t) + Q;
-            Q = t;
-            Qc += s_sqc[i];
-            MN = fmin(MN, s_min[i]);
-            MX = fmax(MX, s_max[i]);
-            NF += s_nf[i];
+    for (int w = (int)blockDim.x / 2; w > 0; w >>= 1) {
+        if (t < w) {
+            const int o = t + w;
+            double a = s_sum[t], b = s_sum[o], r = a + b;
+            s_c[t] += s_c[o] + ((fabs(a) >= fabs(b)) ? (a - r) + b : (b - r) + a);
+            s_sum[t] = r;
+            a = s_sq[t];
+            b = s_sq[o];
+            r = a + b;
+            s_sqc[t] += s_sqc[o] + ((fabs(a) >= fabs(b)) ? (a - r) + b : (b - r) + a);
+            s_sq[t] = r;
+            s_min[t] = fmin(s_min[t], s_min[o]);
+            s_max[t] = fmax(s_max[t], s_max[o]);
+            s_nf[t] += s_nf[o];
         }
-        out[RED_SUM] = S + Cc;
-        out[RED_SUMSQ] = Q + Qc;
-        out[RED_MIN] = MN;
-        out[RED_MAX] = MX;
-        out[RED_NONFINITE] = NF;
+        __syncthreads();
     }
+    if (t == 0) {
+        out[RED_SUM] = s_sum[0] + s_c[0];
+        out[RED_SUMSQ] = s_sq[0] + s_sqc[0];
+        out[RED_MIN] = s_min[0];
+        out[RED_MAX] = s_max[0];
+        out[RED_NONFINITE] = s_nf[0];
+    }
+}
+
+// Number of non-finite values among n reals.  A non-finite cell makes every
+// coefficient of the spectrum non-finite and vice versa, so counting over the
+// spectral state answers "is the field finite" without a transform.
+template <typename R> __global__ void k_count_nonfinite(const R *__restrict__ x, long long n, unsigned *__restrict__ count)
+{
+    unsigned local = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        local += isfinite(x[i]) ? 0u : 1u;
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
 }
 
 static unsigned ew_blocks(long long n)
@@ -223,8 +243,8 @@ template <typename R> static int ctx_alloc(gopf_ctx *ctx)
     ctx->nred_blocks = ((g.Y + ctx->LBx - 1) / ctx->LBx) * g.Z;
     CK(cudaMalloc(&ctx->d_red, sizeof(double) * RED_SLOTS * ctx->nred_blocks));
     CK(cudaMalloc(&ctx->d_redout, sizeof(double) * RED_SLOTS));
-    CK(cudaMalloc(&ctx->d_status, sizeof(unsigned)));
-    CK(cudaMemset(ctx->d_status, 0, sizeof(unsigned)));
+    CK(cudaMalloc(&ctx->d_status, 2 * sizeof(unsigned))); // [0] status word, [1] non-finite count
+    CK(cudaMemset(ctx->d_status, 0, 2 * sizeof(unsigned)));
     ctx->dev_bytes += sizeof(double) * RED_SLOTS * (ctx->nred_blocks + 1) + sizeof(unsigned);
     CK(cudaMemset(ctx->d_state, 0, sizeof(V) * g.C));
     CK(cudaMemset(ctx->d_T, 0, sizeof(V) * g.C));
@@ -347,6 +367,7 @@ extern "C" int gopf_set_option(gopf_ctx *ctx, int opt, long long v)
     if (opt == GOPF_OPT_CHECK_FINITE) ctx->check_finite = (int)(v != 0);
     else if (opt == GOPF_OPT_USE_GRAPHS) ctx->use_graphs = (int)(v != 0);
     else if (opt == GOPF_OPT_FAST_KERNELS) ctx->use_fast = (int)(v != 0);
+    else if (opt == GOPF_OPT_PLANE) ctx->use_plane = (int)(v != 0);
     else if (opt == GOPF_OPT_TMA) ctx->use_tma = (int)std::min<long long>(std::max<long long>(v, 0), 2);
     else return gopf_fail(ctx, GOPF_ERR_ARG, "unknown option");
     invalidate_graphs(ctx); // captured launches carry the old choice
@@ -764,9 +785,22 @@ template <typename R> static cudaError_t enqueue_load_state(gopf_ctx *ctx)
 //   last axis   : forward, c-hat <- (c-hat + dt sum_b m^lap_b U_b)/(1 - dt L(m)), T <- inverse(c-hat/N)
 // The elastic part runs from the second step on: the reference's h-field is
 // zero until the first OnStepFinished (pf/homoLinElast.go:130-145).
-template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx)
+// Steps of a run of consecutive Euler steps may hand the work array from one to
+// the next still y-spectral: the depth-plane kernel then does the inverse y
+// pass of one step together with the x pass and the forward y pass of the
+// next.  Only the last step of a run restores T to its usual form.
+static bool plane_path(const gopf_ctx *ctx)
+{
+    return ctx->use_plane && ctx->use_fast && ctx->use_tma && ctx->prec == GOPF_FP32 && plane256_supported(ctx->g) &&
+           ctx->stepper == GOPF_STEPPER_EULER && !ctx->has_elastic && !ctx->has_volcons && ctx->ngroups == 1;
+}
+
+template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx, bool first = true, bool last = true)
 {
     typedef typename VecOf<R>::type V;
+    const bool plane = plane_path(ctx);
+    const bool from_plane = plane && !first; // T arrives y-spectral from the previous step
+    const bool to_plane = plane && !last;    // T leaves y-spectral for the next step
     const bool el = ctx->has_elastic && ctx->el_primed;
     const int G = ctx->ngroups;
     const int GE = G + (el ? 1 : 0); // groups entering the update
@@ -785,7 +819,17 @@ template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx)
         u.gscale[G] = nullptr;
     }
     const bool is3d = ctx->g.Z > 1;
-    if (GE > 0) {
+    if (from_plane) {
+        if constexpr (sizeof(R) == 4) {
+            XPassArgs<R> xa = xargs<R>(ctx);
+            xa.in_mode = XIN_SPECTRAL;
+            xa.in = T;
+            xa.out[0] = U[0];
+            xa.ngrp_out = 1;
+            xa.pw = ctx->pw;
+            LK(launch_plane256(xa, ctx->stream));
+        }
+    } else if (GE > 0) {
         XPassArgs<R> xa = xargs<R>(ctx);
         xa.in_mode = XIN_SPECTRAL;
         xa.in = T;
@@ -839,7 +883,7 @@ template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx)
             pa.nbuf = 1;
             LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
         }
-    } else if (is3d && GE > 0) {
+    } else if (is3d && GE > 0 && !from_plane) {
         PassArgs<R> pa = pargs<R>(ctx, false);
         pa.mode = PM_FWD;
         for (int b = 0; b < GE; ++b) pa.buf[b] = U[b];
@@ -857,7 +901,7 @@ template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx)
     fa.upd = u;
     LK(is3d ? launch_spass<R>(fa, ctx->LBz, ctx->stream) : launch_cpass<R>(fa, ctx->LBy, ctx->stream));
     LK(gopf_launch_hermitian_planes(ctx, ctx->d_state));
-    if (is3d) {
+    if (is3d && !to_plane) {
         PassArgs<R> ia = pargs<R>(ctx, false);
         ia.mode = PM_INV;
         ia.buf[0] = T;
@@ -931,7 +975,8 @@ template <typename R> static cudaError_t enqueue_rk4(gopf_ctx *ctx)
 
 template <typename R> static cudaError_t enqueue_steps(gopf_ctx *ctx, int n)
 {
-    for (int i = 0; i < n; ++i) LK(ctx->stepper == GOPF_STEPPER_RK4 ? enqueue_rk4<R>(ctx) : enqueue_euler<R>(ctx));
+    for (int i = 0; i < n; ++i)
+        LK(ctx->stepper == GOPF_STEPPER_RK4 ? enqueue_rk4<R>(ctx) : enqueue_euler<R>(ctx, i == 0, i == n - 1));
     return cudaSuccess;
 }
 
@@ -948,6 +993,17 @@ static int capture_graph(gopf_ctx *ctx, int nsteps, cudaGraphExec_t *exec)
     cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &graph);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "capture");
     if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "cudaStreamEndCapture");
+    // count the kernel nodes: the number of launches one replay makes
+    size_t nn = 0, nk = 0;
+    if (cudaGraphGetNodes(graph, nullptr, &nn) == cudaSuccess && nn > 0) {
+        std::vector<cudaGraphNode_t> nodes(nn);
+        if (cudaGraphGetNodes(graph, nodes.data(), &nn) == cudaSuccess)
+            for (size_t i = 0; i < nn; ++i) {
+                cudaGraphNodeType t;
+                if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++nk;
+            }
+    }
+    (nsteps == 1 ? ctx->graph_kernels1 : ctx->graph_kernelsK) = (long long)nk;
     e = cudaGraphInstantiate(exec, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
@@ -1059,6 +1115,25 @@ static int reduce_all(gopf_ctx *ctx, double *host5)
     return GOPF_OK;
 }
 
+// Non-finite values in the state (stream-synchronising); GOPF_ERR_NAN when there are any.
+static int check_finite_state(gopf_ctx *ctx)
+{
+    unsigned *cnt = ctx->d_status + 1;
+    CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned), ctx->stream));
+    const long long nr = 2 * ctx->g.C;
+    const unsigned blocks = (unsigned)std::min<long long>((nr + 255) / 256, 152 * 8);
+    if (ctx->prec == GOPF_FP32) k_count_nonfinite<float><<<blocks, 256, 0, ctx->stream>>>((const float *)ctx->d_state, nr, cnt);
+    else k_count_nonfinite<double><<<blocks, 256, 0, ctx->stream>>>((const double *)ctx->d_state, nr, cnt);
+    CK(cudaGetLastError());
+    unsigned h = 0;
+    CK(cudaMemcpyAsync(&h, cnt, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (h)
+        return gopf_fail(ctx, GOPF_ERR_NAN, "field contains non-finite values after step " + std::to_string(ctx->step) +
+                                                " (" + std::to_string(h) + " non-finite spectral components)");
+    return GOPF_OK;
+}
+
 extern "C" int gopf_reduce(gopf_ctx *ctx, int field, int what, double *out)
 {
     if (!ctx || !out) return gopf_fail(ctx, GOPF_ERR_ARG, "null argument");
@@ -1103,11 +1178,7 @@ extern "C" int gopf_step(gopf_ctx *ctx, long long nsteps)
         }
         if (ctx->check_finite) {
             if ((rc = check_device_status(ctx))) return rc;
-            double r[5];
-            if ((rc = reduce_all(ctx, r))) return rc;
-            if (r[RED_NONFINITE] > 0)
-                return gopf_fail(ctx, GOPF_ERR_NAN, "field contains non-finite values after step " +
-                                                        std::to_string(ctx->step));
+            if ((rc = check_finite_state(ctx))) return rc;
         }
         return GOPF_OK;
     }
@@ -1138,11 +1209,7 @@ extern "C" int gopf_step(gopf_ctx *ctx, long long nsteps)
     ctx->step += nsteps;
     if (ctx->check_finite) {
         if ((rc = check_device_status(ctx))) return rc;
-        double r[5];
-        if ((rc = reduce_all(ctx, r))) return rc;
-        if (r[RED_NONFINITE] > 0)
-            return gopf_fail(ctx, GOPF_ERR_NAN, "field contains " + std::to_string((long long)r[RED_NONFINITE]) +
-                                                    " non-finite values after step " + std::to_string(ctx->step));
+        if ((rc = check_finite_state(ctx))) return rc;
     }
     return GOPF_OK;
 }
@@ -1385,6 +1452,17 @@ extern "C" int gopf_device_bytes(gopf_ctx *ctx, size_t *bytes)
 
 static void step_slots(gopf_ctx *ctx, std::vector<std::string> &names, std::vector<double> &bytes);
 
+extern "C" int gopf_kernel_launches(gopf_ctx *ctx, long long nsteps, long long *count)
+{
+    if (!ctx || !count || nsteps < 0) return GOPF_ERR_ARG;
+    if (ctx->use_graphs && ctx->stepper != GOPF_STEPPER_IMPLICIT_EULER && ctx->graph_kernels1 > 0 &&
+        (nsteps < ctx->graphK || ctx->graph_kernelsK > 0)) {
+        *count = (nsteps / ctx->graphK) * ctx->graph_kernelsK + (nsteps % ctx->graphK) * ctx->graph_kernels1;
+        return GOPF_OK;
+    }
+    return gopf_fail(ctx, GOPF_ERR_STATE, "launch counts are known for graph-replayed steps after the graphs exist");
+}
+
 extern "C" int gopf_kernels_per_step(gopf_ctx *ctx, int *n)
 {
     if (!ctx || !n) return GOPF_ERR_ARG;
@@ -1416,6 +1494,12 @@ static void step_slots(gopf_ctx *ctx, std::vector<std::string> &names, std::vect
         names.push_back(n);
         bytes.push_back(b);
     };
+    if (plane_path(ctx)) { // a step inside a run: y inverse + x + y forward per plane, then z
+        add("plane_yinv_x_yfwd", 2.0 * C);
+        add("zpass_update", 4.0 * C);
+        add("hermitian_planes", 4.0 * C / ctx->g.KX);
+        return;
+    }
     if (GE > 0) add("xpass_pointwise", (1.0 + GE) * C);
     if (ctx->has_volcons) add("volcons_multiplier", 0.0);
     if (el) {
@@ -1449,13 +1533,27 @@ extern "C" int gopf_profile_step(gopf_ctx *ctx, int nsteps, double *avg_ms, doub
     std::vector<cudaEvent_t> ev(1 + ns * nsteps);
     for (auto &e : ev) CK(cudaEventCreate(&e));
     std::vector<double> acc(ns, 0.0);
+    const bool plane = plane_path(ctx);
+    cudaError_t e = cudaSuccess;
+    // inside a run of steps (plane path) the profiled steps are preceded by the run's first step
+    if (plane) e = (ctx->prec == GOPF_FP32) ? enqueue_euler<float>(ctx, true, false) : enqueue_euler<double>(ctx, true, false);
     CK(cudaEventRecord(ev[0], ctx->stream));
     ctx->prof_events = &ev;
     ctx->prof_next = 1;
-    cudaError_t e = cudaSuccess;
     for (int s = 0; s < nsteps && e == cudaSuccess; ++s)
-        e = (ctx->prec == GOPF_FP32) ? enqueue_euler<float>(ctx) : enqueue_euler<double>(ctx);
+        e = (ctx->prec == GOPF_FP32) ? enqueue_euler<float>(ctx, !plane, !plane)
+                                     : enqueue_euler<double>(ctx, !plane, !plane);
     ctx->prof_events = nullptr;
+    // ... and followed by the run's closing inverse y pass
+    if (plane && e == cudaSuccess) {
+        if (ctx->prec == GOPF_FP32) {
+            PassArgs<float> ia = pargs<float>(ctx, false);
+            ia.mode = PM_INV;
+            ia.buf[0] = (float2 *)ctx->d_T;
+            ia.nbuf = 1;
+            e = launch_cpass<float>(ia, ctx->LBy, ctx->stream);
+        }
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e == cudaSuccess && ctx->prof_next != ev.size()) e = cudaErrorInvalidValue;
     if (e == cudaSuccess) {
@@ -1465,7 +1563,7 @@ extern "C" int gopf_profile_step(gopf_ctx *ctx, int nsteps, double *avg_ms, doub
                 cudaEventElapsedTime(&ms, ev[s * ns + k], ev[s * ns + k + 1]);
                 acc[k] += ms;
             }
-        ctx->step += nsteps;
+        ctx->step += nsteps + (plane ? 1 : 0);
     }
     for (auto &x : ev) cudaEventDestroy(x);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "profile");

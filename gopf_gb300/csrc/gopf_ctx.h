@@ -104,6 +104,7 @@ struct gopf_ctx {
     cudaGraphExec_t gexec1 = nullptr;
     cudaGraphExec_t gexecK = nullptr;
     int graphK = 16;
+    long long graph_kernels1 = 0, graph_kernelsK = 0; // kernel nodes of the two graphs
     bool graphs_dirty = true;
 
     // Khachaturyan term (at most one per context)
@@ -140,6 +141,7 @@ struct gopf_ctx {
     int use_graphs = 1;
     int use_fast = 1;
     int use_tma = 1;
+    int use_plane = 0;
 
     // ImplicitEuler's Newton-Krylov controls (DefaultNonLinSolver, pf/implicitEuler.go:221-228) and
     // the outcome of the last step

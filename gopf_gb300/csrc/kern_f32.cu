@@ -4,9 +4,26 @@
 #include <mutex>
 
 #include "fast256.cuh"
+#include "plane256.cuh"
 #include "gopf_kernels_impl.cuh"
 
 namespace gopf {
+
+bool plane256_supported(const Geom &g) { return g.X == 256 && g.Y == 256 && g.KX == 129 && g.Z > 1; }
+
+cudaError_t launch_plane256(const XPassArgs<float> &a, cudaStream_t st)
+{
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+        attr_err = cudaFuncSetAttribute(f256::k_plane256, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        f256::plane256_smem_bytes());
+    });
+    if (attr_err != cudaSuccess) return attr_err;
+    if (!plane256_supported(a.g) || a.ngrp_out != 1 || a.program != XP_POLY) return cudaErrorInvalidValue;
+    f256::k_plane256<<<(unsigned)(a.g.Z * f256::PL_CLUSTER), f256::NT, f256::plane256_smem_bytes(), st>>>(a);
+    return cudaGetLastError();
+}
 
 // [Z][S] view of a z-pass array with 16 x 256 boxes
 static bool z_map(CUtensorMap *m, const float2 *p, const Geom &g)

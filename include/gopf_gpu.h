@@ -89,8 +89,10 @@ enum {
     GOPF_OPT_CHECK_FINITE = 0, /* 1 (default): gopf_step synchronises and checks the field for NaN/Inf */
     GOPF_OPT_USE_GRAPHS = 1,   /* 1 (default): steps are replayed from captured CUDA graphs */
     GOPF_OPT_FAST_KERNELS = 2, /* 1 (default): register-resident kernels serve the lengths they cover */
-    GOPF_OPT_TMA = 3           /* those kernels move their tiles with TMA tensor copies: 0 no, 1 one tile
+    GOPF_OPT_TMA = 3,          /* those kernels move their tiles with TMA tensor copies: 0 no, 1 one tile
                                   per block (default), 2 also the persistent double-buffered z pass */
+    GOPF_OPT_PLANE = 4,        /* 1: consecutive FP32 Euler steps on 256 x 256 x Z grids do the inverse y,
+                                  x and forward y passes of each depth plane in one cluster launch */
 };
 
 #define GOPF_MAX_FACTORS 8
@@ -239,6 +241,9 @@ const char *gopf_noalloc_last_error(void);
 /* Bytes of device memory held by the context. */
 int gopf_device_bytes(gopf_ctx *ctx, size_t *bytes);
 /* Number of kernel launches enqueued by one step of the current stepper. */
+/* Kernel launches that gopf_step(ctx, nsteps) makes through its captured graphs (known once both
+ * graphs exist, i.e. after a gopf_step of at least 16 steps).  No counterpart in the reference. */
+int gopf_kernel_launches(gopf_ctx *ctx, long long nsteps, long long *count);
 int gopf_kernels_per_step(gopf_ctx *ctx, int *n);
 /* Run nsteps Euler steps launch by launch with CUDA events between kernels on the
  * context's stream; per kernel slot of one step write the average device time (ms)
