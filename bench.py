@@ -550,6 +550,60 @@ def run_elastic(args):
     return 0
 
 
+def run_c1(args):
+    """2D Cahn-Hilliard 128^2 (gamma = 1, M = 1, dt = 0.1, c0 = 0.5 + U(-0.05, 0.05) seed 0), 1000 steps:
+    FP64 and FP32 device steps/s (graph replays; the grid is L2-resident, so this is launch- and
+    latency-bound, not an HBM roofline case), rel-L2 of both against the committed FP64 oracle
+    fixture tests/golden/ch2d_128.npz, and the FP64 CPU oracle's steps/s on the host cores."""
+    import torch
+
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+    from oracle import oracle as O
+
+    dims, n, steps = [128, 128], 128 * 128, 1000
+    c0 = uniform_field(0, n, 0.5, 0.05)
+    ref = np.load(os.path.join(HERE, "tests", "golden", "ch2d_128.npz"))["field"]
+
+    def run(prec):
+        m = G.Model(dims, prec, device=0)
+        m.set_option(G._lib.OPT_CHECK_FINITE, 0)
+        m.add_field("conc")
+        m.add_scalar("gamma", 1.0)
+        m.add_scalar("M", 1.0)
+        m.add_scalar("m1", -1.0)
+        m.add_equation(CH_EQ)
+        m.init()
+        m.set_stepper("euler", 0.1)
+        m.upload(0, c0)
+        m.step(warmup_steps(args))
+        m.upload(0, c0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m.step(steps)
+        m.synchronize()
+        rate = steps / (time.perf_counter() - t0)
+        err = float(np.linalg.norm(m.download_real(0) - ref) / np.linalg.norm(ref))
+        return rate, err
+
+    r64, e64 = run("fp64")
+    r32, e32 = run("fp32")
+    O.build()
+    o = O.cahn_hilliard(dims, gamma=1.0, M=1.0)
+    o.set_field(0, c0)
+    t0 = time.perf_counter()
+    o.step_euler(0.1, steps)
+    cpu = steps / (time.perf_counter() - t0)
+    out = {"metric": "2D CH 128^2 steps/s (1000 steps) and rel-L2 vs the FP64 oracle fixture",
+           "workload": "cahn_hilliard_2d_128_gamma1_dt0.1", "fp64_steps_per_s": r64, "fp64_rel_l2": e64,
+           "fp32_steps_per_s": r32, "fp32_rel_l2": e32,
+           "cpu_baseline": {"value": cpu, "unit": "steps/s", "cores": O.num_threads(), "kind": "port",
+                            "sample": "the same 1000 FP64 Euler steps on the host cores"},
+           "note": "16k cells: L2-resident, launch/latency-bound"}
+    print(json.dumps(out))
+    return 0
+
+
 def run_precision(args):
     """3D CH 256^3: FP64 device mode steps/s, FP64 device vs the FP64 oracle at full size (few steps),
     FP32 vs FP64 device rel-L2 and mass drift after --check-steps steps."""
@@ -623,7 +677,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--grid", type=int, default=256, help="cube side (256 is the benchmark workload)")
-    ap.add_argument("--workload", default="ch3d", choices=["ch3d", "sweep", "adjoint", "elastic", "precision"])
+    ap.add_argument("--workload", default="ch3d", choices=["ch3d", "sweep", "adjoint", "elastic", "precision", "c1"])
     ap.add_argument("--tma", type=int, default=None, choices=[0, 1, 2],
                     help="tile movement of the 256-point kernels: 0 plain loads, 1 TMA, 2 TMA + persistent z pass")
     ap.add_argument("--plane", type=int, default=None, choices=[0, 1],
@@ -640,6 +694,8 @@ def main():
         return run_elastic(args)
     if args.workload == "precision":
         return run_precision(args)
+    if args.workload == "c1":
+        return run_c1(args)
     return run_gpu(args)
 
 

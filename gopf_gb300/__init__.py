@@ -47,6 +47,15 @@ class GopfError(RuntimeError):
         self.message = message
 
 
+def vandeven(order: int) -> np.ndarray:
+    """NewVandeven(order).Data (pf/vandeven.go:13-27), computed by the library."""
+    out = np.empty(1000)
+    rc = load().gopf_vandeven_table(int(order), _dptr(out), 1000)
+    if rc != 0:
+        raise GopfError(rc, "bad Vandeven order")
+    return out
+
+
 def load():
     return _lib.load()
 
@@ -191,6 +200,14 @@ class Model:
     # ---- pf.TimeStepper mirror ----
     def set_stepper(self, name: str, dt: float) -> None:
         self._ck(self._L.gopf_set_stepper(self._h, _STEPPERS[name], dt))
+
+    def set_modal_filter(self, table) -> None:
+        """Euler/RK4 SetFilter with a tabulated filter on [0, 1] (None removes it)."""
+        if table is None:
+            self._ck(self._L.gopf_set_modal_filter(self._h, None, 0))
+            return
+        t = np.ascontiguousarray(table, dtype=np.float64)
+        self._ck(self._L.gopf_set_modal_filter(self._h, _dptr(t), t.size))
 
     def set_newton_krylov(self, maxiter: int = 50, step_size: float = 1e-3, tol: float = 1e-7, stencil: int = 6,
                           restart: int = 50) -> None:

@@ -99,6 +99,8 @@ SIGNATURES = {
     "gopf_adjoint_release": ([_vp], _i),
     "gopf_reduce_noalloc": ([_vp, _sz, _dp, _vp], _i),
     "gopf_noalloc_last_error": ([], _cp),
+    "gopf_set_modal_filter": ([_vp, _dp, _i], _i),
+    "gopf_vandeven_table": ([_i, _dp, _i], _i),
     "gopf_kernel_launches": ([_vp, _ll, ctypes.POINTER(ctypes.c_longlong)], _i),
     "gopf_set_newton_krylov": ([_vp, _i, ctypes.c_double, ctypes.c_double, _i, _i], _i),
     "gopf_newton_stats": ([_vp, _ip, _ip, _dp, _ip], _i),

@@ -26,12 +26,61 @@ constexpr int N = 256;
 constexpr int R = 16;
 constexpr int NT = 256; // threads per block: 16 lines x 16 radix positions
 
+// ---------------------------------------------------------------------------
+// Radix-16 on packed FP32x2 (Blackwell's two-lane FADD2/FFMA2): a complex
+// add or subtract is one instruction.  Each lane rounds once, exactly as the
+// scalar code does, so the results are bitwise those of dft16 in fft_core.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+
+// a -/+ i d (forward: a - i d = (a.x + d.y, a.y - d.x); inverse: a + i d), with the swapped pair of d
+template <bool INV> __device__ __forceinline__ float2 pmi_add(float2 a, float2 d)
+{
+    const float2 sw = make_float2(d.y, d.x);
+    return __ffma2_rn(sw, INV ? make_float2(-1.f, 1.f) : make_float2(1.f, -1.f), a);
+}
+
+template <bool INV> __device__ __forceinline__ void pdft4(float2 &v0, float2 &v1, float2 &v2, float2 &v3)
+{
+    const float2 a0 = padd(v0, v2), a1 = psub(v0, v2);
+    const float2 a2 = padd(v1, v3), d = psub(v1, v3);
+    v0 = padd(a0, a2);
+    v2 = psub(a0, a2);
+    v1 = pmi_add<INV>(a1, d);
+    v3 = pmi_add<!INV>(a1, d);
+}
+
+template <bool INV> __device__ __forceinline__ void pdft16(float2 (&v)[16])
+{
+#pragma unroll
+    for (int n1 = 0; n1 < 4; ++n1) pdft4<INV>(v[n1], v[4 + n1], v[8 + n1], v[12 + n1]);
+    v[5] = tw16<1, INV>(v[5]);
+    v[6] = tw16<2, INV>(v[6]);
+    v[7] = tw16<3, INV>(v[7]);
+    v[9] = tw16<2, INV>(v[9]);
+    v[10] = tw16<4, INV>(v[10]);
+    v[11] = tw16<6, INV>(v[11]);
+    v[13] = tw16<3, INV>(v[13]);
+    v[14] = tw16<6, INV>(v[14]);
+    v[15] = tw16<9, INV>(v[15]);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) pdft4<INV>(v[4 * k1 + 0], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
+    float2 t[16];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+        for (int k2 = 0; k2 < 4; ++k2) t[k1 + 4 * k2] = v[4 * k1 + k2];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = t[i];
+}
+
 // 256-point FFT of the thread's v[i] = x[r + 16 i]; result v[i] = X[r + 16 i].
 // at(a, b) is the shared-memory slot of element (a, b) of this thread's line.
 template <bool INV, typename AT>
 __device__ __forceinline__ void fft256(float2 (&v)[16], int r, const float2 *__restrict__ tw, AT &&at)
 {
-    dft16<INV>(v);
+    pdft16<INV>(v);
 #pragma unroll
     for (int k1 = 1; k1 < 16; ++k1) {
         const float2 w = tw[k1 * 16 + r]; // W256^(r k1), laid out [k1][r]: conflict free
@@ -42,7 +91,7 @@ __device__ __forceinline__ void fft256(float2 (&v)[16], int r, const float2 *__r
     __syncthreads();
 #pragma unroll
     for (int n2 = 0; n2 < 16; ++n2) v[n2] = at(n2, r);
-    dft16<INV>(v);
+    pdft16<INV>(v);
     __syncthreads(); // slots may be reused after return
 }
 
@@ -59,8 +108,9 @@ __device__ __forceinline__ float fsqf(int i, int n)
     return f * f;
 }
 
-// Kernels with the update take NZ: true only for models with a noise term, so
-// the Philox/Box-Muller code is not carried by the noise-free instantiations.
+// Kernels with the update take NZ: true only for models with a noise term or a
+// modal filter, so the Philox/Box-Muller and filter code is not carried by the
+// plain instantiations.
 
 // k-space update coefficients staged in registers once per thread
 struct UpdRegs {
@@ -104,6 +154,34 @@ __device__ __forceinline__ float mkpow(float mk, int p)
     }
 }
 
+// ApplyModalFilter (pf/util.go:125-132) with the Vandeven.Eval interpolation (pf/vandeven.go:30-40):
+// c * filter(2|f|/pi), |f|^2 = f2 in cycles per sample
+__device__ __forceinline__ float2 modal_filter(const UpdTable &u, float2 c, float f2)
+{
+    const float *__restrict__ tab = static_cast<const float *>(u.filt);
+    const int n = u.nfilt;
+    const float x = sqrtf(f2) * 0.636619772367581343f;
+    const float nn = (float)(n - 1);
+    const int idx = (int)(x * nn);
+    float s;
+    if (idx >= n - 1) {
+        s = tab[n - 1];
+    } else {
+        const float dx = 1.f / nn;
+        s = tab[idx] + (x - (float)idx * dx) * (tab[idx + 1] - tab[idx]) / dx;
+    }
+    return make_float2(c.x * s, c.y * s);
+}
+
+// 1/d from the hardware reciprocal estimate refined by one Newton step (error well below
+// an FP32 ulp before the final rounding; d is near 1 here, never denormal)
+__device__ __forceinline__ float recip_nr(float d)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(d));
+    return r * (2.f - d * r);
+}
+
 // k-space update of one element (pf/euler.go:32-34 with the term algebra of pf/rhsBuilder.go):
 // c <- (c + dt sum_b s_b m^p_b U_b) / (1 - dt L(m)),  m = -k^2
 __device__ __forceinline__ float2 euler_update(const UpdRegs &R, const UpdTable &u, float2 c0, float2 U0, float2 U1,
@@ -124,7 +202,7 @@ __device__ __forceinline__ float2 euler_update(const UpdRegs &R, const UpdTable 
         L = 0.f;
         for (int q = u.nimp - 1; q >= 0; --q) L = L * mk + (float)u.imp[q];
     }
-    const float rden = 1.f / (1.f - R.dt * L);
+    const float rden = recip_nr(1.f - R.dt * L);
     return make_float2((c0.x + R.dt * nh.x) * rden, (c0.y + R.dt * nh.y) * rden);
 }
 
@@ -192,6 +270,7 @@ __global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_z256_fused(const PassAr
                 c0.y += R.dt * (float)ni;
             }
             cn = euler_update(R, u, c0, v[i], (NG > 1) ? w[NG > 1 ? i : 0] : v[i], mk);
+            if (NZ && u.filt) cn = modal_filter(u, cn, fl + s_fz[k]);
         }
         state[gi] = cn;
         v[i] = make_float2(cn.x * R.invN, cn.y * R.invN);
@@ -301,6 +380,7 @@ __global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2)
                 c0.y += R.dt * (float)ni;
             }
             cn = euler_update(R, u, c0, v[i], (NG > 1) ? w[NG > 1 ? i : 0] : v[i], mk);
+            if (NZ && u.filt) cn = modal_filter(u, cn, fl + s_fz[k]);
         }
         tS[k * 16 + l] = cn; // each thread rewrites exactly the elements it read
         v[i] = make_float2(cn.x * R.invN, cn.y * R.invN);
@@ -403,6 +483,7 @@ __global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_y256(const PassArgs<flo
                     c0.y += R.dt * (float)ni;
                 }
                 cn = euler_update(R, u, c0, v[i], (NG > 1) ? w[NG > 1 ? i : 0] : v[i], mk);
+                if (NZ && u.filt) cn = modal_filter(u, cn, fl + s_fy[k]);
             }
             state[gi] = cn;
         }
@@ -647,6 +728,7 @@ __global__ void __launch_bounds__(NT, 2)
                     c0.y += R.dt * (float)ni;
                 }
                 cn = euler_update(R, u, c0, v[i], v[i], mk);
+                if (NZ && u.filt) cn = modal_filter(u, cn, fl + s_fz[k]);
             }
             tS[k * 16 + l] = cn;
             v[i] = make_float2(cn.x * R.invN, cn.y * R.invN);

@@ -269,7 +269,8 @@ static void ctx_free(gopf_ctx *ctx)
         if (p) cudaFree(p);
     for (int i = 1; i < GOPF_MAX_GROUPS; ++i)
         if (ctx->d_U[i]) cudaFree(ctx->d_U[i]);
-    void *more[] = {ctx->d_bsym, ctx->d_U0, ctx->d_UH, ctx->d_vc, ctx->d_red2, ctx->d_rkF, ctx->d_stepctr, ctx->d_status};
+    void *more[] = {ctx->d_bsym, ctx->d_U0, ctx->d_UH, ctx->d_vc, ctx->d_red2, ctx->d_rkF, ctx->d_stepctr, ctx->d_status,
+                    ctx->d_filter};
     for (void *p : more)
         if (p) cudaFree(p);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -585,6 +586,8 @@ int gopf_compile_model(gopf_ctx *ctx)
     u.noise = noise;
     ctx->noise = noise;
     ctx->pw = pw;
+    u.filt = ctx->upd.nfilt ? ctx->d_filter : nullptr; // a filter set earlier survives a re-init
+    u.nfilt = ctx->upd.nfilt;
     ctx->upd = u;
     ctx->ngroups = u.ngrp;
     // the elastic step's x-pass also emits H(c) = 3c^2 - 2c^3 as an extra group
@@ -722,7 +725,7 @@ static void prof_mark(gopf_ctx *ctx)
     } while (0)
 
 // From T (after the inverse y/z passes) produce real rows and/or reductions.
-template <typename R> static cudaError_t enqueue_xpass_out(gopf_ctx *ctx, R *rout, double *red)
+template <typename R> static XPassArgs<R> xargs_out(gopf_ctx *ctx, R *rout, double *red)
 {
     XPassArgs<R> xa = xargs<R>(ctx);
     xa.in_mode = XIN_SPECTRAL;
@@ -730,7 +733,12 @@ template <typename R> static cudaError_t enqueue_xpass_out(gopf_ctx *ctx, R *rou
     xa.rout = rout;
     xa.red = red;
     xa.ngrp_out = 0;
-    return launch_xpass<R>(xa, ctx->LBx, ctx->stream);
+    return xa;
+}
+
+template <typename R> static cudaError_t enqueue_xpass_out(gopf_ctx *ctx, R *rout, double *red)
+{
+    return launch_xpass<R>(xargs_out<R>(ctx, rout, red), ctx->LBx, ctx->stream);
 }
 
 // Load real field d_real into the state: c-hat = FFT(c), T = partial inverse of c-hat/N.
@@ -1108,7 +1116,10 @@ static int reduce_all(gopf_ctx *ctx, double *host5)
     cudaError_t e = (ctx->prec == GOPF_FP32) ? enqueue_xpass_out<float>(ctx, nullptr, ctx->d_red)
                                              : enqueue_xpass_out<double>(ctx, nullptr, ctx->d_red);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "reduction pass");
-    k_finish_reduce<<<1, 256, 0, ctx->stream>>>(ctx->d_red, ctx->nred_blocks, ctx->d_redout);
+    const int nb = (ctx->prec == GOPF_FP32) ? xpass_red_blocks<float>(xargs_out<float>(ctx, nullptr, ctx->d_red), ctx->LBx)
+                                            : xpass_red_blocks<double>(xargs_out<double>(ctx, nullptr, ctx->d_red), ctx->LBx);
+    if (nb > ctx->nred_blocks) return gopf_fail(ctx, GOPF_ERR_STATE, "reduction partials exceed their buffer");
+    k_finish_reduce<<<1, 256, 0, ctx->stream>>>(ctx->d_red, nb, ctx->d_redout);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(host5, ctx->d_redout, sizeof(double) * 5, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -1278,6 +1289,7 @@ template <typename R> static cudaError_t enqueue_ie_rhs(gopf_ctx *ctx, void *npr
     fa.upd.dt = ctx->dt;
     fa.upd.invN = 1.0 / (double)ctx->g.N;
     fa.upd.etd = 1;
+    fa.upd.filt = nullptr; // ImplicitEuler ignores filters (pf/implicitEuler.go:209-213)
     fa.rkF = (V *)nprev;
     LK(is3d ? launch_spass<R>(fa, ctx->LBz, ctx->stream) : launch_cpass<R>(fa, ctx->LBy, ctx->stream));
     return cudaSuccess;
@@ -1326,6 +1338,7 @@ static cudaError_t enqueue_ie_residual(gopf_ctx *ctx, const R *x, R *F, const vo
     fa.upd.dt = ctx->dt;
     fa.upd.invN = 1.0 / (double)ctx->g.N;
     fa.upd.etd = 2;
+    fa.upd.filt = nullptr;
     fa.rkF = (V *)const_cast<void *>(nprev);
     LK(is3d ? launch_spass<R>(fa, ctx->LBz, ctx->stream) : launch_cpass<R>(fa, ctx->LBy, ctx->stream));
     if (is3d) {
@@ -1361,6 +1374,54 @@ int gopf_ie_euler_guess(gopf_ctx *ctx, void *x0)
         e = (ctx->prec == GOPF_FP32) ? enqueue_xpass_out<float>(ctx, (float *)x0, nullptr)
                                      : enqueue_xpass_out<double>(ctx, (double *)x0, nullptr);
     return (e == cudaSuccess) ? GOPF_OK : cuda_fail(ctx, e, "implicit Euler: explicit guess");
+}
+
+// NewVandeven (pf/vandeven.go:13-27): the 1000-point table
+// 1 - Gamma(2p)/Gamma(p)^2 * integral_0^x (t(1-t))^(p-1) dt by the trapezoid rule.
+extern "C" int gopf_vandeven_table(int order, double *out, int n)
+{
+    if (order < 1 || !out || n != 1000) return GOPF_ERR_ARG;
+    const double pref = std::tgamma((double)(2 * order)) / (std::tgamma((double)order) * std::tgamma((double)order));
+    const double dx = 1.0 / 999.0;
+    out[0] = 1.0;
+    for (int i = 1; i < 1000; ++i) {
+        const double x = (double)i * dx, x1 = x - dx;
+        const double i2 = std::pow(x * (1.0 - x), (double)(order - 1));
+        const double i1 = std::pow(x1 * (1.0 - x1), (double)(order - 1));
+        out[i] = out[i - 1] - pref * 0.5 * (i1 + i2) * dx;
+    }
+    return GOPF_OK;
+}
+
+extern "C" int gopf_set_modal_filter(gopf_ctx *ctx, const double *table, int n)
+{
+    if (!ctx) return GOPF_ERR_ARG;
+    if (n == 0 || !table) {
+        ctx->upd.filt = nullptr;
+        ctx->upd.nfilt = 0;
+        invalidate_graphs(ctx);
+        return GOPF_OK;
+    }
+    if (n < 2 || n > 65536) return gopf_fail(ctx, GOPF_ERR_ARG, "a filter table needs 2 to 65536 samples");
+    if (!ctx->initialised) return gopf_fail(ctx, GOPF_ERR_STATE, "set the filter after gopf_init");
+    int rc;
+    if ((rc = set_device(ctx))) return rc;
+    if (ctx->d_filter) {
+        cudaFree(ctx->d_filter);
+        ctx->d_filter = nullptr;
+    }
+    const size_t eb = (ctx->prec == GOPF_FP32) ? sizeof(float) : sizeof(double);
+    CK(cudaMalloc(&ctx->d_filter, eb * (size_t)n));
+    if (ctx->prec == GOPF_FP32) {
+        std::vector<float> t(table, table + n);
+        CK(cudaMemcpy(ctx->d_filter, t.data(), eb * (size_t)n, cudaMemcpyHostToDevice));
+    } else {
+        CK(cudaMemcpy(ctx->d_filter, table, eb * (size_t)n, cudaMemcpyHostToDevice));
+    }
+    ctx->upd.filt = ctx->d_filter;
+    ctx->upd.nfilt = n;
+    invalidate_graphs(ctx);
+    return GOPF_OK;
 }
 
 extern "C" int gopf_set_newton_krylov(gopf_ctx *ctx, int maxiter, double step_size, double tol, int stencil,

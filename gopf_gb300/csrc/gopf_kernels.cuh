@@ -16,6 +16,8 @@
 namespace gopf {
 // Launchers (return cudaError_t of the launch)
 template <typename R> cudaError_t launch_xpass(const XPassArgs<R> &a, int LB, cudaStream_t st);
+// number of FP64 partial-sum rows launch_xpass writes to a.red for this launch
+template <typename R> int xpass_red_blocks(const XPassArgs<R> &a, int LB);
 template <typename R> cudaError_t launch_cpass(const PassArgs<R> &a, int LB, cudaStream_t st); // contiguous y axis
 template <typename R> cudaError_t launch_spass(const PassArgs<R> &a, int LB, cudaStream_t st); // strided z axis
 // FP32 256 x 256 planes: inverse y, x pass (one group), forward y of every depth plane in one launch

@@ -477,6 +477,21 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
                 const R den = (R)1 - dt * L;
                 cn = cmk<V>((c0.x + dt * nhat.x) / den, (c0.y + dt * nhat.y) / den);
             }
+            if (u.filt) { // ApplyModalFilter (pf/util.go:125-132), Vandeven.Eval (pf/vandeven.go:30-40)
+                const R *__restrict__ tab = static_cast<const R *>(u.filt);
+                const int nf = u.nfilt;
+                const R x = sqrt(fline[l] + fpos[p]) * (R)0.63661977236758134307553505349006;
+                const R nn = (R)(nf - 1);
+                const int idx = (int)(x * nn);
+                R sg;
+                if (idx >= nf - 1) {
+                    sg = tab[nf - 1];
+                } else {
+                    const R dx = (R)1 / nn;
+                    sg = tab[idx] + (x - (R)idx * dx) * (tab[idx + 1] - tab[idx]) / dx;
+                }
+                cn = cmk<V>(cn.x * sg, cn.y * sg);
+            }
         }
         state[gi] = cn;
         sm[p * pitch + l] = cmk<V>(cn.x * invN, cn.y * invN);

@@ -101,6 +101,10 @@ struct UpdTable {
     //   etd == 2: buf[ngrp] holds FFT(x); tile <- (FFT(x) - c e^(L dt) - I(L, N, rkF)) / N for the
     //             inverse pass (the Newton residual); the state is not changed
     int etd;
+    // optional modal filter (pf/util.go:125-132): the updated c-hat is multiplied by
+    // filter(2|f|/pi), a table of nfilt samples on [0, 1] (R elements, device memory)
+    const void *filt;
+    int nfilt;
 };
 
 // Reduction slots written by the x-pass (FP64, compensated per block)

@@ -6,6 +6,7 @@
 #include "fast256.cuh"
 #include "plane256.cuh"
 #include "gopf_kernels_impl.cuh"
+#include "x256_io.cuh"
 
 namespace gopf {
 
@@ -102,7 +103,7 @@ static bool launch_z_tma(const PassArgs<float> &a, cudaStream_t st, cudaError_t 
         mU1 = mU0;
     }
     const unsigned grid = (unsigned)(a.g.S / 16);
-    const bool nz = a.upd.noise.kind != 0;
+    const bool nz = (a.upd.noise.kind != 0 || a.upd.filt != nullptr);
     if (a.nbuf == 1 && (a.allow_fast & 4)) {
         // persistent double-buffered variant: two blocks per SM
         static int nsm = 0;
@@ -152,8 +153,75 @@ static bool fast_z(const PassArgs<float> &a)
            (a.mode == PM_FUSED || a.mode == PM_INIT) && a.nbuf <= 2 && a.upd.rk_stage == 0 && a.upd.etd == 0;
 }
 
+// 256-column x passes that start or end in real space
+static bool fast_x_c2r(const XPassArgs<float> &a)
+{
+    return (a.allow_fast & 2) && a.g.X == 256 && a.g.KX == 129 && a.g.Y % f256::XROWS == 0 &&
+           a.in_mode == XIN_SPECTRAL && a.program == XP_POLY && a.ngrp_out == 0 && (a.rout || a.red) && !a.red2;
+}
+
+static bool fast_x_r2c(const XPassArgs<float> &a)
+{
+    return (a.allow_fast & 2) && a.g.X == 256 && a.g.KX == 129 && a.g.Y % f256::XROWS == 0 && a.in_mode == XIN_REAL &&
+           a.program == XP_POLY && !a.rout && !a.red && !a.red2 && a.ngrp_out >= 1 && a.ngrp_out <= GOPF_MAX_GROUPS;
+}
+
+static cudaError_t io_attributes()
+{
+    static std::once_flag once;
+    static cudaError_t err = cudaSuccess;
+    std::call_once(once, [] {
+        const int sm = f256::x256_io_smem_bytes();
+        err = cudaFuncSetAttribute(f256::k_x256_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(f256::k_x256_r2c<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(f256::k_x256_r2c<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    });
+    return err;
+}
+
+static bool launch_x_io(const XPassArgs<float> &a, cudaStream_t st, cudaError_t *err)
+{
+    if (io_attributes() != cudaSuccess) return false;
+    dim3 grid(a.g.Y / f256::XROWS, a.g.Z);
+    const int sm = f256::x256_io_smem_bytes();
+    if (fast_x_c2r(a)) {
+        CUtensorMap mi;
+        if (!x_map(&mi, a.in, a.g)) return false;
+        f256::k_x256_c2r<<<grid, f256::NT, sm, st>>>(a, mi);
+        *err = cudaGetLastError();
+        return true;
+    }
+    if (fast_x_r2c(a)) {
+        CUtensorMap mo[GOPF_MAX_GROUPS];
+        for (int b = 0; b < GOPF_MAX_GROUPS; ++b) {
+            if (b < a.ngrp_out) {
+                if (!x_map(&mo[b], a.out[b], a.g)) return false;
+            } else {
+                mo[b] = mo[0];
+            }
+        }
+        if (a.ngrp_out == 1) f256::k_x256_r2c<1><<<grid, f256::NT, sm, st>>>(a, mo[0], mo[1], mo[2], mo[3]);
+        else f256::k_x256_r2c<0><<<grid, f256::NT, sm, st>>>(a, mo[0], mo[1], mo[2], mo[3]);
+        *err = cudaGetLastError();
+        return true;
+    }
+    return false;
+}
+
+template <> int xpass_red_blocks<float>(const XPassArgs<float> &a, int LB)
+{
+    if (fast_x_c2r(a)) return (a.g.Y / f256::XROWS) * a.g.Z;
+    return ((a.g.Y + LB - 1) / LB) * a.g.Z;
+}
+
 template <> cudaError_t launch_xpass<float>(const XPassArgs<float> &a, int LB, cudaStream_t st)
 {
+    {
+        cudaError_t e;
+        if (launch_x_io(a, st, &e)) return e;
+    }
     if (fast_x(a)) {
         cudaError_t e;
         if ((a.allow_fast & 2) && launch_x_tma(a, st, &e)) return e;
@@ -171,7 +239,7 @@ template <> cudaError_t launch_cpass<float>(const PassArgs<float> &a, int LB, cu
         const long long nlines = (long long)a.g.Z * a.g.KX;
         const bool fused = (a.mode == PM_FUSED || a.mode == PM_INIT);
         dim3 grid((unsigned)((nlines + 15) / 16), fused ? 1 : a.nbuf);
-        const bool nz = fused && a.upd.noise.kind != 0;
+        const bool nz = fused && (a.upd.noise.kind != 0 || a.upd.filt != nullptr);
         if (fused && a.nbuf > 1) {
             if (nz) f256::k_y256<2, true><<<grid, f256::NT, 0, st>>>(a);
             else f256::k_y256<2, false><<<grid, f256::NT, 0, st>>>(a);
@@ -190,7 +258,7 @@ template <> cudaError_t launch_spass<float>(const PassArgs<float> &a, int LB, cu
         cudaError_t e;
         if ((a.allow_fast & 2) && launch_z_tma(a, st, &e)) return e;
         const unsigned grid = (unsigned)(a.g.S / 16);
-        const bool nz = a.upd.noise.kind != 0;
+        const bool nz = (a.upd.noise.kind != 0 || a.upd.filt != nullptr);
         if (a.nbuf > 1) {
             if (nz) f256::k_z256_fused<2, true><<<grid, f256::NT, 0, st>>>(a);
             else f256::k_z256_fused<2, false><<<grid, f256::NT, 0, st>>>(a);

@@ -6,6 +6,10 @@ template <> cudaError_t launch_xpass<double>(const XPassArgs<double> &a, int LB,
 {
     return launch_xpass_generic<double>(a, LB, st);
 }
+template <> int xpass_red_blocks<double>(const XPassArgs<double> &a, int LB)
+{
+    return ((a.g.Y + LB - 1) / LB) * a.g.Z;
+}
 template <> cudaError_t launch_cpass<double>(const PassArgs<double> &a, int LB, cudaStream_t st)
 {
     return launch_cpass_generic<double>(a, LB, st);

@@ -17,9 +17,9 @@
 //   y fwd    16 lines per block; line 0 of block 0 is split back into rows 0 and 128
 //   store    one bulk copy per block (block 0 also row 128)
 //
-// Remote writes use st.shared::cluster; two cluster barriers separate the
+// Remote writes use st.shared::cluster; cluster barriers separate the
 // phases.  The input and output may be the same array: every block has read
-// its rows before the first cluster barrier and writes only after the second.
+// its rows before the first cluster barrier and writes only after the last.
 #pragma once
 #include "fast256.cuh"
 
@@ -63,22 +63,24 @@ constexpr int PL_LINES = 16;                    // y lines (kx rows) per block
 constexpr int PL_TILE = PL_LINES * N * 8;       // 32 KB
 constexpr int PL_A = PL_TILE + N * 8 + 256;     // line tile + row 128, reused as the x exchange [256][16] + pad
 constexpr int PL_RX = 129 * XROWS * 8;          // [129 kx][32 y] x-pass input
-constexpr int PL_RY = PL_TILE;                  // [16 lines][256 ky]
 
 __host__ __device__ constexpr int plane256_smem_bytes()
 {
-    return 128 + PL_A + PL_RX + PL_RY + N * 8 + GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1) * 4 + 16;
+    return 128 + PL_A + PL_RX + N * 8 + GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1) * 4 + 16;
 }
 
-__global__ void __cluster_dims__(PL_CLUSTER, 1, 1) __launch_bounds__(NT, 2) k_plane256(const XPassArgs<float> a)
+// Three blocks per SM: the lines of the forward y pass (Ry) reuse the line
+// tile, so the x pass keeps its separated outputs in registers until every
+// block of the cluster is done with its tile (one extra cluster barrier).
+__global__ void __cluster_dims__(PL_CLUSTER, 1, 1) __launch_bounds__(NT, 3) k_plane256(const XPassArgs<float> a)
 {
     extern __shared__ unsigned char pl_dsm[];
     unsigned char *base = pl_dsm + ((128u - (smem_u32(pl_dsm) & 127u)) & 127u);
     float2 *tA = reinterpret_cast<float2 *>(base);
     float2 *rowX = tA + PL_LINES * N; // row kx = 128 (block 0)
     float2 *Rx = reinterpret_cast<float2 *>(base + PL_A);
-    float2 *Ry = reinterpret_cast<float2 *>(base + PL_A + PL_RX);
-    float2 *s_tw = reinterpret_cast<float2 *>(base + PL_A + PL_RX + PL_RY);
+    float2 *Ry = tA;                  // [16 lines][256 ky], after the x pass
+    float2 *s_tw = reinterpret_cast<float2 *>(base + PL_A + PL_RX);
     float *s_poly = reinterpret_cast<float *>(s_tw + N);
     uint64_t *bar = reinterpret_cast<uint64_t *>(s_poly + GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1));
     int *s_ok = reinterpret_cast<int *>(bar + 1);
@@ -160,24 +162,32 @@ __global__ void __cluster_dims__(PL_CLUSTER, 1, 1) __launch_bounds__(NT, 2) k_pl
 #pragma unroll
         for (int i = 0; i < 16; ++i) tA[(r + 16 * i) * 16 + j] = v[i];
         __syncthreads();
-        // separation X_a(k) = (Z(k) + conj Z(-k))/2, X_b(k) = (Z(k) - conj Z(-k))/(2i), then scatter
-        // kx = 1..127 to block kx/16 line kx%16; kx = 0 and 128 (both real) to block 0 line 0 as A + iB
+        // separation X_a(k) = (Z(k) + conj Z(-k))/2, X_b(k) = (Z(k) - conj Z(-k))/(2i) into registers;
+        // kx = 1..127 go to block kx/16 line kx%16, kx = 0 and 128 (both real) to block 0 line 0 as A + iB
         const int yy = tid & 31, jj = yy >> 1, odd = yy & 1, kx0 = tid >> 5;
         const int ygl = XROWS * (int)c + yy;
-#pragma unroll 4
+        float2 o[16];
+#pragma unroll
         for (int q = 0; q < 16; ++q) {
             const int kx = kx0 + 8 * q; // 0 .. 127
             const float2 P = tA[kx * 16 + jj];
             if (kx == 0) {
                 const float2 P2 = tA[128 * 16 + jj];
-                const float2 o = odd ? make_float2(P.y, P2.y) : make_float2(P.x, P2.x);
-                st_cluster(map_rank(smem_u32(&Ry[ygl]), 0), o);
+                o[q] = odd ? make_float2(P.y, P2.y) : make_float2(P.x, P2.x);
             } else {
                 const float2 Q = tA[(N - kx) * 16 + jj];
-                const float2 o = odd ? make_float2(0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x))
-                                     : make_float2(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y));
-                st_cluster(map_rank(smem_u32(&Ry[(kx & 15) * N + ygl]), (uint32_t)(kx >> 4)), o);
+                o[q] = odd ? make_float2(0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x))
+                           : make_float2(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y));
             }
+        }
+        cluster_arrive();
+        cluster_wait(); // every block has read its tile: the line buffers may be overwritten
+        const uint32_t ry = smem_u32(Ry);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            const int kx = kx0 + 8 * q;
+            const int off = ((kx == 0) ? ygl : (kx & 15) * N + ygl) * 8;
+            st_cluster(map_rank(ry + (uint32_t)off, (uint32_t)(kx >> 4)), o[q]);
         }
     }
     cluster_arrive();

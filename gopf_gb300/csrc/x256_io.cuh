@@ -1,0 +1,177 @@
+// x256_io.cuh -- 256-column x passes that start or end in real space (FP32).
+//
+// k_x256_c2r: half spectrum -> real rows (download, the Newton residual, the
+//   adjoint's state readout) and/or the FP64 block sums behind gopf_reduce.
+// k_x256_r2c: real rows -> r2c of the pointwise groups (upload, the Newton
+//   residual's FFT(x) and FFT(g(x))).
+// Both use the register-resident 256-point engine of fast256.cuh on 32 rows
+// (16 packed row pairs) of one depth plane per block.  Real rows move
+// through a [32][257]-float shared tile: the odd pitch makes both the
+// row-pair accesses of the transform and the row-contiguous global accesses
+// conflict free, and every global access of a warp is 128 contiguous bytes.
+#pragma once
+#include "fast256.cuh"
+#include "gopf_kernels_impl.cuh"
+
+namespace gopf {
+namespace f256 {
+
+constexpr int XR_PITCH = N + 1;
+
+__host__ __device__ constexpr int x256_io_smem_bytes()
+{
+    return 128 + XT_XCH_BYTES + XT_TILE_BYTES + N * 8 + GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1) * 4 + 16;
+}
+
+// half spectrum -> real rows (a.rout, optional) and FP64 partial sums (a.red, optional; one
+// [RED_SLOTS] row per block, blocks ordered blockIdx.y * gridDim.x + blockIdx.x)
+__global__ void __launch_bounds__(NT, 3) k_x256_c2r(const XPassArgs<float> a, const __grid_constant__ CUtensorMap mIn)
+{
+    extern __shared__ unsigned char c_dsm[];
+    unsigned char *base = c_dsm + ((128u - (smem_u32(c_dsm) & 127u)) & 127u);
+    float2 *s_x = reinterpret_cast<float2 *>(base);                           // input tile, then exchange slots
+    float *s_r = reinterpret_cast<float *>(base + XT_XCH_BYTES);              // real rows [32][257]
+    float2 *s_tw = reinterpret_cast<float2 *>(base + XT_XCH_BYTES + XT_TILE_BYTES);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(s_tw + N);
+    int *s_ok = reinterpret_cast<int *>(bar + 1);
+
+    const Geom &g = a.g;
+    const int tid = threadIdx.x;
+    const int j = tid & 15, r = tid >> 4;
+    const int y0 = blockIdx.x * XROWS;
+    const int z = blockIdx.y;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        mbar_arrive_expect_tx(bar, (uint32_t)XT_TILE_BYTES);
+        tma_load_3d(s_x, &mIn, y0, 0, z, bar);
+    }
+    load_twiddles(s_tw, a.twX);
+    if (tid == 0) *s_ok = tma_wait_or_flag(bar, 0, a.status) ? 1 : 0;
+    __syncthreads();
+    if (!*s_ok) return;
+
+    float2 v[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int k = r + 16 * i;
+        if (k <= 128) {
+            const float4 ab = *reinterpret_cast<const float4 *>(&s_x[k * XROWS + 2 * j]);
+            v[i] = make_float2(ab.x - ab.w, ab.y + ab.z);
+        } else {
+            const float4 ab = *reinterpret_cast<const float4 *>(&s_x[(N - k) * XROWS + 2 * j]);
+            v[i] = make_float2(ab.x + ab.w, -ab.y + ab.z);
+        }
+    }
+    __syncthreads();
+    auto at = [&](int x, int y) -> float2 & { return s_x[(x * 16 + y) * 16 + j]; };
+    fft256<true>(v, r, s_tw, at);
+    // v[i] = c(row 2j, col r + 16 i) + i c(row 2j+1, col r + 16 i)
+
+    if (a.red) {
+        double vals[RED_SLOTS];
+#pragma unroll
+        for (int s = 0; s < RED_SLOTS; ++s) vals[s] = 0.0;
+        vals[RED_MIN] = INFINITY;
+        vals[RED_MAX] = -INFINITY;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const double c0 = (double)v[i].x, c1 = (double)v[i].y;
+            vals[RED_SUM] += c0 + c1;
+            vals[RED_SUMSQ] += c0 * c0 + c1 * c1;
+            vals[RED_MIN] = fmin(vals[RED_MIN], fmin(c0, c1));
+            vals[RED_MAX] = fmax(vals[RED_MAX], fmax(c0, c1));
+            vals[RED_NONFINITE] += (isfinite(c0) ? 0.0 : 1.0) + (isfinite(c1) ? 0.0 : 1.0);
+        }
+        __shared__ double shred[8 * RED_SLOTS];
+        block_reduce_store(vals, a.red, shred);
+    }
+    if (a.rout) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const int k = r + 16 * i;
+            s_r[(2 * j) * XR_PITCH + k] = v[i].x;
+            s_r[(2 * j + 1) * XR_PITCH + k] = v[i].y;
+        }
+        __syncthreads();
+        float *__restrict__ out = a.rout + ((long long)z * g.Y + y0) * N;
+#pragma unroll 8
+        for (int q = 0; q < XROWS; ++q) out[q * N + tid] = s_r[q * XR_PITCH + tid];
+    }
+}
+
+// real rows -> r2c of the pointwise groups into a.out[grp] (a.identity: group 0 is the field itself)
+template <int NG>
+__global__ void __launch_bounds__(NT, 3)
+    k_x256_r2c(const XPassArgs<float> a, const __grid_constant__ CUtensorMap mO0, const __grid_constant__ CUtensorMap mO1,
+               const __grid_constant__ CUtensorMap mO2, const __grid_constant__ CUtensorMap mO3)
+{
+    extern __shared__ unsigned char r_dsm[];
+    unsigned char *base = r_dsm + ((128u - (smem_u32(r_dsm) & 127u)) & 127u);
+    float2 *s_x = reinterpret_cast<float2 *>(base);                        // real rows, then exchange slots
+    float2 *s_o = reinterpret_cast<float2 *>(base + XT_XCH_BYTES);         // output tile [129][32]
+    float2 *s_tw = reinterpret_cast<float2 *>(base + XT_XCH_BYTES + XT_TILE_BYTES);
+    float *s_poly = reinterpret_cast<float *>(s_tw + N);
+    float *s_r = reinterpret_cast<float *>(s_x);
+
+    const Geom &g = a.g;
+    const int tid = threadIdx.x;
+    const int j = tid & 15, r = tid >> 4;
+    const int y0 = blockIdx.x * XROWS;
+    const int z = blockIdx.y;
+    const float *__restrict__ in = a.rin + ((long long)z * g.Y + y0) * N;
+#pragma unroll 8
+    for (int q = 0; q < XROWS; ++q) s_r[q * XR_PITCH + tid] = in[q * N + tid];
+    for (int t = tid; t < GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1); t += NT)
+        s_poly[t] = (float)a.pw.dense[t / (GOPF_MAX_DEG + 1)][t % (GOPF_MAX_DEG + 1)];
+    load_twiddles(s_tw, a.twX);
+    __syncthreads();
+    float2 v[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int k = r + 16 * i;
+        v[i] = make_float2(s_r[(2 * j) * XR_PITCH + k], s_r[(2 * j + 1) * XR_PITCH + k]);
+    }
+    __syncthreads();
+    auto at = [&](int x, int y) -> float2 & { return s_x[(x * 16 + y) * 16 + j]; };
+
+    const int ng = (NG == 1) ? 1 : a.ngrp_out;
+    const int yy = tid & 31, jj = yy >> 1, odd = yy & 1, kx0 = tid >> 5;
+    for (int grp = 0; grp < ng; ++grp) {
+        float2 w[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) w[i] = v[i];
+        if (!(a.identity && grp == 0)) apply_poly(w, a, grp, s_poly + grp * (GOPF_MAX_DEG + 1));
+        fft256<false>(w, r, s_tw, at);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) s_x[(r + 16 * i) * 16 + j] = w[i];
+        if (grp > 0 && tid == 0) bulk_wait_read_all(); // the previous group's store has read s_o
+        __syncthreads();
+#pragma unroll 4
+        for (int q = 0; q < 17; ++q) {
+            const int kx = kx0 + 8 * q;
+            if (kx <= 128) {
+                const float2 P = s_x[kx * 16 + jj];
+                const float2 Q = s_x[((N - kx) & (N - 1)) * 16 + jj];
+                float2 o;
+                if (!odd) o = make_float2(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y));
+                else o = make_float2(0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
+                s_o[kx * XROWS + yy] = o;
+            }
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            const CUtensorMap *m = (grp == 0) ? &mO0 : (grp == 1) ? &mO1 : (grp == 2) ? &mO2 : &mO3;
+            tma_store_3d(m, y0, 0, z, s_o);
+            bulk_commit();
+        }
+    }
+    if (tid == 0) bulk_wait_read_all();
+}
+
+} // namespace f256
+} // namespace gopf

@@ -161,6 +161,14 @@ int gopf_set_terms(gopf_ctx *ctx, int nfields, const gopf_derived *derived, int 
 
 /* ---- stepping (pf.TimeStepper) ---- */
 int gopf_set_stepper(gopf_ctx *ctx, int stepper, double dt);
+/* Euler.SetFilter / RK4.SetFilter (pf/euler.go:61-64, pf/rk4.go:137-140) for a tabulated
+ * ModalFilter: after every update c-hat(k) is multiplied by filter(2|f|/pi) (ApplyModalFilter,
+ * pf/util.go:125-132), interpolated in the n samples of [0, 1] as Vandeven.Eval does
+ * (pf/vandeven.go:30-40).  n = 0 (or table = NULL) removes the filter.  Call after gopf_init.
+ * ImplicitEuler ignores filters, as the reference's does. */
+int gopf_set_modal_filter(gopf_ctx *ctx, const double *table, int n);
+/* NewVandeven(order).Data (pf/vandeven.go:13-27) into out[1000]. */
+int gopf_vandeven_table(int order, double *out, int n);
 /* ImplicitEuler's Newton-Krylov controls: the fields of nonlin.NewtonKrylov that DefaultNonLinSolver
  * sets (pf/implicitEuler.go:221-228; defaults maxiter 50, step 1e-3, tol 1e-7, stencil 6) plus the
  * GMRES basis size (default 50; each vector is one real field on the device).  tol bounds

@@ -359,6 +359,8 @@ typedef struct {
     or_volcons vc[OR_MAXSPECIAL];
     long current_step;
     double *freq; /* 3 * N cached frequencies */
+    double *filter; /* modal filter table (ModalFilter.Eval of a Vandeven-style table), NULL = none */
+    int nfilter;
 } or_model;
 
 or_model *or_model_create(int ndim, const int *dims, int nfields)
@@ -383,7 +385,65 @@ void or_model_destroy(or_model *m)
     for (int d = 0; d < m->nder; ++d) free(m->der[d].data);
     for (int e = 0; e < m->nel; ++e) { free(m->el[e].h); free(m->el[e].disp_override); }
     free(m->freq);
+    free(m->filter);
     free(m);
+}
+
+/* NewVandeven (pf/vandeven.go:13-27): 1000-point table of
+ * 1 - C(2p) / C(p)^2 * integral_0^x (t(1-t))^(p-1) dt, trapezoid rule, C = Gamma. */
+int or_vandeven_table(int order, double *out, int n)
+{
+    if (order < 1 || n != 1000) return 1;
+    const double pref = tgamma((double)(2 * order)) / (tgamma((double)order) * tgamma((double)order));
+    const double dx = 1.0 / 999.0;
+    out[0] = 1.0;
+    for (int i = 1; i < 1000; ++i) {
+        const double x = (double)i * dx;
+        const double i2 = pow(x * (1.0 - x), (double)(order - 1));
+        const double x1 = x - dx;
+        const double i1 = pow(x1 * (1.0 - x1), (double)(order - 1));
+        out[i] = out[i - 1] - pref * 0.5 * (i1 + i2) * dx;
+    }
+    return 0;
+}
+
+/* Vandeven.Eval (pf/vandeven.go:30-40): linear interpolation in the table, the last entry beyond it */
+double or_filter_eval(const double *tab, int n, double x)
+{
+    const double Nn = (double)(n - 1);
+    const int idx = (int)(x * Nn);
+    if (idx >= n - 1) return tab[n - 1];
+    const double dx = 1.0 / Nn;
+    const double dy = tab[idx + 1] - tab[idx];
+    const double x0 = (double)idx * dx;
+    return tab[idx] + (x - x0) * dy / dx;
+}
+
+/* Euler.SetFilter / RK4.SetFilter with a tabulated filter; n = 0 removes it */
+int or_set_filter(or_model *m, const double *tab, int n)
+{
+    free(m->filter);
+    m->filter = NULL;
+    m->nfilter = 0;
+    if (n <= 0) return 0;
+    if (n < 2) return 1;
+    m->filter = (double *)malloc(sizeof(double) * (size_t)n);
+    memcpy(m->filter, tab, sizeof(double) * (size_t)n);
+    m->nfilter = n;
+    return 0;
+}
+
+/* ApplyModalFilter (pf/util.go:125-132): d(k) *= Eval(2 |f| / pi) */
+static void or_apply_filter(or_model *m, cpx *d)
+{
+    if (!m->filter) return;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < m->N; ++i) {
+        const double *f = m->freq + 3 * i;
+        double r2 = 0.0;
+        for (int k = 0; k < m->ndim; ++k) r2 += f[k] * f[k];
+        d[i] *= or_filter_eval(m->filter, m->nfilter, sqrt(r2) * 2.0 / 3.14159265358979323846);
+    }
 }
 
 double *or_field(or_model *m, int f) { return (double *)m->fields[f]; }
@@ -784,6 +844,7 @@ int or_step_euler(or_model *m, double dt, long nsteps, int hooks)
             cpx *d = m->fields[f];
 #pragma omp parallel for schedule(static)
             for (long j = 0; j < N; ++j) d[j] = (d[j] + dt * rhs[j]) / (1.0 - dt * den[j]);
+            or_apply_filter(m, d);
         }
         or_ifft_fields(m);
         m->current_step++;
@@ -849,6 +910,7 @@ int or_step_rk4(or_model *m, double dt, long nsteps, int hooks, int advance)
             or_get_denum(m, f, den, tmp);
             for (long j = 0; j < N; ++j) fin[f][j] /= (1.0 - dt * den[j]);
             memcpy(m->fields[f], fin[f], sizeof(cpx) * (size_t)N);
+            or_apply_filter(m, m->fields[f]);
         }
         or_ifft_fields(m);
         if (advance) m->current_step++;

@@ -86,6 +86,12 @@ def lib():
         L.or_uniform_field.argtypes = [ctypes.c_uint64, ctypes.c_long, ctypes.c_double, ctypes.c_double, dp]
         L.or_num_threads.restype = ctypes.c_int
         L.or_set_num_threads.argtypes = [ctypes.c_int]
+        L.or_vandeven_table.argtypes = [ctypes.c_int, dp, ctypes.c_int]
+        L.or_vandeven_table.restype = ctypes.c_int
+        L.or_filter_eval.argtypes = [dp, ctypes.c_int, ctypes.c_double]
+        L.or_filter_eval.restype = ctypes.c_double
+        L.or_set_filter.argtypes = [vp, dp, ctypes.c_int]
+        L.or_set_filter.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -129,6 +135,20 @@ def uniform_field(seed: int, n: int, center: float, half_width: float) -> np.nda
     out = np.empty(n, dtype=np.float64)
     lib().or_uniform_field(seed, n, center, half_width, _dp(out))
     return out
+
+
+def vandeven(order: int) -> np.ndarray:
+    """NewVandeven(order).Data (pf/vandeven.go:13-27): the 1000-point filter table."""
+    out = np.empty(1000)
+    if lib().or_vandeven_table(int(order), _dp(out), 1000) != 0:
+        raise ValueError("bad order")
+    return out
+
+
+def filter_eval(table: np.ndarray, x: float) -> float:
+    """Vandeven.Eval (pf/vandeven.go:30-40)."""
+    t = np.ascontiguousarray(table, dtype=np.float64)
+    return float(lib().or_filter_eval(_dp(t), t.size, float(x)))
 
 
 def set_num_threads(n: int) -> None:
@@ -223,6 +243,16 @@ class Model:
 
     def volcons_multiplier(self, v: int) -> float:
         return float(self._L.or_volcons_multiplier(self._h, v))
+
+    def set_filter(self, table) -> None:
+        """Euler.SetFilter / RK4.SetFilter with a tabulated filter (None removes it)."""
+        if table is None:
+            self._L.or_set_filter(self._h, None, 0)
+            return
+        t = np.ascontiguousarray(table, dtype=np.float64)
+        self._keep_filter = t
+        if self._L.or_set_filter(self._h, _dp(t), t.size) != 0:
+            raise ValueError("bad filter table")
 
     # --- stepping ---
     def step_euler(self, dt: float, nsteps: int, hooks: bool = True) -> None:

@@ -314,7 +314,8 @@ def test_fast_kernels_2d_256_vs_oracle(oracle):
 def test_tma_tiles_match_plain_loads(two_groups):
     """The x and z kernels that move their tiles with TMA (one tile per block, and the persistent
     double-buffered z pass) compute exactly what the plain-load kernels do (same arithmetic, different
-    data movement): bitwise equal after 10 steps, 256^3 FP32."""
+    data movement): bitwise equal after 10 steps, 256^3 FP32 (upload and download through the same
+    kernels in all three runs)."""
     import gopf_gb300 as G
     from gopf_gb300.synthetic import uniform_field
 
@@ -327,8 +328,8 @@ def test_tma_tiles_match_plain_loads(two_groups):
         else:
             m = ch_gpu(dims, "fp32", 0.5, 0.05, c0)
         m.set_option(G._lib.OPT_TMA, tma)
-        m.upload(0, c0)
         m.step(10)
+        m.set_option(G._lib.OPT_TMA, 1)  # the same transform back to real space for all three
         models.append(m.download(0).real)
     assert np.array_equal(models[0], models[2])
     assert np.array_equal(models[1], models[2])
@@ -354,3 +355,35 @@ def test_plane_clusters_match_separate_passes(oracle):
     o = ch_oracle(oracle, dims, 0.5, c0)
     o.step_euler(0.05, 27)
     assert rel_l2(res[0], o.field(0).real) <= 1e-4
+
+
+def test_real_space_x_kernels_match_generic():
+    """Upload (real -> spectrum), download (spectrum -> real) and the FP64 reductions through the
+    256-column real-space kernels agree with the generic x pass to FP32 round-off."""
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+
+    dims = [256, 256, 256]
+    c0 = uniform_field(9, 256 ** 3, 0.2, 0.1)
+    out = []
+    for tma in (1, 0):
+        m = G.Model(dims, "fp32", device=0)
+        m.set_option(G._lib.OPT_TMA, tma)
+        m.add_field("conc")
+        m.add_scalar("gamma", 0.5)
+        m.add_scalar("m1", -1.0)
+        m.add_equation("dconc/dt = LAP conc^3 + m1*LAP conc + m1*gamma*LAP^2 conc")
+        m.init()
+        m.set_stepper("euler", 0.05)
+        m.upload(0, c0)
+        d = m.download_real(0)
+        assert np.max(np.abs(d - c0)) < 2e-6  # the round trip
+        out.append((d, m.mass(0), m.reduce(0, G.RED_MIN), m.reduce(0, G.RED_MAX), m.reduce(0, G.RED_SUMSQ)))
+        m.step(5)
+        out[-1] = out[-1] + (m.download_real(0),)
+    (d1, s1, mn1, mx1, q1, e1), (d0, s0, mn0, mx0, q0, e0) = out
+    assert rel_l2(d1, d0) < 1e-6 and rel_l2(e1, e0) < 1e-6
+    # both sums are FP64 over FP32 cells; the FP32 field itself carries ~1e-8 relative error
+    assert abs(s1 - s0) <= 1e-9 * abs(s0) and abs(s1 - c0.sum()) < 1e-7 * abs(c0.sum())
+    assert abs(mn1 - c0.min()) < 2e-6 and abs(mx1 - c0.max()) < 2e-6
+    assert abs(q1 - q0) <= 1e-6 * q0
