@@ -201,6 +201,17 @@ class Model:
     def set_stepper(self, name: str, dt: float) -> None:
         self._ck(self._L.gopf_set_stepper(self._h, _STEPPERS[name], dt))
 
+    def save_float64(self, path: str, field: int = 0, asynchronous: bool = False) -> None:
+        """Float64IO/SaveFloat64: raw big-endian float64 file of the real field (pf/fileIO.go)."""
+        self._ck(self._L.gopf_save_float64(self._h, field, path.encode(), int(asynchronous)))
+
+    def io_wait(self) -> None:
+        self._ck(self._L.gopf_io_wait(self._h))
+
+    def load_float64(self, path: str, field: int = 0) -> None:
+        """LoadFloat64 + upload (restart from a saved field)."""
+        self._ck(self._L.gopf_load_float64(self._h, field, path.encode()))
+
     def set_modal_filter(self, table) -> None:
         """Euler/RK4 SetFilter with a tabulated filter on [0, 1] (None removes it)."""
         if table is None:

@@ -25,7 +25,7 @@ DER_PRODUCT, DER_POLY, DER_INDICATOR, DER_INDICATOR_D, DER_INDICATOR_HD, DER_WHI
 NOISE_WHITE, NOISE_CONSERVATIVE = 1, 2
 SRC_NONE, SRC_FIELD, SRC_DERIVED = range(3)
 RED_SUM, RED_SUMSQ, RED_MIN, RED_MAX, RED_NONFINITE = range(5)
-OPT_CHECK_FINITE, OPT_USE_GRAPHS, OPT_FAST_KERNELS, OPT_TMA, OPT_PLANE = 0, 1, 2, 3, 4
+OPT_CHECK_FINITE, OPT_USE_GRAPHS, OPT_FAST_KERNELS, OPT_TMA, OPT_PLANE, OPT_DIRECT_HOST = 0, 1, 2, 3, 4, 5
 MAX_FACTORS = 8
 
 
@@ -99,6 +99,9 @@ SIGNATURES = {
     "gopf_adjoint_release": ([_vp], _i),
     "gopf_reduce_noalloc": ([_vp, _sz, _dp, _vp], _i),
     "gopf_noalloc_last_error": ([], _cp),
+    "gopf_save_float64": ([_vp, _i, _cp, _i], _i),
+    "gopf_io_wait": ([_vp], _i),
+    "gopf_load_float64": ([_vp, _i, _cp], _i),
     "gopf_set_modal_filter": ([_vp, _dp, _i], _i),
     "gopf_vandeven_table": ([_i, _dp, _i], _i),
     "gopf_kernel_launches": ([_vp, _ll, ctypes.POINTER(ctypes.c_longlong)], _i),

@@ -77,7 +77,15 @@ template <bool INV> __device__ __forceinline__ void pdft16(float2 (&v)[16])
 
 // 256-point FFT of the thread's v[i] = x[r + 16 i]; result v[i] = X[r + 16 i].
 // at(a, b) is the shared-memory slot of element (a, b) of this thread's line.
-template <bool INV, typename AT>
+// WARP: the 16 threads of every line are one half-warp and its slots are its
+// own, so the exchange only has to be ordered within the warp.
+__device__ __forceinline__ void xsync(bool warp)
+{
+    if (warp) __syncwarp();
+    else __syncthreads();
+}
+
+template <bool INV, bool WARP = false, typename AT>
 __device__ __forceinline__ void fft256(float2 (&v)[16], int r, const float2 *__restrict__ tw, AT &&at)
 {
     pdft16<INV>(v);
@@ -88,11 +96,11 @@ __device__ __forceinline__ void fft256(float2 (&v)[16], int r, const float2 *__r
     }
 #pragma unroll
     for (int k1 = 0; k1 < 16; ++k1) at(r, k1) = v[k1];
-    __syncthreads();
+    xsync(WARP);
 #pragma unroll
     for (int n2 = 0; n2 < 16; ++n2) v[n2] = at(n2, r);
     pdft16<INV>(v);
-    __syncthreads(); // slots may be reused after return
+    xsync(WARP); // slots may be reused after return
 }
 
 // s_tw[k1*16 + r] = W256^(r*k1)
@@ -443,21 +451,21 @@ __global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_y256(const PassArgs<flo
     __syncthreads();
     auto at = [&](int x, int y) -> float2 & { return s_x[l * N + x * 16 + ((x + y) & 15)]; };
     if (!fused) {
-        if (a.mode == PM_FWD) fft256<false>(v, r, s_tw, at);
-        else fft256<true>(v, r, s_tw, at);
+        if (a.mode == PM_FWD) fft256<false, true>(v, r, s_tw, at);
+        else fft256<true, true>(v, r, s_tw, at);
 #pragma unroll
         for (int i = 0; i < 16; ++i)
             if (valid) buf[q * N + r + 16 * i] = v[i];
         return;
     }
-    fft256<false>(v, r, s_tw, at);
+    fft256<false, true>(v, r, s_tw, at);
     const int ngrp = (NG == 1) ? (a.upd.ngrp > 0 ? 1 : 0) : a.upd.ngrp;
     float2 w[NG == 1 ? 1 : 16];
     if (NG > 1 && ngrp > 1) {
         const float2 *__restrict__ U1 = a.buf[1];
 #pragma unroll
         for (int i = 0; i < 16; ++i) w[i] = valid ? U1[q * N + r + 16 * i] : zero;
-        fft256<false>(reinterpret_cast<float2(&)[16]>(w), r, s_tw, at);
+        fft256<false, true>(reinterpret_cast<float2(&)[16]>(w), r, s_tw, at);
     }
     const UpdTable &u = a.upd;
     const UpdRegs R = load_upd(u, ngrp);
@@ -489,7 +497,7 @@ __global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_y256(const PassArgs<flo
         }
         v[i] = make_float2(cn.x * R.invN, cn.y * R.invN);
     }
-    fft256<true>(v, r, s_tw, at);
+    fft256<true, true>(v, r, s_tw, at);
     float2 *__restrict__ T = a.tout;
 #pragma unroll
     for (int i = 0; i < 16; ++i)

@@ -257,9 +257,11 @@ template <typename R> static int ctx_alloc(gopf_ctx *ctx)
 
 void gopf_ie_free(gopf_ctx *ctx);
 int gopf_ie_step(gopf_ctx *ctx);
+void gopf_io_free(gopf_ctx *ctx);
 
 static void ctx_free(gopf_ctx *ctx)
 {
+    gopf_io_free(ctx);
     gopf_ie_free(ctx);
     if (ctx->gexec1) cudaGraphExecDestroy(ctx->gexec1);
     if (ctx->gexecK) cudaGraphExecDestroy(ctx->gexecK);
@@ -369,6 +371,7 @@ extern "C" int gopf_set_option(gopf_ctx *ctx, int opt, long long v)
     else if (opt == GOPF_OPT_USE_GRAPHS) ctx->use_graphs = (int)(v != 0);
     else if (opt == GOPF_OPT_FAST_KERNELS) ctx->use_fast = (int)(v != 0);
     else if (opt == GOPF_OPT_PLANE) ctx->use_plane = (int)(v != 0);
+    else if (opt == GOPF_OPT_DIRECT_HOST) ctx->use_direct_host = (int)(v != 0);
     else if (opt == GOPF_OPT_TMA) ctx->use_tma = (int)std::min<long long>(std::max<long long>(v, 0), 2);
     else return gopf_fail(ctx, GOPF_ERR_ARG, "unknown option");
     invalidate_graphs(ctx); // captured launches carry the old choice
@@ -1029,9 +1032,34 @@ static int require_ready(gopf_ctx *ctx, int field)
     return GOPF_OK;
 }
 
+// Device address of a host buffer the GPU may read and write directly (pinned or registered
+// host memory under unified addressing), or nullptr for pageable memory, which goes through a
+// staging copy.  On Grace-Blackwell the direct path streams over NVLink-C2C from every SM
+// instead of through one copy engine.
+static void *direct_host_ptr(gopf_ctx *ctx, const void *p)
+{
+    if (!ctx->use_direct_host) return nullptr;
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return (pa.type == cudaMemoryTypeHost && pa.devicePointer) ? pa.devicePointer : nullptr;
+}
+
 template <typename R> static int upload_impl(gopf_ctx *ctx, const double *data, bool complex_in)
 {
     const long long N = ctx->g.N;
+    if (void *dp = direct_host_ptr(ctx, data)) {
+        if (complex_in)
+            k_c128_to_real<R><<<ew_blocks(N), 256, 0, ctx->stream>>>((const double2 *)dp, (R *)ctx->d_real, N);
+        else
+            k_double_to_real<R><<<ew_blocks(N), 256, 0, ctx->stream>>>((const double *)dp, (R *)ctx->d_real, N);
+        CK(cudaGetLastError());
+        CK(enqueue_load_state<R>(ctx));
+        CK(cudaStreamSynchronize(ctx->stream));
+        return GOPF_OK;
+    }
     if (complex_in) {
         CK(cudaMemcpyAsync(ctx->d_c128, data, sizeof(double2) * N, cudaMemcpyHostToDevice, ctx->stream));
         k_c128_to_real<R><<<ew_blocks(N), 256, 0, ctx->stream>>>(ctx->d_c128, (R *)ctx->d_real, N);
@@ -1049,6 +1077,15 @@ template <typename R> static int download_impl(gopf_ctx *ctx, double *data, bool
 {
     const long long N = ctx->g.N;
     CK(enqueue_xpass_out<R>(ctx, (R *)ctx->d_real, nullptr));
+    if (void *dp = direct_host_ptr(ctx, data)) {
+        if (complex_out)
+            k_real_to_c128<R><<<ew_blocks(N), 256, 0, ctx->stream>>>((const R *)ctx->d_real, (double2 *)dp, N);
+        else
+            k_real_to_double<R><<<ew_blocks(N), 256, 0, ctx->stream>>>((const R *)ctx->d_real, (double *)dp, N);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(ctx->stream));
+        return GOPF_OK;
+    }
     if (complex_out) {
         k_real_to_c128<R><<<ew_blocks(N), 256, 0, ctx->stream>>>((const R *)ctx->d_real, ctx->d_c128, N);
         CK(cudaGetLastError());

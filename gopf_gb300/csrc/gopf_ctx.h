@@ -59,6 +59,7 @@ struct gopf_special {
 };
 
 struct gopf_ie_work;
+struct gopf_io_state;
 
 struct gopf_ctx {
     int device = 0;
@@ -143,6 +144,7 @@ struct gopf_ctx {
     int use_fast = 1;
     int use_tma = 1;
     int use_plane = 0;
+    int use_direct_host = 1;
 
     // ImplicitEuler's Newton-Krylov controls (DefaultNonLinSolver, pf/implicitEuler.go:221-228) and
     // the outcome of the last step
@@ -155,6 +157,7 @@ struct gopf_ctx {
     int nk_last_newton = 0, nk_last_krylov = 0, nk_last_converged = 0;
     double nk_last_residual = 0.0;
     gopf_ie_work *ie = nullptr;
+    gopf_io_state *io = nullptr; // field files: pinned staging buffer and writer thread
     std::string err;
 };
 

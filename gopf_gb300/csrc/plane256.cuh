@@ -120,7 +120,7 @@ __global__ void __cluster_dims__(PL_CLUSTER, 1, 1) __launch_bounds__(NT, 3) k_pl
         }
         __syncthreads();
         auto at = [&](int x, int y) -> float2 & { return tA[l * N + x * 16 + ((x + y) & 15)]; };
-        fft256<true>(v, r, s_tw, at);
+        fft256<true, true>(v, r, s_tw, at);
 
         // scatter to the owners of the rows: y = r + 16 i lives in block i/2 at column r + 16 (i & 1)
         cluster_wait(); // every block of the cluster has started
@@ -201,7 +201,7 @@ __global__ void __cluster_dims__(PL_CLUSTER, 1, 1) __launch_bounds__(NT, 3) k_pl
         for (int i = 0; i < 16; ++i) v[i] = Ry[l * N + r + 16 * i];
         __syncthreads();
         auto at = [&](int x, int y) -> float2 & { return Ry[l * N + x * 16 + ((x + y) & 15)]; };
-        fft256<false>(v, r, s_tw, at);
+        fft256<false, true>(v, r, s_tw, at);
 #pragma unroll
         for (int i = 0; i < 16; ++i) Ry[l * N + r + 16 * i] = v[i];
         __syncthreads();

@@ -93,6 +93,8 @@ enum {
                                   per block (default), 2 also the persistent double-buffered z pass */
     GOPF_OPT_PLANE = 4,        /* 1: consecutive FP32 Euler steps on 256 x 256 x Z grids do the inverse y,
                                   x and forward y passes of each depth plane in one cluster launch */
+    GOPF_OPT_DIRECT_HOST = 5   /* 1 (default): pinned host buffers given to upload/download are read and
+                                  written by kernels in place; pageable buffers are staged */
 };
 
 #define GOPF_MAX_FACTORS 8
@@ -190,6 +192,16 @@ int gopf_step(gopf_ctx *ctx, long long nsteps);
 int gopf_get_time(gopf_ctx *ctx, double *t);
 int gopf_get_step(gopf_ctx *ctx, long long *step);
 int gopf_synchronize(gopf_ctx *ctx);
+
+/* ---- field files (pf/fileIO.go) ----
+ * Float64IO.SaveFields / SaveFloat64 (pf/fileIO.go:45-97): the real field as raw big-endian
+ * float64 in node order, readable by LoadFloat64 and by the XDMF files of pf.WriteXDMF.  The byte
+ * swap runs on the GPU; with async != 0 the call returns once the copy is queued and a host thread
+ * writes the file while the device keeps stepping (the next save or gopf_io_wait collects it). */
+int gopf_save_float64(gopf_ctx *ctx, int field_id, const char *path, int async);
+int gopf_io_wait(gopf_ctx *ctx);
+/* LoadFloat64 (pf/fileIO.go:64-83) followed by gopf_field_upload_real: restart from a saved field. */
+int gopf_load_float64(gopf_ctx *ctx, int field_id, const char *path);
 
 /* ---- monitors ---- */
 int gopf_reduce(gopf_ctx *ctx, int field_id, int what, double *out);

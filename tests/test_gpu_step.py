@@ -387,3 +387,31 @@ def test_real_space_x_kernels_match_generic():
     assert abs(s1 - s0) <= 1e-9 * abs(s0) and abs(s1 - c0.sum()) < 1e-7 * abs(c0.sum())
     assert abs(mn1 - c0.min()) < 2e-6 and abs(mx1 - c0.max()) < 2e-6
     assert abs(q1 - q0) <= 1e-6 * q0
+
+
+def test_pinned_host_buffers_read_in_place():
+    """Upload from and download to pinned host memory (read and written by kernels in place) give
+    exactly what the staged path gives for pageable memory."""
+    import ctypes
+
+    import torch
+
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+
+    dims = [64, 64, 64]
+    n = 64 ** 3
+    c0 = uniform_field(4, n, 0.0, 0.1)
+    m = ch_gpu(dims, "fp32", 0.5, 0.05, c0)
+    L = G.load()
+    pinned = torch.zeros(2 * n, dtype=torch.float64, pin_memory=True)
+    pinned.numpy()[0::2] = c0
+    dp = ctypes.cast(pinned.data_ptr(), ctypes.POINTER(ctypes.c_double))
+    m._ck(L.gopf_field_upload(m.handle, 0, dp, n))
+    m.step(3)
+    m._ck(L.gopf_field_download(m.handle, 0, dp, n))
+    a = pinned.numpy().copy()
+    m.upload(0, c0)            # pageable numpy buffer: staged
+    m.step(3)
+    b = m.download(0)          # pageable
+    assert np.array_equal(a[0::2], b.real) and np.all(a[1::2] == 0.0)
