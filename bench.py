@@ -40,8 +40,8 @@ UNIT = "steps/s"
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of each step kernel, from
 # one ncu capture of `python bench.py --steps 10 --warmup 3 --no-cpu-baseline --no-e2e` on a GB300
 # (profiles/launches_ch3d_256_fp32.md).  Bytes that a launch leaves in L2 are not in these counts.
-NCU_TRAFFIC = {"zpass_update": 205.5e6, "xpass_pointwise": 72.8e6, "ypass_forward": 72.1e6,
-               "ypass_inverse": 72.1e6}
+NCU_TRAFFIC = {"zpass_update": 206.8e6, "xpass_pointwise": 72.3e6, "ypass_forward": 72.2e6,
+               "ypass_inverse": 72.2e6}
 DIMS = [256, 256, 256]
 GAMMA, M, DT, SEED = 0.5, 1.0, 0.05, 1
 CH_EQ = "dconc/dt = M*LAP conc^3 + m1*LAP conc + m1*gamma*LAP^2 conc"

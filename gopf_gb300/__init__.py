@@ -142,6 +142,15 @@ class Model:
         m = np.ascontiguousarray(misfit, dtype=np.float64).reshape(9)
         self._ck(self._L.gopf_register_elastic(self._h, name.encode(), field.encode(), _dptr(c), _dptr(m)))
 
+    def register_hessian(self, name: str, K) -> None:
+        """RegisterImplicitTerm(name, &TensorialHessian{K: K}, nil)."""
+        k = np.ascontiguousarray(K, dtype=np.float64).reshape(-1)
+        self._ck(self._L.gopf_register_hessian(self._h, name.encode(), _dptr(k), k.size))
+
+    def register_spectral_viscosity(self, name: str, eps: float, threshold: float, power: int) -> None:
+        """RegisterImplicitTerm(name, &SpectralViscosity{eps, threshold, power}, nil)."""
+        self._ck(self._L.gopf_register_spectral_viscosity(self._h, name.encode(), eps, threshold, int(power)))
+
     def register_volcons(self, name: str, field: str, indicator: str, dt: float) -> None:
         self._ck(self._L.gopf_register_volcons(self._h, name.encode(), field.encode(), indicator.encode(), dt))
 

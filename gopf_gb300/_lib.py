@@ -99,6 +99,8 @@ SIGNATURES = {
     "gopf_adjoint_release": ([_vp], _i),
     "gopf_reduce_noalloc": ([_vp, _sz, _dp, _vp], _i),
     "gopf_noalloc_last_error": ([], _cp),
+    "gopf_register_hessian": ([_vp, _cp, _dp, _i], _i),
+    "gopf_register_spectral_viscosity": ([_vp, _cp, ctypes.c_double, ctypes.c_double, _i], _i),
     "gopf_save_float64": ([_vp, _i, _cp, _i], _i),
     "gopf_io_wait": ([_vp], _i),
     "gopf_load_float64": ([_vp, _i, _cp], _i),

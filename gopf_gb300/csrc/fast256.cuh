@@ -138,28 +138,24 @@ __device__ __forceinline__ UpdRegs load_upd(const UpdTable &u, int ng)
     R.ng = ng;
 #pragma unroll
     for (int b = 0; b < 2; ++b) {
-        R.gs[b] = (b < ng && u.gscale[b]) ? (float)(*u.gscale[b]) : 1.f;
+        // a group the model does not have contributes nothing (scale 0)
+        R.gs[b] = (b < ng) ? (u.gscale[b] ? (float)(*u.gscale[b]) : 1.f) : 0.f;
         R.gl[b] = (b < ng) ? u.glap[b] : 0;
     }
-    R.nimp = u.nimp;
+    R.nimp = u.nimp; // at most 4 on this path (the launchers check)
 #pragma unroll
     for (int q = 0; q < 4; ++q) R.imp[q] = (q < u.nimp) ? (float)u.imp[q] : 0.f;
     return R;
 }
 
+// m^p for a uniform 0 <= p < 8 without branches in the unrolled update loops
 __device__ __forceinline__ float mkpow(float mk, int p)
 {
-    switch (p) {
-    case 0: return 1.f;
-    case 1: return mk;
-    case 2: return mk * mk;
-    case 3: return mk * mk * mk;
-    default: {
-        float f = 1.f;
-        for (int q = 0; q < p; ++q) f *= mk;
-        return f;
-    }
-    }
+    const float m2 = mk * mk;
+    float f = (p & 1) ? mk : 1.f;
+    f *= (p & 2) ? m2 : 1.f;
+    if (p & 4) f *= m2 * m2;
+    return f;
 }
 
 // ApplyModalFilter (pf/util.go:125-132) with the Vandeven.Eval interpolation (pf/vandeven.go:30-40):
@@ -192,24 +188,17 @@ __device__ __forceinline__ float recip_nr(float d)
 
 // k-space update of one element (pf/euler.go:32-34 with the term algebra of pf/rhsBuilder.go):
 // c <- (c + dt sum_b s_b m^p_b U_b) / (1 - dt L(m)),  m = -k^2
-__device__ __forceinline__ float2 euler_update(const UpdRegs &R, const UpdTable &u, float2 c0, float2 U0, float2 U1,
-                                               float mk)
+template <int NG>
+__device__ __forceinline__ float2 euler_update(const UpdRegs &R, float2 c0, float2 U0, float2 U1, float mk)
 {
     const float f0 = R.gs[0] * mkpow(mk, R.gl[0]);
     float2 nh = make_float2(f0 * U0.x, f0 * U0.y);
-    if (R.ng > 1) {
+    if (NG > 1 && R.ng > 1) {
         const float f1 = R.gs[1] * mkpow(mk, R.gl[1]);
         nh.x += f1 * U1.x;
         nh.y += f1 * U1.y;
     }
-    if (R.ng == 0) nh = make_float2(0.f, 0.f);
-    float L;
-    if (R.nimp <= 4) {
-        L = ((R.imp[3] * mk + R.imp[2]) * mk + R.imp[1]) * mk + R.imp[0];
-    } else {
-        L = 0.f;
-        for (int q = u.nimp - 1; q >= 0; --q) L = L * mk + (float)u.imp[q];
-    }
+    const float L = ((R.imp[3] * mk + R.imp[2]) * mk + R.imp[1]) * mk + R.imp[0];
     const float rden = recip_nr(1.f - R.dt * L);
     return make_float2((c0.x + R.dt * nh.x) * rden, (c0.y + R.dt * nh.y) * rden);
 }
@@ -277,7 +266,7 @@ __global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_z256_fused(const PassAr
                 c0.x += R.dt * (float)nr;
                 c0.y += R.dt * (float)ni;
             }
-            cn = euler_update(R, u, c0, v[i], (NG > 1) ? w[NG > 1 ? i : 0] : v[i], mk);
+            cn = euler_update<NG>(R, c0, v[i], (NG > 1) ? w[NG > 1 ? i : 0] : v[i], mk);
             if (NZ && u.filt) cn = modal_filter(u, cn, fl + s_fz[k]);
         }
         state[gi] = cn;
@@ -387,7 +376,7 @@ __global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2)
                 c0.x += R.dt * (float)nr;
                 c0.y += R.dt * (float)ni;
             }
-            cn = euler_update(R, u, c0, v[i], (NG > 1) ? w[NG > 1 ? i : 0] : v[i], mk);
+            cn = euler_update<NG>(R, c0, v[i], (NG > 1) ? w[NG > 1 ? i : 0] : v[i], mk);
             if (NZ && u.filt) cn = modal_filter(u, cn, fl + s_fz[k]);
         }
         tS[k * 16 + l] = cn; // each thread rewrites exactly the elements it read
@@ -490,7 +479,7 @@ __global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_y256(const PassArgs<flo
                     c0.x += R.dt * (float)nr;
                     c0.y += R.dt * (float)ni;
                 }
-                cn = euler_update(R, u, c0, v[i], (NG > 1) ? w[NG > 1 ? i : 0] : v[i], mk);
+                cn = euler_update<NG>(R, c0, v[i], (NG > 1) ? w[NG > 1 ? i : 0] : v[i], mk);
                 if (NZ && u.filt) cn = modal_filter(u, cn, fl + s_fy[k]);
             }
             state[gi] = cn;
@@ -735,7 +724,7 @@ __global__ void __launch_bounds__(NT, 2)
                     c0.x += R.dt * (float)nr;
                     c0.y += R.dt * (float)ni;
                 }
-                cn = euler_update(R, u, c0, v[i], v[i], mk);
+                cn = euler_update<1>(R, c0, v[i], v[i], mk);
                 if (NZ && u.filt) cn = modal_filter(u, cn, fl + s_fz[k]);
             }
             tS[k * 16 + l] = cn;

@@ -563,6 +563,19 @@ int gopf_compile_model(gopf_ctx *ctx)
             noise.lap = sp.lap;
             noise_strength = nz.strength;
             noise_seed = nz.seed;
+        } else if (sp.kind == 4) {
+            const gopf_modeldef::ImplicitSym &is = ctx->def.isym[sp.index];
+            if (u.nxs >= GOPF_MAX_XSYM) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "too many implicit user terms");
+            XSym &x = u.xs[u.nxs++];
+            memset(&x, 0, sizeof(x));
+            x.kind = is.kind;
+            x.coef = sp.coef;
+            x.lap = sp.lap;
+            memcpy(x.K, is.K, sizeof(x.K));
+            x.dk = (is.nk == 9) ? 3 : 2;
+            x.eps = is.eps;
+            x.threshold = is.threshold;
+            x.power = is.power;
         } else {
             return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "user-defined term kind has no device implementation");
         }
@@ -668,7 +681,7 @@ extern "C" int gopf_equation_summary(gopf_ctx *ctx, int eq, int *ne, int *ni)
     for (const gopf_term &t : ctx->terms)
         if (t.eq == eq) (t.implicit ? *ni : *ne) += 1;
     for (const gopf_special &s : ctx->specials)
-        if (s.eq == eq) *ne += 1;
+        if (s.eq == eq) (s.kind == 4 ? *ni : *ne) += 1; // kind 4: implicit user terms (RHS.Denum)
     return GOPF_OK;
 }
 

@@ -252,7 +252,7 @@ extern "C" int gopf_batch_create(gopf_ctx *const *ctxs, int n, gopf_batch **out)
         if (c->ndim != 2) return bfail(b, GOPF_ERR_UNSUPPORTED, "batches step 2D contexts");
         if (!c->initialised || !(c->dt > 0.0) || !c->state_valid)
             return bfail(b, GOPF_ERR_STATE, "every context needs its model, stepper and field set");
-        if (c->stepper != GOPF_STEPPER_EULER || c->has_elastic || c->has_volcons || c->noise.kind || c->upd.filt)
+        if (c->stepper != GOPF_STEPPER_EULER || c->has_elastic || c->has_volcons || c->noise.kind || c->upd.filt || c->upd.nxs)
             return bfail(b, GOPF_ERR_UNSUPPORTED, "batches step Euler models without user-defined terms, noise or filters");
         b->ctx.push_back(c);
     }

@@ -44,6 +44,15 @@ struct gopf_modeldef {
         unsigned long long seed;
     };
     std::vector<Noise> noise;                                    // WhiteNoise / ConservativeNoise
+    struct ImplicitSym {
+        std::string name;
+        int kind; // 1 TensorialHessian, 2 SpectralViscosity
+        double K[9];
+        int nk;
+        double eps, threshold;
+        int power;
+    };
+    std::vector<ImplicitSym> isym;                               // RegisterImplicitTerm with a symbol
     std::vector<std::string> equations;                          // AddEquation (spaces removed)
     std::vector<std::string> derived_names;                      // derived fields, in registration order
     std::vector<gopf_derived> derived;

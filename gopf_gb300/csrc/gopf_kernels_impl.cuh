@@ -431,6 +431,71 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
             // implicit symbol L = sum_p imp[p] (-k^2)^p
             R L = (R)0;
             for (int q = u.nimp - 1; q >= 0; --q) L = L * mk + (R)u.imp[q];
+            // With a tensorial Hessian the reference's symbol differs between k and -k on Nyquist
+            // lines (Freq keeps +1/2 for both).  Its complex field then carries an anti-Hermitian
+            // part; the real field is the Hermitian part of its step, i.e. the update divides by
+            // the mean of 1/(1 - a L(k)) and 1/(1 - a L(-k)).  Lm is L(-k); Lm == L elsewhere.
+            R Lm = L;
+            if (u.nxs) { // implicit user terms with a per-frequency symbol (XSym)
+                long long kx, yy, zz;
+                if (CONTIG) {
+                    const long long q = l0 + l;
+                    zz = q / g.KX;
+                    kx = q - zz * g.KX;
+                    yy = p;
+                } else {
+                    const long long i = l0 + l;
+                    kx = i / g.Y;
+                    yy = i - kx * g.Y;
+                    zz = p;
+                }
+                const int dim = (g.Z > 1) ? 3 : 2;
+                // the reference's Freq: row, col, depth in cycles per sample, +1/2 kept at Nyquist
+                const double f[3] = {(double)((2 * yy > g.Y) ? yy - g.Y : yy) / (double)g.Y, (double)kx / (double)g.X,
+                                     (double)((2 * zz > g.Z) ? zz - g.Z : zz) / (double)g.Z};
+                double fm[3]; // Freq of the conjugate node
+                for (int j = 0; j < 3; ++j) fm[j] = (f[j] == 0.5) ? 0.5 : -f[j];
+                const double pi2 = 9.8696044010893586188344909998762; // pi^2
+                auto xsym = [&](const XSym &x, const double *ff) -> double {
+                    double sym = 0.0;
+                    if (x.kind == 1) {
+                        for (int j = 0; j < dim; ++j) sym += -4.0 * pi2 * ff[j] * ff[j] * x.K[j * x.dk + j];
+                        for (int j = 0; j < dim; ++j)
+                            for (int k2 = j + 1; k2 < dim; ++k2) sym += -8.0 * pi2 * ff[j] * ff[k2] * x.K[j * x.dk + k2];
+                    } else {
+                        double r2 = 0.0;
+                        for (int j = 0; j < dim; ++j) r2 += ff[j] * ff[j];
+                        const double fr = sqrt(r2), lo = x.threshold / 3.0;
+                        double qv;
+                        if (fr < lo) qv = 0.0;
+                        else if (fr > x.threshold) qv = 1.0;
+                        else {
+                            const double xx = 1.5 * (fr - lo) / x.threshold;
+                            qv = 2.0 * xx * xx - 3.0 * xx * xx * xx;
+                        }
+                        double pw = 1.0;
+                        for (int q = 0; q < x.power; ++q) pw *= fr;
+                        sym = -x.eps * qv * pw;
+                    }
+                    double lapf = 1.0;
+                    for (int q = 0; q < x.lap; ++q) lapf *= (double)mk;
+                    return x.coef * lapf * sym;
+                };
+                double addp = 0.0, addm = 0.0;
+                for (int xi = 0; xi < u.nxs; ++xi) {
+                    addp += xsym(u.xs[xi], f);
+                    addm += xsym(u.xs[xi], fm);
+                }
+                Lm = L + (R)addm;
+                L += (R)addp;
+            }
+            // (c, a) -> c / (1 - a L), or the mean over k and -k where their symbols differ
+            auto implicit_div = [&](V c, R a) -> V {
+                const R d = (R)1 - a * L;
+                if (Lm == L) return cmk<V>(c.x / d, c.y / d);
+                const R r = (R)0.5 * ((R)1 / d + (R)1 / ((R)1 - a * Lm));
+                return cmk<V>(c.x * r, c.y * r);
+            };
             const V c0 = state[gi];
             if (u.etd == 1) { // ImplicitEuler: the explicit RHS at the step's start
                 a.rkF[gi] = nhat;
@@ -466,16 +531,13 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
                 if (u.rk_stage < 4) {
                     a.rkF[gi] = F;
                     const R ay = (R)u.rk_ay;
-                    const R d = (R)1 - (R)u.rk_fden * L;
-                    const V nx = cmk<V>((c0.x + ay * nhat.x) / d, (c0.y + ay * nhat.y) / d);
+                    const V nx = implicit_div(cmk<V>(c0.x + ay * nhat.x, c0.y + ay * nhat.y), (R)u.rk_fden);
                     sm[p * pitch + l] = cmk<V>(nx.x * invN, nx.y * invN);
                     return; // the state changes only in the last stage
                 }
-                const R d = (R)1 - dt * L;
-                cn = cmk<V>(F.x / d, F.y / d);
+                cn = implicit_div(F, dt);
             } else {
-                const R den = (R)1 - dt * L;
-                cn = cmk<V>((c0.x + dt * nhat.x) / den, (c0.y + dt * nhat.y) / den);
+                cn = implicit_div(cmk<V>(c0.x + dt * nhat.x, c0.y + dt * nhat.y), dt);
             }
             if (u.filt) { // ApplyModalFilter (pf/util.go:125-132), Vandeven.Eval (pf/vandeven.go:30-40)
                 const R *__restrict__ tab = static_cast<const R *>(u.filt);

@@ -314,6 +314,11 @@ struct Ctx {
                 kind = 2;
                 return (int)i;
             }
+        for (size_t i = 0; i < d.isym.size(); ++i)
+            if (d.isym[i].name == name) {
+                kind = 4; // implicit user term: its symbol joins the denominator (pf/rhsBuilder.go:39-40)
+                return (int)i;
+            }
         return -1;
     }
 };
@@ -550,6 +555,43 @@ extern "C" int gopf_register_elastic(gopf_ctx *ctx, const char *term, const char
     memcpy(e.C, C81, sizeof(e.C));
     memcpy(e.misfit, misfit9, sizeof(e.misfit));
     ctx->def.elastic.push_back(e);
+    ctx->initialised = false;
+    return GOPF_OK;
+}
+
+// RegisterImplicitTerm(name, &TensorialHessian{K: K}, nil) (pf/tensorialHessian.go:38-80)
+extern "C" int gopf_register_hessian(gopf_ctx *ctx, const char *term, const double *K, int nk)
+{
+    if (!ctx || !term || !*term || !K) return gopf_fail(ctx, GOPF_ERR_ARG, "null argument");
+    if (name_is_reserved(term))
+        return gopf_fail(ctx, GOPF_ERR_ARG, "names may not start with the reserved words -, LAP^4, LAP^2, LAP, *");
+    if (nk != 4 && nk != 9) return gopf_fail(ctx, GOPF_ERR_ARG, "K has 4 (2D) or 9 (3D) entries");
+    gopf_modeldef::ImplicitSym h{};
+    h.name = term;
+    h.kind = 1;
+    h.nk = nk;
+    memcpy(h.K, K, sizeof(double) * (size_t)nk);
+    ctx->def.isym.push_back(h);
+    ctx->initialised = false;
+    return GOPF_OK;
+}
+
+// RegisterImplicitTerm(name, &SpectralViscosity{Eps, DissipationThreshold, Power}, nil)
+// (pf/spectralViscosity.go:22-58)
+extern "C" int gopf_register_spectral_viscosity(gopf_ctx *ctx, const char *term, double eps, double threshold,
+                                                int power)
+{
+    if (!ctx || !term || !*term) return gopf_fail(ctx, GOPF_ERR_ARG, "null argument");
+    if (name_is_reserved(term))
+        return gopf_fail(ctx, GOPF_ERR_ARG, "names may not start with the reserved words -, LAP^4, LAP^2, LAP, *");
+    if (!(threshold > 0.0) || power < 0) return gopf_fail(ctx, GOPF_ERR_ARG, "threshold > 0 and power >= 0 required");
+    gopf_modeldef::ImplicitSym v{};
+    v.name = term;
+    v.kind = 2;
+    v.eps = eps;
+    v.threshold = threshold;
+    v.power = power;
+    ctx->def.isym.push_back(v);
     ctx->initialised = false;
     return GOPF_OK;
 }

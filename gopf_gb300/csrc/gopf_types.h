@@ -79,6 +79,22 @@ struct NoiseParams {
     const unsigned long long *step; // device step counter
 };
 
+// Implicit user terms with a per-frequency symbol (added to the denominator sum L):
+//   kind 1: TensorialHessian (pf/tensorialHessian.go:38-70): sum_j -4 pi^2 f_j^2 K_jj + sum_{j<k} -8 pi^2 f_j f_k K_jk
+//   kind 2: SpectralViscosity (pf/spectralViscosity.go:22-58): -eps * Q(|f|; threshold) * |f|^power
+// f in cycles per sample in the reference's order (row, col, depth); the term's sign and LAP
+// prefixes give coef * m^lap.
+#define GOPF_MAX_XSYM 4
+struct XSym {
+    int kind;
+    double coef;
+    int lap;
+    double K[9];
+    int dk; // 2 or 3: the tensor's dimension
+    double eps, threshold;
+    int power;
+};
+
 // k-space update: c_new = (c + dt * sum_g m^glap[g] U_g) / (1 - dt * sum_p imp[p] m^p),  m = -k^2
 struct UpdTable {
     double dt;
@@ -105,6 +121,9 @@ struct UpdTable {
     // filter(2|f|/pi), a table of nfilt samples on [0, 1] (R elements, device memory)
     const void *filt;
     int nfilt;
+    // implicit user terms beyond the polynomial (generic kernels only)
+    int nxs;
+    XSym xs[GOPF_MAX_XSYM];
 };
 
 // Reduction slots written by the x-pass (FP64, compensated per block)

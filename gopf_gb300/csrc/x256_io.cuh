@@ -72,20 +72,38 @@ __global__ void __launch_bounds__(NT, 3) k_x256_c2r(const XPassArgs<float> a, co
     // v[i] = c(row 2j, col r + 16 i) + i c(row 2j+1, col r + 16 i)
 
     if (a.red) {
-        double vals[RED_SLOTS];
-#pragma unroll
-        for (int s = 0; s < RED_SLOTS; ++s) vals[s] = 0.0;
-        vals[RED_MIN] = INFINITY;
-        vals[RED_MAX] = -INFINITY;
+        // Per thread in FP32 with compensation (GB300's FP64 rate is 1/64 of FP32): Kahan sums of the
+        // values and of their exact squares (v*v plus its FMA residual); FP64 from the block level on.
+        float s = 0.f, sc = 0.f, q = 0.f, qc = 0.f, mn = INFINITY, mx = -INFINITY;
+        int nf = 0;
+        auto kahan = [](float &acc, float &comp, float x) {
+            const float y = x - comp;
+            const float t = acc + y;
+            comp = (t - acc) - y;
+            acc = t;
+        };
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
-            const double c0 = (double)v[i].x, c1 = (double)v[i].y;
-            vals[RED_SUM] += c0 + c1;
-            vals[RED_SUMSQ] += c0 * c0 + c1 * c1;
-            vals[RED_MIN] = fmin(vals[RED_MIN], fmin(c0, c1));
-            vals[RED_MAX] = fmax(vals[RED_MAX], fmax(c0, c1));
-            vals[RED_NONFINITE] += (isfinite(c0) ? 0.0 : 1.0) + (isfinite(c1) ? 0.0 : 1.0);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const float c = h ? v[i].y : v[i].x;
+                kahan(s, sc, c);
+                const float p = c * c;
+                kahan(q, qc, p);
+                qc -= fmaf(c, c, -p); // the square's rounding residual
+                mn = fminf(mn, c);
+                mx = fmaxf(mx, c);
+                nf += isfinite(c) ? 0 : 1;
+            }
         }
+        double vals[RED_SLOTS];
+#pragma unroll
+        for (int k = 0; k < RED_SLOTS; ++k) vals[k] = 0.0;
+        vals[RED_SUM] = (double)s - (double)sc;
+        vals[RED_SUMSQ] = (double)q - (double)qc;
+        vals[RED_MIN] = (double)mn;
+        vals[RED_MAX] = (double)mx;
+        vals[RED_NONFINITE] = (double)nf;
         __shared__ double shred[8 * RED_SLOTS];
         block_reduce_store(vals, a.red, shred);
     }

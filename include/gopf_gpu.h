@@ -139,6 +139,11 @@ int gopf_register_function(gopf_ctx *ctx, const char *name, int kind, const char
 int gopf_register_elastic(gopf_ctx *ctx, const char *term_name, const char *field, const double *C81,
                           const double *misfit9);
 /* NewVolumeConservingLP + RegisterExplicitTerm(term_name, ...) */
+/* Model.RegisterImplicitTerm with a TensorialHessian (pf/tensorialHessian.go:38-80): K has 4 (2D) or
+ * 9 (3D) entries, row-major over the reference's axis order (row, col, depth). */
+int gopf_register_hessian(gopf_ctx *ctx, const char *term_name, const double *K, int nk);
+/* Model.RegisterImplicitTerm with a SpectralViscosity (pf/spectralViscosity.go:22-58). */
+int gopf_register_spectral_viscosity(gopf_ctx *ctx, const char *term_name, double eps, double threshold, int power);
 int gopf_register_volcons(gopf_ctx *ctx, const char *term_name, const char *field, const char *indicator,
                           double dt);
 /* WhiteNoise (pf/noise.go:11-23) registered as a function, or ConservativeNoise

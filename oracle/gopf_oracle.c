@@ -297,7 +297,7 @@ enum {
 };
 
 enum { OR_SRC_NONE = 0, OR_SRC_FIELD = 1, OR_SRC_DERIVED = 2 };
-enum { OR_SPECIAL_NONE = 0, OR_SPECIAL_ELASTIC = 1, OR_SPECIAL_VOLCONS = 2 };
+enum { OR_SPECIAL_NONE = 0, OR_SPECIAL_ELASTIC = 1, OR_SPECIAL_VOLCONS = 2, OR_SPECIAL_HESSIAN = 3, OR_SPECIAL_VISCOSITY = 4 };
 
 #define OR_MAXFAC_D 8
 #define OR_MAXTERMS 64
@@ -322,6 +322,16 @@ typedef struct {
     int lap;   /* LAP power applied to the term (pf/rhsBuilder.go:153-173) */
     int sign_flips; /* prefixes '-' applied after (constructFunc) folded into coef */
 } or_term;
+
+/* implicit user terms: TensorialHessian (pf/tensorialHessian.go:38-70), SpectralViscosity
+ * (pf/spectralViscosity.go:22-58) */
+typedef struct {
+    int kind;
+    double K[9];
+    int nk;
+    double eps, threshold;
+    int power;
+} or_isym;
 
 typedef struct {
     int field;
@@ -357,6 +367,8 @@ typedef struct {
     or_elastic el[OR_MAXSPECIAL];
     int nvc;
     or_volcons vc[OR_MAXSPECIAL];
+    int nis;
+    or_isym is[OR_MAXSPECIAL];
     long current_step;
     double *freq; /* 3 * N cached frequencies */
     double *filter; /* modal filter table (ModalFilter.Eval of a Vandeven-style table), NULL = none */
@@ -734,9 +746,88 @@ static void or_elastic_eval(or_model *m, or_elastic *e, cpx *out)
 }
 
 /* Evaluate one term into out (k space).  Implements ConcreteTerm + constructFunc. */
+/* interpolant (pf/spectralViscosity.go:28-38) */
+double or_sv_interpolant(double f, double peak)
+{
+    const double frac = 1.0 / 3.0;
+    if (f < frac * peak) return 0.0;
+    if (f > peak) return 1.0;
+    const double x = 1.5 * (f - frac * peak) / peak;
+    return 2.0 * x * x - 3.0 * x * x * x;
+}
+
+/* TensorialHessian.GetCoeff (pf/tensorialHessian.go:73-80) */
+static double or_hess_coeff(const or_isym *h, int i, int j)
+{
+    const int d = (h->nk == 9) ? 3 : 2;
+    return h->K[i * d + j];
+}
+
+/* the symbol of an implicit user term at frequency f (reference order: row, col, depth) */
+static double or_isym_eval(const or_model *m, const or_isym *s, const double *f)
+{
+    if (s->kind == OR_SPECIAL_HESSIAN) {
+        double v = 0.0;
+        const int dim = m->ndim;
+        for (int j = 0; j < dim; ++j) v += -4.0 * OR_PI * OR_PI * f[j] * f[j] * or_hess_coeff(s, j, j);
+        for (int j = 0; j < dim; ++j)
+            for (int k = j + 1; k < dim; ++k) v += -8.0 * OR_PI * OR_PI * f[j] * f[k] * or_hess_coeff(s, j, k);
+        return v;
+    }
+    double r2 = 0.0;
+    for (int j = 0; j < m->ndim; ++j) r2 += f[j] * f[j];
+    const double fr = sqrt(r2);
+    return -s->eps * or_sv_interpolant(fr, s->threshold) * pow(fr, (double)s->power);
+}
+
+int or_add_hessian(or_model *m, int eq, const double *K, int nk, double coef_re, int lap)
+{
+    if (m->nis >= OR_MAXSPECIAL || m->nterms >= OR_MAXTERMS || (nk != 4 && nk != 9)) return -1;
+    or_isym *h = &m->is[m->nis];
+    memset(h, 0, sizeof(*h));
+    h->kind = OR_SPECIAL_HESSIAN;
+    h->nk = nk;
+    memcpy(h->K, K, sizeof(double) * (size_t)nk);
+    or_term *t = &m->terms[m->nterms++];
+    memset(t, 0, sizeof(*t));
+    t->eq = eq;
+    t->implicit = 1;
+    t->special = OR_SPECIAL_HESSIAN;
+    t->special_idx = m->nis++;
+    t->coef = coef_re;
+    t->lap = lap;
+    return 0;
+}
+
+int or_add_viscosity(or_model *m, int eq, double eps, double threshold, int power, double coef_re, int lap)
+{
+    if (m->nis >= OR_MAXSPECIAL || m->nterms >= OR_MAXTERMS) return -1;
+    or_isym *v = &m->is[m->nis];
+    memset(v, 0, sizeof(*v));
+    v->kind = OR_SPECIAL_VISCOSITY;
+    v->eps = eps;
+    v->threshold = threshold;
+    v->power = power;
+    or_term *t = &m->terms[m->nterms++];
+    memset(t, 0, sizeof(*t));
+    t->eq = eq;
+    t->implicit = 1;
+    t->special = OR_SPECIAL_VISCOSITY;
+    t->special_idx = m->nis++;
+    t->coef = coef_re;
+    t->lap = lap;
+    return 0;
+}
+
 static void or_term_eval(or_model *m, const or_term *t, cpx *out)
 {
     long N = m->N;
+    if (t->special == OR_SPECIAL_HESSIAN || t->special == OR_SPECIAL_VISCOSITY) {
+        const or_isym *s = &m->is[t->special_idx];
+        for (long i = 0; i < N; ++i)
+            out[i] = t->coef * or_isym_eval(m, s, m->freq + 3 * i) * or_lap_symbol(m->freq + 3 * i, t->lap);
+        return;
+    }
     if (t->special == OR_SPECIAL_ELASTIC) {
         or_elastic_eval(m, &m->el[t->special_idx], out);
         for (long i = 0; i < N; ++i) out[i] *= t->coef * or_lap_symbol(m->freq + 3 * i, t->lap);

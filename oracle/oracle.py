@@ -86,6 +86,13 @@ def lib():
         L.or_uniform_field.argtypes = [ctypes.c_uint64, ctypes.c_long, ctypes.c_double, ctypes.c_double, dp]
         L.or_num_threads.restype = ctypes.c_int
         L.or_set_num_threads.argtypes = [ctypes.c_int]
+        L.or_add_hessian.argtypes = [vp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+        L.or_add_hessian.restype = ctypes.c_int
+        L.or_add_viscosity.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                       ctypes.c_double, ctypes.c_int]
+        L.or_add_viscosity.restype = ctypes.c_int
+        L.or_sv_interpolant.argtypes = [ctypes.c_double, ctypes.c_double]
+        L.or_sv_interpolant.restype = ctypes.c_double
         L.or_vandeven_table.argtypes = [ctypes.c_int, dp, ctypes.c_int]
         L.or_vandeven_table.restype = ctypes.c_int
         L.or_filter_eval.argtypes = [dp, ctypes.c_int, ctypes.c_double]
@@ -143,6 +150,11 @@ def vandeven(order: int) -> np.ndarray:
     if lib().or_vandeven_table(int(order), _dp(out), 1000) != 0:
         raise ValueError("bad order")
     return out
+
+
+def sv_interpolant(f: float, peak: float) -> float:
+    """interpolant (pf/spectralViscosity.go:28-38)."""
+    return float(lib().or_sv_interpolant(float(f), float(peak)))
 
 
 def filter_eval(table: np.ndarray, x: float) -> float:
@@ -243,6 +255,18 @@ class Model:
 
     def volcons_multiplier(self, v: int) -> float:
         return float(self._L.or_volcons_multiplier(self._h, v))
+
+    def add_hessian(self, eq: int, K, coef: float = 1.0, lap: int = 0) -> None:
+        """RegisterImplicitTerm with a TensorialHessian (pf/tensorialHessian.go)."""
+        k = np.ascontiguousarray(K, dtype=np.float64).reshape(-1)
+        if self._L.or_add_hessian(self._h, eq, _dp(k), k.size, coef, lap) != 0:
+            raise ValueError("bad hessian")
+
+    def add_viscosity(self, eq: int, eps: float, threshold: float, power: int, coef: float = 1.0,
+                      lap: int = 0) -> None:
+        """RegisterImplicitTerm with a SpectralViscosity (pf/spectralViscosity.go)."""
+        if self._L.or_add_viscosity(self._h, eq, eps, threshold, power, coef, lap) != 0:
+            raise ValueError("bad viscosity term")
 
     def set_filter(self, table) -> None:
         """Euler.SetFilter / RK4.SetFilter with a tabulated filter (None removes it)."""
