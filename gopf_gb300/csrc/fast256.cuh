@@ -518,6 +518,48 @@ template <typename F> __device__ __forceinline__ float polyf(const PwTable &pw, 
     return acc;
 }
 
+// Rows 2j and 2j+1 of a [129 kx][32 y] half-spectrum tile as one complex line a + i b of 256
+// columns, Hermitian-extended: column k holds A(k) + i B(k) for k <= 128 and
+// conj A(256 - k) + i conj B(256 - k) above.  k = r + 16 i is <= 128 exactly when i < 8, or i == 8
+// and r == 0, so only i == 8 needs a (uniform-cost) select.
+__device__ __forceinline__ void load_pair_line(const float2 *__restrict__ t, int r, int j, float2 (&v)[16])
+{
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int k = r + 16 * i;
+        if (i < 8) {
+            const float4 ab = *reinterpret_cast<const float4 *>(&t[k * XROWS + 2 * j]);
+            v[i] = make_float2(ab.x - ab.w, ab.y + ab.z);
+        } else if (i > 8) {
+            const float4 ab = *reinterpret_cast<const float4 *>(&t[(N - k) * XROWS + 2 * j]);
+            v[i] = make_float2(ab.x + ab.w, -ab.y + ab.z);
+        } else {
+            const bool lo = (r == 0);
+            const float4 ab = *reinterpret_cast<const float4 *>(&t[(lo ? 128 : N - k) * XROWS + 2 * j]);
+            v[i] = lo ? make_float2(ab.x - ab.w, ab.y + ab.z) : make_float2(ab.x + ab.w, -ab.y + ab.z);
+        }
+    }
+}
+
+// Separation of a transformed row pair Z = FFT(a + i b) into the rows' half spectra,
+// X_a(k) = (Z(k) + conj Z(-k))/2 (row 2p) and X_b(k) = (Z(k) - conj Z(-k))/(2i) (row 2p + 1),
+// from the exchange slots z[k*16 + p] into the output tile o[kx][32].  A thread takes pair
+// p = tid % 16 at kx = tid/16 + 16 q and writes both rows with one 16-byte store; kx = 128 falls
+// to the first 16 threads.
+__device__ __forceinline__ void separate_pairs(const float2 *__restrict__ z, float2 *__restrict__ o, int tid)
+{
+    const int p = tid & 15, k0 = tid >> 4;
+    auto one = [&](int kx) {
+        const float2 P = z[kx * 16 + p];
+        const float2 Q = z[((N - kx) & (N - 1)) * 16 + p];
+        *reinterpret_cast<float4 *>(&o[kx * XROWS + 2 * p]) =
+            make_float4(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y), 0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
+    };
+#pragma unroll
+    for (int q = 0; q < 8; ++q) one(k0 + 16 * q);
+    if (k0 == 0) one(128);
+}
+
 // Pointwise polynomial of the packed row pair, forward transform and separation
 // of the two rows' half spectra into out[grp] (v is overwritten).
 template <typename AT>
@@ -588,17 +630,7 @@ __global__ void __launch_bounds__(NT, 2) k_x256(const XPassArgs<float> a)
     __syncthreads();
     // Hermitian extension, rows (2j, 2j+1) packed as a + i b
     float2 v[16];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) {
-        const int k = r + 16 * i;
-        if (k <= 128) {
-            const float4 ab = *reinterpret_cast<const float4 *>(&s_x[k * XROWS + 2 * j]);
-            v[i] = make_float2(ab.x - ab.w, ab.y + ab.z);
-        } else {
-            const float4 ab = *reinterpret_cast<const float4 *>(&s_x[(N - k) * XROWS + 2 * j]);
-            v[i] = make_float2(ab.x + ab.w, -ab.y + ab.z);
-        }
-    }
+    load_pair_line(s_x, r, j, v);
     __syncthreads();
     auto at = [&](int x, int y) -> float2 & { return s_x[(x * 16 + y) * 16 + j]; };
     fft256<true>(v, r, s_tw, at);
@@ -856,24 +888,13 @@ __global__ void __launch_bounds__(NT, 3)
 
     // Hermitian extension, rows (2j, 2j+1) packed as a + i b
     float2 v[16];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) {
-        const int k = r + 16 * i;
-        if (k <= 128) {
-            const float4 ab = *reinterpret_cast<const float4 *>(&s_x[k * XROWS + 2 * j]);
-            v[i] = make_float2(ab.x - ab.w, ab.y + ab.z);
-        } else {
-            const float4 ab = *reinterpret_cast<const float4 *>(&s_x[(N - k) * XROWS + 2 * j]);
-            v[i] = make_float2(ab.x + ab.w, -ab.y + ab.z);
-        }
-    }
+    load_pair_line(s_x, r, j, v);
     __syncthreads();
     auto at = [&](int x, int y) -> float2 & { return s_x[(x * 16 + y) * 16 + j]; };
     fft256<true>(v, r, s_tw, at);
     // v[i] = c(row 2j, col r + 16 i) + i c(row 2j+1, col r + 16 i)
 
     const int ng = (NG == 1) ? 1 : a.ngrp_out;
-    const int yy = tid & 31, jj = yy >> 1, odd = yy & 1, kx0 = tid >> 5;
     for (int grp = 0; grp < ng; ++grp) {
         float2 w[16];
 #pragma unroll
@@ -885,18 +906,7 @@ __global__ void __launch_bounds__(NT, 3)
         if (grp > 0 && tid == 0) bulk_wait_read_all(); // the previous group's store has read s_o
         __syncthreads();
         // separation: X_a(k) = (Z(k) + conj Z(-k))/2 (even rows), X_b(k) = (Z(k) - conj Z(-k))/(2i) (odd rows)
-#pragma unroll 4
-        for (int q = 0; q < 17; ++q) {
-            const int kx = kx0 + 8 * q;
-            if (kx <= 128) {
-                const float2 P = s_x[kx * 16 + jj];
-                const float2 Q = s_x[((N - kx) & (N - 1)) * 16 + jj];
-                float2 o;
-                if (!odd) o = make_float2(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y));
-                else o = make_float2(0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
-                s_o[kx * XROWS + yy] = o;
-            }
-        }
+        separate_pairs(s_x, s_o, tid);
         fence_async_smem();
         __syncthreads();
         if (tid == 0) {

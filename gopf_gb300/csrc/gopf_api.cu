@@ -276,6 +276,9 @@ static void ctx_free(gopf_ctx *ctx)
     for (void *p : more)
         if (p) cudaFree(p);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
 }
 
 extern "C" int gopf_ctx_create(int ndim, const int *domain_size, int precision, int device, gopf_ctx **out)
@@ -326,6 +329,9 @@ extern "C" int gopf_ctx_create(int ndim, const int *domain_size, int precision, 
     if (device < 0) return GOPF_OK; // host-only: equations can be defined and compiled, nothing runs
     if ((rc = set_device(ctx))) return rc;
     cudaError_t e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamCreate");
     ctx->stream = ctx->own_stream;
     rc = (precision == GOPF_FP32) ? ctx_alloc<float>(ctx) : ctx_alloc<double>(ctx);
@@ -924,7 +930,17 @@ template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx, bool first
     fa.tout = T;
     fa.upd = u;
     LK(is3d ? launch_spass<R>(fa, ctx->LBz, ctx->stream) : launch_cpass<R>(fa, ctx->LBy, ctx->stream));
-    LK(gopf_launch_hermitian_planes(ctx, ctx->d_state));
+    // The projection touches only c-hat, the inverse y pass only T: outside per-kernel profiling
+    // they run as two branches (a fork/join that a captured graph keeps).
+    const bool fork = is3d && !to_plane && !ctx->prof_events;
+    if (fork) {
+        LK(cudaEventRecord(ctx->ev_fork, ctx->stream));
+        LK(cudaStreamWaitEvent(ctx->side_stream, ctx->ev_fork, 0));
+        LK(gopf_launch_hermitian_planes(ctx, ctx->d_state, ctx->side_stream));
+        LK(cudaEventRecord(ctx->ev_join, ctx->side_stream));
+    } else {
+        LK(gopf_launch_hermitian_planes(ctx, ctx->d_state));
+    }
     if (is3d && !to_plane) {
         PassArgs<R> ia = pargs<R>(ctx, false);
         ia.mode = PM_INV;
@@ -932,6 +948,7 @@ template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx, bool first
         ia.nbuf = 1;
         LK(launch_cpass<R>(ia, ctx->LBy, ctx->stream));
     }
+    if (fork) LK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
     return cudaSuccess;
 }
 
@@ -1115,6 +1132,7 @@ template <typename R> static int download_impl(gopf_ctx *ctx, double *data, bool
 static int transfer(gopf_ctx *ctx, int field, double *data, size_t n, bool up, bool cplx)
 {
     if (!ctx || !data) return gopf_fail(ctx, GOPF_ERR_ARG, "null argument");
+    gopf_nvtx_scope trace(up ? "gopf_field_upload" : "gopf_field_download");
     int rc;
     if ((rc = require_ready(ctx, field))) return rc;
     if ((long long)n != ctx->g.N)
@@ -1198,6 +1216,7 @@ static int check_finite_state(gopf_ctx *ctx)
 extern "C" int gopf_reduce(gopf_ctx *ctx, int field, int what, double *out)
 {
     if (!ctx || !out) return gopf_fail(ctx, GOPF_ERR_ARG, "null argument");
+    gopf_nvtx_scope trace("gopf_reduce");
     int rc;
     if ((rc = require_ready(ctx, field))) return rc;
     if (what < 0 || what > GOPF_RED_NONFINITE) return gopf_fail(ctx, GOPF_ERR_ARG, "unknown reduction");
@@ -1216,6 +1235,7 @@ extern "C" int gopf_reduce(gopf_ctx *ctx, int field, int what, double *out)
 extern "C" int gopf_step(gopf_ctx *ctx, long long nsteps)
 {
     if (!ctx) return GOPF_ERR_ARG;
+    gopf_nvtx_scope trace("gopf_step");
     if (nsteps < 0) return gopf_fail(ctx, GOPF_ERR_ARG, "negative step count");
     if (!ctx->initialised) return gopf_fail(ctx, GOPF_ERR_STATE, "model not initialised (gopf_init/gopf_set_terms)");
     if (!(ctx->dt > 0.0)) return gopf_fail(ctx, GOPF_ERR_STATE, "no stepper set (gopf_set_stepper)");

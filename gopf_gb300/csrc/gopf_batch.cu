@@ -53,9 +53,9 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2))
         __syncthreads();
         const int2 it = items[w];
         const BatchInst<R> &b = inst[it.x];
-        if (b.lby == 16) pass_tile<R, 16, 16, true>(b.pa, it.y, 0);
-        else if (b.lby == 8) pass_tile<R, 8, 16, true>(b.pa, it.y, 0);
-        else pass_tile<R, 4, 16, true>(b.pa, it.y, 0);
+        if (b.lby == 16) pass_tile<R, 16, 16, true, false>(b.pa, it.y, 0);
+        else if (b.lby == 8) pass_tile<R, 8, 16, true, false>(b.pa, it.y, 0);
+        else pass_tile<R, 4, 16, true, false>(b.pa, it.y, 0);
     }
 }
 

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "../../include/gopf_gpu.h"
 #include "gopf_types.h"
@@ -78,6 +79,8 @@ struct gopf_ctx {
     gopf::Geom g{};
     int LBx = 16, LBy = 16, LBz = 16; // tile widths of the x, y and z passes
     cudaStream_t own_stream = nullptr;
+    cudaStream_t side_stream = nullptr;        // second branch of a step (Hermitian projection)
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaStream_t stream = nullptr;
 
     // device buffers (element type float2/double2 for spectral, float/double for real)
@@ -174,4 +177,11 @@ int gopf_fail(gopf_ctx *ctx, int code, const std::string &msg);
 int gopf_compile_model(gopf_ctx *ctx);
 int gopf_elastic_table(gopf_ctx *ctx);
 cudaError_t gopf_launch_volcons_finalize(gopf_ctx *ctx);
-cudaError_t gopf_launch_hermitian_planes(gopf_ctx *ctx, void *state);
+cudaError_t gopf_launch_hermitian_planes(gopf_ctx *ctx, void *state, cudaStream_t st = nullptr);
+
+// NVTX range for the lifetime of a scope (a host-side trace marker; a no-op unless a profiler
+// or tracer is attached)
+struct gopf_nvtx_scope {
+    explicit gopf_nvtx_scope(const char *name) { nvtxRangePushA(name); }
+    ~gopf_nvtx_scope() { nvtxRangePop(); }
+};

@@ -291,6 +291,7 @@ int stencil_weights(int pts, double *w)
 // One ImplicitEuler step of the context's single field.
 int gopf_ie_step(gopf_ctx *ctx)
 {
+    gopf_nvtx_scope trace("implicit_euler_step");
     int rc;
     if ((rc = ie_alloc(ctx))) return rc;
     gopf_ie_work *ws = ctx->ie;

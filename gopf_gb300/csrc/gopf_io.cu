@@ -104,6 +104,7 @@ extern "C" int gopf_save_float64(gopf_ctx *ctx, int field, const char *path, int
     if (!ctx || !path) return GOPF_ERR_ARG;
     if (field != 0) return gopf_fail(ctx, GOPF_ERR_ARG, "bad field id");
     if (!ctx->state_valid) return gopf_fail(ctx, GOPF_ERR_STATE, "field has not been uploaded");
+    gopf_nvtx_scope trace("gopf_save_float64");
     int rc;
     if ((rc = join_writer(ctx))) return rc; // the staging buffer is free again
     if (cudaSetDevice(ctx->device) != cudaSuccess) return gopf_fail(ctx, GOPF_ERR_CUDA, "cudaSetDevice");

@@ -303,7 +303,9 @@ template <int LB, bool CONTIG, typename F> __device__ __forceinline__ void tile_
 
 // One tile of a y (CONTIG) or z pass: LB lines starting at line tile*LB;
 // bsel selects the buffer in the FWD/INV modes.
-template <typename R, int LB, int PERB, bool CONTIG>
+// EXTRA = false compiles the plain Euler update only (no noise, modal filter, implicit user
+// terms, RK4 stages or ImplicitEuler modes): the batched sweep, which rejects those, uses it.
+template <typename R, int LB, int PERB, bool CONTIG, bool EXTRA = true>
 __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, int bsel)
 {
     typedef typename VecOf<R>::type V;
@@ -410,7 +412,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
                 nhat.x += f * tv.x;
                 nhat.y += f * tv.y;
             }
-            if (u.noise.kind) {
+            if (EXTRA && u.noise.kind) {
                 long long kx, yy, zz;
                 if (CONTIG) {
                     const long long q = l0 + l;
@@ -436,7 +438,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
             // part; the real field is the Hermitian part of its step, i.e. the update divides by
             // the mean of 1/(1 - a L(k)) and 1/(1 - a L(-k)).  Lm is L(-k); Lm == L elsewhere.
             R Lm = L;
-            if (u.nxs) { // implicit user terms with a per-frequency symbol (XSym)
+            if (EXTRA && u.nxs) { // implicit user terms with a per-frequency symbol (XSym)
                 long long kx, yy, zz;
                 if (CONTIG) {
                     const long long q = l0 + l;
@@ -497,12 +499,12 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
                 return cmk<V>(c.x * r, c.y * r);
             };
             const V c0 = state[gi];
-            if (u.etd == 1) { // ImplicitEuler: the explicit RHS at the step's start
+            if (EXTRA && u.etd == 1) { // ImplicitEuler: the explicit RHS at the step's start
                 a.rkF[gi] = nhat;
                 sm[p * pitch + l] = zero;
                 return;
             }
-            if (u.etd == 2) {
+            if (EXTRA && u.etd == 2) {
                 // ImplicitEuler residual (pf/implicitEuler.go:68-94): c_n e^(L dt) + integral of the RHS
                 // interpolated linearly between N_n and N(x) (nonlinearIntegral, :151-162), in FP64
                 const double Ld = (double)L, dtd = u.dt;
@@ -524,7 +526,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
                 sm[p * pitch + l] = cmk<V>((R)(rr * u.invN), (R)(ri * u.invN));
                 return;
             }
-            if (u.rk_stage > 0) {
+            if (EXTRA && u.rk_stage > 0) {
                 const R af = (R)u.rk_afin;
                 V F = (u.rk_stage == 1) ? c0 : a.rkF[gi];
                 F = cmk<V>(F.x + af * nhat.x, F.y + af * nhat.y);
@@ -539,7 +541,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
             } else {
                 cn = implicit_div(cmk<V>(c0.x + dt * nhat.x, c0.y + dt * nhat.y), dt);
             }
-            if (u.filt) { // ApplyModalFilter (pf/util.go:125-132), Vandeven.Eval (pf/vandeven.go:30-40)
+            if (EXTRA && u.filt) { // ApplyModalFilter (pf/util.go:125-132), Vandeven.Eval (pf/vandeven.go:30-40)
                 const R *__restrict__ tab = static_cast<const R *>(u.filt);
                 const int nf = u.nfilt;
                 const R x = sqrt(fline[l] + fpos[p]) * (R)0.63661977236758134307553505349006;

@@ -170,13 +170,14 @@ template <typename V> __global__ void k_hermitian_planes(V *__restrict__ c, Geom
 
 using namespace gopf;
 
-cudaError_t gopf_launch_hermitian_planes(gopf_ctx *ctx, void *state)
+cudaError_t gopf_launch_hermitian_planes(gopf_ctx *ctx, void *state, cudaStream_t st)
 {
     const long long n = 2LL * ctx->g.Y * ctx->g.Z;
     const unsigned blocks = (unsigned)std::min<long long>((n + 255) / 256, 152 * 8);
     unsigned long long *ctr = (state == ctx->d_state && ctx->noise.kind) ? ctx->d_stepctr : nullptr;
-    if (ctx->prec == GOPF_FP32) k_hermitian_planes<float2><<<blocks, 256, 0, ctx->stream>>>((float2 *)state, ctx->g, ctr);
-    else k_hermitian_planes<double2><<<blocks, 256, 0, ctx->stream>>>((double2 *)state, ctx->g, ctr);
+    if (!st) st = ctx->stream;
+    if (ctx->prec == GOPF_FP32) k_hermitian_planes<float2><<<blocks, 256, 0, st>>>((float2 *)state, ctx->g, ctr);
+    else k_hermitian_planes<double2><<<blocks, 256, 0, st>>>((double2 *)state, ctx->g, ctr);
     return cudaGetLastError();
 }
 

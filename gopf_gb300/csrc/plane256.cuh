@@ -144,17 +144,7 @@ __global__ void __cluster_dims__(PL_CLUSTER, 1, 1) __launch_bounds__(NT, 3) k_pl
     {
         const int j = tid & 15, r = tid >> 4;
         float2 v[16];
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-            const int k = r + 16 * i;
-            if (k <= 128) {
-                const float4 ab = *reinterpret_cast<const float4 *>(&Rx[k * XROWS + 2 * j]);
-                v[i] = make_float2(ab.x - ab.w, ab.y + ab.z);
-            } else {
-                const float4 ab = *reinterpret_cast<const float4 *>(&Rx[(N - k) * XROWS + 2 * j]);
-                v[i] = make_float2(ab.x + ab.w, -ab.y + ab.z);
-            }
-        }
+        load_pair_line(Rx, r, j, v);
         auto at = [&](int x, int y) -> float2 & { return tA[(x * 16 + y) * 16 + j]; };
         fft256<true>(v, r, s_tw, at);
         if (!a.identity) apply_poly(v, a, 0, s_poly);

@@ -55,17 +55,7 @@ __global__ void __launch_bounds__(NT, 3) k_x256_c2r(const XPassArgs<float> a, co
     if (!*s_ok) return;
 
     float2 v[16];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) {
-        const int k = r + 16 * i;
-        if (k <= 128) {
-            const float4 ab = *reinterpret_cast<const float4 *>(&s_x[k * XROWS + 2 * j]);
-            v[i] = make_float2(ab.x - ab.w, ab.y + ab.z);
-        } else {
-            const float4 ab = *reinterpret_cast<const float4 *>(&s_x[(N - k) * XROWS + 2 * j]);
-            v[i] = make_float2(ab.x + ab.w, -ab.y + ab.z);
-        }
-    }
+    load_pair_line(s_x, r, j, v);
     __syncthreads();
     auto at = [&](int x, int y) -> float2 & { return s_x[(x * 16 + y) * 16 + j]; };
     fft256<true>(v, r, s_tw, at);
@@ -157,7 +147,6 @@ __global__ void __launch_bounds__(NT, 3)
     auto at = [&](int x, int y) -> float2 & { return s_x[(x * 16 + y) * 16 + j]; };
 
     const int ng = (NG == 1) ? 1 : a.ngrp_out;
-    const int yy = tid & 31, jj = yy >> 1, odd = yy & 1, kx0 = tid >> 5;
     for (int grp = 0; grp < ng; ++grp) {
         float2 w[16];
 #pragma unroll
@@ -168,18 +157,7 @@ __global__ void __launch_bounds__(NT, 3)
         for (int i = 0; i < 16; ++i) s_x[(r + 16 * i) * 16 + j] = w[i];
         if (grp > 0 && tid == 0) bulk_wait_read_all(); // the previous group's store has read s_o
         __syncthreads();
-#pragma unroll 4
-        for (int q = 0; q < 17; ++q) {
-            const int kx = kx0 + 8 * q;
-            if (kx <= 128) {
-                const float2 P = s_x[kx * 16 + jj];
-                const float2 Q = s_x[((N - kx) & (N - 1)) * 16 + jj];
-                float2 o;
-                if (!odd) o = make_float2(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y));
-                else o = make_float2(0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
-                s_o[kx * XROWS + yy] = o;
-            }
-        }
+        separate_pairs(s_x, s_o, tid);
         fence_async_smem();
         __syncthreads();
         if (tid == 0) {
