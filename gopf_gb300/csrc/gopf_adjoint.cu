@@ -293,15 +293,15 @@ extern "C" int gopf_adjoint_forward(gopf_ctx *ctx, double gamma, double M, doubl
     if (st->nckpt < nck || st->every != every) {
         if (st->d_ckpt) cudaFree(st->d_ckpt);
         if (st->d_seg) cudaFree(st->d_seg);
-        ACK(cudaMalloc(&st->d_ckpt, rb * nck));
-        ACK(cudaMalloc(&st->d_seg, rb * (every + 1)));
+        ACK(gopf_malloc(&st->d_ckpt, rb * nck));
+        ACK(gopf_malloc(&st->d_seg, rb * (every + 1)));
         st->nckpt = nck;
     }
     for (int i = 0; i < 4; ++i)
-        if (!st->d_r[i]) ACK(cudaMalloc(&st->d_r[i], rb));
+        if (!st->d_r[i]) ACK(gopf_malloc(&st->d_r[i], rb));
     for (int i = 0; i < 3; ++i)
-        if (!st->d_s[i]) ACK(cudaMalloc(&st->d_s[i], sb));
-    if (!st->d_sums) ACK(cudaMalloc(&st->d_sums, 2 * sizeof(double)));
+        if (!st->d_s[i]) ACK(gopf_malloc(&st->d_s[i], sb));
+    if (!st->d_sums) ACK(gopf_malloc(&st->d_sums, 2 * sizeof(double)));
     st->nsteps = nsteps;
     st->every = every;
     st->gamma = gamma;

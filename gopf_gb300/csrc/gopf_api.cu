@@ -1,6 +1,8 @@
 // gopf_api.cu -- C ABI of the GB300 spectral stepper: contexts, device
 // buffers, plans, the step sequence and its CUDA-graph replay.
 #include <algorithm>
+#include <atomic>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -94,7 +96,7 @@ template <typename R> static int upload_table(gopf_ctx *ctx, int n, void **dptr)
         h[t].x = (R)cosl(ang);
         h[t].y = (R)sinl(ang);
     }
-    CK(cudaMalloc(dptr, sizeof(V) * n));
+    CK(gopf_malloc(dptr, sizeof(V) * n));
     ctx->dev_bytes += sizeof(V) * n;
     CK(cudaMemcpy(*dptr, h.data(), sizeof(V) * n, cudaMemcpyHostToDevice));
     return GOPF_OK;
@@ -203,6 +205,23 @@ template <typename R> __global__ void k_count_nonfinite(const R *__restrict__ x,
     if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
 }
 
+cudaError_t gopf_malloc(void **p, size_t bytes)
+{
+    static std::atomic<long long> countdown{-2}; // -2: not read yet, -1: hook off
+    long long c = countdown.load();
+    if (c == -2) {
+        const char *e = std::getenv("GOPF_TEST_FAIL_ALLOC");
+        const long long k = e ? std::atoll(e) : 0;
+        long long expect = -2;
+        countdown.compare_exchange_strong(expect, k > 0 ? k : -1);
+    }
+    if (countdown.load() > 0 && countdown.fetch_sub(1) == 1) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes);
+}
+
 static unsigned ew_blocks(long long n)
 {
     long long b = (n + 255) / 256;
@@ -235,15 +254,15 @@ template <typename R> static int ctx_alloc(gopf_ctx *ctx)
 {
     typedef typename VecOf<R>::type V;
     const Geom &g = ctx->g;
-    CK(cudaMalloc(&ctx->d_state, sizeof(V) * g.C));
-    CK(cudaMalloc(&ctx->d_T, sizeof(V) * g.C));
-    CK(cudaMalloc(&ctx->d_real, sizeof(R) * g.N));
-    CK(cudaMalloc(&ctx->d_c128, sizeof(double2) * g.N));
+    CK(gopf_malloc(&ctx->d_state, sizeof(V) * g.C));
+    CK(gopf_malloc(&ctx->d_T, sizeof(V) * g.C));
+    CK(gopf_malloc(&ctx->d_real, sizeof(R) * g.N));
+    CK(gopf_malloc(&ctx->d_c128, sizeof(double2) * g.N));
     ctx->dev_bytes += 2 * sizeof(V) * g.C + sizeof(R) * g.N + sizeof(double2) * g.N;
     ctx->nred_blocks = ((g.Y + ctx->LBx - 1) / ctx->LBx) * g.Z;
-    CK(cudaMalloc(&ctx->d_red, sizeof(double) * RED_SLOTS * ctx->nred_blocks));
-    CK(cudaMalloc(&ctx->d_redout, sizeof(double) * RED_SLOTS));
-    CK(cudaMalloc(&ctx->d_status, 2 * sizeof(unsigned))); // [0] status word, [1] non-finite count
+    CK(gopf_malloc(&ctx->d_red, sizeof(double) * RED_SLOTS * ctx->nred_blocks));
+    CK(gopf_malloc(&ctx->d_redout, sizeof(double) * RED_SLOTS));
+    CK(gopf_malloc(&ctx->d_status, 2 * sizeof(unsigned))); // [0] status word, [1] non-finite count
     CK(cudaMemset(ctx->d_status, 0, 2 * sizeof(unsigned)));
     ctx->dev_bytes += sizeof(double) * RED_SLOTS * (ctx->nred_blocks + 1) + sizeof(unsigned);
     CK(cudaMemset(ctx->d_state, 0, sizeof(V) * g.C));
@@ -454,8 +473,8 @@ static int alloc_spectral(gopf_ctx *ctx, void **p)
 {
     if (ctx->device < 0 || *p) return GOPF_OK;
     const size_t vb = (ctx->prec == GOPF_FP32) ? sizeof(float2) : sizeof(double2);
-    cudaError_t e = cudaMalloc(p, vb * ctx->g.C);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(work buffer)");
+    cudaError_t e = gopf_malloc(p, vb * ctx->g.C);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "gopf_malloc(work buffer)");
     ctx->dev_bytes += vb * ctx->g.C;
     return GOPF_OK;
 }
@@ -599,7 +618,7 @@ int gopf_compile_model(gopf_ctx *ctx)
     u.nimp = maxp;
     if (noise.kind && ctx->device >= 0) {
         if (!ctx->d_stepctr) {
-            CK(cudaMalloc(&ctx->d_stepctr, sizeof(unsigned long long)));
+            CK(gopf_malloc(&ctx->d_stepctr, sizeof(unsigned long long)));
             ctx->dev_bytes += sizeof(unsigned long long);
         }
         CK(cudaMemset(ctx->d_stepctr, 0, sizeof(unsigned long long)));
@@ -636,8 +655,8 @@ int gopf_compile_model(gopf_ctx *ctx)
         }
         if (ctx->has_volcons) {
             if (!ctx->d_vc) {
-                CK(cudaMalloc(&ctx->d_vc, sizeof(double) * 8));
-                CK(cudaMalloc(&ctx->d_red2, sizeof(double) * RED_SLOTS * ctx->nred_blocks));
+                CK(gopf_malloc(&ctx->d_vc, sizeof(double) * 8));
+                CK(gopf_malloc(&ctx->d_red2, sizeof(double) * RED_SLOTS * ctx->nred_blocks));
                 ctx->dev_bytes += sizeof(double) * (8 + RED_SLOTS * ctx->nred_blocks);
             }
             CK(cudaMemset(ctx->d_vc, 0, sizeof(double) * 8));
@@ -1481,7 +1500,7 @@ extern "C" int gopf_set_modal_filter(gopf_ctx *ctx, const double *table, int n)
         ctx->d_filter = nullptr;
     }
     const size_t eb = (ctx->prec == GOPF_FP32) ? sizeof(float) : sizeof(double);
-    CK(cudaMalloc(&ctx->d_filter, eb * (size_t)n));
+    CK(gopf_malloc(&ctx->d_filter, eb * (size_t)n));
     if (ctx->prec == GOPF_FP32) {
         std::vector<float> t(table, table + n);
         CK(cudaMemcpy(ctx->d_filter, t.data(), eb * (size_t)n, cudaMemcpyHostToDevice));

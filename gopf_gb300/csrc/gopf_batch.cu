@@ -180,10 +180,10 @@ template <typename R> static int batch_build(gopf_batch *b)
     b->nx = (int)xi.size();
     b->ny = (int)yi.size();
     b->herm_total = hoff;
-    BCK(cudaMalloc(&b->d_inst, sizeof(BatchInst<R>) * inst.size()));
+    BCK(gopf_malloc(&b->d_inst, sizeof(BatchInst<R>) * inst.size()));
     BCK(cudaMemcpy(b->d_inst, inst.data(), sizeof(BatchInst<R>) * inst.size(), cudaMemcpyHostToDevice));
-    BCK(cudaMalloc(&b->d_xitems, sizeof(int2) * std::max(1, b->nx)));
-    BCK(cudaMalloc(&b->d_yitems, sizeof(int2) * std::max(1, b->ny)));
+    BCK(gopf_malloc(&b->d_xitems, sizeof(int2) * std::max(1, b->nx)));
+    BCK(gopf_malloc(&b->d_yitems, sizeof(int2) * std::max(1, b->ny)));
     BCK(cudaMemcpy(b->d_xitems, xi.data(), sizeof(int2) * b->nx, cudaMemcpyHostToDevice));
     BCK(cudaMemcpy(b->d_yitems, yi.data(), sizeof(int2) * b->ny, cudaMemcpyHostToDevice));
     BCK(cudaFuncSetAttribute(k_batch_xpass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, b->smem_x));

@@ -185,3 +185,12 @@ struct gopf_nvtx_scope {
     explicit gopf_nvtx_scope(const char *name) { nvtxRangePushA(name); }
     ~gopf_nvtx_scope() { nvtxRangePop(); }
 };
+
+// cudaMalloc for the library's device buffers.  Test hook: when the environment variable
+// GOPF_TEST_FAIL_ALLOC=k is set, the k-th allocation of the process fails with
+// cudaErrorMemoryAllocation (host-side fault injection; the GPU is never touched).
+cudaError_t gopf_malloc(void **p, size_t bytes);
+template <typename T> inline cudaError_t gopf_malloc(T **p, size_t bytes)
+{
+    return gopf_malloc(reinterpret_cast<void **>(p), bytes);
+}

@@ -127,7 +127,7 @@ template <typename R> int fft_impl(gopf_ctx *ctx, int sign, double *data)
 {
     const Geom &g = ctx->g;
     void *dbuf = nullptr;
-    int rc = ck(ctx, cudaMalloc(&dbuf, sizeof(typename VecOf<R>::type) * g.C), "cudaMalloc");
+    int rc = ck(ctx, gopf_malloc(&dbuf, sizeof(typename VecOf<R>::type) * g.C), "cudaMalloc");
     if (rc) return rc;
     std::complex<double> *x = reinterpret_cast<std::complex<double> *>(data);
     std::vector<double> a(g.N), b(g.N);

@@ -187,17 +187,17 @@ int ie_alloc(gopf_ctx *ctx)
     ws->rb = (size_t)ws->n * (ctx->prec == GOPF_FP32 ? sizeof(float) : sizeof(double));
     const size_t cb = (size_t)ctx->g.C * (ctx->prec == GOPF_FP32 ? sizeof(float2) : sizeof(double2));
     void **vecs[] = {&ws->x, &ws->F, &ws->xp, &ws->Fp, &ws->w};
-    for (void **p : vecs) IE_CK(cudaMalloc(p, ws->rb));
+    for (void **p : vecs) IE_CK(gopf_malloc(p, ws->rb));
     ws->V.assign(restart + 1, nullptr);
-    for (auto &p : ws->V) IE_CK(cudaMalloc(&p, ws->rb));
-    IE_CK(cudaMalloc(&ws->d_V, sizeof(void *) * (restart + 1)));
+    for (auto &p : ws->V) IE_CK(gopf_malloc(&p, ws->rb));
+    IE_CK(gopf_malloc(&ws->d_V, sizeof(void *) * (restart + 1)));
     IE_CK(cudaMemcpy(ws->d_V, ws->V.data(), sizeof(void *) * (restart + 1), cudaMemcpyHostToDevice));
-    IE_CK(cudaMalloc(&ws->chat0, cb));
-    IE_CK(cudaMalloc(&ws->nprev, cb));
-    IE_CK(cudaMalloc(&ws->tmp0, cb));
-    IE_CK(cudaMalloc(&ws->d_part, sizeof(double) * kBlocks * (restart + 2)));
-    IE_CK(cudaMalloc(&ws->d_out, sizeof(double) * (restart + 2)));
-    IE_CK(cudaMalloc(&ws->d_coef, sizeof(double) * (restart + 2)));
+    IE_CK(gopf_malloc(&ws->chat0, cb));
+    IE_CK(gopf_malloc(&ws->nprev, cb));
+    IE_CK(gopf_malloc(&ws->tmp0, cb));
+    IE_CK(gopf_malloc(&ws->d_part, sizeof(double) * kBlocks * (restart + 2)));
+    IE_CK(gopf_malloc(&ws->d_out, sizeof(double) * (restart + 2)));
+    IE_CK(gopf_malloc(&ws->d_coef, sizeof(double) * (restart + 2)));
     IE_CK(cudaMallocHost(&ws->h_out, sizeof(double) * (restart + 2)));
     ctx->dev_bytes += ws->rb * (5 + restart + 1) + 3 * cb;
     return GOPF_OK;

@@ -189,8 +189,8 @@ int gopf_elastic_table(gopf_ctx *ctx)
     p.ndim = ctx->ndim;
     const size_t eb = (ctx->prec == GOPF_FP32) ? sizeof(float) : sizeof(double);
     if (!ctx->d_bsym) {
-        cudaError_t e = cudaMalloc(&ctx->d_bsym, eb * ctx->g.C);
-        if (e != cudaSuccess) return gopf_fail(ctx, GOPF_ERR_OOM, "cudaMalloc(elastic symbol)");
+        cudaError_t e = gopf_malloc(&ctx->d_bsym, eb * ctx->g.C);
+        if (e != cudaSuccess) return gopf_fail(ctx, GOPF_ERR_OOM, "gopf_malloc(elastic symbol)");
         ctx->dev_bytes += eb * ctx->g.C;
     }
     const unsigned blocks = (unsigned)std::min<long long>((ctx->g.C + 255) / 256, 152 * 32);

@@ -45,6 +45,11 @@ __device__ __forceinline__ void st_cluster(uint32_t addr, float2 v)
 {
     asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(addr), "f"(v.x), "f"(v.y) : "memory");
 }
+__device__ __forceinline__ void st_cluster4(uint32_t addr, float4 v)
+{
+    asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+                 : "memory");
+}
 __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
 {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
@@ -152,33 +157,28 @@ __global__ void __cluster_dims__(PL_CLUSTER, 1, 1) __launch_bounds__(NT, 3) k_pl
 #pragma unroll
         for (int i = 0; i < 16; ++i) tA[(r + 16 * i) * 16 + j] = v[i];
         __syncthreads();
-        // separation X_a(k) = (Z(k) + conj Z(-k))/2, X_b(k) = (Z(k) - conj Z(-k))/(2i) into registers;
-        // kx = 1..127 go to block kx/16 line kx%16, kx = 0 and 128 (both real) to block 0 line 0 as A + iB
-        const int yy = tid & 31, jj = yy >> 1, odd = yy & 1, kx0 = tid >> 5;
-        const int ygl = XROWS * (int)c + yy;
-        float2 o[16];
+        // separation X_a(k) = (Z(k) + conj Z(-k))/2, X_b(k) = (Z(k) - conj Z(-k))/(2i) into registers,
+        // both rows of pair p at once: kx = k0 + 16 q (q = 0..7) goes to block q, line k0, as one
+        // 16-byte store; kx = 0 and 128 (both real) go to block 0 line 0 as A + iB
+        const int p = tid & 15, k0 = tid >> 4;
+        float4 o[8];
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            const int kx = kx0 + 8 * q; // 0 .. 127
-            const float2 P = tA[kx * 16 + jj];
+        for (int q = 0; q < 8; ++q) {
+            const int kx = k0 + 16 * q;
+            const float2 P = tA[kx * 16 + p];
             if (kx == 0) {
-                const float2 P2 = tA[128 * 16 + jj];
-                o[q] = odd ? make_float2(P.y, P2.y) : make_float2(P.x, P2.x);
+                const float2 P2 = tA[128 * 16 + p];
+                o[q] = make_float4(P.x, P2.x, P.y, P2.y);
             } else {
-                const float2 Q = tA[(N - kx) * 16 + jj];
-                o[q] = odd ? make_float2(0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x))
-                           : make_float2(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y));
+                const float2 Q = tA[(N - kx) * 16 + p];
+                o[q] = make_float4(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y), 0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
             }
         }
         cluster_arrive();
         cluster_wait(); // every block has read its tile: the line buffers may be overwritten
-        const uint32_t ry = smem_u32(Ry);
+        const uint32_t ry = smem_u32(Ry) + (uint32_t)((k0 * N + XROWS * (int)c + 2 * p) * 8);
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            const int kx = kx0 + 8 * q;
-            const int off = ((kx == 0) ? ygl : (kx & 15) * N + ygl) * 8;
-            st_cluster(map_rank(ry + (uint32_t)off, (uint32_t)(kx >> 4)), o[q]);
-        }
+        for (int q = 0; q < 8; ++q) st_cluster4(map_rank(ry, (uint32_t)q), o[q]);
     }
     cluster_arrive();
     cluster_wait(); // no remote writes after this point

@@ -1,6 +1,6 @@
 """FP64 numpy reference of the Cahn-Hilliard forward step and its adjoint.
 
-Test infrastructure only (the checker of gopf_adjoint_*).  The forward step
+Test infrastructure only (the reference computation for gopf_adjoint_*).  The forward step
 restates Euler.Step (pf/euler.go:16-47) for "dconc/dt = M*LAP MU -
 M*gamma*LAP^2 conc", MU = conc^3 - conc, with numpy's real FFTs; frequencies
 follow Freq (pfutil/fftWrap.go:57-74): k^2 = (2 pi)^2 |f|^2.

@@ -1,7 +1,8 @@
 /*
  * gopf_oracle.c -- CPU FP64 restatement of gopf's spectral time-stepping path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker for the GPU library:
+ * TEST INFRASTRUCTURE ONLY.  This file is the reference computation the GPU
+ * library is tested against:
  * only the test-suite, the smoke check and the CPU-baseline leg of the
  * benchmark load it.  Nothing in the product path links or calls it.
  *

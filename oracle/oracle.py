@@ -1,8 +1,8 @@
 """ctypes front end of the CPU FP64 oracle (oracle/gopf_oracle.c).
 
 Test infrastructure only: the test-suite, the smoke check and the CPU-baseline
-leg of bench.py use this module as the checker.  The product path never
-imports it.
+leg of bench.py use this module as the reference computation.  The product
+path never imports it.
 
 The model object mirrors how gopf's pf.Model is driven by pf.Solver:
 fields are complex128 arrays in the reference's node order
