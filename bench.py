@@ -40,8 +40,8 @@ UNIT = "steps/s"
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of each step kernel, from
 # one ncu capture of `python bench.py --steps 10 --warmup 3 --no-cpu-baseline --no-e2e` on a GB300
 # (profiles/launches_ch3d_256_fp32.md).  Bytes that a launch leaves in L2 are not in these counts.
-NCU_TRAFFIC = {"zpass_update": 206.8e6, "xpass_pointwise": 72.3e6, "ypass_forward": 72.2e6,
-               "ypass_inverse": 72.2e6}
+NCU_TRAFFIC = {"zpass_update": 207.4e6, "xpass_pointwise": 72.9e6, "ypass_forward": 72.7e6,
+               "ypass_inverse": 72.7e6}
 DIMS = [256, 256, 256]
 GAMMA, M, DT, SEED = 0.5, 1.0, 0.05, 1
 CH_EQ = "dconc/dt = M*LAP conc^3 + m1*LAP conc + m1*gamma*LAP^2 conc"
@@ -169,7 +169,6 @@ def run_reference(args):
     if rank != 0:
         return 0
     budget = float(os.environ.get("GOPF_REF_SECONDS", "120"))
-    per_step = max(budget / max(args.steps + args.warmup, 1), 1.0)
     rate, steps, el, threads = cpu_oracle_step_rate(DIMS, max_seconds=budget, max_steps=args.steps,
                                                     warmup=min(args.warmup, 1))
     sample = (f"{steps} Euler steps of the 256^3 grid in FP64 (complex128 fields, Z2Z FFTs, as the reference), "
@@ -182,7 +181,6 @@ def run_reference(args):
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    del per_step
     print(json.dumps(out))
     return 0
 
