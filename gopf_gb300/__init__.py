@@ -283,6 +283,14 @@ class Model:
         self._ck(self._L.gopf_get_step(self._h, ctypes.byref(s)))
         return s.value
 
+    def point_values(self, field: int, sites) -> np.ndarray:
+        """PointMonitor.Add (pf/monitor.go:27-30) for several sites: the real field there."""
+        idx = np.ascontiguousarray(sites, dtype=np.int64)
+        out = np.empty(idx.size)
+        self._ck(self._L.gopf_point_values(self._h, field, idx.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+                                           int(idx.size), _dptr(out)))
+        return out
+
     def reduce(self, field: int, what: int) -> float:
         out = ctypes.c_double()
         self._ck(self._L.gopf_reduce(self._h, field, what, ctypes.byref(out)))

@@ -87,6 +87,7 @@ SIGNATURES = {
     "gopf_get_step": ([_vp, ctypes.POINTER(_ll)], _i),
     "gopf_synchronize": ([_vp], _i),
     "gopf_reduce": ([_vp, _i, _i, _dp], _i),
+    "gopf_point_values": ([_vp, _i, ctypes.POINTER(_ll), _i, _dp], _i),
     "gopf_fft": ([_vp, _i, _dp, _sz], _i),
     "gopf_freq": ([_vp, _ll, _dp], _i),
     "gopf_conjugate_node": ([_vp, _ll], _ll),

@@ -290,6 +290,13 @@ static void ctx_free(gopf_ctx *ctx)
         if (p) cudaFree(p);
     for (int i = 1; i < GOPF_MAX_GROUPS; ++i)
         if (ctx->d_U[i]) cudaFree(ctx->d_U[i]);
+    for (int f = 1; f < GOPF_MAX_FIELDS; ++f) {
+        if (ctx->d_fstate[f]) cudaFree(ctx->d_fstate[f]);
+        if (ctx->d_fT[f]) cudaFree(ctx->d_fT[f]);
+        if (ctx->d_frkF[f]) cudaFree(ctx->d_frkF[f]);
+    }
+    for (int i = 0; i < GOPF_MAX_XOUT; ++i)
+        if (ctx->d_mU[i]) cudaFree(ctx->d_mU[i]);
     void *more[] = {ctx->d_bsym, ctx->d_U0, ctx->d_UH, ctx->d_vc, ctx->d_red2, ctx->d_rkF, ctx->d_stepctr, ctx->d_status,
                     ctx->d_filter};
     for (void *p : more)
@@ -479,10 +486,249 @@ static int alloc_spectral(gopf_ctx *ctx, void **p)
     return GOPF_OK;
 }
 
+// ---- multi-field models ----
+
+// per-field device arrays: field 0 uses the context's own, fields 1.. the multi-field set
+static void *field_state(gopf_ctx *ctx, int f) { return f == 0 ? ctx->d_state : ctx->d_fstate[f]; }
+static void *field_T(gopf_ctx *ctx, int f) { return f == 0 ? ctx->d_T : ctx->d_fT[f]; }
+static void *field_rkF(gopf_ctx *ctx, int f) { return f == 0 ? ctx->d_rkF : ctx->d_frkF[f]; }
+
+struct Mono {
+    double coef;
+    unsigned char pw[GOPF_MAX_FIELDS];
+};
+
+// A derived field as monomials of the model's fields (pf/util.go:38-65: products of
+// field powers; RegisterFunction polynomials and the indicator functions of one field).
+static int derived_mono(gopf_ctx *ctx, const gopf_derived &d, std::vector<Mono> &out)
+{
+    out.clear();
+    auto field_ok = [&](int f, int p) {
+        return f >= 0 && f < ctx->nfields && p >= 0 && p <= 64;
+    };
+    if (d.kind == GOPF_DER_PRODUCT) {
+        Mono m{1.0, {0, 0, 0, 0}};
+        for (int j = 0; j < d.nfac; ++j) {
+            if (!field_ok(d.field[j], d.power[j]))
+                return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "derived field with a negative or too large power");
+            m.pw[d.field[j]] = (unsigned char)(m.pw[d.field[j]] + d.power[j]);
+        }
+        out.push_back(m);
+        return GOPF_OK;
+    }
+    if (d.kind == GOPF_DER_POLY) {
+        for (int j = 0; j < d.nfac; ++j) {
+            if (!field_ok(d.field[j], d.power[j]))
+                return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "polynomial with a negative or too large power");
+            Mono m{d.coef[j], {0, 0, 0, 0}};
+            m.pw[d.field[j]] = (unsigned char)d.power[j];
+            out.push_back(m);
+        }
+        return GOPF_OK;
+    }
+    if (d.kind == GOPF_DER_WHITE_NOISE)
+        return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "noise terms are stepped in single-field models only");
+    std::vector<std::pair<double, int>> poly;
+    gopf_derived d0 = d;
+    d0.field[0] = 0; // derived_poly expands the indicator kinds of one field
+    int rc = derived_poly(ctx, d0, poly);
+    if (rc) return rc;
+    if (!field_ok(d.field[0], 0)) return gopf_fail(ctx, GOPF_ERR_ARG, "bad field index");
+    for (auto &pc : poly) {
+        Mono m{pc.first, {0, 0, 0, 0}};
+        m.pw[d.field[0]] = (unsigned char)pc.second;
+        out.push_back(m);
+    }
+    return GOPF_OK;
+}
+
+// Term table of a model with several fields -> one monomial table for the shared x-pass and
+// one update table per equation (equation e evolves field e, pf/euler.go:33-44).
+//
+// Euler.Step updates the fields one after the other in place, in k space, before any inverse
+// transform (pf/euler.go:31-42): an explicit term that is another field f itself (a Field brick,
+// "LAP conc" in the phi equation) reads f's c-hat as it is at that moment, i.e. already updated
+// when f < e.  Derived fields were synced at the start of the step.  So with kfield set (the
+// Euler plan) such terms stay in k space (UpdTable::xf_*) and read the state arrays, which the
+// per-equation updates rewrite in the same order.  RK4 evaluates every right-hand side after all
+// fields of a stage are formed (pf/rk4.go:101-127): its plan (kfield false) puts them in the
+// x-pass like any product.
+static int build_multi_plan(gopf_ctx *ctx, bool kfield, std::vector<gopf_ctx::EqPlan> &eqs, MonoTable &mt,
+                            int &nextra)
+{
+    const int nf = ctx->nfields;
+    eqs.assign(nf, gopf_ctx::EqPlan());
+    for (auto &ep : eqs) {
+        memset(&ep, 0, sizeof(ep));
+        for (int b = 0; b < GOPF_MAX_GROUPS; ++b) ep.ubuf[b] = -1;
+    }
+    // per equation: groups keyed by LAP power, each a list of monomials
+    std::vector<std::vector<std::vector<Mono>>> gm(nf);
+    std::vector<int> maxp(nf, 0);
+    for (const gopf_term &t : ctx->terms) {
+        if (t.eq < 0 || t.eq >= nf) return gopf_fail(ctx, GOPF_ERR_ARG, "term refers to an equation that does not exist");
+        if (t.lap < 0 || t.lap >= GOPF_MAX_IMP) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "LAP power out of range");
+        gopf_ctx::EqPlan &ep = eqs[t.eq];
+        UpdTable &u = ep.upd;
+        if (t.implicit) {
+            u.imp[t.lap] += t.coef;
+            maxp[t.eq] = std::max(maxp[t.eq], t.lap + 1);
+            continue;
+        }
+        std::vector<Mono> ms;
+        if (t.source == GOPF_SRC_FIELD) {
+            if (t.src_index < 0 || t.src_index >= nf) return gopf_fail(ctx, GOPF_ERR_ARG, "bad field index");
+            if (kfield) {
+                int at = -1;
+                for (int q = 0; q < u.nxf; ++q)
+                    if (ep.xf_field[q] == t.src_index && u.xf_lap[q] == t.lap) at = q;
+                if (at < 0) {
+                    if (u.nxf >= GOPF_MAX_FIELDS)
+                        return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "too many field terms in one equation");
+                    at = u.nxf++;
+                    ep.xf_field[at] = t.src_index;
+                    u.xf_lap[at] = t.lap;
+                    u.xf_coef[at] = 0.0;
+                }
+                u.xf_coef[at] += t.coef;
+                continue;
+            }
+            Mono m{1.0, {0, 0, 0, 0}};
+            m.pw[t.src_index] = 1;
+            ms.push_back(m);
+        } else if (t.source == GOPF_SRC_DERIVED) {
+            if (t.src_index < 0 || t.src_index >= (int)ctx->der.size())
+                return gopf_fail(ctx, GOPF_ERR_ARG, "bad derived-field index");
+            int rc = derived_mono(ctx, ctx->der[t.src_index], ms);
+            if (rc) return rc;
+        } else {
+            return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED,
+                             "a term without a field (constant in k space) has no device implementation");
+        }
+        int grp = -1;
+        for (int b = 0; b < u.ngrp; ++b)
+            if (u.glap[b] == t.lap) grp = b;
+        if (grp < 0) {
+            if (u.ngrp >= GOPF_MAX_GROUPS) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "too many distinct LAP powers");
+            grp = u.ngrp++;
+            u.glap[grp] = t.lap;
+            gm[t.eq].emplace_back();
+        }
+        for (const Mono &m : ms) { // merge equal power vectors
+            bool merged = false;
+            for (Mono &q : gm[t.eq][grp])
+                if (!memcmp(q.pw, m.pw, sizeof(m.pw))) {
+                    q.coef += t.coef * m.coef;
+                    merged = true;
+                }
+            if (!merged) {
+                if ((int)gm[t.eq][grp].size() >= GOPF_MAX_MONO)
+                    return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "too many distinct products in one term group");
+                gm[t.eq][grp].push_back({t.coef * m.coef, {m.pw[0], m.pw[1], m.pw[2], m.pw[3]}});
+            }
+        }
+    }
+    for (const gopf_special &sp : ctx->specials) {
+        if (sp.eq < 0 || sp.eq >= nf) return gopf_fail(ctx, GOPF_ERR_ARG, "term refers to an equation that does not exist");
+        if (sp.kind != 4)
+            return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED,
+                             "elastic, volume-conserving and noise terms are stepped in single-field models only");
+        const gopf_modeldef::ImplicitSym &is = ctx->def.isym[sp.index];
+        UpdTable &u = eqs[sp.eq].upd;
+        if (u.nxs >= GOPF_MAX_XSYM) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "too many implicit user terms");
+        XSym &x = u.xs[u.nxs++];
+        memset(&x, 0, sizeof(x));
+        x.kind = is.kind;
+        x.coef = sp.coef;
+        x.lap = sp.lap;
+        memcpy(x.K, is.K, sizeof(x.K));
+        x.dk = (is.nk == 9) ? 3 : 2;
+        x.eps = is.eps;
+        x.threshold = is.threshold;
+        x.power = is.power;
+    }
+    memset(&mt, 0, sizeof(mt));
+    mt.nin = nf;
+    nextra = 0;
+    for (int e = 0; e < nf; ++e) {
+        UpdTable &u = eqs[e].upd;
+        u.nimp = maxp[e];
+        eqs[e].first = mt.ngrp;
+        for (int b = 0; b < u.ngrp; ++b) {
+            if (mt.ngrp >= GOPF_MAX_XOUT)
+                return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "too many term groups over all equations");
+            const int j = mt.ngrp++;
+            mt.nmono[j] = (int)gm[e][b].size();
+            for (int m = 0; m < mt.nmono[j]; ++m) {
+                mt.coef[j][m] = gm[e][b][m].coef;
+                memcpy(mt.pw[j][m], gm[e][b][m].pw, GOPF_MAX_FIELDS);
+            }
+            eqs[e].ubuf[b] = (b == 0) ? -1 : nextra++;
+        }
+    }
+    return GOPF_OK;
+}
+
+static int compile_multi(gopf_ctx *ctx)
+{
+    const int nf = ctx->nfields;
+    if (nf > GOPF_MAX_FIELDS)
+        return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "at most " + std::to_string(GOPF_MAX_FIELDS) + " fields per model");
+    std::vector<gopf_ctx::EqPlan> eqs, eqs_rk;
+    MonoTable mt, mt_rk;
+    int nx = 0, nx_rk = 0, rc;
+    if ((rc = build_multi_plan(ctx, true, eqs, mt, nx))) return rc;
+    if ((rc = build_multi_plan(ctx, false, eqs_rk, mt_rk, nx_rk))) return rc;
+    const int nextra = std::max(nx, nx_rk);
+    // x-pass tile width: nf + 1 tiles of KX x LB elements in shared memory
+    const int vb = (ctx->prec == GOPF_FP32) ? 8 : 16;
+    auto smem_of = [&](int lbx) { return (long long)(nf + 1) * ctx->g.KX * lbx * vb; };
+    int lb = ctx->LBx;
+    while (lb > 4 && smem_of(lb) > 200 * 1024) lb /= 2;
+    if (smem_of(lb) > 200 * 1024)
+        return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "too many fields for this column count (shared memory)");
+    if (ctx->device >= 0) {
+        for (int f = 1; f < nf; ++f) {
+            const bool fresh = !ctx->d_fstate[f];
+            if ((rc = alloc_spectral(ctx, &ctx->d_fstate[f]))) return rc;
+            if ((rc = alloc_spectral(ctx, &ctx->d_fT[f]))) return rc;
+            if (fresh) { // fields start at zero, like pf.NewField(name, n, nil)
+                const size_t vbytes = (size_t)vb * ctx->g.C;
+                CK(cudaMemset(ctx->d_fstate[f], 0, vbytes));
+                CK(cudaMemset(ctx->d_fT[f], 0, vbytes));
+            }
+        }
+        for (int i = 0; i < nextra; ++i)
+            if ((rc = alloc_spectral(ctx, &ctx->d_mU[i]))) return rc;
+    }
+    ctx->multi = true;
+    ctx->eqs = eqs;
+    ctx->mono = mt;
+    ctx->eqs_rk = eqs_rk;
+    ctx->mono_rk = mt_rk;
+    ctx->LBm = lb;
+    memset(&ctx->pw, 0, sizeof(ctx->pw));
+    // ctx->upd only carries the modal filter (gopf_set_modal_filter); each equation's table is in eqs
+    UpdTable u0;
+    memset(&u0, 0, sizeof(u0));
+    u0.filt = ctx->upd.nfilt ? ctx->d_filter : nullptr;
+    u0.nfilt = ctx->upd.nfilt;
+    ctx->upd = u0;
+    ctx->ngroups = mt.ngrp;
+    ctx->has_elastic = ctx->has_volcons = false;
+    ctx->vc_group = -1;
+    memset(&ctx->noise, 0, sizeof(ctx->noise));
+    ctx->el_primed = false;
+    ctx->initialised = true;
+    invalidate_graphs(ctx);
+    return GOPF_OK;
+}
+
 int gopf_compile_model(gopf_ctx *ctx)
 {
-    if (ctx->nfields != 1)
-        return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "the device stepper supports single-field models");
+    if (ctx->nfields < 1) return gopf_fail(ctx, GOPF_ERR_ARG, "the model has no fields");
+    if (ctx->nfields > 1) return compile_multi(ctx);
+    ctx->multi = false;
     PwTable pw;
     memset(&pw, 0, sizeof(pw));
     UpdTable u;
@@ -766,30 +1012,32 @@ static void prof_mark(gopf_ctx *ctx)
     } while (0)
 
 // From T (after the inverse y/z passes) produce real rows and/or reductions.
-template <typename R> static XPassArgs<R> xargs_out(gopf_ctx *ctx, R *rout, double *red)
+template <typename R> static XPassArgs<R> xargs_out(gopf_ctx *ctx, R *rout, double *red, int f = 0)
 {
     XPassArgs<R> xa = xargs<R>(ctx);
     xa.in_mode = XIN_SPECTRAL;
-    xa.in = (const typename VecOf<R>::type *)ctx->d_T;
+    xa.in = (const typename VecOf<R>::type *)field_T(ctx, f);
     xa.rout = rout;
     xa.red = red;
     xa.ngrp_out = 0;
     return xa;
 }
 
-template <typename R> static cudaError_t enqueue_xpass_out(gopf_ctx *ctx, R *rout, double *red)
+template <typename R> static cudaError_t enqueue_xpass_out(gopf_ctx *ctx, R *rout, double *red, int f = 0)
 {
-    return launch_xpass<R>(xargs_out<R>(ctx, rout, red), ctx->LBx, ctx->stream);
+    return launch_xpass<R>(xargs_out<R>(ctx, rout, red, f), ctx->LBx, ctx->stream);
 }
 
-// Load real field d_real into the state: c-hat = FFT(c), T = partial inverse of c-hat/N.
-template <typename R> static cudaError_t enqueue_load_state(gopf_ctx *ctx)
+// Load real field d_real into the state of field f: c-hat = FFT(c), T = partial inverse of c-hat/N.
+template <typename R> static cudaError_t enqueue_load_state(gopf_ctx *ctx, int f = 0)
 {
     typedef typename VecOf<R>::type V;
+    V *T = (V *)field_T(ctx, f);
+    V *state = (V *)field_state(ctx, f);
     XPassArgs<R> xa = xargs<R>(ctx);
     xa.in_mode = XIN_REAL;
     xa.rin = (const R *)ctx->d_real;
-    xa.out[0] = (V *)ctx->d_T;
+    xa.out[0] = T;
     xa.ngrp_out = 1;
     xa.identity = 1;
     LK(launch_xpass<R>(xa, ctx->LBx, ctx->stream));
@@ -799,30 +1047,30 @@ template <typename R> static cudaError_t enqueue_load_state(gopf_ctx *ctx)
     if (ctx->g.Z > 1) {
         PassArgs<R> pa = pargs<R>(ctx, false);
         pa.mode = PM_FWD;
-        pa.buf[0] = (V *)ctx->d_T;
+        pa.buf[0] = T;
         pa.nbuf = 1;
         LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
         PassArgs<R> sa = pargs<R>(ctx, true);
         sa.mode = PM_INIT;
-        sa.buf[0] = (V *)ctx->d_T;
+        sa.buf[0] = T;
         sa.nbuf = 1;
-        sa.state = (V *)ctx->d_state;
-        sa.tout = (V *)ctx->d_T;
+        sa.state = state;
+        sa.tout = T;
         sa.upd = u;
         LK(launch_spass<R>(sa, ctx->LBz, ctx->stream));
-        LK(gopf_launch_hermitian_planes(ctx, ctx->d_state));
+        LK(gopf_launch_hermitian_planes(ctx, state));
         pa.mode = PM_INV;
         LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
     } else {
         PassArgs<R> pa = pargs<R>(ctx, false);
         pa.mode = PM_INIT;
-        pa.buf[0] = (V *)ctx->d_T;
+        pa.buf[0] = T;
         pa.nbuf = 1;
-        pa.state = (V *)ctx->d_state;
-        pa.tout = (V *)ctx->d_T;
+        pa.state = state;
+        pa.tout = T;
         pa.upd = u;
         LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
-        LK(gopf_launch_hermitian_planes(ctx, ctx->d_state));
+        LK(gopf_launch_hermitian_planes(ctx, state));
     }
     return cudaSuccess;
 }
@@ -840,7 +1088,8 @@ template <typename R> static cudaError_t enqueue_load_state(gopf_ctx *ctx)
 // next.  Only the last step of a run restores T to its usual form.
 static bool plane_path(const gopf_ctx *ctx)
 {
-    return ctx->use_plane && ctx->use_fast && ctx->use_tma && ctx->prec == GOPF_FP32 && plane256_supported(ctx->g) &&
+    return !ctx->multi && ctx->use_plane && ctx->use_fast && ctx->use_tma && ctx->prec == GOPF_FP32 &&
+           plane256_supported(ctx->g) &&
            ctx->stepper == GOPF_STEPPER_EULER && !ctx->has_elastic && !ctx->has_volcons && ctx->ngroups == 1;
 }
 
@@ -1033,10 +1282,94 @@ template <typename R> static cudaError_t enqueue_rk4(gopf_ctx *ctx)
     return cudaSuccess;
 }
 
+// One Euler (rk_stage 0) step or one RK4 stage of a multi-field model (pf/euler.go:16-47 and
+// pf/rk4.go:29-127 loop over m.Fields; every field's RHS sees every field at the stage's start):
+//   x-pass   : c2r of T of every field -> monomial groups of every equation -> r2c
+//   per eq.  : [3D] forward y of its groups; fused last-axis update of its c-hat, T <- inverse
+//   per field: Hermitian projection; [3D] inverse y of all T in one launch
+template <typename R> static cudaError_t enqueue_multi_stage(gopf_ctx *ctx, int stage)
+{
+    typedef typename VecOf<R>::type V;
+    const int nf = ctx->nfields;
+    const bool is3d = ctx->g.Z > 1;
+    const double dt = ctx->dt;
+    const std::vector<gopf_ctx::EqPlan> &eqs = (stage > 0) ? ctx->eqs_rk : ctx->eqs;
+    const MonoTable &mono = (stage > 0) ? ctx->mono_rk : ctx->mono;
+    auto gbuf = [&](int e, int b) -> V * {
+        const int k = eqs[e].ubuf[b];
+        return (V *)(k < 0 ? field_T(ctx, e) : ctx->d_mU[k]);
+    };
+    if (mono.ngrp > 0) {
+        XPassArgs<R> xa = xargs<R>(ctx);
+        xa.in_mode = XIN_SPECTRAL;
+        xa.program = XP_MULTI;
+        xa.allow_fast = 0;
+        for (int f = 0; f < nf; ++f) xa.inF[f] = (const V *)field_T(ctx, f);
+        for (int e = 0; e < nf; ++e)
+            for (int b = 0; b < eqs[e].upd.ngrp; ++b) xa.out[eqs[e].first + b] = gbuf(e, b);
+        xa.ngrp_out = mono.ngrp;
+        xa.mono = mono;
+        LK(launch_xpass<R>(xa, ctx->LBm, ctx->stream));
+    }
+    for (int e = 0; e < nf; ++e) {
+        const gopf_ctx::EqPlan &ep = eqs[e];
+        const int G = ep.upd.ngrp;
+        if (is3d && G > 0) {
+            PassArgs<R> pa = pargs<R>(ctx, false);
+            pa.mode = PM_FWD;
+            for (int b = 0; b < G; ++b) pa.buf[b] = gbuf(e, b);
+            pa.nbuf = G;
+            LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+        }
+        UpdTable u = ep.upd;
+        u.dt = dt;
+        u.invN = 1.0 / (double)ctx->g.N;
+        u.filt = ctx->upd.filt;
+        u.nfilt = ctx->upd.nfilt;
+        for (int q = 0; q < u.nxf; ++q) u.xf_src[q] = field_state(ctx, ep.xf_field[q]);
+        if (stage > 0) {
+            const double afin[4] = {dt / 6.0, dt / 3.0, dt / 3.0, dt / 6.0};
+            const double ay[3] = {0.5 * dt, 0.5 * dt, dt};
+            u.rk_stage = stage;
+            u.rk_afin = afin[stage - 1];
+            u.rk_ay = (stage < 4) ? ay[stage - 1] : 0.0;
+            u.rk_fden = (stage < 4) ? ay[stage - 1] : dt;
+        }
+        const int nb = std::max(G, 1);
+        PassArgs<R> fa = pargs<R>(ctx, is3d);
+        fa.mode = PM_FUSED;
+        for (int b = 0; b < nb; ++b) fa.buf[b] = gbuf(e, b);
+        fa.nbuf = nb;
+        fa.state = (V *)field_state(ctx, e);
+        fa.tout = (V *)field_T(ctx, e);
+        fa.upd = u;
+        fa.rkF = (V *)field_rkF(ctx, e);
+        LK(is3d ? launch_spass<R>(fa, ctx->LBz, ctx->stream) : launch_cpass<R>(fa, ctx->LBy, ctx->stream));
+    }
+    if (stage == 0 || stage == 4)
+        for (int f = 0; f < nf; ++f) LK(gopf_launch_hermitian_planes(ctx, field_state(ctx, f)));
+    if (is3d) {
+        PassArgs<R> ia = pargs<R>(ctx, false);
+        ia.mode = PM_INV;
+        for (int f = 0; f < nf; ++f) ia.buf[f] = (V *)field_T(ctx, f);
+        ia.nbuf = nf;
+        LK(launch_cpass<R>(ia, ctx->LBy, ctx->stream));
+    }
+    return cudaSuccess;
+}
+
 template <typename R> static cudaError_t enqueue_steps(gopf_ctx *ctx, int n)
 {
-    for (int i = 0; i < n; ++i)
+    for (int i = 0; i < n; ++i) {
+        if (ctx->multi) {
+            if (ctx->stepper == GOPF_STEPPER_RK4)
+                for (int s = 1; s <= 4; ++s) LK(enqueue_multi_stage<R>(ctx, s));
+            else
+                LK(enqueue_multi_stage<R>(ctx, 0));
+            continue;
+        }
         LK(ctx->stepper == GOPF_STEPPER_RK4 ? enqueue_rk4<R>(ctx) : enqueue_euler<R>(ctx, i == 0, i == n - 1));
+    }
     return cudaSuccess;
 }
 
@@ -1096,7 +1429,7 @@ static void *direct_host_ptr(gopf_ctx *ctx, const void *p)
     return (pa.type == cudaMemoryTypeHost && pa.devicePointer) ? pa.devicePointer : nullptr;
 }
 
-template <typename R> static int upload_impl(gopf_ctx *ctx, const double *data, bool complex_in)
+template <typename R> static int upload_impl(gopf_ctx *ctx, const double *data, bool complex_in, int f)
 {
     const long long N = ctx->g.N;
     if (void *dp = direct_host_ptr(ctx, data)) {
@@ -1105,7 +1438,7 @@ template <typename R> static int upload_impl(gopf_ctx *ctx, const double *data, 
         else
             k_double_to_real<R><<<ew_blocks(N), 256, 0, ctx->stream>>>((const double *)dp, (R *)ctx->d_real, N);
         CK(cudaGetLastError());
-        CK(enqueue_load_state<R>(ctx));
+        CK(enqueue_load_state<R>(ctx, f));
         CK(cudaStreamSynchronize(ctx->stream));
         return GOPF_OK;
     }
@@ -1117,15 +1450,15 @@ template <typename R> static int upload_impl(gopf_ctx *ctx, const double *data, 
         k_double_to_real<R><<<ew_blocks(N), 256, 0, ctx->stream>>>((const double *)ctx->d_c128, (R *)ctx->d_real, N);
     }
     CK(cudaGetLastError());
-    CK(enqueue_load_state<R>(ctx));
+    CK(enqueue_load_state<R>(ctx, f));
     CK(cudaStreamSynchronize(ctx->stream));
     return GOPF_OK;
 }
 
-template <typename R> static int download_impl(gopf_ctx *ctx, double *data, bool complex_out)
+template <typename R> static int download_impl(gopf_ctx *ctx, double *data, bool complex_out, int f)
 {
     const long long N = ctx->g.N;
-    CK(enqueue_xpass_out<R>(ctx, (R *)ctx->d_real, nullptr));
+    CK(enqueue_xpass_out<R>(ctx, (R *)ctx->d_real, nullptr, f));
     if (void *dp = direct_host_ptr(ctx, data)) {
         if (complex_out)
             k_real_to_c128<R><<<ew_blocks(N), 256, 0, ctx->stream>>>((const R *)ctx->d_real, (double2 *)dp, N);
@@ -1158,12 +1491,14 @@ static int transfer(gopf_ctx *ctx, int field, double *data, size_t n, bool up, b
         return gopf_fail(ctx, GOPF_ERR_ARG, "Inconsistent domain size and number of grid points");
     if ((rc = set_device(ctx))) return rc;
     if (up) {
-        rc = (ctx->prec == GOPF_FP32) ? upload_impl<float>(ctx, data, cplx) : upload_impl<double>(ctx, data, cplx);
+        rc = (ctx->prec == GOPF_FP32) ? upload_impl<float>(ctx, data, cplx, field)
+                                      : upload_impl<double>(ctx, data, cplx, field);
         if (!rc) ctx->state_valid = true;
         return rc;
     }
     if (!ctx->state_valid) return gopf_fail(ctx, GOPF_ERR_STATE, "field has not been uploaded");
-    return (ctx->prec == GOPF_FP32) ? download_impl<float>(ctx, data, cplx) : download_impl<double>(ctx, data, cplx);
+    return (ctx->prec == GOPF_FP32) ? download_impl<float>(ctx, data, cplx, field)
+                                    : download_impl<double>(ctx, data, cplx, field);
 }
 
 extern "C" int gopf_field_upload(gopf_ctx *ctx, int f, const double *d, size_t n)
@@ -1198,13 +1533,14 @@ static int check_device_status(gopf_ctx *ctx)
     return GOPF_OK;
 }
 
-static int reduce_all(gopf_ctx *ctx, double *host5)
+static int reduce_all(gopf_ctx *ctx, double *host5, int f = 0)
 {
-    cudaError_t e = (ctx->prec == GOPF_FP32) ? enqueue_xpass_out<float>(ctx, nullptr, ctx->d_red)
-                                             : enqueue_xpass_out<double>(ctx, nullptr, ctx->d_red);
+    cudaError_t e = (ctx->prec == GOPF_FP32) ? enqueue_xpass_out<float>(ctx, nullptr, ctx->d_red, f)
+                                             : enqueue_xpass_out<double>(ctx, nullptr, ctx->d_red, f);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "reduction pass");
-    const int nb = (ctx->prec == GOPF_FP32) ? xpass_red_blocks<float>(xargs_out<float>(ctx, nullptr, ctx->d_red), ctx->LBx)
-                                            : xpass_red_blocks<double>(xargs_out<double>(ctx, nullptr, ctx->d_red), ctx->LBx);
+    const int nb = (ctx->prec == GOPF_FP32)
+                       ? xpass_red_blocks<float>(xargs_out<float>(ctx, nullptr, ctx->d_red, f), ctx->LBx)
+                       : xpass_red_blocks<double>(xargs_out<double>(ctx, nullptr, ctx->d_red, f), ctx->LBx);
     if (nb > ctx->nred_blocks) return gopf_fail(ctx, GOPF_ERR_STATE, "reduction partials exceed their buffer");
     k_finish_reduce<<<1, 256, 0, ctx->stream>>>(ctx->d_red, nb, ctx->d_redout);
     CK(cudaGetLastError());
@@ -1220,9 +1556,12 @@ static int check_finite_state(gopf_ctx *ctx)
     CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned), ctx->stream));
     const long long nr = 2 * ctx->g.C;
     const unsigned blocks = (unsigned)std::min<long long>((nr + 255) / 256, 152 * 8);
-    if (ctx->prec == GOPF_FP32) k_count_nonfinite<float><<<blocks, 256, 0, ctx->stream>>>((const float *)ctx->d_state, nr, cnt);
-    else k_count_nonfinite<double><<<blocks, 256, 0, ctx->stream>>>((const double *)ctx->d_state, nr, cnt);
-    CK(cudaGetLastError());
+    for (int f = 0; f < std::max(ctx->nfields, 1); ++f) {
+        const void *st = field_state(ctx, f);
+        if (ctx->prec == GOPF_FP32) k_count_nonfinite<float><<<blocks, 256, 0, ctx->stream>>>((const float *)st, nr, cnt);
+        else k_count_nonfinite<double><<<blocks, 256, 0, ctx->stream>>>((const double *)st, nr, cnt);
+        CK(cudaGetLastError());
+    }
     unsigned h = 0;
     CK(cudaMemcpyAsync(&h, cnt, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -1242,8 +1581,62 @@ extern "C" int gopf_reduce(gopf_ctx *ctx, int field, int what, double *out)
     if (!ctx->state_valid) return gopf_fail(ctx, GOPF_ERR_STATE, "field has not been uploaded");
     if ((rc = set_device(ctx))) return rc;
     double r[5];
-    if ((rc = reduce_all(ctx, r))) return rc;
+    if ((rc = reduce_all(ctx, r, field))) return rc;
     *out = r[what];
+    return GOPF_OK;
+}
+
+// PointMonitor.Add (pf/monitor.go:27-30) for n sites: the real field at node i is the inverse x
+// transform of T's row (z, y) at column x, c = Re T(0) + (-1)^x Re T(H) + 2 sum_{0<kx<H} Re(T(kx)
+// e^{2 pi i kx x / X}) (T is c-hat/N already inverse-transformed along z and y).  One warp per
+// site, FP64 sums.
+template <typename R>
+__global__ void k_point_values(const typename VecOf<R>::type *__restrict__ T, Geom g, const long long *__restrict__ sites,
+                               int n, double *__restrict__ out)
+{
+    const int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (w >= n) return;
+    const long long i = sites[w];
+    const long long x = i % g.X, y = (i / g.X) % g.Y, z = i / ((long long)g.X * g.Y);
+    double acc = 0.0;
+    for (int kx = lane; kx < g.KX; kx += 32) {
+        const typename VecOf<R>::type t = T[z * g.S + (long long)kx * g.Y + y];
+        if (kx == 0 || kx == g.H) {
+            acc += ((kx == 0 || (x & 1) == 0) ? 1.0 : -1.0) * (double)t.x;
+        } else {
+            double sn, cs;
+            sincospi(2.0 * (double)(((long long)kx * x) % g.X) / (double)g.X, &sn, &cs);
+            acc += 2.0 * ((double)t.x * cs - (double)t.y * sn);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) out[w] = acc;
+}
+
+extern "C" int gopf_point_values(gopf_ctx *ctx, int field, const long long *sites, int n, double *out)
+{
+    if (!ctx || !sites || !out || n < 1) return gopf_fail(ctx, GOPF_ERR_ARG, "null argument or no sites");
+    gopf_nvtx_scope trace("gopf_point_values");
+    int rc;
+    if ((rc = require_ready(ctx, field))) return rc;
+    if (!ctx->state_valid) return gopf_fail(ctx, GOPF_ERR_STATE, "field has not been uploaded");
+    if ((long long)n > ctx->g.N) return gopf_fail(ctx, GOPF_ERR_ARG, "more sites than nodes");
+    for (int k = 0; k < n; ++k)
+        if (sites[k] < 0 || sites[k] >= ctx->g.N) return gopf_fail(ctx, GOPF_ERR_ARG, "site outside the domain");
+    if ((rc = set_device(ctx))) return rc;
+    // scratch: the sites and the values share the transfer buffer (16 N bytes)
+    long long *d_sites = reinterpret_cast<long long *>(ctx->d_c128);
+    double *d_out = reinterpret_cast<double *>(d_sites + n);
+    CK(cudaMemcpyAsync(d_sites, sites, sizeof(long long) * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+    const unsigned blocks = (unsigned)(((long long)n * 32 + 255) / 256);
+    if (ctx->prec == GOPF_FP32)
+        k_point_values<float><<<blocks, 256, 0, ctx->stream>>>((const float2 *)field_T(ctx, field), ctx->g, d_sites, n, d_out);
+    else
+        k_point_values<double><<<blocks, 256, 0, ctx->stream>>>((const double2 *)field_T(ctx, field), ctx->g, d_sites, n,
+                                                                d_out);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, d_out, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     return GOPF_OK;
 }
 
@@ -1265,7 +1658,12 @@ extern "C" int gopf_step(gopf_ctx *ctx, long long nsteps)
         if (ctx->has_elastic || ctx->has_volcons || ctx->noise.kind)
             return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "user-defined and noise terms are stepped with Euler only");
         if ((rc = alloc_spectral(ctx, &ctx->d_rkF))) return rc;
+        if (ctx->multi)
+            for (int f = 1; f < ctx->nfields; ++f)
+                if ((rc = alloc_spectral(ctx, &ctx->d_frkF[f]))) return rc;
     }
+    if (ctx->stepper == GOPF_STEPPER_IMPLICIT_EULER && ctx->multi)
+        return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "implicit Euler steps single-field models (multi-field: Euler, RK4)");
     if (ctx->stepper == GOPF_STEPPER_IMPLICIT_EULER) {
         if (ctx->has_elastic || ctx->has_volcons || ctx->noise.kind)
             return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "user-defined and noise terms are stepped with Euler only");
@@ -1316,12 +1714,14 @@ extern "C" int gopf_step(gopf_ctx *ctx, long long nsteps)
 
 // ---- device-side helpers for the adjoint (stream-ordered, no synchronisation) ----
 
-int gopf_state_to_real(gopf_ctx *ctx, void *dst)
+int gopf_field_to_real(gopf_ctx *ctx, int f, void *dst)
 {
-    cudaError_t e = (ctx->prec == GOPF_FP32) ? enqueue_xpass_out<float>(ctx, (float *)dst, nullptr)
-                                             : enqueue_xpass_out<double>(ctx, (double *)dst, nullptr);
+    cudaError_t e = (ctx->prec == GOPF_FP32) ? enqueue_xpass_out<float>(ctx, (float *)dst, nullptr, f)
+                                             : enqueue_xpass_out<double>(ctx, (double *)dst, nullptr, f);
     return (e == cudaSuccess) ? GOPF_OK : cuda_fail(ctx, e, "state to real");
 }
+
+int gopf_state_to_real(gopf_ctx *ctx, void *dst) { return gopf_field_to_real(ctx, 0, dst); }
 
 int gopf_real_to_state(gopf_ctx *ctx, const void *src)
 {
@@ -1671,7 +2071,8 @@ extern "C" int gopf_profile_step(gopf_ctx *ctx, int nsteps, double *avg_ms, doub
     if (!ctx || !nslots || nsteps < 1) return gopf_fail(ctx, GOPF_ERR_ARG, "bad argument");
     if (!ctx->initialised || !ctx->state_valid || !(ctx->dt > 0.0))
         return gopf_fail(ctx, GOPF_ERR_STATE, "model, stepper and field must be set before profiling");
-    if (ctx->stepper != GOPF_STEPPER_EULER) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "profiling covers the Euler step");
+    if (ctx->stepper != GOPF_STEPPER_EULER || ctx->multi)
+        return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "profiling covers the Euler step of single-field models");
     if (ctx->has_elastic && !ctx->el_primed) return gopf_fail(ctx, GOPF_ERR_STATE, "take one step before profiling");
     int rc;
     if ((rc = set_device(ctx))) return rc;

@@ -141,6 +141,26 @@ struct gopf_ctx {
 
     void *d_rkF = nullptr; // RK4 accumulator
 
+    // Multi-field models (pf.Model with several fields, pf/euler.go:26-40 loops over them).
+    // Field 0 keeps d_state / d_T / d_rkF; fields 1.. have their own arrays.  One x-pass reads
+    // every field and writes the explicit groups of every equation (mono); each equation then
+    // gets its own forward pass and fused update with its own UpdTable.  Equation e's first
+    // group lands in T of field e, its further groups in d_mU.
+    bool multi = false;
+    void *d_fstate[GOPF_MAX_FIELDS] = {nullptr, nullptr, nullptr, nullptr};
+    void *d_fT[GOPF_MAX_FIELDS] = {nullptr, nullptr, nullptr, nullptr};
+    void *d_frkF[GOPF_MAX_FIELDS] = {nullptr, nullptr, nullptr, nullptr};
+    void *d_mU[GOPF_MAX_XOUT] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    struct EqPlan {
+        gopf::UpdTable upd; // ngrp, glap, imp, implicit user terms, k-space field terms
+        int first;          // index of its first group in mono
+        int ubuf[GOPF_MAX_GROUPS]; // -1: T of the field; else an index into d_mU
+        int xf_field[GOPF_MAX_FIELDS]; // field of each k-space field term (upd.xf_*)
+    };
+    std::vector<EqPlan> eqs, eqs_rk; // Euler plan (field terms in k space), RK4 plan
+    gopf::MonoTable mono{}, mono_rk{};
+    int LBm = 4; // x-pass tile width of the multi-field x-pass (nfields + 1 tiles in shared memory)
+
     // Gaussian noise term (at most one per context) and the device step counter keying it
     gopf::NoiseParams noise{};
     unsigned long long *d_stepctr = nullptr;

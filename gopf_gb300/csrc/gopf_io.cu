@@ -18,7 +18,7 @@
 #include "gopf_ctx.h"
 
 int gopf_fail(gopf_ctx *ctx, int code, const std::string &msg);
-int gopf_state_to_real(gopf_ctx *ctx, void *dst);
+int gopf_field_to_real(gopf_ctx *ctx, int f, void *dst);
 
 struct gopf_io_state {
     double *h_stage = nullptr; // pinned, N doubles
@@ -102,7 +102,7 @@ extern "C" int gopf_io_wait(gopf_ctx *ctx)
 extern "C" int gopf_save_float64(gopf_ctx *ctx, int field, const char *path, int async)
 {
     if (!ctx || !path) return GOPF_ERR_ARG;
-    if (field != 0) return gopf_fail(ctx, GOPF_ERR_ARG, "bad field id");
+    if (field < 0 || field >= std::max(ctx->nfields, 1)) return gopf_fail(ctx, GOPF_ERR_ARG, "bad field id");
     if (!ctx->state_valid) return gopf_fail(ctx, GOPF_ERR_STATE, "field has not been uploaded");
     gopf_nvtx_scope trace("gopf_save_float64");
     int rc;
@@ -119,7 +119,7 @@ extern "C" int gopf_save_float64(gopf_ctx *ctx, int field, const char *path, int
         io->n = n;
     }
     // spectral state -> real rows (d_real) -> big-endian FP64 (the staging area d_c128)
-    if ((rc = gopf_state_to_real(ctx, ctx->d_real))) return rc;
+    if ((rc = gopf_field_to_real(ctx, field, ctx->d_real))) return rc;
     const unsigned blocks = (unsigned)std::min<long long>(((long long)n + 255) / 256, 152 * 16);
     unsigned long long *d_be = reinterpret_cast<unsigned long long *>(ctx->d_c128);
     if (ctx->prec == GOPF_FP32) k_to_be64<float><<<blocks, 256, 0, ctx->stream>>>((const float *)ctx->d_real, d_be, (long long)n);
@@ -155,7 +155,7 @@ extern "C" int gopf_save_float64(gopf_ctx *ctx, int field, const char *path, int
 extern "C" int gopf_load_float64(gopf_ctx *ctx, int field, const char *path)
 {
     if (!ctx || !path) return GOPF_ERR_ARG;
-    if (field != 0) return gopf_fail(ctx, GOPF_ERR_ARG, "bad field id");
+    if (field < 0 || field >= std::max(ctx->nfields, 1)) return gopf_fail(ctx, GOPF_ERR_ARG, "bad field id");
     const size_t n = (size_t)ctx->g.N;
     FILE *f = std::fopen(path, "rb");
     if (!f) return gopf_fail(ctx, GOPF_ERR_ARG, std::string("cannot open ") + path);

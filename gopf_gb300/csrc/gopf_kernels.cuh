@@ -33,7 +33,7 @@ inline int lb_for(int n, int vbytes)
     while (lb > 4 && lb * n > 4096) lb /= 2;
     return lb;
 }
-inline int xpass_smem_bytes(const Geom &g, int LB, int vbytes);
+inline int xpass_smem_bytes(const Geom &g, int LB, int vbytes, int ntiles = 2);
 inline int cpass_smem_bytes(const Geom &g, int n, int LB, int nbuf, int vbytes);
 inline int spass_smem_bytes(const Geom &g, int n, int LB, int nbuf, int vbytes);
 

@@ -186,6 +186,35 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
     const V zero = cmk<V>((R)0, (R)0);
     const V *__restrict__ twX = a.twX;
 
+    if (a.program == XP_MULTI) {
+        // one tile per field, then each group's monomials into the tile after them
+        const MonoTable &mt = a.mono;
+        const int tsz = KX * LB;
+        V *Bm = A + mt.nin * tsz;
+        for (int f = 0; f < mt.nin; ++f) xload_c2r<R, LB, PERB>(A + f * tsz, a.inF[f], sbase, nl, g, a.planH, twX);
+        for (int grp = 0; grp < mt.ngrp; ++grp) {
+            for (int e = tid; e < H * LB; e += nt) {
+                R vx = (R)0, vy = (R)0;
+                for (int m = 0; m < mt.nmono[grp]; ++m) {
+                    R px = (R)mt.coef[grp][m], py = px;
+                    for (int f = 0; f < mt.nin; ++f) {
+                        const V c = A[f * tsz + e];
+                        for (int i = 0; i < mt.pw[grp][m][f]; ++i) {
+                            px *= c.x;
+                            py *= c.y;
+                        }
+                    }
+                    vx += px;
+                    vy += py;
+                }
+                Bm[e] = cmk<V>(vx, vy);
+            }
+            __syncthreads();
+            xr2c_store<R, LB, PERB>(Bm, a.out[grp], sbase, nl, g, a.planH, twX);
+        }
+        return;
+    }
+
     if (a.in_mode == XIN_SPECTRAL) {
         xload_c2r<R, LB, PERB>(A, a.in, sbase, nl, g, a.planH, twX);
     } else {
@@ -412,6 +441,15 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
                 nhat.x += f * tv.x;
                 nhat.y += f * tv.y;
             }
+            if (EXTRA && u.nxf) { // explicit terms in another field's c-hat (multi-field Euler)
+                for (int q = 0; q < u.nxf; ++q) {
+                    R f = (R)u.xf_coef[q];
+                    for (int i = 0; i < u.xf_lap[q]; ++i) f *= mk;
+                    const V sv = static_cast<const V *>(u.xf_src[q])[gi];
+                    nhat.x += f * sv.x;
+                    nhat.y += f * sv.y;
+                }
+            }
             if (EXTRA && u.noise.kind) {
                 long long kx, yy, zz;
                 if (CONTIG) {
@@ -605,14 +643,14 @@ template <typename K> static cudaError_t ensure_smem(K kern, int smem, int &have
     return e;
 }
 
-inline int xpass_smem_bytes(const Geom &g, int LB, int vbytes) { return 2 * g.KX * LB * vbytes; }
+inline int xpass_smem_bytes(const Geom &g, int LB, int vbytes, int ntiles) { return ntiles * g.KX * LB * vbytes; }
 inline int cpass_smem_bytes(const Geom &g, int n, int LB, int nbuf, int vbytes) { return nbuf * n * (LB + 1) * vbytes; }
 inline int spass_smem_bytes(const Geom &g, int n, int LB, int nbuf, int vbytes) { return nbuf * n * LB * vbytes; }
 
 template <typename R, int LB> static cudaError_t launch_xpass_lb(const XPassArgs<R> &a, cudaStream_t st)
 {
     typedef typename VecOf<R>::type V;
-    const int smem = xpass_smem_bytes(a.g, LB, sizeof(V));
+    const int smem = xpass_smem_bytes(a.g, LB, sizeof(V), a.program == XP_MULTI ? a.mono.nin + 1 : 2);
     auto kern = k_xpass<R, LB, perb<R>()>;
     static int have = 48 * 1024; // one per kernel instantiation
     cudaError_t e = ensure_smem(kern, smem, have);

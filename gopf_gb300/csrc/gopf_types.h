@@ -28,6 +28,10 @@ struct LinePlan {
 #define GOPF_MAX_GROUPS 4
 #define GOPF_MAX_POLY 8
 #define GOPF_MAX_IMP 9
+// multi-field models: fields per model, spectral outputs of one x-pass, monomials per group
+#define GOPF_MAX_FIELDS 4
+#define GOPF_MAX_XOUT 8
+#define GOPF_MAX_MONO 8
 
 struct Geom {
     int X, Y, Z; // cols (fastest real axis), rows, depth (1 in 2D)
@@ -67,6 +71,18 @@ inline void pw_densify(PwTable &pw)
         pw.deg[g] = ok ? d : -1;
     }
 }
+
+// Real-space pointwise polynomials of several fields (multi-field models):
+//   g_j(c_0, .., c_{nin-1}) = sum_m coef[j][m] * prod_f c_f^pw[j][m][f]
+// One output group j per (equation, LAP power); the products are the derived fields of
+// pf/util.go:38-65 with factors from different fields.
+struct MonoTable {
+    int nin;  // fields read
+    int ngrp; // output groups
+    int nmono[GOPF_MAX_XOUT];
+    double coef[GOPF_MAX_XOUT][GOPF_MAX_MONO];
+    unsigned char pw[GOPF_MAX_XOUT][GOPF_MAX_MONO][GOPF_MAX_FIELDS];
+};
 
 // k-space Gaussian noise term (white or conservative), drawn per mode and step
 struct NoiseParams {
@@ -124,6 +140,13 @@ struct UpdTable {
     // implicit user terms beyond the polynomial (generic kernels only)
     int nxs;
     XSym xs[GOPF_MAX_XSYM];
+    // explicit terms of another field of a multi-field Euler step, added in k space:
+    // N += xf_coef[q] m^xf_lap[q] xf_src[q](k) (that field's c-hat as it is when this
+    // equation's update runs; generic kernels only)
+    int nxf;
+    double xf_coef[GOPF_MAX_FIELDS];
+    int xf_lap[GOPF_MAX_FIELDS];
+    const void *xf_src[GOPF_MAX_FIELDS];
 };
 
 // Reduction slots written by the x-pass (FP64, compensated per block)
@@ -144,7 +167,7 @@ template <typename R> struct XPassArgs {
     const V *in;
     const R *rin;
     R *rout;              // optional: write real rows of c
-    V *out[GOPF_MAX_GROUPS];
+    V *out[GOPF_MAX_XOUT];
     int ngrp_out;         // number of spectral outputs (0 = none)
     int identity;         // 1: output group 0 is r2c(c) itself
     PwTable pw;
@@ -159,9 +182,12 @@ template <typename R> struct XPassArgs {
     double *red2;
     int allow_fast; // 1: a specialised kernel may serve this launch
     unsigned *status; // device status word (bounded waits that ran out set bits)
+    // program XP_MULTI: inF[f] = T of field f; out[j] = r2c(mono group j)
+    const V *inF[GOPF_MAX_FIELDS];
+    MonoTable mono;
 };
 
-enum XProgram { XP_POLY = 0, XP_ELASTIC_Q = 1 };
+enum XProgram { XP_POLY = 0, XP_ELASTIC_Q = 1, XP_MULTI = 2 };
 
 // PM_ELASTIC_K: forward transform buf[0], multiply by bsym(k)/N, inverse transform in place
 enum PassMode { PM_FWD = 0, PM_INV = 1, PM_FUSED = 2, PM_INIT = 3, PM_ELASTIC_K = 4 };

@@ -144,14 +144,14 @@ static bool fast_y(const PassArgs<float> &a)
     if (!a.allow_fast || a.plan.n != 256 || a.g.Y != 256) return false;
     if (a.mode == PM_FWD || a.mode == PM_INV) return true;
     return (a.mode == PM_FUSED || a.mode == PM_INIT) && a.g.Z == 1 && a.nbuf <= 2 && a.upd.rk_stage == 0 &&
-           a.upd.etd == 0 && a.upd.nxs == 0 && a.upd.nimp <= 4;
+           a.upd.etd == 0 && a.upd.nxs == 0 && a.upd.nxf == 0 && a.upd.nimp <= 4;
 }
 
 static bool fast_z(const PassArgs<float> &a)
 {
     return a.allow_fast && a.plan.n == 256 && a.g.Z == 256 && a.g.S % 16 == 0 &&
            (a.mode == PM_FUSED || a.mode == PM_INIT) && a.nbuf <= 2 && a.upd.rk_stage == 0 && a.upd.etd == 0 &&
-           a.upd.nxs == 0 && a.upd.nimp <= 4;
+           a.upd.nxs == 0 && a.upd.nxf == 0 && a.upd.nimp <= 4;
 }
 
 // 256-column x passes that start or end in real space

@@ -24,7 +24,8 @@
  *   pf.HomogeneousModulusLinElast pf/homoLinElast.go:33-150 -> gopf_register_elastic
  *   pf.VolumeConservingLP pf/volumeConserving.go:8-61 -> gopf_register_volcons
  *   Field.Data access (host <-> device)   -> gopf_field_upload / gopf_field_download
- *   mass check pf/solver_test.go:20-27, PointMonitor pf/monitor.go:27-30 -> gopf_reduce
+ *   mass check pf/solver_test.go:20-27 -> gopf_reduce
+ *   PointMonitor pf/monitor.go:8-30       -> gopf_point_values
  */
 #ifndef GOPF_GPU_H
 #define GOPF_GPU_H
@@ -186,7 +187,13 @@ int gopf_set_newton_krylov(gopf_ctx *ctx, int maxiter, double step_size, double 
  * pf/implicitEuler.go:199-201; so does gopf_step). */
 int gopf_newton_stats(gopf_ctx *ctx, int *newton_iters, int *krylov_iters, double *residual, int *converged);
 /* Field.Data <-> device. data is a []complex128 (interleaved re, im; n complex values).
- * Upload takes the real part; the stepped fields are real. */
+ * Upload takes the real part; the stepped fields are real.  field_id is the field's
+ * Model.AddField position: a model may hold up to 4 fields, equation i evolving field i
+ * (pf/euler.go:26-47, pf/rk4.go:29-74 loop over m.Fields with m.RHS[i]).  Fields never
+ * uploaded start at zero, like pf.NewField(name, n, nil).  Multi-field models step with
+ * Euler or RK4; their explicit terms are products of powers of any fields and their
+ * implicit terms polynomials in the Laplacian or TensorialHessian / SpectralViscosity
+ * symbols.  Elastic, volume-conserving and noise terms need a single-field model. */
 int gopf_field_upload(gopf_ctx *ctx, int field_id, const double *data, size_t n);
 int gopf_field_download(gopf_ctx *ctx, int field_id, double *data, size_t n);
 /* Real-valued variants (n doubles) */
@@ -210,6 +217,9 @@ int gopf_load_float64(gopf_ctx *ctx, int field_id, const char *path);
 
 /* ---- monitors ---- */
 int gopf_reduce(gopf_ctx *ctx, int field_id, int what, double *out);
+/* PointMonitor.Add (pf/monitor.go:27-30) for n sites at once: out[k] = real(field[sites[k]]), sites
+ * being node indices (pfutil/indexPositionConversion.go:23-34).  Only the n values cross the bus. */
+int gopf_point_values(gopf_ctx *ctx, int field_id, const long long *sites, int n, double *out);
 
 /* ---- FourierTransform (pfutil/fftWrap.go) on host data, not a hot path ---- */
 /* sign -1: forward FFT, +1: unnormalised backward, of a []complex128 of length N. */

@@ -205,3 +205,70 @@ def test_size_mismatch_is_an_argument_error():
     a = np.zeros(2 * 100)
     rc = m._L.gopf_field_upload(m.handle, 0, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 100)
     assert rc == 1
+
+
+def test_reaction_diffusion_split():
+    """TestReactionDiffusion (pf/model_test.go:45-110): three fields, the derived field
+    concA^2*concB^3, and (terms, denominators) = (2, 1), (2, 1), (1, 2)."""
+    import gopf_gb300 as G
+
+    m = _host_model()
+    for f in ("concA", "concB", "concC"):
+        m.add_field(f)
+    m.add_scalar("kf", 2.0)
+    m.add_scalar("kr", 0.2)
+    m.add_equation("dconcA/dt = LAP concA - kf*concA^2*concB^3 + kr*concC")
+    m.add_equation("dconcB/dt = LAP concB - kf*concA^2*concB^3 + kr*concC")
+    m.add_equation("dconcC/dt = LAP concC - kr*concC + kf*concA^2*concB^3")
+    m.init()
+    assert [m.summary(e) for e in range(3)] == [(2, 1), (2, 1), (1, 2)]
+    assert m.derived() == [dict(kind=0, field=[0, 1], power=[2, 3], coef=[1.0, 1.0])]
+    field_terms = [t for t in m.terms() if t["source"] == G.SRC_FIELD and not t["implicit"]]
+    assert [(t["eq"], t["src_index"], t["coef"]) for t in field_terms] == [(0, 2, 0.2), (1, 2, 0.2)]
+
+
+def test_concrete_term_and_factor_order_split():
+    """TestConcreteTerm (pf/rhsBuilder_test.go:95-110) and the factor-order case at :250-270:
+    products of other fields are explicit derived fields named in sorted factor order."""
+    m = _host_model()
+    for f in ("current", "voltage", "magnetic"):
+        m.add_field(f)
+    m.add_scalar("resistance", 2.0)
+    m.add_equation("dcurrent/dt = voltage^2")
+    m.add_equation("dvoltage/dt = resistance*current^2")
+    m.add_equation("dmagnetic/dt = current*magnetic^3")
+    m.init()
+    assert [m.summary(e) for e in range(3)] == [(1, 0), (1, 0), (1, 0)]
+    assert [(d["field"], d["power"]) for d in m.derived()] == [([1], [2]), ([0], [2]), ([0, 2], [1, 3])]
+    m2 = _host_model()
+    m2.add_field("cluster")
+    m2.add_field("solute")
+    m2.add_equation("dcluster/dt = LAP cluster")
+    m2.add_equation("dsolute/dt = solute*cluster")
+    m2.init()
+    assert m2.summary(1) == (1, 0)
+    assert m2.derived() == [dict(kind=0, field=[0, 1], power=[1, 1], coef=[1.0, 1.0])]
+
+
+def test_multifield_limits():
+    """Several fields compile on the host; what the device does not step in multi-field
+    models (the elastic term, more than four fields) is rejected at init."""
+    import gopf_gb300 as G
+
+    m = _host_model()
+    m.add_field("conc")
+    m.add_field("phase")
+    m.register_elastic("LIN_ELAST", "phase", np.zeros((3, 3, 3, 3)), np.eye(3) * 0.01)
+    m.add_equation("dconc/dt = LAP conc")
+    m.add_equation("dphase/dt = LAP phase + LIN_ELAST")
+    with pytest.raises(G.GopfError) as e:
+        m.init()
+    assert e.value.status == 6
+    m5 = _host_model()
+    for i in range(5):
+        m5.add_field(f"f{i}")
+    for i in range(5):
+        m5.add_equation(f"df{i}/dt = LAP f{i}")
+    with pytest.raises(G.GopfError) as e:
+        m5.init()
+    assert e.value.status == 6

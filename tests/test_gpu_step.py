@@ -415,3 +415,30 @@ def test_pinned_host_buffers_read_in_place():
     m.step(3)
     b = m.download(0)          # pageable
     assert np.array_equal(a[0::2], b.real) and np.all(a[1::2] == 0.0)
+
+
+@pytest.mark.parametrize("dims,prec,tol", [([48, 32], "fp64", 1e-13), ([24, 24, 24], "fp64", 1e-13),
+                                           ([64, 64, 64], "fp32", 2e-6)])
+def test_point_monitor_matches_download(dims, prec, tol):
+    """PointMonitor.Add (pf/monitor.go:27-30): the value at a node, read from the device state
+    without downloading the field; node order of pfutil/indexPositionConversion.go:23-34."""
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+
+    n = int(np.prod(dims))
+    m = G.Model(dims, prec, device=0)
+    m.add_field("conc")
+    m.add_scalar("gamma", 0.5)
+    m.add_scalar("m1", -1.0)
+    m.add_equation("dconc/dt = LAP conc^3 + m1*LAP conc + m1*gamma*LAP^2 conc")
+    m.init()
+    m.set_stepper("euler", 0.05)
+    m.upload(0, uniform_field(5, n, 0.0, 0.1))
+    m.step(7)
+    full = m.download_real(0)
+    sites = np.array([0, 1, n - 1, n // 2, 12345 % n, dims[1] - 1, dims[1]])
+    vals = m.point_values(0, sites)
+    assert np.max(np.abs(vals - full[sites])) <= tol * np.max(np.abs(full))
+    with pytest.raises(G.GopfError) as e:
+        m.point_values(0, [n])
+    assert e.value.status == 1
