@@ -37,7 +37,7 @@ from ._lib import (  # noqa: F401
 __all__ = ["Model", "Batch", "GopfError", "load", "build"]
 
 _STEPPERS = {"euler": _lib.GOPF_STEPPER_EULER, "rk4": _lib.GOPF_STEPPER_RK4,
-             "implicit_euler": _lib.GOPF_STEPPER_IMPLICIT_EULER}
+             "implicit_euler": _lib.GOPF_STEPPER_IMPLICIT_EULER, "sdd": _lib.GOPF_STEPPER_SDD}
 
 
 class GopfError(RuntimeError):
@@ -282,6 +282,39 @@ class Model:
         s = ctypes.c_longlong()
         self._ck(self._L.gopf_get_step(self._h, ctypes.byref(s)))
         return s.value
+
+    # --- shrinking-dimer dynamics (pf/sdd.go); step with set_stepper("sdd", dt) ---
+    def sdd_init(self, init, final) -> None:
+        """SDD.Init: the orientation is final - init (all fields, field after field)."""
+        a = np.ascontiguousarray(np.real(init), dtype=np.float64).reshape(-1)
+        b = np.ascontiguousarray(np.real(final), dtype=np.float64).reshape(-1)
+        if a.size != b.size:
+            raise ValueError("init and final differ in size")
+        self._ck(self._L.gopf_sdd_init(self._h, _dptr(a), _dptr(b), a.size))
+
+    def sdd_set_orientation(self, v) -> None:
+        """SDD.SetInitialOrientation."""
+        a = np.ascontiguousarray(v, dtype=np.float64).reshape(-1)
+        self._ck(self._L.gopf_sdd_set_orientation(self._h, _dptr(a), a.size))
+
+    def sdd_set_params(self, alpha: float = 0.5, tau_orientation: float = 1.0, tau_length: float = 1.0,
+                       init_length: float = 0.0, min_length: float = 0.0) -> None:
+        self._ck(self._L.gopf_sdd_set_params(self._h, alpha, tau_orientation, tau_length, init_length, min_length))
+
+    def sdd_orientation(self) -> np.ndarray:
+        out = np.empty(self.N * max(1, len(self.field_names)))
+        self._ck(self._L.gopf_sdd_get_orientation(self._h, _dptr(out), out.size))
+        return out
+
+    def sdd_monitor(self) -> dict:
+        out = np.empty(5)
+        self._ck(self._L.gopf_sdd_monitor(self._h, _dptr(out)))
+        return dict(zip(("max_force", "force_power_spectrum", "max_torque", "field_norm", "field_norm_change"), out))
+
+    def sdd_dimer_length(self, t: float) -> float:
+        out = ctypes.c_double()
+        self._ck(self._L.gopf_sdd_dimer_length(self._h, t, ctypes.byref(out)))
+        return out.value
 
     def point_values(self, field: int, sites) -> np.ndarray:
         """PointMonitor.Add (pf/monitor.go:27-30) for several sites: the real field there."""

@@ -20,7 +20,7 @@ STATUS = {
     8: "GOPF_ERR_PARSE",
 }
 GOPF_FP32, GOPF_FP64 = 0, 1
-GOPF_STEPPER_EULER, GOPF_STEPPER_RK4, GOPF_STEPPER_IMPLICIT_EULER = 0, 1, 2
+GOPF_STEPPER_EULER, GOPF_STEPPER_RK4, GOPF_STEPPER_IMPLICIT_EULER, GOPF_STEPPER_SDD = 0, 1, 2, 3
 DER_PRODUCT, DER_POLY, DER_INDICATOR, DER_INDICATOR_D, DER_INDICATOR_HD, DER_WHITE_NOISE = range(6)
 NOISE_WHITE, NOISE_CONSERVATIVE = 1, 2
 SRC_NONE, SRC_FIELD, SRC_DERIVED = range(3)
@@ -88,6 +88,12 @@ SIGNATURES = {
     "gopf_synchronize": ([_vp], _i),
     "gopf_reduce": ([_vp, _i, _i, _dp], _i),
     "gopf_point_values": ([_vp, _i, ctypes.POINTER(_ll), _i, _dp], _i),
+    "gopf_sdd_init": ([_vp, _dp, _dp, _sz], _i),
+    "gopf_sdd_set_orientation": ([_vp, _dp, _sz], _i),
+    "gopf_sdd_set_params": ([_vp] + [ctypes.c_double] * 5, _i),
+    "gopf_sdd_get_orientation": ([_vp, _dp, _sz], _i),
+    "gopf_sdd_monitor": ([_vp, _dp], _i),
+    "gopf_sdd_dimer_length": ([_vp, ctypes.c_double, _dp], _i),
     "gopf_fft": ([_vp, _i, _dp, _sz], _i),
     "gopf_freq": ([_vp, _ll, _dp], _i),
     "gopf_conjugate_node": ([_vp, _ll], _ll),

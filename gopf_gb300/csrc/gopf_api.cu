@@ -276,12 +276,15 @@ template <typename R> static int ctx_alloc(gopf_ctx *ctx)
 
 void gopf_ie_free(gopf_ctx *ctx);
 int gopf_ie_step(gopf_ctx *ctx);
+void gopf_sdd_free(gopf_ctx *ctx);
+int gopf_sdd_step(gopf_ctx *ctx, long long nsteps);
 void gopf_io_free(gopf_ctx *ctx);
 
 static void ctx_free(gopf_ctx *ctx)
 {
     gopf_io_free(ctx);
     gopf_ie_free(ctx);
+    gopf_sdd_free(ctx);
     if (ctx->gexec1) cudaGraphExecDestroy(ctx->gexec1);
     if (ctx->gexecK) cudaGraphExecDestroy(ctx->gexecK);
     void *ptrs[] = {ctx->d_state, ctx->d_T, ctx->d_real, ctx->d_c128, ctx->d_red, ctx->d_redout,
@@ -488,10 +491,6 @@ static int alloc_spectral(gopf_ctx *ctx, void **p)
 
 // ---- multi-field models ----
 
-// per-field device arrays: field 0 uses the context's own, fields 1.. the multi-field set
-static void *field_state(gopf_ctx *ctx, int f) { return f == 0 ? ctx->d_state : ctx->d_fstate[f]; }
-static void *field_T(gopf_ctx *ctx, int f) { return f == 0 ? ctx->d_T : ctx->d_fT[f]; }
-static void *field_rkF(gopf_ctx *ctx, int f) { return f == 0 ? ctx->d_rkF : ctx->d_frkF[f]; }
 
 struct Mono {
     double coef;
@@ -959,7 +958,8 @@ extern "C" int gopf_equation_summary(gopf_ctx *ctx, int eq, int *ne, int *ni)
 extern "C" int gopf_set_stepper(gopf_ctx *ctx, int stepper, double dt)
 {
     if (!ctx) return GOPF_ERR_ARG;
-    if (stepper != GOPF_STEPPER_EULER && stepper != GOPF_STEPPER_RK4 && stepper != GOPF_STEPPER_IMPLICIT_EULER)
+    if (stepper != GOPF_STEPPER_EULER && stepper != GOPF_STEPPER_RK4 && stepper != GOPF_STEPPER_IMPLICIT_EULER &&
+        stepper != GOPF_STEPPER_SDD)
         return gopf_fail(ctx, GOPF_ERR_ARG, "unknown stepper");
     if (!(dt > 0.0) || !std::isfinite(dt)) return gopf_fail(ctx, GOPF_ERR_ARG, "dt must be positive");
     ctx->stepper = stepper;
@@ -1661,6 +1661,16 @@ extern "C" int gopf_step(gopf_ctx *ctx, long long nsteps)
         if (ctx->multi)
             for (int f = 1; f < ctx->nfields; ++f)
                 if ((rc = alloc_spectral(ctx, &ctx->d_frkF[f]))) return rc;
+    }
+    if (ctx->stepper == GOPF_STEPPER_SDD) {
+        // a host-driven saddle search (pf/sdd.go): no graphs
+        if ((rc = gopf_sdd_step(ctx, nsteps))) return rc;
+        ctx->step += nsteps;
+        if (ctx->check_finite) {
+            if ((rc = check_device_status(ctx))) return rc;
+            if ((rc = check_finite_state(ctx))) return rc;
+        }
+        return GOPF_OK;
     }
     if (ctx->stepper == GOPF_STEPPER_IMPLICIT_EULER && ctx->multi)
         return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "implicit Euler steps single-field models (multi-field: Euler, RK4)");

@@ -69,6 +69,7 @@ struct gopf_special {
 };
 
 struct gopf_ie_work;
+struct gopf_sdd_work;
 struct gopf_io_state;
 
 struct gopf_ctx {
@@ -189,9 +190,18 @@ struct gopf_ctx {
     int nk_last_newton = 0, nk_last_krylov = 0, nk_last_converged = 0;
     double nk_last_residual = 0.0;
     gopf_ie_work *ie = nullptr;
+    // shrinking-dimer dynamics (pf/sdd.go): parameters of SDD and its device workspace
+    double sdd_alpha = 0.5, sdd_tau_orient = 1.0, sdd_tau_len = 1.0, sdd_init_len = 0.0, sdd_min_len = 0.0;
+    long long sdd_step = 0; // SDD.CurrentStep
+    gopf_sdd_work *sdd = nullptr;
     gopf_io_state *io = nullptr; // field files: pinned staging buffer and writer thread
     std::string err;
 };
+
+// per-field device arrays: field 0 uses the context's own, fields 1.. the multi-field set
+inline void *field_state(gopf_ctx *ctx, int f) { return f == 0 ? ctx->d_state : ctx->d_fstate[f]; }
+inline void *field_T(gopf_ctx *ctx, int f) { return f == 0 ? ctx->d_T : ctx->d_fT[f]; }
+inline void *field_rkF(gopf_ctx *ctx, int f) { return f == 0 ? ctx->d_rkF : ctx->d_frkF[f]; }
 
 int gopf_fail(gopf_ctx *ctx, int code, const std::string &msg);
 int gopf_compile_model(gopf_ctx *ctx);

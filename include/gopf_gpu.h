@@ -15,6 +15,7 @@
  *   pf.Euler.Step    pf/euler.go:16-47    -> gopf_step (GOPF_STEPPER_EULER)
  *   pf.RK4.Step      pf/rk4.go:29-74      -> gopf_step (GOPF_STEPPER_RK4)
  *   pf.ImplicitEuler.Step pf/implicitEuler.go:165-207 -> gopf_step (GOPF_STEPPER_IMPLICIT_EULER)
+ *   pf.SDD (shrinking-dimer dynamics) pf/sdd.go:86-470 -> gopf_step (GOPF_STEPPER_SDD), gopf_sdd_*
  *   pf.FourierTransform pf/solver.go:22-26, pfutil/fftWrap.go:26-95
  *                                         -> gopf_fft / gopf_freq / gopf_conjugate_node
  *   pf.Model.AddField/AddScalar/AddEquation/RegisterFunction/Init
@@ -55,7 +56,7 @@ enum {
 enum { GOPF_FP32 = 0, GOPF_FP64 = 1 };
 
 /* time steppers */
-enum { GOPF_STEPPER_EULER = 0, GOPF_STEPPER_RK4 = 1, GOPF_STEPPER_IMPLICIT_EULER = 2 };
+enum { GOPF_STEPPER_EULER = 0, GOPF_STEPPER_RK4 = 1, GOPF_STEPPER_IMPLICIT_EULER = 2, GOPF_STEPPER_SDD = 3 };
 
 /* derived-field kinds (real-space pointwise functions of one field) */
 enum {
@@ -214,6 +215,25 @@ int gopf_save_float64(gopf_ctx *ctx, int field_id, const char *path, int async);
 int gopf_io_wait(gopf_ctx *ctx);
 /* LoadFloat64 (pf/fileIO.go:64-83) followed by gopf_field_upload_real: restart from a saved field. */
 int gopf_load_float64(gopf_ctx *ctx, int field_id, const char *path);
+
+/* ---- shrinking-dimer dynamics (pf/sdd.go), stepped by gopf_step with GOPF_STEPPER_SDD ----
+ * The orientation is nfields * N reals, field after field in node order.  gopf_sdd_init is
+ * SDD.Init (pf/sdd.go:386-404: final - init, its length the initial dimer length) and
+ * gopf_sdd_set_orientation SDD.SetInitialOrientation (:409-424); either starts a new dimer at
+ * time 0, as NewSDD does.  gopf_sdd_set_params sets Alpha, TimeConstants.Orientation,
+ * TimeConstants.DimerLength, InitDimerLength (when > 0) and MinDimerLength (defaults 0.5, 1, 1,
+ * -, 0, pf/sdd.go:118-127).  gopf_sdd_monitor gives the SDDMonitor fields (:27-52): MaxForce,
+ * ForcePowerSpectrum, MaxTorque, FieldNorm, FieldNormChange.  SDD steps models with polynomial
+ * explicit terms and Laplacian-polynomial implicit terms; it rejects modal filters, as the
+ * reference's SetFilter panics (:426-430). */
+int gopf_sdd_init(gopf_ctx *ctx, const double *init, const double *final, size_t n);
+int gopf_sdd_set_orientation(gopf_ctx *ctx, const double *orientation, size_t n);
+int gopf_sdd_set_params(gopf_ctx *ctx, double alpha, double tau_orientation, double tau_length, double init_length,
+                        double min_length);
+int gopf_sdd_get_orientation(gopf_ctx *ctx, double *orientation, size_t n);
+int gopf_sdd_monitor(gopf_ctx *ctx, double *out5);
+/* DimerLength(t) (pf/sdd.go:355-362) */
+int gopf_sdd_dimer_length(gopf_ctx *ctx, double t, double *length);
 
 /* ---- monitors ---- */
 int gopf_reduce(gopf_ctx *ctx, int field_id, int what, double *out);

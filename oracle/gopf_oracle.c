@@ -1123,3 +1123,238 @@ void or_uniform_field(uint64_t seed, long n, double center, double half_width, d
         out[i] = center + half_width * (2.0 * u - 1.0);
     }
 }
+
+/* ------------------------------------------------------------------ */
+/* Shrinking-dimer dynamics, SDD (pf/sdd.go:86-470)                    */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+    or_model *m;
+    double *orient; /* nfields * N, unit length */
+    double alpha, dt, tau_orient, tau_len, init_len, min_len;
+    long step;
+    /* SDDMonitor (pf/sdd.go:27-52): MaxForce, ForcePowerSpectrum, MaxTorque, FieldNorm, FieldNormChange */
+    double mon[5];
+} or_sdd;
+
+/* NewSDD (pf/sdd.go:118-127): alpha 0.5, both time constants 1 */
+or_sdd *or_sdd_create(or_model *m)
+{
+    or_sdd *s = (or_sdd *)calloc(1, sizeof(or_sdd));
+    s->m = m;
+    s->orient = (double *)calloc((size_t)m->N * (size_t)m->nfields, sizeof(double));
+    s->alpha = 0.5;
+    s->tau_orient = 1.0;
+    s->tau_len = 1.0;
+    return s;
+}
+
+void or_sdd_destroy(or_sdd *s)
+{
+    if (!s) return;
+    free(s->orient);
+    free(s);
+}
+
+void or_sdd_set_params(or_sdd *s, double alpha, double dt, double tau_orient, double tau_len, double init_len,
+                       double min_len)
+{
+    s->alpha = alpha;
+    s->dt = dt;
+    s->tau_orient = tau_orient;
+    s->tau_len = tau_len;
+    if (init_len > 0.0) s->init_len = init_len;
+    s->min_len = min_len;
+}
+
+double *or_sdd_orientation(or_sdd *s) { return s->orient; }
+double *or_sdd_monitor(or_sdd *s) { return s->mon; }
+double or_sdd_init_length(or_sdd *s) { return s->init_len; }
+
+static void or_sdd_normalise(or_sdd *s, long n)
+{
+    double len = 0.0;
+    for (long i = 0; i < n; ++i) len += s->orient[i] * s->orient[i];
+    len = sqrt(len);
+    for (long i = 0; i < n; ++i) s->orient[i] /= len;
+}
+
+/* Init (pf/sdd.go:386-404): orientation = final - init (real parts, all fields), its length is
+ * the initial dimer length. */
+void or_sdd_init(or_sdd *s, const double *init, const double *final)
+{
+    const long n = s->m->N * s->m->nfields;
+    double len = 0.0;
+    for (long i = 0; i < n; ++i) {
+        s->orient[i] = final[i] - init[i];
+        len += s->orient[i] * s->orient[i];
+    }
+    s->init_len = sqrt(len);
+    for (long i = 0; i < n; ++i) s->orient[i] /= s->init_len;
+}
+
+/* SetInitialOrientation (pf/sdd.go:409-424) */
+void or_sdd_set_orientation(or_sdd *s, const double *v)
+{
+    const long n = s->m->N * s->m->nfields;
+    double len = 0.0;
+    for (long i = 0; i < n; ++i) len += v[i] * v[i];
+    s->init_len = sqrt(len);
+    for (long i = 0; i < n; ++i) s->orient[i] = v[i] / s->init_len;
+}
+
+/* DimerLength (pf/sdd.go:355-362) */
+double or_sdd_dimer_length(const or_sdd *s, double t)
+{
+    const double l = s->init_len * exp(-t / s->tau_len);
+    return (l < s->min_len) ? s->min_len : l;
+}
+
+/* householder (pf/sdd.go:303-318): data -= sigma * o * (sum data conj(o)) / num_nodes */
+void or_householder(double *data_, const double *orient_, double sigma, long n, long num_nodes)
+{
+    cpx *data = (cpx *)data_;
+    const cpx *o = (const cpx *)orient_;
+    cpx dot = 0.0;
+    for (long i = 0; i < n; ++i) dot += data[i] * conj(o[i]);
+    dot /= (double)num_nodes;
+    for (long i = 0; i < n; ++i) data[i] = data[i] - sigma * o[i] * dot;
+}
+
+/* diagonalShermannMorrison.dot (pf/sdd.go:456-470): vec <- (D + u v^T)^-1 vec with D^-1 = inv_diag */
+void or_dsm_dot(const double *inv_diag_, const double *u_, const double *v_, long n, double *vec_)
+{
+    const cpx *d = (const cpx *)inv_diag_, *u = (const cpx *)u_, *v = (const cpx *)v_;
+    cpx *x = (cpx *)vec_;
+    cpx den = 1.0, vdx = 0.0;
+    for (long i = 0; i < n; ++i) {
+        den += u[i] * d[i] * v[i];
+        vdx += v[i] * d[i] * x[i];
+    }
+    for (long i = 0; i < n; ++i) x[i] = d[i] * x[i] - d[i] * u[i] * vdx / den;
+}
+
+/* householderDenum (pf/sdd.go:320-339) followed by its dot: vec <- (I - dt (denum - sigma denum o o^H / n))^-1 vec */
+static void or_sdd_denum_solve(const cpx *denum, const cpx *o, double sigma, double dt, long n, cpx *vec, cpx *w3)
+{
+    cpx *inv = w3, *v = w3 + n;
+    for (long i = 0; i < n; ++i) {
+        inv[i] = 1.0 / (1.0 - dt * denum[i]);
+        v[i] = sigma * denum[i] * dt * conj(o[i]) / (double)n;
+    }
+    or_dsm_dot((const double *)inv, (const double *)o, (const double *)v, n, (double *)vec);
+}
+
+void or_sdd_denum_dot(const double *denum, const double *orient, double sigma, double dt, long n, double *vec)
+{
+    cpx *w = (cpx *)malloc(sizeof(cpx) * 2 * (size_t)n);
+    or_sdd_denum_solve((const cpx *)denum, (const cpx *)orient, sigma, dt, n, (cpx *)vec, w);
+    free(w);
+}
+
+static void or_sdd_shift(or_sdd *s, double scale)
+{
+    or_model *m = s->m;
+    long k = 0;
+    for (int f = 0; f < m->nfields; ++f)
+        for (long j = 0; j < m->N; ++j, ++k) m->fields[f][j] += scale * s->orient[k];
+}
+
+/* the model's fields (synced derived fields first) to k space, and back */
+static void or_sdd_fft(or_model *m)
+{
+    or_sync_derived(m);
+    or_fft_fields(m, -1);
+    or_fft_derived(m);
+}
+
+/* SDD.Step (pf/sdd.go:159-285) */
+int or_sdd_step(or_sdd *s, long nsteps)
+{
+    or_model *m = s->m;
+    const long N = m->N;
+    const int nf = m->nfields;
+    if (s->dt < 1e-16) return 1; /* checkTimeStep panics */
+    cpx *ftO = (cpx *)malloc(sizeof(cpx) * (size_t)N * nf);
+    cpx *rs = (cpx *)malloc(sizeof(cpx) * (size_t)N * nf);
+    cpx *re = (cpx *)malloc(sizeof(cpx) * (size_t)N * nf);
+    cpx *work = (cpx *)malloc(sizeof(cpx) * (size_t)N);
+    cpx *orig = (cpx *)malloc(sizeof(cpx) * (size_t)N);
+    cpx *tmp = (cpx *)malloc(sizeof(cpx) * (size_t)N);
+    cpx *den = (cpx *)malloc(sizeof(cpx) * (size_t)N);
+    cpx *w3 = (cpx *)malloc(sizeof(cpx) * 2 * (size_t)N);
+    for (long st = 0; st < nsteps; ++st) {
+        double fnorm = 0.0;
+        for (int f = 0; f < nf; ++f)
+            for (long j = 0; j < N; ++j) {
+                const double a = cabs(m->fields[f][j]);
+                fnorm += a * a;
+            }
+        s->mon[4] = s->mon[3] - fnorm;
+        s->mon[3] = fnorm;
+        for (long i = 0; i < N * nf; ++i) ftO[i] = s->orient[i];
+        for (int f = 0; f < nf; ++f) or_fft(m, ftO + (long)f * N, -1);
+        const double t = (double)s->step * s->dt;
+        const double l = or_sdd_dimer_length(s, t);
+
+        or_sdd_shift(s, -0.5 * l); /* start image */
+        or_sdd_fft(m);
+        for (int f = 0; f < nf; ++f) or_get_rhs(m, f, rs + (long)f * N, tmp);
+        or_ifft_fields(m);
+        or_sdd_shift(s, l); /* end image */
+        or_sdd_fft(m);
+        for (int f = 0; f < nf; ++f) or_get_rhs(m, f, re + (long)f * N, tmp);
+        or_ifft_fields(m);
+        or_sdd_shift(s, -0.5 * l); /* back to the centre */
+        or_sdd_fft(m);
+
+        double maxf = 0.0, fps = 0.0;
+        for (int f = 0; f < nf; ++f) {
+            cpx *d = m->fields[f];
+            memcpy(orig, d, sizeof(cpx) * (size_t)N);
+            /* the force at the centre: the reference weighs the first field's start and end
+             * right-hand sides for every field (rhsStart[j], rhsEnd[j] with j < NumNodes) */
+            for (long j = 0; j < N; ++j) work[j] = s->alpha * rs[j] + (1.0 - s->alpha) * re[j];
+            or_householder((double *)work, (const double *)(ftO + (long)f * N), 2.0, N, N);
+            for (long j = 0; j < N; ++j) d[j] = d[j] + s->dt * work[j];
+            or_get_denum(m, f, den, tmp);
+            or_sdd_denum_solve(den, ftO + (long)f * N, 2.0, s->dt, N, d, w3);
+            for (long j = 0; j < N; ++j) {
+                const double diff = cabs((d[j] - orig[j]) / s->dt);
+                fps += diff * diff / (double)N;
+                if (diff > maxf) maxf = diff;
+            }
+        }
+        s->mon[0] = maxf;
+        s->mon[1] = sqrt(fps / (double)(nf * N));
+
+        /* torque: F(start) - F(end) plus the linear part -L v l */
+        for (long i = 0; i < N * nf; ++i) rs[i] = rs[i] - re[i];
+        for (int f = 0; f < nf; ++f) {
+            or_get_denum(m, f, den, tmp);
+            for (long j = 0; j < N; ++j) rs[(long)f * N + j] -= den[j] * ftO[(long)f * N + j] * l;
+        }
+        or_householder((double *)rs, (const double *)ftO, 1.0, N * nf, N);
+        for (int f = 0; f < nf; ++f) or_fft(m, rs + (long)f * N, +1);
+        for (long i = 0; i < N * nf; ++i) rs[i] /= (double)N;
+        double maxt = 0.0;
+        const double lt = or_sdd_dimer_length(s, t);
+        for (long i = 0; i < N * nf; ++i) {
+            s->orient[i] -= s->dt * creal(rs[i]) / (lt * s->tau_orient);
+            if (fabs(creal(rs[i])) > maxt) maxt = fabs(creal(rs[i]));
+        }
+        s->mon[2] = maxt;
+        or_sdd_normalise(s, N * nf);
+        or_ifft_fields(m);
+        s->step++;
+    }
+    free(ftO);
+    free(rs);
+    free(re);
+    free(work);
+    free(orig);
+    free(tmp);
+    free(den);
+    free(w3);
+    return 0;
+}

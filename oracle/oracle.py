@@ -99,6 +99,25 @@ def lib():
         L.or_filter_eval.restype = ctypes.c_double
         L.or_set_filter.argtypes = [vp, dp, ctypes.c_int]
         L.or_set_filter.restype = ctypes.c_int
+        L.or_sdd_create.argtypes = [vp]
+        L.or_sdd_create.restype = vp
+        L.or_sdd_destroy.argtypes = [vp]
+        L.or_sdd_set_params.argtypes = [vp] + [ctypes.c_double] * 6
+        L.or_sdd_orientation.argtypes = [vp]
+        L.or_sdd_orientation.restype = dp
+        L.or_sdd_monitor.argtypes = [vp]
+        L.or_sdd_monitor.restype = dp
+        L.or_sdd_init_length.argtypes = [vp]
+        L.or_sdd_init_length.restype = ctypes.c_double
+        L.or_sdd_init.argtypes = [vp, dp, dp]
+        L.or_sdd_set_orientation.argtypes = [vp, dp]
+        L.or_sdd_dimer_length.argtypes = [vp, ctypes.c_double]
+        L.or_sdd_dimer_length.restype = ctypes.c_double
+        L.or_sdd_step.argtypes = [vp, ctypes.c_long]
+        L.or_sdd_step.restype = ctypes.c_int
+        L.or_householder.argtypes = [dp, dp, ctypes.c_double, ctypes.c_long, ctypes.c_long]
+        L.or_dsm_dot.argtypes = [dp, dp, dp, ctypes.c_long, dp]
+        L.or_sdd_denum_dot.argtypes = [dp, dp, ctypes.c_double, ctypes.c_double, ctypes.c_long, dp]
         _lib = L
     return _lib
 
@@ -324,3 +343,80 @@ def cahn_hilliard(dims, gamma: float, M: float = 1.0, splitting: str = "plain") 
     else:
         raise ValueError(splitting)
     return m
+
+
+def _cdp(a):
+    return a.view(np.float64).ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def householder(data, orient, sigma: float, num_nodes: int) -> np.ndarray:
+    """SDD.householder (pf/sdd.go:303-318) on copies of two complex vectors."""
+    d = np.array(data, dtype=np.complex128)
+    o = np.ascontiguousarray(orient, dtype=np.complex128)
+    lib().or_householder(_cdp(d), _cdp(o), float(sigma), d.size, int(num_nodes))
+    return d
+
+
+def dsm_dot(inv_diag, u, v, vec) -> np.ndarray:
+    """diagonalShermannMorrison.dot (pf/sdd.go:456-470)."""
+    arrs = [np.ascontiguousarray(a, dtype=np.complex128) for a in (inv_diag, u, v)]
+    x = np.array(vec, dtype=np.complex128)
+    lib().or_dsm_dot(_cdp(arrs[0]), _cdp(arrs[1]), _cdp(arrs[2]), x.size, _cdp(x))
+    return x
+
+
+def sdd_denum_dot(denum, orient, sigma: float, dt: float, vec) -> np.ndarray:
+    """SDD.householderDenum(denum, orient, sigma).dot(vec) (pf/sdd.go:320-339)."""
+    d = np.ascontiguousarray(denum, dtype=np.complex128)
+    o = np.ascontiguousarray(orient, dtype=np.complex128)
+    x = np.array(vec, dtype=np.complex128)
+    lib().or_sdd_denum_dot(_cdp(d), _cdp(o), float(sigma), float(dt), x.size, _cdp(x))
+    return x
+
+
+class SDD:
+    """Shrinking-dimer dynamics stepper (pf/sdd.go) over an oracle Model."""
+
+    def __init__(self, model: Model):
+        self.model = model
+        self._L = lib()
+        self._h = self._L.or_sdd_create(model._h)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._L.or_sdd_destroy(h)
+            self._h = None
+
+    def set_params(self, dt: float, alpha: float = 0.5, tau_orient: float = 1.0, tau_len: float = 1.0,
+                   init_len: float = 0.0, min_len: float = 0.0) -> None:
+        self._L.or_sdd_set_params(self._h, alpha, dt, tau_orient, tau_len, init_len, min_len)
+
+    def init(self, init_fields, final_fields) -> None:
+        a = np.ascontiguousarray(np.real(init_fields), dtype=np.float64).reshape(-1)
+        b = np.ascontiguousarray(np.real(final_fields), dtype=np.float64).reshape(-1)
+        self._L.or_sdd_init(self._h, _dp(a), _dp(b))
+
+    def set_orientation(self, v) -> None:
+        a = np.ascontiguousarray(v, dtype=np.float64).reshape(-1)
+        self._L.or_sdd_set_orientation(self._h, _dp(a))
+
+    def dimer_length(self, t: float) -> float:
+        return float(self._L.or_sdd_dimer_length(self._h, t))
+
+    @property
+    def init_length(self) -> float:
+        return float(self._L.or_sdd_init_length(self._h))
+
+    def step(self, nsteps: int) -> None:
+        if self._L.or_sdd_step(self._h, nsteps) != 0:
+            raise ValueError("SDD: time step not set")
+
+    def orientation(self) -> np.ndarray:
+        p = self._L.or_sdd_orientation(self._h)
+        return np.ctypeslib.as_array(p, shape=(self.model.N * self.model.nfields,)).copy()
+
+    def monitor(self) -> dict:
+        p = self._L.or_sdd_monitor(self._h)
+        v = np.ctypeslib.as_array(p, shape=(5,)).copy()
+        return dict(zip(("max_force", "force_power_spectrum", "max_torque", "field_norm", "field_norm_change"), v))
