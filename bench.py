@@ -418,7 +418,8 @@ def run_sweep(args):
            "config": {"workload": "sweep_64_ch2d_uneven_fp32", "sides": [p[0] for p in params], "cells": cells,
                       "dt": 0.05, "params_seed": 2, "init": "c0 = 0.5 + U(-0.05, 0.05), seed 1000 + i"},
            "sequential_value": seq, "speedup_vs_sequential": batched / seq,
-           "cell_updates_per_s": batched * cells, "clocks": clk.summary(), "gpu_launches": 3 * args.steps}
+           "cell_updates_per_s": batched * cells, "clocks": clk.summary(),
+           "gpu_launches": batch.kernels_per_step() * args.steps}
     if args.check_steps > 0:
         # per-instance rel-L2 of the FP32 batch against sequential FP64 runs after check_steps steps
         a = sweep_models("fp32", params)

@@ -394,6 +394,11 @@ class Batch:
     def step(self, nsteps: int) -> None:
         self._ck(self._L.gopf_batch_step(self._h, int(nsteps)))
 
+    def kernels_per_step(self) -> int:
+        n = ctypes.c_int()
+        self._ck(self._L.gopf_batch_kernels_per_step(self._h, ctypes.byref(n)))
+        return n.value
+
     def set_stream(self, stream_handle: int | None) -> None:
         self._ck(self._L.gopf_batch_set_stream(self._h, ctypes.c_void_p(stream_handle or 0)))
 

@@ -1,0 +1,385 @@
+// fastline.cuh -- register-resident FP32 line transforms of length L = 16 T (T = 16, 24, 32, 48,
+// 64: L = 256, 384, 512, 768, 1024) for the batched 2D sweep.
+//
+// A line is held by T threads, 16 values each.  Forward transform (decimation in time):
+//   A: thread r holds x[r + T i] (i < 16): radix-16 DFT over i in registers, twiddle W_L^(r k1)
+//      -> Y[r][k1]; exchange through shared memory;
+//   B: X[k1 + 16 k2] = sum_r W_T^(r k2) Y[r][k1], a DFT of length T = P U per k1, split as
+//      r = U s + u: a radix-P DFT over s in registers (P = 16, or two radix-8 DFTs for two k1
+//      when T = 8 U), twiddle W_T^(u c), then a radix-U DFT across the U threads of a column:
+//      warp shuffles for U = 2, 4, a second shared-memory exchange for U = 3.
+// The output stays distributed ("B layout": a thread holds X[k1 + 16 c + 16 P' d] for its own
+// column and one d), which is where the k-space update happens.  The inverse transform runs the
+// same steps in reverse order with conjugate twiddles (decimation in frequency), so it takes the
+// B layout and ends in the A layout x[r + T i] that was loaded: the update pass reads and writes
+// every line in place, coalesced.  L = 256 (T = 16, U = 1) is the engine of fast256.cuh.
+//
+// The x pass packs two real rows a, b as one complex line a + i b of L columns (Hermitian
+// extension of their half spectra on input, separation of the two spectra on output), so both
+// passes of a 2D step use the same engine with L = the side of the instance.
+#pragma once
+#include "fast256.cuh"
+
+namespace gopf {
+namespace fl {
+
+using f256::pdft16;
+
+template <int L> struct Geo {
+    static constexpr int T = L / 16;                 // threads per line
+    static constexpr bool P8 = (T == 24);            // second stage: two radix-8 DFTs per thread
+    static constexpr int P = P8 ? 8 : 16;            // radix of the in-register second stage
+    static constexpr int U = T / P;                  // threads sharing one column DFT (1, 2, 3, 4)
+    static constexpr int NT = (U == 3) ? 192 : 256;  // threads per block
+    static constexpr int LPB = NT / T;               // lines per block
+    static constexpr int PAD = (T == 24) ? 4 : 0;    // slot offset between lines (bank spread)
+    static constexpr int LREG = 16 * T + PAD;        // shared slots per line
+    static_assert(L == 256 || L == 384 || L == 512 || L == 768 || L == 1024, "line length");
+};
+
+// low 4 bits of a row -> a permutation whose bit 3 is the row's bit 0: rows that differ in bit 0
+// land in opposite halves of the 16 banks (conflict-free column reads for U = 2, 4)
+__device__ __forceinline__ int hsw(int row) { return ((row & 1) << 3) | ((row >> 1) & 7); }
+__device__ __forceinline__ int slot(int row, int col) { return row * 16 + (col ^ hsw(row)); }
+
+// the thread's role in stage B: column k1 (or the pair a, a + 8), its u, and the d it keeps
+template <int L> struct Role {
+    int k1, u, d;
+    __device__ __forceinline__ Role(int r)
+    {
+        typedef Geo<L> G;
+        if constexpr (G::U == 1) {
+            k1 = r;
+            u = 0;
+        } else if constexpr (G::U == 2) {
+            u = (r >> 3) & 1;
+            k1 = (r & 7) | ((r >> 4) << 3);
+        } else if constexpr (G::U == 4) {
+            u = (r >> 3) & 3;
+            k1 = (r & 7) | ((r >> 5) << 3);
+        } else if constexpr (G::P8) { // T = 24
+            u = r >> 3;
+            k1 = r & 7; // and k1 + 8
+        } else { // T = 48
+            u = r >> 4;
+            k1 = r & 15;
+        }
+        d = (G::U == 4) ? (((u & 1) << 1) | (u >> 1)) : u;
+    }
+    // index along the line of the thread's value j in the B layout
+    __device__ __forceinline__ int elem(int j) const
+    {
+        typedef Geo<L> G;
+        if constexpr (G::P8) return k1 + ((j >> 3) << 3) + 16 * (j & 7) + 128 * d;
+        else return k1 + 16 * j + 256 * d;
+    }
+};
+
+__device__ __forceinline__ float2 cm(float2 a, float2 w) { return make_float2(a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x); }
+__device__ __forceinline__ float2 cmc(float2 a, float2 w) { return make_float2(a.x * w.x + a.y * w.y, a.y * w.x - a.x * w.y); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 shfl2(float2 v, int m)
+{
+    return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+// multiply by -i (forward) or +i (inverse)
+template <bool INV> __device__ __forceinline__ float2 mi(float2 a) { return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x); }
+
+// radix-U DFT across the U threads of a column, U = 2 or 4 (forward keeps d, inverse ends in u)
+template <int U, bool INV> __device__ __forceinline__ void xdft_fwd(float2 (&v)[16], int u)
+{
+    if constexpr (U == 2) {
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+            const float2 o = shfl2(v[c], 8);
+            v[c] = u ? sub2(o, v[c]) : add2(v[c], o);
+        }
+    } else { // U = 4, u = 2 u1 + u0: first across u1 (lane bit 4), then across u0 (lane bit 3)
+        const int u0 = u & 1, u1 = u >> 1;
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+            const float2 o = shfl2(v[c], 16);
+            float2 e = u1 ? sub2(o, v[c]) : add2(v[c], o); // E[u0][d0 = u1]
+            if (u0 && u1) e = mi<INV>(e);                   // W_4^(u0 d0)
+            const float2 o2 = shfl2(e, 8);
+            v[c] = u0 ? sub2(o2, e) : add2(e, o2);         // X[d0 + 2 d1], d1 = u0
+        }
+    }
+}
+
+template <int U, bool INV> __device__ __forceinline__ void xdft_inv(float2 (&v)[16], int u)
+{
+    if constexpr (U == 2) {
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+            const float2 o = shfl2(v[c], 8);
+            v[c] = u ? sub2(o, v[c]) : add2(v[c], o);
+        }
+    } else {
+        const int u0 = u & 1, u1 = u >> 1;
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+            const float2 o = shfl2(v[c], 8);
+            float2 g = u0 ? sub2(o, v[c]) : add2(v[c], o); // G[d0 = u1][u0]
+            if (u0 && u1) g = mi<INV>(g);                   // conj(W_4^(u0 d0)) on the inverse
+            const float2 o2 = shfl2(g, 16);
+            v[c] = u1 ? sub2(o2, g) : add2(g, o2);
+        }
+    }
+}
+
+// radix-3 across the three threads of a column through shared memory (U = 3): the thread keeps
+// output d = u.  z is this line's slot region; the caller synchronises around.
+template <int L, bool INV>
+__device__ __forceinline__ void xdft3(float2 (&v)[16], const Role<L> &ro, float2 *z)
+{
+    typedef Geo<L> G;
+    // slot of (u, j, column): j < 16 values of the column
+    auto s3 = [&](int uu, int j, int col) -> float2 & {
+        if constexpr (G::P8) return z[(uu * 8 + (j & 7)) * 16 + ((col + (j >> 3) * 8) ^ ((uu & 1) << 3))];
+        else return z[(uu * 16 + j) * 16 + col];
+    };
+#pragma unroll
+    for (int j = 0; j < 16; ++j) s3(ro.u, j, ro.k1) = v[j];
+    __syncthreads();
+    const float c3 = -0.5f, s3v = INV ? 0.86602540378443864676f : -0.86602540378443864676f;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        const float2 a = s3(0, j, ro.k1), b = s3(1, j, ro.k1), c = s3(2, j, ro.k1);
+        if (ro.u == 0) v[j] = add2(a, add2(b, c));
+        else {
+            // X_d = a + W3^d b + W3^(2d) c, W3 = c3 + i s3v (forward: s3v < 0)
+            const float sd = (ro.u == 1) ? s3v : -s3v;
+            const float2 w1 = make_float2(c3, sd);
+            v[j] = add2(a, add2(cm(b, w1), cm(c, make_float2(c3, -sd))));
+        }
+    }
+    __syncthreads();
+}
+
+// radix-8 DFT (natural order in and out) on v[o .. o+7]
+template <bool INV> __device__ __forceinline__ void dft8at(float2 (&v)[16], int o)
+{
+    float2 t[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) t[q] = v[o + q];
+    dft8<INV>(t);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[o + q] = t[q];
+}
+
+// Forward transform of the thread's line: in v[i] = x[r + T i]; out v[j] = X[ro.elem(j)].
+// z: the line's slot region; tw: W_L^t (t < L).  Leaves the slots free (ends with a barrier).
+template <int L>
+__device__ __forceinline__ void line_fwd(float2 (&v)[16], int r, const Role<L> &ro, float2 *z, const float2 *tw)
+{
+    typedef Geo<L> G;
+    pdft16<false>(v);
+#pragma unroll
+    for (int k1 = 1; k1 < 16; ++k1) v[k1] = cm(v[k1], tw[r * k1]);
+#pragma unroll
+    for (int k1 = 0; k1 < 16; ++k1) z[slot(r, k1)] = v[k1];
+    __syncthreads();
+    if constexpr (G::P8) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int s = 0; s < 8; ++s) v[8 * h + s] = z[slot(G::U * s + ro.u, ro.k1 + 8 * h)];
+        __syncthreads();
+        dft8at<false>(v, 0);
+        dft8at<false>(v, 8);
+        if (ro.u)
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+                if (j & 7) v[j] = cm(v[j], tw[16 * ro.u * (j & 7)]); // W_T^(u c) = W_L^(16 u c)
+    } else {
+#pragma unroll
+        for (int s = 0; s < 16; ++s) v[s] = z[slot(G::U * s + ro.u, ro.k1)];
+        __syncthreads();
+        pdft16<false>(v);
+        if (G::U > 1 && ro.u)
+#pragma unroll
+            for (int c = 1; c < 16; ++c) v[c] = cm(v[c], tw[16 * ro.u * c]);
+    }
+    if constexpr (G::U == 2 || G::U == 4) xdft_fwd<G::U, false>(v, ro.u);
+    else if constexpr (G::U == 3) xdft3<L, false>(v, ro, z);
+}
+
+// Inverse (unnormalised) transform: in v[j] = X[ro.elem(j)]; out v[i] = x[r + T i] * L.
+template <int L>
+__device__ __forceinline__ void line_inv(float2 (&v)[16], int r, const Role<L> &ro, float2 *z, const float2 *tw)
+{
+    typedef Geo<L> G;
+    if constexpr (G::U == 2 || G::U == 4) xdft_inv<G::U, true>(v, ro.u);
+    else if constexpr (G::U == 3) xdft3<L, true>(v, ro, z);
+    if constexpr (G::P8) {
+        if (ro.u)
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+                if (j & 7) v[j] = cmc(v[j], tw[16 * ro.u * (j & 7)]);
+        dft8at<true>(v, 0);
+        dft8at<true>(v, 8);
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int s = 0; s < 8; ++s) z[slot(G::U * s + ro.u, ro.k1 + 8 * h)] = v[8 * h + s];
+    } else {
+        if (G::U > 1 && ro.u)
+#pragma unroll
+            for (int c = 1; c < 16; ++c) v[c] = cmc(v[c], tw[16 * ro.u * c]);
+        pdft16<true>(v);
+#pragma unroll
+        for (int s = 0; s < 16; ++s) z[slot(G::U * s + ro.u, ro.k1)] = v[s];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k1 = 0; k1 < 16; ++k1) v[k1] = z[slot(r, k1)];
+    __syncthreads();
+#pragma unroll
+    for (int k1 = 1; k1 < 16; ++k1) v[k1] = cmc(v[k1], tw[r * k1]);
+    pdft16<true>(v);
+}
+
+template <int L> constexpr int yline_smem_bytes() { return (Geo<L>::LPB * Geo<L>::LREG + L + L) * 8; }
+
+// One y tile of the 2D fused Euler update (pf/euler.go:16-47; plain form, no noise or filter):
+// LPB lines q0 .. of length L = g.Y, groups a.buf[0 .. ng), c-hat a.state, T <- inverse(c_new/N).
+template <int L, int NG> __device__ __forceinline__ void yline_tile(const PassArgs<float> &a, long long tile)
+{
+    typedef Geo<L> G;
+    extern __shared__ __align__(16) unsigned char fl_dsm[];
+    float2 *s_x = reinterpret_cast<float2 *>(fl_dsm);
+    float2 *s_tw = s_x + G::LPB * G::LREG;
+    float *s_fy = reinterpret_cast<float *>(s_tw + L);
+    const Geom &g = a.g;
+    const int l = threadIdx.x / G::T, r = threadIdx.x - l * G::T;
+    const long long nlines = (long long)g.Z * g.KX;
+    const long long q = tile * G::LPB + l;
+    const bool valid = q < nlines;
+    float2 *z = s_x + l * G::LREG;
+    const float2 zero = make_float2(0.f, 0.f);
+    for (int t = threadIdx.x; t < L; t += G::NT) {
+        s_tw[t] = a.tw[t];
+        s_fy[t] = f256::fsqf(t, g.Y);
+    }
+    const Role<L> ro(r);
+    const float2 *__restrict__ U0 = a.buf[0];
+    float2 v[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = valid ? U0[q * L + r + G::T * i] : zero;
+    __syncthreads();
+    line_fwd<L>(v, r, ro, z, s_tw);
+    const UpdTable &u = a.upd;
+    const int ngrp = (NG == 1) ? (u.ngrp > 0 ? 1 : 0) : u.ngrp;
+    float2 w[NG == 1 ? 1 : 16];
+    if (NG > 1 && ngrp > 1) {
+        const float2 *__restrict__ U1 = a.buf[1];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) w[i] = valid ? U1[q * L + r + G::T * i] : zero;
+        line_fwd<L>(reinterpret_cast<float2(&)[16]>(w), r, ro, z, s_tw);
+    }
+    const f256::UpdRegs R = f256::load_upd(u, ngrp);
+    float fl = 0.f;
+    if (valid) {
+        const int zz = (int)(q / g.KX), kx = (int)(q - (long long)zz * g.KX);
+        const float fx = (float)kx / (float)g.X;
+        fl = fx * fx + f256::fsqf(zz, g.Z);
+    }
+    float2 *__restrict__ state = a.state;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        const int k = ro.elem(j);
+        float2 cn = zero;
+        if (valid) {
+            const float mk = -39.478417604357434f * (fl + s_fy[k]);
+            const long long gi = q * L + k;
+            cn = f256::euler_update<NG>(R, state[gi], v[j], (NG > 1) ? w[NG > 1 ? j : 0] : v[j], mk);
+            state[gi] = cn;
+        }
+        v[j] = make_float2(cn.x * R.invN, cn.y * R.invN);
+    }
+    line_inv<L>(v, r, ro, z, s_tw);
+    float2 *__restrict__ T = a.tout;
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+        if (valid) T[q * L + r + G::T * i] = v[i];
+}
+
+// one shared array holds, in turn, the spectral tile [L/2 + 1][2 LPB], the exchange slots of the
+// LPB lines and the separation slots [LPB][L + 1]; then twiddles and polynomial coefficients
+template <int L> __host__ __device__ constexpr int xline_area()
+{
+    constexpr int a = (L / 2 + 1) * 2 * Geo<L>::LPB, b = Geo<L>::LPB * Geo<L>::LREG, c = Geo<L>::LPB * (L + 1);
+    return (a > b ? (a > c ? a : c) : (b > c ? b : c));
+}
+template <int L> constexpr int xline_smem_bytes() { return (xline_area<L>() + L) * 8 + GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1) * 4; }
+
+// One x tile: 2 LPB rows from y0 of depth plane zp; c2r -> polynomial groups -> r2c into
+// a.out[grp] (L = g.X columns).
+template <int L> __device__ __forceinline__ void xline_tile(const XPassArgs<float> &a, int ty, int zp)
+{
+    typedef Geo<L> G;
+    constexpr int H = L / 2, KX = H + 1, RB = 2 * G::LPB;
+    extern __shared__ __align__(16) unsigned char fl_dsm[];
+    float2 *s_a = reinterpret_cast<float2 *>(fl_dsm); // input tile, then exchange slots
+    float2 *s_sep = s_a;                               // [LPB][L + 1], once the exchange is done
+    float2 *s_tw = s_a + xline_area<L>();
+    float *s_poly = reinterpret_cast<float *>(s_tw + L);
+    const Geom &g = a.g;
+    const int l = threadIdx.x / G::T, r = threadIdx.x - l * G::T;
+    const int y0 = ty * RB;
+    const long long sbase = (long long)zp * g.S + y0;
+    const int Y = g.Y;
+    for (int t = threadIdx.x; t < L; t += G::NT) s_tw[t] = a.twX[t];
+    for (int t = threadIdx.x; t < GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1); t += G::NT)
+        s_poly[t] = (float)a.pw.dense[t / (GOPF_MAX_DEG + 1)][t % (GOPF_MAX_DEG + 1)];
+    const float2 *__restrict__ in = a.in;
+    for (int e = threadIdx.x; e < KX * RB; e += G::NT) {
+        const int kx = e / RB, y = e - kx * RB;
+        s_a[e] = (y0 + y < Y) ? in[sbase + (long long)kx * Y + y] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const Role<L> ro(r);
+    // Hermitian extension of rows (2l, 2l + 1) packed as a + i b, in the B layout
+    float2 v[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        const int k = ro.elem(j);
+        if (k <= H) {
+            const float2 A = s_a[k * RB + 2 * l], B = s_a[k * RB + 2 * l + 1];
+            v[j] = make_float2(A.x - B.y, A.y + B.x);
+        } else {
+            const float2 A = s_a[(L - k) * RB + 2 * l], B = s_a[(L - k) * RB + 2 * l + 1];
+            v[j] = make_float2(A.x + B.y, -A.y + B.x);
+        }
+    }
+    __syncthreads(); // the tile becomes the exchange slots
+    float2 *z = s_a + l * G::LREG;
+    line_inv<L>(v, r, ro, z, s_tw);
+    // v[i] = c(row 2l, col r + T i) + i c(row 2l + 1, col r + T i)
+    const int ng = a.ngrp_out;
+    for (int grp = 0; grp < ng; ++grp) {
+        float2 w[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) w[i] = v[i];
+        if (!a.identity) f256::apply_poly(w, a, grp, s_poly + grp * (GOPF_MAX_DEG + 1));
+        line_fwd<L>(w, r, ro, z, s_tw);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) s_sep[l * (L + 1) + ro.elem(j)] = w[j];
+        __syncthreads();
+        float2 *__restrict__ out = a.out[grp];
+        for (int e = threadIdx.x; e < KX * G::LPB; e += G::NT) {
+            const int kx = e / G::LPB, p = e - kx * G::LPB;
+            const float2 P = s_sep[p * (L + 1) + kx];
+            const float2 Q = s_sep[p * (L + 1) + (kx ? L - kx : 0)];
+            if (y0 + 2 * p < Y)
+                *reinterpret_cast<float4 *>(&out[sbase + (long long)kx * Y + 2 * p]) =
+                    make_float4(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y), 0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
+        }
+        __syncthreads();
+    }
+}
+
+} // namespace fl
+} // namespace gopf

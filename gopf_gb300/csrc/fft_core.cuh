@@ -234,4 +234,83 @@ __device__ __forceinline__ void fft_tile(V *buf, int pitch, const LinePlan &pl, 
     }
 }
 
+// ------------------------------------------------------------------
+// Compile-time plans: the same stages as a runtime LinePlan of length N (radix 3s first, then
+// 2^(a mod 4), then 16s; the twiddle stride of a table of N * TWS entries), but with every
+// index known to the compiler and each stage inlined.  Results are bitwise those of fft_tile.
+// ------------------------------------------------------------------
+
+template <int N> struct CtPlan {
+    __host__ __device__ static constexpr int pow2(int n) { return (n % 2 == 0) ? 1 + pow2(n / 2) : 0; }
+    __host__ __device__ static constexpr int odd(int n) { return (n % 2 == 0) ? odd(n / 2) : n; }
+    __host__ __device__ static constexpr int pow3(int n) { return (n % 3 == 0) ? 1 + pow3(n / 3) : 0; }
+    static constexpr int a = pow2(N), b = pow3(odd(N));
+    static constexpr int nst = b + ((a % 4) ? 1 : 0) + a / 4;
+    __host__ __device__ static constexpr int rad(int s) { return (s < b) ? 3 : ((a % 4) && s == b) ? (1 << (a % 4)) : 16; }
+    __host__ __device__ static constexpr int ns(int s) { return (s == 0) ? 1 : ns(s - 1) * rad(s - 1); }
+};
+
+template <int RAD, bool INV, int LB, int PERB, int N, int NS, int TWM, typename V>
+__device__ __forceinline__ void fft_stage_ct(V *buf, int pitch, const V *__restrict__ tw)
+{
+    constexpr int MAXPER = (PERB + RAD - 1) / RAD;
+    constexpr int LBSH = (LB == 1) ? 0 : (LB == 2) ? 1 : (LB == 4) ? 2 : (LB == 8) ? 3 : (LB == 16) ? 4 : 5;
+    constexpr int m = N / RAD;
+    constexpr int total = m * LB;
+    constexpr bool p2 = (NS & (NS - 1)) == 0;
+    const int nt = blockDim.x;
+    V v[MAXPER][RAD];
+#pragma unroll
+    for (int p = 0; p < MAXPER; ++p) {
+        const int bf = threadIdx.x + p * nt;
+        if (bf < total) {
+            const int line = bf & (LB - 1);
+            const int j = bf >> LBSH;
+#pragma unroll
+            for (int r = 0; r < RAD; ++r) v[p][r] = buf[(j + r * m) * pitch + line];
+            const int k = p2 ? (j & (NS - 1)) : (j % NS);
+            if (k != 0) {
+#pragma unroll
+                for (int r = 1; r < RAD; ++r) {
+                    V w = __ldg(&tw[r * k * TWM]);
+                    v[p][r] = INV ? cmulc(v[p][r], w) : cmul(v[p][r], w);
+                }
+            }
+            dft<RAD, INV>(v[p]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int p = 0; p < MAXPER; ++p) {
+        const int bf = threadIdx.x + p * nt;
+        if (bf < total) {
+            const int line = bf & (LB - 1);
+            const int j = bf >> LBSH;
+            const int k = p2 ? (j & (NS - 1)) : (j % NS);
+            const int base = (j - k) * RAD + k;
+#pragma unroll
+            for (int r = 0; r < RAD; ++r) buf[(base + r * NS) * pitch + line] = v[p][r];
+        }
+    }
+    __syncthreads();
+}
+
+template <bool INV, int LB, int PERB, int N, int TWS, int S = 0, typename V>
+__device__ __forceinline__ void fft_tile_ct(V *buf, int pitch, const V *__restrict__ tw)
+{
+    if constexpr (S < CtPlan<N>::nst) {
+        constexpr int R = CtPlan<N>::rad(S), NS = CtPlan<N>::ns(S);
+        fft_stage_ct<R, INV, LB, PERB, N, NS, N * TWS / (NS * R)>(buf, pitch, tw);
+        fft_tile_ct<INV, LB, PERB, N, TWS, S + 1>(buf, pitch, tw);
+    }
+}
+
+// a tile transform with a compile-time plan when NCT > 0, else the runtime plan
+template <bool INV, int LB, int PERB, int NCT, int TWS, typename V>
+__device__ __forceinline__ void fft_tile_any(V *buf, int pitch, const LinePlan &pl, const V *__restrict__ tw)
+{
+    if constexpr (NCT > 0) fft_tile_ct<INV, LB, PERB, NCT, TWS>(buf, pitch, tw);
+    else fft_tile<INV, LB, PERB>(buf, pitch, pl, tw);
+}
+
 } // namespace gopf

@@ -13,6 +13,7 @@
 #include <string>
 #include <vector>
 
+#include "fastline.cuh"
 #include "gopf_ctx.h"
 #include "gopf_kernels_impl.cuh"
 
@@ -30,18 +31,32 @@ template <typename R, int LB> __device__ __forceinline__ void batch_x_item(const
     xpass_tile<R, LB, 16>(a, ty, 0);
 }
 
+// Copy an instance's pass arguments into shared memory (as 8-byte words) for the item: the tile
+// code then reads them there instead of the compiler staging the whole struct in local memory.
+template <typename T> __device__ __forceinline__ void stage_args(T *dst, const T *src)
+{
+    static_assert(sizeof(T) % 8 == 0, "pass arguments are 8-byte aligned");
+    const unsigned long long *s = reinterpret_cast<const unsigned long long *>(src);
+    unsigned long long *d = reinterpret_cast<unsigned long long *>(dst);
+    for (int k = threadIdx.x; k < (int)(sizeof(T) / 8); k += blockDim.x) d[k] = s[k];
+}
+
 template <typename R>
 __global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2))
     k_batch_xpass(const BatchInst<R> *__restrict__ inst, const int2 *__restrict__ items, int nitems)
 {
+    __shared__ __align__(16) XPassArgs<R> s_a;
+    __shared__ int s_lb;
     for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
         __syncthreads(); // shared memory of the previous item is free
         const int2 it = items[w];
-        const BatchInst<R> &b = inst[it.x];
-        if (b.xa.ngrp_out == 0) continue;
-        if (b.lbx == 16) batch_x_item<R, 16>(b.xa, it.y);
-        else if (b.lbx == 8) batch_x_item<R, 8>(b.xa, it.y);
-        else batch_x_item<R, 4>(b.xa, it.y);
+        stage_args(&s_a, &inst[it.x].xa);
+        if (threadIdx.x == 0) s_lb = inst[it.x].lbx;
+        __syncthreads();
+        if (s_a.ngrp_out == 0) continue;
+        if (s_lb == 16) batch_x_item<R, 16>(s_a, it.y);
+        else if (s_lb == 8) batch_x_item<R, 8>(s_a, it.y);
+        else batch_x_item<R, 4>(s_a, it.y);
     }
 }
 
@@ -49,14 +64,124 @@ template <typename R>
 __global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2))
     k_batch_ypass(const BatchInst<R> *__restrict__ inst, const int2 *__restrict__ items, int nitems)
 {
+    __shared__ __align__(16) PassArgs<R> s_a;
+    __shared__ int s_lb;
     for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
         __syncthreads();
         const int2 it = items[w];
-        const BatchInst<R> &b = inst[it.x];
-        if (b.lby == 16) pass_tile<R, 16, 16, true, false>(b.pa, it.y, 0);
-        else if (b.lby == 8) pass_tile<R, 8, 16, true, false>(b.pa, it.y, 0);
-        else pass_tile<R, 4, 16, true, false>(b.pa, it.y, 0);
+        stage_args(&s_a, &inst[it.x].pa);
+        if (threadIdx.x == 0) s_lb = inst[it.x].lby;
+        __syncthreads();
+        if (s_lb == 16) pass_tile<R, 16, 16, true, false>(s_a, it.y, 0);
+        else if (s_lb == 8) pass_tile<R, 8, 16, true, false>(s_a, it.y, 0);
+        else pass_tile<R, 4, 16, true, false>(s_a, it.y, 0);
     }
+}
+
+// Size classes of the sweep's sides (128 ... 1024) in FP32: one kernel per (length, tile width)
+// with a compile-time plan, every stage inlined with its radix, stride and twiddle step known.
+// One block per item (a persistent loop around the inlined stages makes the compiler spill
+// kilobytes per thread); each class is its own launch with its own register allocation, and the
+// classes of a pass run as parallel branches of the step's graph.  The (length, tile width)
+// pairs are those lb_for gives the contexts; any other instance goes through k_batch_xpass /
+// k_batch_ypass.
+template <int LB, int H>
+__global__ void __launch_bounds__(256, 3) k_batch_x_ct(const BatchInst<float> *__restrict__ inst,
+                                                      const int2 *__restrict__ items, int nitems)
+{
+    const int2 it = items[blockIdx.x];
+    const XPassArgs<float> &a = inst[it.x].xa;
+    if (a.ngrp_out == 0) return;
+    xpass_tile<float, LB, 16, false, H>(a, it.y, 0);
+}
+
+template <int LB, int N>
+__global__ void __launch_bounds__(256, 3) k_batch_y_ct(const BatchInst<float> *__restrict__ inst,
+                                                      const int2 *__restrict__ items, int nitems)
+{
+    const int2 it = items[blockIdx.x];
+    pass_tile<float, LB, 16, true, false, N>(inst[it.x].pa, it.y, 0);
+}
+
+// Sides 256 ... 1024 in FP32 go further, to the register-resident line engine (fastline.cuh):
+// one block per tile of rows (x) or lines (y).
+template <int L>
+__global__ void __launch_bounds__(fl::Geo<L>::NT, 3) k_batch_xl(const BatchInst<float> *__restrict__ inst,
+                                                               const int2 *__restrict__ items, int nitems)
+{
+    const int2 it = items[blockIdx.x];
+    const XPassArgs<float> &a = inst[it.x].xa;
+    if (a.ngrp_out == 0) return;
+    fl::xline_tile<L>(a, it.y, 0);
+}
+
+template <int L, int NG>
+__global__ void __launch_bounds__(fl::Geo<L>::NT, 3) k_batch_yl(const BatchInst<float> *__restrict__ inst,
+                                                               const int2 *__restrict__ items, int nitems)
+{
+    const int2 it = items[blockIdx.x];
+    fl::yline_tile<L, NG>(inst[it.x].pa, it.y);
+}
+
+// Classes: 0 any size (runtime plan); 1 .. 6 compile-time plans (x by H, y by the line length);
+// 11 .. 15 the line engine for sides FL_L (y: 11 .. 15 one group, 21 .. 25 two groups).
+constexpr int NCLASS = 26;
+constexpr int XCLS_H[7] = {0, 64, 128, 192, 256, 384, 512}, XCLS_LB[7] = {0, 16, 16, 16, 16, 8, 8};
+constexpr int YCLS_N[7] = {0, 128, 256, 384, 512, 768, 1024}, YCLS_LB[7] = {0, 16, 16, 8, 8, 4, 4};
+constexpr int FL_L[5] = {256, 384, 512, 768, 1024};
+constexpr int FL_LPB[5] = {fl::Geo<256>::LPB, fl::Geo<384>::LPB, fl::Geo<512>::LPB, fl::Geo<768>::LPB,
+                           fl::Geo<1024>::LPB};
+constexpr int FL_NT[5] = {fl::Geo<256>::NT, fl::Geo<384>::NT, fl::Geo<512>::NT, fl::Geo<768>::NT, fl::Geo<1024>::NT};
+constexpr int FL_XSMEM[5] = {fl::xline_smem_bytes<256>(), fl::xline_smem_bytes<384>(), fl::xline_smem_bytes<512>(),
+                             fl::xline_smem_bytes<768>(), fl::xline_smem_bytes<1024>()};
+constexpr int FL_YSMEM[5] = {fl::yline_smem_bytes<256>(), fl::yline_smem_bytes<384>(), fl::yline_smem_bytes<512>(),
+                             fl::yline_smem_bytes<768>(), fl::yline_smem_bytes<1024>()};
+
+template <typename R> static const void *x_kernel(int cls)
+{
+    if constexpr (sizeof(R) == 4) {
+        switch (cls) {
+        case 1: return (const void *)k_batch_x_ct<16, 64>;
+        case 2: return (const void *)k_batch_x_ct<16, 128>;
+        case 3: return (const void *)k_batch_x_ct<16, 192>;
+        case 4: return (const void *)k_batch_x_ct<16, 256>;
+        case 5: return (const void *)k_batch_x_ct<8, 384>;
+        case 6: return (const void *)k_batch_x_ct<8, 512>;
+        case 11: return (const void *)k_batch_xl<256>;
+        case 12: return (const void *)k_batch_xl<384>;
+        case 13: return (const void *)k_batch_xl<512>;
+        case 14: return (const void *)k_batch_xl<768>;
+        case 15: return (const void *)k_batch_xl<1024>;
+        default: break;
+        }
+    }
+    return (const void *)k_batch_xpass<R>;
+}
+
+template <typename R> static const void *y_kernel(int cls)
+{
+    if constexpr (sizeof(R) == 4) {
+        switch (cls) {
+        case 1: return (const void *)k_batch_y_ct<16, 128>;
+        case 2: return (const void *)k_batch_y_ct<16, 256>;
+        case 3: return (const void *)k_batch_y_ct<8, 384>;
+        case 4: return (const void *)k_batch_y_ct<8, 512>;
+        case 5: return (const void *)k_batch_y_ct<4, 768>;
+        case 6: return (const void *)k_batch_y_ct<4, 1024>;
+        case 11: return (const void *)k_batch_yl<256, 1>;
+        case 12: return (const void *)k_batch_yl<384, 1>;
+        case 13: return (const void *)k_batch_yl<512, 1>;
+        case 14: return (const void *)k_batch_yl<768, 1>;
+        case 15: return (const void *)k_batch_yl<1024, 1>;
+        case 21: return (const void *)k_batch_yl<256, 2>;
+        case 22: return (const void *)k_batch_yl<384, 2>;
+        case 23: return (const void *)k_batch_yl<512, 2>;
+        case 24: return (const void *)k_batch_yl<768, 2>;
+        case 25: return (const void *)k_batch_yl<1024, 2>;
+        default: break;
+        }
+    }
+    return (const void *)k_batch_ypass<R>;
 }
 
 // Hermitian projection of the kx = 0 and kx = X/2 lines of every instance (2D)
@@ -96,17 +221,24 @@ __global__ void k_batch_herm(const BatchInst<R> *__restrict__ inst, int ninst, l
 
 using namespace gopf;
 
+// one launch of a pass: the items of one size class
+struct BatchLaunch {
+    const void *fn = nullptr;
+    int2 *d_items = nullptr;
+    int nitems = 0;
+    int grid = 0, smem = 0, threads = 256;
+};
+
 struct gopf_batch {
     std::vector<gopf_ctx *> ctx;
     int device = 0;
     int prec = GOPF_FP32;
     cudaStream_t own_stream = nullptr, stream = nullptr;
     void *d_inst = nullptr;
-    int2 *d_xitems = nullptr, *d_yitems = nullptr;
-    int nx = 0, ny = 0;
+    std::vector<BatchLaunch> xl, yl; // the x and y passes, one launch per size class present
+    std::vector<cudaStream_t> side;  // branch streams of a pass's launches
+    std::vector<cudaEvent_t> ev;     // [0] fork, [1 ..] joins
     long long herm_total = 0;
-    int smem_x = 0, smem_y = 0;
-    int grid_x = 0, grid_y = 0;
     cudaGraphExec_t g1 = nullptr, gK = nullptr;
     int K = 16;
     std::string err;
@@ -128,8 +260,9 @@ template <typename R> static int batch_build(gopf_batch *b)
 {
     typedef typename VecOf<R>::type V;
     std::vector<BatchInst<R>> inst(b->ctx.size());
-    std::vector<int2> xi, yi;
-    std::vector<std::pair<int, int2>> xs, ys; // (cost, item)
+    std::vector<std::pair<int, int2>> xs[NCLASS], ys[NCLASS]; // (cost, item) per size class
+    int smem_x[NCLASS] = {0}, smem_y[NCLASS] = {0}, thr_x[NCLASS], thr_y[NCLASS];
+    for (int k = 0; k < NCLASS; ++k) thr_x[k] = thr_y[k] = 256;
     long long hoff = 0;
     const int vb = sizeof(V);
     for (size_t i = 0; i < b->ctx.size(); ++i) {
@@ -165,46 +298,127 @@ template <typename R> static int batch_build(gopf_batch *b)
         bi.lby = c->LBy;
         bi.herm_off = hoff;
         hoff += 2LL * g.Y;
-        const int ntx = (g.Y + c->LBx - 1) / c->LBx;
-        for (int t = 0; t < ntx; ++t) xs.push_back({g.H * c->LBx, make_int2((int)i, t)});
-        const int nty = (int)((g.KX + c->LBy - 1) / c->LBy);
-        for (int t = 0; t < nty; ++t) ys.push_back({g.Y * c->LBy, make_int2((int)i, t)});
-        b->smem_x = std::max(b->smem_x, xpass_smem_bytes(g, c->LBx, vb));
-        b->smem_y = std::max(b->smem_y, cpass_smem_bytes(g, g.Y, c->LBy, nb, vb) + (c->LBy + g.Y) * (int)sizeof(R));
+        int xc = 0, yc = 0, fx = -1, fy = -1;
+        if (sizeof(R) == 4) {
+            for (int k = 1; k < 7; ++k) {
+                if (g.H == XCLS_H[k] && c->LBx == XCLS_LB[k]) xc = k;
+                if (g.Y == YCLS_N[k] && c->LBy == YCLS_LB[k]) yc = k;
+            }
+            for (int k = 0; k < 5; ++k) {
+                if (g.X == FL_L[k] && g.Y % (2 * FL_LPB[k]) == 0) fx = k;
+                if (g.Y == FL_L[k] && nb <= 2 && c->upd.nimp <= 4) fy = k;
+            }
+        }
+        if (fx >= 0) { // line engine: tiles of 2 LPB rows
+            xc = 11 + fx;
+            const int ntx = g.Y / (2 * FL_LPB[fx]);
+            for (int t = 0; t < ntx; ++t) xs[xc].push_back({g.X * 2 * FL_LPB[fx], make_int2((int)i, t)});
+            smem_x[xc] = FL_XSMEM[fx];
+            thr_x[xc] = FL_NT[fx];
+        } else {
+            const int ntx = (g.Y + c->LBx - 1) / c->LBx;
+            for (int t = 0; t < ntx; ++t) xs[xc].push_back({g.H * c->LBx, make_int2((int)i, t)});
+            smem_x[xc] = std::max(smem_x[xc], xpass_smem_bytes(g, c->LBx, vb));
+        }
+        if (fy >= 0) { // line engine: tiles of LPB lines
+            yc = (nb > 1 ? 21 : 11) + fy;
+            const int nty = (int)((g.KX + FL_LPB[fy] - 1) / FL_LPB[fy]);
+            for (int t = 0; t < nty; ++t) ys[yc].push_back({g.Y * FL_LPB[fy], make_int2((int)i, t)});
+            smem_y[yc] = FL_YSMEM[fy];
+            thr_y[yc] = FL_NT[fy];
+        } else {
+            const int nty = (int)((g.KX + c->LBy - 1) / c->LBy);
+            for (int t = 0; t < nty; ++t) ys[yc].push_back({g.Y * c->LBy, make_int2((int)i, t)});
+            smem_y[yc] = std::max(smem_y[yc], cpass_smem_bytes(g, g.Y, c->LBy, nb, vb) + (c->LBy + g.Y) * (int)sizeof(R));
+        }
     }
-    auto bycost = [](const std::pair<int, int2> &a, const std::pair<int, int2> &c) { return a.first > c.first; };
-    std::stable_sort(xs.begin(), xs.end(), bycost);
-    std::stable_sort(ys.begin(), ys.end(), bycost);
-    for (auto &p : xs) xi.push_back(p.second);
-    for (auto &p : ys) yi.push_back(p.second);
-    b->nx = (int)xi.size();
-    b->ny = (int)yi.size();
     b->herm_total = hoff;
     BCK(gopf_malloc(&b->d_inst, sizeof(BatchInst<R>) * inst.size()));
     BCK(cudaMemcpy(b->d_inst, inst.data(), sizeof(BatchInst<R>) * inst.size(), cudaMemcpyHostToDevice));
-    BCK(gopf_malloc(&b->d_xitems, sizeof(int2) * std::max(1, b->nx)));
-    BCK(gopf_malloc(&b->d_yitems, sizeof(int2) * std::max(1, b->ny)));
-    BCK(cudaMemcpy(b->d_xitems, xi.data(), sizeof(int2) * b->nx, cudaMemcpyHostToDevice));
-    BCK(cudaMemcpy(b->d_yitems, yi.data(), sizeof(int2) * b->ny, cudaMemcpyHostToDevice));
-    BCK(cudaFuncSetAttribute(k_batch_xpass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, b->smem_x));
-    BCK(cudaFuncSetAttribute(k_batch_ypass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, b->smem_y));
-    int nsm = 0, bx = 0, by = 0;
+    int nsm = 0;
     BCK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, b->device));
-    BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bx, k_batch_xpass<R>, 256, b->smem_x));
-    BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&by, k_batch_ypass<R>, 256, b->smem_y));
-    b->grid_x = std::max(1, std::min(b->nx, nsm * std::max(bx, 1)));
-    b->grid_y = std::max(1, std::min(b->ny, nsm * std::max(by, 1)));
+    auto bycost = [](const std::pair<int, int2> &a, const std::pair<int, int2> &c) { return a.first > c.first; };
+    // one launch per class present, largest classes first (they start first in the graph)
+    auto make = [&](std::vector<std::pair<int, int2>> *lists, const int *smem, const int *thr, bool xpass,
+                    std::vector<BatchLaunch> &out) -> int {
+        std::vector<std::pair<long long, int>> order;
+        for (int k = 0; k < NCLASS; ++k)
+            if (!lists[k].empty()) {
+                long long cost = 0;
+                for (auto &p : lists[k]) cost += p.first;
+                order.push_back({cost, k});
+            }
+        std::sort(order.begin(), order.end(), [](auto &a, auto &c) { return a.first > c.first; });
+        for (auto &o : order) {
+            const int k = o.second;
+            std::stable_sort(lists[k].begin(), lists[k].end(), bycost);
+            std::vector<int2> items;
+            for (auto &p : lists[k]) items.push_back(p.second);
+            BatchLaunch L;
+            L.fn = xpass ? x_kernel<R>(k) : y_kernel<R>(k);
+            L.nitems = (int)items.size();
+            L.smem = smem[k];
+            L.threads = thr[k];
+            BCK(gopf_malloc(&L.d_items, sizeof(int2) * items.size()));
+            out.push_back(L); // owned by the batch from here on (freed with it)
+            BCK(cudaMemcpy(L.d_items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice));
+            BCK(cudaFuncSetAttribute(L.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, L.smem));
+            int occ = 0;
+            BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, L.fn, L.threads, L.smem));
+            // the compile-time classes take one block per item; the generic kernels loop
+            out.back().grid = (k > 0) ? L.nitems : std::max(1, std::min(L.nitems, nsm * std::max(occ, 1)));
+        }
+        return GOPF_OK;
+    };
+    int rc;
+    if ((rc = make(xs, smem_x, thr_x, true, b->xl))) return rc;
+    if ((rc = make(ys, smem_y, thr_y, false, b->yl))) return rc;
+    const size_t nbranch = std::max(b->xl.size(), b->yl.size());
+    while (b->side.size() + 1 < nbranch) {
+        cudaStream_t st;
+        BCK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        b->side.push_back(st);
+    }
+    while (b->ev.size() < nbranch + 1) {
+        cudaEvent_t e;
+        BCK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        b->ev.push_back(e);
+    }
     return GOPF_OK;
+}
+
+// The launches of one pass as parallel branches: the first on the batch's stream, the others on
+// side streams forked from it and joined back.
+template <typename R> static cudaError_t batch_pass(gopf_batch *b, const std::vector<BatchLaunch> &ls)
+{
+    const BatchInst<R> *inst = (const BatchInst<R> *)b->d_inst;
+    cudaError_t e;
+    if (ls.size() > 1) {
+        if ((e = cudaEventRecord(b->ev[0], b->stream)) != cudaSuccess) return e;
+        for (size_t i = 1; i < ls.size(); ++i)
+            if ((e = cudaStreamWaitEvent(b->side[i - 1], b->ev[0], 0)) != cudaSuccess) return e;
+    }
+    for (size_t i = 0; i < ls.size(); ++i) {
+        const BatchLaunch &L = ls[i];
+        cudaStream_t st = (i == 0) ? b->stream : b->side[i - 1];
+        const int2 *items = L.d_items;
+        int n = L.nitems;
+        void *args[] = {(void *)&inst, (void *)&items, (void *)&n};
+        if ((e = cudaLaunchKernel(L.fn, dim3(L.grid), dim3(L.threads), args, (size_t)L.smem, st)) != cudaSuccess)
+            return e;
+        if (i > 0 && (e = cudaEventRecord(b->ev[i], st)) != cudaSuccess) return e;
+    }
+    for (size_t i = 1; i < ls.size(); ++i)
+        if ((e = cudaStreamWaitEvent(b->stream, b->ev[i], 0)) != cudaSuccess) return e;
+    return cudaSuccess;
 }
 
 template <typename R> static cudaError_t batch_enqueue(gopf_batch *b)
 {
     const BatchInst<R> *inst = (const BatchInst<R> *)b->d_inst;
-    k_batch_xpass<R><<<b->grid_x, 256, b->smem_x, b->stream>>>(inst, b->d_xitems, b->nx);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_batch_ypass<R><<<b->grid_y, 256, b->smem_y, b->stream>>>(inst, b->d_yitems, b->ny);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    cudaError_t e;
+    if ((e = batch_pass<R>(b, b->xl)) != cudaSuccess) return e;
+    if ((e = batch_pass<R>(b, b->yl)) != cudaSuccess) return e;
     const unsigned hb = (unsigned)std::min<long long>((b->herm_total + 255) / 256, 152 * 4);
     k_batch_herm<R><<<hb, 256, 0, b->stream>>>(inst, (int)b->ctx.size(), b->herm_total);
     return cudaGetLastError();
@@ -274,9 +488,12 @@ extern "C" int gopf_batch_destroy(gopf_batch *b)
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->g1) cudaGraphExecDestroy(b->g1);
     if (b->gK) cudaGraphExecDestroy(b->gK);
-    void *ptrs[] = {b->d_inst, b->d_xitems, b->d_yitems};
-    for (void *p : ptrs)
-        if (p) cudaFree(p);
+    if (b->d_inst) cudaFree(b->d_inst);
+    for (auto *ls : {&b->xl, &b->yl})
+        for (BatchLaunch &L : *ls)
+            if (L.d_items) cudaFree(L.d_items);
+    for (cudaStream_t st : b->side) cudaStreamDestroy(st);
+    for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
     if (b->own_stream) cudaStreamDestroy(b->own_stream);
     delete b;
     return GOPF_OK;
@@ -316,6 +533,6 @@ extern "C" int gopf_batch_step(gopf_batch *b, long long nsteps)
 extern "C" int gopf_batch_kernels_per_step(gopf_batch *b, int *n)
 {
     if (!b || !n) return GOPF_ERR_ARG;
-    *n = 3;
+    *n = (int)(b->xl.size() + b->yl.size()) + 1;
     return GOPF_OK;
 }

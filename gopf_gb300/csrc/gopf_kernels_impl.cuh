@@ -73,14 +73,14 @@ __device__ __forceinline__ void block_reduce_store(double *vals, double *red, do
 // Load the spectral tile (z, all kx, LB rows from y0) of `in`, undo the r2c
 // packing and inverse transform along x: on return A[m*LB + l] = (c[2m],
 // c[2m+1]) of row y0 + l (times the transform's normalisation).
-template <typename R, int LB, int PERB>
+template <typename R, int LB, int PERB, int NCT = 0>
 __device__ __forceinline__ void xload_c2r(typename VecOf<R>::type *A, const typename VecOf<R>::type *__restrict__ in,
                                           long long sbase, int nl, const Geom &g, const LinePlan &planH,
                                           const typename VecOf<R>::type *__restrict__ twX)
 {
     typedef typename VecOf<R>::type V;
     constexpr int LBSH = Log2<LB>::v;
-    const int H = g.H, KX = g.KX, Y = g.Y;
+    const int H = NCT ? NCT : g.H, KX = H + 1, Y = g.Y;
     const int tid = threadIdx.x, nt = blockDim.x;
     const V zero = cmk<V>((R)0, (R)0);
     for (int e = tid; e < KX * LB; e += nt) {
@@ -110,21 +110,21 @@ __device__ __forceinline__ void xload_c2r(typename VecOf<R>::type *A, const type
         }
     }
     __syncthreads();
-    fft_tile<true, LB, PERB>(A, LB, planH, twX);
+    fft_tile_any<true, LB, PERB, NCT, 2>(A, LB, planH, twX);
 }
 
 // r2c along x of the packed real rows in B (B[m*LB+l] = (g[2m], g[2m+1])) and
 // store the half spectrum of the tile into out.
-template <typename R, int LB, int PERB>
+template <typename R, int LB, int PERB, int NCT = 0>
 __device__ __forceinline__ void xr2c_store(typename VecOf<R>::type *B, typename VecOf<R>::type *__restrict__ out,
                                            long long sbase, int nl, const Geom &g, const LinePlan &planH,
                                            const typename VecOf<R>::type *__restrict__ twX)
 {
     typedef typename VecOf<R>::type V;
     constexpr int LBSH = Log2<LB>::v;
-    const int H = g.H, KX = g.KX, Y = g.Y;
+    const int H = NCT ? NCT : g.H, KX = H + 1, Y = g.Y;
     const int tid = threadIdx.x, nt = blockDim.x;
-    fft_tile<false, LB, PERB>(B, LB, planH, twX);
+    fft_tile_any<false, LB, PERB, NCT, 2>(B, LB, planH, twX);
     const int npair = H / 2 + 1;
     const R half = (R)0.5;
     for (int e = tid; e < npair * LB; e += nt) {
@@ -168,15 +168,17 @@ template <typename R> __device__ __forceinline__ R elastic_q(R c, R w, R e0, R s
 // x-pass: c2r (or real load) -> pointwise -> r2c
 // ------------------------------------------------------------------
 
-// One x-pass tile: LB rows starting at row ty*LB of depth plane z.
-template <typename R, int LB, int PERB>
+// One x-pass tile: LB rows starting at row ty*LB of depth plane z.  MULTI: the multi-field
+// program only (a separate instantiation, so the single-field kernels do not carry its registers).
+// NCT > 0: the x transform has the compile-time length NCT (== g.H).
+template <typename R, int LB, int PERB, bool MULTI = false, int NCT = 0>
 __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
 {
     typedef typename VecOf<R>::type V;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int LBSH = Log2<LB>::v;
     const Geom &g = a.g;
-    const int H = g.H, KX = g.KX, Y = g.Y;
+    const int H = NCT ? NCT : g.H, KX = H + 1, Y = g.Y;
     V *A = reinterpret_cast<V *>(smem_raw);
     V *B = A + KX * LB;
     const int y0 = ty * LB;
@@ -186,12 +188,12 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
     const V zero = cmk<V>((R)0, (R)0);
     const V *__restrict__ twX = a.twX;
 
-    if (a.program == XP_MULTI) {
+    if constexpr (MULTI) {
         // one tile per field, then each group's monomials into the tile after them
         const MonoTable &mt = a.mono;
         const int tsz = KX * LB;
         V *Bm = A + mt.nin * tsz;
-        for (int f = 0; f < mt.nin; ++f) xload_c2r<R, LB, PERB>(A + f * tsz, a.inF[f], sbase, nl, g, a.planH, twX);
+        for (int f = 0; f < mt.nin; ++f) xload_c2r<R, LB, PERB, NCT>(A + f * tsz, a.inF[f], sbase, nl, g, a.planH, twX);
         for (int grp = 0; grp < mt.ngrp; ++grp) {
             for (int e = tid; e < H * LB; e += nt) {
                 R vx = (R)0, vy = (R)0;
@@ -210,13 +212,13 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
                 Bm[e] = cmk<V>(vx, vy);
             }
             __syncthreads();
-            xr2c_store<R, LB, PERB>(Bm, a.out[grp], sbase, nl, g, a.planH, twX);
+            xr2c_store<R, LB, PERB, NCT>(Bm, a.out[grp], sbase, nl, g, a.planH, twX);
         }
         return;
     }
 
     if (a.in_mode == XIN_SPECTRAL) {
-        xload_c2r<R, LB, PERB>(A, a.in, sbase, nl, g, a.planH, twX);
+        xload_c2r<R, LB, PERB, NCT>(A, a.in, sbase, nl, g, a.planH, twX);
     } else {
         const V *rin2 = reinterpret_cast<const V *>(a.rin) + ((long long)z * Y + y0) * H;
         for (int e = tid; e < LB * H; e += nt) {
@@ -258,14 +260,14 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
 
     if (a.program == XP_ELASTIC_Q) {
         // w = c2r(in2) into B, then q into B, then r2c into out[0]
-        xload_c2r<R, LB, PERB>(B, a.in2, sbase, nl, g, a.planH, twX);
+        xload_c2r<R, LB, PERB, NCT>(B, a.in2, sbase, nl, g, a.planH, twX);
         const R e0 = (R)a.e0, es = (R)a.escale;
         for (int e = tid; e < H * LB; e += nt) {
             const V c = A[e], w = B[e];
             B[e] = cmk<V>(elastic_q<R>(c.x, w.x, e0, es), elastic_q<R>(c.y, w.y, e0, es));
         }
         __syncthreads();
-        xr2c_store<R, LB, PERB>(B, a.out[0], sbase, nl, g, a.planH, twX);
+        xr2c_store<R, LB, PERB, NCT>(B, a.out[0], sbase, nl, g, a.planH, twX);
         return;
     }
 
@@ -288,7 +290,7 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
             block_reduce_store(vals, a.red2, shred2);
         }
         __syncthreads();
-        xr2c_store<R, LB, PERB>(B, a.out[grp], sbase, nl, g, a.planH, twX);
+        xr2c_store<R, LB, PERB, NCT>(B, a.out[grp], sbase, nl, g, a.planH, twX);
     }
 }
 
@@ -334,14 +336,15 @@ template <int LB, bool CONTIG, typename F> __device__ __forceinline__ void tile_
 // bsel selects the buffer in the FWD/INV modes.
 // EXTRA = false compiles the plain Euler update only (no noise, modal filter, implicit user
 // terms, RK4 stages or ImplicitEuler modes): the batched sweep, which rejects those, uses it.
-template <typename R, int LB, int PERB, bool CONTIG, bool EXTRA = true>
+// NCT > 0: the transform has the compile-time length NCT (== a.plan.n).
+template <typename R, int LB, int PERB, bool CONTIG, bool EXTRA = true, int NCT = 0>
 __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, int bsel)
 {
     typedef typename VecOf<R>::type V;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int pitch = CONTIG ? LB + 1 : LB;
     const Geom &g = a.g;
-    const int n = a.plan.n;
+    const int n = NCT ? NCT : a.plan.n;
     const int tid = threadIdx.x, nt = blockDim.x;
     const long long nlines = CONTIG ? (long long)g.Z * g.KX : g.S;
     const long long l0 = tix * LB;
@@ -366,8 +369,8 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
         V *__restrict__ buf = a.buf[bsel];
         load(sm, buf);
         __syncthreads();
-        if (a.mode == PM_FWD) fft_tile<false, LB, PERB>(sm, pitch, a.plan, a.tw);
-        else fft_tile<true, LB, PERB>(sm, pitch, a.plan, a.tw);
+        if (a.mode == PM_FWD) fft_tile_any<false, LB, PERB, NCT, 1>(sm, pitch, a.plan, a.tw);
+        else fft_tile_any<true, LB, PERB, NCT, 1>(sm, pitch, a.plan, a.tw);
         store(buf, sm);
         return;
     }
@@ -377,7 +380,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
         V *__restrict__ buf = a.buf[0];
         load(sm, buf);
         __syncthreads();
-        fft_tile<false, LB, PERB>(sm, pitch, a.plan, a.tw);
+        fft_tile_any<false, LB, PERB, NCT, 1>(sm, pitch, a.plan, a.tw);
         const R invN = (R)a.upd.invN;
         tile_foreach<LB, CONTIG>(n, [&](int p, int l) {
             if (l >= nl) return;
@@ -386,7 +389,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
             sm[p * pitch + l] = cmk<V>(v.x * b, v.y * b);
         });
         __syncthreads();
-        fft_tile<true, LB, PERB>(sm, pitch, a.plan, a.tw);
+        fft_tile_any<true, LB, PERB, NCT, 1>(sm, pitch, a.plan, a.tw);
         store(buf, sm);
         return;
     }
@@ -416,7 +419,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
     }
     for (int p = tid; p < n; p += nt) fpos[p] = CONTIG ? fsq_index<R>(p, g.Y) : fsq_index<R>(p, g.Z);
     __syncthreads();
-    for (int b = 0; b < nb; ++b) fft_tile<false, LB, PERB>(sm + b * tile, pitch, a.plan, a.tw);
+    for (int b = 0; b < nb; ++b) fft_tile_any<false, LB, PERB, NCT, 1>(sm + b * tile, pitch, a.plan, a.tw);
 
     const UpdTable &u = a.upd;
     const R dt = (R)u.dt, invN = (R)u.invN;
@@ -599,14 +602,14 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
         sm[p * pitch + l] = cmk<V>(cn.x * invN, cn.y * invN);
     });
     __syncthreads();
-    fft_tile<true, LB, PERB>(sm, pitch, a.plan, a.tw);
+    fft_tile_any<true, LB, PERB, NCT, 1>(sm, pitch, a.plan, a.tw);
     store(a.tout, sm);
 }
 
-template <typename R, int LB, int PERB>
+template <typename R, int LB, int PERB, bool MULTI = false>
 __global__ void __launch_bounds__(256, (sizeof(R) == 4 ? 3 : 2)) k_xpass(const XPassArgs<R> a)
 {
-    xpass_tile<R, LB, PERB>(a, blockIdx.x, blockIdx.y);
+    xpass_tile<R, LB, PERB, MULTI>(a, blockIdx.x, blockIdx.y);
 }
 
 template <typename R, int LB, int PERB, bool CONTIG>
@@ -650,15 +653,23 @@ inline int spass_smem_bytes(const Geom &g, int n, int LB, int nbuf, int vbytes) 
 template <typename R, int LB> static cudaError_t launch_xpass_lb(const XPassArgs<R> &a, cudaStream_t st)
 {
     typedef typename VecOf<R>::type V;
-    const int smem = xpass_smem_bytes(a.g, LB, sizeof(V), a.program == XP_MULTI ? a.mono.nin + 1 : 2);
-    auto kern = k_xpass<R, LB, perb<R>()>;
-    static int have = 48 * 1024; // one per kernel instantiation
-    cudaError_t e = ensure_smem(kern, smem, have);
-    if (e != cudaSuccess) return e;
+    const bool multi = (a.program == XP_MULTI);
+    const int smem = xpass_smem_bytes(a.g, LB, sizeof(V), multi ? a.mono.nin + 1 : 2);
     if (!threads_ok((long long)LB * a.g.H, perb<R>())) return cudaErrorInvalidConfiguration;
     const int nt = pick_threads((long long)LB * a.g.H, perb<R>());
     dim3 grid((a.g.Y + LB - 1) / LB, a.g.Z);
-    kern<<<grid, nt, smem, st>>>(a);
+    cudaError_t e;
+    if (multi) {
+        auto kern = k_xpass<R, LB, perb<R>(), true>;
+        static int have = 48 * 1024; // one per kernel instantiation
+        if ((e = ensure_smem(kern, smem, have)) != cudaSuccess) return e;
+        kern<<<grid, nt, smem, st>>>(a);
+    } else {
+        auto kern = k_xpass<R, LB, perb<R>(), false>;
+        static int have = 48 * 1024;
+        if ((e = ensure_smem(kern, smem, have)) != cudaSuccess) return e;
+        kern<<<grid, nt, smem, st>>>(a);
+    }
     return cudaGetLastError();
 }
 

@@ -101,3 +101,25 @@ def test_batch_with_large_instances_runs_and_stays_finite():
         d = m.download(0).real
         assert np.all(np.isfinite(d))
         assert abs(d.sum() - m0) / d.size <= 1e-5
+
+
+def test_batch_size_classes_equal_generic_contexts():
+    """The sweep's sides go through compile-time-plan kernels (one per size class, run as parallel
+    graph branches); they compute what the runtime-plan kernels of single contexts compute."""
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+
+    sides = [1024, 768, 512, 384, 256, 128, 128, 512]
+    a_models, b_models = [], []
+    for i, side in enumerate(sides):
+        c0 = uniform_field(3000 + i, side * side, 0.5, 0.05)
+        a_models.append(ch_ctx(side, "fp32", 0.4 + 0.1 * i, 1.0, 0.05, c0, fast=False))
+        b_models.append(ch_ctx(side, "fp32", 0.4 + 0.1 * i, 1.0, 0.05, c0, fast=False))
+    batch = G.Batch(a_models)
+    assert batch.kernels_per_step() == 6 + 6 + 1
+    batch.step(12)
+    for m in b_models:
+        m.step(12)
+    for a, b in zip(a_models, b_models):
+        x, y = a.download_real(0), b.download_real(0)
+        assert np.max(np.abs(x - y)) <= 1e-6 * np.max(np.abs(y))
