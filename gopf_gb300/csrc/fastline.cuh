@@ -4,12 +4,14 @@
 // A line is held by T threads, 16 values each.  Forward transform (decimation in time):
 //   A: thread r holds x[r + T i] (i < 16): radix-16 DFT over i in registers, twiddle W_L^(r k1)
 //      -> Y[r][k1]; exchange through shared memory;
-//   B: X[k1 + 16 k2] = sum_r W_T^(r k2) Y[r][k1], a DFT of length T = P U per k1, split as
-//      r = U s + u: a radix-P DFT over s in registers (P = 16, or two radix-8 DFTs for two k1
-//      when T = 8 U), twiddle W_T^(u c), then a radix-U DFT across the U threads of a column:
-//      warp shuffles for U = 2, 4, a second shared-memory exchange for U = 3.
-// The output stays distributed ("B layout": a thread holds X[k1 + 16 c + 16 P' d] for its own
-// column and one d), which is where the k-space update happens.  The inverse transform runs the
+//   B: X[k1 + 16 k2] = sum_r W_T^(r k2) Y[r][k1], a DFT of length T = P U per k1.
+//      U = 1, 2, 4 (T = 16, 32, 64): r = U s + u, a radix-16 DFT over s in registers, twiddle
+//      W_T^(u c), then a radix-U DFT across the U threads of a column by warp shuffles.
+//      U = 3 (T = 48, 24): r = s + P t, k2 = 3 c + d; the thread computing output d forms the
+//      radix-3 over t while reading its column from the exchange, then twiddles W_T^(s d) and
+//      runs a radix-P DFT over s (P = 16, or two radix-8 DFTs for two columns when T = 24).
+// The output stays distributed ("B layout": a thread holds X[k] for one column and one d),
+// which is where the k-space update happens.  The inverse transform runs the
 // same steps in reverse order with conjugate twiddles (decimation in frequency), so it takes the
 // B layout and ends in the A layout x[r + T i] that was loaded: the update pass reads and writes
 // every line in place, coalesced.  L = 256 (T = 16, U = 1) is the engine of fast256.cuh.
@@ -70,8 +72,12 @@ template <int L> struct Role {
     __device__ __forceinline__ int elem(int j) const
     {
         typedef Geo<L> G;
-        if constexpr (G::P8) return k1 + ((j >> 3) << 3) + 16 * (j & 7) + 128 * d;
-        else return k1 + 16 * j + 256 * d;
+        if constexpr (G::U == 3) { // k2 = 3 c + d
+            if constexpr (G::P8) return k1 + ((j >> 3) << 3) + 48 * (j & 7) + 16 * d;
+            else return k1 + 48 * j + 16 * d;
+        } else {
+            return k1 + 16 * j + 256 * d;
+        }
     }
 };
 
@@ -129,33 +135,13 @@ template <int U, bool INV> __device__ __forceinline__ void xdft_inv(float2 (&v)[
     }
 }
 
-// radix-3 across the three threads of a column through shared memory (U = 3): the thread keeps
-// output d = u.  z is this line's slot region; the caller synchronises around.
-template <int L, bool INV>
-__device__ __forceinline__ void xdft3(float2 (&v)[16], const Role<L> &ro, float2 *z)
+// one output of a radix-3 DFT: a0 + W3^d a1 + W3^(2d) a2 (W3 = exp(-2 pi i/3), conjugate on the inverse)
+template <bool INV> __device__ __forceinline__ float2 dft3_out(float2 a0, float2 a1, float2 a2, int d)
 {
-    typedef Geo<L> G;
-    // slot of (u, j, column): j < 16 values of the column
-    auto s3 = [&](int uu, int j, int col) -> float2 & {
-        if constexpr (G::P8) return z[(uu * 8 + (j & 7)) * 16 + ((col + (j >> 3) * 8) ^ ((uu & 1) << 3))];
-        else return z[(uu * 16 + j) * 16 + col];
-    };
-#pragma unroll
-    for (int j = 0; j < 16; ++j) s3(ro.u, j, ro.k1) = v[j];
-    __syncthreads();
-    const float c3 = -0.5f, s3v = INV ? 0.86602540378443864676f : -0.86602540378443864676f;
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-        const float2 a = s3(0, j, ro.k1), b = s3(1, j, ro.k1), c = s3(2, j, ro.k1);
-        if (ro.u == 0) v[j] = add2(a, add2(b, c));
-        else {
-            // X_d = a + W3^d b + W3^(2d) c, W3 = c3 + i s3v (forward: s3v < 0)
-            const float sd = (ro.u == 1) ? s3v : -s3v;
-            const float2 w1 = make_float2(c3, sd);
-            v[j] = add2(a, add2(cm(b, w1), cm(c, make_float2(c3, -sd))));
-        }
-    }
-    __syncthreads();
+    if (d == 0) return add2(a0, add2(a1, a2));
+    const float c3 = -0.5f, s3 = INV ? 0.86602540378443864676f : -0.86602540378443864676f;
+    const float sd = (d == 1) ? s3 : -s3;
+    return add2(a0, add2(cm(a1, make_float2(c3, sd)), cm(a2, make_float2(c3, -sd))));
 }
 
 // radix-8 DFT (natural order in and out) on v[o .. o+7]
@@ -181,18 +167,28 @@ __device__ __forceinline__ void line_fwd(float2 (&v)[16], int r, const Role<L> &
 #pragma unroll
     for (int k1 = 0; k1 < 16; ++k1) z[slot(r, k1)] = v[k1];
     __syncthreads();
-    if constexpr (G::P8) {
+    if constexpr (G::U == 3) {
+        // T = 3 P: r = s + P t, k2 = 3 c + d.  The thread's output d: radix-3 over t (reading the
+        // three rows of each s), twiddle W_T^(s d) = W_L^(16 s d), radix-P over s.
+        constexpr int P = G::P;
 #pragma unroll
-        for (int h = 0; h < 2; ++h)
+        for (int h = 0; h < 16 / P; ++h)
 #pragma unroll
-            for (int s = 0; s < 8; ++s) v[8 * h + s] = z[slot(G::U * s + ro.u, ro.k1 + 8 * h)];
+            for (int s = 0; s < P; ++s) {
+                const int col = ro.k1 + 8 * h;
+                v[P * h + s] = dft3_out<false>(z[slot(s, col)], z[slot(s + P, col)], z[slot(s + 2 * P, col)], ro.d);
+            }
         __syncthreads();
-        dft8at<false>(v, 0);
-        dft8at<false>(v, 8);
-        if (ro.u)
+        if (ro.d)
 #pragma unroll
             for (int j = 0; j < 16; ++j)
-                if (j & 7) v[j] = cm(v[j], tw[16 * ro.u * (j & 7)]); // W_T^(u c) = W_L^(16 u c)
+                if (j % P) v[j] = cm(v[j], tw[16 * ro.d * (j % P)]);
+        if constexpr (G::P8) {
+            dft8at<false>(v, 0);
+            dft8at<false>(v, 8);
+        } else {
+            pdft16<false>(v);
+        }
     } else {
 #pragma unroll
         for (int s = 0; s < 16; ++s) v[s] = z[slot(G::U * s + ro.u, ro.k1)];
@@ -201,9 +197,8 @@ __device__ __forceinline__ void line_fwd(float2 (&v)[16], int r, const Role<L> &
         if (G::U > 1 && ro.u)
 #pragma unroll
             for (int c = 1; c < 16; ++c) v[c] = cm(v[c], tw[16 * ro.u * c]);
+        if constexpr (G::U == 2 || G::U == 4) xdft_fwd<G::U, false>(v, ro.u);
     }
-    if constexpr (G::U == 2 || G::U == 4) xdft_fwd<G::U, false>(v, ro.u);
-    else if constexpr (G::U == 3) xdft3<L, false>(v, ro, z);
 }
 
 // Inverse (unnormalised) transform: in v[j] = X[ro.elem(j)]; out v[i] = x[r + T i] * L.
@@ -211,31 +206,43 @@ template <int L>
 __device__ __forceinline__ void line_inv(float2 (&v)[16], int r, const Role<L> &ro, float2 *z, const float2 *tw)
 {
     typedef Geo<L> G;
-    if constexpr (G::U == 2 || G::U == 4) xdft_inv<G::U, true>(v, ro.u);
-    else if constexpr (G::U == 3) xdft3<L, true>(v, ro, z);
-    if constexpr (G::P8) {
-        if (ro.u)
+    if constexpr (G::U == 3) {
+        // reverse of the forward: radix-P over c, conjugate twiddle, then the radix-3 over d is
+        // formed by the reading thread r = s + P t from the three d slots of (s, column)
+        constexpr int P = G::P;
+        if constexpr (G::P8) {
+            dft8at<true>(v, 0);
+            dft8at<true>(v, 8);
+        } else {
+            pdft16<true>(v);
+        }
+        if (ro.d)
 #pragma unroll
             for (int j = 0; j < 16; ++j)
-                if (j & 7) v[j] = cmc(v[j], tw[16 * ro.u * (j & 7)]);
-        dft8at<true>(v, 0);
-        dft8at<true>(v, 8);
+                if (j % P) v[j] = cmc(v[j], tw[16 * ro.d * (j % P)]);
 #pragma unroll
-        for (int h = 0; h < 2; ++h)
+        for (int h = 0; h < 16 / P; ++h)
 #pragma unroll
-            for (int s = 0; s < 8; ++s) z[slot(G::U * s + ro.u, ro.k1 + 8 * h)] = v[8 * h + s];
+            for (int s = 0; s < P; ++s) z[slot(ro.d * P + s, ro.k1 + 8 * h)] = v[P * h + s];
+        __syncthreads();
+        const int s0 = r % P, t0 = r / P;
+#pragma unroll
+        for (int k1 = 0; k1 < 16; ++k1)
+            v[k1] = dft3_out<true>(z[slot(s0, k1)], z[slot(P + s0, k1)], z[slot(2 * P + s0, k1)], t0);
+        __syncthreads();
     } else {
+        if constexpr (G::U == 2 || G::U == 4) xdft_inv<G::U, true>(v, ro.u);
         if (G::U > 1 && ro.u)
 #pragma unroll
             for (int c = 1; c < 16; ++c) v[c] = cmc(v[c], tw[16 * ro.u * c]);
         pdft16<true>(v);
 #pragma unroll
         for (int s = 0; s < 16; ++s) z[slot(G::U * s + ro.u, ro.k1)] = v[s];
-    }
-    __syncthreads();
+        __syncthreads();
 #pragma unroll
-    for (int k1 = 0; k1 < 16; ++k1) v[k1] = z[slot(r, k1)];
-    __syncthreads();
+        for (int k1 = 0; k1 < 16; ++k1) v[k1] = z[slot(r, k1)];
+        __syncthreads();
+    }
 #pragma unroll
     for (int k1 = 1; k1 < 16; ++k1) v[k1] = cmc(v[k1], tw[r * k1]);
     pdft16<true>(v);

@@ -227,6 +227,7 @@ struct BatchLaunch {
     int2 *d_items = nullptr;
     int nitems = 0;
     int grid = 0, smem = 0, threads = 256;
+    std::vector<int> inst; // the instances it covers (sorted)
 };
 
 struct gopf_batch {
@@ -236,6 +237,10 @@ struct gopf_batch {
     cudaStream_t own_stream = nullptr, stream = nullptr;
     void *d_inst = nullptr;
     std::vector<BatchLaunch> xl, yl; // the x and y passes, one launch per size class present
+    // When the x and y classes cover the same instance sets (square instances), class i's y pass
+    // depends only on class i's x pass: each class runs x then y on its own branch (chain[i] =
+    // indices into xl, yl), with no pass-wide join.  Empty: two pass-wide phases.
+    std::vector<std::pair<int, int>> chain;
     std::vector<cudaStream_t> side;  // branch streams of a pass's launches
     std::vector<cudaEvent_t> ev;     // [0] fork, [1 ..] joins
     long long herm_total = 0;
@@ -355,6 +360,9 @@ template <typename R> static int batch_build(gopf_batch *b)
             std::vector<int2> items;
             for (auto &p : lists[k]) items.push_back(p.second);
             BatchLaunch L;
+            for (auto &it : items) L.inst.push_back(it.x);
+            std::sort(L.inst.begin(), L.inst.end());
+            L.inst.erase(std::unique(L.inst.begin(), L.inst.end()), L.inst.end());
             L.fn = xpass ? x_kernel<R>(k) : y_kernel<R>(k);
             L.nitems = (int)items.size();
             L.smem = smem[k];
@@ -373,6 +381,13 @@ template <typename R> static int batch_build(gopf_batch *b)
     int rc;
     if ((rc = make(xs, smem_x, thr_x, true, b->xl))) return rc;
     if ((rc = make(ys, smem_y, thr_y, false, b->yl))) return rc;
+    b->chain.clear();
+    if (b->xl.size() == b->yl.size()) {
+        for (size_t i = 0; i < b->xl.size(); ++i)
+            for (size_t j = 0; j < b->yl.size(); ++j)
+                if (b->xl[i].inst == b->yl[j].inst) b->chain.push_back({(int)i, (int)j});
+        if (b->chain.size() != b->xl.size()) b->chain.clear();
+    }
     const size_t nbranch = std::max(b->xl.size(), b->yl.size());
     while (b->side.size() + 1 < nbranch) {
         cudaStream_t st;
@@ -413,12 +428,46 @@ template <typename R> static cudaError_t batch_pass(gopf_batch *b, const std::ve
     return cudaSuccess;
 }
 
+template <typename R> static cudaError_t launch_one(gopf_batch *b, const BatchLaunch &L, cudaStream_t st)
+{
+    const BatchInst<R> *inst = (const BatchInst<R> *)b->d_inst;
+    const int2 *items = L.d_items;
+    int n = L.nitems;
+    void *args[] = {(void *)&inst, (void *)&items, (void *)&n};
+    return cudaLaunchKernel(L.fn, dim3(L.grid), dim3(L.threads), args, (size_t)L.smem, st);
+}
+
+// class chains: x then y of each class on its own branch
+template <typename R> static cudaError_t batch_chains(gopf_batch *b)
+{
+    cudaError_t e;
+    const size_t n = b->chain.size();
+    if (n > 1) {
+        if ((e = cudaEventRecord(b->ev[0], b->stream)) != cudaSuccess) return e;
+        for (size_t i = 1; i < n; ++i)
+            if ((e = cudaStreamWaitEvent(b->side[i - 1], b->ev[0], 0)) != cudaSuccess) return e;
+    }
+    for (size_t i = 0; i < n; ++i) {
+        cudaStream_t st = (i == 0) ? b->stream : b->side[i - 1];
+        if ((e = launch_one<R>(b, b->xl[b->chain[i].first], st)) != cudaSuccess) return e;
+        if ((e = launch_one<R>(b, b->yl[b->chain[i].second], st)) != cudaSuccess) return e;
+        if (i > 0 && (e = cudaEventRecord(b->ev[i], st)) != cudaSuccess) return e;
+    }
+    for (size_t i = 1; i < n; ++i)
+        if ((e = cudaStreamWaitEvent(b->stream, b->ev[i], 0)) != cudaSuccess) return e;
+    return cudaSuccess;
+}
+
 template <typename R> static cudaError_t batch_enqueue(gopf_batch *b)
 {
     const BatchInst<R> *inst = (const BatchInst<R> *)b->d_inst;
     cudaError_t e;
-    if ((e = batch_pass<R>(b, b->xl)) != cudaSuccess) return e;
-    if ((e = batch_pass<R>(b, b->yl)) != cudaSuccess) return e;
+    if (!b->chain.empty()) {
+        if ((e = batch_chains<R>(b)) != cudaSuccess) return e;
+    } else {
+        if ((e = batch_pass<R>(b, b->xl)) != cudaSuccess) return e;
+        if ((e = batch_pass<R>(b, b->yl)) != cudaSuccess) return e;
+    }
     const unsigned hb = (unsigned)std::min<long long>((b->herm_total + 255) / 256, 152 * 4);
     k_batch_herm<R><<<hb, 256, 0, b->stream>>>(inst, (int)b->ctx.size(), b->herm_total);
     return cudaGetLastError();

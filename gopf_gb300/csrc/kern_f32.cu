@@ -4,6 +4,7 @@
 #include <mutex>
 
 #include "fast256.cuh"
+#include "fastline.cuh"
 #include "plane256.cuh"
 #include "gopf_kernels_impl.cuh"
 #include "x256_io.cuh"
@@ -217,6 +218,83 @@ template <> int xpass_red_blocks<float>(const XPassArgs<float> &a, int LB)
     return ((a.g.Y + LB - 1) / LB) * a.g.Z;
 }
 
+// ---- the register-resident line engine for 2D lines of 384 ... 1024 (fastline.cuh) ----
+
+template <int L, int NG> __global__ void __launch_bounds__(fl::Geo<L>::NT, 3) k_yline(const PassArgs<float> a)
+{
+    fl::yline_tile<L, NG>(a, blockIdx.x);
+}
+template <int L> __global__ void __launch_bounds__(fl::Geo<L>::NT, 3) k_xline(const XPassArgs<float> a)
+{
+    fl::xline_tile<L>(a, blockIdx.x, blockIdx.y);
+}
+
+static bool line_len(int n) { return n == 384 || n == 512 || n == 768 || n == 1024; }
+
+static bool fast_x_line(const XPassArgs<float> &a)
+{
+    return a.allow_fast && line_len(a.g.X) && a.in_mode == XIN_SPECTRAL && a.program == XP_POLY && !a.identity &&
+           !a.rout && !a.red && !a.red2 && a.ngrp_out > 0;
+}
+
+// the 2D fused Euler update without noise, filters, symbols or field terms
+static bool fast_y_line(const PassArgs<float> &a)
+{
+    const UpdTable &u = a.upd;
+    return a.allow_fast && line_len(a.plan.n) && a.g.Y == a.plan.n && a.g.Z == 1 && a.mode == PM_FUSED && a.nbuf <= 2 &&
+           u.rk_stage == 0 && u.etd == 0 && u.nxs == 0 && u.nxf == 0 && u.nimp <= 4 && !u.noise.kind && !u.filt;
+}
+
+template <typename K> static cudaError_t line_smem(K kern, int bytes)
+{
+    return bytes > 48 * 1024 ? cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)
+                             : cudaSuccess;
+}
+
+template <int L> static cudaError_t launch_xline(const XPassArgs<float> &a, cudaStream_t st)
+{
+    typedef fl::Geo<L> G;
+    if (a.g.Y % (2 * G::LPB)) return cudaErrorNotSupported;
+    static const cudaError_t attr = line_smem(k_xline<L>, fl::xline_smem_bytes<L>());
+    if (attr != cudaSuccess) return attr;
+    k_xline<L><<<dim3(a.g.Y / (2 * G::LPB), a.g.Z), G::NT, fl::xline_smem_bytes<L>(), st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int L, int NG> static cudaError_t launch_yline(const PassArgs<float> &a, cudaStream_t st)
+{
+    typedef fl::Geo<L> G;
+    static const cudaError_t attr = line_smem(k_yline<L, NG>, fl::yline_smem_bytes<L>());
+    if (attr != cudaSuccess) return attr;
+    k_yline<L, NG><<<(unsigned)((a.g.KX + G::LPB - 1) / G::LPB), G::NT, fl::yline_smem_bytes<L>(), st>>>(a);
+    return cudaGetLastError();
+}
+
+static bool launch_x_line(const XPassArgs<float> &a, cudaStream_t st, cudaError_t *e)
+{
+    if (!fast_x_line(a)) return false;
+    switch (a.g.X) {
+    case 384: *e = launch_xline<384>(a, st); break;
+    case 512: *e = launch_xline<512>(a, st); break;
+    case 768: *e = launch_xline<768>(a, st); break;
+    default: *e = launch_xline<1024>(a, st); break;
+    }
+    return *e != cudaErrorNotSupported;
+}
+
+static bool launch_y_line(const PassArgs<float> &a, cudaStream_t st, cudaError_t *e)
+{
+    if (!fast_y_line(a)) return false;
+    const bool two = a.nbuf > 1;
+    switch (a.plan.n) {
+    case 384: *e = two ? launch_yline<384, 2>(a, st) : launch_yline<384, 1>(a, st); break;
+    case 512: *e = two ? launch_yline<512, 2>(a, st) : launch_yline<512, 1>(a, st); break;
+    case 768: *e = two ? launch_yline<768, 2>(a, st) : launch_yline<768, 1>(a, st); break;
+    default: *e = two ? launch_yline<1024, 2>(a, st) : launch_yline<1024, 1>(a, st); break;
+    }
+    return true;
+}
+
 template <> cudaError_t launch_xpass<float>(const XPassArgs<float> &a, int LB, cudaStream_t st)
 {
     {
@@ -230,6 +308,10 @@ template <> cudaError_t launch_xpass<float>(const XPassArgs<float> &a, int LB, c
         if (a.ngrp_out == 1) f256::k_x256<1><<<grid, f256::NT, 0, st>>>(a);
         else f256::k_x256<0><<<grid, f256::NT, 0, st>>>(a);
         return cudaGetLastError();
+    }
+    {
+        cudaError_t e;
+        if (launch_x_line(a, st, &e)) return e;
     }
     return launch_xpass_generic<float>(a, LB, st);
 }
@@ -249,6 +331,10 @@ template <> cudaError_t launch_cpass<float>(const PassArgs<float> &a, int LB, cu
             else f256::k_y256<1, false><<<grid, f256::NT, 0, st>>>(a);
         }
         return cudaGetLastError();
+    }
+    {
+        cudaError_t e;
+        if (launch_y_line(a, st, &e)) return e;
     }
     return launch_cpass_generic<float>(a, LB, st);
 }

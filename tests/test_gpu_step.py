@@ -276,10 +276,11 @@ def _two_group_model(dims, prec, c0, fast):
     return m
 
 
-@pytest.mark.parametrize("dims", [[256, 256, 256], [256, 256]])
+@pytest.mark.parametrize("dims", [[256, 256, 256], [256, 256], [384, 384], [512, 512], [768, 768], [1024, 1024]])
 @pytest.mark.parametrize("two_groups", [False, True])
 def test_fast_kernels_match_generic(dims, two_groups):
-    """The 256-point register kernels and the generic Stockham kernels agree (FP32, 20 steps)."""
+    """The register kernels (the 256-point engine, and the line engine for 2D sides 384 ... 1024)
+    and the generic Stockham kernels agree (FP32, 20 steps)."""
     import gopf_gb300 as G
     from gopf_gb300.synthetic import uniform_field
 
@@ -442,3 +443,18 @@ def test_point_monitor_matches_download(dims, prec, tol):
     with pytest.raises(G.GopfError) as e:
         m.point_values(0, [n])
     assert e.value.status == 1
+
+
+@pytest.mark.parametrize("side", [384, 512, 768, 1024])
+def test_line_engine_2d_vs_oracle(oracle, side):
+    """2D FP32 Cahn-Hilliard on the line engine against the FP64 oracle (rel-L2 <= 1e-5, 10 steps)."""
+    from gopf_gb300.synthetic import uniform_field
+
+    dims = [side, side]
+    c0 = uniform_field(7, side * side, 0.5, 0.05)
+    g = ch_gpu(dims, "fp32", 0.5, 0.05, c0)
+    g.step(10)
+    o = oracle.cahn_hilliard(dims, gamma=0.5)
+    o.set_field(0, c0)
+    o.step_euler(0.05, 10)
+    assert rel_l2(g.download_real(0), o.field(0).real) <= 1e-5
