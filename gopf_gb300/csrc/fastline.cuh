@@ -272,9 +272,14 @@ template <int L, int NG> __device__ __forceinline__ void yline_tile(const PassAr
     }
     const Role<L> ro(r);
     const float2 *__restrict__ U0 = a.buf[0];
-    float2 v[16];
+    float2 *__restrict__ state = a.state;
+    float2 v[16], cs[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = valid ? U0[q * L + r + G::T * i] : zero;
+    // c-hat of the thread's B-layout elements, requested before the transform so that its
+    // latency overlaps the forward FFT
+#pragma unroll
+    for (int j = 0; j < 16; ++j) cs[j] = valid ? state[q * L + ro.elem(j)] : zero;
     __syncthreads();
     line_fwd<L>(v, r, ro, z, s_tw);
     const UpdTable &u = a.upd;
@@ -293,16 +298,14 @@ template <int L, int NG> __device__ __forceinline__ void yline_tile(const PassAr
         const float fx = (float)kx / (float)g.X;
         fl = fx * fx + f256::fsqf(zz, g.Z);
     }
-    float2 *__restrict__ state = a.state;
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
         const int k = ro.elem(j);
         float2 cn = zero;
         if (valid) {
             const float mk = -39.478417604357434f * (fl + s_fy[k]);
-            const long long gi = q * L + k;
-            cn = f256::euler_update<NG>(R, state[gi], v[j], (NG > 1) ? w[NG > 1 ? j : 0] : v[j], mk);
-            state[gi] = cn;
+            cn = f256::euler_update<NG>(R, cs[j], v[j], (NG > 1) ? w[NG > 1 ? j : 0] : v[j], mk);
+            state[q * L + k] = cn;
         }
         v[j] = make_float2(cn.x * R.invN, cn.y * R.invN);
     }
