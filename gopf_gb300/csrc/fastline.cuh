@@ -325,31 +325,44 @@ template <int L> __host__ __device__ constexpr int xline_area()
 }
 template <int L> constexpr int xline_smem_bytes() { return (xline_area<L>() + L) * 8 + GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1) * 4; }
 
-// One x tile: 2 LPB rows from y0 of depth plane zp; c2r -> polynomial groups -> r2c into
-// a.out[grp] (L = g.X columns).
-template <int L> __device__ __forceinline__ void xline_tile(const XPassArgs<float> &a, int ty, int zp)
+// 16-byte asynchronous global -> shared copy (no register staging), completed by cp_async_wait
+__device__ __forceinline__ void cp_async16(void *dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Request the spectral tile of x tile ty (kx = 0 .. L/2, rows y0 .. y0 + 2 LPB) into area[kx][row]
+// with asynchronous copies (g.Y must be a multiple of 2 LPB).
+template <int L> __device__ __forceinline__ void xline_request(float2 *area, const XPassArgs<float> &a, int ty, int zp)
+{
+    typedef Geo<L> G;
+    constexpr int KX = L / 2 + 1, RB = 2 * G::LPB, CH = RB / 2;
+    const long long sbase = (long long)zp * a.g.S + (long long)ty * RB;
+    const float2 *__restrict__ in = a.in;
+    for (int e = threadIdx.x; e < KX * CH; e += G::NT) {
+        const int kx = e / CH, c = e - kx * CH;
+        cp_async16(&area[kx * RB + 2 * c], &in[sbase + (long long)kx * a.g.Y + 2 * c]);
+    }
+    cp_async_commit();
+}
+
+// One x tile from its spectral tile in area (which then serves as exchange and separation
+// space): c2r of 2 LPB rows -> polynomial groups -> r2c into a.out[grp] (L = g.X columns).
+// s_poly: this instance's dense polynomial coefficients.  Ends with a barrier.
+template <int L>
+__device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float> &a, int ty, int zp,
+                                              const float2 *s_tw, const float *s_poly)
 {
     typedef Geo<L> G;
     constexpr int H = L / 2, KX = H + 1, RB = 2 * G::LPB;
-    extern __shared__ __align__(16) unsigned char fl_dsm[];
-    float2 *s_a = reinterpret_cast<float2 *>(fl_dsm); // input tile, then exchange slots
-    float2 *s_sep = s_a;                               // [LPB][L + 1], once the exchange is done
-    float2 *s_tw = s_a + xline_area<L>();
-    float *s_poly = reinterpret_cast<float *>(s_tw + L);
+    float2 *s_sep = s_a; // [LPB][L + 1], once the exchange is done
     const Geom &g = a.g;
     const int l = threadIdx.x / G::T, r = threadIdx.x - l * G::T;
     const int y0 = ty * RB;
     const long long sbase = (long long)zp * g.S + y0;
     const int Y = g.Y;
-    for (int t = threadIdx.x; t < L; t += G::NT) s_tw[t] = a.twX[t];
-    for (int t = threadIdx.x; t < GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1); t += G::NT)
-        s_poly[t] = (float)a.pw.dense[t / (GOPF_MAX_DEG + 1)][t % (GOPF_MAX_DEG + 1)];
-    const float2 *__restrict__ in = a.in;
-    for (int e = threadIdx.x; e < KX * RB; e += G::NT) {
-        const int kx = e / RB, y = e - kx * RB;
-        s_a[e] = (y0 + y < Y) ? in[sbase + (long long)kx * Y + y] : make_float2(0.f, 0.f);
-    }
-    __syncthreads();
     const Role<L> ro(r);
     // Hermitian extension of rows (2l, 2l + 1) packed as a + i b, in the B layout
     float2 v[16];
@@ -389,6 +402,27 @@ template <int L> __device__ __forceinline__ void xline_tile(const XPassArgs<floa
         }
         __syncthreads();
     }
+}
+
+template <int L> __device__ __forceinline__ void load_xconsts(const XPassArgs<float> &a, float2 *s_tw, float *s_poly)
+{
+    for (int t = threadIdx.x; t < L; t += Geo<L>::NT) s_tw[t] = a.twX[t];
+    for (int t = threadIdx.x; t < GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1); t += Geo<L>::NT)
+        s_poly[t] = (float)a.pw.dense[t / (GOPF_MAX_DEG + 1)][t % (GOPF_MAX_DEG + 1)];
+}
+
+// One x tile: 2 LPB rows from row ty * 2 LPB of depth plane zp (g.Y a multiple of 2 LPB).
+template <int L> __device__ __forceinline__ void xline_tile(const XPassArgs<float> &a, int ty, int zp)
+{
+    extern __shared__ __align__(16) unsigned char fl_dsm[];
+    float2 *s_a = reinterpret_cast<float2 *>(fl_dsm);
+    float2 *s_tw = s_a + xline_area<L>();
+    float *s_poly = reinterpret_cast<float *>(s_tw + L);
+    xline_request<L>(s_a, a, ty, zp);
+    load_xconsts<L>(a, s_tw, s_poly);
+    cp_async_wait<0>();
+    __syncthreads();
+    xline_compute<L>(s_a, a, ty, zp, s_tw, s_poly);
 }
 
 } // namespace fl
