@@ -21,6 +21,24 @@ namespace gopf {
 template <int LB> struct Log2 { static constexpr int v = (LB == 1) ? 0 : 1 + Log2<LB / 2>::v; };
 template <> struct Log2<1> { static constexpr int v = 0; };
 
+// Asynchronous global -> shared copy of one spectral element (8 or 16 bytes), or zeros when
+// `valid` is false; the copies of a tile are issued back to back and completed together by
+// ga_wait() before the barrier that publishes the tile.
+template <typename V> __device__ __forceinline__ void ga_copy(V *dst, const V *src, bool valid)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    const int n = valid ? (int)sizeof(V) : 0;
+    if constexpr (sizeof(V) == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(n) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(src), "r"(n) : "memory");
+}
+__device__ __forceinline__ void ga_wait()
+{
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
 template <typename R> __device__ __forceinline__ R poly_eval(const PwTable &pw, int grp, R c)
 {
     const int d = pw.deg[grp];
@@ -82,11 +100,11 @@ __device__ __forceinline__ void xload_c2r(typename VecOf<R>::type *A, const type
     constexpr int LBSH = Log2<LB>::v;
     const int H = NCT ? NCT : g.H, KX = H + 1, Y = g.Y;
     const int tid = threadIdx.x, nt = blockDim.x;
-    const V zero = cmk<V>((R)0, (R)0);
     for (int e = tid; e < KX * LB; e += nt) {
         const int kx = e >> LBSH, l = e & (LB - 1);
-        A[e] = (l < nl) ? in[sbase + (long long)kx * Y + l] : zero;
+        ga_copy(&A[e], in + sbase + (long long)kx * Y + (l < nl ? l : 0), l < nl);
     }
+    ga_wait();
     __syncthreads();
     const int npair = H / 2 + 1;
     for (int e = tid; e < npair * LB; e += nt) {
@@ -223,8 +241,9 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
         const V *rin2 = reinterpret_cast<const V *>(a.rin) + ((long long)z * Y + y0) * H;
         for (int e = tid; e < LB * H; e += nt) {
             const int l = e / H, m = e - l * H;
-            A[m * LB + l] = (l < nl) ? rin2[(long long)l * H + m] : zero;
+            ga_copy(&A[m * LB + l], rin2 + (long long)(l < nl ? l : 0) * H + m, l < nl);
         }
+        ga_wait();
         __syncthreads();
     }
 
@@ -356,8 +375,8 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
     V *sm = reinterpret_cast<V *>(smem_raw);
     const V zero = cmk<V>((R)0, (R)0);
     auto gidx = [&](int p, int l) -> long long { return gbase + p * pstride + l * lstride; };
-    auto load = [&](V *dst, const V *__restrict__ src) {
-        tile_foreach<LB, CONTIG>(n, [&](int p, int l) { dst[p * pitch + l] = (l < nl) ? src[gidx(p, l)] : zero; });
+    auto load = [&](V *dst, const V *__restrict__ src) { // completed by ga_wait() before the next barrier
+        tile_foreach<LB, CONTIG>(n, [&](int p, int l) { ga_copy(&dst[p * pitch + l], src + gidx(p, l < nl ? l : 0), l < nl); });
     };
     auto store = [&](V *__restrict__ dst, const V *s) {
         tile_foreach<LB, CONTIG>(n, [&](int p, int l) {
@@ -368,6 +387,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
     if (a.mode == PM_FWD || a.mode == PM_INV) {
         V *__restrict__ buf = a.buf[bsel];
         load(sm, buf);
+        ga_wait();
         __syncthreads();
         if (a.mode == PM_FWD) fft_tile_any<false, LB, PERB, NCT, 1>(sm, pitch, a.plan, a.tw);
         else fft_tile_any<true, LB, PERB, NCT, 1>(sm, pitch, a.plan, a.tw);
@@ -379,6 +399,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
         // w-hat = b(k) * H-hat / N along the last axis, then back (pf/homoLinElast.go:53-75)
         V *__restrict__ buf = a.buf[0];
         load(sm, buf);
+        ga_wait();
         __syncthreads();
         fft_tile_any<false, LB, PERB, NCT, 1>(sm, pitch, a.plan, a.tw);
         const R invN = (R)a.upd.invN;
@@ -401,6 +422,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
     R *fline = reinterpret_cast<R *>(sm + nb * tile);
     R *fpos = fline + LB;
     for (int b = 0; b < nb; ++b) load(sm + b * tile, a.buf[b]);
+    ga_wait();
     for (int l = tid; l < LB; l += nt) {
         const long long q = l0 + l;
         R f2 = (R)0;
