@@ -383,6 +383,7 @@ def run_sweep(args):
 
     params = sweep_params()
     cells = sum(s * s for s, _, _ in params)
+    sweep_bytes = float(sum(6 * (s // 2 + 1) * s * 8 for s, _, _ in params))
     models = sweep_models("fp32", params)
     batch = G.Batch(models)
     stream = torch.cuda.Stream()
@@ -418,6 +419,10 @@ def run_sweep(args):
            "config": {"workload": "sweep_64_ch2d_uneven_fp32", "sides": [p[0] for p in params], "cells": cells,
                       "dt": 0.05, "params_seed": 2, "init": "c0 = 0.5 + U(-0.05, 0.05), seed 1000 + i"},
            "sequential_value": seq, "speedup_vs_sequential": batched / seq,
+           # bytes one sweep step moves: per instance the x pass reads T and writes the group (2C),
+           # the fused y pass reads the group and c-hat and writes c-hat and T (4C); FP32, C = (X/2+1) Y 8 B
+           "step_bytes_moved": sweep_bytes,
+           "fraction_of_hbm": sweep_bytes * batched / (peaks()[0] * 1e9),
            "cell_updates_per_s": batched * cells, "clocks": clk.summary(),
            "gpu_launches": batch.kernels_per_step() * args.steps}
     if args.check_steps > 0:
