@@ -283,6 +283,18 @@ class Model:
         self._ck(self._L.gopf_get_step(self._h, ctypes.byref(s)))
         return s.value
 
+    # --- point sources (Model.AddSource, pf/sourceTerm.go) ---
+    def add_source(self, eq: int, pos) -> int:
+        p = np.ascontiguousarray(pos, dtype=np.float64)
+        sid = ctypes.c_int()
+        self._ck(self._L.gopf_add_source(self._h, eq, _dptr(p), int(p.size), ctypes.byref(sid)))
+        return sid.value
+
+    def set_source_amplitudes(self, amps) -> None:
+        """amps[s, i] = f_s(t) at the i-th step from the current one, one row per source."""
+        a = np.ascontiguousarray(np.atleast_2d(amps), dtype=np.float64)
+        self._ck(self._L.gopf_set_source_amplitudes(self._h, _dptr(a), a.shape[0], a.shape[1]))
+
     # --- shrinking-dimer dynamics (pf/sdd.go); step with set_stepper("sdd", dt) ---
     def sdd_init(self, init, final) -> None:
         """SDD.Init: the orientation is final - init (all fields, field after field)."""

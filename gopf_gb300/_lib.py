@@ -88,6 +88,8 @@ SIGNATURES = {
     "gopf_synchronize": ([_vp], _i),
     "gopf_reduce": ([_vp, _i, _i, _dp], _i),
     "gopf_point_values": ([_vp, _i, ctypes.POINTER(_ll), _i, _dp], _i),
+    "gopf_add_source": ([_vp, _i, _dp, _i, _ip], _i),
+    "gopf_set_source_amplitudes": ([_vp, _dp, _i, _i], _i),
     "gopf_sdd_init": ([_vp, _dp, _dp, _sz], _i),
     "gopf_sdd_set_orientation": ([_vp, _dp, _sz], _i),
     "gopf_sdd_set_params": ([_vp] + [ctypes.c_double] * 5, _i),

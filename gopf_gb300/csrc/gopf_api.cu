@@ -300,8 +300,8 @@ static void ctx_free(gopf_ctx *ctx)
     }
     for (int i = 0; i < GOPF_MAX_XOUT; ++i)
         if (ctx->d_mU[i]) cudaFree(ctx->d_mU[i]);
-    void *more[] = {ctx->d_bsym, ctx->d_U0, ctx->d_UH, ctx->d_vc, ctx->d_red2, ctx->d_rkF, ctx->d_stepctr, ctx->d_status,
-                    ctx->d_filter};
+    void *more[] = {ctx->d_bsym, ctx->d_U0, ctx->d_UH,      ctx->d_vc,      ctx->d_red2,    ctx->d_rkF,
+                    ctx->d_stepctr, ctx->d_status, ctx->d_filter, ctx->d_srcamp, ctx->d_srcctr};
     for (void *p : more)
         if (p) cudaFree(p);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -1086,6 +1086,25 @@ template <typename R> static cudaError_t enqueue_load_state(gopf_ctx *ctx, int f
 // the next still y-spectral: the depth-plane kernel then does the inverse y
 // pass of one step together with the x pass and the forward y pass of the
 // next.  Only the last step of a run restores T to its usual form.
+// The point sources of equation eq into its update table (pointers of the current amplitude table).
+static void apply_sources(const gopf_ctx *ctx, UpdTable &u, int eq)
+{
+    u.nsrc = 0;
+    for (size_t k = 0; k < ctx->sources.size(); ++k) {
+        const gopf_ctx::SourceDef &sd = ctx->sources[k];
+        if (sd.eq != eq || u.nsrc >= GOPF_MAX_SRC) continue;
+        for (int d = 0; d < 3; ++d) u.src_pos[u.nsrc][d] = sd.pos[d];
+        u.src_row[u.nsrc] = (int)k;
+        ++u.nsrc;
+    }
+    u.src_amp = ctx->d_srcamp;
+    u.src_stride = (int)ctx->src_len;
+    u.src_ctr = ctx->d_srcctr;
+}
+
+// the sources' step counter advances once per step (after every launch of the step)
+__global__ void k_src_tick(unsigned long long *ctr) { *ctr += 1ull; }
+
 static bool plane_path(const gopf_ctx *ctx)
 {
     return !ctx->multi && ctx->use_plane && ctx->use_fast && ctx->use_tma && ctx->prec == GOPF_FP32 &&
@@ -1111,6 +1130,7 @@ template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx, bool first
     UpdTable u = ctx->upd;
     u.dt = ctx->dt;
     u.invN = 1.0 / (double)ctx->g.N;
+    apply_sources(ctx, u, 0);
     if (el) {
         u.ngrp = GE;
         u.glap[G] = ctx->el_lap;
@@ -1256,6 +1276,7 @@ template <typename R> static cudaError_t enqueue_rk4(gopf_ctx *ctx)
         UpdTable u = ctx->upd;
         u.dt = dt;
         u.invN = 1.0 / (double)ctx->g.N;
+        apply_sources(ctx, u, 0); // RK4 evaluates every stage at the step's start time (pf/rk4.go:101-127)
         u.rk_stage = stage;
         u.rk_afin = afin[stage - 1];
         u.rk_ay = (stage < 4) ? ay[stage - 1] : 0.0;
@@ -1326,6 +1347,7 @@ template <typename R> static cudaError_t enqueue_multi_stage(gopf_ctx *ctx, int 
         u.invN = 1.0 / (double)ctx->g.N;
         u.filt = ctx->upd.filt;
         u.nfilt = ctx->upd.nfilt;
+        apply_sources(ctx, u, e);
         for (int q = 0; q < u.nxf; ++q) u.xf_src[q] = field_state(ctx, ep.xf_field[q]);
         if (stage > 0) {
             const double afin[4] = {dt / 6.0, dt / 3.0, dt / 3.0, dt / 6.0};
@@ -1366,11 +1388,58 @@ template <typename R> static cudaError_t enqueue_steps(gopf_ctx *ctx, int n)
                 for (int s = 1; s <= 4; ++s) LK(enqueue_multi_stage<R>(ctx, s));
             else
                 LK(enqueue_multi_stage<R>(ctx, 0));
-            continue;
+        } else {
+            LK(ctx->stepper == GOPF_STEPPER_RK4 ? enqueue_rk4<R>(ctx) : enqueue_euler<R>(ctx, i == 0, i == n - 1));
         }
-        LK(ctx->stepper == GOPF_STEPPER_RK4 ? enqueue_rk4<R>(ctx) : enqueue_euler<R>(ctx, i == 0, i == n - 1));
+        if (!ctx->sources.empty()) {
+            k_src_tick<<<1, 1, 0, ctx->stream>>>(ctx->d_srcctr);
+            LK(cudaGetLastError());
+        }
     }
     return cudaSuccess;
+}
+
+extern "C" int gopf_add_source(gopf_ctx *ctx, int eq, const double *pos, int npos, int *source_id)
+{
+    if (!ctx || !pos || npos != ctx->ndim) return gopf_fail(ctx, GOPF_ERR_ARG, "a source needs one coordinate per dimension");
+    const int neq = std::max(ctx->nfields, (int)ctx->def.equations.size());
+    if (eq < 0 || (neq > 0 && eq >= neq)) return gopf_fail(ctx, GOPF_ERR_ARG, "bad equation index");
+    int per_eq = 0;
+    for (const gopf_ctx::SourceDef &sd : ctx->sources) per_eq += (sd.eq == eq);
+    if (per_eq >= GOPF_MAX_SRC)
+        return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "at most " + std::to_string(GOPF_MAX_SRC) + " sources per equation");
+    gopf_ctx::SourceDef sd;
+    sd.eq = eq;
+    for (int d = 0; d < 3; ++d) sd.pos[d] = (d < npos) ? pos[d] : 0.0;
+    ctx->sources.push_back(sd);
+    if (source_id) *source_id = (int)ctx->sources.size() - 1;
+    ctx->src_len = 0; // amplitudes must be given again for every source
+    invalidate_graphs(ctx);
+    return GOPF_OK;
+}
+
+extern "C" int gopf_set_source_amplitudes(gopf_ctx *ctx, const double *amps, int nsources, int nsteps)
+{
+    if (!ctx || !amps || nsteps < 1) return gopf_fail(ctx, GOPF_ERR_ARG, "null table or no steps");
+    if (nsources != (int)ctx->sources.size())
+        return gopf_fail(ctx, GOPF_ERR_ARG, "one row of amplitudes per source, in gopf_add_source order");
+    int rc;
+    if ((rc = set_device(ctx))) return rc;
+    const size_t need = (size_t)nsources * (size_t)nsteps;
+    if (need > ctx->srcamp_cap || !ctx->d_srcctr) {
+        if (ctx->d_srcamp) cudaFree(ctx->d_srcamp);
+        ctx->d_srcamp = nullptr;
+        CK(gopf_malloc(&ctx->d_srcamp, sizeof(double) * need));
+        ctx->srcamp_cap = need;
+        if (!ctx->d_srcctr) CK(gopf_malloc(&ctx->d_srcctr, sizeof(unsigned long long)));
+    }
+    CK(cudaStreamSynchronize(ctx->stream)); // steps in flight may still read the old table
+    CK(cudaMemcpy(ctx->d_srcamp, amps, sizeof(double) * need, cudaMemcpyHostToDevice));
+    CK(cudaMemset(ctx->d_srcctr, 0, sizeof(unsigned long long)));
+    ctx->src_base = ctx->step;
+    ctx->src_len = nsteps;
+    invalidate_graphs(ctx); // the table's stride is part of the captured launches
+    return GOPF_OK;
 }
 
 static cudaError_t enqueue_steps_any(gopf_ctx *ctx, int n)
@@ -1661,6 +1730,13 @@ extern "C" int gopf_step(gopf_ctx *ctx, long long nsteps)
         if (ctx->multi)
             for (int f = 1; f < ctx->nfields; ++f)
                 if ((rc = alloc_spectral(ctx, &ctx->d_frkF[f]))) return rc;
+    }
+    if (!ctx->sources.empty()) {
+        if (ctx->stepper == GOPF_STEPPER_SDD || ctx->stepper == GOPF_STEPPER_IMPLICIT_EULER)
+            return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "sources are stepped with Euler and RK4");
+        if (ctx->step < ctx->src_base || ctx->step + nsteps > ctx->src_base + ctx->src_len)
+            return gopf_fail(ctx, GOPF_ERR_STATE,
+                             "source amplitudes do not cover these steps (gopf_set_source_amplitudes)");
     }
     if (ctx->stepper == GOPF_STEPPER_SDD) {
         // a host-driven saddle search (pf/sdd.go): no graphs

@@ -518,6 +518,7 @@ extern "C" int gopf_batch_create(gopf_ctx *const *ctxs, int n, gopf_batch **out)
         if (c->stepper != GOPF_STEPPER_EULER || c->has_elastic || c->has_volcons || c->noise.kind || c->upd.filt || c->upd.nxs)
             return bfail(b, GOPF_ERR_UNSUPPORTED, "batches step Euler models without user-defined terms, noise or filters");
         if (c->multi) return bfail(b, GOPF_ERR_UNSUPPORTED, "batches step single-field models");
+        if (!c->sources.empty()) return bfail(b, GOPF_ERR_UNSUPPORTED, "batches step models without sources");
         b->ctx.push_back(c);
     }
     cudaError_t e = cudaSetDevice(b->device);

@@ -162,6 +162,19 @@ struct gopf_ctx {
     gopf::MonoTable mono{}, mono_rk{};
     int LBm = 4; // x-pass tile width of the multi-field x-pass (nfields + 1 tiles in shared memory)
 
+    // point sources (Model.AddSource, pf/sourceTerm.go): equation and position; the amplitudes
+    // f_s(t) of the steps [src_base, src_base + src_len) in d_srcamp[s * src_len + i], and the
+    // device count of steps taken since src_base (the graphs read it)
+    struct SourceDef {
+        int eq;
+        double pos[3];
+    };
+    std::vector<SourceDef> sources;
+    double *d_srcamp = nullptr;
+    size_t srcamp_cap = 0;
+    unsigned long long *d_srcctr = nullptr;
+    long long src_base = 0, src_len = 0;
+
     // Gaussian noise term (at most one per context) and the device step counter keying it
     gopf::NoiseParams noise{};
     unsigned long long *d_stepctr = nullptr;

@@ -475,6 +475,45 @@ __device__ __forceinline__ void pass_tile(const PassArgs<R> &a, long long tix, i
                     nhat.y += f * sv.y;
                 }
             }
+            if (EXTRA && u.nsrc) {
+                // Source.Eval with the reference's Freq (row, col, depth; +1/2 kept at Nyquist).  The
+                // real field carries the Hermitian part of exp(-2 pi i f.pos): on Nyquist components the
+                // phase factor exp(-i pi pos_j) of k and -k averages to cos(pi sum pos_j)
+                long long kx, yy, zz;
+                if (CONTIG) {
+                    const long long q = l0 + l;
+                    zz = q / g.KX;
+                    kx = q - zz * g.KX;
+                    yy = p;
+                } else {
+                    const long long i = l0 + l;
+                    kx = i / g.Y;
+                    yy = i - kx * g.Y;
+                    zz = p;
+                }
+                const double f[3] = {(double)((2 * yy > g.Y) ? yy - g.Y : yy) / (double)g.Y, (double)kx / (double)g.X,
+                                     (double)((2 * zz > g.Z) ? zz - g.Z : zz) / (double)g.Z};
+                const int dim = (g.Z > 1) ? 3 : 2;
+                const unsigned long long st = *u.src_ctr;
+                for (int sidx = 0; sidx < u.nsrc; ++sidx) {
+                    const double amp = u.src_amp[(long long)u.src_row[sidx] * u.src_stride + (long long)st];
+                    double ph = 0.0, npos = 0.0;
+                    bool nyq = false;
+                    for (int j = 0; j < dim; ++j) {
+                        if (f[j] == 0.5) {
+                            nyq = true;
+                            npos += u.src_pos[sidx][j];
+                        } else {
+                            ph += f[j] * u.src_pos[sidx][j];
+                        }
+                    }
+                    double sn, cs;
+                    sincospi(2.0 * ph, &sn, &cs);
+                    const double fac = nyq ? amp * cospi(npos) : amp;
+                    nhat.x += (R)(fac * cs);
+                    nhat.y -= (R)(fac * sn);
+                }
+            }
             if (EXTRA && u.noise.kind) {
                 long long kx, yy, zz;
                 if (CONTIG) {

@@ -30,6 +30,7 @@ struct LinePlan {
 #define GOPF_MAX_IMP 9
 // multi-field models: fields per model, spectral outputs of one x-pass, monomials per group
 #define GOPF_MAX_FIELDS 4
+#define GOPF_MAX_SRC 4
 #define GOPF_MAX_XOUT 8
 #define GOPF_MAX_MONO 8
 
@@ -147,6 +148,15 @@ struct UpdTable {
     double xf_coef[GOPF_MAX_FIELDS];
     int xf_lap[GOPF_MAX_FIELDS];
     const void *xf_src[GOPF_MAX_FIELDS];
+    // point sources of this equation (pf/sourceTerm.go:25-30): N += f_s(t) exp(-2 pi i Freq . pos_s),
+    // f_s(t) = src_amp[src_row[s] * src_stride + *src_ctr] (the step's entry of a host-supplied
+    // table); generic kernels only
+    int nsrc;
+    int src_row[GOPF_MAX_SRC];
+    double src_pos[GOPF_MAX_SRC][3];
+    const double *src_amp;
+    int src_stride;
+    const unsigned long long *src_ctr;
 };
 
 // Reduction slots written by the x-pass (FP64, compensated per block)

@@ -145,14 +145,14 @@ static bool fast_y(const PassArgs<float> &a)
     if (!a.allow_fast || a.plan.n != 256 || a.g.Y != 256) return false;
     if (a.mode == PM_FWD || a.mode == PM_INV) return true;
     return (a.mode == PM_FUSED || a.mode == PM_INIT) && a.g.Z == 1 && a.nbuf <= 2 && a.upd.rk_stage == 0 &&
-           a.upd.etd == 0 && a.upd.nxs == 0 && a.upd.nxf == 0 && a.upd.nimp <= 4;
+           a.upd.etd == 0 && a.upd.nxs == 0 && a.upd.nxf == 0 && a.upd.nsrc == 0 && a.upd.nimp <= 4;
 }
 
 static bool fast_z(const PassArgs<float> &a)
 {
     return a.allow_fast && a.plan.n == 256 && a.g.Z == 256 && a.g.S % 16 == 0 &&
            (a.mode == PM_FUSED || a.mode == PM_INIT) && a.nbuf <= 2 && a.upd.rk_stage == 0 && a.upd.etd == 0 &&
-           a.upd.nxs == 0 && a.upd.nxf == 0 && a.upd.nimp <= 4;
+           a.upd.nxs == 0 && a.upd.nxf == 0 && a.upd.nsrc == 0 && a.upd.nimp <= 4;
 }
 
 // 256-column x passes that start or end in real space
@@ -242,7 +242,8 @@ static bool fast_y_line(const PassArgs<float> &a)
 {
     const UpdTable &u = a.upd;
     return a.allow_fast && line_len(a.plan.n) && a.g.Y == a.plan.n && a.g.Z == 1 && a.mode == PM_FUSED && a.nbuf <= 2 &&
-           u.rk_stage == 0 && u.etd == 0 && u.nxs == 0 && u.nxf == 0 && u.nimp <= 4 && !u.noise.kind && !u.filt;
+           u.rk_stage == 0 && u.etd == 0 && u.nxs == 0 && u.nxf == 0 && u.nsrc == 0 && u.nimp <= 4 && !u.noise.kind &&
+           !u.filt;
 }
 
 template <typename K> static cudaError_t line_smem(K kern, int bytes)

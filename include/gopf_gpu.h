@@ -27,6 +27,7 @@
  *   Field.Data access (host <-> device)   -> gopf_field_upload / gopf_field_download
  *   mass check pf/solver_test.go:20-27 -> gopf_reduce
  *   PointMonitor pf/monitor.go:8-30       -> gopf_point_values
+ *   Model.AddSource / Source pf/model.go:152-154, pf/sourceTerm.go:14-30 -> gopf_add_source
  */
 #ifndef GOPF_GPU_H
 #define GOPF_GPU_H
@@ -215,6 +216,19 @@ int gopf_save_float64(gopf_ctx *ctx, int field_id, const char *path, int async);
 int gopf_io_wait(gopf_ctx *ctx);
 /* LoadFloat64 (pf/fileIO.go:64-83) followed by gopf_field_upload_real: restart from a saved field. */
 int gopf_load_float64(gopf_ctx *ctx, int field_id, const char *path);
+
+/* ---- point sources (Model.AddSource, pf/model.go:152-154; Source, pf/sourceTerm.go:14-30) ----
+ * A source adds f(t) exp(-2 pi i Freq(k) . pos) to the right-hand side of equation eq (pos: one
+ * coordinate per dimension, in the reference's (row, col, depth) order).  f is a Go closure, so
+ * its values come from the caller: gopf_set_source_amplitudes takes amps[s * nsteps + i] =
+ * f_s(t) for the steps starting at the current one (t = step dt at the start of each step, the
+ * time Euler and RK4 pass to GetRHS), for every source in gopf_add_source order; gopf_step
+ * fails with GOPF_ERR_STATE for steps the table does not cover.  Euler and RK4 (one or several
+ * fields); at most 4 sources per equation.  A real field carries the Hermitian part of the
+ * source: for positions off the grid the Nyquist components contribute cos(pi pos) (the
+ * reference's complex field also carries an imaginary part there). */
+int gopf_add_source(gopf_ctx *ctx, int eq, const double *pos, int npos, int *source_id);
+int gopf_set_source_amplitudes(gopf_ctx *ctx, const double *amps, int nsources, int nsteps);
 
 /* ---- shrinking-dimer dynamics (pf/sdd.go), stepped by gopf_step with GOPF_STEPPER_SDD ----
  * The orientation is nfields * N reals, field after field in node order.  gopf_sdd_init is

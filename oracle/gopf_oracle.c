@@ -371,6 +371,13 @@ typedef struct {
     int nis;
     or_isym is[OR_MAXSPECIAL];
     long current_step;
+    /* point sources (pf/sourceTerm.go): equation, position (row, col, depth), amplitude table
+     * amp[step - amp_base] standing for the Go closure f(t) at t = step dt */
+    int nsrc;
+    int src_eq[OR_MAXSPECIAL];
+    double src_pos[OR_MAXSPECIAL][3];
+    double *src_amp[OR_MAXSPECIAL];
+    long src_len[OR_MAXSPECIAL];
     double *freq; /* 3 * N cached frequencies */
     double *filter; /* modal filter table (ModalFilter.Eval of a Vandeven-style table), NULL = none */
     int nfilter;
@@ -394,6 +401,7 @@ or_model *or_model_create(int ndim, const int *dims, int nfields)
 void or_model_destroy(or_model *m)
 {
     if (!m) return;
+    for (int k = 0; k < m->nsrc; ++k) free(m->src_amp[k]);
     for (int f = 0; f < m->nfields; ++f) free(m->fields[f]);
     for (int d = 0; d < m->nder; ++d) free(m->der[d].data);
     for (int e = 0; e < m->nel; ++e) { free(m->el[e].h); free(m->el[e].disp_override); }
@@ -863,6 +871,31 @@ static void or_get_rhs(or_model *m, int eq, cpx *rhs, cpx *tmp)
         or_term_eval(m, t, tmp);
         for (long i = 0; i < N; ++i) rhs[i] += tmp[i];
     }
+    /* Source.Eval (pf/sourceTerm.go:25-30): f(t) exp(-2 pi i Freq(i) . pos), t = CurrentStep dt */
+    for (int k = 0; k < m->nsrc; ++k) {
+        if (m->src_eq[k] != eq) continue;
+        const long s = m->current_step;
+        const double amp = (s >= 0 && s < m->src_len[k]) ? m->src_amp[k][s] : 0.0;
+        for (long i = 0; i < N; ++i) {
+            const double *f = m->freq + 3 * i;
+            double dot = 0.0;
+            for (int d = 0; d < m->ndim; ++d) dot += f[d] * m->src_pos[k][d];
+            rhs[i] += amp * cexp(-I * 6.283185307179586476925286766559 * dot);
+        }
+    }
+}
+
+/* Model.AddSource(eq, NewSource(pos, f)) with f given as its values at steps 0 .. n - 1 */
+int or_add_source(or_model *m, int eq, const double *pos, const double *amps, long n)
+{
+    if (m->nsrc >= OR_MAXSPECIAL || eq < 0 || eq >= m->nfields || n < 1) return -1;
+    const int k = m->nsrc++;
+    m->src_eq[k] = eq;
+    for (int d = 0; d < 3; ++d) m->src_pos[k][d] = (d < m->ndim) ? pos[d] : 0.0;
+    m->src_amp[k] = (double *)malloc(sizeof(double) * (size_t)n);
+    memcpy(m->src_amp[k], amps, sizeof(double) * (size_t)n);
+    m->src_len[k] = n;
+    return k;
 }
 
 static void or_get_denum(or_model *m, int eq, cpx *den, cpx *tmp)

@@ -99,6 +99,8 @@ def lib():
         L.or_filter_eval.restype = ctypes.c_double
         L.or_set_filter.argtypes = [vp, dp, ctypes.c_int]
         L.or_set_filter.restype = ctypes.c_int
+        L.or_add_source.argtypes = [vp, ctypes.c_int, dp, dp, ctypes.c_long]
+        L.or_add_source.restype = ctypes.c_int
         L.or_sdd_create.argtypes = [vp]
         L.or_sdd_create.restype = vp
         L.or_sdd_destroy.argtypes = [vp]
@@ -286,6 +288,17 @@ class Model:
         """RegisterImplicitTerm with a SpectralViscosity (pf/spectralViscosity.go)."""
         if self._L.or_add_viscosity(self._h, eq, eps, threshold, power, coef, lap) != 0:
             raise ValueError("bad viscosity term")
+
+    def add_source(self, eq: int, pos, amps) -> int:
+        """Model.AddSource(eq, NewSource(pos, f)) (pf/model.go:152-154, pf/sourceTerm.go) with
+        f(step dt) = amps[step]."""
+        p = np.zeros(3)
+        p[: len(pos)] = pos
+        a = np.ascontiguousarray(amps, dtype=np.float64)
+        k = self._L.or_add_source(self._h, eq, _dp(p), _dp(a), a.size)
+        if k < 0:
+            raise ValueError("bad source")
+        return k
 
     def set_filter(self, table) -> None:
         """Euler.SetFilter / RK4.SetFilter with a tabulated filter (None removes it)."""
