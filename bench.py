@@ -305,9 +305,34 @@ def run_e2e(args, m, stream, c0, n, world, dist, torch, G):
         t = torch.tensor([e2e_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
-    return {"value": world * k_e2e / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": 16 * n,
-            "d2h_bytes_per_step": 16 * n, "steps": k_e2e,
+    link = host_link(torch, host, stream)
+    bound = 1.0 / (16 * n / (link["h2d_gbs"] * 1e9) + 16 * n / (link["d2h_gbs"] * 1e9))
+    value = world * k_e2e / (e2e_ms / 1000.0)
+    # the step's own copies alone, at the link's measured rates, allow `bound` steps/s per GPU
+    link.update({"bound_steps_per_s": bound * world, "frac": value / (bound * world)})
+    return {"value": value, "unit": UNIT, "h2d_bytes_per_step": 16 * n,
+            "d2h_bytes_per_step": 16 * n, "steps": k_e2e, "host_link": link,
             "path": "gopf_field_upload ([]complex128, pinned) + gopf_step(1) + gopf_field_download per step"}
+
+
+def host_link(torch, host, stream, reps=5):
+    """Copy-engine bandwidth of the host link for the e2e buffer (pinned host <-> device, one
+    direction at a time), timed with CUDA events on the stepping stream."""
+    dev = torch.empty(host.numel(), dtype=host.dtype, device="cuda")
+    nbytes = host.numel() * host.element_size()
+    out = {}
+    with torch.cuda.stream(stream):
+        for key, dst, src in (("h2d_gbs", dev, host), ("d2h_gbs", host, dev)):
+            dst.copy_(src, non_blocking=True)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                dst.copy_(src, non_blocking=True)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            out[key] = reps * nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9
+    del dev
+    return out
 
 
 def emit(args, m, world, rank, value, per_step_ms, mass0, mass1, finite, prof, dom, hbm, peak_kind, achieved,
