@@ -16,6 +16,7 @@ import numpy as np
 from . import _lib
 from ._lib import (  # noqa: F401
     DER_INDICATOR,
+    DER_MPOLY,
     DER_INDICATOR_D,
     DER_INDICATOR_HD,
     DER_POLY,
@@ -136,6 +137,17 @@ class Model:
         c = (ctypes.c_double * max(n, 1))(*(coefs or [0.0]))
         p = (ctypes.c_int * max(n, 1))(*(powers or [0]))
         self._ck(self._L.gopf_register_function(self._h, name.encode(), kind, field.encode(), c, p, n))
+
+    def register_polynomial(self, name: str, coefs, powers) -> None:
+        """RegisterFunction for a polynomial of several fields: sum_t coefs[t] * prod_f field_f^powers[t][f]
+        (f in AddField order; powers has one row per term and one column per field it covers)."""
+        p = np.ascontiguousarray(powers, dtype=np.int32)
+        if p.ndim != 2 or p.shape[0] != len(coefs):
+            raise ValueError("powers needs one row per coefficient")
+        c = np.ascontiguousarray(coefs, dtype=np.float64)
+        self._ck(self._L.gopf_register_polynomial(self._h, name.encode(), _dptr(c),
+                                                  p.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), p.shape[0],
+                                                  p.shape[1]))
 
     def register_elastic(self, name: str, field: str, C, misfit) -> None:
         c = np.ascontiguousarray(C, dtype=np.float64).reshape(81)
@@ -339,6 +351,12 @@ class Model:
     def reduce(self, field: int, what: int) -> float:
         out = ctypes.c_double()
         self._ck(self._L.gopf_reduce(self._h, field, what, ctypes.byref(out)))
+        return out.value
+
+    def volcons_multiplier(self) -> float:
+        """VolumeConservingLP.Multiplier after the steps taken so far."""
+        out = ctypes.c_double()
+        self._ck(self._L.gopf_volcons_multiplier(self._h, ctypes.byref(out)))
         return out.value
 
     def mass(self, field: int = 0) -> float:

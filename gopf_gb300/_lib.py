@@ -21,7 +21,7 @@ STATUS = {
 }
 GOPF_FP32, GOPF_FP64 = 0, 1
 GOPF_STEPPER_EULER, GOPF_STEPPER_RK4, GOPF_STEPPER_IMPLICIT_EULER, GOPF_STEPPER_SDD = 0, 1, 2, 3
-DER_PRODUCT, DER_POLY, DER_INDICATOR, DER_INDICATOR_D, DER_INDICATOR_HD, DER_WHITE_NOISE = range(6)
+DER_PRODUCT, DER_POLY, DER_INDICATOR, DER_INDICATOR_D, DER_INDICATOR_HD, DER_WHITE_NOISE, DER_MPOLY = range(7)
 NOISE_WHITE, NOISE_CONSERVATIVE = 1, 2
 SRC_NONE, SRC_FIELD, SRC_DERIVED = range(3)
 RED_SUM, RED_SUMSQ, RED_MIN, RED_MAX, RED_NONFINITE = range(5)
@@ -68,8 +68,10 @@ SIGNATURES = {
     "gopf_add_field": ([_vp, _cp, _ip], _i),
     "gopf_add_scalar": ([_vp, _cp, ctypes.c_double, ctypes.c_double], _i),
     "gopf_register_function": ([_vp, _cp, _i, _cp, _dp, _ip, _i], _i),
+    "gopf_register_polynomial": ([_vp, _cp, _dp, _ip, _i, _i], _i),
     "gopf_register_elastic": ([_vp, _cp, _cp, _dp, _dp], _i),
     "gopf_register_volcons": ([_vp, _cp, _cp, _cp, ctypes.c_double], _i),
+    "gopf_volcons_multiplier": ([_vp, _dp], _i),
     "gopf_add_equation": ([_vp, _cp], _i),
     "gopf_register_noise": ([_vp, _cp, _i, _cp, ctypes.c_double, ctypes.c_ulonglong], _i),
     "gopf_init": ([_vp], _i),

@@ -381,11 +381,8 @@ __device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float
     float2 *z = s_a + l * G::LREG;
     line_inv<L>(v, r, ro, z, s_tw);
     // v[i] = c(row 2l, col r + T i) + i c(row 2l + 1, col r + T i)
-    const int ng = a.ngrp_out;
-    for (int grp = 0; grp < ng; ++grp) {
-        float2 w[16];
-#pragma unroll
-        for (int i = 0; i < 16; ++i) w[i] = v[i];
+    // group grp from w: polynomial, forward line transform, separation of the two rows' spectra
+    auto emit = [&](float2(&w)[16], int grp) {
         if (!a.identity) f256::apply_poly(w, a, grp, s_poly + grp * (GOPF_MAX_DEG + 1));
         line_fwd<L>(w, r, ro, z, s_tw);
 #pragma unroll
@@ -401,7 +398,17 @@ __device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float
                     make_float4(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y), 0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
         }
         __syncthreads();
+    };
+    // every group but the last works on a copy; the last one on v itself, so that a single group
+    // (the usual case) does not hold two lines in registers
+    const int ng = a.ngrp_out;
+    for (int grp = 0; grp + 1 < ng; ++grp) {
+        float2 w[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) w[i] = v[i];
+        emit(w, grp);
     }
+    if (ng > 0) emit(v, ng - 1);
 }
 
 template <int L> __device__ __forceinline__ void load_xconsts(const XPassArgs<float> &a, float2 *s_tw, float *s_poly)

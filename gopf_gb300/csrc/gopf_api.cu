@@ -300,8 +300,8 @@ static void ctx_free(gopf_ctx *ctx)
     }
     for (int i = 0; i < GOPF_MAX_XOUT; ++i)
         if (ctx->d_mU[i]) cudaFree(ctx->d_mU[i]);
-    void *more[] = {ctx->d_bsym, ctx->d_U0, ctx->d_UH,      ctx->d_vc,      ctx->d_red2,    ctx->d_rkF,
-                    ctx->d_stepctr, ctx->d_status, ctx->d_filter, ctx->d_srcamp, ctx->d_srcctr};
+    void *more[] = {ctx->d_bsym,    ctx->d_U0,     ctx->d_UH,     ctx->d_vc,     ctx->d_red2,   ctx->d_rkF,
+                    ctx->d_stepctr, ctx->d_status, ctx->d_filter, ctx->d_srcamp, ctx->d_srcctr, ctx->d_vcred};
     for (void *p : more)
         if (p) cudaFree(p);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -441,6 +441,14 @@ static int derived_poly(gopf_ctx *ctx, const gopf_derived &d, std::vector<std::p
             out.push_back({d.coef[j], d.power[j]});
         }
         break;
+    case GOPF_DER_MPOLY:
+        for (int j = 0; j < d.nfac; ++j) {
+            const unsigned packed = (unsigned)d.power[j];
+            if (packed >> 8)
+                return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "derived fields of several fields are not on the device yet");
+            out.push_back({d.coef[j], (int)packed});
+        }
+        break;
     case GOPF_DER_INDICATOR: out = {{3.0, 2}, {-2.0, 3}}; break;
     case GOPF_DER_INDICATOR_D: out = {{6.0, 1}, {-6.0, 2}}; break;
     case GOPF_DER_INDICATOR_HD: out = {{18.0, 3}, {-30.0, 4}, {12.0, 5}}; break;
@@ -489,6 +497,56 @@ static int alloc_spectral(gopf_ctx *ctx, void **p)
     return GOPF_OK;
 }
 
+// Block sums of the volume-conserving term: enough slots for any x-pass grid (tile width >= 4).
+static long long vc_red_blocks(const gopf_ctx *ctx) { return (long long)((ctx->g.Y + 3) / 4) * ctx->g.Z; }
+
+static int alloc_volcons(gopf_ctx *ctx, bool field_sums)
+{
+    const size_t bytes = sizeof(double) * RED_SLOTS * (size_t)vc_red_blocks(ctx);
+    if (!ctx->d_vc) {
+        CK(gopf_malloc(&ctx->d_vc, sizeof(double) * 8));
+        CK(gopf_malloc(&ctx->d_red2, bytes));
+        ctx->dev_bytes += sizeof(double) * 8 + bytes;
+    }
+    if (field_sums && !ctx->d_vcred) {
+        CK(gopf_malloc(&ctx->d_vcred, bytes));
+        ctx->dev_bytes += bytes;
+    }
+    CK(cudaMemset(ctx->d_vc, 0, sizeof(double) * 8));
+    return GOPF_OK;
+}
+
+// HomogeneousModulusLinElast's constants (pf/homoLinElast.go:47-99): the stiffness, the effective
+// stress A = C : misfit (elasticity/rank4.go:62-75) and the misfit energy density e0
+// (elasticity/linearElasticity.go:86-98).
+static void set_elastic_params(gopf_ctx *ctx, const gopf_modeldef::Elastic &e, const gopf_special &sp)
+{
+    memcpy(ctx->el_C, e.C, sizeof(ctx->el_C));
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double a = 0.0;
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) a += e.C[i * 27 + j * 9 + k * 3 + l] * e.misfit[k * 3 + l];
+            ctx->el_A[i * 3 + j] = a;
+        }
+    double e0 = 0.0;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l)
+                    e0 += e.C[i * 27 + j * 9 + k * 3 + l] * e.misfit[i * 3 + j] * e.misfit[k * 3 + l];
+    ctx->el_e0 = 0.5 * e0;
+    ctx->el_coef = sp.coef;
+    ctx->el_lap = sp.lap;
+}
+
+static int find_derived(const gopf_ctx *ctx, const std::string &name)
+{
+    for (size_t i = 0; i < ctx->def.derived_names.size(); ++i)
+        if (ctx->def.derived_names[i] == name) return (int)i;
+    return -1;
+}
+
 // ---- multi-field models ----
 
 
@@ -521,6 +579,20 @@ static int derived_mono(gopf_ctx *ctx, const gopf_derived &d, std::vector<Mono> 
                 return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "polynomial with a negative or too large power");
             Mono m{d.coef[j], {0, 0, 0, 0}};
             m.pw[d.field[j]] = (unsigned char)d.power[j];
+            out.push_back(m);
+        }
+        return GOPF_OK;
+    }
+    if (d.kind == GOPF_DER_MPOLY) {
+        for (int j = 0; j < d.nfac; ++j) {
+            Mono m{d.coef[j], {0, 0, 0, 0}};
+            const unsigned packed = (unsigned)d.power[j];
+            for (int f = 0; f < GOPF_MAX_FIELDS; ++f) {
+                const int p = (int)((packed >> (8 * f)) & 0xffu);
+                if (p && !field_ok(f, p))
+                    return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "polynomial of a field the model does not have");
+                m.pw[f] = (unsigned char)p;
+            }
             out.push_back(m);
         }
         return GOPF_OK;
@@ -627,11 +699,52 @@ static int build_multi_plan(gopf_ctx *ctx, bool kfield, std::vector<gopf_ctx::Eq
             }
         }
     }
+    // The elastic and volume-conserving terms are stepped with Euler only (gopf_step rejects RK4
+    // for them), so only the Euler plan carries them.
+    bool have_el = false, have_vc = false;
     for (const gopf_special &sp : ctx->specials) {
         if (sp.eq < 0 || sp.eq >= nf) return gopf_fail(ctx, GOPF_ERR_ARG, "term refers to an equation that does not exist");
+        if (sp.kind == 1) {
+            if (have_el) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "one elastic term per model");
+            have_el = true;
+            if (!kfield) continue;
+            const gopf_modeldef::Elastic &e = ctx->def.elastic[sp.index];
+            if (e.field < 0 || e.field >= nf) return gopf_fail(ctx, GOPF_ERR_ARG, "bad field index");
+            if (eqs[sp.eq].upd.ngrp >= GOPF_MAX_GROUPS)
+                return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "too many term groups with the elastic term");
+            ctx->el_field = e.field;
+            ctx->el_eq = sp.eq;
+            set_elastic_params(ctx, e, sp);
+            continue;
+        }
+        if (sp.kind == 2) {
+            if (have_vc) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "one volume-conserving term per model");
+            have_vc = true;
+            if (!kfield) continue;
+            const gopf_modeldef::Volcons &v = ctx->def.volcons[sp.index];
+            if (v.field < 0 || v.field >= nf) return gopf_fail(ctx, GOPF_ERR_ARG, "bad field index");
+            const int did = find_derived(ctx, v.indicator);
+            if (did < 0) return gopf_fail(ctx, GOPF_ERR_ARG, "VolumeConservingLP: Indicator is not a derived field");
+            std::vector<Mono> ms;
+            int rc = derived_mono(ctx, ctx->def.derived[did], ms);
+            if (rc) return rc;
+            if ((int)ms.size() > GOPF_MAX_MONO)
+                return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "too many distinct products in one term group");
+            // a group of its own: the update scales it by the device multiplier
+            UpdTable &u = eqs[sp.eq].upd;
+            if (u.ngrp >= GOPF_MAX_GROUPS) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "too many term groups");
+            const int grp = u.ngrp++;
+            u.glap[grp] = sp.lap;
+            gm[sp.eq].emplace_back(ms);
+            ctx->vc_field = v.field;
+            ctx->vc_eq = sp.eq;
+            ctx->vc_local = grp;
+            ctx->vc_dt = v.dt;
+            ctx->vc_coef = sp.coef;
+            continue;
+        }
         if (sp.kind != 4)
-            return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED,
-                             "elastic, volume-conserving and noise terms are stepped in single-field models only");
+            return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "noise terms are stepped in single-field models only");
         const gopf_modeldef::ImplicitSym &is = ctx->def.isym[sp.index];
         UpdTable &u = eqs[sp.eq].upd;
         if (u.nxs >= GOPF_MAX_XSYM) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "too many implicit user terms");
@@ -662,7 +775,26 @@ static int build_multi_plan(gopf_ctx *ctx, bool kfield, std::vector<gopf_ctx::Eq
                 mt.coef[j][m] = gm[e][b][m].coef;
                 memcpy(mt.pw[j][m], gm[e][b][m].pw, GOPF_MAX_FIELDS);
             }
-            eqs[e].ubuf[b] = (b == 0) ? -1 : nextra++;
+            // the first group goes into T of the field, except where the elastic step still
+            // reads that T after the x-pass
+            eqs[e].ubuf[b] = (b == 0 && !(kfield && have_el && e == ctx->el_field)) ? -1 : nextra++;
+        }
+    }
+    if (kfield) {
+        ctx->has_elastic = have_el;
+        ctx->has_volcons = have_vc;
+        ctx->vc_group = have_vc ? eqs[ctx->vc_eq].first + ctx->vc_local : -1;
+        ctx->mono_H = -1;
+        if (have_el) { // H(c) = 3c^2 - 2c^3 of the elastic field, an output of its own (pf/homoLinElast.go:10-12)
+            if (mt.ngrp >= GOPF_MAX_XOUT)
+                return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "too many term groups over all equations");
+            const int j = mt.ngrp++;
+            mt.nmono[j] = 2;
+            mt.coef[j][0] = 3.0;
+            mt.pw[j][0][ctx->el_field] = 2;
+            mt.coef[j][1] = -2.0;
+            mt.pw[j][1][ctx->el_field] = 3;
+            ctx->mono_H = j;
         }
     }
     return GOPF_OK;
@@ -714,9 +846,16 @@ static int compile_multi(gopf_ctx *ctx)
     u0.nfilt = ctx->upd.nfilt;
     ctx->upd = u0;
     ctx->ngroups = mt.ngrp;
-    ctx->has_elastic = ctx->has_volcons = false;
-    ctx->vc_group = -1;
     memset(&ctx->noise, 0, sizeof(ctx->noise));
+    if (ctx->device >= 0 && ctx->has_elastic) {
+        if ((rc = alloc_spectral(ctx, &ctx->d_UH))) return rc;
+        if ((rc = set_device(ctx))) return rc;
+        if ((rc = gopf_elastic_table(ctx))) return rc;
+    }
+    if (ctx->device >= 0 && ctx->has_volcons) {
+        if ((rc = alloc_volcons(ctx, true))) return rc;
+        ctx->eqs[ctx->vc_eq].upd.gscale[ctx->vc_local] = ctx->d_vc + 4;
+    }
     ctx->el_primed = false;
     ctx->initialised = true;
     invalidate_graphs(ctx);
@@ -789,30 +928,13 @@ int gopf_compile_model(gopf_ctx *ctx)
             const gopf_modeldef::Elastic &e = ctx->def.elastic[sp.index];
             if (e.field != 0) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "elastic term must act on field 0");
             ctx->has_elastic = true;
-            memcpy(ctx->el_C, e.C, sizeof(ctx->el_C));
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) {
-                    double a = 0.0;
-                    for (int k = 0; k < 3; ++k)
-                        for (int l = 0; l < 3; ++l) a += e.C[i * 27 + j * 9 + k * 3 + l] * e.misfit[k * 3 + l];
-                    ctx->el_A[i * 3 + j] = a;
-                }
-            double e0 = 0.0;
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j)
-                    for (int k = 0; k < 3; ++k)
-                        for (int l = 0; l < 3; ++l)
-                            e0 += e.C[i * 27 + j * 9 + k * 3 + l] * e.misfit[i * 3 + j] * e.misfit[k * 3 + l];
-            ctx->el_e0 = 0.5 * e0;
-            ctx->el_coef = sp.coef;
-            ctx->el_lap = sp.lap;
+            ctx->el_field = ctx->el_eq = 0;
+            set_elastic_params(ctx, e, sp);
         } else if (sp.kind == 2) {
             if (ctx->has_volcons) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "one volume-conserving term per model");
             const gopf_modeldef::Volcons &v = ctx->def.volcons[sp.index];
             if (v.field != 0) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "volume-conserving term must act on field 0");
-            int did = -1;
-            for (size_t i = 0; i < ctx->def.derived_names.size(); ++i)
-                if (ctx->def.derived_names[i] == v.indicator) did = (int)i;
+            const int did = find_derived(ctx, v.indicator);
             if (did < 0) return gopf_fail(ctx, GOPF_ERR_ARG, "VolumeConservingLP: Indicator is not a derived field");
             std::vector<std::pair<double, int>> poly;
             int rc = derived_poly(ctx, ctx->def.derived[did], poly);
@@ -899,12 +1021,7 @@ int gopf_compile_model(gopf_ctx *ctx)
             if ((rc = gopf_elastic_table(ctx))) return rc;
         }
         if (ctx->has_volcons) {
-            if (!ctx->d_vc) {
-                CK(gopf_malloc(&ctx->d_vc, sizeof(double) * 8));
-                CK(gopf_malloc(&ctx->d_red2, sizeof(double) * RED_SLOTS * ctx->nred_blocks));
-                ctx->dev_bytes += sizeof(double) * (8 + RED_SLOTS * ctx->nred_blocks);
-            }
-            CK(cudaMemset(ctx->d_vc, 0, sizeof(double) * 8));
+            if ((rc = alloc_volcons(ctx, false))) return rc;
             ctx->upd.gscale[ctx->vc_group] = ctx->d_vc + 4;
         }
     }
@@ -1161,7 +1278,7 @@ template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx, bool first
         }
         LK(launch_xpass<R>(xa, ctx->LBx, ctx->stream));
     }
-    if (ctx->has_volcons) LK(gopf_launch_volcons_finalize(ctx));
+    if (ctx->has_volcons) LK(gopf_launch_volcons_finalize(ctx, ctx->d_red, ctx->nred_blocks));
     if (el) {
         if (is3d) {
             PassArgs<R> pa = pargs<R>(ctx, false);
@@ -1320,7 +1437,15 @@ template <typename R> static cudaError_t enqueue_multi_stage(gopf_ctx *ctx, int 
         const int k = eqs[e].ubuf[b];
         return (V *)(k < 0 ? field_T(ctx, e) : ctx->d_mU[k]);
     };
-    if (mono.ngrp > 0) {
+    // the elastic term (pf/homoLinElast.go:47-98) from the second step on: H(c) of its field is
+    // the last x-pass output; before that the term sees the reference's zero field and is left out
+    const bool euler = (stage == 0);
+    const bool el = euler && ctx->has_elastic && ctx->el_primed;
+    const bool vc = euler && ctx->has_volcons;
+    V *UH = (V *)ctx->d_UH;
+    MonoTable xm = mono;
+    if (euler && ctx->has_elastic && !el) xm.ngrp = ctx->mono_H; // H(c) is the last output
+    if (xm.ngrp > 0) {
         XPassArgs<R> xa = xargs<R>(ctx);
         xa.in_mode = XIN_SPECTRAL;
         xa.program = XP_MULTI;
@@ -1328,9 +1453,53 @@ template <typename R> static cudaError_t enqueue_multi_stage(gopf_ctx *ctx, int 
         for (int f = 0; f < nf; ++f) xa.inF[f] = (const V *)field_T(ctx, f);
         for (int e = 0; e < nf; ++e)
             for (int b = 0; b < eqs[e].upd.ngrp; ++b) xa.out[eqs[e].first + b] = gbuf(e, b);
-        xa.ngrp_out = mono.ngrp;
-        xa.mono = mono;
+        if (el) xa.out[ctx->mono_H] = UH;
+        xa.ngrp_out = xm.ngrp;
+        xa.mono = xm;
+        if (vc) { // block sums of the field and of the indicator group (pf/volumeConserving.go:30-50)
+            xa.red = ctx->d_vcred;
+            xa.redfield = ctx->vc_field;
+            xa.red2 = ctx->d_red2;
+            xa.redgrp = ctx->vc_group;
+        }
         LK(launch_xpass<R>(xa, ctx->LBm, ctx->stream));
+    }
+    if (vc) LK(gopf_launch_volcons_finalize(ctx, ctx->d_vcred, ((ctx->g.Y + ctx->LBm - 1) / ctx->LBm) * ctx->g.Z));
+    if (el) {
+        // H-hat -> w = b(k) H-hat / N in real space -> q = s H'(c) (w - 2 e0 H(c)) -> q-hat, as the
+        // single-field step does, with c the elastic field's T from before this step's updates
+        PassArgs<R> pa = pargs<R>(ctx, false);
+        pa.buf[0] = UH;
+        pa.nbuf = 1;
+        if (is3d) {
+            pa.mode = PM_FWD;
+            LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+        }
+        PassArgs<R> ka = pargs<R>(ctx, is3d);
+        ka.mode = PM_ELASTIC_K;
+        ka.buf[0] = UH;
+        ka.nbuf = 1;
+        ka.upd.invN = 1.0 / (double)ctx->g.N;
+        ka.bsym = (const R *)ctx->d_bsym;
+        LK(is3d ? launch_spass<R>(ka, ctx->LBz, ctx->stream) : launch_cpass<R>(ka, ctx->LBy, ctx->stream));
+        if (is3d) {
+            pa.mode = PM_INV;
+            LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+        }
+        XPassArgs<R> xc = xargs<R>(ctx);
+        xc.in_mode = XIN_SPECTRAL;
+        xc.in = (const V *)field_T(ctx, ctx->el_field);
+        xc.program = XP_ELASTIC_Q;
+        xc.in2 = UH;
+        xc.out[0] = UH;
+        xc.ngrp_out = 1;
+        xc.e0 = ctx->el_e0;
+        xc.escale = ctx->el_coef;
+        LK(launch_xpass<R>(xc, ctx->LBx, ctx->stream));
+        if (is3d) {
+            pa.mode = PM_FWD;
+            LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+        }
     }
     for (int e = 0; e < nf; ++e) {
         const gopf_ctx::EqPlan &ep = eqs[e];
@@ -1357,10 +1526,19 @@ template <typename R> static cudaError_t enqueue_multi_stage(gopf_ctx *ctx, int 
             u.rk_ay = (stage < 4) ? ay[stage - 1] : 0.0;
             u.rk_fden = (stage < 4) ? ay[stage - 1] : dt;
         }
-        const int nb = std::max(G, 1);
+        const bool el_here = el && e == ctx->el_eq;
+        if (el_here) { // the elastic term as one more group, already forward transformed
+            u.ngrp = G + 1;
+            u.glap[G] = ctx->el_lap;
+            u.gscale[G] = nullptr;
+        }
+        const int GE = G + (el_here ? 1 : 0);
+        const int nb = std::max(GE, 1);
         PassArgs<R> fa = pargs<R>(ctx, is3d);
         fa.mode = PM_FUSED;
-        for (int b = 0; b < nb; ++b) fa.buf[b] = gbuf(e, b);
+        for (int b = 0; b < G; ++b) fa.buf[b] = gbuf(e, b);
+        if (el_here) fa.buf[G] = UH;
+        if (GE == 0) fa.buf[0] = gbuf(e, 0);
         fa.nbuf = nb;
         fa.state = (V *)field_state(ctx, e);
         fa.tout = (V *)field_T(ctx, e);
@@ -1680,6 +1858,29 @@ __global__ void k_point_values(const typename VecOf<R>::type *__restrict__ T, Ge
     }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) out[w] = acc;
+}
+
+extern "C" int gopf_volcons_multiplier(gopf_ctx *ctx, double *out)
+{
+    if (!ctx || !out) return gopf_fail(ctx, GOPF_ERR_ARG, "null argument");
+    if (!ctx->initialised || !ctx->has_volcons || !ctx->d_vc)
+        return gopf_fail(ctx, GOPF_ERR_STATE, "the model has no volume-conserving term");
+    int rc;
+    if ((rc = set_device(ctx))) return rc;
+    double vc[4];
+    CK(cudaMemcpyAsync(vc, ctx->d_vc, sizeof(vc), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    // The device applies OnStepFinished's update (pf/volumeConserving.go:30-50) at the start of
+    // the next step, where it is first needed; after n >= 2 steps the update of step n is still
+    // pending: lambda - (I_n - I_{n-1}) / (dt * indicator integral of step n).
+    *out = vc[0];
+    if (vc[3] >= 2.0) {
+        double r[5];
+        const int f = ctx->multi ? ctx->vc_field : 0;
+        if ((rc = reduce_all(ctx, r, f))) return rc;
+        *out = vc[0] - (r[GOPF_RED_SUM] - vc[1]) / (ctx->vc_dt * vc[2]);
+    }
+    return GOPF_OK;
 }
 
 extern "C" int gopf_point_values(gopf_ctx *ctx, int field, const long long *sites, int n, double *out)

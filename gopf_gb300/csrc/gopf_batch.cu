@@ -109,10 +109,14 @@ template <int L>
 __global__ void __launch_bounds__(fl::Geo<L>::NT, 3) k_batch_xl(const BatchInst<float> *__restrict__ inst,
                                                                const int2 *__restrict__ items, int nitems)
 {
+    // the instance's arguments in shared memory: read from global memory, the fields the tile
+    // code needs would be held in registers for its whole length (and spill)
+    __shared__ __align__(16) XPassArgs<float> s_a;
     const int2 it = items[blockIdx.x];
-    const XPassArgs<float> &a = inst[it.x].xa;
-    if (a.ngrp_out == 0) return;
-    fl::xline_tile<L>(a, it.y, 0);
+    stage_args(&s_a, &inst[it.x].xa);
+    __syncthreads();
+    if (s_a.ngrp_out == 0) return;
+    fl::xline_tile<L>(s_a, it.y, 0);
 }
 
 template <int L, int NG>

@@ -127,6 +127,8 @@ struct gopf_ctx {
     double el_A[9] = {0};
     double el_e0 = 0.0, el_coef = 1.0;
     int el_lap = 0;
+    int el_field = 0, el_eq = 0; // multi-field models: the field of H(c) and the equation of the term
+    int mono_H = -1;             // multi-field models: index of H(c) in the Euler plan's monomial table
     bool el_primed = false; // false until the first step: the reference's h-field starts at zero
     void *d_bsym = nullptr;
     void *d_U0 = nullptr; // group-0 buffer separate from T (T must survive the elastic step)
@@ -139,6 +141,10 @@ struct gopf_ctx {
     double vc_dt = 0.0, vc_coef = 1.0;
     double *d_vc = nullptr;   // [lambda, current integral, previous indicator integral, count, coef*lambda]
     double *d_red2 = nullptr; // block sums of the indicator
+    // multi-field models: the term's field and equation, the indicator's index in the monomial
+    // table (vc_group), and block sums of the field over the multi-field x-pass grid
+    int vc_field = 0, vc_eq = 0, vc_local = -1;
+    double *d_vcred = nullptr;
 
     void *d_rkF = nullptr; // RK4 accumulator
 
@@ -219,7 +225,9 @@ inline void *field_rkF(gopf_ctx *ctx, int f) { return f == 0 ? ctx->d_rkF : ctx-
 int gopf_fail(gopf_ctx *ctx, int code, const std::string &msg);
 int gopf_compile_model(gopf_ctx *ctx);
 int gopf_elastic_table(gopf_ctx *ctx);
-cudaError_t gopf_launch_volcons_finalize(gopf_ctx *ctx);
+// the multiplier update of VolumeConservingLP from the block sums of the field (red_field) and of
+// the indicator (d_red2) over an x-pass grid of nblocks blocks
+cudaError_t gopf_launch_volcons_finalize(gopf_ctx *ctx, const double *red_field, int nblocks);
 cudaError_t gopf_launch_hermitian_planes(gopf_ctx *ctx, void *state, cudaStream_t st = nullptr);
 
 // NVTX range for the lifetime of a scope (a host-side trace marker; a no-op unless a profiler

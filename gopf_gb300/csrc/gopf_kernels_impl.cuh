@@ -212,7 +212,20 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
         const int tsz = KX * LB;
         V *Bm = A + mt.nin * tsz;
         for (int f = 0; f < mt.nin; ++f) xload_c2r<R, LB, PERB, NCT>(A + f * tsz, a.inF[f], sbase, nl, g, a.planH, twX);
+        if (a.red) { // FP64 block sum of one field's real-space values (the rows of this tile)
+            double vals[RED_SLOTS];
+#pragma unroll
+            for (int s = 0; s < RED_SLOTS; ++s) vals[s] = 0.0;
+            vals[RED_MIN] = INFINITY;
+            vals[RED_MAX] = -INFINITY;
+            const V *F = A + a.redfield * tsz;
+            for (int e = tid; e < H * LB; e += nt)
+                if ((e & (LB - 1)) < nl) vals[RED_SUM] += (double)F[e].x + (double)F[e].y;
+            __shared__ double shredm[32 * RED_SLOTS];
+            block_reduce_store(vals, a.red, shredm);
+        }
         for (int grp = 0; grp < mt.ngrp; ++grp) {
+            double gsum = 0.0;
             for (int e = tid; e < H * LB; e += nt) {
                 R vx = (R)0, vy = (R)0;
                 for (int m = 0; m < mt.nmono[grp]; ++m) {
@@ -228,6 +241,17 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
                     vy += py;
                 }
                 Bm[e] = cmk<V>(vx, vy);
+                if (a.red2 && grp == a.redgrp && (e & (LB - 1)) < nl) gsum += (double)vx + (double)vy;
+            }
+            if (a.red2 && grp == a.redgrp) {
+                double vals[RED_SLOTS];
+#pragma unroll
+                for (int s = 0; s < RED_SLOTS; ++s) vals[s] = 0.0;
+                vals[RED_SUM] = gsum;
+                vals[RED_MIN] = INFINITY;
+                vals[RED_MAX] = -INFINITY;
+                __shared__ double shredm2[32 * RED_SLOTS];
+                block_reduce_store(vals, a.red2, shredm2);
             }
             __syncthreads();
             xr2c_store<R, LB, PERB, NCT>(Bm, a.out[grp], sbase, nl, g, a.planH, twX);

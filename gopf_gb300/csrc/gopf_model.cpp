@@ -543,6 +543,37 @@ extern "C" int gopf_register_function(gopf_ctx *ctx, const char *name, int kind,
     return GOPF_OK;
 }
 
+extern "C" int gopf_register_polynomial(gopf_ctx *ctx, const char *name, const double *coefs, const int *powers,
+                                        int nterms, int nfields)
+{
+    if (!ctx || !name || !*name) return gopf_fail(ctx, GOPF_ERR_ARG, "function name required");
+    if (name_is_reserved(name))
+        return gopf_fail(ctx, GOPF_ERR_ARG, "names may not start with the reserved words -, LAP^4, LAP^2, LAP, *");
+    if (nterms < 1 || nterms > GOPF_MAX_FACTORS || !coefs || !powers)
+        return gopf_fail(ctx, GOPF_ERR_ARG, "polynomial needs 1..8 terms");
+    if (nfields < 1 || nfields > 4 || nfields > (int)ctx->def.fields.size())
+        return gopf_fail(ctx, GOPF_ERR_ARG, "powers must cover 1..4 fields that have been added");
+    gopf_derived dv;
+    memset(&dv, 0, sizeof(dv));
+    dv.kind = GOPF_DER_MPOLY;
+    dv.nfac = nterms;
+    for (int t = 0; t < nterms; ++t) {
+        unsigned packed = 0;
+        for (int f = 0; f < nfields; ++f) {
+            const int p = powers[t * nfields + f];
+            if (p < 0 || p > 64) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "powers are 0..64 on the device");
+            packed |= (unsigned)p << (8 * f);
+        }
+        dv.power[t] = (int)packed;
+        dv.coef[t] = coefs[t];
+        dv.field[t] = -1;
+    }
+    ctx->def.derived.push_back(dv);
+    ctx->def.derived_names.push_back(name);
+    ctx->initialised = false;
+    return GOPF_OK;
+}
+
 extern "C" int gopf_register_elastic(gopf_ctx *ctx, const char *term, const char *field, const double *C81,
                                      const double *misfit9)
 {

@@ -202,9 +202,8 @@ int gopf_elastic_table(gopf_ctx *ctx)
     return GOPF_OK;
 }
 
-cudaError_t gopf_launch_volcons_finalize(gopf_ctx *ctx)
+cudaError_t gopf_launch_volcons_finalize(gopf_ctx *ctx, const double *red_field, int nblocks)
 {
-    k_volcons_finalize<<<1, 32, 0, ctx->stream>>>(ctx->d_red, ctx->d_red2, ctx->nred_blocks, ctx->vc_dt, ctx->vc_coef,
-                                                  ctx->d_vc);
+    k_volcons_finalize<<<1, 32, 0, ctx->stream>>>(red_field, ctx->d_red2, nblocks, ctx->vc_dt, ctx->vc_coef, ctx->d_vc);
     return cudaGetLastError();
 }

@@ -195,6 +195,7 @@ template <typename R> struct XPassArgs {
     // program XP_MULTI: inF[f] = T of field f; out[j] = r2c(mono group j)
     const V *inF[GOPF_MAX_FIELDS];
     MonoTable mono;
+    int redfield; // XP_MULTI with red: the field whose real-space values are summed into red
 };
 
 enum XProgram { XP_POLY = 0, XP_ELASTIC_Q = 1, XP_MULTI = 2 };

@@ -66,7 +66,9 @@ enum {
     GOPF_DER_INDICATOR = 2,   /* 3x^2 - 2x^3 (pf/homoLinElast.go:10-12) */
     GOPF_DER_INDICATOR_D = 3, /* 6x - 6x^2 (pf/homoLinElast.go:15-17) */
     GOPF_DER_INDICATOR_HD = 4, /* Indicator(x) * IndicatorDeriv(x) */
-    GOPF_DER_WHITE_NOISE = 5   /* N(0, 2S) per cell and step (WhiteNoise.Generate, pf/noise.go:20-23) */
+    GOPF_DER_WHITE_NOISE = 5,  /* N(0, 2S) per cell and step (WhiteNoise.Generate, pf/noise.go:20-23) */
+    GOPF_DER_MPOLY = 6         /* sum_t coef_t * prod_f field_f^p_tf, a polynomial of several fields:
+                                  power[t] packs p_tf in bits 8f..8f+7 (fields 0..3), field[] unused */
 };
 
 /* noise kinds for gopf_register_noise */
@@ -149,6 +151,16 @@ int gopf_register_hessian(gopf_ctx *ctx, const char *term_name, const double *K,
 int gopf_register_spectral_viscosity(gopf_ctx *ctx, const char *term_name, double eps, double threshold, int power);
 int gopf_register_volcons(gopf_ctx *ctx, const char *term_name, const char *field, const char *indicator,
                           double dt);
+/* VolumeConservingLP.Multiplier (pf/volumeConserving.go:9) as the device holds it after the steps
+ * taken so far (GOPF_ERR_STATE when the model has no such term). */
+int gopf_volcons_multiplier(gopf_ctx *ctx, double *out);
+/* Model.RegisterFunction for a closure that is a polynomial of several fields (the chemical
+ * potentials of examples/strain_single_precipitate/main.go:36-55, for instance):
+ * value = sum_t coefs[t] * prod_f field_f^powers[t * nfields + f], where field f is the f-th
+ * field added (AddField order), nfields <= the fields added so far (at most 4), 1 <= nterms <= 8
+ * and 0 <= powers <= 64.  Registered as a derived field of kind GOPF_DER_MPOLY. */
+int gopf_register_polynomial(gopf_ctx *ctx, const char *name, const double *coefs, const int *powers, int nterms,
+                             int nfields);
 /* WhiteNoise (pf/noise.go:11-23) registered as a function, or ConservativeNoise
  * (pf/noise.go:25-99) registered as an explicit term, with strength S and a seed for
  * the device's counter-based generator.  The noise is drawn per mode in k space with

@@ -294,7 +294,10 @@ enum {
     OR_DER_POLY = 1,        /* sum_t coef_t * field^p_t (user pointwise function) */
     OR_DER_INDICATOR = 2,   /* 3x^2 - 2x^3            (pf/homoLinElast.go:10-12) */
     OR_DER_INDICATOR_D = 3, /* 6x - 6x^2              (pf/homoLinElast.go:15-17) */
-    OR_DER_INDICATOR_HD = 4 /* Indicator(x)*IndicatorDeriv(x)                   */
+    OR_DER_INDICATOR_HD = 4, /* Indicator(x)*IndicatorDeriv(x)                   */
+    OR_DER_MPOLY = 6         /* sum_t coef_t * prod_f field_f^p_tf, a user pointwise function of
+                                several fields (examples/strain_single_precipitate/main.go:36-55);
+                                power[t] packs p_tf in bits 8f..8f+7                         */
 };
 
 enum { OR_SRC_NONE = 0, OR_SRC_FIELD = 1, OR_SRC_DERIVED = 2 };
@@ -617,6 +620,15 @@ static void or_sync_derived(or_model *m)
                 for (int j = 0; j < D->nfac; ++j) v += D->coef[j] * or_ipow(x, D->power[j]);
                 break;
             }
+            case OR_DER_MPOLY:
+                v = 0.0;
+                for (int j = 0; j < D->nfac; ++j) {
+                    cpx t = D->coef[j];
+                    for (int f = 0; f < m->nfields && f < 4; ++f)
+                        t *= or_ipow(m->fields[f][i], (D->power[j] >> (8 * f)) & 0xff);
+                    v += t;
+                }
+                break;
             case OR_DER_INDICATOR:
                 v = or_indicator(creal(m->fields[D->field[0]][i]));
                 break;

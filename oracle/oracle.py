@@ -23,6 +23,7 @@ _LIB_PATH = os.path.join(_HERE, "libgopf_oracle.so")
 _lib = None
 
 DER_PRODUCT, DER_POLY, DER_INDICATOR, DER_INDICATOR_D, DER_INDICATOR_HD = range(5)
+DER_MPOLY = 6
 SRC_NONE, SRC_FIELD, SRC_DERIVED = range(3)
 
 
@@ -244,6 +245,17 @@ class Model:
         """Derived field sum_t coef_t field^p_t (a pointwise user function)."""
         c = np.asarray(coefs, dtype=np.float64)
         d = self._L.or_add_derived(self._h, DER_POLY, len(powers), _ip([field] * len(powers)), _ip(powers), _dp(c))
+        if d < 0:
+            raise RuntimeError("too many derived fields")
+        return d
+
+    def add_mpoly(self, coefs, powers) -> int:
+        """Derived field sum_t coef_t prod_f field_f^powers[t][f] (a pointwise user function of
+        several fields, e.g. the closures of examples/strain_single_precipitate/main.go:36-55)."""
+        p = np.asarray(powers, dtype=np.int64)
+        packed = [int(sum(int(p[t, f]) << (8 * f) for f in range(p.shape[1]))) for t in range(p.shape[0])]
+        c = np.asarray(coefs, dtype=np.float64)
+        d = self._L.or_add_derived(self._h, DER_MPOLY, len(packed), _ip([0] * len(packed)), _ip(packed), _dp(c))
         if d < 0:
             raise RuntimeError("too many derived fields")
         return d

@@ -251,8 +251,8 @@ def test_concrete_term_and_factor_order_split():
 
 
 def test_multifield_limits():
-    """Several fields compile on the host; what the device does not step in multi-field
-    models (the elastic term, more than four fields) is rejected at init."""
+    """Several fields compile on the host, the elastic term included; what the device does not
+    step in multi-field models (noise terms, more than four fields) is rejected at init."""
     import gopf_gb300 as G
 
     m = _host_model()
@@ -261,8 +261,16 @@ def test_multifield_limits():
     m.register_elastic("LIN_ELAST", "phase", np.zeros((3, 3, 3, 3)), np.eye(3) * 0.01)
     m.add_equation("dconc/dt = LAP conc")
     m.add_equation("dphase/dt = LAP phase + LIN_ELAST")
+    m.init()
+    assert m.summary(1) == (1, 1)
+    mn = _host_model()
+    mn.add_field("conc")
+    mn.add_field("phase")
+    mn.register_noise("NOISE", "conservative", "phase", 1e-3, 1)
+    mn.add_equation("dconc/dt = LAP conc")
+    mn.add_equation("dphase/dt = LAP phase + NOISE")
     with pytest.raises(G.GopfError) as e:
-        m.init()
+        mn.init()
     assert e.value.status == 6
     m5 = _host_model()
     for i in range(5):

@@ -184,6 +184,9 @@ def test_volume_conserving_fp64_parity(oracle, dims):
     g.step(40)
     o.step_euler(dt, 40)
     assert rel_l2(g.download(0).real, o.field(0).real) <= 1e-11
+    lam = o.volcons_multiplier(0)
+    assert lam != 0.0
+    assert abs(g.volcons_multiplier() - lam) <= 1e-9 * max(1.0, abs(lam))
     # volume held near the value after the first step
     g1, o1 = _volcons_models(oracle, dims, c0, dt)
     o1.step_euler(dt, 1)

@@ -368,3 +368,17 @@ def test_elastic_symbol_is_hermitian_part_of_reference_term(dims):
     mine = O.fftn((Hd * (w - 2 * e0 * H)).astype(complex), dims, -1)
     assert np.abs(herm - mine).max() <= 1e-12 * np.abs(ref).max()
     del A
+
+
+def test_oracle_polynomial_of_several_fields(oracle):
+    """A derived field sum_t coef_t prod_f field_f^p_tf (a RegisterFunction closure that is a
+    polynomial of two fields, examples/strain_single_precipitate/main.go:36-50) against numpy."""
+    rng = np.random.default_rng(3)
+    a, b = rng.random(64), rng.random(64)
+    m = oracle.Model([8, 8], 2)
+    m.set_field(0, a)
+    m.set_field(1, b)
+    d = m.add_mpoly([2.0, -1.5, 0.5], [[1, 2], [0, 3], [2, 0]])
+    m.add_term(0, 1.0, src_kind=oracle.SRC_DERIVED, src=d)
+    expect = np.fft.fft2((2.0 * a * b ** 2 - 1.5 * b ** 3 + 0.5 * a ** 2).reshape(8, 8)).ravel()
+    assert np.max(np.abs(m.eval_rhs(0) - expect)) < 1e-12
