@@ -636,6 +636,9 @@ static int build_multi_plan(gopf_ctx *ctx, bool kfield, std::vector<gopf_ctx::Eq
     // per equation: groups keyed by LAP power, each a list of monomials
     std::vector<std::vector<std::vector<Mono>>> gm(nf);
     std::vector<int> maxp(nf, 0);
+    int noise_eq = -1; // the equation with the model's noise term (WhiteNoise / ConservativeNoise)
+    double noise_strength = 0.0;
+    unsigned long long noise_seed = 0;
     for (const gopf_term &t : ctx->terms) {
         if (t.eq < 0 || t.eq >= nf) return gopf_fail(ctx, GOPF_ERR_ARG, "term refers to an equation that does not exist");
         if (t.lap < 0 || t.lap >= GOPF_MAX_IMP) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "LAP power out of range");
@@ -670,6 +673,16 @@ static int build_multi_plan(gopf_ctx *ctx, bool kfield, std::vector<gopf_ctx::Eq
         } else if (t.source == GOPF_SRC_DERIVED) {
             if (t.src_index < 0 || t.src_index >= (int)ctx->der.size())
                 return gopf_fail(ctx, GOPF_ERR_ARG, "bad derived-field index");
+            if (ctx->der[t.src_index].kind == GOPF_DER_WHITE_NOISE) { // drawn in the equation's update
+                if (noise_eq >= 0) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "one noise term per model");
+                noise_eq = t.eq;
+                u.noise.kind = 1;
+                u.noise.coef = t.coef;
+                u.noise.lap = t.lap;
+                noise_strength = ctx->der[t.src_index].coef[0];
+                noise_seed = noise_seed_of(ctx, t.src_index);
+                continue;
+            }
             int rc = derived_mono(ctx, ctx->der[t.src_index], ms);
             if (rc) return rc;
         } else {
@@ -743,8 +756,19 @@ static int build_multi_plan(gopf_ctx *ctx, bool kfield, std::vector<gopf_ctx::Eq
             ctx->vc_coef = sp.coef;
             continue;
         }
-        if (sp.kind != 4)
-            return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "noise terms are stepped in single-field models only");
+        if (sp.kind == 3) {
+            const gopf_modeldef::Noise &nz = ctx->def.noise[sp.index];
+            if (noise_eq >= 0) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "one noise term per model");
+            noise_eq = sp.eq;
+            UpdTable &u = eqs[sp.eq].upd;
+            u.noise.kind = 2;
+            u.noise.coef = sp.coef;
+            u.noise.lap = sp.lap;
+            noise_strength = nz.strength;
+            noise_seed = nz.seed;
+            continue;
+        }
+        if (sp.kind != 4) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "user-defined term kind has no device implementation");
         const gopf_modeldef::ImplicitSym &is = ctx->def.isym[sp.index];
         UpdTable &u = eqs[sp.eq].upd;
         if (u.nxs >= GOPF_MAX_XSYM) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "too many implicit user terms");
@@ -780,7 +804,15 @@ static int build_multi_plan(gopf_ctx *ctx, bool kfield, std::vector<gopf_ctx::Eq
             eqs[e].ubuf[b] = (b == 0 && !(kfield && have_el && e == ctx->el_field)) ? -1 : nextra++;
         }
     }
+    if (noise_eq >= 0) { // the draw's parameters, as in a single-field model; the counter is set at compile
+        NoiseParams &nz = eqs[noise_eq].upd.noise;
+        nz.ndim = ctx->ndim;
+        nz.amp = sqrt((double)ctx->g.N * 2.0 * noise_strength);
+        nz.seed_lo = (uint32_t)(noise_seed & 0xffffffffu);
+        nz.seed_hi = (uint32_t)(noise_seed >> 32);
+    }
     if (kfield) {
+        ctx->noise_eq = noise_eq;
         ctx->has_elastic = have_el;
         ctx->has_volcons = have_vc;
         ctx->vc_group = have_vc ? eqs[ctx->vc_eq].first + ctx->vc_local : -1;
@@ -847,6 +879,19 @@ static int compile_multi(gopf_ctx *ctx)
     ctx->upd = u0;
     ctx->ngroups = mt.ngrp;
     memset(&ctx->noise, 0, sizeof(ctx->noise));
+    if (ctx->noise_eq >= 0) {
+        // the step counter keying the draws advances with field 0's Hermitian projection, once per step
+        if (ctx->device >= 0) {
+            if (!ctx->d_stepctr) {
+                CK(gopf_malloc(&ctx->d_stepctr, sizeof(unsigned long long)));
+                ctx->dev_bytes += sizeof(unsigned long long);
+            }
+            CK(cudaMemset(ctx->d_stepctr, 0, sizeof(unsigned long long)));
+        }
+        for (auto *plan : {&ctx->eqs, &ctx->eqs_rk})
+            (*plan)[ctx->noise_eq].upd.noise.step = ctx->d_stepctr;
+        ctx->noise = ctx->eqs[ctx->noise_eq].upd.noise;
+    }
     if (ctx->device >= 0 && ctx->has_elastic) {
         if ((rc = alloc_spectral(ctx, &ctx->d_UH))) return rc;
         if ((rc = set_device(ctx))) return rc;
@@ -867,6 +912,7 @@ int gopf_compile_model(gopf_ctx *ctx)
     if (ctx->nfields < 1) return gopf_fail(ctx, GOPF_ERR_ARG, "the model has no fields");
     if (ctx->nfields > 1) return compile_multi(ctx);
     ctx->multi = false;
+    ctx->noise_eq = -1;
     PwTable pw;
     memset(&pw, 0, sizeof(pw));
     UpdTable u;
@@ -1949,13 +1995,18 @@ extern "C" int gopf_step(gopf_ctx *ctx, long long nsteps)
         }
         return GOPF_OK;
     }
-    if (ctx->stepper == GOPF_STEPPER_IMPLICIT_EULER && ctx->multi)
-        return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "implicit Euler steps single-field models (multi-field: Euler, RK4)");
     if (ctx->stepper == GOPF_STEPPER_IMPLICIT_EULER) {
         if (ctx->has_elastic || ctx->has_volcons || ctx->noise.kind)
             return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "user-defined and noise terms are stepped with Euler only");
-        if (ctx->ngroups + 1 > GOPF_MAX_GROUPS)
+        if (!ctx->multi && ctx->ngroups + 1 > GOPF_MAX_GROUPS)
             return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "implicit Euler supports at most 3 explicit groups");
+        if (ctx->multi) { // the residual adds FFT(x_f) to each equation's groups and to the x-pass outputs
+            if (ctx->mono_rk.ngrp + ctx->nfields > GOPF_MAX_XOUT)
+                return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "implicit Euler: too many term groups over all equations");
+            for (const auto &ep : ctx->eqs_rk)
+                if (ep.upd.ngrp + 1 > GOPF_MAX_GROUPS)
+                    return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "implicit Euler supports at most 3 explicit groups");
+        }
         // a host-driven Newton-Krylov solve per step: no graphs
         for (long long s = 0; s < nsteps; ++s) {
             if ((rc = gopf_ie_step(ctx))) return rc;
@@ -2010,12 +2061,16 @@ int gopf_field_to_real(gopf_ctx *ctx, int f, void *dst)
 
 int gopf_state_to_real(gopf_ctx *ctx, void *dst) { return gopf_field_to_real(ctx, 0, dst); }
 
+// src = [field 0 | field 1 | ...] (one field for single-field models)
 int gopf_real_to_state(gopf_ctx *ctx, const void *src)
 {
     const size_t rb = (ctx->prec == GOPF_FP32 ? sizeof(float) : sizeof(double)) * ctx->g.N;
-    CK(cudaMemcpyAsync(ctx->d_real, src, rb, cudaMemcpyDeviceToDevice, ctx->stream));
-    cudaError_t e = (ctx->prec == GOPF_FP32) ? enqueue_load_state<float>(ctx) : enqueue_load_state<double>(ctx);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "real to state");
+    const int nf = ctx->multi ? ctx->nfields : 1;
+    for (int f = 0; f < nf; ++f) {
+        CK(cudaMemcpyAsync(ctx->d_real, (const char *)src + f * rb, rb, cudaMemcpyDeviceToDevice, ctx->stream));
+        cudaError_t e = (ctx->prec == GOPF_FP32) ? enqueue_load_state<float>(ctx, f) : enqueue_load_state<double>(ctx, f);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "real to state");
+    }
     ctx->state_valid = true;
     return GOPF_OK;
 }
@@ -2127,6 +2182,138 @@ static cudaError_t enqueue_ie_residual(gopf_ctx *ctx, const R *x, R *F, const vo
     return enqueue_xpass_out<R>(ctx, F, nullptr);
 }
 
+// Models of several fields (ImplicitEuler.Step over m.Fields, pf/implicitEuler.go:68-94, 165-207):
+// the unknown is [field 0 | field 1 | ...] in real space, every right-hand side is evaluated from
+// all fields at once (the RK4 plan: field terms are x-pass products), and grp[j] are spectral
+// scratch buffers, j < (monomial groups) + (fields).  The RHS pass leaves T and the state alone.
+template <typename R> static cudaError_t enqueue_ie_rhs_multi(gopf_ctx *ctx, void *nprev, void *const *grp)
+{
+    typedef typename VecOf<R>::type V;
+    const int nf = ctx->nfields;
+    const bool is3d = ctx->g.Z > 1;
+    const std::vector<gopf_ctx::EqPlan> &eqs = ctx->eqs_rk;
+    const MonoTable &mono = ctx->mono_rk;
+    const long long C = ctx->g.C;
+    if (mono.ngrp > 0) {
+        XPassArgs<R> xa = xargs<R>(ctx);
+        xa.in_mode = XIN_SPECTRAL;
+        xa.program = XP_MULTI;
+        xa.allow_fast = 0;
+        for (int f = 0; f < nf; ++f) xa.inF[f] = (const V *)field_T(ctx, f);
+        for (int j = 0; j < mono.ngrp; ++j) xa.out[j] = (V *)grp[j];
+        xa.ngrp_out = mono.ngrp;
+        xa.mono = mono;
+        LK(launch_xpass<R>(xa, ctx->LBm, ctx->stream));
+    }
+    for (int e = 0; e < nf; ++e) {
+        const int G = eqs[e].upd.ngrp, first = eqs[e].first;
+        if (is3d && G > 0) {
+            PassArgs<R> pa = pargs<R>(ctx, false);
+            pa.mode = PM_FWD;
+            for (int b = 0; b < G; ++b) pa.buf[b] = (V *)grp[first + b];
+            pa.nbuf = G;
+            LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+        }
+        PassArgs<R> fa = pargs<R>(ctx, is3d);
+        fa.mode = PM_FUSED;
+        const int nb = std::max(G, 1);
+        for (int b = 0; b < nb; ++b) fa.buf[b] = (V *)grp[G > 0 ? first + b : mono.ngrp];
+        fa.nbuf = nb;
+        fa.state = (V *)field_state(ctx, e);
+        fa.tout = (V *)grp[mono.ngrp + nf]; // written as zeros
+        fa.upd = eqs[e].upd;
+        fa.upd.dt = ctx->dt;
+        fa.upd.invN = 1.0 / (double)ctx->g.N;
+        fa.upd.etd = 1;
+        fa.upd.filt = nullptr;
+        fa.rkF = (V *)nprev + e * C;
+        LK(is3d ? launch_spass<R>(fa, ctx->LBz, ctx->stream) : launch_cpass<R>(fa, ctx->LBy, ctx->stream));
+    }
+    return cudaSuccess;
+}
+
+// F_f(x) = x_f - IFFT(c_f e^(L dt) + I(L, N_f(x), N_f,n)) / N for every field f; T is work space.
+template <typename R>
+static cudaError_t enqueue_ie_residual_multi(gopf_ctx *ctx, const R *x, R *F, const void *chat0, const void *nprev,
+                                             void *const *grp)
+{
+    typedef typename VecOf<R>::type V;
+    const int nf = ctx->nfields;
+    const bool is3d = ctx->g.Z > 1;
+    const std::vector<gopf_ctx::EqPlan> &eqs = ctx->eqs_rk;
+    const long long C = ctx->g.C, N = ctx->g.N;
+    // the equations' groups, then FFT_x(x_f) of every field (one monomial x_f each)
+    MonoTable mono = ctx->mono_rk;
+    const int G0 = mono.ngrp;
+    for (int f = 0; f < nf; ++f) {
+        const int j = mono.ngrp++;
+        mono.nmono[j] = 1;
+        mono.coef[j][0] = 1.0;
+        memset(mono.pw[j][0], 0, GOPF_MAX_FIELDS);
+        mono.pw[j][0][f] = 1;
+    }
+    XPassArgs<R> xa = xargs<R>(ctx);
+    xa.in_mode = XIN_REAL;
+    xa.program = XP_MULTI;
+    xa.allow_fast = 0;
+    for (int f = 0; f < nf; ++f) xa.rinF[f] = x + f * N;
+    for (int j = 0; j < mono.ngrp; ++j) xa.out[j] = (V *)grp[j];
+    xa.ngrp_out = mono.ngrp;
+    xa.mono = mono;
+    LK(launch_xpass<R>(xa, ctx->LBm, ctx->stream));
+    for (int e = 0; e < nf; ++e) {
+        const int G = eqs[e].upd.ngrp, first = eqs[e].first;
+        V *buf[GOPF_MAX_GROUPS];
+        for (int b = 0; b < G; ++b) buf[b] = (V *)grp[first + b];
+        buf[G] = (V *)grp[G0 + e]; // FFT(x_e)
+        if (is3d) {
+            PassArgs<R> pa = pargs<R>(ctx, false);
+            pa.mode = PM_FWD;
+            for (int b = 0; b <= G; ++b) pa.buf[b] = buf[b];
+            pa.nbuf = G + 1;
+            LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+        }
+        PassArgs<R> fa = pargs<R>(ctx, is3d);
+        fa.mode = PM_FUSED;
+        for (int b = 0; b <= G; ++b) fa.buf[b] = buf[b];
+        fa.nbuf = G + 1;
+        fa.state = (V *)const_cast<void *>(chat0) + e * C;
+        fa.tout = (V *)field_T(ctx, e);
+        fa.upd = eqs[e].upd;
+        fa.upd.dt = ctx->dt;
+        fa.upd.invN = 1.0 / (double)N;
+        fa.upd.etd = 2;
+        fa.upd.filt = nullptr;
+        fa.rkF = (V *)const_cast<void *>(nprev) + e * C;
+        LK(is3d ? launch_spass<R>(fa, ctx->LBz, ctx->stream) : launch_cpass<R>(fa, ctx->LBy, ctx->stream));
+    }
+    if (is3d) {
+        PassArgs<R> ia = pargs<R>(ctx, false);
+        ia.mode = PM_INV;
+        for (int f = 0; f < nf; ++f) ia.buf[f] = (V *)field_T(ctx, f);
+        ia.nbuf = nf;
+        LK(launch_cpass<R>(ia, ctx->LBy, ctx->stream));
+    }
+    for (int f = 0; f < nf; ++f) LK(enqueue_xpass_out<R>(ctx, F + f * N, nullptr, f));
+    return cudaSuccess;
+}
+
+int gopf_ie_rhs_multi(gopf_ctx *ctx, void *nprev, void *const *grp)
+{
+    cudaError_t e = (ctx->prec == GOPF_FP32) ? enqueue_ie_rhs_multi<float>(ctx, nprev, grp)
+                                             : enqueue_ie_rhs_multi<double>(ctx, nprev, grp);
+    return (e == cudaSuccess) ? GOPF_OK : cuda_fail(ctx, e, "implicit Euler: RHS");
+}
+
+int gopf_ie_residual_multi(gopf_ctx *ctx, const void *x, void *F, const void *chat0, const void *nprev,
+                           void *const *grp)
+{
+    cudaError_t e = (ctx->prec == GOPF_FP32)
+                        ? enqueue_ie_residual_multi<float>(ctx, (const float *)x, (float *)F, chat0, nprev, grp)
+                        : enqueue_ie_residual_multi<double>(ctx, (const double *)x, (double *)F, chat0, nprev, grp);
+    return (e == cudaSuccess) ? GOPF_OK : cuda_fail(ctx, e, "implicit Euler: residual");
+}
+
 int gopf_ie_rhs(gopf_ctx *ctx, void *nprev, void *tmp0)
 {
     cudaError_t e = (ctx->prec == GOPF_FP32) ? enqueue_ie_rhs<float>(ctx, nprev, tmp0)
@@ -2143,12 +2330,17 @@ int gopf_ie_residual(gopf_ctx *ctx, const void *x, void *F, const void *chat0, c
 }
 
 // One explicit Euler step of the state (the Newton start, pf/implicitEuler.go:182-190); x0 <- real field.
+// (several fields: Euler.Step's in-place sweep over the fields, then x0 = [field 0 | field 1 | ...])
 int gopf_ie_euler_guess(gopf_ctx *ctx, void *x0)
 {
-    cudaError_t e = (ctx->prec == GOPF_FP32) ? enqueue_euler<float>(ctx) : enqueue_euler<double>(ctx);
-    if (e == cudaSuccess)
-        e = (ctx->prec == GOPF_FP32) ? enqueue_xpass_out<float>(ctx, (float *)x0, nullptr)
-                                     : enqueue_xpass_out<double>(ctx, (double *)x0, nullptr);
+    const bool f32 = (ctx->prec == GOPF_FP32);
+    cudaError_t e;
+    if (ctx->multi) e = f32 ? enqueue_multi_stage<float>(ctx, 0) : enqueue_multi_stage<double>(ctx, 0);
+    else e = f32 ? enqueue_euler<float>(ctx) : enqueue_euler<double>(ctx);
+    const int nf = ctx->multi ? ctx->nfields : 1;
+    for (int f = 0; f < nf && e == cudaSuccess; ++f)
+        e = f32 ? enqueue_xpass_out<float>(ctx, (float *)x0 + f * ctx->g.N, nullptr, f)
+                : enqueue_xpass_out<double>(ctx, (double *)x0 + f * ctx->g.N, nullptr, f);
     return (e == cudaSuccess) ? GOPF_OK : cuda_fail(ctx, e, "implicit Euler: explicit guess");
 }
 

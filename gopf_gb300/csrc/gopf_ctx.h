@@ -183,6 +183,7 @@ struct gopf_ctx {
 
     // Gaussian noise term (at most one per context) and the device step counter keying it
     gopf::NoiseParams noise{};
+    int noise_eq = -1; // multi-field models: the equation drawing the noise (-1: none)
     unsigned long long *d_stepctr = nullptr;
     void *d_filter = nullptr; // modal filter table (precision of the context)
     unsigned *d_status = nullptr; // device status word of the bounded waits (0 = clean)

@@ -32,6 +32,9 @@ int gopf_fail(gopf_ctx *ctx, int code, const std::string &msg);
 int gopf_ie_rhs(gopf_ctx *ctx, void *nprev, void *tmp0);
 int gopf_ie_residual(gopf_ctx *ctx, const void *x, void *F, const void *chat0, const void *nprev, void *tmp0);
 int gopf_ie_euler_guess(gopf_ctx *ctx, void *x0);
+int gopf_ie_rhs_multi(gopf_ctx *ctx, void *nprev, void *const *grp);
+int gopf_ie_residual_multi(gopf_ctx *ctx, const void *x, void *F, const void *chat0, const void *nprev,
+                           void *const *grp);
 int gopf_real_to_state(gopf_ctx *ctx, const void *src);
 
 namespace {
@@ -145,7 +148,9 @@ struct gopf_ie_work {
     void *x = nullptr, *F = nullptr, *xp = nullptr, *Fp = nullptr, *w = nullptr;
     std::vector<void *> V;
     void **d_V = nullptr;
-    void *chat0 = nullptr, *nprev = nullptr, *tmp0 = nullptr;
+    void *chat0 = nullptr, *nprev = nullptr, *tmp0 = nullptr; // chat0, nprev: one spectrum per field
+    int nfields = 1;
+    std::vector<void *> grp; // several fields: spectral scratch of the x-pass outputs
     double *d_part = nullptr, *d_out = nullptr, *d_coef = nullptr;
     double *h_out = nullptr; // pinned
 };
@@ -159,6 +164,8 @@ void gopf_ie_free(gopf_ctx *ctx)
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : ws->V)
+        if (p) cudaFree(p);
+    for (void *p : ws->grp)
         if (p) cudaFree(p);
     if (ws->h_out) cudaFreeHost(ws->h_out);
     delete ws;
@@ -177,12 +184,16 @@ namespace {
 int ie_alloc(gopf_ctx *ctx)
 {
     const int restart = ctx->nk_restart;
-    if (ctx->ie && ctx->ie->restart == restart) return GOPF_OK;
+    const int nf = ctx->multi ? ctx->nfields : 1;
+    const int ngrp = ctx->multi ? ctx->mono_rk.ngrp + nf + 1 : 0;
+    if (ctx->ie && ctx->ie->restart == restart && ctx->ie->nfields == nf && (int)ctx->ie->grp.size() == ngrp)
+        return GOPF_OK;
     gopf_ie_free(ctx);
     gopf_ie_work *ws = new gopf_ie_work();
     ctx->ie = ws;
     ws->prec = ctx->prec;
-    ws->n = ctx->g.N;
+    ws->nfields = nf;
+    ws->n = ctx->g.N * nf; // [field 0 | field 1 | ...] (fields2vec, pf/implicitEuler.go:44-66)
     ws->restart = restart;
     ws->rb = (size_t)ws->n * (ctx->prec == GOPF_FP32 ? sizeof(float) : sizeof(double));
     const size_t cb = (size_t)ctx->g.C * (ctx->prec == GOPF_FP32 ? sizeof(float2) : sizeof(double2));
@@ -192,9 +203,12 @@ int ie_alloc(gopf_ctx *ctx)
     for (auto &p : ws->V) IE_CK(gopf_malloc(&p, ws->rb));
     IE_CK(gopf_malloc(&ws->d_V, sizeof(void *) * (restart + 1)));
     IE_CK(cudaMemcpy(ws->d_V, ws->V.data(), sizeof(void *) * (restart + 1), cudaMemcpyHostToDevice));
-    IE_CK(gopf_malloc(&ws->chat0, cb));
-    IE_CK(gopf_malloc(&ws->nprev, cb));
+    IE_CK(gopf_malloc(&ws->chat0, cb * nf));
+    IE_CK(gopf_malloc(&ws->nprev, cb * nf));
     IE_CK(gopf_malloc(&ws->tmp0, cb));
+    ws->grp.assign(ngrp, nullptr);
+    for (auto &p : ws->grp) IE_CK(gopf_malloc(&p, cb));
+    ctx->dev_bytes += cb * (2 * (nf - 1) + ngrp);
     IE_CK(gopf_malloc(&ws->d_part, sizeof(double) * kBlocks * (restart + 2)));
     IE_CK(gopf_malloc(&ws->d_out, sizeof(double) * (restart + 2)));
     IE_CK(gopf_malloc(&ws->d_coef, sizeof(double) * (restart + 2)));
@@ -288,7 +302,7 @@ int stencil_weights(int pts, double *w)
 
 } // namespace
 
-// One ImplicitEuler step of the context's single field.
+// One ImplicitEuler step of the context's fields (one Newton-Krylov solve over all of them).
 int gopf_ie_step(gopf_ctx *ctx)
 {
     gopf_nvtx_scope trace("implicit_euler_step");
@@ -303,12 +317,18 @@ int gopf_ie_step(gopf_ctx *ctx)
     if (nw == 0) return gopf_fail(ctx, GOPF_ERR_ARG, "finite-difference stencil must have 2, 4, 6 or 8 points");
 
     // N_n, c_n, and the explicit Euler start
-    if ((rc = gopf_ie_rhs(ctx, ws->nprev, ws->tmp0))) return rc;
+    const bool multi = ctx->multi;
+    if ((rc = multi ? gopf_ie_rhs_multi(ctx, ws->nprev, ws->grp.data()) : gopf_ie_rhs(ctx, ws->nprev, ws->tmp0)))
+        return rc;
     const size_t cb = (size_t)ctx->g.C * (ctx->prec == GOPF_FP32 ? sizeof(float2) : sizeof(double2));
-    IE_CK(cudaMemcpyAsync(ws->chat0, ctx->d_state, cb, cudaMemcpyDeviceToDevice, st));
+    for (int f = 0; f < ws->nfields; ++f)
+        IE_CK(cudaMemcpyAsync((char *)ws->chat0 + f * cb, field_state(ctx, f), cb, cudaMemcpyDeviceToDevice, st));
     if ((rc = gopf_ie_euler_guess(ctx, ws->x))) return rc;
 
-    auto Feval = [&](const void *x, void *F) { return gopf_ie_residual(ctx, x, F, ws->chat0, ws->nprev, ws->tmp0); };
+    auto Feval = [&](const void *x, void *F) {
+        return multi ? gopf_ie_residual_multi(ctx, x, F, ws->chat0, ws->nprev, ws->grp.data())
+                     : gopf_ie_residual(ctx, x, F, ws->chat0, ws->nprev, ws->tmp0);
+    };
 
     double fl2 = 0.0, finf = 0.0, xl2 = 0.0, xinf = 0.0;
     if ((rc = Feval(ws->x, ws->F))) return rc;

@@ -211,7 +211,20 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
         const MonoTable &mt = a.mono;
         const int tsz = KX * LB;
         V *Bm = A + mt.nin * tsz;
-        for (int f = 0; f < mt.nin; ++f) xload_c2r<R, LB, PERB, NCT>(A + f * tsz, a.inF[f], sbase, nl, g, a.planH, twX);
+        if (a.in_mode == XIN_SPECTRAL) {
+            for (int f = 0; f < mt.nin; ++f)
+                xload_c2r<R, LB, PERB, NCT>(A + f * tsz, a.inF[f], sbase, nl, g, a.planH, twX);
+        } else { // real rows of every field (rinF[f]), as pairs A[m*LB + l] = (c[2m], c[2m+1])
+            for (int f = 0; f < mt.nin; ++f) {
+                const V *rin2 = reinterpret_cast<const V *>(a.rinF[f]) + ((long long)z * Y + y0) * H;
+                for (int e = tid; e < LB * H; e += nt) {
+                    const int l = e / H, m = e - l * H;
+                    ga_copy(&A[f * tsz + m * LB + l], rin2 + (long long)(l < nl ? l : 0) * H + m, l < nl);
+                }
+            }
+            ga_wait();
+            __syncthreads();
+        }
         if (a.red) { // FP64 block sum of one field's real-space values (the rows of this tile)
             double vals[RED_SLOTS];
 #pragma unroll

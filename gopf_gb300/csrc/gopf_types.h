@@ -196,6 +196,7 @@ template <typename R> struct XPassArgs {
     const V *inF[GOPF_MAX_FIELDS];
     MonoTable mono;
     int redfield; // XP_MULTI with red: the field whose real-space values are summed into red
+    const R *rinF[GOPF_MAX_FIELDS]; // XP_MULTI with XIN_REAL: the real rows of field f
 };
 
 enum XProgram { XP_POLY = 0, XP_ELASTIC_Q = 1, XP_MULTI = 2 };

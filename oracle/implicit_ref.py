@@ -17,45 +17,61 @@ import numpy as np
 
 
 def residual_fn(model, dims, dt: float):
-    """F for the model's current field (which becomes c_n); model's field is left at c_n."""
+    """F over x = [field 0 | field 1 | ...] for the model's current fields (which become c_n): every
+    equation's right-hand side is evaluated from all fields of x (updateEquation, :68-94).  The
+    model's fields are left at c_n."""
     from oracle import oracle as O
 
-    c = model.field(0).real.copy()
-    n = c.size
-    chat = O.fftn(c.astype(np.complex128), dims)
-    nprev = model.eval_rhs(0)
-    L = model.eval_denum(0)
-    f = np.exp(L * dt)
-    small = np.abs(L) < 1e-5
-    Ls = np.where(small, 1.0, L)
-    c1 = (f - 1.0) / Ls
-    c2 = (f - L * dt - 1.0) / (Ls * Ls)
+    nf = model.nfields
+    cs = [model.field(f).real.copy() for f in range(nf)]
+    n = cs[0].size
+    chats = [O.fftn(c.astype(np.complex128), dims) for c in cs]
+    nprevs = [model.eval_rhs(e) for e in range(nf)]
+    parts = []
+    for e in range(nf):
+        L = model.eval_denum(e)
+        f = np.exp(L * dt)
+        small = np.abs(L) < 1e-5
+        Ls = np.where(small, 1.0, L)
+        parts.append((f, small, (f - 1.0) / Ls, (f - L * dt - 1.0) / (Ls * Ls)))
 
     def F(x):
-        model.set_field(0, np.asarray(x, dtype=np.float64))
-        nx = model.eval_rhs(0)
-        integral = np.where(small, 0.5 * dt * (nx + nprev * f), nprev * c1 + (nx - nprev) / dt * c2)
-        upd = chat * f + integral
-        r = O.fftn(np.asarray(x, dtype=np.complex128), dims) - upd
-        out = O.fftn(r, dims, sign=1).real / n
-        model.set_field(0, c)
-        return out
+        xs = np.asarray(x, dtype=np.float64).reshape(nf, n)
+        for fi in range(nf):
+            model.set_field(fi, xs[fi])
+        out = []
+        for e in range(nf):
+            f, small, c1, c2 = parts[e]
+            nx = model.eval_rhs(e)
+            nprev = nprevs[e]
+            integral = np.where(small, 0.5 * dt * (nx + nprev * f), nprev * c1 + (nx - nprev) / dt * c2)
+            upd = chats[e] * f + integral
+            r = O.fftn(xs[e].astype(np.complex128), dims) - upd
+            out.append(O.fftn(r, dims, sign=1).real / n)
+        for fi in range(nf):
+            model.set_field(fi, cs[fi])
+        return np.concatenate(out)
 
-    return F, c
+    return F, cs[0] if nf == 1 else cs
 
 
 def implicit_euler_step(model, dims, dt: float, tol: float = 1e-12) -> dict:
-    """One ImplicitEuler step of a single-field oracle model, in place.  Returns solver info."""
+    """One ImplicitEuler step of an oracle model (all its fields), in place.  Returns solver info."""
     from scipy.optimize import newton_krylov
 
-    F, c = residual_fn(model, dims, dt)
+    nf = model.nfields
+    F, _ = residual_fn(model, dims, dt)
+    cs = [model.field(f).real.copy() for f in range(nf)]
     model.step_euler(dt, 1, hooks=False)
-    x0 = model.field(0).real.copy()
-    model.set_field(0, c)
+    x0 = np.concatenate([model.field(f).real.copy() for f in range(nf)])
+    for f in range(nf):
+        model.set_field(f, cs[f])
     if np.max(np.abs(F(x0))) <= tol:
         x = x0
     else:
         x = newton_krylov(F, x0, method="gmres", f_tol=tol, maxiter=100)
     res = float(np.max(np.abs(F(x))))
-    model.set_field(0, x)
+    xs = np.asarray(x).reshape(nf, -1)
+    for f in range(nf):
+        model.set_field(f, xs[f])
     return {"residual": res}

@@ -251,8 +251,9 @@ def test_concrete_term_and_factor_order_split():
 
 
 def test_multifield_limits():
-    """Several fields compile on the host, the elastic term included; what the device does not
-    step in multi-field models (noise terms, more than four fields) is rejected at init."""
+    """Several fields compile on the host, the elastic and noise terms included; what the device
+    does not step in multi-field models (two noise terms, more than four fields) is rejected at
+    init."""
     import gopf_gb300 as G
 
     m = _host_model()
@@ -267,7 +268,8 @@ def test_multifield_limits():
     mn.add_field("conc")
     mn.add_field("phase")
     mn.register_noise("NOISE", "conservative", "phase", 1e-3, 1)
-    mn.add_equation("dconc/dt = LAP conc")
+    mn.register_noise("NOISE2", "conservative", "conc", 1e-3, 2)
+    mn.add_equation("dconc/dt = LAP conc + NOISE2")
     mn.add_equation("dphase/dt = LAP phase + NOISE")
     with pytest.raises(G.GopfError) as e:
         mn.init()

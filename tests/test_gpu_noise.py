@@ -96,3 +96,38 @@ def test_noise_with_cahn_hilliard_stays_finite():
     d = m.download_real(0)
     assert np.all(np.isfinite(d))
     assert abs(d.sum() - c0.sum()) / d.size < 1e-6
+
+
+@pytest.mark.parametrize("kind", ["white", "conservative"])
+def test_noise_in_a_model_of_two_fields(kind):
+    """A noise term in the second equation of a two-field model draws exactly what the same term
+    draws in a model of its own (the draws are keyed by seed, step and mode); the other field
+    steps as without noise."""
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+
+    dims, dt, n = [64, 64], 0.1, 64 * 64
+    a0 = uniform_field(3, n, 0.2, 0.1)
+    two = G.Model(dims, "fp64", device=0)
+    two.add_field("a")
+    two.add_field("b")
+    two.add_scalar("m1", -1.0)
+    two.register_noise("NOISE", kind, "b", 0.5, 11)
+    two.add_equation("da/dt = m1*a")
+    two.add_equation("db/dt = NOISE")
+    two.init()
+    two.set_stepper("euler", dt)
+    two.upload(0, a0)
+    two.upload(1, np.zeros(n))
+    one = G.Model(dims, "fp64", device=0)
+    one.add_field("b")
+    one.register_noise("NOISE", kind, "b", 0.5, 11)
+    one.add_equation("db/dt = NOISE")
+    one.init()
+    one.set_stepper("euler", dt)
+    one.upload(0, np.zeros(n))
+    for m in (two, one):
+        m.step(7)
+    assert np.array_equal(two.download(1), one.download(0))
+    assert np.std(one.download_real(0)) > 0.0
+    np.testing.assert_allclose(two.download_real(0), a0 / (1.0 + dt) ** 7, rtol=1e-12, atol=1e-14)

@@ -2,8 +2,9 @@
 and the device Newton-Krylov solve against the oracle and the same analytic tests.
 
 TestImplicitEuler (pf/implicitEuler_test.go:10-108): 8x8 fields, dt = 0.01, 100 steps, tolerance 5e-3
-against the ODE solutions (the two-field case is out of the device's single-field scope and is run
-on the oracle only).  TestDissipatingHeatEquation (:160-223): 128^2, dt = 0.005, 10 steps, 1e-3.
+against the ODE solutions, the two coupled fields included.  TestDissipatingHeatEquation (:160-223):
+128^2, dt = 0.005, 10 steps, 1e-3.  Device against oracle (FP64, both solved to max|F| <= 1e-12):
+rel-L2 <= 1e-9.
 """
 import math
 
@@ -166,3 +167,99 @@ def test_device_implicit_cahn_hilliard_matches_oracle(oracle, dims):
         implicit_euler_step(o, dims, dt, tol=1e-12)
     ref = o.field(0).real
     assert np.linalg.norm(g.download_real(0) - ref) / np.linalg.norm(ref) <= 1e-9
+
+
+def test_oracle_implicit_euler_coupled_fields_restatement(oracle):
+    """The two-field case of TestImplicitEuler through the oracle's ImplicitEuler restatement (one
+    Newton-Krylov solve over both fields per step)."""
+    from oracle.implicit_ref import implicit_euler_step
+
+    m = oracle.Model([8, 8], 2)
+    m.set_field(0, np.ones(64))
+    m.set_field(1, np.ones(64))
+    m.add_term(0, -1.0, src_kind=oracle.SRC_DERIVED, src=m.add_product([0, 1], [1, 1]))
+    m.add_term(1, -1.0, implicit=True)
+    for _ in range(100):
+        implicit_euler_step(m, [8, 8], 0.01)
+    assert np.max(np.abs(m.field(0).real - math.exp(math.exp(-1.0) - 1.0))) < 5e-3
+    assert np.max(np.abs(m.field(1).real - math.exp(-1.0))) < 5e-3
+
+
+def gpu_coupled(prec, n=8):
+    import gopf_gb300 as G
+
+    m = G.Model([n, n], prec, device=0)
+    m.add_field("conc1")
+    m.add_field("conc2")
+    m.add_equation("dconc1/dt = -conc1*conc2")
+    m.add_equation("dconc2/dt = -conc2")
+    m.init()
+    m.set_stepper("implicit_euler", 0.01)
+    m.upload(0, np.ones(n * n))
+    m.upload(1, np.ones(n * n))
+    return m
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_device_implicit_euler_coupled_fields(oracle, prec):
+    """The two-field case of TestImplicitEuler on the device: the ODE solutions within 5e-3, and in
+    FP64 the oracle's restatement within 1e-9."""
+    from oracle.implicit_ref import implicit_euler_step
+
+    m = gpu_coupled(prec)
+    m.step(100)
+    _, _, _, conv = m.newton_stats()
+    assert conv
+    assert np.max(np.abs(m.download_real(0) - math.exp(math.exp(-1.0) - 1.0))) < 5e-3
+    assert np.max(np.abs(m.download_real(1) - math.exp(-1.0))) < 5e-3
+    if prec == "fp64":
+        o = oracle.Model([8, 8], 2)
+        o.set_field(0, np.ones(64))
+        o.set_field(1, np.ones(64))
+        o.add_term(0, -1.0, src_kind=oracle.SRC_DERIVED, src=o.add_product([0, 1], [1, 1]))
+        o.add_term(1, -1.0, implicit=True)
+        for _ in range(100):
+            implicit_euler_step(o, [8, 8], 0.01, tol=1e-12)
+        for f in range(2):
+            assert np.max(np.abs(m.download_real(f) - o.field(f).real)) < 1e-9
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dims", [[32, 32], [16, 16, 16]])
+def test_device_implicit_two_fields_matches_oracle(oracle, dims):
+    """Two spatially varying coupled fields, da/dt = LAP a - a b, db/dt = -b + a^2 (ImplicitEuler,
+    FP64): the device and the oracle reach the same root every step (both to max|F| <= 1e-12)."""
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+    from oracle.implicit_ref import implicit_euler_step
+
+    n = int(np.prod(dims))
+    a0, b0 = uniform_field(41, n, 0.3, 0.1), uniform_field(42, n, 0.2, 0.1)
+    dt = 0.05
+    g = G.Model(dims, "fp64", device=0)
+    g.add_field("a")
+    g.add_field("b")
+    g.add_scalar("m1", -1.0)
+    g.add_equation("da/dt = LAP a - a*b")
+    g.add_equation("db/dt = m1*b + a^2")
+    g.init()
+    g.set_stepper("implicit_euler", dt)
+    g.set_newton_krylov(tol=1e-12)
+    g.upload(0, a0)
+    g.upload(1, b0)
+    o = oracle.Model(dims, 2)
+    o.set_field(0, a0)
+    o.set_field(1, b0)
+    o.add_term(0, 1.0, lap=1, implicit=True)
+    o.add_term(0, -1.0, src_kind=oracle.SRC_DERIVED, src=o.add_product([0, 1], [1, 1]))
+    o.add_term(1, -1.0, implicit=True)
+    o.add_term(1, 1.0, src_kind=oracle.SRC_DERIVED, src=o.add_product([0], [2]))
+    for _ in range(3):
+        g.step(1)
+        _, _, res, conv = g.newton_stats()
+        assert conv and res <= 1e-12
+        implicit_euler_step(o, dims, dt, tol=1e-12)
+    for f in range(2):
+        ref = o.field(f).real
+        assert np.linalg.norm(g.download_real(f) - ref) / np.linalg.norm(ref) <= 1e-9
