@@ -560,6 +560,28 @@ __device__ __forceinline__ void separate_pairs(const float2 *__restrict__ z, flo
     if (k0 == 0) one(128);
 }
 
+// Forward transform of the packed row pair and separation of the two rows' half spectra into
+// out (v is overwritten).
+template <typename AT>
+__device__ __forceinline__ void x_fwd_store(float2 (&v)[16], float2 *__restrict__ out, int r, int j,
+                                            const float2 *s_tw, AT &&at, float2 *s_x, long long sbase, int KX, int Y)
+{
+    fft256<false>(v, r, s_tw, at);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) s_x[(r + 16 * i) * 16 + j] = v[i];
+    __syncthreads();
+    for (int e = threadIdx.x; e < KX * XROWS; e += NT) {
+        const int kx = e >> 5, y = e & 31, jj = y >> 1;
+        const float2 P = s_x[kx * 16 + jj];
+        const float2 Q = s_x[((N - kx) & (N - 1)) * 16 + jj];
+        float2 o;
+        if ((y & 1) == 0) o = make_float2(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y));
+        else o = make_float2(0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
+        out[sbase + (long long)kx * Y + y] = o;
+    }
+    __syncthreads();
+}
+
 // Pointwise polynomial of the packed row pair, forward transform and separation
 // of the two rows' half spectra into out[grp] (v is overwritten).
 template <typename AT>
@@ -587,22 +609,9 @@ __device__ __forceinline__ void xpoint_fwd_store(float2 (&v)[16], const XPassArg
             v[i] = make_float2(px, py);
         }
     }
-    fft256<false>(v, r, s_tw, at);
-#pragma unroll
-    for (int i = 0; i < 16; ++i) s_x[(r + 16 * i) * 16 + j] = v[i];
-    __syncthreads();
-    float2 *__restrict__ out = a.out[grp];
-    for (int e = threadIdx.x; e < KX * XROWS; e += NT) {
-        const int kx = e >> 5, y = e & 31, jj = y >> 1;
-        const float2 P = s_x[kx * 16 + jj];
-        const float2 Q = s_x[((N - kx) & (N - 1)) * 16 + jj];
-        float2 o;
-        if ((y & 1) == 0) o = make_float2(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y));
-        else o = make_float2(0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
-        out[sbase + (long long)kx * Y + y] = o;
-    }
-    __syncthreads();
+    x_fwd_store(v, a.out[grp], r, j, s_tw, at, s_x, sbase, KX, Y);
 }
+
 
 // NG == 1: one output group, transformed in place; NG == 0: any number of groups
 template <int NG>

@@ -7,6 +7,7 @@
 #include "fastline.cuh"
 #include "plane256.cuh"
 #include "gopf_kernels_impl.cuh"
+#include "elastic256.cuh"
 #include "x256_io.cuh"
 
 namespace gopf {
@@ -153,6 +154,18 @@ static bool fast_z(const PassArgs<float> &a)
     return a.allow_fast && a.plan.n == 256 && a.g.Z == 256 && a.g.S % 16 == 0 &&
            (a.mode == PM_FUSED || a.mode == PM_INIT) && a.nbuf <= 2 && a.upd.rk_stage == 0 && a.upd.etd == 0 &&
            a.upd.nxs == 0 && a.upd.nxf == 0 && a.upd.nsrc == 0 && a.upd.nimp <= 4;
+}
+
+// the elastic term's passes on 256-point axes (elastic256.cuh)
+static bool fast_x_elq(const XPassArgs<float> &a)
+{
+    return a.allow_fast && a.g.X == 256 && a.g.Y % f256::XROWS == 0 && a.in_mode == XIN_SPECTRAL &&
+           a.program == XP_ELASTIC_Q && !a.rout && !a.red && !a.red2;
+}
+
+static bool fast_z_elk(const PassArgs<float> &a)
+{
+    return a.allow_fast && a.plan.n == 256 && a.g.Z == 256 && a.g.S % 16 == 0 && a.mode == PM_ELASTIC_K;
 }
 
 // 256-column x passes that start or end in real space
@@ -302,6 +315,17 @@ template <> cudaError_t launch_xpass<float>(const XPassArgs<float> &a, int LB, c
         cudaError_t e;
         if (launch_x_io(a, st, &e)) return e;
     }
+    if (fast_x_elq(a)) {
+        static std::once_flag once;
+        static cudaError_t attr = cudaSuccess;
+        std::call_once(once, [] {
+            attr = cudaFuncSetAttribute(f256::k_x256_elq, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        f256::x256_elq_smem_bytes());
+        });
+        if (attr != cudaSuccess) return attr;
+        f256::k_x256_elq<<<dim3(a.g.Y / f256::XROWS, a.g.Z), f256::NT, f256::x256_elq_smem_bytes(), st>>>(a);
+        return cudaGetLastError();
+    }
     if (fast_x(a)) {
         cudaError_t e;
         if ((a.allow_fast & 2) && launch_x_tma(a, st, &e)) return e;
@@ -342,6 +366,10 @@ template <> cudaError_t launch_cpass<float>(const PassArgs<float> &a, int LB, cu
 
 template <> cudaError_t launch_spass<float>(const PassArgs<float> &a, int LB, cudaStream_t st)
 {
+    if (fast_z_elk(a)) {
+        f256::k_z256_elk<<<(unsigned)(a.g.S / 16), f256::NT, 0, st>>>(a);
+        return cudaGetLastError();
+    }
     if (fast_z(a)) {
         cudaError_t e;
         if ((a.allow_fast & 2) && launch_z_tma(a, st, &e)) return e;

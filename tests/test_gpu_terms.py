@@ -150,6 +150,29 @@ def test_elastic_graph_equals_eager():
     assert np.array_equal(a.download(0), b.download(0))
 
 
+@pytest.mark.parametrize("dims", [[256, 256, 256], [256, 256]])
+def test_elastic_256_kernels_match_generic(oracle, dims):
+    """The 256-point elastic passes (k_z256_elk, k_x256_elq) against the generic kernels, FP32, on
+    the C4 configuration's grid and in 2D: rel-L2 <= 2e-6 after 5 steps (the first one without the
+    term); in 2D also the oracle (FP32 tolerance 1e-4)."""
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+
+    n = int(np.prod(dims))
+    c0 = uniform_field(3, n, 0.3, 0.02)
+    fast = elastic_gpu(dims, "fp32", c0, 0.02)
+    gen = elastic_gpu(dims, "fp32", c0, 0.02)
+    gen.set_option(G._lib.OPT_FAST_KERNELS, 0)
+    fast.step(5)
+    gen.step(5)
+    a, b = fast.download_real(0), gen.download_real(0)
+    assert rel_l2(a, b) <= 2e-6
+    if len(dims) == 2:
+        o = elastic_oracle(oracle, dims, c0)
+        o.step_euler(0.02, 5)
+        assert rel_l2(a, o.field(0).real) <= 1e-4
+
+
 def _volcons_models(O, dims, c0, dt):
     import gopf_gb300 as G
 
