@@ -25,8 +25,11 @@ __global__ void __launch_bounds__(NT, 3) k_z256_elk(const PassArgs<float> a)
     float2 *__restrict__ buf = a.buf[0];
     const float *__restrict__ bsym = a.bsym;
     float2 v[16];
+    float b[16]; // the symbol's values are requested with the line, before the transform
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = buf[i0 + l + (long long)(r + 16 * i) * S];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) b[i] = __ldg(&bsym[i0 + l + (long long)(r + 16 * i) * S]);
     load_twiddles(s_tw, a.tw);
     __syncthreads();
     auto at = [&](int x, int y) -> float2 & { return s_x[(x * 16 + y) * 16 + l]; };
@@ -34,8 +37,8 @@ __global__ void __launch_bounds__(NT, 3) k_z256_elk(const PassArgs<float> a)
     const float invN = (float)a.upd.invN;
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
-        const float b = bsym[i0 + l + (long long)(r + 16 * i) * S] * invN;
-        v[i] = make_float2(v[i].x * b, v[i].y * b);
+        const float bi = b[i] * invN;
+        v[i] = make_float2(v[i].x * bi, v[i].y * bi);
     }
     fft256<true>(v, r, s_tw, at);
 #pragma unroll
