@@ -15,7 +15,7 @@ namespace gopf {
 namespace f256 {
 
 // PM_ELASTIC_K along z: lines are 16 consecutive inner indices i0 + l of the S = KX*Y plane.
-__global__ void __launch_bounds__(NT, 3) k_z256_elk(const PassArgs<float> a)
+static __global__ void __launch_bounds__(NT, 3) k_z256_elk(const PassArgs<float> a)
 {
     __shared__ __align__(16) float2 s_x[N * 16];
     __shared__ float2 s_tw[N];
@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(NT, 3) k_z256_elk(const PassArgs<float> a)
 // one arrives while the first is transformed.
 __host__ __device__ constexpr int x256_elq_smem_bytes() { return (N * 16 + 64 + 129 * XROWS) * 8; }
 
-__global__ void __launch_bounds__(NT, 2) k_x256_elq(const XPassArgs<float> a)
+static __global__ void __launch_bounds__(NT, 2) k_x256_elq(const XPassArgs<float> a)
 {
     extern __shared__ __align__(16) unsigned char elq_dsm[];
     float2 *s_x = reinterpret_cast<float2 *>(elq_dsm); // [N * 16 + 64]: tile of in, then the exchange slots

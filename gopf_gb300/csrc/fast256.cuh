@@ -927,5 +927,62 @@ __global__ void __launch_bounds__(NT, 3)
     if (tid == 0) bulk_wait_read_all();
 }
 
+// One output group (the Cahn-Hilliard x pass): the tile arrives by one TMA copy as in k_x256_tma,
+// but the separated half spectra leave by coalesced stores (a warp writes 256 contiguous bytes of
+// one kx row) instead of through an output tile, so a block needs no second 33 KB of shared
+// memory and four blocks fit on an SM.
+__host__ __device__ constexpr int x256_tl_smem_bytes()
+{
+    return 128 + XT_XCH_BYTES + N * 8 + GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1) * 4 + 16;
+}
+
+static __global__ void __launch_bounds__(NT, 4) k_x256_tl(const XPassArgs<float> a, const __grid_constant__ CUtensorMap mIn)
+{
+    extern __shared__ unsigned char xl_dsm[];
+    unsigned char *base = xl_dsm + ((128u - (smem_u32(xl_dsm) & 127u)) & 127u);
+    float2 *s_x = reinterpret_cast<float2 *>(base); // input tile, then exchange slots
+    float2 *s_tw = reinterpret_cast<float2 *>(base + XT_XCH_BYTES);
+    float *s_poly = reinterpret_cast<float *>(s_tw + N);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(s_poly + GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1));
+    int *s_ok = reinterpret_cast<int *>(bar + 1);
+
+    const int tid = threadIdx.x;
+    const int j = tid & 15, r = tid >> 4;
+    const int y0 = blockIdx.x * XROWS;
+    const int z = blockIdx.y;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        mbar_arrive_expect_tx(bar, (uint32_t)XT_TILE_BYTES);
+        tma_load_3d(s_x, &mIn, y0, 0, z, bar);
+    }
+    for (int t = tid; t < GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1); t += NT)
+        s_poly[t] = (float)a.pw.dense[t / (GOPF_MAX_DEG + 1)][t % (GOPF_MAX_DEG + 1)];
+    load_twiddles(s_tw, a.twX);
+    if (tid == 0) *s_ok = tma_wait_or_flag(bar, 0, a.status) ? 1 : 0;
+    __syncthreads();
+    if (!*s_ok) return;
+
+    float2 v[16];
+    load_pair_line(s_x, r, j, v);
+    __syncthreads();
+    auto at = [&](int x, int y) -> float2 & { return s_x[(x * 16 + y) * 16 + j]; };
+    fft256<true>(v, r, s_tw, at);
+    switch (a.identity ? -1 : a.pw.deg[0]) { // the launch guarantees a dense degree <= 6
+    case 0: poly_regs<0>(v, s_poly); break;
+    case 1: poly_regs<1>(v, s_poly); break;
+    case 2: poly_regs<2>(v, s_poly); break;
+    case 3: poly_regs<3>(v, s_poly); break;
+    case 4: poly_regs<4>(v, s_poly); break;
+    case 5: poly_regs<5>(v, s_poly); break;
+    case 6: poly_regs<6>(v, s_poly); break;
+    default: break;
+    }
+    x_fwd_store(v, a.out[0], r, j, s_tw, at, s_x, (long long)z * a.g.S + y0, a.g.KX, a.g.Y);
+}
+
 } // namespace f256
 } // namespace gopf

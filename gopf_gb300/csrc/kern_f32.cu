@@ -61,6 +61,12 @@ static bool launch_x_tma(const XPassArgs<float> &a, cudaStream_t st, cudaError_t
     if (attr_err != cudaSuccess || a.g.KX != 129 || a.ngrp_out > GOPF_MAX_GROUPS) return false;
     CUtensorMap mi, mo[GOPF_MAX_GROUPS];
     if (!x_map(&mi, a.in, a.g)) return false;
+    if (a.ngrp_out == 1 && (a.identity || (a.pw.deg[0] >= 0 && a.pw.deg[0] <= 6))) {
+        // one dense polynomial group: four blocks per SM, direct stores
+        f256::k_x256_tl<<<dim3(a.g.Y / f256::XROWS, a.g.Z), f256::NT, f256::x256_tl_smem_bytes(), st>>>(a, mi);
+        *err = cudaGetLastError();
+        return true;
+    }
     for (int b = 0; b < GOPF_MAX_GROUPS; ++b) {
         if (b < a.ngrp_out) {
             if (!x_map(&mo[b], a.out[b], a.g)) return false;
