@@ -40,7 +40,7 @@ UNIT = "steps/s"
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of each step kernel, from
 # one ncu capture of `python bench.py --steps 10 --warmup 3 --no-cpu-baseline --no-e2e` on a GB300
 # (profiles/launches_ch3d_256_fp32.md).  Bytes that a launch leaves in L2 are not in these counts.
-NCU_TRAFFIC = {"zpass_update": 207.4e6, "xpass_pointwise": 72.9e6, "ypass_forward": 72.7e6,
+NCU_TRAFFIC = {"zpass_update": 207.4e6, "xpass_pointwise": 72.8e6, "ypass_forward": 72.7e6,
                "ypass_inverse": 72.7e6}
 DIMS = [256, 256, 256]
 GAMMA, M, DT, SEED = 0.5, 1.0, 0.05, 1
