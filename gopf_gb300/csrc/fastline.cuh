@@ -351,7 +351,9 @@ template <int L> __device__ __forceinline__ void xline_request(float2 *area, con
 // One x tile from its spectral tile in area (which then serves as exchange and separation
 // space): c2r of 2 LPB rows -> polynomial groups -> r2c into a.out[grp] (L = g.X columns).
 // s_poly: this instance's dense polynomial coefficients.  Ends with a barrier.
-template <int L>
+// ONE: exactly one output group, a dense polynomial of degree <= 6 (the caller checks), so only one
+// line is held in registers and the polynomial is unrolled for its degree
+template <int L, bool ONE = false>
 __device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float> &a, int ty, int zp,
                                               const float2 *s_tw, const float *s_poly)
 {
@@ -399,6 +401,32 @@ __device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float
         }
         __syncthreads();
     };
+    if constexpr (ONE) {
+        switch (a.pw.deg[0]) {
+        case 0: f256::poly_regs<0>(v, s_poly); break;
+        case 1: f256::poly_regs<1>(v, s_poly); break;
+        case 2: f256::poly_regs<2>(v, s_poly); break;
+        case 3: f256::poly_regs<3>(v, s_poly); break;
+        case 4: f256::poly_regs<4>(v, s_poly); break;
+        case 5: f256::poly_regs<5>(v, s_poly); break;
+        default: f256::poly_regs<6>(v, s_poly); break;
+        }
+        line_fwd<L>(v, r, ro, z, s_tw);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) s_sep[l * (L + 1) + ro.elem(j)] = v[j];
+        __syncthreads();
+        float2 *__restrict__ out = a.out[0];
+        for (int e = threadIdx.x; e < KX * G::LPB; e += G::NT) {
+            const int kx = e / G::LPB, p = e - kx * G::LPB;
+            const float2 P = s_sep[p * (L + 1) + kx];
+            const float2 Q = s_sep[p * (L + 1) + (kx ? L - kx : 0)];
+            if (y0 + 2 * p < Y)
+                *reinterpret_cast<float4 *>(&out[sbase + (long long)kx * Y + 2 * p]) =
+                    make_float4(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y), 0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
+        }
+        __syncthreads();
+        return;
+    }
     // every group but the last works on a copy; the last one on v itself, so that a single group
     // (the usual case) does not hold two lines in registers
     const int ng = a.ngrp_out;
@@ -419,7 +447,7 @@ template <int L> __device__ __forceinline__ void load_xconsts(const XPassArgs<fl
 }
 
 // One x tile: 2 LPB rows from row ty * 2 LPB of depth plane zp (g.Y a multiple of 2 LPB).
-template <int L> __device__ __forceinline__ void xline_tile(const XPassArgs<float> &a, int ty, int zp)
+template <int L, bool ONE = false> __device__ __forceinline__ void xline_tile(const XPassArgs<float> &a, int ty, int zp)
 {
     extern __shared__ __align__(16) unsigned char fl_dsm[];
     float2 *s_a = reinterpret_cast<float2 *>(fl_dsm);
@@ -429,7 +457,7 @@ template <int L> __device__ __forceinline__ void xline_tile(const XPassArgs<floa
     load_xconsts<L>(a, s_tw, s_poly);
     cp_async_wait<0>();
     __syncthreads();
-    xline_compute<L>(s_a, a, ty, zp, s_tw, s_poly);
+    xline_compute<L, ONE>(s_a, a, ty, zp, s_tw, s_poly);
 }
 
 } // namespace fl

@@ -119,6 +119,18 @@ __global__ void __launch_bounds__(fl::Geo<L>::NT, 3) k_batch_xl(const BatchInst<
     fl::xline_tile<L>(s_a, it.y, 0);
 }
 
+// Instances with one dense polynomial group (Cahn-Hilliard): one line in registers, four blocks per SM.
+template <int L>
+__global__ void __launch_bounds__(fl::Geo<L>::NT, 4) k_batch_xl1(const BatchInst<float> *__restrict__ inst,
+                                                                const int2 *__restrict__ items, int nitems)
+{
+    __shared__ __align__(16) XPassArgs<float> s_a;
+    const int2 it = items[blockIdx.x];
+    stage_args(&s_a, &inst[it.x].xa);
+    __syncthreads();
+    fl::xline_tile<L, true>(s_a, it.y, 0);
+}
+
 template <int L, int NG>
 __global__ void __launch_bounds__(fl::Geo<L>::NT, 3) k_batch_yl(const BatchInst<float> *__restrict__ inst,
                                                                const int2 *__restrict__ items, int nitems)
@@ -128,8 +140,9 @@ __global__ void __launch_bounds__(fl::Geo<L>::NT, 3) k_batch_yl(const BatchInst<
 }
 
 // Classes: 0 any size (runtime plan); 1 .. 6 compile-time plans (x by H, y by the line length);
-// 11 .. 15 the line engine for sides FL_L (y: 11 .. 15 one group, 21 .. 25 two groups).
-constexpr int NCLASS = 26;
+// 11 .. 15 the line engine for sides FL_L (y: 11 .. 15 one group, 21 .. 25 two groups; x: 31 .. 35
+// for instances with one dense polynomial group).
+constexpr int NCLASS = 36;
 constexpr int XCLS_H[7] = {0, 64, 128, 192, 256, 384, 512}, XCLS_LB[7] = {0, 16, 16, 16, 16, 8, 8};
 constexpr int YCLS_N[7] = {0, 128, 256, 384, 512, 768, 1024}, YCLS_LB[7] = {0, 16, 16, 8, 8, 4, 4};
 constexpr int FL_L[5] = {256, 384, 512, 768, 1024};
@@ -156,6 +169,11 @@ template <typename R> static const void *x_kernel(int cls)
         case 13: return (const void *)k_batch_xl<512>;
         case 14: return (const void *)k_batch_xl<768>;
         case 15: return (const void *)k_batch_xl<1024>;
+        case 31: return (const void *)k_batch_xl1<256>;
+        case 32: return (const void *)k_batch_xl1<384>;
+        case 33: return (const void *)k_batch_xl1<512>;
+        case 34: return (const void *)k_batch_xl1<768>;
+        case 35: return (const void *)k_batch_xl1<1024>;
         default: break;
         }
     }
@@ -318,8 +336,9 @@ template <typename R> static int batch_build(gopf_batch *b)
                 if (g.Y == FL_L[k] && nb <= 2 && c->upd.nimp <= 4) fy = k;
             }
         }
-        if (fx >= 0) { // line engine: tiles of 2 LPB rows
-            xc = 11 + fx;
+        if (fx >= 0) { // line engine: tiles of 2 LPB rows (31 ..: one dense polynomial group)
+            const bool one = (G == 1 && c->pw.deg[0] >= 0 && c->pw.deg[0] <= 6);
+            xc = (one ? 31 : 11) + fx;
             const int ntx = g.Y / (2 * FL_LPB[fx]);
             for (int t = 0; t < ntx; ++t) xs[xc].push_back({g.X * 2 * FL_LPB[fx], make_int2((int)i, t)});
             smem_x[xc] = FL_XSMEM[fx];
