@@ -247,6 +247,11 @@ template <int L> __global__ void __launch_bounds__(fl::Geo<L>::NT, 3) k_xline(co
 {
     fl::xline_tile<L>(a, blockIdx.x, blockIdx.y);
 }
+// one dense polynomial group of degree <= 6: one line in registers, four blocks per SM
+template <int L> __global__ void __launch_bounds__(fl::Geo<L>::NT, 4) k_xline1(const XPassArgs<float> a)
+{
+    fl::xline_tile<L, true>(a, blockIdx.x, blockIdx.y);
+}
 
 static bool line_len(int n) { return n == 384 || n == 512 || n == 768 || n == 1024; }
 
@@ -275,9 +280,16 @@ template <int L> static cudaError_t launch_xline(const XPassArgs<float> &a, cuda
 {
     typedef fl::Geo<L> G;
     if (a.g.Y % (2 * G::LPB)) return cudaErrorNotSupported;
+    const dim3 grid(a.g.Y / (2 * G::LPB), a.g.Z);
+    if (a.ngrp_out == 1 && a.pw.deg[0] >= 0 && a.pw.deg[0] <= 6) {
+        static const cudaError_t attr1 = line_smem(k_xline1<L>, fl::xline_smem_bytes<L>());
+        if (attr1 != cudaSuccess) return attr1;
+        k_xline1<L><<<grid, G::NT, fl::xline_smem_bytes<L>(), st>>>(a);
+        return cudaGetLastError();
+    }
     static const cudaError_t attr = line_smem(k_xline<L>, fl::xline_smem_bytes<L>());
     if (attr != cudaSuccess) return attr;
-    k_xline<L><<<dim3(a.g.Y / (2 * G::LPB), a.g.Z), G::NT, fl::xline_smem_bytes<L>(), st>>>(a);
+    k_xline<L><<<grid, G::NT, fl::xline_smem_bytes<L>(), st>>>(a);
     return cudaGetLastError();
 }
 
