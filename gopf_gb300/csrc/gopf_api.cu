@@ -598,7 +598,7 @@ static int derived_mono(gopf_ctx *ctx, const gopf_derived &d, std::vector<Mono> 
         return GOPF_OK;
     }
     if (d.kind == GOPF_DER_WHITE_NOISE)
-        return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "noise terms are stepped in single-field models only");
+        return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "white noise enters only as a term of its own");
     std::vector<std::pair<double, int>> poly;
     gopf_derived d0 = d;
     d0.field[0] = 0; // derived_poly expands the indicator kinds of one field

@@ -205,9 +205,10 @@ int gopf_newton_stats(gopf_ctx *ctx, int *newton_iters, int *krylov_iters, doubl
  * Model.AddField position: a model may hold up to 4 fields, equation i evolving field i
  * (pf/euler.go:26-47, pf/rk4.go:29-74 loop over m.Fields with m.RHS[i]).  Fields never
  * uploaded start at zero, like pf.NewField(name, n, nil).  Multi-field models step with
- * Euler or RK4; their explicit terms are products of powers of any fields and their
- * implicit terms polynomials in the Laplacian or TensorialHessian / SpectralViscosity
- * symbols.  Elastic, volume-conserving and noise terms need a single-field model. */
+ * Euler, RK4 or ImplicitEuler; their explicit terms are products of powers of any fields
+ * (gopf_register_polynomial for sums of them) and their implicit terms polynomials in the
+ * Laplacian or TensorialHessian / SpectralViscosity symbols.  The elastic, volume-conserving
+ * and noise terms (one of each per model, on any field and in any equation) step with Euler. */
 int gopf_field_upload(gopf_ctx *ctx, int field_id, const double *data, size_t n);
 int gopf_field_download(gopf_ctx *ctx, int field_id, double *data, size_t n);
 /* Real-valued variants (n doubles) */
