@@ -36,6 +36,9 @@ template <int L> struct Geo {
     static constexpr int LPB = NT / T;               // lines per block
     static constexpr int PAD = (T == 24) ? 4 : 0;    // slot offset between lines (bank spread)
     static constexpr int LREG = 16 * T + PAD;        // shared slots per line
+    // separation pitch: the readers take (line p, column kx) with p fastest over LPB lines, so a
+    // pitch of 32 / LPB (mod 16) float2 spreads a warp's 32 reads over all 16 bank pairs
+    static constexpr int SEP = L + 32 / LPB;
     static_assert(L == 256 || L == 384 || L == 512 || L == 768 || L == 1024, "line length");
 };
 
@@ -317,10 +320,10 @@ template <int L, int NG> __device__ __forceinline__ void yline_tile(const PassAr
 }
 
 // one shared array holds, in turn, the spectral tile [L/2 + 1][2 LPB], the exchange slots of the
-// LPB lines and the separation slots [LPB][L + 1]; then twiddles and polynomial coefficients
+// LPB lines and the separation slots [LPB][SEP]; then twiddles and polynomial coefficients
 template <int L> __host__ __device__ constexpr int xline_area()
 {
-    constexpr int a = (L / 2 + 1) * 2 * Geo<L>::LPB, b = Geo<L>::LPB * Geo<L>::LREG, c = Geo<L>::LPB * (L + 1);
+    constexpr int a = (L / 2 + 1) * 2 * Geo<L>::LPB, b = Geo<L>::LPB * Geo<L>::LREG, c = Geo<L>::LPB * Geo<L>::SEP;
     return (a > b ? (a > c ? a : c) : (b > c ? b : c));
 }
 template <int L> constexpr int xline_smem_bytes() { return (xline_area<L>() + L) * 8 + GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1) * 4; }
@@ -359,7 +362,7 @@ __device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float
 {
     typedef Geo<L> G;
     constexpr int H = L / 2, KX = H + 1, RB = 2 * G::LPB;
-    float2 *s_sep = s_a; // [LPB][L + 1], once the exchange is done
+    float2 *s_sep = s_a; // [LPB][SEP], once the exchange is done
     const Geom &g = a.g;
     const int l = threadIdx.x / G::T, r = threadIdx.x - l * G::T;
     const int y0 = ty * RB;
@@ -388,13 +391,13 @@ __device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float
         if (!a.identity) f256::apply_poly(w, a, grp, s_poly + grp * (GOPF_MAX_DEG + 1));
         line_fwd<L>(w, r, ro, z, s_tw);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) s_sep[l * (L + 1) + ro.elem(j)] = w[j];
+        for (int j = 0; j < 16; ++j) s_sep[l * G::SEP + ro.elem(j)] = w[j];
         __syncthreads();
         float2 *__restrict__ out = a.out[grp];
         for (int e = threadIdx.x; e < KX * G::LPB; e += G::NT) {
             const int kx = e / G::LPB, p = e - kx * G::LPB;
-            const float2 P = s_sep[p * (L + 1) + kx];
-            const float2 Q = s_sep[p * (L + 1) + (kx ? L - kx : 0)];
+            const float2 P = s_sep[p * G::SEP + kx];
+            const float2 Q = s_sep[p * G::SEP + (kx ? L - kx : 0)];
             if (y0 + 2 * p < Y)
                 *reinterpret_cast<float4 *>(&out[sbase + (long long)kx * Y + 2 * p]) =
                     make_float4(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y), 0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
@@ -413,13 +416,13 @@ __device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float
         }
         line_fwd<L>(v, r, ro, z, s_tw);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) s_sep[l * (L + 1) + ro.elem(j)] = v[j];
+        for (int j = 0; j < 16; ++j) s_sep[l * G::SEP + ro.elem(j)] = v[j];
         __syncthreads();
         float2 *__restrict__ out = a.out[0];
         for (int e = threadIdx.x; e < KX * G::LPB; e += G::NT) {
             const int kx = e / G::LPB, p = e - kx * G::LPB;
-            const float2 P = s_sep[p * (L + 1) + kx];
-            const float2 Q = s_sep[p * (L + 1) + (kx ? L - kx : 0)];
+            const float2 P = s_sep[p * G::SEP + kx];
+            const float2 Q = s_sep[p * G::SEP + (kx ? L - kx : 0)];
             if (y0 + 2 * p < Y)
                 *reinterpret_cast<float4 *>(&out[sbase + (long long)kx * Y + 2 * p]) =
                     make_float4(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y), 0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
