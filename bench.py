@@ -38,8 +38,9 @@ sys.path.insert(0, HERE)
 METRIC = ("CH steps/s at 256³ FP32 vs GPU FP64 (rel-L2≤1e-4); FFT % of HBM peak; sweep steps/s")
 UNIT = "steps/s"
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of each step kernel, from
-# one ncu capture of `python bench.py --steps 10 --warmup 3 --no-cpu-baseline --no-e2e` on a GB300
-# (profiles/launches_ch3d_256_fp32.md).  Bytes that a launch leaves in L2 are not in these counts.
+# one ncu capture on a GB300 of `python bench.py --steps 20 --warmup 17 --no-cpu-baseline --no-e2e
+# --no-precision` (the kernels' summaries under profiles/).  Bytes that a launch leaves in L2 are not
+# in these counts.
 NCU_TRAFFIC = {"zpass_update": 207.4e6, "xpass_pointwise": 72.8e6, "ypass_forward": 72.7e6,
                "ypass_inverse": 72.7e6}
 DIMS = [256, 256, 256]
@@ -134,8 +135,9 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_oracle_step_rate(dims, max_seconds: float, max_steps: int, warmup: int = 0):
-    """Steps/s of the FP64 CPU oracle's Euler step (all host threads)."""
+def cpu_oracle_step_rate(dims, max_seconds: float, max_steps: int, warmup: int = 0, keep_field: bool = False):
+    """Steps/s of the FP64 CPU oracle's Euler step (all host threads); with keep_field, also the
+    oracle's real field after the steps it took (warm-up included)."""
     from gopf_gb300.synthetic import uniform_field
     from oracle import oracle as O
 
@@ -154,6 +156,8 @@ def cpu_oracle_step_rate(dims, max_seconds: float, max_steps: int, warmup: int =
         if time.perf_counter() - t0 > max_seconds:
             break
     el = time.perf_counter() - t0
+    if keep_field:
+        return steps / el, steps, el, threads, m.field(0).real.copy()
     return steps / el, steps, el, threads
 
 
@@ -206,24 +210,15 @@ def run_gpu(args):
     n = int(np.prod(DIMS))
     c0 = uniform_field(SEED, n, 0.0, 0.1)
 
-    m = G.Model(DIMS, "fp32", device=local)
-    m.add_field("conc")
-    m.add_scalar("gamma", GAMMA)
-    m.add_scalar("M", M)
-    m.add_scalar("m1", -M)
-    m.add_equation(CH_EQ)
-    m.init()
-    m.set_stepper("euler", DT)
     stream = torch.cuda.Stream()
-    m.set_stream(stream.cuda_stream)
-    m.set_option(G._lib.OPT_CHECK_FINITE, 0)
+    m = ch3d_model(G, "fp32", c0, local, stream)
     if args.tma is not None:
         m.set_option(G._lib.OPT_TMA, args.tma)
     if args.plane is not None:
         m.set_option(G._lib.OPT_PLANE, args.plane)
-    m.upload(0, c0)
     mass0 = m.mass(0)
-    m.step(warmup_steps(args))  # warm-up: captures both CUDA graphs (1 and 16 steps) before timing
+    m.prepare_graphs(args.steps)  # capture the graphs the timed steps replay (no stepping)
+    m.step(warmup_steps(args))
     torch.cuda.synchronize()
 
     # ---- device-resident timed region ----
@@ -260,8 +255,21 @@ def run_gpu(args):
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(args, m, stream, c0, n, world, dist, torch, G)
-    out = emit(args, m, world, rank, value, per_step_ms, mass0, mass1, finite, prof, dom, hbm, peak_kind, achieved,
-               step_bytes, e2e, clocks, n)
+    gpu_launches = m.kernel_launches(args.steps)
+    m.close()
+    # ---- CPU baseline (the FP64 oracle on the host cores) and the metric's precision half ----
+    cpu, oracle_run = None, None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rate, steps, el, threads, ofield = cpu_oracle_step_rate(DIMS, max_seconds=args.cpu_seconds, max_steps=50,
+                                                                keep_field=True)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{steps} FP64 Euler steps of the 256^3 grid ({el:.1f} s) on the host cores"}
+        oracle_run = (steps, ofield)
+    precision = None
+    if rank == 0 and not args.no_precision:
+        precision = measure_precision(args, G, torch, c0, n, stream, value / world, oracle_run)
+    out = emit(args, world, rank, value, per_step_ms, mass0, mass1, finite, prof, dom, hbm, peak_kind, achieved,
+               step_bytes, e2e, clocks, n, cpu, precision, gpu_launches)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -269,9 +277,77 @@ def run_gpu(args):
 
 
 def warmup_steps(args) -> int:
-    """At least 3 warm-up steps, and at least one full 16-step graph so that both CUDA graphs
-    (1 and 16 steps) are captured before the timed region."""
-    return max(args.warmup, 3, 17)
+    """Untimed warm-up steps (at least 3).  The graphs the timed steps replay are captured
+    beforehand by prepare_graphs, so the warm-up needs no minimum of its own."""
+    return max(args.warmup, 3)
+
+
+def ch3d_model(G, prec, c0, device, stream, dims=None):
+    """The benchmark's model: 3D CH, the examples/cahnHilliard splitting, Euler dt 0.05."""
+    m = G.Model(dims or DIMS, prec, device=device)
+    m.add_field("conc")
+    m.add_scalar("gamma", GAMMA)
+    m.add_scalar("M", M)
+    m.add_scalar("m1", -M)
+    m.add_equation(CH_EQ)
+    m.init()
+    m.set_stepper("euler", DT)
+    if stream is not None:
+        m.set_stream(stream.cuda_stream)
+    m.set_option(G._lib.OPT_CHECK_FINITE, 0)
+    m.upload(0, c0)
+    return m
+
+
+def timed_steps(m, torch, stream, k):
+    """Device time (ms) of k graph-replayed steps, CUDA events on the stepping stream."""
+    m.prepare_graphs(k)
+    m.step(3)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    m.step(k)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def measure_precision(args, G, torch, c0, n, stream, fp32_rate, oracle_run):
+    """The metric's other clauses on the same workload:
+    - the FP64 device mode's steps/s (the same kernels' FP64 form) and the FP32/FP64 ratio;
+    - FP64 device against the FP64 oracle after the steps the CPU baseline took (full size);
+    - FP32 against FP64 device after `precision_steps` steps (1000: the metric's horizon):
+      rel-L2 and each run's mass drift per cell."""
+    out = {}
+    if oracle_run is not None:
+        k, ofield = oracle_run
+        a = ch3d_model(G, "fp64", c0, 0, stream)
+        a.step(k)
+        d = a.download_real(0)
+        out["fp64_vs_oracle"] = {"steps": k, "rel_l2": float(np.linalg.norm(d - ofield) / np.linalg.norm(ofield)),
+                                 "tolerance": 1e-11}
+        a.close()
+    k64 = 20
+    a = ch3d_model(G, "fp64", c0, 0, stream)
+    ms = timed_steps(a, torch, stream, k64)
+    a.close()
+    fp64_rate = k64 / (ms / 1000.0)
+    out["fp64_steps_per_s"] = fp64_rate
+    out["fp32_over_fp64"] = fp32_rate / fp64_rate
+    S = args.precision_steps
+    if S > 0:
+        a32 = ch3d_model(G, "fp32", c0, 0, stream)
+        a64 = ch3d_model(G, "fp64", c0, 0, stream)
+        a32.step(S)
+        a64.step(S)
+        d32, d64 = a32.download_real(0), a64.download_real(0)
+        out["fp32_vs_fp64"] = {"steps": S, "rel_l2": float(np.linalg.norm(d32 - d64) / np.linalg.norm(d64)),
+                               "tolerance": 1e-4,
+                               "mass_drift_per_cell": {"fp32": abs(a32.mass(0) - c0.sum()) / n,
+                                                       "fp64": abs(a64.mass(0) - c0.sum()) / n}}
+        a32.close()
+        a64.close()
+    return out
 
 
 def run_e2e(args, m, stream, c0, n, world, dist, torch, G):
@@ -335,15 +411,10 @@ def host_link(torch, host, stream, reps=5):
     return out
 
 
-def emit(args, m, world, rank, value, per_step_ms, mass0, mass1, finite, prof, dom, hbm, peak_kind, achieved,
-         step_bytes, e2e, clocks, n):
+def emit(args, world, rank, value, per_step_ms, mass0, mass1, finite, prof, dom, hbm, peak_kind, achieved,
+         step_bytes, e2e, clocks, n, cpu, precision, gpu_launches):
     out = None
     if rank == 0:
-        cpu = None
-        if world == 1 and not args.no_cpu_baseline:
-            rate, steps, el, threads = cpu_oracle_step_rate(DIMS, max_seconds=args.cpu_seconds, max_steps=50)
-            cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                   "sample": f"{steps} FP64 Euler steps of the 256^3 grid ({el:.1f} s) on the host cores"}
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": warmup_steps(args), "ms_per_step": per_step_ms, "higher_is_better": True, "scaling": "weak",
@@ -352,7 +423,11 @@ def emit(args, m, world, rank, value, per_step_ms, mass0, mass1, finite, prof, d
                               "cell_updates_per_s": value * n,
                               "step_bytes_algorithmic": step_bytes,
                               "step_fraction_of_hbm": (step_bytes * value / world / 1e9) / hbm,
-                              "mass_drift_per_cell": abs(mass1 - mass0) / n, "finite": bool(finite)}),
+                              "mass_drift_per_cell": abs(mass1 - mass0) / n, "finite": bool(finite),
+                              "precision": precision,
+                              "per_pass_gbs": {p["name"]: p["bytes"] / p["ms"] / 1e6 for p in prof if p["ms"] > 0},
+                              "per_pass_frac_of_hbm": {p["name"]: p["bytes"] / p["ms"] / 1e6 / hbm
+                                                       for p in prof if p["ms"] > 0}}),
             "e2e": e2e,
             "roofline": {"bound": "hbm", "kernel": dom["name"], "achieved": achieved, "peak": hbm,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
@@ -361,7 +436,7 @@ def emit(args, m, world, rank, value, per_step_ms, mass0, mass1, finite, prof, d
                                          "bytes": p["bytes"]} for p in prof]},
             "cpu_baseline": cpu,
             "clocks": clocks,
-            "gpu_launches": m.kernel_launches(args.steps),
+            "gpu_launches": gpu_launches,
         }
         print(json.dumps(out))
     return out
@@ -554,6 +629,7 @@ def run_elastic(args):
     m.upload(0, c0)
     mass0 = m.mass(0)
     m.step(warmup_steps(args))
+    m.prepare_graphs(args.steps)  # after the first (unreplayed) elastic step
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(0) as clk:
@@ -605,6 +681,7 @@ def run_c1(args):
         m.init()
         m.set_stepper("euler", 0.1)
         m.upload(0, c0)
+        m.prepare_graphs(steps)
         m.step(warmup_steps(args))
         m.upload(0, c0)
         torch.cuda.synchronize()
@@ -705,6 +782,10 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="skip the FP64 rate and the FP32-vs-FP64 / FP64-vs-oracle checks of the default line")
+    ap.add_argument("--precision-steps", type=int, default=1000,
+                    help="steps of the FP32-vs-FP64 device comparison in the default line")
     ap.add_argument("--grid", type=int, default=256, help="cube side (256 is the benchmark workload)")
     ap.add_argument("--workload", default="ch3d", choices=["ch3d", "sweep", "adjoint", "elastic", "precision", "c1"])
     ap.add_argument("--tma", type=int, default=None, choices=[0, 1, 2],

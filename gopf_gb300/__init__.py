@@ -280,6 +280,10 @@ class Model:
     def step(self, nsteps: int) -> None:
         self._ck(self._L.gopf_step(self._h, int(nsteps)))
 
+    def prepare_graphs(self, nsteps: int) -> None:
+        """Capture the graphs that step(nsteps) replays, without stepping."""
+        self._ck(self._L.gopf_prepare_graphs(self._h, int(nsteps)))
+
     def synchronize(self) -> None:
         self._ck(self._L.gopf_synchronize(self._h))
 

@@ -26,6 +26,7 @@ NOISE_WHITE, NOISE_CONSERVATIVE = 1, 2
 SRC_NONE, SRC_FIELD, SRC_DERIVED = range(3)
 RED_SUM, RED_SUMSQ, RED_MIN, RED_MAX, RED_NONFINITE = range(5)
 OPT_CHECK_FINITE, OPT_USE_GRAPHS, OPT_FAST_KERNELS, OPT_TMA, OPT_PLANE, OPT_DIRECT_HOST = 0, 1, 2, 3, 4, 5
+OPT_WAIT_LIMIT_NS = 6
 MAX_FACTORS = 8
 
 
@@ -85,6 +86,7 @@ SIGNATURES = {
     "gopf_field_upload_real": ([_vp, _i, _dp, _sz], _i),
     "gopf_field_download_real": ([_vp, _i, _dp, _sz], _i),
     "gopf_step": ([_vp, _ll], _i),
+    "gopf_prepare_graphs": ([_vp, _ll], _i),
     "gopf_get_time": ([_vp, _dp], _i),
     "gopf_get_step": ([_vp, ctypes.POINTER(_ll)], _i),
     "gopf_synchronize": ([_vp], _i),

@@ -262,8 +262,10 @@ template <typename R> static int ctx_alloc(gopf_ctx *ctx)
     ctx->nred_blocks = ((g.Y + ctx->LBx - 1) / ctx->LBx) * g.Z;
     CK(gopf_malloc(&ctx->d_red, sizeof(double) * RED_SLOTS * ctx->nred_blocks));
     CK(gopf_malloc(&ctx->d_redout, sizeof(double) * RED_SLOTS));
-    CK(gopf_malloc(&ctx->d_status, 2 * sizeof(unsigned))); // [0] status word, [1] non-finite count
-    CK(cudaMemset(ctx->d_status, 0, 2 * sizeof(unsigned)));
+    // [0] status word, [1] non-finite count, [2..3] the first-wait limit of the bounded waits in ns
+    // (an unsigned long long; 0 = the built-in 2 s)
+    CK(gopf_malloc(&ctx->d_status, 4 * sizeof(unsigned)));
+    CK(cudaMemset(ctx->d_status, 0, 4 * sizeof(unsigned)));
     ctx->dev_bytes += sizeof(double) * RED_SLOTS * (ctx->nred_blocks + 1) + sizeof(unsigned);
     CK(cudaMemset(ctx->d_state, 0, sizeof(V) * g.C));
     CK(cudaMemset(ctx->d_T, 0, sizeof(V) * g.C));
@@ -408,7 +410,16 @@ extern "C" int gopf_set_option(gopf_ctx *ctx, int opt, long long v)
     else if (opt == GOPF_OPT_PLANE) ctx->use_plane = (int)(v != 0);
     else if (opt == GOPF_OPT_DIRECT_HOST) ctx->use_direct_host = (int)(v != 0);
     else if (opt == GOPF_OPT_TMA) ctx->use_tma = (int)std::min<long long>(std::max<long long>(v, 0), 2);
-    else return gopf_fail(ctx, GOPF_ERR_ARG, "unknown option");
+    else if (opt == GOPF_OPT_WAIT_LIMIT_NS) {
+        if (v < 0) return gopf_fail(ctx, GOPF_ERR_ARG, "negative wait limit");
+        if (!ctx->d_status) return gopf_fail(ctx, GOPF_ERR_STATE, "context has no device");
+        int rc;
+        if ((rc = set_device(ctx))) return rc;
+        const unsigned long long lim = (unsigned long long)v;
+        CK(cudaMemcpyAsync(ctx->d_status + 2, &lim, sizeof(lim), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        return GOPF_OK; // kernels read the limit at run time: captured graphs stay valid
+    } else return gopf_fail(ctx, GOPF_ERR_ARG, "unknown option");
     invalidate_graphs(ctx); // captured launches carry the old choice
     return GOPF_OK;
 }
@@ -1960,6 +1971,47 @@ extern "C" int gopf_point_values(gopf_ctx *ctx, int field, const long long *site
 // stepping
 // ------------------------------------------------------------------
 
+// Work buffers of the stepper beyond the context's own (RK4's accumulator), allocated on first use.
+static int stepper_buffers(gopf_ctx *ctx)
+{
+    int rc;
+    if (ctx->stepper == GOPF_STEPPER_RK4) {
+        if (ctx->has_elastic || ctx->has_volcons || ctx->noise.kind)
+            return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "user-defined and noise terms are stepped with Euler only");
+        if ((rc = alloc_spectral(ctx, &ctx->d_rkF))) return rc;
+        if (ctx->multi)
+            for (int f = 1; f < ctx->nfields; ++f)
+                if ((rc = alloc_spectral(ctx, &ctx->d_frkF[f]))) return rc;
+    }
+    return GOPF_OK;
+}
+
+// The graphs a run of `left` graph-stepped steps replays: one step, and graphK steps when the run is
+// that long.  Capturing records the launches without running them.
+static int ensure_graphs(gopf_ctx *ctx, long long left)
+{
+    int rc;
+    if (!ctx->gexec1 && (rc = capture_graph(ctx, 1, &ctx->gexec1))) return rc;
+    if (left >= ctx->graphK && !ctx->gexecK && (rc = capture_graph(ctx, ctx->graphK, &ctx->gexecK))) return rc;
+    return GOPF_OK;
+}
+
+extern "C" int gopf_prepare_graphs(gopf_ctx *ctx, long long nsteps)
+{
+    if (!ctx) return GOPF_ERR_ARG;
+    if (nsteps < 0) return gopf_fail(ctx, GOPF_ERR_ARG, "negative step count");
+    if (!ctx->initialised) return gopf_fail(ctx, GOPF_ERR_STATE, "model not initialised (gopf_init/gopf_set_terms)");
+    if (!(ctx->dt > 0.0)) return gopf_fail(ctx, GOPF_ERR_STATE, "no stepper set (gopf_set_stepper)");
+    if (!ctx->state_valid) return gopf_fail(ctx, GOPF_ERR_STATE, "field has not been uploaded");
+    int rc;
+    if ((rc = set_device(ctx))) return rc;
+    if (!ctx->use_graphs || ctx->stepper == GOPF_STEPPER_SDD || ctx->stepper == GOPF_STEPPER_IMPLICIT_EULER)
+        return GOPF_OK; // host-driven steppers replay no graphs
+    if ((rc = stepper_buffers(ctx))) return rc;
+    if (ctx->has_elastic && !ctx->el_primed) return GOPF_OK; // the first elastic step is not replayed
+    return ensure_graphs(ctx, nsteps);
+}
+
 extern "C" int gopf_step(gopf_ctx *ctx, long long nsteps)
 {
     if (!ctx) return GOPF_ERR_ARG;
@@ -1970,14 +2022,7 @@ extern "C" int gopf_step(gopf_ctx *ctx, long long nsteps)
     if (!ctx->state_valid) return gopf_fail(ctx, GOPF_ERR_STATE, "field has not been uploaded");
     int rc;
     if ((rc = set_device(ctx))) return rc;
-    if (ctx->stepper == GOPF_STEPPER_RK4) {
-        if (ctx->has_elastic || ctx->has_volcons || ctx->noise.kind)
-            return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "user-defined and noise terms are stepped with Euler only");
-        if ((rc = alloc_spectral(ctx, &ctx->d_rkF))) return rc;
-        if (ctx->multi)
-            for (int f = 1; f < ctx->nfields; ++f)
-                if ((rc = alloc_spectral(ctx, &ctx->d_frkF[f]))) return rc;
-    }
+    if ((rc = stepper_buffers(ctx))) return rc;
     if (!ctx->sources.empty()) {
         if (ctx->stepper == GOPF_STEPPER_SDD || ctx->stepper == GOPF_STEPPER_IMPLICIT_EULER)
             return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "sources are stepped with Euler and RK4");
@@ -2028,8 +2073,7 @@ extern "C" int gopf_step(gopf_ctx *ctx, long long nsteps)
         --left;
     }
     if (ctx->use_graphs) {
-        if (!ctx->gexec1 && (rc = capture_graph(ctx, 1, &ctx->gexec1))) return rc;
-        if (left >= ctx->graphK && !ctx->gexecK && (rc = capture_graph(ctx, ctx->graphK, &ctx->gexecK))) return rc;
+        if ((rc = ensure_graphs(ctx, left))) return rc;
         while (left >= ctx->graphK) {
             CK(cudaGraphLaunch(ctx->gexecK, ctx->stream));
             left -= ctx->graphK;

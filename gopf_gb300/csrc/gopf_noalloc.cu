@@ -21,11 +21,14 @@
 // overlap on the GPU (different streams, or different host threads without
 // ordering) race on the array and must be serialised by the caller.
 //
-// The device address of the array is looked up once per device, on the first
-// call made with that device current (cudaGetSymbolAddress).  Make that first
-// call before any stream capture.
+// Host code cannot use the array's name as a device address.  Every call looks
+// the address up with cudaGetSymbolAddress while the caller's device (and
+// context) is current, so a device reset or another context made current on
+// the device never leaves a stale address behind.  The first call on a device
+// also loads the library's device code there; make that first call before any
+// stream capture.  The call is synchronous: it waits on its stream until the
+// result is on the host.
 #include <cmath>
-#include <mutex>
 #include <string>
 
 #include <cuda_runtime.h>
@@ -39,23 +42,35 @@ static __device__ __align__(256) double g_noalloc_scratch[(GOPF_NOALLOC_MAX_BLOC
 
 namespace {
 
+__device__ __forceinline__ void neumaier_add(double &sum, double &err, double v)
+{
+    const double t = sum + v;
+    err += (fabs(sum) >= fabs(v)) ? (sum - t) + v : (v - t) + sum;
+    sum = t;
+}
+
 // slots: 0 sum, 1 sum of squares, 2 min, 3 max, 4 non-finite count (as gopf_reduce)
 __global__ void k_noalloc_partials(const double *__restrict__ x, long long n, double *__restrict__ rows)
 {
     const long long b0 = (long long)blockIdx.x * GOPF_NOALLOC_ELEMS_PER_BLOCK;
     const long long b1 = (b0 + GOPF_NOALLOC_ELEMS_PER_BLOCK < n) ? b0 + GOPF_NOALLOC_ELEMS_PER_BLOCK : n;
-    double s = 0.0, q = 0.0, mn = INFINITY, mx = -INFINITY, nf = 0.0;
+    // Neumaier-compensated sums per thread, folded with their error terms at each combination
+    double s = 0.0, sc = 0.0, q = 0.0, qc = 0.0, mn = INFINITY, mx = -INFINITY, nf = 0.0;
     for (long long i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
         const double v = x[i];
-        s += v;
-        q += v * v;
+        neumaier_add(s, sc, v);
+        neumaier_add(q, qc, v * v);
         mn = fmin(mn, v);
         mx = fmax(mx, v);
         nf += isfinite(v) ? 0.0 : 1.0;
     }
     for (int o = 16; o > 0; o >>= 1) {
-        s += __shfl_xor_sync(0xffffffffu, s, o);
-        q += __shfl_xor_sync(0xffffffffu, q, o);
+        const double so = __shfl_xor_sync(0xffffffffu, s, o), sco = __shfl_xor_sync(0xffffffffu, sc, o);
+        const double qo = __shfl_xor_sync(0xffffffffu, q, o), qco = __shfl_xor_sync(0xffffffffu, qc, o);
+        sc += sco;
+        neumaier_add(s, sc, so);
+        qc += qco;
+        neumaier_add(q, qc, qo);
         mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
         mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         nf += __shfl_xor_sync(0xffffffffu, nf, o);
@@ -63,8 +78,8 @@ __global__ void k_noalloc_partials(const double *__restrict__ x, long long n, do
     __shared__ double sh[32][5];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) {
-        sh[warp][0] = s;
-        sh[warp][1] = q;
+        sh[warp][0] = s + sc;
+        sh[warp][1] = q + qc;
         sh[warp][2] = mn;
         sh[warp][3] = mx;
         sh[warp][4] = nf;
@@ -72,15 +87,18 @@ __global__ void k_noalloc_partials(const double *__restrict__ x, long long n, do
     __syncthreads();
     if (threadIdx.x == 0) {
         const int nw = (blockDim.x + 31) / 32;
+        double bs = sh[0][0], bsc = 0.0, bq = sh[0][1], bqc = 0.0;
         for (int w = 1; w < nw; ++w) {
-            sh[0][0] += sh[w][0];
-            sh[0][1] += sh[w][1];
+            neumaier_add(bs, bsc, sh[w][0]);
+            neumaier_add(bq, bqc, sh[w][1]);
             sh[0][2] = fmin(sh[0][2], sh[w][2]);
             sh[0][3] = fmax(sh[0][3], sh[w][3]);
             sh[0][4] += sh[w][4];
         }
         double *row = rows + (long long)blockIdx.x * GOPF_NOALLOC_SLOTS;
-        for (int k = 0; k < 5; ++k) row[k] = sh[0][k];
+        row[0] = bs + bsc;
+        row[1] = bq + bqc;
+        for (int k = 2; k < 5; ++k) row[k] = sh[0][k];
         for (int k = 5; k < GOPF_NOALLOC_SLOTS; ++k) row[k] = 0.0;
     }
 }
@@ -111,9 +129,6 @@ __global__ void k_noalloc_finish(const double *__restrict__ rows, int nblocks, d
     for (int k = 5; k < GOPF_NOALLOC_SLOTS; ++k) res[k] = 0.0;
 }
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-double *g_addr[kMaxDevices] = {nullptr};
 thread_local std::string g_err;
 
 int fail(int code, const std::string &m)
@@ -122,21 +137,16 @@ int fail(int code, const std::string &m)
     return code;
 }
 
-// Device address of the scratch array for the current device (looked up once per device).
+// Device address of the scratch array in the current device's current context.  Looked up on
+// every call: the lookup allocates nothing, and an address cached across a device reset or a
+// change of context would point at memory that no longer holds the array.
 int scratch_address(double **out)
 {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return fail(GOPF_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return fail(GOPF_ERR_UNSUPPORTED, "device index out of range");
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return fail(GOPF_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        g_addr[dev] = (double *)p;
-    }
-    *out = g_addr[dev];
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+        return fail(GOPF_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    *out = (double *)p;
     return GOPF_OK;
 }
 

@@ -64,12 +64,20 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
 }
 
 // Wait for a TMA load's barrier.  On timeout: flag the status word, wait once
-// more (bounded) for the copy still in flight, and report failure so the
-// caller returns without touching the tile.
+// more (bounded by the built-in 2 s) for the copy still in flight, and report
+// failure so the caller returns without touching the tile.  The first wait's
+// limit is the unsigned long long at status + 2 when it is non-zero (a context
+// option, GOPF_OPT_WAIT_LIMIT_NS), else 2 s; the second wait never shortens, so
+// a block leaves only after its copy has landed.
 __device__ __forceinline__ bool tma_wait_or_flag(uint64_t *bar, uint32_t parity, unsigned *status)
 {
     const unsigned long long lim = 2000000000ull; // 2 s: orders of magnitude above a 32 KB copy
-    if (mbar_wait_bounded(bar, parity, lim)) return true;
+    unsigned long long first = lim;
+    if (status) {
+        const unsigned long long l = *reinterpret_cast<const volatile unsigned long long *>(status + 2);
+        if (l) first = l;
+    }
+    if (mbar_wait_bounded(bar, parity, first)) return true;
     if (status) atomicOr(status, (unsigned)DS_TMA_TIMEOUT);
     mbar_wait_bounded(bar, parity, lim);
     return false;

@@ -2,8 +2,8 @@
  * gopf_gpu.h -- C ABI of the GB300 spectral time stepper.
  *
  * This is the drop-in boundary for gopf's hot path.  A Go program binds it
- * with cgo and gets a pf.TimeStepper whose fields stay
- * resident in device memory between steps.  Every entry point returns an
+ * with cgo and gets a pf.TimeStepper whose fields stay resident in device
+ * memory between steps.  Every entry point returns an
  * int status (GOPF_OK == 0); nothing throws or aborts across the ABI.  Host
  * pointers are borrowed for the duration of the call only.  A context is not
  * thread-safe: calls on one context must be serialised by the caller.  Each
@@ -98,8 +98,13 @@ enum {
                                   per block (default), 2 also the persistent double-buffered z pass */
     GOPF_OPT_PLANE = 4,        /* 1: consecutive FP32 Euler steps on 256 x 256 x Z grids do the inverse y,
                                   x and forward y passes of each depth plane in one cluster launch */
-    GOPF_OPT_DIRECT_HOST = 5   /* 1 (default): pinned host buffers given to upload/download are read and
+    GOPF_OPT_DIRECT_HOST = 5,  /* 1 (default): pinned host buffers given to upload/download are read and
                                   written by kernels in place; pageable buffers are staged */
+    GOPF_OPT_WAIT_LIMIT_NS = 6 /* limit (ns) of a kernel's first wait for a tile copy; 0 (default) = 2 s.
+                                  A wait that runs out flags the step (GOPF_ERR_TIMEOUT from gopf_step or
+                                  gopf_synchronize), waits up to 2 s more for the copy still in flight and
+                                  leaves the tile alone, so the field must be uploaded again.  Meant for
+                                  testing that error path; the reference has no counterpart. */
 };
 
 #define GOPF_MAX_FACTORS 8
@@ -216,6 +221,12 @@ int gopf_field_upload_real(gopf_ctx *ctx, int field_id, const double *data, size
 int gopf_field_download_real(gopf_ctx *ctx, int field_id, double *data, size_t n);
 /* Solver.Propagate(nsteps): nsteps steps plus the per-step OnStepFinished hooks of device terms. */
 int gopf_step(gopf_ctx *ctx, long long nsteps);
+/* Capture the CUDA graphs that gopf_step(ctx, nsteps) replays without running any step, so that a
+ * later timed or latency-critical gopf_step pays no capture.  Host-driven steppers (ImplicitEuler,
+ * SDD) and contexts with graphs switched off have nothing to prepare; an elastic model prepares
+ * after its first step (that step sees the reference's zero h-field and is not replayed).  No
+ * counterpart in the reference (pf.Solver has no set-up phase). */
+int gopf_prepare_graphs(gopf_ctx *ctx, long long nsteps);
 int gopf_get_time(gopf_ctx *ctx, double *t);
 int gopf_get_step(gopf_ctx *ctx, long long *step);
 int gopf_synchronize(gopf_ctx *ctx);
@@ -308,13 +319,19 @@ int gopf_batch_kernels_per_step(gopf_batch *batch, int *n);
  * that manages all device memory itself, an allocator budget enforced outside CUDA,
  * a pool that must not be touched).  Reduces a real FP64 field the caller holds in
  * device memory; out receives, on the host, {sum, sum of squares, min, max,
- * non-finite count} as gopf_reduce reports them.  Its only scratch is a static
- * device array of GOPF_NOALLOC_MAX_BLOCKS + 1 rows of 8 doubles (about 1 MiB per GPU
- * that loads the library, held until exit), so n is limited to
- * GOPF_NOALLOC_MAX_BLOCKS * 4096 elements; larger n returns GOPF_ERR_ARG.  The first
- * call on a device looks the scratch address up and should come before any stream
- * capture.  Calls share the scratch: calls that overlap on the GPU race and must be
- * serialised by the caller.  stream may be NULL (the default stream). */
+ * non-finite count}.  Sums are compensated (Neumaier) as in gopf_reduce, so for a
+ * finite field the values agree with gopf_reduce's within rounding.  Non-finite
+ * cells: the count is exact, min and max skip NaN (IEEE fmin/fmax) but see +-Inf, and
+ * the sums follow IEEE arithmetic (a context cannot hold a single non-finite cell:
+ * its spectral state turns every cell non-finite, so gopf_reduce counts them all).
+ * Its only scratch is a static device array of GOPF_NOALLOC_MAX_BLOCKS + 1 rows of
+ * 8 doubles (about 1 MiB per GPU that loads the library, held until exit), so n is
+ * limited to GOPF_NOALLOC_MAX_BLOCKS * 4096 elements; larger n returns GOPF_ERR_ARG.
+ * Each call looks the scratch address up with the caller's device current; the first
+ * call on a device also loads the device code and should come before any stream
+ * capture.  The call is synchronous: it returns once the result is on the host.
+ * Calls share the scratch: calls that overlap on the GPU race and must be serialised
+ * by the caller.  stream may be NULL (the default stream). */
 #define GOPF_NOALLOC_MAX_BLOCKS 16384
 int gopf_reduce_noalloc(const double *field, size_t n, double *out, void *cuda_stream);
 const char *gopf_noalloc_last_error(void);
