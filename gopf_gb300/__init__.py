@@ -357,6 +357,23 @@ class Model:
         self._ck(self._L.gopf_reduce(self._h, field, what, ctypes.byref(out)))
         return out.value
 
+    def free_energy(self, field: int = 0, coefs=(0.0, 0.0, -0.5, 0.0, 0.25), kappa: float = 1.0):
+        """(bulk, gradient, total) of sum_cells sum_p coefs[p] c^p + (kappa/2) sum_cells |grad c|^2 on the
+        device; the defaults with kappa = gamma are the Cahn-Hilliard free energy."""
+        c = np.ascontiguousarray(coefs, dtype=np.float64)
+        out = np.empty(3)
+        self._ck(self._L.gopf_free_energy(self._h, field, _dptr(c), int(c.size), float(kappa), _dptr(out)))
+        return float(out[0]), float(out[1]), float(out[2])
+
+    def elastic_energy(self, C, misfit, field: int = 0, indicator: bool = False) -> float:
+        """HomogeneousModulusEnergy (elasticity/linearElasticity.go:101-165) of the field, or of its
+        Indicator 3c^2 - 2c^3, on the device."""
+        c = np.ascontiguousarray(C, dtype=np.float64).reshape(81)
+        m = np.ascontiguousarray(misfit, dtype=np.float64).reshape(9)
+        out = ctypes.c_double()
+        self._ck(self._L.gopf_elastic_energy(self._h, field, int(indicator), _dptr(c), _dptr(m), ctypes.byref(out)))
+        return out.value
+
     def volcons_multiplier(self) -> float:
         """VolumeConservingLP.Multiplier after the steps taken so far."""
         out = ctypes.c_double()

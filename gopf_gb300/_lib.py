@@ -92,6 +92,8 @@ SIGNATURES = {
     "gopf_synchronize": ([_vp], _i),
     "gopf_reduce": ([_vp, _i, _i, _dp], _i),
     "gopf_point_values": ([_vp, _i, ctypes.POINTER(_ll), _i, _dp], _i),
+    "gopf_free_energy": ([_vp, _i, _dp, _i, ctypes.c_double, _dp], _i),
+    "gopf_elastic_energy": ([_vp, _i, _i, _dp, _dp, _dp], _i),
     "gopf_add_source": ([_vp, _i, _dp, _i, _ip], _i),
     "gopf_set_source_amplitudes": ([_vp, _dp, _i, _i], _i),
     "gopf_sdd_init": ([_vp, _dp, _dp, _sz], _i),
@@ -128,6 +130,7 @@ SIGNATURES = {
     "gopf_batch_set_stream": ([_vp, _vp], _i),
     "gopf_batch_step": ([_vp, _ll], _i),
     "gopf_batch_kernels_per_step": ([_vp, _ip], _i),
+    "gopf_sweep_partition": ([ctypes.POINTER(_ll), _i, _i, _ip, ctypes.POINTER(_ll)], _i),
 }
 
 _lib = None

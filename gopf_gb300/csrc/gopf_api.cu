@@ -281,10 +281,12 @@ int gopf_ie_step(gopf_ctx *ctx);
 void gopf_sdd_free(gopf_ctx *ctx);
 int gopf_sdd_step(gopf_ctx *ctx, long long nsteps);
 void gopf_io_free(gopf_ctx *ctx);
+void gopf_energy_free(gopf_ctx *ctx);
 
 static void ctx_free(gopf_ctx *ctx)
 {
     gopf_io_free(ctx);
+    gopf_energy_free(ctx);
     gopf_ie_free(ctx);
     gopf_sdd_free(ctx);
     if (ctx->gexec1) cudaGraphExecDestroy(ctx->gexec1);

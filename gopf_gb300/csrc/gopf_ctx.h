@@ -71,6 +71,7 @@ struct gopf_special {
 struct gopf_ie_work;
 struct gopf_sdd_work;
 struct gopf_io_state;
+struct gopf_energy_work;
 
 struct gopf_ctx {
     int device = 0;
@@ -215,6 +216,7 @@ struct gopf_ctx {
     long long sdd_step = 0; // SDD.CurrentStep
     gopf_sdd_work *sdd = nullptr;
     gopf_io_state *io = nullptr; // field files: pinned staging buffer and writer thread
+    gopf_energy_work *energy = nullptr; // energy monitors (gopf_energy.cu): work buffers
     std::string err;
 };
 

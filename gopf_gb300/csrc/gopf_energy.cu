@@ -1,0 +1,482 @@
+// gopf_energy.cu -- energy monitors of a device-resident field.
+//
+// gopf's solver runs its monitors once per epoch on host fields
+// (pf/solver.go:110-117, the Monitor interface of pf/monitor.go:4-6).  These
+// two monitors run on the device instead, on the field where it lives, and
+// return a few FP64 numbers:
+//
+// * gopf_free_energy: F = sum_cells sum_p a_p c^p + (kappa/2) sum_cells |grad c|^2.
+//   The gradient part comes from the half spectrum by Parseval,
+//   sum_cells |grad c|^2 = (1/N) sum_k |k|^2 |c-hat(k)|^2 with k = 2 pi Freq (the
+//   symbol the model's LAP uses, pf/diffOp.go:25-30, Nyquist at +1/2), each
+//   stored half-spectrum mode counted twice unless it is its own partner
+//   (kx = 0 or kx = X/2).  With a = (0, 0, -1/2, 0, 1/4) and kappa = gamma this
+//   is the Cahn-Hilliard free energy whose variational derivative is the
+//   chemical potential of examples/cahnHilliard/main.go:33.
+//
+// * gopf_elastic_energy: elasticity.HomogeneousModulusEnergy
+//   (elasticity/linearElasticity.go:101-165) of an indicator x (the field, or
+//   3c^2 - 2c^3 of it): the effective force of the misfit stress A = C:eps*
+//   (elasticity/effectiveForce.go:26-35), the displacement solve
+//   (Displacements, :33-63, no Nyquist zeroing), the six strains (Strain,
+//   :67-83, Nyquist components of f zeroed), the misfit subtracted where the
+//   indicator exceeds 1/2, the energy density (:86-98) summed and divided by
+//   sum x.  Every strain is linear in x-hat: eps-hat_mn(k) = x-hat(k) s_mn(k),
+//   s_mn = (f~_n v_m + f~_m v_n)/2, v = Gamma'(f)^-1 A f,
+//   Gamma'_mn = sum_jl C_mjnl f_j f_l.  The reference keeps real(IFFT(.)), which
+//   for a real x is the inverse transform of the part of x-hat s that is
+//   Hermitian, i.e. of x-hat (s(k) + s(-k))/2: the symbol is symmetrised here so
+//   the strains can use the real-to-complex passes.
+//
+// All sums are FP64 with Neumaier compensation; the fields and transforms are
+// in the context's precision.  Work buffers are allocated on the first call
+// and kept with the context.
+#include <cmath>
+#include <cstring>
+
+#include "gopf_ctx.h"
+#include "gopf_kernels.cuh"
+
+using namespace gopf;
+
+struct gopf_energy_work {
+    double *part = nullptr; // block partials [EN_BLOCKS][EN_SLOTS]
+    double *out = nullptr;  // finished sums [EN_SLOTS]
+    void *xh = nullptr;     // half spectrum of the indicator
+    void *bh = nullptr;     // half spectrum of one strain component
+    void *ind = nullptr;    // real indicator (N)
+    void *strain = nullptr; // six real strain fields (6 N)
+};
+
+int gopf_field_to_real(gopf_ctx *ctx, int f, void *dst);
+
+namespace {
+
+constexpr int EN_BLOCKS = 152 * 8;
+constexpr int EN_SLOTS = 4;
+constexpr int EN_THREADS = 256;
+constexpr int EN_MAX_DEG = 12;
+
+__device__ __forceinline__ void nadd(double &s, double &c, double v)
+{
+    const double t = s + v;
+    c += (fabs(s) >= fabs(v)) ? (s - t) + v : (v - t) + s;
+    s = t;
+}
+
+// Block-wide compensated sum of (s, c) per slot; thread 0 writes part[blockIdx.x][slot].
+template <int NS> __device__ void block_store(double (&s)[NS], double (&c)[NS], double *part)
+{
+    __shared__ double sh_s[EN_THREADS / 32][NS], sh_c[EN_THREADS / 32][NS];
+    for (int k = 0; k < NS; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            const double so = __shfl_xor_sync(0xffffffffu, s[k], o), co = __shfl_xor_sync(0xffffffffu, c[k], o);
+            c[k] += co;
+            nadd(s[k], c[k], so);
+        }
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0)
+        for (int k = 0; k < NS; ++k) {
+            sh_s[w][k] = s[k];
+            sh_c[w][k] = c[k];
+        }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int k = 0; k < NS; ++k) {
+            double ss = 0.0, cc = 0.0;
+            for (int q = 0; q < EN_THREADS / 32; ++q) {
+                cc += sh_c[q][k];
+                nadd(ss, cc, sh_s[q][k]);
+            }
+            part[(long long)blockIdx.x * EN_SLOTS + k] = ss + cc;
+        }
+}
+
+struct BulkPoly {
+    int deg;
+    double a[EN_MAX_DEG + 1];
+};
+
+// slot 0: sum of the polynomial, slot 1: sum of x, slot 2: non-finite cells
+template <typename R> __global__ void k_bulk(const R *__restrict__ x, long long n, BulkPoly p, double *__restrict__ part)
+{
+    double s[3] = {0.0, 0.0, 0.0}, c[3] = {0.0, 0.0, 0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double v = (double)x[i];
+        double h = p.a[p.deg];
+        for (int q = p.deg - 1; q >= 0; --q) h = fma(h, v, p.a[q]);
+        nadd(s[0], c[0], h);
+        nadd(s[1], c[1], v);
+        s[2] += isfinite(v) ? 0.0 : 1.0;
+    }
+    block_store<3>(s, c, part);
+}
+
+__device__ __forceinline__ double fold(long long i, long long n)
+{
+    const double f = (double)i / (double)n;
+    return (f > 0.5) ? f - 1.0 : f;
+}
+
+// slot 0: sum over the full spectrum of |f|^2 |c-hat|^2 (f in cycles per sample)
+template <typename V> __global__ void k_grad(const V *__restrict__ st, Geom g, double *__restrict__ part)
+{
+    double s[1] = {0.0}, c[1] = {0.0};
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < g.C;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long z = idx / g.S, rem = idx - z * g.S;
+        const long long kx = rem / g.Y, y = rem - kx * g.Y;
+        const double fr = fold(y, g.Y), fc = fold(kx, g.X), fd = fold(z, g.Z);
+        const double w = (kx == 0 || 2 * kx == g.X) ? 1.0 : 2.0;
+        const V v = st[idx];
+        const double a = (double)v.x, b = (double)v.y;
+        nadd(s[0], c[0], w * (fr * fr + fc * fc + fd * fd) * (a * a + b * b));
+    }
+    block_store<1>(s, c, part);
+}
+
+// one block: compensated sums of the block partials, slot by slot
+__global__ void k_finish(const double *__restrict__ part, int nblocks, double *__restrict__ out)
+{
+    __shared__ double sh_s[EN_THREADS], sh_c[EN_THREADS];
+    for (int k = 0; k < EN_SLOTS; ++k) {
+        double s = 0.0, c = 0.0;
+        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) nadd(s, c, part[(long long)b * EN_SLOTS + k]);
+        sh_s[threadIdx.x] = s;
+        sh_c[threadIdx.x] = c;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double ss = 0.0, cc = 0.0;
+            for (int q = 0; q < (int)blockDim.x; ++q) {
+                cc += sh_c[q];
+                nadd(ss, cc, sh_s[q]);
+            }
+            out[k] = ss + cc;
+        }
+        __syncthreads();
+    }
+}
+
+template <typename R> __global__ void k_indicator(R *__restrict__ x, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double v = (double)x[i];
+        x[i] = (R)(3.0 * v * v - 2.0 * v * v * v); // Indicator, pf/homoLinElast.go:10-12
+    }
+}
+
+struct StrainParams {
+    double C[81];
+    double A[9];     // C : misfit
+    double mis[9];   // misfit strain
+    int m, n;        // strain component of k_strain
+    double scale;    // 1/N
+};
+
+// v = Gamma'(f)^-1 A f (0 at f = 0, as Displacements leaves the zero mode), Gaussian elimination
+// with partial pivoting
+__device__ void disp_dir(const StrainParams &p, const double f[3], double v[3])
+{
+    const double tol = 1e-10;
+    v[0] = v[1] = v[2] = 0.0;
+    if (fabs(f[0]) < tol && fabs(f[1]) < tol && fabs(f[2]) < tol) return;
+    double G[3][3], b[3];
+    for (int m = 0; m < 3; ++m) {
+        for (int n = 0; n < 3; ++n) {
+            double e = 0.0;
+            for (int j = 0; j < 3; ++j)
+                for (int l = 0; l < 3; ++l) e += p.C[m * 27 + j * 9 + n * 3 + l] * f[j] * f[l];
+            G[m][n] = e;
+        }
+        b[m] = p.A[m * 3 + 0] * f[0] + p.A[m * 3 + 1] * f[1] + p.A[m * 3 + 2] * f[2];
+    }
+    for (int c = 0; c < 3; ++c) {
+        int best = c;
+        for (int r = c + 1; r < 3; ++r)
+            if (fabs(G[r][c]) > fabs(G[best][c])) best = r;
+        if (best != c) {
+            for (int k = 0; k < 3; ++k) {
+                const double t = G[c][k];
+                G[c][k] = G[best][k];
+                G[best][k] = t;
+            }
+            const double t = b[c];
+            b[c] = b[best];
+            b[best] = t;
+        }
+        for (int r = c + 1; r < 3; ++r) {
+            const double fct = G[r][c] / G[c][c];
+            for (int k = c; k < 3; ++k) G[r][k] -= fct * G[c][k];
+            b[r] -= fct * b[c];
+        }
+    }
+    for (int r = 2; r >= 0; --r) {
+        double s = b[r];
+        for (int q = r + 1; q < 3; ++q) s -= G[r][q] * v[q];
+        v[r] = s / G[r][r];
+    }
+}
+
+__device__ double strain_symbol(const StrainParams &p, const double f[3])
+{
+    double v[3];
+    disp_dir(p, f, v);
+    const double tol = 1e-10;
+    const double fm = (fabs(fabs(f[p.m]) - 0.5) < tol) ? 0.0 : f[p.m];
+    const double fn = (fabs(fabs(f[p.n]) - 0.5) < tol) ? 0.0 : f[p.n];
+    return 0.5 * (fn * v[p.m] + fm * v[p.n]);
+}
+
+// out = x-hat * (s_mn(k) + s_mn(-k)) / 2 / N
+template <typename V> __global__ void k_strain(const V *__restrict__ xh, Geom g, int ndim, StrainParams p, V *__restrict__ out)
+{
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < g.C;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long z = idx / g.S, rem = idx - z * g.S;
+        const long long kx = rem / g.Y, y = rem - kx * g.Y;
+        // the reference's order: f[0] row, f[1] col, f[2] depth (0 in 2D: its 3-vector wrapper)
+        const double f[3] = {fold(y, g.Y), fold(kx, g.X), ndim == 3 ? fold(z, g.Z) : 0.0};
+        const double fmk[3] = {fold((g.Y - y) % g.Y, g.Y), fold((g.X - kx) % g.X, g.X),
+                               ndim == 3 ? fold((g.Z - z) % g.Z, g.Z) : 0.0};
+        const double s = 0.5 * (strain_symbol(p, f) + strain_symbol(p, fmk)) * p.scale;
+        V v = xh[idx];
+        v.x = (decltype(v.x))((double)v.x * s);
+        v.y = (decltype(v.y))((double)v.y * s);
+        out[idx] = v;
+    }
+}
+
+// slot 0: sum of the energy density, slot 1: sum of x; components in the order 00 01 02 11 12 22
+template <typename R>
+__global__ void k_elastic_density(const R *__restrict__ x, const R *__restrict__ strain, long long n, StrainParams p,
+                                  double *__restrict__ part)
+{
+    double s[2] = {0.0, 0.0}, c[2] = {0.0, 0.0};
+    const int ci[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double xv = (double)x[i];
+        const bool inside = xv > 0.5;
+        double e[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) e[q] = (double)strain[q * n + i];
+        double E[3][3];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) E[a][b] = e[ci[a][b]] - (inside ? p.mis[a * 3 + b] : 0.0);
+        double d = 0.0;
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                double t = 0.0;
+                for (int k = 0; k < 3; ++k)
+                    for (int l = 0; l < 3; ++l) t += p.C[a * 27 + b * 9 + k * 3 + l] * E[k][l];
+                d += E[a][b] * t;
+            }
+        nadd(s[0], c[0], 0.5 * d);
+        nadd(s[1], c[1], xv);
+    }
+    block_store<2>(s, c, part);
+}
+
+int ck(gopf_ctx *ctx, cudaError_t e, const char *where)
+{
+    if (e == cudaSuccess) return GOPF_OK;
+    return gopf_fail(ctx, e == cudaErrorMemoryAllocation ? GOPF_ERR_OOM : GOPF_ERR_CUDA,
+                     std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+int prepare(gopf_ctx *ctx, int field)
+{
+    if (!ctx) return GOPF_ERR_ARG;
+    if (ctx->device < 0) return gopf_fail(ctx, GOPF_ERR_STATE, "host-only context (device < 0)");
+    if (field < 0 || (ctx->nfields > 0 && field >= ctx->nfields) || (ctx->nfields == 0 && field != 0))
+        return gopf_fail(ctx, GOPF_ERR_ARG, "bad field id");
+    if (!ctx->state_valid) return gopf_fail(ctx, GOPF_ERR_STATE, "field has not been uploaded");
+    int rc;
+    if ((rc = ck(ctx, cudaSetDevice(ctx->device), "cudaSetDevice"))) return rc;
+    if (!ctx->energy) ctx->energy = new gopf_energy_work();
+    gopf_energy_work *w = ctx->energy;
+    if (!w->part) {
+        if ((rc = ck(ctx, gopf_malloc(&w->part, sizeof(double) * EN_BLOCKS * EN_SLOTS), "gopf_malloc"))) return rc;
+        if ((rc = ck(ctx, gopf_malloc(&w->out, sizeof(double) * EN_SLOTS), "gopf_malloc"))) return rc;
+        ctx->dev_bytes += sizeof(double) * (EN_BLOCKS + 1) * EN_SLOTS;
+    }
+    return GOPF_OK;
+}
+
+unsigned grid_for(long long n) { return (unsigned)std::min<long long>((n + EN_THREADS - 1) / EN_THREADS, EN_BLOCKS); }
+
+// finish the partials of the last kernel and copy the sums to the host (stream-synchronising)
+int finish(gopf_ctx *ctx, double *host)
+{
+    gopf_energy_work *w = ctx->energy;
+    k_finish<<<1, EN_THREADS, 0, ctx->stream>>>(w->part, EN_BLOCKS, w->out);
+    int rc;
+    if ((rc = ck(ctx, cudaGetLastError(), "finish"))) return rc;
+    if ((rc = ck(ctx, cudaMemcpyAsync(host, w->out, sizeof(double) * EN_SLOTS, cudaMemcpyDeviceToHost, ctx->stream),
+                 "D2H")))
+        return rc;
+    return ck(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+}
+
+template <typename R> XPassArgs<R> xbase(gopf_ctx *ctx)
+{
+    typedef typename VecOf<R>::type V;
+    XPassArgs<R> a;
+    memset(&a, 0, sizeof(a));
+    a.g = ctx->g;
+    a.planH = ctx->planH;
+    a.twX = (const V *)ctx->d_twX;
+    a.allow_fast = ctx->use_fast;
+    a.status = ctx->d_status;
+    return a;
+}
+
+template <typename R> PassArgs<R> pbase(gopf_ctx *ctx, bool zaxis, int mode, void *buf)
+{
+    typedef typename VecOf<R>::type V;
+    PassArgs<R> a;
+    memset(&a, 0, sizeof(a));
+    a.g = ctx->g;
+    a.plan = zaxis ? ctx->planZ : ctx->planY;
+    a.tw = (const V *)(zaxis ? ctx->d_twZ : ctx->d_twY);
+    a.mode = mode;
+    a.buf[0] = (V *)buf;
+    a.nbuf = 1;
+    a.allow_fast = ctx->use_fast;
+    a.status = ctx->d_status;
+    return a;
+}
+
+template <typename R> int free_energy_impl(gopf_ctx *ctx, int field, const BulkPoly &p, double kappa, double *out3)
+{
+    typedef typename VecOf<R>::type V;
+    const Geom &g = ctx->g;
+    gopf_energy_work *w = ctx->energy;
+    int rc;
+    if ((rc = gopf_field_to_real(ctx, field, ctx->d_real))) return rc;
+    k_bulk<R><<<EN_BLOCKS, EN_THREADS, 0, ctx->stream>>>((const R *)ctx->d_real, g.N, p, w->part);
+    if ((rc = ck(ctx, cudaGetLastError(), "bulk sums"))) return rc;
+    double bulk[EN_SLOTS];
+    if ((rc = finish(ctx, bulk))) return rc;
+    k_grad<V><<<EN_BLOCKS, EN_THREADS, 0, ctx->stream>>>((const V *)field_state(ctx, field), g, w->part);
+    if ((rc = ck(ctx, cudaGetLastError(), "gradient sums"))) return rc;
+    double grad[EN_SLOTS];
+    if ((rc = finish(ctx, grad))) return rc;
+    const double fourpi2 = 39.47841760435743;
+    out3[0] = bulk[0];
+    out3[1] = 0.5 * kappa * fourpi2 * grad[0] / (double)g.N;
+    out3[2] = out3[0] + out3[1];
+    if (bulk[2] != 0.0) return gopf_fail(ctx, GOPF_ERR_NAN, "the field holds non-finite values");
+    return GOPF_OK;
+}
+
+template <typename R> int elastic_energy_impl(gopf_ctx *ctx, int field, int indicator, StrainParams p, double *out)
+{
+    typedef typename VecOf<R>::type V;
+    const Geom &g = ctx->g;
+    gopf_energy_work *w = ctx->energy;
+    int rc;
+    if (!w->xh) {
+        if ((rc = ck(ctx, gopf_malloc(&w->xh, sizeof(V) * g.C), "gopf_malloc"))) return rc;
+        if ((rc = ck(ctx, gopf_malloc(&w->bh, sizeof(V) * g.C), "gopf_malloc"))) return rc;
+        if ((rc = ck(ctx, gopf_malloc(&w->ind, sizeof(R) * g.N), "gopf_malloc"))) return rc;
+        if ((rc = ck(ctx, gopf_malloc(&w->strain, sizeof(R) * 6 * g.N), "gopf_malloc"))) return rc;
+        ctx->dev_bytes += 2 * sizeof(V) * g.C + 7 * sizeof(R) * g.N;
+    }
+    // the indicator x in real space
+    if ((rc = gopf_field_to_real(ctx, field, w->ind))) return rc;
+    if (indicator) {
+        k_indicator<R><<<grid_for(g.N), EN_THREADS, 0, ctx->stream>>>((R *)w->ind, g.N);
+        if ((rc = ck(ctx, cudaGetLastError(), "indicator"))) return rc;
+    }
+    // x-hat
+    XPassArgs<R> xa = xbase<R>(ctx);
+    xa.in_mode = XIN_REAL;
+    xa.rin = (const R *)w->ind;
+    xa.out[0] = (V *)w->xh;
+    xa.ngrp_out = 1;
+    xa.identity = 1;
+    if ((rc = ck(ctx, launch_xpass<R>(xa, ctx->LBx, ctx->stream), "x pass"))) return rc;
+    if ((rc = ck(ctx, launch_cpass<R>(pbase<R>(ctx, false, PM_FWD, w->xh), ctx->LBy, ctx->stream), "y pass"))) return rc;
+    if (g.Z > 1 &&
+        (rc = ck(ctx, launch_spass<R>(pbase<R>(ctx, true, PM_FWD, w->xh), ctx->LBz, ctx->stream), "z pass")))
+        return rc;
+    // the six strains: symbol times x-hat / N, then the inverse transform to real rows
+    const int comps[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
+    p.scale = 1.0 / (double)g.N;
+    for (int q = 0; q < 6; ++q) {
+        p.m = comps[q][0];
+        p.n = comps[q][1];
+        k_strain<V><<<grid_for(g.C), EN_THREADS, 0, ctx->stream>>>((const V *)w->xh, g, ctx->ndim, p, (V *)w->bh);
+        if ((rc = ck(ctx, cudaGetLastError(), "strain symbol"))) return rc;
+        if (g.Z > 1 &&
+            (rc = ck(ctx, launch_spass<R>(pbase<R>(ctx, true, PM_INV, w->bh), ctx->LBz, ctx->stream), "z pass")))
+            return rc;
+        if ((rc = ck(ctx, launch_cpass<R>(pbase<R>(ctx, false, PM_INV, w->bh), ctx->LBy, ctx->stream), "y pass")))
+            return rc;
+        XPassArgs<R> xo = xbase<R>(ctx);
+        xo.in_mode = XIN_SPECTRAL;
+        xo.in = (const V *)w->bh;
+        xo.rout = (R *)w->strain + (long long)q * g.N;
+        if ((rc = ck(ctx, launch_xpass<R>(xo, ctx->LBx, ctx->stream), "x pass"))) return rc;
+    }
+    k_elastic_density<R><<<EN_BLOCKS, EN_THREADS, 0, ctx->stream>>>((const R *)w->ind, (const R *)w->strain, g.N, p,
+                                                                     w->part);
+    if ((rc = ck(ctx, cudaGetLastError(), "energy density"))) return rc;
+    double sums[EN_SLOTS];
+    if ((rc = finish(ctx, sums))) return rc;
+    if (!(sums[1] != 0.0)) return gopf_fail(ctx, GOPF_ERR_ARG, "the indicator sums to zero (no volume)");
+    *out = sums[0] / sums[1];
+    return GOPF_OK;
+}
+
+} // namespace
+
+void gopf_energy_free(gopf_ctx *ctx)
+{
+    gopf_energy_work *w = ctx->energy;
+    if (!w) return;
+    void *ptrs[] = {w->part, w->out, w->xh, w->bh, w->ind, w->strain};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    delete w;
+    ctx->energy = nullptr;
+}
+
+extern "C" int gopf_free_energy(gopf_ctx *ctx, int field, const double *coefs, int ncoefs, double kappa, double *out3)
+{
+    int rc;
+    if ((rc = prepare(ctx, field))) return rc;
+    if (!out3 || (ncoefs > 0 && !coefs)) return gopf_fail(ctx, GOPF_ERR_ARG, "null argument");
+    if (ncoefs < 0 || ncoefs > EN_MAX_DEG + 1)
+        return gopf_fail(ctx, GOPF_ERR_ARG, "the bulk polynomial takes 0 to 13 coefficients (degree <= 12)");
+    BulkPoly p;
+    memset(&p, 0, sizeof(p));
+    p.deg = ncoefs > 0 ? ncoefs - 1 : 0;
+    for (int q = 0; q < ncoefs; ++q) p.a[q] = coefs[q];
+    gopf_nvtx_scope trace("gopf_free_energy");
+    return (ctx->prec == GOPF_FP32) ? free_energy_impl<float>(ctx, field, p, kappa, out3)
+                                    : free_energy_impl<double>(ctx, field, p, kappa, out3);
+}
+
+extern "C" int gopf_elastic_energy(gopf_ctx *ctx, int field, int indicator, const double *C81, const double *misfit9,
+                                   double *out)
+{
+    int rc;
+    if ((rc = prepare(ctx, field))) return rc;
+    if (!C81 || !misfit9 || !out) return gopf_fail(ctx, GOPF_ERR_ARG, "null argument");
+    StrainParams p;
+    memset(&p, 0, sizeof(p));
+    memcpy(p.C, C81, sizeof(p.C));
+    memcpy(p.mis, misfit9, sizeof(p.mis));
+    for (int i = 0; i < 3; ++i) // A = C : misfit (Rank4.ContractLast, elasticity/rank4.go:62-75)
+        for (int j = 0; j < 3; ++j) {
+            double a = 0.0;
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) a += C81[i * 27 + j * 9 + k * 3 + l] * misfit9[k * 3 + l];
+            p.A[i * 3 + j] = a;
+        }
+    gopf_nvtx_scope trace("gopf_elastic_energy");
+    return (ctx->prec == GOPF_FP32) ? elastic_energy_impl<float>(ctx, field, indicator != 0, p, out)
+                                    : elastic_energy_impl<double>(ctx, field, indicator != 0, p, out);
+}

@@ -27,6 +27,8 @@
  *   Field.Data access (host <-> device)   -> gopf_field_upload / gopf_field_download
  *   mass check pf/solver_test.go:20-27 -> gopf_reduce
  *   PointMonitor pf/monitor.go:8-30       -> gopf_point_values
+ *   Monitor pf/monitor.go:4-6, HomogeneousModulusEnergy elasticity/linearElasticity.go:101-165
+ *                                         -> gopf_free_energy / gopf_elastic_energy
  *   Model.AddSource / Source pf/model.go:152-154, pf/sourceTerm.go:14-30 -> gopf_add_source
  */
 #ifndef GOPF_GPU_H
@@ -279,6 +281,23 @@ int gopf_reduce(gopf_ctx *ctx, int field_id, int what, double *out);
  * being node indices (pfutil/indexPositionConversion.go:23-34).  Only the n values cross the bus. */
 int gopf_point_values(gopf_ctx *ctx, int field_id, const long long *sites, int n, double *out);
 
+/* ---- energy monitors (the Monitor hook of pf/monitor.go:4-6, run per epoch by Solver.Solve,
+ * pf/solver.go:110-117), evaluated on the device-resident field ----
+ * gopf_free_energy: out3 = {bulk, gradient, total} of
+ *   F = sum_cells sum_p coefs[p] c^p + (kappa/2) sum_cells |grad c|^2
+ * (0 <= ncoefs <= 13), the gradient part from the spectrum with |k|^2 = 4 pi^2 |Freq|^2, the symbol
+ * the model's LAP uses.  coefs = {0, 0, -1/2, 0, 1/4} and kappa = gamma give the free energy of the
+ * Cahn-Hilliard string of examples/cahnHilliard/main.go:33.  FP64 compensated sums; GOPF_ERR_NAN
+ * when the field holds non-finite values.  No counterpart in the reference (its monitors are user
+ * code). */
+int gopf_free_energy(gopf_ctx *ctx, int field, const double *coefs, int ncoefs, double kappa, double *out3);
+/* elasticity.HomogeneousModulusEnergy (elasticity/linearElasticity.go:101-165) of the indicator x =
+ * the field (indicator == 0) or its Indicator 3c^2 - 2c^3 (indicator != 0, pf/homoLinElast.go:10-12):
+ * elastic energy over sum x, the misfit subtracted where x > 1/2.  C81 and misfit9 as in
+ * gopf_register_elastic.  FP64 sums; the transforms run in the context's precision. */
+int gopf_elastic_energy(gopf_ctx *ctx, int field, int indicator, const double *C81, const double *misfit9,
+                        double *out);
+
 /* ---- FourierTransform (pfutil/fftWrap.go) on host data, not a hot path ---- */
 /* sign -1: forward FFT, +1: unnormalised backward, of a []complex128 of length N. */
 int gopf_fft(gopf_ctx *ctx, int sign, double *data, size_t n);
@@ -313,6 +332,15 @@ const char *gopf_batch_last_error(const gopf_batch *batch);
 int gopf_batch_set_stream(gopf_batch *batch, void *cuda_stream);
 int gopf_batch_step(gopf_batch *batch, long long nsteps);
 int gopf_batch_kernels_per_step(gopf_batch *batch, int *n);
+
+/* ---- sweeps over several GPUs, one process each ----
+ * The sweep workflow (README.md:21-33) runs one pf.Solver per parameter set; its instances are
+ * independent, so processes split them with no exchange.  gopf_sweep_partition assigns instance i
+ * (cells[i] grid cells) to owner[i] in [0, world): greedy bin packing on cells, instances in
+ * decreasing size (ties: lower index) to the least-loaded rank (ties: lower rank).  Deterministic,
+ * so every process computes the same partition alone; rank_cells (world entries, may be NULL)
+ * receives each rank's total.  Host-only: needs no device. */
+int gopf_sweep_partition(const long long *cells, int n, int world, int *owner, long long *rank_cells);
 
 /* ---- reduction without device allocation (no counterpart in the reference) ----
  * For callers that cannot allocate device memory at the point of the call (a host

@@ -193,6 +193,26 @@ def num_threads() -> int:
     return int(lib().or_num_threads())
 
 
+def free_energy(field: np.ndarray, dims, coefs, kappa: float):
+    """(bulk, gradient) parts of F = sum_cells sum_p coefs[p] c^p + (kappa/2) sum_cells |grad c|^2 of a
+    real field in node order, the gradient through the spectrum with k = 2 pi Freq: the symbol of
+    LaplacianN (pf/diffOp.go:25-30) and the frequencies of pfutil/fftWrap.go:57-74 (Nyquist +1/2,
+    the same |k| either sign).  numpy, FP64; test infrastructure only."""
+    c = np.asarray(field, dtype=np.float64).reshape(-1)
+    bulk = float(np.polynomial.polynomial.polyval(c, np.asarray(coefs, dtype=np.float64)).sum())
+    shape = mem_shape(dims)
+    ch = np.fft.fftn(c.reshape(shape))
+    k2 = np.zeros(shape)
+    for ax, n in enumerate(shape):
+        f = np.fft.fftfreq(n)
+        f[np.isclose(f, -0.5)] = 0.5
+        sh = [1] * len(shape)
+        sh[ax] = n
+        k2 = k2 + (f.reshape(sh)) ** 2
+    grad = float(4.0 * np.pi ** 2 * (k2 * np.abs(ch) ** 2).sum() / c.size)
+    return bulk, 0.5 * kappa * grad
+
+
 def homogeneous_modulus_energy(indicator: np.ndarray, dims, misfit, C) -> float:
     ind = np.ascontiguousarray(indicator, dtype=np.complex128).copy()
     mis = np.ascontiguousarray(misfit, dtype=np.float64).reshape(9)
