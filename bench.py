@@ -214,8 +214,6 @@ def run_gpu(args):
     m = ch3d_model(G, "fp32", c0, local, stream)
     if args.tma is not None:
         m.set_option(G._lib.OPT_TMA, args.tma)
-    if args.plane is not None:
-        m.set_option(G._lib.OPT_PLANE, args.plane)
     mass0 = m.mass(0)
     m.prepare_graphs(args.steps)  # capture the graphs the timed steps replay (no stepping)
     m.step(warmup_steps(args))
@@ -454,13 +452,19 @@ def sweep_params(n=64, seed=2):
             for i in range(n)]
 
 
-def sweep_models(prec, params, fast=True, first=0):
+def sweep_models(prec, params, fast=True, first=0, indices=None, device=0):
+    """Contexts of the sweep instances `indices` (default: all of `params`, numbered from `first`);
+    instance i starts from c0 = 0.5 + U(-0.05, 0.05) with seed 1000 + i."""
     import gopf_gb300 as G
     from gopf_gb300.synthetic import uniform_field
 
+    if indices is None:
+        indices = list(range(first, first + len(params)))
+        params = dict(zip(indices, params))
     models = []
-    for i, (side, gamma, Mv) in enumerate(params):
-        m = G.Model([side, side], prec, device=0)
+    for i in indices:
+        side, gamma, Mv = params[i]
+        m = G.Model([side, side], prec, device=device)
         m.set_option(G._lib.OPT_FAST_KERNELS, int(fast))
         m.set_option(G._lib.OPT_CHECK_FINITE, 0)
         m.add_field("conc")
@@ -470,75 +474,120 @@ def sweep_models(prec, params, fast=True, first=0):
         m.add_equation("dconc/dt = M*LAP conc^3 + mM*LAP conc + mM*gamma*LAP^2 conc")
         m.init()
         m.set_stepper("euler", 0.05)
-        m.upload(0, uniform_field(1000 + first + i, side * side, 0.5, 0.05))
+        m.upload(0, uniform_field(1000 + i, side * side, 0.5, 0.05))
         models.append(m)
     return models
 
 
 def run_sweep(args):
-    """Batched parameter sweep: 64 independent 2D CH instances of uneven size, FP32, dt 0.05."""
+    """Batched parameter sweep: 64 independent 2D CH instances of uneven size, FP32, dt 0.05.
+    Under torchrun the instances are sharded over the ranks (gopf_sweep_partition: greedy bin
+    packing on cells, no collective on the data path); every rank steps its share as one batch and
+    the whole sweep's step time is the slowest rank's.  The total work is fixed (strong scaling)."""
     import torch
 
     import gopf_gb300 as G
+    from gopf_gb300 import sweep
 
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     params = sweep_params()
-    cells = sum(s * s for s, _, _ in params)
+    cells_of = [s * s for s, _, _ in params]
+    owner, rank_cells = sweep.partition(cells_of, world)
+    mine = [i for i, r in enumerate(owner) if r == rank]
+    cells = sum(cells_of)
     sweep_bytes = float(sum(6 * (s // 2 + 1) * s * 8 for s, _, _ in params))
-    models = sweep_models("fp32", params)
+    models = sweep_models("fp32", params, indices=mine, device=local)
     batch = G.Batch(models)
     stream = torch.cuda.Stream()
     batch.set_stream(stream.cuda_stream)
-    batch.step(max(args.warmup, 3))
+    warm = max(args.warmup, 3)
+    batch.step(max(warm, 16))  # warm-up: both graphs of the batch (1 and 16 steps) exist afterwards
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(0) as clk:
+    with ClockSampler(local) as clk:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
         e0.record(stream)
         batch.step(args.steps)
         e1.record(stream)
         torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
     ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
     batched = args.steps / (ms / 1000.0)
-    # sequential: every instance stepped by its own launches (own CUDA graphs)
-    seq_models = sweep_models("fp32", params)
-    for m in seq_models:
-        m.set_stream(stream.cuda_stream)
-        m.step(3)
-    torch.cuda.synchronize()
-    kseq = max(3, min(args.steps, 200))
-    e0.record(stream)
-    for _ in range(kseq):
+    seq = None
+    if world == 1:
+        # sequential: every instance stepped by its own launches (own CUDA graphs)
+        seq_models = sweep_models("fp32", params)
         for m in seq_models:
-            m.step(1)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    seq = kseq / (e0.elapsed_time(e1) / 1000.0)
-    out = {"metric": "sweep steps/s (64 uneven 2D CH instances, one step of all instances)", "value": batched,
-           "unit": "sweep-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
-           "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "f32", "data": "synthetic",
-           "config": {"workload": "sweep_64_ch2d_uneven_fp32", "sides": [p[0] for p in params], "cells": cells,
-                      "dt": 0.05, "params_seed": 2, "init": "c0 = 0.5 + U(-0.05, 0.05), seed 1000 + i"},
-           "sequential_value": seq, "speedup_vs_sequential": batched / seq,
-           # bytes one sweep step moves: per instance the x pass reads T and writes the group (2C),
-           # the fused y pass reads the group and c-hat and writes c-hat and T (4C); FP32, C = (X/2+1) Y 8 B
-           "step_bytes_moved": sweep_bytes,
-           "fraction_of_hbm": sweep_bytes * batched / (peaks()[0] * 1e9),
-           "cell_updates_per_s": batched * cells, "clocks": clk.summary(),
-           "gpu_launches": batch.kernels_per_step() * args.steps}
-    if args.check_steps > 0:
-        # per-instance rel-L2 of the FP32 batch against sequential FP64 runs after check_steps steps
-        a = sweep_models("fp32", params)
-        G.Batch(a).step(args.check_steps)
-        errs = []
-        for i, m in enumerate(a):
-            r = sweep_models("fp64", [params[i]], first=i)[0]
-            r.step(args.check_steps)
-            ref = r.download_real(0)
-            errs.append(float(np.linalg.norm(m.download_real(0) - ref) / np.linalg.norm(ref)))
-            r.close()
-        out["check"] = {"steps": args.check_steps, "rel_l2_max": max(errs), "rel_l2_median": float(np.median(errs)),
-                        "rel_l2": errs}
-    print(json.dumps(out))
+            m.set_stream(stream.cuda_stream)
+            m.step(3)
+        torch.cuda.synchronize()
+        kseq = max(3, min(args.steps, 200))
+        e0.record(stream)
+        for _ in range(kseq):
+            for m in seq_models:
+                m.step(1)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        seq = kseq / (e0.elapsed_time(e1) / 1000.0)
+        for m in seq_models:
+            m.close()
+    launches = batch.kernels_per_step() * args.steps
+    check = None
+    if args.check_steps != 0:
+        # per-instance rel-L2 of the FP32 batch against sequential FP64 runs, each rank checking its
+        # own instances; the results are merged on the host
+        S = args.check_steps if args.check_steps > 0 else 2000
+        a = sweep_models("fp32", params, indices=mine, device=local)
+        G.Batch(a).step(S)
+
+        def work(idx):
+            out = {}
+            for i, m in zip(idx, a):
+                r = sweep_models("fp64", params, indices=[i], device=local)[0]
+                r.step(S)
+                ref = r.download_real(0)
+                out[i] = float(np.linalg.norm(m.download_real(0) - ref) / np.linalg.norm(ref))
+                r.close()
+            return out
+
+        errs = sweep.run_sharded(cells_of, work, rank, world)
+        check = {"steps": S, "rel_l2_max": max(errs), "rel_l2_median": float(np.median(errs)), "tolerance": 1e-4,
+                 "rel_l2": errs}
+    if rank == 0:
+        out = {"metric": "sweep steps/s (64 uneven 2D CH instances, one step of all instances)", "value": batched,
+               "unit": "sweep-steps/s", "n_gpus": world, "steps": args.steps, "warmup": max(warm, 16),
+               "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "strong",
+               "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "config": {"workload": "sweep_64_ch2d_uneven_fp32", "sides": [p[0] for p in params], "cells": cells,
+                          "dt": 0.05, "params_seed": 2, "init": "c0 = 0.5 + U(-0.05, 0.05), seed 1000 + i",
+                          "parallelism": f"instances sharded over {world} GPU(s), no collective"
+                                         if world > 1 else "single GPU",
+                          "rank_cells": rank_cells},
+               "sequential_value": seq, "speedup_vs_sequential": (batched / seq) if seq else None,
+               # bytes one sweep step moves: per instance the x pass reads T and writes the group (2C),
+               # the fused y pass reads the group and c-hat and writes c-hat and T (4C); FP32,
+               # C = (X/2+1) Y 8 B
+               "step_bytes_moved": sweep_bytes,
+               "fraction_of_hbm": sweep_bytes * batched / (peaks()[0] * 1e9 * world),
+               "cell_updates_per_s": batched * cells, "clocks": clk.summary(),
+               "gpu_launches": launches, "check": check}
+        print(json.dumps(out))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
     return 0
 
 
@@ -788,11 +837,11 @@ def main():
                     help="steps of the FP32-vs-FP64 device comparison in the default line")
     ap.add_argument("--grid", type=int, default=256, help="cube side (256 is the benchmark workload)")
     ap.add_argument("--workload", default="ch3d", choices=["ch3d", "sweep", "adjoint", "elastic", "precision", "c1"])
-    ap.add_argument("--tma", type=int, default=None, choices=[0, 1, 2],
-                    help="tile movement of the 256-point kernels: 0 plain loads, 1 TMA, 2 TMA + persistent z pass")
-    ap.add_argument("--plane", type=int, default=None, choices=[0, 1],
-                    help="1: depth-plane cluster kernel between consecutive z passes")
-    ap.add_argument("--check-steps", type=int, default=0, help="sweep: compare against FP64 after this many steps")
+    ap.add_argument("--tma", type=int, default=None, choices=[0, 1],
+                    help="tile movement of the 256-point kernels: 0 plain loads, 1 TMA")
+    ap.add_argument("--check-steps", type=int, default=-1,
+                    help="sweep: per-instance rel-L2 against FP64 after this many steps (-1: the configuration's "
+                         "2000; 0: no check)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

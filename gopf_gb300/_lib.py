@@ -25,7 +25,7 @@ DER_PRODUCT, DER_POLY, DER_INDICATOR, DER_INDICATOR_D, DER_INDICATOR_HD, DER_WHI
 NOISE_WHITE, NOISE_CONSERVATIVE = 1, 2
 SRC_NONE, SRC_FIELD, SRC_DERIVED = range(3)
 RED_SUM, RED_SUMSQ, RED_MIN, RED_MAX, RED_NONFINITE = range(5)
-OPT_CHECK_FINITE, OPT_USE_GRAPHS, OPT_FAST_KERNELS, OPT_TMA, OPT_PLANE, OPT_DIRECT_HOST = 0, 1, 2, 3, 4, 5
+OPT_CHECK_FINITE, OPT_USE_GRAPHS, OPT_FAST_KERNELS, OPT_TMA, OPT_DIRECT_HOST = 0, 1, 2, 3, 5
 OPT_WAIT_LIMIT_NS = 6
 MAX_FACTORS = 8
 

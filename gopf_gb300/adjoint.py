@@ -81,22 +81,38 @@ def make_function():
     return CHSolve
 
 
-def fit_gamma_m(runner: AdjointCH, c0, target, gamma0: float, M0: float, iters: int = 20, lr: float = 0.05):
-    """Fit gamma and M to a target microstructure (log-parameters, Adam). Returns the history."""
+def fit_gamma_m(runner: AdjointCH, c0, target, gamma0: float, M0: float, iters: int = 20, lr: float = 0.05,
+                method: str = "adam"):
+    """Fit gamma and M to a target microstructure on log-parameters.  method "adam": `iters` Adam
+    steps of rate lr; "lbfgs": L-BFGS with a strong-Wolfe line search, at most `iters` loss and
+    gradient evaluations (one forward and one adjoint each).  Returns the history of
+    (loss, gamma, M), one entry per evaluation."""
     import torch
 
     CHSolve = make_function()
-    lg = torch.tensor(np.log(gamma0), dtype=torch.float64, requires_grad=True)
-    lm = torch.tensor(np.log(M0), dtype=torch.float64, requires_grad=True)
+    p = torch.tensor([np.log(gamma0), np.log(M0)], dtype=torch.float64, requires_grad=True)
     c0t = torch.from_numpy(np.asarray(c0, dtype=np.float64).reshape(-1))
     tgt = torch.from_numpy(np.asarray(target, dtype=np.float64).reshape(-1))
-    opt = torch.optim.Adam([lg, lm], lr=lr)
     hist = []
-    for _ in range(iters):
+
+    def closure():
         opt.zero_grad()
-        cT = CHSolve.apply(c0t, torch.exp(lg), torch.exp(lm), runner)
+        g, m = torch.exp(p[0]), torch.exp(p[1])
+        cT = CHSolve.apply(c0t, g, m, runner)
         loss = 0.5 * torch.sum((cT - tgt) ** 2)
         loss.backward()
-        opt.step()
-        hist.append((float(loss), float(torch.exp(lg)), float(torch.exp(lm))))
+        hist.append((float(loss.detach()), float(g.detach()), float(m.detach())))
+        return loss
+
+    if method == "lbfgs":
+        opt = torch.optim.LBFGS([p], lr=1.0, max_iter=iters, max_eval=iters, history_size=10,
+                                line_search_fn="strong_wolfe", tolerance_grad=1e-14, tolerance_change=1e-16)
+        opt.step(closure)
+    elif method == "adam":
+        opt = torch.optim.Adam([p], lr=lr)
+        for _ in range(iters):
+            closure()
+            opt.step()
+    else:
+        raise ValueError(f"unknown method {method}")
     return hist

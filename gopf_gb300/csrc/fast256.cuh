@@ -658,144 +658,6 @@ __global__ void __launch_bounds__(NT, 2) k_x256(const XPassArgs<float> a)
 
 
 // ---------------------------------------------------------------------------
-// z axis, persistent and double-buffered (one explicit group).  Two blocks per
-// SM walk the tiles blockIdx.x, blockIdx.x + gridDim.x, ...; the group tile of
-// the next tile is requested a whole iteration ahead and the c-hat tile as soon
-// as the previous one has been read out, so HBM traffic overlaps the
-// transforms instead of waiting on them.  Shared memory: two group tiles (the
-// current one doubles as the exchange buffer and then as the T tile), one
-// c-hat tile, twiddles and frequency tables.
-// ---------------------------------------------------------------------------
-__host__ __device__ constexpr int z256_pipe_smem_bytes()
-{
-    return 128 + ZT_TILE_BYTES * 3 + N * 8 + N * 4 + 16 * 4 + 32;
-}
-
-template <bool NZ>
-__global__ void __launch_bounds__(NT, 2)
-    k_z256_pipe(const PassArgs<float> a, const __grid_constant__ CUtensorMap mU0, const __grid_constant__ CUtensorMap mS,
-                const __grid_constant__ CUtensorMap mT, int ntiles)
-{
-    extern __shared__ unsigned char p_dsm[];
-    unsigned char *base = p_dsm + ((128u - (smem_u32(p_dsm) & 127u)) & 127u);
-    float2 *bufU[2] = {reinterpret_cast<float2 *>(base), reinterpret_cast<float2 *>(base + ZT_TILE_BYTES)};
-    float2 *tS = reinterpret_cast<float2 *>(base + 2 * ZT_TILE_BYTES);
-    float2 *s_tw = reinterpret_cast<float2 *>(base + 3 * ZT_TILE_BYTES);
-    float *s_fz = reinterpret_cast<float *>(s_tw + N);
-    float *s_fl = s_fz + N;
-    uint64_t *barU = reinterpret_cast<uint64_t *>(s_fl + 16); // [2]
-    uint64_t *barS = barU + 2;
-    int *s_ok = reinterpret_cast<int *>(barS + 1);
-
-    const Geom &g = a.g;
-    const int tid = threadIdx.x;
-    const int l = tid & 15, r = tid >> 4;
-    const bool init = (a.mode == PM_INIT);
-    const int ngrp = (a.upd.ngrp > 0) ? 1 : 0;
-    int tile = blockIdx.x;
-    if (tile >= ntiles) return;
-
-    if (tid == 0) {
-        mbar_init(&barU[0], 1);
-        mbar_init(&barU[1], 1);
-        mbar_init(barS, 1);
-        fence_mbar_init();
-        mbar_arrive_expect_tx(&barU[0], (uint32_t)ZT_TILE_BYTES);
-        tma_load_2d(bufU[0], &mU0, tile * 16, 0, &barU[0]);
-        if (!init) {
-            mbar_arrive_expect_tx(barS, (uint32_t)ZT_TILE_BYTES);
-            tma_load_2d(tS, &mS, tile * 16, 0, barS);
-        }
-        *s_ok = 1;
-    }
-    load_twiddles(s_tw, a.tw);
-    s_fz[tid] = fsqf(tid, g.Z);
-    const UpdTable &u = a.upd;
-    const UpdRegs R = load_upd(u, ngrp);
-    const float fourpi2 = 39.478417604357434f;
-    auto wait_flag = [&](uint64_t *bar, uint32_t parity) {
-        if (tid == 0 && !tma_wait_or_flag(bar, parity, a.status)) {
-            *s_ok = 0;
-            bulk_wait_read_all(); // stores in flight finish reading before the block leaves
-        }
-        __syncthreads();
-        return *s_ok != 0;
-    };
-
-    for (int it = 0; tile < ntiles; ++it, tile += gridDim.x) {
-        const int cur = it & 1;
-        const int next = tile + gridDim.x;
-        const int i0 = tile * 16;
-        float2 *tU = bufU[cur];
-        if (tid == 0 && next < ntiles) {
-            bulk_wait_read_all(); // the previous tile's stores have read bufU[cur ^ 1]
-            mbar_arrive_expect_tx(&barU[cur ^ 1], (uint32_t)ZT_TILE_BYTES);
-            tma_load_2d(bufU[cur ^ 1], &mU0, next * 16, 0, &barU[cur ^ 1]);
-        }
-        if (tid < 16) {
-            const int q = i0 + tid;
-            const int kx = q / g.Y, y = q - kx * g.Y;
-            const float fx = (float)kx / (float)g.X;
-            s_fl[tid] = fx * fx + fsqf(y, g.Y);
-        }
-        if (!wait_flag(&barU[cur], (uint32_t)((it >> 1) & 1))) return;
-
-        float2 v[16];
-#pragma unroll
-        for (int i = 0; i < 16; ++i) v[i] = tU[(r + 16 * i) * 16 + l];
-        __syncthreads(); // the group tile becomes the exchange buffer
-        auto at = [&](int x, int y) -> float2 & { return tU[(x * 16 + y) * 16 + l]; };
-        fft256<false>(v, r, s_tw, at);
-
-        if (!init && !wait_flag(barS, (uint32_t)(it & 1))) return;
-        const float fl = s_fl[l];
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-            const int k = r + 16 * i;
-            float2 cn;
-            if (init) {
-                cn = v[i];
-            } else {
-                const float mk = -fourpi2 * (fl + s_fz[k]);
-                float2 c0 = tS[k * 16 + l];
-                if (NZ && u.noise.kind) {
-                    const long long q = i0 + l, kx = q / g.Y, yy = q - kx * g.Y;
-                    double nr, ni;
-                    noise_term(u.noise, g.X, g.Y, g.Z, kx, yy, k, (double)mk, nr, ni);
-                    c0.x += R.dt * (float)nr;
-                    c0.y += R.dt * (float)ni;
-                }
-                cn = euler_update<1>(R, c0, v[i], v[i], mk);
-                if (NZ && u.filt) cn = modal_filter(u, cn, fl + s_fz[k]);
-            }
-            tS[k * 16 + l] = cn;
-            v[i] = make_float2(cn.x * R.invN, cn.y * R.invN);
-        }
-        fence_async_smem();
-        __syncthreads();
-        if (tid == 0) {
-            tma_store_2d(&mS, i0, 0, tS);
-            bulk_commit();
-        }
-        fft256<true>(v, r, s_tw, at);
-#pragma unroll
-        for (int i = 0; i < 16; ++i) tU[(r + 16 * i) * 16 + l] = v[i];
-        fence_async_smem();
-        __syncthreads();
-        if (tid == 0) {
-            tma_store_2d(&mT, i0, 0, tU);
-            bulk_commit();
-            if (next < ntiles && !init) {
-                asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); // the c-hat store has read tS
-                mbar_arrive_expect_tx(barS, (uint32_t)ZT_TILE_BYTES);
-                tma_load_2d(tS, &mS, next * 16, 0, barS);
-            }
-        }
-    }
-    if (tid == 0) bulk_wait_read_all();
-}
-
-// ---------------------------------------------------------------------------
 // x axis with TMA tiles.  The block's input is the [129 kx][32 y] half
 // spectrum of 32 rows of one depth plane (one 3D tensor copy); each output
 // group's [129][32] tile is assembled in shared memory by the separation step

@@ -409,9 +409,8 @@ extern "C" int gopf_set_option(gopf_ctx *ctx, int opt, long long v)
     if (opt == GOPF_OPT_CHECK_FINITE) ctx->check_finite = (int)(v != 0);
     else if (opt == GOPF_OPT_USE_GRAPHS) ctx->use_graphs = (int)(v != 0);
     else if (opt == GOPF_OPT_FAST_KERNELS) ctx->use_fast = (int)(v != 0);
-    else if (opt == GOPF_OPT_PLANE) ctx->use_plane = (int)(v != 0);
     else if (opt == GOPF_OPT_DIRECT_HOST) ctx->use_direct_host = (int)(v != 0);
-    else if (opt == GOPF_OPT_TMA) ctx->use_tma = (int)std::min<long long>(std::max<long long>(v, 0), 2);
+    else if (opt == GOPF_OPT_TMA) ctx->use_tma = (int)(v != 0);
     else if (opt == GOPF_OPT_WAIT_LIMIT_NS) {
         if (v < 0) return gopf_fail(ctx, GOPF_ERR_ARG, "negative wait limit");
         if (!ctx->d_status) return gopf_fail(ctx, GOPF_ERR_STATE, "context has no device");
@@ -1156,7 +1155,7 @@ template <typename R> static XPassArgs<R> xargs(gopf_ctx *ctx)
     a.g = ctx->g;
     a.planH = ctx->planH;
     a.twX = (const V *)ctx->d_twX;
-    a.allow_fast = ctx->use_fast ? (ctx->use_tma >= 2 ? 7 : ctx->use_tma ? 3 : 1) : 0;
+    a.allow_fast = ctx->use_fast ? (ctx->use_tma ? 3 : 1) : 0;
     a.status = ctx->d_status;
     return a;
 }
@@ -1169,7 +1168,7 @@ template <typename R> static PassArgs<R> pargs(gopf_ctx *ctx, bool zaxis)
     a.g = ctx->g;
     a.plan = zaxis ? ctx->planZ : ctx->planY;
     a.tw = (const V *)(zaxis ? ctx->d_twZ : ctx->d_twY);
-    a.allow_fast = ctx->use_fast ? (ctx->use_tma >= 2 ? 7 : ctx->use_tma ? 3 : 1) : 0;
+    a.allow_fast = ctx->use_fast ? (ctx->use_tma ? 3 : 1) : 0;
     a.status = ctx->d_status;
     return a;
 }
@@ -1258,10 +1257,6 @@ template <typename R> static cudaError_t enqueue_load_state(gopf_ctx *ctx, int f
 //   last axis   : forward, c-hat <- (c-hat + dt sum_b m^lap_b U_b)/(1 - dt L(m)), T <- inverse(c-hat/N)
 // The elastic part runs from the second step on: the reference's h-field is
 // zero until the first OnStepFinished (pf/homoLinElast.go:130-145).
-// Steps of a run of consecutive Euler steps may hand the work array from one to
-// the next still y-spectral: the depth-plane kernel then does the inverse y
-// pass of one step together with the x pass and the forward y pass of the
-// next.  Only the last step of a run restores T to its usual form.
 // The point sources of equation eq into its update table (pointers of the current amplitude table).
 static void apply_sources(const gopf_ctx *ctx, UpdTable &u, int eq)
 {
@@ -1281,19 +1276,9 @@ static void apply_sources(const gopf_ctx *ctx, UpdTable &u, int eq)
 // the sources' step counter advances once per step (after every launch of the step)
 __global__ void k_src_tick(unsigned long long *ctr) { *ctr += 1ull; }
 
-static bool plane_path(const gopf_ctx *ctx)
-{
-    return !ctx->multi && ctx->use_plane && ctx->use_fast && ctx->use_tma && ctx->prec == GOPF_FP32 &&
-           plane256_supported(ctx->g) &&
-           ctx->stepper == GOPF_STEPPER_EULER && !ctx->has_elastic && !ctx->has_volcons && ctx->ngroups == 1;
-}
-
-template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx, bool first = true, bool last = true)
+template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx)
 {
     typedef typename VecOf<R>::type V;
-    const bool plane = plane_path(ctx);
-    const bool from_plane = plane && !first; // T arrives y-spectral from the previous step
-    const bool to_plane = plane && !last;    // T leaves y-spectral for the next step
     const bool el = ctx->has_elastic && ctx->el_primed;
     const int G = ctx->ngroups;
     const int GE = G + (el ? 1 : 0); // groups entering the update
@@ -1313,17 +1298,7 @@ template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx, bool first
         u.gscale[G] = nullptr;
     }
     const bool is3d = ctx->g.Z > 1;
-    if (from_plane) {
-        if constexpr (sizeof(R) == 4) {
-            XPassArgs<R> xa = xargs<R>(ctx);
-            xa.in_mode = XIN_SPECTRAL;
-            xa.in = T;
-            xa.out[0] = U[0];
-            xa.ngrp_out = 1;
-            xa.pw = ctx->pw;
-            LK(launch_plane256(xa, ctx->stream));
-        }
-    } else if (GE > 0) {
+    if (GE > 0) {
         XPassArgs<R> xa = xargs<R>(ctx);
         xa.in_mode = XIN_SPECTRAL;
         xa.in = T;
@@ -1377,7 +1352,7 @@ template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx, bool first
             pa.nbuf = 1;
             LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
         }
-    } else if (is3d && GE > 0 && !from_plane) {
+    } else if (is3d && GE > 0) {
         PassArgs<R> pa = pargs<R>(ctx, false);
         pa.mode = PM_FWD;
         for (int b = 0; b < GE; ++b) pa.buf[b] = U[b];
@@ -1396,7 +1371,7 @@ template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx, bool first
     LK(is3d ? launch_spass<R>(fa, ctx->LBz, ctx->stream) : launch_cpass<R>(fa, ctx->LBy, ctx->stream));
     // The projection touches only c-hat, the inverse y pass only T: outside per-kernel profiling
     // they run as two branches (a fork/join that a captured graph keeps).
-    const bool fork = is3d && !to_plane && !ctx->prof_events;
+    const bool fork = is3d && !ctx->prof_events;
     if (fork) {
         LK(cudaEventRecord(ctx->ev_fork, ctx->stream));
         LK(cudaStreamWaitEvent(ctx->side_stream, ctx->ev_fork, 0));
@@ -1405,7 +1380,7 @@ template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx, bool first
     } else {
         LK(gopf_launch_hermitian_planes(ctx, ctx->d_state));
     }
-    if (is3d && !to_plane) {
+    if (is3d) {
         PassArgs<R> ia = pargs<R>(ctx, false);
         ia.mode = PM_INV;
         ia.buf[0] = T;
@@ -1626,7 +1601,7 @@ template <typename R> static cudaError_t enqueue_steps(gopf_ctx *ctx, int n)
             else
                 LK(enqueue_multi_stage<R>(ctx, 0));
         } else {
-            LK(ctx->stepper == GOPF_STEPPER_RK4 ? enqueue_rk4<R>(ctx) : enqueue_euler<R>(ctx, i == 0, i == n - 1));
+            LK(ctx->stepper == GOPF_STEPPER_RK4 ? enqueue_rk4<R>(ctx) : enqueue_euler<R>(ctx));
         }
         if (!ctx->sources.empty()) {
             k_src_tick<<<1, 1, 0, ctx->stream>>>(ctx->d_srcctr);
@@ -2569,12 +2544,6 @@ static void step_slots(gopf_ctx *ctx, std::vector<std::string> &names, std::vect
         names.push_back(n);
         bytes.push_back(b);
     };
-    if (plane_path(ctx)) { // a step inside a run: y inverse + x + y forward per plane, then z
-        add("plane_yinv_x_yfwd", 2.0 * C);
-        add("zpass_update", 4.0 * C);
-        add("hermitian_planes", 4.0 * C / ctx->g.KX);
-        return;
-    }
     if (GE > 0) add("xpass_pointwise", (1.0 + GE) * C);
     if (ctx->has_volcons) add("volcons_multiplier", 0.0);
     if (el) {
@@ -2609,27 +2578,13 @@ extern "C" int gopf_profile_step(gopf_ctx *ctx, int nsteps, double *avg_ms, doub
     std::vector<cudaEvent_t> ev(1 + ns * nsteps);
     for (auto &e : ev) CK(cudaEventCreate(&e));
     std::vector<double> acc(ns, 0.0);
-    const bool plane = plane_path(ctx);
     cudaError_t e = cudaSuccess;
-    // inside a run of steps (plane path) the profiled steps are preceded by the run's first step
-    if (plane) e = (ctx->prec == GOPF_FP32) ? enqueue_euler<float>(ctx, true, false) : enqueue_euler<double>(ctx, true, false);
     CK(cudaEventRecord(ev[0], ctx->stream));
     ctx->prof_events = &ev;
     ctx->prof_next = 1;
     for (int s = 0; s < nsteps && e == cudaSuccess; ++s)
-        e = (ctx->prec == GOPF_FP32) ? enqueue_euler<float>(ctx, !plane, !plane)
-                                     : enqueue_euler<double>(ctx, !plane, !plane);
+        e = (ctx->prec == GOPF_FP32) ? enqueue_euler<float>(ctx) : enqueue_euler<double>(ctx);
     ctx->prof_events = nullptr;
-    // ... and followed by the run's closing inverse y pass
-    if (plane && e == cudaSuccess) {
-        if (ctx->prec == GOPF_FP32) {
-            PassArgs<float> ia = pargs<float>(ctx, false);
-            ia.mode = PM_INV;
-            ia.buf[0] = (float2 *)ctx->d_T;
-            ia.nbuf = 1;
-            e = launch_cpass<float>(ia, ctx->LBy, ctx->stream);
-        }
-    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e == cudaSuccess && ctx->prof_next != ev.size()) e = cudaErrorInvalidValue;
     if (e == cudaSuccess) {
@@ -2639,7 +2594,7 @@ extern "C" int gopf_profile_step(gopf_ctx *ctx, int nsteps, double *avg_ms, doub
                 cudaEventElapsedTime(&ms, ev[s * ns + k], ev[s * ns + k + 1]);
                 acc[k] += ms;
             }
-        ctx->step += nsteps + (plane ? 1 : 0);
+        ctx->step += nsteps;
     }
     for (auto &x : ev) cudaEventDestroy(x);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "profile");

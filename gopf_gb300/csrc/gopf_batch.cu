@@ -3,11 +3,14 @@
 // The parameter-sweep workflow of gopf (one FieldDB per swept run, README.md:21-33)
 // steps every instance separately.  A batch takes N contexts of arbitrary
 // (2D) sizes, each with its own equation, coefficients and dt, and steps them
-// together: one persistent x-pass launch and one persistent fused y-pass
-// launch per step walk a work list of (instance, tile) items ordered largest
-// first, so small instances no longer leave the GPU idle and the launch
-// overhead is paid once per pass instead of once per instance.  The step
-// (three launches) is captured in a CUDA graph and replayed.
+// together.  Instances are grouped into size classes; per step each class
+// present gets one x-pass launch and one fused y-pass launch over its
+// (instance, tile) items, ordered largest first, so small instances no longer
+// leave the GPU idle and the launch overhead is paid once per class instead of
+// once per instance.  The classes run as parallel branches of the step's CUDA
+// graph (a class's y pass follows its own x pass when the classes of both
+// passes cover the same instances), followed by one Hermitian-projection
+// launch over every instance: 2 x (classes) + 1 launches per step.
 #include <algorithm>
 #include <cstring>
 #include <string>

@@ -197,7 +197,6 @@ struct gopf_ctx {
     int use_graphs = 1;
     int use_fast = 1;
     int use_tma = 1;
-    int use_plane = 0;
     int use_direct_host = 1;
 
     // ImplicitEuler's Newton-Krylov controls (DefaultNonLinSolver, pf/implicitEuler.go:221-228) and

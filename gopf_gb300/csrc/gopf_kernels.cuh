@@ -20,10 +20,6 @@ template <typename R> cudaError_t launch_xpass(const XPassArgs<R> &a, int LB, cu
 template <typename R> int xpass_red_blocks(const XPassArgs<R> &a, int LB);
 template <typename R> cudaError_t launch_cpass(const PassArgs<R> &a, int LB, cudaStream_t st); // contiguous y axis
 template <typename R> cudaError_t launch_spass(const PassArgs<R> &a, int LB, cudaStream_t st); // strided z axis
-// FP32 256 x 256 planes: inverse y, x pass (one group), forward y of every depth plane in one launch
-// (8-block clusters); a.in holds the y-spectral input, a.out[0] receives the y-spectral output.
-cudaError_t launch_plane256(const XPassArgs<float> &a, cudaStream_t st);
-bool plane256_supported(const Geom &g);
 
 // Tile width (lines per tile) for a transform of length n: 128 bytes per tile
 // row where the 256-thread block can hold LB*n/16 butterfly inputs.

@@ -5,28 +5,11 @@
 
 #include "fast256.cuh"
 #include "fastline.cuh"
-#include "plane256.cuh"
 #include "gopf_kernels_impl.cuh"
 #include "elastic256.cuh"
 #include "x256_io.cuh"
 
 namespace gopf {
-
-bool plane256_supported(const Geom &g) { return g.X == 256 && g.Y == 256 && g.KX == 129 && g.Z > 1; }
-
-cudaError_t launch_plane256(const XPassArgs<float> &a, cudaStream_t st)
-{
-    static std::once_flag once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(once, [] {
-        attr_err = cudaFuncSetAttribute(f256::k_plane256, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        f256::plane256_smem_bytes());
-    });
-    if (attr_err != cudaSuccess) return attr_err;
-    if (!plane256_supported(a.g) || a.ngrp_out != 1 || a.program != XP_POLY) return cudaErrorInvalidValue;
-    f256::k_plane256<<<(unsigned)(a.g.Z * f256::PL_CLUSTER), f256::NT, f256::plane256_smem_bytes(), st>>>(a);
-    return cudaGetLastError();
-}
 
 // [Z][S] view of a z-pass array with 16 x 256 boxes
 static bool z_map(CUtensorMap *m, const float2 *p, const Geom &g)
@@ -95,12 +78,6 @@ static bool launch_z_tma(const PassArgs<float> &a, cudaStream_t st, cudaError_t 
         for (int i = 0; i < 4 && attr_err == cudaSuccess; ++i)
             attr_err = cudaFuncSetAttribute(k[i], cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             f256::z256_tma_smem_bytes(1 + (i & 1)));
-        if (attr_err == cudaSuccess)
-            attr_err = cudaFuncSetAttribute(f256::k_z256_pipe<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            f256::z256_pipe_smem_bytes());
-        if (attr_err == cudaSuccess)
-            attr_err = cudaFuncSetAttribute(f256::k_z256_pipe<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            f256::z256_pipe_smem_bytes());
     });
     if (attr_err != cudaSuccess) return false;
     CUtensorMap mU0, mU1, mS, mT;
@@ -112,23 +89,6 @@ static bool launch_z_tma(const PassArgs<float> &a, cudaStream_t st, cudaError_t 
     }
     const unsigned grid = (unsigned)(a.g.S / 16);
     const bool nz = (a.upd.noise.kind != 0 || a.upd.filt != nullptr);
-    if (a.nbuf == 1 && (a.allow_fast & 4)) {
-        // persistent double-buffered variant: two blocks per SM
-        static int nsm = 0;
-        if (!nsm) {
-            int dev = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-            if (nsm <= 0) nsm = 1;
-        }
-        const int ntiles = (int)grid;
-        const unsigned pg = (unsigned)std::min(ntiles, 2 * nsm);
-        const int smp = f256::z256_pipe_smem_bytes();
-        if (nz) f256::k_z256_pipe<true><<<pg, f256::NT, smp, st>>>(a, mU0, mS, mT, ntiles);
-        else f256::k_z256_pipe<false><<<pg, f256::NT, smp, st>>>(a, mU0, mS, mT, ntiles);
-        *err = cudaGetLastError();
-        return true;
-    }
     const int sm1 = f256::z256_tma_smem_bytes(1), sm2 = f256::z256_tma_smem_bytes(2);
     if (a.nbuf > 1) {
         if (nz) f256::k_z256_tma<2, true><<<grid, f256::NT, sm2, st>>>(a, mU0, mU1, mS, mT);

@@ -96,10 +96,8 @@ enum {
     GOPF_OPT_CHECK_FINITE = 0, /* 1 (default): gopf_step synchronises and checks the field for NaN/Inf */
     GOPF_OPT_USE_GRAPHS = 1,   /* 1 (default): steps are replayed from captured CUDA graphs */
     GOPF_OPT_FAST_KERNELS = 2, /* 1 (default): register-resident kernels serve the lengths they cover */
-    GOPF_OPT_TMA = 3,          /* those kernels move their tiles with TMA tensor copies: 0 no, 1 one tile
-                                  per block (default), 2 also the persistent double-buffered z pass */
-    GOPF_OPT_PLANE = 4,        /* 1: consecutive FP32 Euler steps on 256 x 256 x Z grids do the inverse y,
-                                  x and forward y passes of each depth plane in one cluster launch */
+    GOPF_OPT_TMA = 3,          /* 1 (default): those kernels move their tiles with TMA tensor copies;
+                                  0: plain loads (value 4 is unused) */
     GOPF_OPT_DIRECT_HOST = 5,  /* 1 (default): pinned host buffers given to upload/download are read and
                                   written by kernels in place; pageable buffers are staged */
     GOPF_OPT_WAIT_LIMIT_NS = 6 /* limit (ns) of a kernel's first wait for a tile copy; 0 (default) = 2 s.
@@ -322,7 +320,9 @@ int gopf_adjoint_release(gopf_ctx *ctx);
  * sweep database serves, README.md:21-33, pf/database.go:67-80); it has no
  * single counterpart in the reference.  Every context keeps its own model,
  * dt and device state; gopf_batch_step(nsteps) advances all of them by
- * nsteps Euler steps with three launches per step (captured in a CUDA graph).
+ * nsteps Euler steps: per step one x-pass and one y-pass launch for each size
+ * class present plus one projection launch (gopf_batch_kernels_per_step),
+ * captured in a CUDA graph.
  * Contexts must be 2D, single-field, Euler, without user-defined terms, on one
  * device and precision, and stay alive while the batch exists. */
 typedef struct gopf_batch gopf_batch;

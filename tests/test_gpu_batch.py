@@ -104,8 +104,9 @@ def test_batch_with_large_instances_runs_and_stays_finite():
 
 
 def test_batch_size_classes_equal_generic_contexts():
-    """The sweep's sides go through compile-time-plan kernels (one per size class, run as parallel
-    graph branches); they compute what the runtime-plan kernels of single contexts compute."""
+    """The sweep's sides go through one kernel per size class (the register line engine for FP32 sides
+    256 ... 1024, compile-time Stockham plans for 128), run as parallel graph branches; they compute
+    what the runtime-plan kernels of single contexts compute, to FP32 rounding."""
     import gopf_gb300 as G
     from gopf_gb300.synthetic import uniform_field
 
@@ -123,3 +124,34 @@ def test_batch_size_classes_equal_generic_contexts():
     for a, b in zip(a_models, b_models):
         x, y = a.download_real(0), b.download_real(0)
         assert np.max(np.abs(x - y)) <= 1e-6 * np.max(np.abs(y))
+
+
+def test_sweep_draw_fp32_batch_matches_fp64_per_instance():
+    """The sweep configuration's own draw (64 instances, sides from {128 ... 1024} by seed 2, gamma ~
+    U(0.2, 2), M ~ U(0.5, 2), c0 = 0.5 + U(-0.05, 0.05) with seed 1000 + i, dt 0.05): the first
+    instance of every side class, batched in FP32 (line engine for 256 ... 1024), against each
+    instance stepped alone in FP64, 200 steps: per-instance rel-L2 <= 1e-4."""
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import splitmix64_uniform, uniform_field
+
+    sides = [128, 256, 384, 512, 768, 1024]
+    u = splitmix64_uniform(2, 3 * 64)
+    draw = [(sides[min(int(u[3 * i] * 6), 5)], 0.2 + 1.8 * u[3 * i + 1], 0.5 + 1.5 * u[3 * i + 2]) for i in range(64)]
+    first = {}
+    for i, p in enumerate(draw):
+        first.setdefault(p[0], i)
+    assert sorted(first) == sides  # the draw holds every class
+    pick = [first[s] for s in sides]
+    a, b = [], []
+    for i in pick:
+        side, gamma, M = draw[i]
+        c0 = uniform_field(1000 + i, side * side, 0.5, 0.05)
+        a.append(ch_ctx(side, "fp32", gamma, M, 0.05, c0))
+        b.append(ch_ctx(side, "fp64", gamma, M, 0.05, c0))
+    G.Batch(a).step(200)
+    for m in b:
+        m.step(200)
+    for i, x, y in zip(pick, a, b):
+        ref = y.download_real(0)
+        err = np.linalg.norm(x.download_real(0) - ref) / np.linalg.norm(ref)
+        assert err <= 1e-4, (i, draw[i], err)
