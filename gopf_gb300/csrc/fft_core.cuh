@@ -157,11 +157,74 @@ template <bool INV, typename V> __device__ __forceinline__ void dft16(V *v)
     for (int i = 0; i < 16; ++i) v[i] = t[i];
 }
 
+// DFT of odd prime length P (5, 7) from its definition, pairing n and P - n:
+//   X_0 = x_0 + sum_n t_n,   t_n = x_n + x_{P-n},   u_n = x_n - x_{P-n}   (n = 1 .. (P-1)/2)
+//   a_m = x_0 + sum_n cos(2 pi n m / P) t_n,   b_m = sum_n sin(2 pi n m / P) u_n
+//   X_m = a_m - i b_m,   X_{P-m} = a_m + i b_m   (forward; the inverse flips the sign of i)
+template <int P> struct PrimeTab;
+template <> struct PrimeTab<5> {
+    // cos, sin of 2 pi q / 5, q = 0 .. 4
+    __device__ static constexpr double c(int q)
+    {
+        return q == 0 ? 1.0 : (q == 1 || q == 4) ? 0.30901699437494742410 : -0.80901699437494742410;
+    }
+    __device__ static constexpr double s(int q)
+    {
+        return q == 0 ? 0.0 : q == 1 ? 0.95105651629515357212 : q == 2 ? 0.58778525229247312917
+               : q == 3 ? -0.58778525229247312917 : -0.95105651629515357212;
+    }
+};
+template <> struct PrimeTab<7> {
+    __device__ static constexpr double c(int q)
+    {
+        return q == 0 ? 1.0 : (q == 1 || q == 6) ? 0.62348980185873353053
+               : (q == 2 || q == 5) ? -0.22252093395631440429 : -0.90096886790241912624;
+    }
+    __device__ static constexpr double s(int q)
+    {
+        return q == 0 ? 0.0 : q == 1 ? 0.78183148246802980871 : q == 2 ? 0.97492791218182360702
+               : q == 3 ? 0.43388373911755812048 : q == 4 ? -0.43388373911755812048
+               : q == 5 ? -0.97492791218182360702 : -0.78183148246802980871;
+    }
+};
+
+template <int P, bool INV, typename V> __device__ __forceinline__ void dft_prime(V *v)
+{
+    typedef typename RealOf<V>::type R;
+    constexpr int H = (P - 1) / 2;
+    V t[H], u[H];
+#pragma unroll
+    for (int n = 1; n <= H; ++n) {
+        t[n - 1] = cadd(v[n], v[P - n]);
+        u[n - 1] = csub(v[n], v[P - n]);
+    }
+    const V x0 = v[0];
+    V sum = x0;
+#pragma unroll
+    for (int n = 0; n < H; ++n) sum = cadd(sum, t[n]);
+    v[0] = sum;
+#pragma unroll
+    for (int m = 1; m <= H; ++m) {
+        V a = x0, b = cmk<V>((R)0, (R)0);
+#pragma unroll
+        for (int n = 1; n <= H; ++n) {
+            const R cc = (R)PrimeTab<P>::c((n * m) % P), ss = (R)PrimeTab<P>::s((n * m) % P);
+            a = cadd(a, cscale(t[n - 1], cc));
+            b = cadd(b, cscale(u[n - 1], ss));
+        }
+        const V ib = cmul_mi<INV>(b); // -i b forward, +i b inverse
+        v[m] = cadd(a, ib);
+        v[P - m] = csub(a, ib);
+    }
+}
+
 template <int R, bool INV, typename V> __device__ __forceinline__ void dft(V *v)
 {
     if (R == 2) dft2<INV>(v[0], v[1]);
     else if (R == 3) dft3<INV>(v[0], v[1], v[2]);
     else if (R == 4) dft4<INV>(v[0], v[1], v[2], v[3]);
+    else if (R == 5) dft_prime<5, INV>(v);
+    else if (R == 7) dft_prime<7, INV>(v);
     else if (R == 8) dft8<INV>(v);
     else if (R == 16) dft16<INV>(v);
 }
@@ -230,6 +293,8 @@ __device__ __forceinline__ void fft_tile(V *buf, int pitch, const LinePlan &pl, 
         else if (R == 8) fft_stage<8, INV, LB, PERB>(buf, pitch, pl.n, ns, msk, twm, tw);
         else if (R == 4) fft_stage<4, INV, LB, PERB>(buf, pitch, pl.n, ns, msk, twm, tw);
         else if (R == 3) fft_stage<3, INV, LB, PERB>(buf, pitch, pl.n, ns, msk, twm, tw);
+        else if (R == 5) fft_stage<5, INV, LB, PERB>(buf, pitch, pl.n, ns, msk, twm, tw);
+        else if (R == 7) fft_stage<7, INV, LB, PERB>(buf, pitch, pl.n, ns, msk, twm, tw);
         else fft_stage<2, INV, LB, PERB>(buf, pitch, pl.n, ns, msk, twm, tw);
     }
 }

@@ -66,12 +66,17 @@ static bool make_plan(int n, int tws, LinePlan &pl)
     memset(&pl, 0, sizeof(pl));
     pl.n = n;
     if (n < 1) return false;
-    int m = n, a = 0, b = 0;
+    int m = n, a = 0, b = 0, c5 = 0, c7 = 0;
     while (m % 2 == 0) { m /= 2; ++a; }
     while (m % 3 == 0) { m /= 3; ++b; }
+    while (m % 5 == 0) { m /= 5; ++c5; }
+    while (m % 7 == 0) { m /= 7; ++c7; }
     if (m != 1) return false;
+    // radix 3s, 5s, 7s, then 2^(a mod 4), then 16s (for 2^a 3^b the order of the compile-time plans)
     std::vector<int> rad;
     for (int i = 0; i < b; ++i) rad.push_back(3);
+    for (int i = 0; i < c5; ++i) rad.push_back(5);
+    for (int i = 0; i < c7; ++i) rad.push_back(7);
     if (a % 4) rad.push_back(1 << (a % 4));
     for (int i = 0; i < a / 4; ++i) rad.push_back(16);
     if ((int)rad.size() > GOPF_MAX_STAGES) return false;
@@ -246,7 +251,7 @@ static int check_len(int n, const char *what, gopf_ctx *ctx)
     LinePlan p;
     if (!make_plan(n, 1, p))
         return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED,
-                         std::string(what) + " length " + std::to_string(n) + " must be 2^a*3^b");
+                         std::string(what) + " length " + std::to_string(n) + " must be 2^a*3^b*5^c*7^d");
     return GOPF_OK;
 }
 
