@@ -570,16 +570,25 @@ __device__ __forceinline__ void x_fwd_store(float2 (&v)[16], float2 *__restrict_
 #pragma unroll
     for (int i = 0; i < 16; ++i) s_x[(r + 16 * i) * 16 + j] = v[i];
     __syncthreads();
-    for (int e = threadIdx.x; e < KX * XROWS; e += NT) {
-        const int kx = e >> 5, y = e & 31, jj = y >> 1;
-        const float2 P = s_x[kx * 16 + jj];
-        const float2 Q = s_x[((N - kx) & (N - 1)) * 16 + jj];
-        float2 o;
-        if ((y & 1) == 0) o = make_float2(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y));
-        else o = make_float2(0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
-        out[sbase + (long long)kx * Y + y] = o;
+    // a thread takes pair p = tid % 16 at kx = tid / 16 + 16 q and writes both rows (2p, 2p + 1)
+    // with one 16-byte store: a half-warp covers the 256 contiguous bytes of one kx row
+    const int p = threadIdx.x & 15, k0 = threadIdx.x >> 4;
+    float2 *o = out + sbase + (long long)k0 * Y + 2 * p;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int kx = k0 + 16 * q;
+        const float2 P = s_x[kx * 16 + p];
+        const float2 Q = s_x[((N - kx) & (N - 1)) * 16 + p];
+        *reinterpret_cast<float4 *>(o + (long long)(16 * q) * Y) =
+            make_float4(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y), 0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
+    }
+    if (k0 == 0) { // kx = 128
+        const float2 P = s_x[128 * 16 + p];
+        *reinterpret_cast<float4 *>(out + sbase + 128LL * Y + 2 * p) =
+            make_float4(0.5f * (P.x + P.x), 0.5f * (P.y - P.y), 0.5f * (P.y + P.y), 0.5f * (P.x - P.x));
     }
     __syncthreads();
+    (void)KX;
 }
 
 // Pointwise polynomial of the packed row pair, forward transform and separation
@@ -673,21 +682,20 @@ __host__ __device__ constexpr int x256_tma_smem_bytes()
     return 128 + XT_XCH_BYTES + XT_TILE_BYTES + N * 8 + GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1) * 4 + 16;
 }
 
-template <int D> __device__ __forceinline__ float horner_f(const float (&c)[GOPF_MAX_DEG + 1], float x)
-{
-    float acc = c[D];
-#pragma unroll
-    for (int q = D - 1; q >= 0; --q) acc = acc * x + c[q];
-    return acc;
-}
-
+// g(c) on both packed rows at once: Horner on FP32x2 pairs (one FFMA2 per degree), rounding
+// exactly as the scalar Horner of each component
 template <int D> __device__ __forceinline__ void poly_regs(float2 (&v)[16], const float *cf)
 {
-    float c[GOPF_MAX_DEG + 1];
+    float2 c[GOPF_MAX_DEG + 1];
 #pragma unroll
-    for (int q = 0; q <= D; ++q) c[q] = cf[q];
+    for (int q = 0; q <= D; ++q) c[q] = make_float2(cf[q], cf[q]);
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = make_float2(horner_f<D>(c, v[i].x), horner_f<D>(c, v[i].y));
+    for (int i = 0; i < 16; ++i) {
+        float2 acc = c[D];
+#pragma unroll
+        for (int q = D - 1; q >= 0; --q) acc = __ffma2_rn(acc, v[i], c[q]);
+        v[i] = acc;
+    }
 }
 
 // g(c) of group grp on both packed rows, with the degree resolved once per block

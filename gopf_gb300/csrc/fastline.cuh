@@ -39,8 +39,24 @@ template <int L> struct Geo {
     // separation pitch: the readers take (line p, column kx) with p fastest over LPB lines, so a
     // pitch of 32 / LPB (mod 16) float2 spreads a warp's 32 reads over all 16 bank pairs
     static constexpr int SEP = L + 32 / LPB;
+    // the x pass's input tile is [2 LPB rows][PX] (kx contiguous): with 8 rows (L = 768, 1024) a
+    // pitch of 4 (mod 16) float2 spreads the copies of (row, kx), row fastest, over all 16 bank
+    // pairs; with 16 or 32 rows the odd KX itself does
+    static constexpr int KX = L / 2 + 1;
+    static constexpr int PX = (2 * LPB == 8) ? KX + ((4 - KX % 16) + 16) % 16 : KX;
     static_assert(L == 256 || L == 384 || L == 512 || L == 768 || L == 1024, "line length");
 };
+
+// First-stage twiddles W_L^(r k1) (r < T, k1 < 16) laid out [k1][r]: the T threads of a line read
+// consecutive slots (conflict free) instead of the strided W_L table entries r k1.
+template <int L> __device__ __forceinline__ void load_twr(float2 *twr, const float2 *__restrict__ tw, int nt)
+{
+    constexpr int T = Geo<L>::T;
+    for (int t = threadIdx.x; t < L; t += nt) {
+        const int k1 = t / T, r = t - k1 * T;
+        twr[t] = tw[r * k1];
+    }
+}
 
 // low 4 bits of a row -> a permutation whose bit 3 is the row's bit 0: rows that differ in bit 0
 // land in opposite halves of the 16 banks (conflict-free column reads for U = 2, 4)
@@ -161,12 +177,13 @@ template <bool INV> __device__ __forceinline__ void dft8at(float2 (&v)[16], int 
 // Forward transform of the thread's line: in v[i] = x[r + T i]; out v[j] = X[ro.elem(j)].
 // z: the line's slot region; tw: W_L^t (t < L).  Leaves the slots free (ends with a barrier).
 template <int L>
-__device__ __forceinline__ void line_fwd(float2 (&v)[16], int r, const Role<L> &ro, float2 *z, const float2 *tw)
+__device__ __forceinline__ void line_fwd(float2 (&v)[16], int r, const Role<L> &ro, float2 *z, const float2 *tw,
+                                         const float2 *twr)
 {
     typedef Geo<L> G;
     pdft16<false>(v);
 #pragma unroll
-    for (int k1 = 1; k1 < 16; ++k1) v[k1] = cm(v[k1], tw[r * k1]);
+    for (int k1 = 1; k1 < 16; ++k1) v[k1] = cm(v[k1], twr[k1 * G::T + r]);
 #pragma unroll
     for (int k1 = 0; k1 < 16; ++k1) z[slot(r, k1)] = v[k1];
     __syncthreads();
@@ -206,7 +223,8 @@ __device__ __forceinline__ void line_fwd(float2 (&v)[16], int r, const Role<L> &
 
 // Inverse (unnormalised) transform: in v[j] = X[ro.elem(j)]; out v[i] = x[r + T i] * L.
 template <int L>
-__device__ __forceinline__ void line_inv(float2 (&v)[16], int r, const Role<L> &ro, float2 *z, const float2 *tw)
+__device__ __forceinline__ void line_inv(float2 (&v)[16], int r, const Role<L> &ro, float2 *z, const float2 *tw,
+                                         const float2 *twr)
 {
     typedef Geo<L> G;
     if constexpr (G::U == 3) {
@@ -247,11 +265,11 @@ __device__ __forceinline__ void line_inv(float2 (&v)[16], int r, const Role<L> &
         __syncthreads();
     }
 #pragma unroll
-    for (int k1 = 1; k1 < 16; ++k1) v[k1] = cmc(v[k1], tw[r * k1]);
+    for (int k1 = 1; k1 < 16; ++k1) v[k1] = cmc(v[k1], twr[k1 * G::T + r]);
     pdft16<true>(v);
 }
 
-template <int L> constexpr int yline_smem_bytes() { return (Geo<L>::LPB * Geo<L>::LREG + L + L) * 8; }
+template <int L> constexpr int yline_smem_bytes() { return (Geo<L>::LPB * Geo<L>::LREG + L + L + L) * 8; }
 
 // One y tile of the 2D fused Euler update (pf/euler.go:16-47; plain form, no noise or filter):
 // LPB lines q0 .. of length L = g.Y, groups a.buf[0 .. ng), c-hat a.state, T <- inverse(c_new/N).
@@ -261,7 +279,8 @@ template <int L, int NG> __device__ __forceinline__ void yline_tile(const PassAr
     extern __shared__ __align__(16) unsigned char fl_dsm[];
     float2 *s_x = reinterpret_cast<float2 *>(fl_dsm);
     float2 *s_tw = s_x + G::LPB * G::LREG;
-    float *s_fy = reinterpret_cast<float *>(s_tw + L);
+    float2 *s_twr = s_tw + L;
+    float *s_fy = reinterpret_cast<float *>(s_twr + L);
     const Geom &g = a.g;
     const int l = threadIdx.x / G::T, r = threadIdx.x - l * G::T;
     const long long nlines = (long long)g.Z * g.KX;
@@ -273,6 +292,7 @@ template <int L, int NG> __device__ __forceinline__ void yline_tile(const PassAr
         s_tw[t] = a.tw[t];
         s_fy[t] = f256::fsqf(t, g.Y);
     }
+    load_twr<L>(s_twr, a.tw, G::NT);
     const Role<L> ro(r);
     const float2 *__restrict__ U0 = a.buf[0];
     float2 *__restrict__ state = a.state;
@@ -284,7 +304,7 @@ template <int L, int NG> __device__ __forceinline__ void yline_tile(const PassAr
 #pragma unroll
     for (int j = 0; j < 16; ++j) cs[j] = valid ? state[q * L + ro.elem(j)] : zero;
     __syncthreads();
-    line_fwd<L>(v, r, ro, z, s_tw);
+    line_fwd<L>(v, r, ro, z, s_tw, s_twr);
     const UpdTable &u = a.upd;
     const int ngrp = (NG == 1) ? (u.ngrp > 0 ? 1 : 0) : u.ngrp;
     float2 w[NG == 1 ? 1 : 16];
@@ -292,7 +312,7 @@ template <int L, int NG> __device__ __forceinline__ void yline_tile(const PassAr
         const float2 *__restrict__ U1 = a.buf[1];
 #pragma unroll
         for (int i = 0; i < 16; ++i) w[i] = valid ? U1[q * L + r + G::T * i] : zero;
-        line_fwd<L>(reinterpret_cast<float2(&)[16]>(w), r, ro, z, s_tw);
+        line_fwd<L>(reinterpret_cast<float2(&)[16]>(w), r, ro, z, s_tw, s_twr);
     }
     const f256::UpdRegs R = f256::load_upd(u, ngrp);
     float fl = 0.f;
@@ -312,56 +332,111 @@ template <int L, int NG> __device__ __forceinline__ void yline_tile(const PassAr
         }
         v[j] = make_float2(cn.x * R.invN, cn.y * R.invN);
     }
-    line_inv<L>(v, r, ro, z, s_tw);
+    line_inv<L>(v, r, ro, z, s_tw, s_twr);
     float2 *__restrict__ T = a.tout;
 #pragma unroll
     for (int i = 0; i < 16; ++i)
         if (valid) T[q * L + r + G::T * i] = v[i];
 }
 
-// one shared array holds, in turn, the spectral tile [L/2 + 1][2 LPB], the exchange slots of the
-// LPB lines and the separation slots [LPB][SEP]; then twiddles and polynomial coefficients
+// one shared array holds, in turn, the spectral tile [2 LPB rows][PX], the exchange slots of the
+// LPB lines and the separation slots [LPB][SEP]; then two twiddle tables and the polynomial
+// coefficients
 template <int L> __host__ __device__ constexpr int xline_area()
 {
-    constexpr int a = (L / 2 + 1) * 2 * Geo<L>::LPB, b = Geo<L>::LPB * Geo<L>::LREG, c = Geo<L>::LPB * Geo<L>::SEP;
+    constexpr int a = 2 * Geo<L>::LPB * Geo<L>::PX, b = Geo<L>::LPB * Geo<L>::LREG, c = Geo<L>::LPB * Geo<L>::SEP;
     return (a > b ? (a > c ? a : c) : (b > c ? b : c));
 }
-template <int L> constexpr int xline_smem_bytes() { return (xline_area<L>() + L) * 8 + GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1) * 4; }
+template <int L> constexpr int xline_smem_bytes()
+{
+    return (xline_area<L>() + 2 * L) * 8 + GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1) * 4;
+}
 
 // 16-byte asynchronous global -> shared copy (no register staging), completed by cp_async_wait
 __device__ __forceinline__ void cp_async16(void *dst, const void *src)
 {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
+// 8-byte asynchronous copy (through L1: the neighbouring rows of the same sector follow at once)
+__device__ __forceinline__ void cp_async8(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-// Request the spectral tile of x tile ty (kx = 0 .. L/2, rows y0 .. y0 + 2 LPB) into area[kx][row]
-// with asynchronous copies (g.Y must be a multiple of 2 LPB).
+// Request the spectral tile of x tile ty (kx = 0 .. L/2, rows y0 .. y0 + 2 LPB) into area[row][kx]
+// (pitch PX) with 8-byte asynchronous copies, row fastest (g.Y must be a multiple of 2 LPB).
 template <int L> __device__ __forceinline__ void xline_request(float2 *area, const XPassArgs<float> &a, int ty, int zp)
 {
     typedef Geo<L> G;
-    constexpr int KX = L / 2 + 1, RB = 2 * G::LPB, CH = RB / 2;
+    constexpr int KX = G::KX, RB = 2 * G::LPB;
     const long long sbase = (long long)zp * a.g.S + (long long)ty * RB;
     const float2 *__restrict__ in = a.in;
-    for (int e = threadIdx.x; e < KX * CH; e += G::NT) {
-        const int kx = e / CH, c = e - kx * CH;
-        cp_async16(&area[kx * RB + 2 * c], &in[sbase + (long long)kx * a.g.Y + 2 * c]);
+    for (int e = threadIdx.x; e < KX * RB; e += G::NT) {
+        const int kx = e / RB, row = e - kx * RB;
+        cp_async8(&area[row * G::PX + kx], &in[sbase + (long long)kx * a.g.Y + row]);
     }
     cp_async_commit();
 }
 
+// Rows (2l, 2l + 1) of the tile as one complex line a + i b of L columns, Hermitian-extended, in
+// the A layout (v[i] = column r + T i), conjugated: conj(A(k) + i B(k)) for k <= L/2 and
+// conj(conj A(L - k) + i conj B(L - k)) above.  Consecutive r read consecutive slots.
+template <int L> __device__ __forceinline__ void xline_gather_conj(const float2 *s_a, int l, int r, float2 (&v)[16])
+{
+    typedef Geo<L> G;
+    constexpr int H = L / 2;
+    const float2 *ra = s_a + (2 * l) * G::PX, *rb = ra + G::PX;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int k = r + G::T * i;
+        const bool lo = (i < 8) || (i == 8 && r == 0); // k <= H
+        const int kk = lo ? k : L - k;
+        const float2 A = ra[kk], B = rb[kk];
+        // lo: A + i B = (A.x - B.y, A.y + B.x); hi: conj A + i conj B = (A.x + B.y, B.x - A.y)
+        v[i] = lo ? make_float2(A.x - B.y, -(A.y + B.x)) : make_float2(A.x + B.y, A.y - B.x);
+    }
+    (void)H;
+}
+
+// The separation slots of the line's forward spectrum Z (A layout, v holding conj Z) and the
+// coalesced stores of the two rows' half spectra X_a(k) = (Z(k) + conj Z(-k))/2 (row 2p) and
+// X_b(k) = (Z(k) - conj Z(-k))/(2i) (row 2p + 1).
+template <int L>
+__device__ __forceinline__ void xline_separate(float2 (&v)[16], float2 *s_sep, int l, int r, float2 *__restrict__ out,
+                                               long long sbase, int y0, int Y)
+{
+    typedef Geo<L> G;
+    constexpr int KX = G::KX;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) s_sep[l * G::SEP + r + G::T * i] = make_float2(v[i].x, -v[i].y);
+    __syncthreads();
+    for (int e = threadIdx.x; e < KX * G::LPB; e += G::NT) {
+        const int kx = e / G::LPB, p = e - kx * G::LPB;
+        const float2 P = s_sep[p * G::SEP + kx];
+        const float2 Q = s_sep[p * G::SEP + (kx ? L - kx : 0)];
+        if (y0 + 2 * p < Y)
+            *reinterpret_cast<float4 *>(&out[sbase + (long long)kx * Y + 2 * p]) =
+                make_float4(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y), 0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
+    }
+    __syncthreads();
+}
+
 // One x tile from its spectral tile in area (which then serves as exchange and separation
 // space): c2r of 2 LPB rows -> polynomial groups -> r2c into a.out[grp] (L = g.X columns).
-// s_poly: this instance's dense polynomial coefficients.  Ends with a barrier.
+// The inverse transform is the forward line transform of the conjugate (A layout in, B layout
+// out) and the forward transform the inverse line transform of the conjugate (B in, A out), so
+// the tile is read and the spectra are separated in the A layout, where a line's threads touch
+// consecutive slots.  s_poly: this instance's dense polynomial coefficients.  Ends with a barrier.
 // ONE: exactly one output group, a dense polynomial of degree <= 6 (the caller checks), so only one
 // line is held in registers and the polynomial is unrolled for its degree
 template <int L, bool ONE = false>
 __device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float> &a, int ty, int zp,
-                                              const float2 *s_tw, const float *s_poly)
+                                              const float2 *s_tw, const float2 *s_twr, const float *s_poly)
 {
     typedef Geo<L> G;
-    constexpr int H = L / 2, KX = H + 1, RB = 2 * G::LPB;
+    constexpr int RB = 2 * G::LPB;
     float2 *s_sep = s_a; // [LPB][SEP], once the exchange is done
     const Geom &g = a.g;
     const int l = threadIdx.x / G::T, r = threadIdx.x - l * G::T;
@@ -369,40 +444,21 @@ __device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float
     const long long sbase = (long long)zp * g.S + y0;
     const int Y = g.Y;
     const Role<L> ro(r);
-    // Hermitian extension of rows (2l, 2l + 1) packed as a + i b, in the B layout
     float2 v[16];
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-        const int k = ro.elem(j);
-        if (k <= H) {
-            const float2 A = s_a[k * RB + 2 * l], B = s_a[k * RB + 2 * l + 1];
-            v[j] = make_float2(A.x - B.y, A.y + B.x);
-        } else {
-            const float2 A = s_a[(L - k) * RB + 2 * l], B = s_a[(L - k) * RB + 2 * l + 1];
-            v[j] = make_float2(A.x + B.y, -A.y + B.x);
-        }
-    }
+    xline_gather_conj<L>(s_a, l, r, v);
     __syncthreads(); // the tile becomes the exchange slots
     float2 *z = s_a + l * G::LREG;
-    line_inv<L>(v, r, ro, z, s_tw);
-    // v[i] = c(row 2l, col r + T i) + i c(row 2l + 1, col r + T i)
-    // group grp from w: polynomial, forward line transform, separation of the two rows' spectra
+    line_fwd<L>(v, r, ro, z, s_tw, s_twr);
+    // conj(v[j]) = c(row 2l, col elem(j)) + i c(row 2l + 1, col elem(j)) (times L)
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j].y = -v[j].y;
+    // group grp from w: polynomial, forward transform as conj(inverse(conj w)), separation
     auto emit = [&](float2(&w)[16], int grp) {
         if (!a.identity) f256::apply_poly(w, a, grp, s_poly + grp * (GOPF_MAX_DEG + 1));
-        line_fwd<L>(w, r, ro, z, s_tw);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) s_sep[l * G::SEP + ro.elem(j)] = w[j];
-        __syncthreads();
-        float2 *__restrict__ out = a.out[grp];
-        for (int e = threadIdx.x; e < KX * G::LPB; e += G::NT) {
-            const int kx = e / G::LPB, p = e - kx * G::LPB;
-            const float2 P = s_sep[p * G::SEP + kx];
-            const float2 Q = s_sep[p * G::SEP + (kx ? L - kx : 0)];
-            if (y0 + 2 * p < Y)
-                *reinterpret_cast<float4 *>(&out[sbase + (long long)kx * Y + 2 * p]) =
-                    make_float4(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y), 0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
-        }
-        __syncthreads();
+        for (int j = 0; j < 16; ++j) w[j].y = -w[j].y;
+        line_inv<L>(w, r, ro, z, s_tw, s_twr);
+        xline_separate<L>(w, s_sep, l, r, a.out[grp], sbase, y0, Y);
     };
     if constexpr (ONE) {
         switch (a.pw.deg[0]) {
@@ -414,20 +470,10 @@ __device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float
         case 5: f256::poly_regs<5>(v, s_poly); break;
         default: f256::poly_regs<6>(v, s_poly); break;
         }
-        line_fwd<L>(v, r, ro, z, s_tw);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) s_sep[l * G::SEP + ro.elem(j)] = v[j];
-        __syncthreads();
-        float2 *__restrict__ out = a.out[0];
-        for (int e = threadIdx.x; e < KX * G::LPB; e += G::NT) {
-            const int kx = e / G::LPB, p = e - kx * G::LPB;
-            const float2 P = s_sep[p * G::SEP + kx];
-            const float2 Q = s_sep[p * G::SEP + (kx ? L - kx : 0)];
-            if (y0 + 2 * p < Y)
-                *reinterpret_cast<float4 *>(&out[sbase + (long long)kx * Y + 2 * p]) =
-                    make_float4(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y), 0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
-        }
-        __syncthreads();
+        for (int j = 0; j < 16; ++j) v[j].y = -v[j].y;
+        line_inv<L>(v, r, ro, z, s_tw, s_twr);
+        xline_separate<L>(v, s_sep, l, r, a.out[0], sbase, y0, Y);
         return;
     }
     // every group but the last works on a copy; the last one on v itself, so that a single group
@@ -442,9 +488,11 @@ __device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float
     if (ng > 0) emit(v, ng - 1);
 }
 
-template <int L> __device__ __forceinline__ void load_xconsts(const XPassArgs<float> &a, float2 *s_tw, float *s_poly)
+template <int L>
+__device__ __forceinline__ void load_xconsts(const XPassArgs<float> &a, float2 *s_tw, float2 *s_twr, float *s_poly)
 {
     for (int t = threadIdx.x; t < L; t += Geo<L>::NT) s_tw[t] = a.twX[t];
+    load_twr<L>(s_twr, a.twX, Geo<L>::NT);
     for (int t = threadIdx.x; t < GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1); t += Geo<L>::NT)
         s_poly[t] = (float)a.pw.dense[t / (GOPF_MAX_DEG + 1)][t % (GOPF_MAX_DEG + 1)];
 }
@@ -455,12 +503,13 @@ template <int L, bool ONE = false> __device__ __forceinline__ void xline_tile(co
     extern __shared__ __align__(16) unsigned char fl_dsm[];
     float2 *s_a = reinterpret_cast<float2 *>(fl_dsm);
     float2 *s_tw = s_a + xline_area<L>();
-    float *s_poly = reinterpret_cast<float *>(s_tw + L);
+    float2 *s_twr = s_tw + L;
+    float *s_poly = reinterpret_cast<float *>(s_twr + L);
     xline_request<L>(s_a, a, ty, zp);
-    load_xconsts<L>(a, s_tw, s_poly);
+    load_xconsts<L>(a, s_tw, s_twr, s_poly);
     cp_async_wait<0>();
     __syncthreads();
-    xline_compute<L, ONE>(s_a, a, ty, zp, s_tw, s_poly);
+    xline_compute<L, ONE>(s_a, a, ty, zp, s_tw, s_twr, s_poly);
 }
 
 } // namespace fl
