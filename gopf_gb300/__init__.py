@@ -453,6 +453,24 @@ class Batch:
     def set_stream(self, stream_handle: int | None) -> None:
         self._ck(self._L.gopf_batch_set_stream(self._h, ctypes.c_void_p(stream_handle or 0)))
 
+    def tune(self, reps: int = 5) -> None:
+        """Time the candidate kernels of every kind of instance and keep the fastest (cached)."""
+        self._ck(self._L.gopf_batch_tune(self._h, int(reps)))
+
+    def force(self, xfam: int = -1, yfam: int = -1, lbx: int = 0, lby: int = 0, xplan: int = 0,
+              yplan: int = 0) -> None:
+        """One kernel choice for every instance (families BATCH_LINE, BATCH_STOCKHAM_CT, BATCH_STOCKHAM)."""
+        self._ck(self._L.gopf_batch_force(self._h, xfam, yfam, lbx, lby, xplan, yplan))
+
+    def choice(self, inst: int) -> dict:
+        out = (ctypes.c_int * 6)()
+        self._ck(self._L.gopf_batch_choice(self._h, int(inst), out))
+        return dict(zip(("xfam", "yfam", "lbx", "lby", "xplan", "yplan"), list(out)))
+
+    @staticmethod
+    def tune_reset() -> None:
+        _lib.load().gopf_batch_tune_reset()
+
     def close(self) -> None:
         h = getattr(self, "_h", None)
         if h is not None and h.value:

@@ -28,6 +28,7 @@ RED_SUM, RED_SUMSQ, RED_MIN, RED_MAX, RED_NONFINITE = range(5)
 OPT_CHECK_FINITE, OPT_USE_GRAPHS, OPT_FAST_KERNELS, OPT_TMA, OPT_DIRECT_HOST = 0, 1, 2, 3, 5
 OPT_WAIT_LIMIT_NS = 6
 MAX_FACTORS = 8
+BATCH_AUTO, BATCH_LINE, BATCH_STOCKHAM_CT, BATCH_STOCKHAM = -1, 0, 1, 2
 
 
 class GopfDerived(ctypes.Structure):
@@ -130,6 +131,10 @@ SIGNATURES = {
     "gopf_batch_set_stream": ([_vp, _vp], _i),
     "gopf_batch_step": ([_vp, _ll], _i),
     "gopf_batch_kernels_per_step": ([_vp, _ip], _i),
+    "gopf_batch_tune": ([_vp, _i], _i),
+    "gopf_batch_tune_reset": ([], _i),
+    "gopf_batch_force": ([_vp, _i, _i, _i, _i, _i, _i], _i),
+    "gopf_batch_choice": ([_vp, _i, _ip], _i),
     "gopf_sweep_partition": ([ctypes.POINTER(_ll), _i, _i, _ip, ctypes.POINTER(_ll)], _i),
 }
 

@@ -61,7 +61,10 @@ extern "C" const char *gopf_last_error(const gopf_ctx *ctx)
 // plans and twiddle tables
 // ------------------------------------------------------------------
 
-static bool make_plan(int n, int tws, LinePlan &pl)
+// Runtime Stockham plan of length n over a twiddle table of n * tws entries.  variant 0: radix 3s,
+// 5s, 7s, then 2^(a mod 4), then 16s; variant 1: the power of two in radix-8 stages (a 2 or 4 for
+// the remainder); variant 2: in radix-4 stages.  All variants use the same table.
+bool gopf_make_plan(int n, int tws, int variant, LinePlan &pl)
 {
     memset(&pl, 0, sizeof(pl));
     pl.n = n;
@@ -77,8 +80,9 @@ static bool make_plan(int n, int tws, LinePlan &pl)
     for (int i = 0; i < b; ++i) rad.push_back(3);
     for (int i = 0; i < c5; ++i) rad.push_back(5);
     for (int i = 0; i < c7; ++i) rad.push_back(7);
-    if (a % 4) rad.push_back(1 << (a % 4));
-    for (int i = 0; i < a / 4; ++i) rad.push_back(16);
+    const int q = (variant == 1) ? 3 : (variant == 2) ? 2 : 4; // log2 of the main radix
+    if (a % q) rad.push_back(1 << (a % q));
+    for (int i = 0; i < a / q; ++i) rad.push_back(1 << q);
     if ((int)rad.size() > GOPF_MAX_STAGES) return false;
     pl.nst = (int)rad.size();
     int ns = 1;
@@ -249,7 +253,7 @@ static int set_device(gopf_ctx *ctx)
 static int check_len(int n, const char *what, gopf_ctx *ctx)
 {
     LinePlan p;
-    if (!make_plan(n, 1, p))
+    if (!gopf_make_plan(n, 1, 0, p))
         return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED,
                          std::string(what) + " length " + std::to_string(n) + " must be 2^a*3^b*5^c*7^d");
     return GOPF_OK;
@@ -361,9 +365,9 @@ extern "C" int gopf_ctx_create(int ndim, const int *domain_size, int precision, 
     ctx->LBz = lb_for(g.Z, vb);
     if ((long long)ctx->LBx * g.H > 4096 || (long long)ctx->LBy * g.Y > 4096 || (long long)ctx->LBz * g.Z > 4096)
         return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "axis longer than 1024 (2048 columns) is not supported");
-    make_plan(g.H, 2, ctx->planH);
-    make_plan(g.Y, 1, ctx->planY);
-    make_plan(g.Z, 1, ctx->planZ);
+    gopf_make_plan(g.H, 2, 0, ctx->planH);
+    gopf_make_plan(g.Y, 1, 0, ctx->planY);
+    gopf_make_plan(g.Z, 1, 0, ctx->planZ);
     if (device < 0) return GOPF_OK; // host-only: equations can be defined and compiled, nothing runs
     if ((rc = set_device(ctx))) return rc;
     cudaError_t e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);

@@ -13,7 +13,10 @@
 // launch over every instance: 2 x (classes) + 1 launches per step.
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "fastline.cuh"
@@ -255,8 +258,20 @@ struct BatchLaunch {
     std::vector<int> inst; // the instances it covers (sorted)
 };
 
+// How one instance's passes run: the kernel family of each pass (GOPF_BATCH_LINE: the register line
+// engine, GOPF_BATCH_STOCKHAM_CT: compile-time Stockham plans, GOPF_BATCH_STOCKHAM: runtime plans,
+// GOPF_BATCH_AUTO: the built-in preference in that order), and for the runtime plans the tile
+// width (0: the context's) and the plan variant (gopf_make_plan).
+struct BatchChoice {
+    int xfam = GOPF_BATCH_AUTO, yfam = GOPF_BATCH_AUTO;
+    int lbx = 0, lby = 0;
+    int xplan = 0, yplan = 0;
+};
+
 struct gopf_batch {
     std::vector<gopf_ctx *> ctx;
+    std::vector<BatchChoice> choice; // requested, per instance
+    std::vector<BatchChoice> eff;    // in effect after the last build, per instance
     int device = 0;
     int prec = GOPF_FP32;
     cudaStream_t own_stream = nullptr, stream = nullptr;
@@ -285,6 +300,10 @@ static int bfail(gopf_batch *b, int code, const std::string &m)
         cudaError_t e_ = (call);                                                                                       \
         if (e_ != cudaSuccess) return bfail(b, GOPF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));    \
     } while (0)
+
+// a runtime-plan tile width the generic batch kernels take for a transform of length n
+// (256 threads hold lb * n / 16 butterfly inputs)
+static bool batch_lb_ok(int lb, int n) { return (lb == 4 || lb == 8 || lb == 16) && lb * n <= 4096; }
 
 template <typename R> static int batch_build(gopf_batch *b)
 {
@@ -339,6 +358,33 @@ template <typename R> static int batch_build(gopf_batch *b)
                 if (g.Y == FL_L[k] && nb <= 2 && c->upd.nimp <= 4) fy = k;
             }
         }
+        // the requested families where they serve this instance, else the built-in preference
+        const BatchChoice &ch = b->choice[i];
+        BatchChoice &ef = b->eff[i];
+        ef = BatchChoice();
+        int xf = ch.xfam, yf = ch.yfam;
+        if ((xf == GOPF_BATCH_LINE && fx < 0) || (xf == GOPF_BATCH_STOCKHAM_CT && xc == 0)) xf = GOPF_BATCH_AUTO;
+        if ((yf == GOPF_BATCH_LINE && fy < 0) || (yf == GOPF_BATCH_STOCKHAM_CT && yc == 0)) yf = GOPF_BATCH_AUTO;
+        if (xf == GOPF_BATCH_AUTO) xf = fx >= 0 ? GOPF_BATCH_LINE : xc > 0 ? GOPF_BATCH_STOCKHAM_CT : GOPF_BATCH_STOCKHAM;
+        if (yf == GOPF_BATCH_AUTO) yf = fy >= 0 ? GOPF_BATCH_LINE : yc > 0 ? GOPF_BATCH_STOCKHAM_CT : GOPF_BATCH_STOCKHAM;
+        if (xf != GOPF_BATCH_LINE) fx = -1;
+        if (yf != GOPF_BATCH_LINE) fy = -1;
+        if (xf == GOPF_BATCH_STOCKHAM) {
+            xc = 0;
+            if (batch_lb_ok(ch.lbx, g.H)) bi.lbx = ch.lbx;
+            if (ch.xplan && gopf_make_plan(g.H, 2, ch.xplan, xa.planH)) ef.xplan = ch.xplan;
+            else xa.planH = c->planH;
+        }
+        if (yf == GOPF_BATCH_STOCKHAM) {
+            yc = 0;
+            if (batch_lb_ok(ch.lby, g.Y)) bi.lby = ch.lby;
+            if (ch.yplan && gopf_make_plan(g.Y, 1, ch.yplan, pa.plan)) ef.yplan = ch.yplan;
+            else pa.plan = c->planY;
+        }
+        ef.xfam = xf;
+        ef.yfam = yf;
+        ef.lbx = (xf == GOPF_BATCH_STOCKHAM) ? bi.lbx : 0;
+        ef.lby = (yf == GOPF_BATCH_STOCKHAM) ? bi.lby : 0;
         if (fx >= 0) { // line engine: tiles of 2 LPB rows (31 ..: one dense polynomial group)
             const bool one = (G == 1 && c->pw.deg[0] >= 0 && c->pw.deg[0] <= 6);
             xc = (one ? 31 : 11) + fx;
@@ -347,9 +393,10 @@ template <typename R> static int batch_build(gopf_batch *b)
             smem_x[xc] = FL_XSMEM[fx];
             thr_x[xc] = FL_NT[fx];
         } else {
-            const int ntx = (g.Y + c->LBx - 1) / c->LBx;
-            for (int t = 0; t < ntx; ++t) xs[xc].push_back({g.H * c->LBx, make_int2((int)i, t)});
-            smem_x[xc] = std::max(smem_x[xc], xpass_smem_bytes(g, c->LBx, vb));
+            const int lb = bi.lbx;
+            const int ntx = (g.Y + lb - 1) / lb;
+            for (int t = 0; t < ntx; ++t) xs[xc].push_back({g.H * lb, make_int2((int)i, t)});
+            smem_x[xc] = std::max(smem_x[xc], xpass_smem_bytes(g, lb, vb));
         }
         if (fy >= 0) { // line engine: tiles of LPB lines
             yc = (nb > 1 ? 21 : 11) + fy;
@@ -358,9 +405,10 @@ template <typename R> static int batch_build(gopf_batch *b)
             smem_y[yc] = FL_YSMEM[fy];
             thr_y[yc] = FL_NT[fy];
         } else {
-            const int nty = (int)((g.KX + c->LBy - 1) / c->LBy);
-            for (int t = 0; t < nty; ++t) ys[yc].push_back({g.Y * c->LBy, make_int2((int)i, t)});
-            smem_y[yc] = std::max(smem_y[yc], cpass_smem_bytes(g, g.Y, c->LBy, nb, vb) + (c->LBy + g.Y) * (int)sizeof(R));
+            const int lb = bi.lby;
+            const int nty = (int)((g.KX + lb - 1) / lb);
+            for (int t = 0; t < nty; ++t) ys[yc].push_back({g.Y * lb, make_int2((int)i, t)});
+            smem_y[yc] = std::max(smem_y[yc], cpass_smem_bytes(g, g.Y, lb, nb, vb) + (lb + g.Y) * (int)sizeof(R));
         }
     }
     b->herm_total = hoff;
@@ -522,12 +570,9 @@ static int batch_capture(gopf_batch *b, int n, cudaGraphExec_t *exec)
     return GOPF_OK;
 }
 
-extern "C" int gopf_batch_create(gopf_ctx *const *ctxs, int n, gopf_batch **out)
+// Check the contexts and set up the batch's streams; no launches yet.
+static int batch_init(gopf_batch *b, gopf_ctx *const *ctxs, int n)
 {
-    if (!out || !ctxs || n < 1) return GOPF_ERR_ARG;
-    *out = nullptr;
-    gopf_batch *b = new gopf_batch();
-    *out = b;
     for (int i = 0; i < n; ++i) {
         gopf_ctx *c = ctxs[i];
         if (!c) return bfail(b, GOPF_ERR_ARG, "null context");
@@ -547,6 +592,8 @@ extern "C" int gopf_batch_create(gopf_ctx *const *ctxs, int n, gopf_batch **out)
         if (!c->sources.empty()) return bfail(b, GOPF_ERR_UNSUPPORTED, "batches step models without sources");
         b->ctx.push_back(c);
     }
+    b->choice.assign(b->ctx.size(), BatchChoice());
+    b->eff.assign(b->ctx.size(), BatchChoice());
     cudaError_t e = cudaSetDevice(b->device);
     if (e != cudaSuccess) return bfail(b, GOPF_ERR_CUDA, cudaGetErrorString(e));
     e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
@@ -554,6 +601,40 @@ extern "C" int gopf_batch_create(gopf_ctx *const *ctxs, int n, gopf_batch **out)
     b->stream = b->own_stream;
     // the contexts' own streams may still hold work
     for (gopf_ctx *c : b->ctx) cudaStreamSynchronize(c->stream);
+    return GOPF_OK;
+}
+
+// Free the launches, item lists and graphs of the last build (the streams and events stay).
+static void batch_release(gopf_batch *b)
+{
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->g1) cudaGraphExecDestroy(b->g1);
+    if (b->gK) cudaGraphExecDestroy(b->gK);
+    b->g1 = b->gK = nullptr;
+    if (b->d_inst) cudaFree(b->d_inst);
+    b->d_inst = nullptr;
+    for (auto *ls : {&b->xl, &b->yl}) {
+        for (BatchLaunch &L : *ls)
+            if (L.d_items) cudaFree(L.d_items);
+        ls->clear();
+    }
+    b->chain.clear();
+}
+
+static int batch_rebuild(gopf_batch *b)
+{
+    batch_release(b);
+    return (b->prec == GOPF_FP32) ? batch_build<float>(b) : batch_build<double>(b);
+}
+
+extern "C" int gopf_batch_create(gopf_ctx *const *ctxs, int n, gopf_batch **out)
+{
+    if (!out || !ctxs || n < 1) return GOPF_ERR_ARG;
+    *out = nullptr;
+    gopf_batch *b = new gopf_batch();
+    *out = b;
+    int rc = batch_init(b, ctxs, n);
+    if (rc) return rc;
     return (b->prec == GOPF_FP32) ? batch_build<float>(b) : batch_build<double>(b);
 }
 
@@ -561,17 +642,200 @@ extern "C" int gopf_batch_destroy(gopf_batch *b)
 {
     if (!b) return GOPF_ERR_ARG;
     cudaSetDevice(b->device);
-    if (b->stream) cudaStreamSynchronize(b->stream);
-    if (b->g1) cudaGraphExecDestroy(b->g1);
-    if (b->gK) cudaGraphExecDestroy(b->gK);
-    if (b->d_inst) cudaFree(b->d_inst);
-    for (auto *ls : {&b->xl, &b->yl})
-        for (BatchLaunch &L : *ls)
-            if (L.d_items) cudaFree(L.d_items);
+    batch_release(b);
     for (cudaStream_t st : b->side) cudaStreamDestroy(st);
     for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
     if (b->own_stream) cudaStreamDestroy(b->own_stream);
     delete b;
+    return GOPF_OK;
+}
+
+// ---- the autotuner ----
+
+namespace {
+
+// Instances that tune alike: same sides, precision, group count, one dense polynomial group or not,
+// and whether the line engine's y pass can take the update.
+typedef std::tuple<int, int, int, int, int, int> TuneKey;
+std::mutex g_tune_mu;
+std::map<TuneKey, BatchChoice> g_tune_cache;
+
+TuneKey tune_key(const gopf_ctx *c)
+{
+    const int G = c->ngroups;
+    const int one = (G == 1 && c->pw.deg[0] >= 0 && c->pw.deg[0] <= 6) ? 1 : 0;
+    const int yl = (std::max(G, 1) <= 2 && c->upd.nimp <= 4) ? 1 : 0;
+    return TuneKey(c->g.X, c->g.Y, c->prec, G, one, yl);
+}
+
+// Device time (ms) per step of a batch of these contexts with one choice for all of them: the
+// 1-step graph is captured, run twice, then timed over `reps` replays with events on the batch's
+// stream.  The contexts' fields are advanced (the caller restores them).
+int time_choice(gopf_batch *parent, const std::vector<gopf_ctx *> &cs, const BatchChoice &ch, int reps, float *ms)
+{
+    gopf_batch t;
+    int rc = batch_init(&t, cs.data(), (int)cs.size());
+    if (!rc) {
+        t.choice.assign(cs.size(), ch);
+        rc = (t.prec == GOPF_FP32) ? batch_build<float>(&t) : batch_build<double>(&t);
+    }
+    if (!rc) rc = batch_capture(&t, 1, &t.g1);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (!rc) {
+        cudaError_t e = cudaEventCreate(&e0);
+        if (e == cudaSuccess) e = cudaEventCreate(&e1);
+        for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaGraphLaunch(t.g1, t.stream);
+        if (e == cudaSuccess) e = cudaEventRecord(e0, t.stream);
+        for (int i = 0; i < reps && e == cudaSuccess; ++i) e = cudaGraphLaunch(t.g1, t.stream);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, t.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(t.stream);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+        if (e != cudaSuccess) rc = bfail(parent, GOPF_ERR_CUDA, std::string("tuning: ") + cudaGetErrorString(e));
+        else *ms /= (float)reps;
+    } else if (rc) {
+        parent->err = "tuning: " + t.err;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    batch_release(&t);
+    for (cudaStream_t st : t.side) cudaStreamDestroy(st);
+    for (cudaEvent_t e : t.ev) cudaEventDestroy(e);
+    if (t.own_stream) cudaStreamDestroy(t.own_stream);
+    return rc;
+}
+
+// candidate choices of one pass for a context (family, tile width, plan variant)
+std::vector<BatchChoice> pass_candidates(const gopf_ctx *c, bool xpass, const BatchChoice &base)
+{
+    std::vector<BatchChoice> out;
+    auto add = [&](int fam, int lb, int plan) {
+        BatchChoice ch = base;
+        if (xpass) {
+            ch.xfam = fam;
+            ch.lbx = lb;
+            ch.xplan = plan;
+        } else {
+            ch.yfam = fam;
+            ch.lby = lb;
+            ch.yplan = plan;
+        }
+        out.push_back(ch);
+    };
+    if (c->prec == GOPF_FP32) {
+        add(GOPF_BATCH_LINE, 0, 0);
+        add(GOPF_BATCH_STOCKHAM_CT, 0, 0);
+    }
+    const int n = xpass ? c->g.H : c->g.Y;
+    for (int lb : {4, 8, 16})
+        if (batch_lb_ok(lb, n))
+            for (int plan = 0; plan < 3; ++plan) {
+                gopf::LinePlan pl;
+                if (gopf_make_plan(n, xpass ? 2 : 1, plan, pl)) add(GOPF_BATCH_STOCKHAM, lb, plan);
+            }
+    return out;
+}
+
+} // namespace
+
+extern "C" int gopf_batch_tune(gopf_batch *b, int reps)
+{
+    if (!b) return GOPF_ERR_ARG;
+    if (reps < 1) reps = 5;
+    BCK(cudaSetDevice(b->device));
+    BCK(cudaStreamSynchronize(b->stream));
+    std::map<TuneKey, std::vector<int>> groups;
+    for (size_t i = 0; i < b->ctx.size(); ++i) groups[tune_key(b->ctx[i])].push_back((int)i);
+    for (auto &kv : groups) {
+        BatchChoice best;
+        bool cached = false;
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            auto it = g_tune_cache.find(kv.first);
+            if (it != g_tune_cache.end()) {
+                best = it->second;
+                cached = true;
+            }
+        }
+        if (!cached) {
+            std::vector<gopf_ctx *> cs;
+            for (int i : kv.second) cs.push_back(b->ctx[i]);
+            // keep the fields: back up c-hat and T of every instance of the group
+            const size_t vb = (b->prec == GOPF_FP32) ? 8 : 16;
+            std::vector<void *> bk;
+            std::vector<long long> steps;
+            int rc = GOPF_OK;
+            for (gopf_ctx *c : cs) {
+                void *p = nullptr;
+                cudaError_t e = gopf_malloc(&p, 2 * vb * c->g.C);
+                if (e != cudaSuccess) { rc = bfail(b, GOPF_ERR_OOM, "tuning: no room for the field backup"); break; }
+                bk.push_back(p);
+                steps.push_back(c->step);
+                e = cudaMemcpy(p, c->d_state, vb * c->g.C, cudaMemcpyDeviceToDevice);
+                if (e == cudaSuccess) e = cudaMemcpy((char *)p + vb * c->g.C, c->d_T, vb * c->g.C, cudaMemcpyDeviceToDevice);
+                if (e != cudaSuccess) { rc = bfail(b, GOPF_ERR_CUDA, cudaGetErrorString(e)); break; }
+            }
+            // x pass first (y by the built-in preference), then the y pass with the best x
+            for (int pass = 0; pass < 2 && !rc; ++pass) {
+                float best_ms = 1e30f;
+                BatchChoice winner = best;
+                for (const BatchChoice &cand : pass_candidates(cs[0], pass == 0, best)) {
+                    float ms = 0.f;
+                    if ((rc = time_choice(b, cs, cand, reps, &ms))) break;
+                    if (ms < best_ms) {
+                        best_ms = ms;
+                        winner = cand;
+                    }
+                }
+                best = winner;
+            }
+            for (size_t k = 0; k < cs.size() && k < bk.size(); ++k) {
+                gopf_ctx *c = cs[k];
+                cudaMemcpy(c->d_state, bk[k], vb * c->g.C, cudaMemcpyDeviceToDevice);
+                cudaMemcpy(c->d_T, (char *)bk[k] + vb * c->g.C, vb * c->g.C, cudaMemcpyDeviceToDevice);
+                c->step = steps[k];
+                cudaFree(bk[k]);
+            }
+            if (rc) return rc;
+            BCK(cudaDeviceSynchronize());
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            g_tune_cache[kv.first] = best;
+        }
+        for (int i : kv.second) b->choice[i] = best;
+    }
+    return batch_rebuild(b);
+}
+
+extern "C" int gopf_batch_tune_reset(void)
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache.clear();
+    return GOPF_OK;
+}
+
+extern "C" int gopf_batch_force(gopf_batch *b, int xfam, int yfam, int lbx, int lby, int xplan, int yplan)
+{
+    if (!b) return GOPF_ERR_ARG;
+    if (xfam < GOPF_BATCH_AUTO || xfam > GOPF_BATCH_STOCKHAM || yfam < GOPF_BATCH_AUTO || yfam > GOPF_BATCH_STOCKHAM ||
+        xplan < 0 || xplan > 2 || yplan < 0 || yplan > 2)
+        return bfail(b, GOPF_ERR_ARG, "unknown kernel family or plan variant");
+    BCK(cudaSetDevice(b->device));
+    BatchChoice ch;
+    ch.xfam = xfam;
+    ch.yfam = yfam;
+    ch.lbx = lbx;
+    ch.lby = lby;
+    ch.xplan = xplan;
+    ch.yplan = yplan;
+    for (auto &c : b->choice) c = ch;
+    return batch_rebuild(b);
+}
+
+extern "C" int gopf_batch_choice(gopf_batch *b, int inst, int *out6)
+{
+    if (!b || !out6 || inst < 0 || inst >= (int)b->eff.size()) return GOPF_ERR_ARG;
+    const BatchChoice &e = b->eff[inst];
+    const int v[6] = {e.xfam, e.yfam, e.lbx, e.lby, e.xplan, e.yplan};
+    for (int k = 0; k < 6; ++k) out6[k] = v[k];
     return GOPF_OK;
 }
 

@@ -225,6 +225,7 @@ inline void *field_T(gopf_ctx *ctx, int f) { return f == 0 ? ctx->d_T : ctx->d_f
 inline void *field_rkF(gopf_ctx *ctx, int f) { return f == 0 ? ctx->d_rkF : ctx->d_frkF[f]; }
 
 int gopf_fail(gopf_ctx *ctx, int code, const std::string &msg);
+bool gopf_make_plan(int n, int tws, int variant, gopf::LinePlan &pl);
 int gopf_compile_model(gopf_ctx *ctx);
 int gopf_elastic_table(gopf_ctx *ctx);
 // the multiplier update of VolumeConservingLP from the block sums of the field (red_field) and of

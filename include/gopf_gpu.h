@@ -332,6 +332,27 @@ const char *gopf_batch_last_error(const gopf_batch *batch);
 int gopf_batch_set_stream(gopf_batch *batch, void *cuda_stream);
 int gopf_batch_step(gopf_batch *batch, long long nsteps);
 int gopf_batch_kernels_per_step(gopf_batch *batch, int *n);
+/* Kernel families of a batch pass (no counterpart in the reference; FFTW's measured planning,
+ * pfutil/fftWrap.go:19-20 with fftw.MEASURE, plays the same role for its CPU transforms). */
+enum {
+    GOPF_BATCH_AUTO = -1,        /* the built-in preference: LINE, else STOCKHAM_CT, else STOCKHAM */
+    GOPF_BATCH_LINE = 0,         /* register-resident line engine (FP32, sides 256, 384, 512, 768, 1024) */
+    GOPF_BATCH_STOCKHAM_CT = 1,  /* Stockham tiles with compile-time plans (FP32, sides 128 ... 1024) */
+    GOPF_BATCH_STOCKHAM = 2      /* Stockham tiles with runtime plans (any supported length, FP32 and FP64) */
+};
+/* Autotuner: for each kind of instance in the batch (sides, precision, term groups) time every
+ * candidate of the x pass (family; for runtime plans the tile width 4, 8, 16 and plan variant 0, 1,
+ * 2: radix 16, 8 or 4 stages) and then of the y pass on the batch's own instances (reps timed
+ * steps each, CUDA events; the fields are restored afterwards), keep the fastest and rebuild the
+ * batch.  Choices are cached per process and kind, so later batches of the same kinds tune without
+ * timing.  gopf_batch_tune_reset empties the cache. */
+int gopf_batch_tune(gopf_batch *batch, int reps);
+int gopf_batch_tune_reset(void);
+/* Force one choice on every instance (a family that cannot serve an instance falls back to the
+ * built-in preference for it; lb 0 keeps the context's tile width) and rebuild the batch. */
+int gopf_batch_force(gopf_batch *batch, int xfam, int yfam, int lbx, int lby, int xplan, int yplan);
+/* The choice in effect for instance inst: {xfam, yfam, lbx, lby, xplan, yplan}. */
+int gopf_batch_choice(gopf_batch *batch, int inst, int *out6);
 
 /* ---- sweeps over several GPUs, one process each ----
  * The sweep workflow (README.md:21-33) runs one pf.Solver per parameter set; its instances are

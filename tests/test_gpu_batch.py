@@ -155,3 +155,95 @@ def test_sweep_draw_fp32_batch_matches_fp64_per_instance():
         ref = y.download_real(0)
         err = np.linalg.norm(x.download_real(0) - ref) / np.linalg.norm(ref)
         assert err <= 1e-4, (i, draw[i], err)
+
+
+# ---------------------------------------------------------------- kernel choices and the autotuner
+
+def _tune_models(prec, sides, seed0=4000):
+    from gopf_gb300.synthetic import uniform_field
+
+    return [ch_ctx(s, prec, 0.4 + 0.1 * i, 1.0 + 0.05 * i, 0.05, uniform_field(seed0 + i, s * s, 0.5, 0.05))
+            for i, s in enumerate(sides)]
+
+
+def test_every_kernel_choice_computes_the_same_fields():
+    """Every candidate the autotuner may pick (line engine, compile-time Stockham, runtime Stockham
+    with each tile width and plan variant) steps the same FP32 fields to rounding (rel <= 2e-6
+    after 12 steps); in FP64 the tile widths agree bitwise and the plan variants to 1e-13."""
+    import gopf_gb300 as G
+    from gopf_gb300 import _lib as L
+
+    sides = [1024, 768, 512, 384, 256, 128]
+    ref = None
+    cands = [(L.BATCH_LINE, L.BATCH_LINE, 0, 0, 0, 0), (L.BATCH_STOCKHAM_CT, L.BATCH_STOCKHAM_CT, 0, 0, 0, 0)]
+    cands += [(L.BATCH_STOCKHAM, L.BATCH_STOCKHAM, lb, lb, p, p) for lb in (4, 8) for p in (0, 1, 2)]
+    for cand in cands:
+        ms = _tune_models("fp32", sides)
+        b = G.Batch(ms)
+        b.force(*cand)
+        b.step(12)
+        got = [m.download_real(0) for m in ms]
+        if ref is None:
+            ref = got
+        else:
+            for x, y in zip(got, ref):
+                assert np.linalg.norm(x - y) <= 2e-6 * np.linalg.norm(y), cand
+    sides64 = [256, 96, 100]
+    base = None
+    for lb in (4, 8, 16):
+        for p in (0, 1, 2):
+            ms = _tune_models("fp64", sides64)
+            b = G.Batch(ms)
+            b.force(L.BATCH_STOCKHAM, L.BATCH_STOCKHAM, lb, lb, p, p)
+            b.step(12)
+            got = [m.download_real(0) for m in ms]
+            if base is None:
+                base = {0: got}
+            if p not in base:
+                base[p] = got
+            for x, y in zip(got, base[p]):  # same plan: the tile width changes nothing
+                assert np.array_equal(x, y)
+            for x, y in zip(got, base[0]):
+                assert np.linalg.norm(x - y) <= 1e-13 * np.linalg.norm(y)
+
+
+def test_autotuner_picks_valid_choices_and_keeps_fields():
+    """gopf_batch_tune times the candidates on the batch's own instances and restores their fields;
+    the tuned batch steps exactly like a batch forced to the same choices; a second batch of the same
+    kinds takes the cached choices."""
+    import gopf_gb300 as G
+    from gopf_gb300 import _lib as L
+
+    G.Batch.tune_reset()
+    sides = [1024, 512, 384, 256, 128, 128]
+    ms = _tune_models("fp32", sides)
+    before = [m.download_real(0) for m in ms]
+    b = G.Batch(ms)
+    b.tune(3)
+    for m, x in zip(ms, before):
+        assert np.array_equal(m.download_real(0), x)  # tuning left the fields alone
+        assert m.current_step == 0
+    choices = [b.choice(i) for i in range(len(sides))]
+    for s, c in zip(sides, choices):
+        assert c["xfam"] in (L.BATCH_LINE, L.BATCH_STOCKHAM_CT, L.BATCH_STOCKHAM)
+        if s == 128:
+            assert c["xfam"] != L.BATCH_LINE and c["yfam"] != L.BATCH_LINE  # no 128-point line engine
+        if c["xfam"] == L.BATCH_STOCKHAM:
+            assert c["lbx"] in (4, 8, 16) and c["lbx"] * s // 2 <= 4096
+    b.step(10)
+    tuned = [m.download_real(0) for m in ms]
+    # the same choices forced instance by instance (one batch per kind) step identically
+    from gopf_gb300.synthetic import uniform_field
+
+    for i, s in enumerate(sides):
+        m2 = ch_ctx(s, "fp32", 0.4 + 0.1 * i, 1.0 + 0.05 * i, 0.05, uniform_field(4000 + i, s * s, 0.5, 0.05))
+        b2 = G.Batch([m2])
+        c = choices[i]
+        b2.force(c["xfam"], c["yfam"], c["lbx"], c["lby"], c["xplan"], c["yplan"])
+        b2.step(10)
+        assert np.array_equal(m2.download_real(0), tuned[i])
+    # cached: a new batch of the same kinds gets the same choices
+    ms3 = _tune_models("fp32", sides)
+    b3 = G.Batch(ms3)
+    b3.tune(3)
+    assert [b3.choice(i) for i in range(len(sides))] == choices
