@@ -504,6 +504,16 @@ def run_sweep(args):
     sweep_bytes = float(sum(6 * (s // 2 + 1) * s * 8 for s, _, _ in params))
     models = sweep_models("fp32", params, indices=mine, device=local)
     batch = G.Batch(models)
+    tuned, tune_s = None, None
+    if not args.no_tune:
+        # the autotuner: kernel family, tile width and plan variant per kind of instance, timed on
+        # this rank's instances before the warm-up (fields restored afterwards)
+        t0 = time.perf_counter()
+        batch.tune(5)
+        tune_s = time.perf_counter() - t0
+        tuned = {}
+        for k, i in enumerate(mine):
+            tuned.setdefault(str(params[i][0]), batch.choice(k))
     stream = torch.cuda.Stream()
     batch.set_stream(stream.cuda_stream)
     warm = max(args.warmup, 3)
@@ -575,7 +585,9 @@ def run_sweep(args):
                           "dt": 0.05, "params_seed": 2, "init": "c0 = 0.5 + U(-0.05, 0.05), seed 1000 + i",
                           "parallelism": f"instances sharded over {world} GPU(s), no collective"
                                          if world > 1 else "single GPU",
-                          "rank_cells": rank_cells},
+                          "rank_cells": rank_cells,
+                          "tuned": tuned, "tune_seconds": tune_s,
+                          "families": "0 line engine, 1 compile-time Stockham, 2 runtime Stockham"},
                "sequential_value": seq, "speedup_vs_sequential": (batched / seq) if seq else None,
                # bytes one sweep step moves: per instance the x pass reads T and writes the group (2C),
                # the fused y pass reads the group and c-hat and writes c-hat and T (4C); FP32,
@@ -839,6 +851,7 @@ def main():
     ap.add_argument("--workload", default="ch3d", choices=["ch3d", "sweep", "adjoint", "elastic", "precision", "c1"])
     ap.add_argument("--tma", type=int, default=None, choices=[0, 1],
                     help="tile movement of the 256-point kernels: 0 plain loads, 1 TMA")
+    ap.add_argument("--no-tune", action="store_true", help="sweep: keep the built-in kernel choices")
     ap.add_argument("--check-steps", type=int, default=-1,
                     help="sweep: per-instance rel-L2 against FP64 after this many steps (-1: the configuration's "
                          "2000; 0: no check)")
