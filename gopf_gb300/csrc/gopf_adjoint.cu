@@ -64,7 +64,7 @@ __global__ void k_adj_kspace(Geom g, typename VecOf<R>::type *__restrict__ lamh,
         const double fx = (double)kx / g.X, fy = (double)jy / g.Y, fz = (double)jz / g.Z;
         const double k2 = fourpi2 * (fx * fx + fy * fy + fz * fz);
         const double D = 1.0 / (1.0 + dtMg * k2 * k2);
-        const double w = (kx == 0 || kx == g.H) ? 1.0 : 2.0;
+        const double w = (kx == 0 || 2 * kx == g.X) ? 1.0 : 2.0;
         const V l = lamh[idx], c = ch[idx], f = fh[idx];
         // Re(conj(l) * c) and Re(conj(l) * f)
         s1 += w * k2 * k2 * D * ((double)l.x * (double)c.x + (double)l.y * (double)c.y);

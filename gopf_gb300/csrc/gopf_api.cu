@@ -349,9 +349,9 @@ extern "C" int gopf_ctx_create(int ndim, const int *domain_size, int precision, 
     g.Y = ctx->dims[0];
     g.Z = (ndim == 3) ? ctx->dims[2] : 1;
     *out = ctx;
-    if (g.X % 2 != 0) return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "the column count (domainSize[1]) must be even");
+    const bool oddx = (g.X % 2) != 0; // odd column counts: row pairs through length-X transforms
     int rc;
-    if ((rc = check_len(g.X / 2, "half column", ctx))) return rc;
+    if ((rc = check_len(oddx ? g.X : g.X / 2, oddx ? "column" : "half column", ctx))) return rc;
     if ((rc = check_len(g.Y, "row", ctx))) return rc;
     if ((rc = check_len(g.Z, "depth", ctx))) return rc;
     g.H = g.X / 2;
@@ -360,12 +360,13 @@ extern "C" int gopf_ctx_create(int ndim, const int *domain_size, int precision, 
     g.C = g.S * g.Z;
     g.N = (long long)g.X * g.Y * g.Z;
     const int vb = (precision == GOPF_FP32) ? 8 : 16;
-    ctx->LBx = lb_for(g.H, vb);
+    ctx->LBx = lb_for(oddx ? g.KX : g.H, vb);
     ctx->LBy = lb_for(g.Y, vb);
     ctx->LBz = lb_for(g.Z, vb);
     if ((long long)ctx->LBx * g.H > 4096 || (long long)ctx->LBy * g.Y > 4096 || (long long)ctx->LBz * g.Z > 4096)
         return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "axis longer than 1024 (2048 columns) is not supported");
-    gopf_make_plan(g.H, 2, 0, ctx->planH);
+    if (oddx) gopf_make_plan(g.X, 1, 0, ctx->planH); // the x transform of the row pairs
+    else gopf_make_plan(g.H, 2, 0, ctx->planH);
     gopf_make_plan(g.Y, 1, 0, ctx->planY);
     gopf_make_plan(g.Z, 1, 0, ctx->planZ);
     if (device < 0) return GOPF_OK; // host-only: equations can be defined and compiled, nothing runs
@@ -1877,8 +1878,9 @@ extern "C" int gopf_reduce(gopf_ctx *ctx, int field, int what, double *out)
 }
 
 // PointMonitor.Add (pf/monitor.go:27-30) for n sites: the real field at node i is the inverse x
-// transform of T's row (z, y) at column x, c = Re T(0) + (-1)^x Re T(H) + 2 sum_{0<kx<H} Re(T(kx)
-// e^{2 pi i kx x / X}) (T is c-hat/N already inverse-transformed along z and y).  One warp per
+// transform of T's row (z, y) at column x, c = Re T(0) + (-1)^x Re T(X/2) + 2 sum_{0<kx<X/2} Re(T(kx)
+// e^{2 pi i kx x / X}) (T is c-hat/N already inverse-transformed along z and y; no Nyquist term for
+// odd X).  One warp per
 // site, FP64 sums.
 template <typename R>
 __global__ void k_point_values(const typename VecOf<R>::type *__restrict__ T, Geom g, const long long *__restrict__ sites,
@@ -1891,7 +1893,7 @@ __global__ void k_point_values(const typename VecOf<R>::type *__restrict__ T, Ge
     double acc = 0.0;
     for (int kx = lane; kx < g.KX; kx += 32) {
         const typename VecOf<R>::type t = T[z * g.S + (long long)kx * g.Y + y];
-        if (kx == 0 || kx == g.H) {
+        if (kx == 0 || 2 * kx == g.X) { // self-conjugate columns (the Nyquist one only for even X)
             acc += ((kx == 0 || (x & 1) == 0) ? 1.0 : -1.0) * (double)t.x;
         } else {
             double sn, cs;

@@ -346,11 +346,11 @@ template <typename R> static int batch_build(gopf_batch *b)
         bi.lbx = c->LBx;
         bi.lby = c->LBy;
         bi.herm_off = hoff;
-        hoff += 2LL * g.Y;
+        hoff += ((g.X & 1) ? 1LL : 2LL) * g.Y; // the kx = 0 line, and kx = X/2 for even X
         int xc = 0, yc = 0, fx = -1, fy = -1;
         if (sizeof(R) == 4) {
             for (int k = 1; k < 7; ++k) {
-                if (g.H == XCLS_H[k] && c->LBx == XCLS_LB[k]) xc = k;
+                if (g.H == XCLS_H[k] && c->LBx == XCLS_LB[k] && !(g.X & 1)) xc = k;
                 if (g.Y == YCLS_N[k] && c->LBy == YCLS_LB[k]) yc = k;
             }
             for (int k = 0; k < 5; ++k) {
@@ -371,8 +371,9 @@ template <typename R> static int batch_build(gopf_batch *b)
         if (yf != GOPF_BATCH_LINE) fy = -1;
         if (xf == GOPF_BATCH_STOCKHAM) {
             xc = 0;
-            if (batch_lb_ok(ch.lbx, g.H)) bi.lbx = ch.lbx;
-            if (ch.xplan && gopf_make_plan(g.H, 2, ch.xplan, xa.planH)) ef.xplan = ch.xplan;
+            const bool odd = (g.X & 1) != 0; // odd X: row pairs through length-X transforms
+            if (batch_lb_ok(ch.lbx, odd ? g.KX : g.H)) bi.lbx = ch.lbx;
+            if (ch.xplan && gopf_make_plan(odd ? g.X : g.H, odd ? 1 : 2, ch.xplan, xa.planH)) ef.xplan = ch.xplan;
             else xa.planH = c->planH;
         }
         if (yf == GOPF_BATCH_STOCKHAM) {
@@ -396,7 +397,7 @@ template <typename R> static int batch_build(gopf_batch *b)
             const int lb = bi.lbx;
             const int ntx = (g.Y + lb - 1) / lb;
             for (int t = 0; t < ntx; ++t) xs[xc].push_back({g.H * lb, make_int2((int)i, t)});
-            smem_x[xc] = std::max(smem_x[xc], xpass_smem_bytes(g, lb, vb));
+            smem_x[xc] = std::max(smem_x[xc], xpass_smem_bytes(g, lb, vb, (g.X & 1) ? 3 : 2));
         }
         if (fy >= 0) { // line engine: tiles of LPB lines
             yc = (nb > 1 ? 21 : 11) + fy;
@@ -725,12 +726,14 @@ std::vector<BatchChoice> pass_candidates(const gopf_ctx *c, bool xpass, const Ba
         add(GOPF_BATCH_LINE, 0, 0);
         add(GOPF_BATCH_STOCKHAM_CT, 0, 0);
     }
-    const int n = xpass ? c->g.H : c->g.Y;
+    const bool odd = xpass && (c->g.X & 1);
+    const int n = xpass ? (odd ? c->g.KX : c->g.H) : c->g.Y;             // tile-width bound
+    const int pn = xpass ? (odd ? c->g.X : c->g.H) : c->g.Y;             // transform length
     for (int lb : {4, 8, 16})
         if (batch_lb_ok(lb, n))
             for (int plan = 0; plan < 3; ++plan) {
                 gopf::LinePlan pl;
-                if (gopf_make_plan(n, xpass ? 2 : 1, plan, pl)) add(GOPF_BATCH_STOCKHAM, lb, plan);
+                if (gopf_make_plan(pn, (xpass && !odd) ? 2 : 1, plan, pl)) add(GOPF_BATCH_STOCKHAM, lb, plan);
             }
     return out;
 }

@@ -91,12 +91,49 @@ __device__ __forceinline__ void block_reduce_store(double *vals, double *red, do
 // Load the spectral tile (z, all kx, LB rows from y0) of `in`, undo the r2c
 // packing and inverse transform along x: on return A[m*LB + l] = (c[2m],
 // c[2m+1]) of row y0 + l (times the transform's normalisation).
+// Odd column counts X (no Nyquist column, KX = (X + 1)/2): rows 2p and 2p + 1 of the tile form one
+// complex line c_2p + i c_2p+1 of length X, transformed by the length-X plan (planH holds it), so
+// the tile holds A[x * LB/2 + p] = (c_2p[x], c_2p+1[x]).  The half spectra are Hermitian-extended
+// into the line from a staging copy of the tile (stage: KX * LB elements after the block's tiles).
+template <typename R, int LB, int PERB>
+__device__ __forceinline__ void xload_c2r_odd(typename VecOf<R>::type *A, typename VecOf<R>::type *stage,
+                                              const typename VecOf<R>::type *__restrict__ in, long long sbase,
+                                              int nl, const Geom &g, const LinePlan &planX,
+                                              const typename VecOf<R>::type *__restrict__ twX)
+{
+    typedef typename VecOf<R>::type V;
+    constexpr int LBSH = Log2<LB>::v, P = LB / 2;
+    const int X = g.X, KX = g.KX, Y = g.Y;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int e = tid; e < KX * LB; e += nt) {
+        const int kx = e >> LBSH, l = e & (LB - 1);
+        ga_copy(&stage[e], in + sbase + (long long)kx * Y + (l < nl ? l : 0), l < nl);
+    }
+    ga_wait();
+    __syncthreads();
+    for (int e = tid; e < KX * P; e += nt) {
+        const int kx = e / P, q = e - kx * P;
+        const V a = stage[kx * LB + 2 * q], b = stage[kx * LB + 2 * q + 1];
+        A[kx * P + q] = cmk<V>(a.x - b.y, a.y + b.x); // A(k) + i B(k)
+        if (kx > 0) A[(X - kx) * P + q] = cmk<V>(a.x + b.y, b.x - a.y); // conj A(k) + i conj B(k) at X - k
+    }
+    __syncthreads();
+    fft_tile<true, P, PERB>(A, P, planX, twX);
+}
+
 template <typename R, int LB, int PERB, int NCT = 0>
 __device__ __forceinline__ void xload_c2r(typename VecOf<R>::type *A, const typename VecOf<R>::type *__restrict__ in,
                                           long long sbase, int nl, const Geom &g, const LinePlan &planH,
-                                          const typename VecOf<R>::type *__restrict__ twX)
+                                          const typename VecOf<R>::type *__restrict__ twX,
+                                          typename VecOf<R>::type *stage = nullptr)
 {
     typedef typename VecOf<R>::type V;
+    if constexpr (NCT == 0) {
+        if (g.X & 1) {
+            xload_c2r_odd<R, LB, PERB>(A, stage, in, sbase, nl, g, planH, twX);
+            return;
+        }
+    }
     constexpr int LBSH = Log2<LB>::v;
     const int H = NCT ? NCT : g.H, KX = H + 1, Y = g.Y;
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -139,6 +176,24 @@ __device__ __forceinline__ void xr2c_store(typename VecOf<R>::type *B, typename 
                                            const typename VecOf<R>::type *__restrict__ twX)
 {
     typedef typename VecOf<R>::type V;
+    if constexpr (NCT == 0) {
+        if (g.X & 1) { // odd X: forward transform of the row pairs, then X_a(k) = (Z(k) + conj Z(-k))/2
+                       // (row 2p) and X_b(k) = (Z(k) - conj Z(-k))/(2i) (row 2p + 1)
+            constexpr int P = LB / 2;
+            const int X = g.X, KX = g.KX, Y = g.Y;
+            fft_tile<false, P, PERB>(B, P, planH, twX);
+            const R half = (R)0.5;
+            for (int e = threadIdx.x; e < KX * LB; e += blockDim.x) {
+                const int kx = e / LB, l = e - kx * LB, q = l >> 1;
+                const V z = B[kx * P + q], w = B[(kx ? X - kx : 0) * P + q];
+                const V o = (l & 1) ? cmk<V>(half * (z.y + w.y), half * (w.x - z.x))
+                                    : cmk<V>(half * (z.x + w.x), half * (z.y - w.y));
+                if (l < nl) out[sbase + (long long)kx * Y + l] = o;
+            }
+            __syncthreads();
+            return;
+        }
+    }
     constexpr int LBSH = Log2<LB>::v;
     const int H = NCT ? NCT : g.H, KX = H + 1, Y = g.Y;
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -189,6 +244,23 @@ template <typename R> __device__ __forceinline__ R elastic_q(R c, R w, R e0, R s
 // One x-pass tile: LB rows starting at row ty*LB of depth plane z.  MULTI: the multi-field
 // program only (a separate instantiation, so the single-field kernels do not carry its registers).
 // NCT > 0: the x transform has the compile-time length NCT (== g.H).
+// Element e of a real-space tile holds two reals.  Even X: A[m*LB + l] = (c[2m], c[2m+1]) of row
+// y0 + l; odd X: A[x*LB/2 + p] = (c[x] of row y0 + 2p, c[x] of row y0 + 2p + 1).  tile_rows gives the
+// tile-relative rows of the two reals and tile_count the number of elements.
+template <int LB> __device__ __forceinline__ void tile_rows(bool odd, int e, int &r0, int &r1)
+{
+    if (odd) {
+        const int p = e & (LB / 2 - 1);
+        r0 = 2 * p;
+        r1 = 2 * p + 1;
+    } else {
+        r0 = r1 = e & (LB - 1);
+    }
+}
+
+// One x-pass tile: LB rows starting at row ty*LB of depth plane z.  MULTI: the multi-field
+// program only (a separate instantiation, so the single-field kernels do not carry its registers).
+// NCT > 0: the x transform has the compile-time length NCT (== g.H).
 template <typename R, int LB, int PERB, bool MULTI = false, int NCT = 0>
 __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
 {
@@ -196,7 +268,9 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int LBSH = Log2<LB>::v;
     const Geom &g = a.g;
+    const bool odd = (NCT == 0) && (g.X & 1);
     const int H = NCT ? NCT : g.H, KX = H + 1, Y = g.Y;
+    const int npos = odd ? g.X * (LB / 2) : H * LB; // tile elements (two reals each)
     V *A = reinterpret_cast<V *>(smem_raw);
     V *B = A + KX * LB;
     const int y0 = ty * LB;
@@ -205,23 +279,39 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
     const int tid = threadIdx.x, nt = blockDim.x;
     const V zero = cmk<V>((R)0, (R)0);
     const V *__restrict__ twX = a.twX;
+    (void)zero;
+    (void)LBSH;
+
+    // real rows of field rin into tile T (asynchronous copies; rows past the grid read as zeros)
+    auto load_real = [&](V *T, const R *rin) {
+        if (odd) {
+            const R *base = rin + ((long long)z * Y + y0) * g.X;
+            for (int e = tid; e < npos; e += nt) {
+                const int x = e / (LB / 2), p = e - x * (LB / 2);
+                R *d = reinterpret_cast<R *>(&T[e]);
+                ga_copy(d, base + (long long)(2 * p < nl ? 2 * p : 0) * g.X + x, 2 * p < nl);
+                ga_copy(d + 1, base + (long long)(2 * p + 1 < nl ? 2 * p + 1 : 0) * g.X + x, 2 * p + 1 < nl);
+            }
+        } else {
+            const V *rin2 = reinterpret_cast<const V *>(rin) + ((long long)z * Y + y0) * H;
+            for (int e = tid; e < LB * H; e += nt) {
+                const int l = e / H, m = e - l * H;
+                ga_copy(&T[m * LB + l], rin2 + (long long)(l < nl ? l : 0) * H + m, l < nl);
+            }
+        }
+    };
 
     if constexpr (MULTI) {
         // one tile per field, then each group's monomials into the tile after them
         const MonoTable &mt = a.mono;
         const int tsz = KX * LB;
         V *Bm = A + mt.nin * tsz;
+        V *stage = A + (mt.nin + 1) * tsz;
         if (a.in_mode == XIN_SPECTRAL) {
             for (int f = 0; f < mt.nin; ++f)
-                xload_c2r<R, LB, PERB, NCT>(A + f * tsz, a.inF[f], sbase, nl, g, a.planH, twX);
-        } else { // real rows of every field (rinF[f]), as pairs A[m*LB + l] = (c[2m], c[2m+1])
-            for (int f = 0; f < mt.nin; ++f) {
-                const V *rin2 = reinterpret_cast<const V *>(a.rinF[f]) + ((long long)z * Y + y0) * H;
-                for (int e = tid; e < LB * H; e += nt) {
-                    const int l = e / H, m = e - l * H;
-                    ga_copy(&A[f * tsz + m * LB + l], rin2 + (long long)(l < nl ? l : 0) * H + m, l < nl);
-                }
-            }
+                xload_c2r<R, LB, PERB, NCT>(A + f * tsz, a.inF[f], sbase, nl, g, a.planH, twX, stage);
+        } else { // real rows of every field (rinF[f])
+            for (int f = 0; f < mt.nin; ++f) load_real(A + f * tsz, a.rinF[f]);
             ga_wait();
             __syncthreads();
         }
@@ -232,14 +322,17 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
             vals[RED_MIN] = INFINITY;
             vals[RED_MAX] = -INFINITY;
             const V *F = A + a.redfield * tsz;
-            for (int e = tid; e < H * LB; e += nt)
-                if ((e & (LB - 1)) < nl) vals[RED_SUM] += (double)F[e].x + (double)F[e].y;
+            for (int e = tid; e < npos; e += nt) {
+                int r0, r1;
+                tile_rows<LB>(odd, e, r0, r1);
+                vals[RED_SUM] += (r0 < nl ? (double)F[e].x : 0.0) + (r1 < nl ? (double)F[e].y : 0.0);
+            }
             __shared__ double shredm[32 * RED_SLOTS];
             block_reduce_store(vals, a.red, shredm);
         }
         for (int grp = 0; grp < mt.ngrp; ++grp) {
             double gsum = 0.0;
-            for (int e = tid; e < H * LB; e += nt) {
+            for (int e = tid; e < npos; e += nt) {
                 R vx = (R)0, vy = (R)0;
                 for (int m = 0; m < mt.nmono[grp]; ++m) {
                     R px = (R)mt.coef[grp][m], py = px;
@@ -254,7 +347,11 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
                     vy += py;
                 }
                 Bm[e] = cmk<V>(vx, vy);
-                if (a.red2 && grp == a.redgrp && (e & (LB - 1)) < nl) gsum += (double)vx + (double)vy;
+                if (a.red2 && grp == a.redgrp) {
+                    int r0, r1;
+                    tile_rows<LB>(odd, e, r0, r1);
+                    gsum += (r0 < nl ? (double)vx : 0.0) + (r1 < nl ? (double)vy : 0.0);
+                }
             }
             if (a.red2 && grp == a.redgrp) {
                 double vals[RED_SLOTS];
@@ -272,24 +369,29 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
         return;
     }
 
+    V *stage = A + 2 * KX * LB;
     if (a.in_mode == XIN_SPECTRAL) {
-        xload_c2r<R, LB, PERB, NCT>(A, a.in, sbase, nl, g, a.planH, twX);
+        xload_c2r<R, LB, PERB, NCT>(A, a.in, sbase, nl, g, a.planH, twX, stage);
     } else {
-        const V *rin2 = reinterpret_cast<const V *>(a.rin) + ((long long)z * Y + y0) * H;
-        for (int e = tid; e < LB * H; e += nt) {
-            const int l = e / H, m = e - l * H;
-            ga_copy(&A[m * LB + l], rin2 + (long long)(l < nl ? l : 0) * H + m, l < nl);
-        }
+        load_real(A, a.rin);
         ga_wait();
         __syncthreads();
     }
 
-    // A[m*LB + l] = (c[2m], c[2m+1]) of row y0 + l
     if (a.rout) {
-        V *rout2 = reinterpret_cast<V *>(a.rout) + ((long long)z * Y + y0) * H;
-        for (int e = tid; e < LB * H; e += nt) {
-            const int l = e / H, m = e - l * H;
-            if (l < nl) rout2[(long long)l * H + m] = A[m * LB + l];
+        if (odd) {
+            R *base = a.rout + ((long long)z * Y + y0) * g.X;
+            for (int e = tid; e < npos; e += nt) {
+                const int x = e / (LB / 2), p = e - x * (LB / 2);
+                if (2 * p < nl) base[(long long)(2 * p) * g.X + x] = A[e].x;
+                if (2 * p + 1 < nl) base[(long long)(2 * p + 1) * g.X + x] = A[e].y;
+            }
+        } else {
+            V *rout2 = reinterpret_cast<V *>(a.rout) + ((long long)z * Y + y0) * H;
+            for (int e = tid; e < LB * H; e += nt) {
+                const int l = e / H, m = e - l * H;
+                if (l < nl) rout2[(long long)l * H + m] = A[m * LB + l];
+            }
         }
     }
     if (a.red) {
@@ -298,17 +400,21 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
         for (int s = 0; s < RED_SLOTS; ++s) vals[s] = 0.0;
         vals[RED_MIN] = INFINITY;
         vals[RED_MAX] = -INFINITY;
-        for (int e = tid; e < H * LB; e += nt) {
-            const int l = e & (LB - 1);
-            if (l < nl) {
-                const V c = A[e];
-                const double c0 = (double)c.x, c1 = (double)c.y;
-                vals[RED_SUM] += c0 + c1;
-                vals[RED_SUMSQ] += c0 * c0 + c1 * c1;
-                vals[RED_MIN] = fmin(vals[RED_MIN], fmin(c0, c1));
-                vals[RED_MAX] = fmax(vals[RED_MAX], fmax(c0, c1));
-                vals[RED_NONFINITE] += (isfinite(c0) ? 0.0 : 1.0) + (isfinite(c1) ? 0.0 : 1.0);
-            }
+        for (int e = tid; e < npos; e += nt) {
+            int r0, r1;
+            tile_rows<LB>(odd, e, r0, r1);
+            const V c = A[e];
+            const double cv[2] = {(double)c.x, (double)c.y};
+            const bool ok[2] = {r0 < nl, r1 < nl};
+#pragma unroll
+            for (int q = 0; q < 2; ++q)
+                if (ok[q]) {
+                    vals[RED_SUM] += cv[q];
+                    vals[RED_SUMSQ] += cv[q] * cv[q];
+                    vals[RED_MIN] = fmin(vals[RED_MIN], cv[q]);
+                    vals[RED_MAX] = fmax(vals[RED_MAX], cv[q]);
+                    vals[RED_NONFINITE] += isfinite(cv[q]) ? 0.0 : 1.0;
+                }
         }
         __shared__ double shred[32 * RED_SLOTS];
         block_reduce_store(vals, a.red, shred);
@@ -316,9 +422,9 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
 
     if (a.program == XP_ELASTIC_Q) {
         // w = c2r(in2) into B, then q into B, then r2c into out[0]
-        xload_c2r<R, LB, PERB, NCT>(B, a.in2, sbase, nl, g, a.planH, twX);
+        xload_c2r<R, LB, PERB, NCT>(B, a.in2, sbase, nl, g, a.planH, twX, stage);
         const R e0 = (R)a.e0, es = (R)a.escale;
-        for (int e = tid; e < H * LB; e += nt) {
+        for (int e = tid; e < npos; e += nt) {
             const V c = A[e], w = B[e];
             B[e] = cmk<V>(elastic_q<R>(c.x, w.x, e0, es), elastic_q<R>(c.y, w.y, e0, es));
         }
@@ -329,11 +435,15 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
 
     for (int grp = 0; grp < a.ngrp_out; ++grp) {
         double gsum = 0.0;
-        for (int e = tid; e < H * LB; e += nt) {
+        for (int e = tid; e < npos; e += nt) {
             const V c = A[e];
             const V r = a.identity ? c : cmk<V>(poly_eval<R>(a.pw, grp, c.x), poly_eval<R>(a.pw, grp, c.y));
             B[e] = r;
-            if (a.red2 && grp == a.redgrp && (e & (LB - 1)) < nl) gsum += (double)r.x + (double)r.y;
+            if (a.red2 && grp == a.redgrp) {
+                int r0, r1;
+                tile_rows<LB>(odd, e, r0, r1);
+                gsum += (r0 < nl ? (double)r.x : 0.0) + (r1 < nl ? (double)r.y : 0.0);
+            }
         }
         if (a.red2 && grp == a.redgrp) {
             double vals[RED_SLOTS];
@@ -752,9 +862,11 @@ template <typename R, int LB> static cudaError_t launch_xpass_lb(const XPassArgs
 {
     typedef typename VecOf<R>::type V;
     const bool multi = (a.program == XP_MULTI);
-    const int smem = xpass_smem_bytes(a.g, LB, sizeof(V), multi ? a.mono.nin + 1 : 2);
-    if (!threads_ok((long long)LB * a.g.H, perb<R>())) return cudaErrorInvalidConfiguration;
-    const int nt = pick_threads((long long)LB * a.g.H, perb<R>());
+    const bool odd = (a.g.X & 1) != 0; // odd column count: a staging tile and length-X row-pair lines
+    const int smem = xpass_smem_bytes(a.g, LB, sizeof(V), (multi ? a.mono.nin + 1 : 2) + (odd ? 1 : 0));
+    const long long work = odd ? (long long)(LB / 2) * a.g.X : (long long)LB * a.g.H;
+    if (!threads_ok(work, perb<R>())) return cudaErrorInvalidConfiguration;
+    const int nt = pick_threads(work, perb<R>());
     dim3 grid((a.g.Y + LB - 1) / LB, a.g.Z);
     cudaError_t e;
     if (multi) {

@@ -60,7 +60,7 @@ __device__ __forceinline__ void mode_of(long long i, const Geom &g, double &m, d
     const int zz = (2 * z > g.Z) ? g.Z - (int)z : (int)z;
     const double fx = (double)kx / (double)g.X, fy = (double)yy / (double)g.Y, fz = (double)zz / (double)g.Z;
     m = -39.478417604357434475337963999504 * (fx * fx + fy * fy + fz * fz);
-    w = (kx == 0 || kx == g.H) ? 1.0 : 2.0;
+    w = (kx == 0 || 2 * kx == g.X) ? 1.0 : 2.0;
 }
 
 __device__ __forceinline__ double sym_eval(const Sym &s, double m)

@@ -137,7 +137,7 @@ __global__ void k_volcons_finalize(const double *__restrict__ red_field, const d
     vc[4] = coef * vc[0];
 }
 
-// Hermitian projection of the self-conjugate planes kx = 0 and kx = X/2 of the
+// Hermitian projection of the self-conjugate planes kx = 0 and (even X) kx = X/2 of the
 // half spectrum: c(k) <- (c(k) + conj c(-k)) / 2 for the pairs (ky, kz) <-> (-ky, -kz).
 // A real field cannot feed back into the anti-Hermitian part of these planes,
 // so without the projection FFT round-off there grows like 1/(1 - dt L(k)) per
@@ -147,7 +147,8 @@ template <typename V> __global__ void k_hermitian_planes(V *__restrict__ c, Geom
 {
     if (stepctr && blockIdx.x == 0 && threadIdx.x == 0) *stepctr += 1; // after this step's noise draws
     const long long per = (long long)g.Y * g.Z;
-    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < 2 * per;
+    const int nplanes = (g.X & 1) ? 1 : 2; // odd X has no Nyquist plane
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < nplanes * per;
          idx += (long long)gridDim.x * blockDim.x) {
         const int plane = (int)(idx / per);
         const long long r = idx - plane * per;
@@ -172,7 +173,7 @@ using namespace gopf;
 
 cudaError_t gopf_launch_hermitian_planes(gopf_ctx *ctx, void *state, cudaStream_t st)
 {
-    const long long n = 2LL * ctx->g.Y * ctx->g.Z;
+    const long long n = ((ctx->g.X & 1) ? 1LL : 2LL) * ctx->g.Y * ctx->g.Z;
     const unsigned blocks = (unsigned)std::min<long long>((n + 255) / 256, 152 * 8);
     unsigned long long *ctr = (state == ctx->d_state && ctx->noise.kind) ? ctx->d_stepctr : nullptr;
     if (!st) st = ctx->stream;

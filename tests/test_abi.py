@@ -165,11 +165,16 @@ def test_cubic_3d_only():
     assert e.value.status == 6
 
 
-def test_odd_columns_rejected():
+def test_lengths_with_prime_factors_above_seven_rejected():
+    """Odd column counts are accepted (8 x 9 has a plan); a factor of 11 or 13 has none."""
     import gopf_gb300 as G
 
-    with pytest.raises(G.GopfError):
-        G.Model([8, 9], "fp32", device=-1)
+    G.Model([8, 9], "fp32", device=-1).close()
+    G.Model([25, 49], "fp64", device=-1).close()
+    for dims in ([8, 11], [13, 8], [22, 22]):
+        with pytest.raises(G.GopfError) as e:
+            G.Model(dims, "fp32", device=-1)
+        assert e.value.status == 6
 
 
 def test_freq_and_conjugate_node_host_only():
