@@ -13,7 +13,12 @@
 // Inner products are taken in k space (Parseval, half spectrum weighted 2
 // off the self-conjugate planes).  The forward run keeps the field every
 // `every` steps; the backward run recomputes each segment from its
-// checkpoint and walks it backwards.
+// checkpoint and walks it backwards.  A segment's recompute and backward
+// walk are one captured CUDA graph (replayed for every segment of that
+// length); a backward step is five launches in 2D: the x pass forming
+// r2c_x(c^3 - c), one y pass forward-transforming that and lambda, the k-space
+// product and gradient sums, one inverse y pass, and an x pass that forms
+// lambda_n = mu - dt M (3c^2 - 1) nu and its r2c_x for the next step.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -24,25 +29,6 @@
 #include "gopf_kernels.cuh"
 
 namespace gopf {
-
-template <typename R> __global__ void k_fpoly(const R *__restrict__ c, R *__restrict__ f, long long n)
-{
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const R x = c[i];
-        f[i] = x * x * x - x;
-    }
-}
-
-// lambda <- mu - dt M (3 c^2 - 1) nu
-template <typename R>
-__global__ void k_adj_real(const R *__restrict__ mu, const R *__restrict__ nu, const R *__restrict__ c, R *__restrict__ lam,
-                           R dtM, long long n)
-{
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const R x = c[i];
-        lam[i] = mu[i] - dtM * ((R)3 * x * x - (R)1) * nu[i];
-    }
-}
 
 // k space: mu = D lam / N, nu = k^2 D lam / N (in place of lam-hat and f-hat),
 // plus the two gradient sums (FP64, atomically accumulated per block).
@@ -110,11 +96,25 @@ struct gopf_adjoint_state {
     double gamma = 0.0, M = 0.0, dt = 0.0;
     void *d_ckpt = nullptr;  // (nsteps/every + 1) real fields
     void *d_seg = nullptr;   // every + 1 real fields
-    void *d_r[4] = {nullptr, nullptr, nullptr, nullptr}; // real work: lambda, f, mu, nu
+    void *d_segs = nullptr;  // every + 1 spectra (c-hat of the recomputed steps)
+    void *d_stage = nullptr; // the checkpoint a segment graph starts from
+    void *d_r[4] = {nullptr, nullptr, nullptr, nullptr}; // real work: lambda (the others unused)
     void *d_s[3] = {nullptr, nullptr, nullptr};           // spectral work
     double *d_sums = nullptr;
     int nckpt = 0;
+    // captured segment sweeps (recompute + backward), full length and the shorter last one
+    cudaGraphExec_t g_full = nullptr, g_tail = nullptr;
+    int g_full_len = 0, g_tail_len = 0;
+    double g_key[3] = {0.0, 0.0, 0.0}; // gamma, M, dt the graphs were captured with
 };
+
+static void adj_drop_graphs(gopf_adjoint_state *st)
+{
+    if (st->g_full) cudaGraphExecDestroy(st->g_full);
+    if (st->g_tail) cudaGraphExecDestroy(st->g_tail);
+    st->g_full = st->g_tail = nullptr;
+    st->g_full_len = st->g_tail_len = 0;
+}
 
 static int afail(gopf_ctx *ctx, cudaError_t e, const char *w)
 {
@@ -130,77 +130,127 @@ static int afail(gopf_ctx *ctx, cudaError_t e, const char *w)
 
 static unsigned ew(long long n) { return (unsigned)std::min<long long>((n + 255) / 256, 152 * 16); }
 
-// real device array -> spectrum (unnormalised forward transform)
-template <typename R> static cudaError_t r2c(gopf_ctx *ctx, const R *real, typename VecOf<R>::type *spec)
-{
-    typedef typename VecOf<R>::type V;
-    XPassArgs<R> xa;
-    memset(&xa, 0, sizeof(xa));
-    xa.g = ctx->g;
-    xa.planH = ctx->planH;
-    xa.twX = (const V *)ctx->d_twX;
-    xa.in_mode = XIN_REAL;
-    xa.rin = real;
-    xa.out[0] = spec;
-    xa.ngrp_out = 1;
-    xa.identity = 1;
-    xa.allow_fast = ctx->use_fast;
-    cudaError_t e = launch_xpass<R>(xa, ctx->LBx, ctx->stream);
-    if (e != cudaSuccess) return e;
-    PassArgs<R> pa;
-    memset(&pa, 0, sizeof(pa));
-    pa.g = ctx->g;
-    pa.plan = ctx->planY;
-    pa.tw = (const V *)ctx->d_twY;
-    pa.mode = PM_FWD;
-    pa.buf[0] = spec;
-    pa.nbuf = 1;
-    pa.allow_fast = ctx->use_fast;
-    if ((e = launch_cpass<R>(pa, ctx->LBy, ctx->stream)) != cudaSuccess) return e;
-    if (ctx->g.Z > 1) {
-        pa.plan = ctx->planZ;
-        pa.tw = (const V *)ctx->d_twZ;
-        if ((e = launch_spass<R>(pa, ctx->LBz, ctx->stream)) != cudaSuccess) return e;
-    }
-    return cudaSuccess;
-}
-
-// spectrum -> real device array (unnormalised inverse transform; spec is overwritten)
-template <typename R> static cudaError_t c2r(gopf_ctx *ctx, typename VecOf<R>::type *spec, R *real)
-{
-    typedef typename VecOf<R>::type V;
-    cudaError_t e;
-    PassArgs<R> pa;
-    memset(&pa, 0, sizeof(pa));
-    pa.g = ctx->g;
-    pa.mode = PM_INV;
-    pa.buf[0] = spec;
-    pa.nbuf = 1;
-    pa.allow_fast = ctx->use_fast;
-    if (ctx->g.Z > 1) {
-        pa.plan = ctx->planZ;
-        pa.tw = (const V *)ctx->d_twZ;
-        if ((e = launch_spass<R>(pa, ctx->LBz, ctx->stream)) != cudaSuccess) return e;
-    }
-    pa.plan = ctx->planY;
-    pa.tw = (const V *)ctx->d_twY;
-    if ((e = launch_cpass<R>(pa, ctx->LBy, ctx->stream)) != cudaSuccess) return e;
-    XPassArgs<R> xa;
-    memset(&xa, 0, sizeof(xa));
-    xa.g = ctx->g;
-    xa.planH = ctx->planH;
-    xa.twX = (const V *)ctx->d_twX;
-    xa.in_mode = XIN_SPECTRAL;
-    xa.in = spec;
-    xa.rout = real;
-    xa.allow_fast = ctx->use_fast;
-    return launch_xpass<R>(xa, ctx->LBx, ctx->stream);
-}
-
 // real field of the current state (c = c2r of T) into dst
 int gopf_state_to_real(gopf_ctx *ctx, void *dst);
 int gopf_real_to_state(gopf_ctx *ctx, const void *src);
 int gopf_step_device(gopf_ctx *ctx, long long n);
+
+// One segment's sweep, stream-ordered (captured into a graph by the caller): recompute c_{s0+1} ..
+// c_{s0+len} from the checkpoint in d_stage, keeping each step's real field and c-hat, then walk
+// the steps backwards.  Per backward step n, with Lx = the x-transformed lambda_{n+1} in S[0]:
+//   x pass   : f(c_n) = c_n^3 - c_n from the real rows, r2c along x          -> S[1]
+//   y (z)    : forward of S[1] and S[0] in one launch                        -> F, Lambda
+//   k space  : the two gradient sums; mu-hat = D Lambda / N -> S[0], nu-hat = k^2 D Lambda / N -> S[1]
+//   (z) y    : inverse of S[0] and S[1] in one launch
+//   x pass   : lambda_n = mu - dt M (3 c_n^2 - 1) nu (into the real lambda) and r2c along x -> S[0]
+template <typename R> static int adj_segment(gopf_ctx *ctx, gopf_adjoint_state *st, int len)
+{
+    typedef typename VecOf<R>::type V;
+    const Geom &g = ctx->g;
+    const size_t rb = sizeof(R) * g.N, sb = sizeof(V) * g.C;
+    R *lam = (R *)st->d_r[0];
+    V *S0 = (V *)st->d_s[0], *S1 = (V *)st->d_s[1];
+    const double dtM = st->dt * st->M, dtMg = st->dt * st->M * st->gamma, invN = 1.0 / (double)g.N;
+    int rc;
+    if ((rc = gopf_real_to_state(ctx, st->d_stage))) return rc;
+    ACK(cudaMemcpyAsync(st->d_seg, st->d_stage, rb, cudaMemcpyDeviceToDevice, ctx->stream));
+    for (int n = 0; n < len; ++n) {
+        if ((rc = gopf_step_device(ctx, 1))) return rc;
+        if ((rc = gopf_state_to_real(ctx, (char *)st->d_seg + (size_t)(n + 1) * rb))) return rc;
+        ACK(cudaMemcpyAsync((char *)st->d_segs + (size_t)(n + 1) * sb, ctx->d_state, sb, cudaMemcpyDeviceToDevice,
+                            ctx->stream));
+    }
+    for (int n = len - 1; n >= 0; --n) {
+        const R *cn = (const R *)((char *)st->d_seg + (size_t)n * rb);
+        const V *chat1 = (const V *)((char *)st->d_segs + (size_t)(n + 1) * sb);
+        XPassArgs<R> xa;
+        memset(&xa, 0, sizeof(xa));
+        xa.g = g;
+        xa.planH = ctx->planH;
+        xa.twX = (const V *)ctx->d_twX;
+        xa.allow_fast = ctx->use_fast;
+        xa.status = ctx->d_status;
+        xa.in_mode = XIN_REAL;
+        xa.rin = cn;
+        xa.out[0] = S1;
+        xa.ngrp_out = 1;
+        xa.pw.ngrp = 1;
+        xa.pw.nterm[0] = 2;
+        xa.pw.pw[0][0] = 3;
+        xa.pw.coef[0][0] = 1.0;
+        xa.pw.pw[0][1] = 1;
+        xa.pw.coef[0][1] = -1.0;
+        pw_densify(xa.pw);
+        ACK(launch_xpass<R>(xa, ctx->LBx, ctx->stream));
+        PassArgs<R> pa;
+        memset(&pa, 0, sizeof(pa));
+        pa.g = g;
+        pa.plan = ctx->planY;
+        pa.tw = (const V *)ctx->d_twY;
+        pa.mode = PM_FWD;
+        pa.buf[0] = S1;
+        pa.buf[1] = S0;
+        pa.nbuf = 2;
+        pa.allow_fast = ctx->use_fast;
+        pa.status = ctx->d_status;
+        ACK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+        if (g.Z > 1) {
+            PassArgs<R> za = pa;
+            za.plan = ctx->planZ;
+            za.tw = (const V *)ctx->d_twZ;
+            ACK(launch_spass<R>(za, ctx->LBz, ctx->stream));
+        }
+        k_adj_kspace<R><<<ew(g.C), 256, 0, ctx->stream>>>(g, S0, S1, chat1, dtMg, invN, st->d_sums);
+        ACK(cudaGetLastError());
+        pa.mode = PM_INV;
+        pa.buf[0] = S0;
+        pa.buf[1] = S1;
+        if (g.Z > 1) {
+            PassArgs<R> za = pa;
+            za.plan = ctx->planZ;
+            za.tw = (const V *)ctx->d_twZ;
+            ACK(launch_spass<R>(za, ctx->LBz, ctx->stream));
+        }
+        ACK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+        XPassArgs<R> xj;
+        memset(&xj, 0, sizeof(xj));
+        xj.g = g;
+        xj.planH = ctx->planH;
+        xj.twX = (const V *)ctx->d_twX;
+        xj.allow_fast = ctx->use_fast;
+        xj.status = ctx->d_status;
+        xj.in_mode = XIN_SPECTRAL;
+        xj.program = XP_ADJ;
+        xj.in = S0;
+        xj.in2 = S1;
+        xj.rin = cn;
+        xj.rout = lam;
+        xj.out[0] = S0;
+        xj.ngrp_out = 1;
+        xj.adj_dtM = dtM;
+        ACK(launch_xpass<R>(xj, ctx->LBx, ctx->stream));
+    }
+    return GOPF_OK;
+}
+
+template <typename R> static int adj_capture(gopf_ctx *ctx, gopf_adjoint_state *st, int len, cudaGraphExec_t *exec)
+{
+    cudaGraph_t graph;
+    ACK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const long long step0 = ctx->step;
+    int rc = adj_segment<R>(ctx, st, len);
+    ctx->step = step0; // capturing runs nothing
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    if (rc) {
+        if (e == cudaSuccess) cudaGraphDestroy(graph);
+        return rc;
+    }
+    ACK(e);
+    e = cudaGraphInstantiate(exec, graph, 0);
+    cudaGraphDestroy(graph);
+    ACK(e);
+    return GOPF_OK;
+}
 
 template <typename R> static int adj_backward(gopf_ctx *ctx, gopf_adjoint_state *st, const double *lamT_host,
                                               double *dgamma, double *dM, double *dc0_host)
@@ -208,41 +258,50 @@ template <typename R> static int adj_backward(gopf_ctx *ctx, gopf_adjoint_state 
     typedef typename VecOf<R>::type V;
     const long long N = ctx->g.N;
     const size_t rb = sizeof(R) * N;
-    R *lam = (R *)st->d_r[0], *f = (R *)st->d_r[1], *mu = (R *)st->d_r[2], *nu = (R *)st->d_r[3];
-    V *Sl = (V *)st->d_s[0], *Sf = (V *)st->d_s[1], *Sc = (V *)st->d_s[2];
-    // lambda_T (host FP64) -> device R
+    R *lam = (R *)st->d_r[0];
+    V *S0 = (V *)st->d_s[0];
+    // lambda_T (host FP64) -> device R, and its r2c along x into S[0]
     std::vector<R> h(N);
     for (long long i = 0; i < N; ++i) h[i] = (R)lamT_host[i];
     ACK(cudaMemcpyAsync(lam, h.data(), rb, cudaMemcpyHostToDevice, ctx->stream));
     ACK(cudaMemsetAsync(st->d_sums, 0, 2 * sizeof(double), ctx->stream));
-    const double dtM = st->dt * st->M, dtMg = st->dt * st->M * st->gamma, invN = 1.0 / (double)N;
+    {
+        XPassArgs<R> xa;
+        memset(&xa, 0, sizeof(xa));
+        xa.g = ctx->g;
+        xa.planH = ctx->planH;
+        xa.twX = (const V *)ctx->d_twX;
+        xa.allow_fast = ctx->use_fast;
+        xa.status = ctx->d_status;
+        xa.in_mode = XIN_REAL;
+        xa.rin = lam;
+        xa.out[0] = S0;
+        xa.ngrp_out = 1;
+        xa.identity = 1;
+        ACK(launch_xpass<R>(xa, ctx->LBx, ctx->stream));
+    }
+    const double key[3] = {st->gamma, st->M, st->dt};
+    if (memcmp(key, st->g_key, sizeof(key)) != 0) { // the graphs bake in gamma, M and dt
+        adj_drop_graphs(st);
+        memcpy(st->g_key, key, sizeof(key));
+    }
+    const double invN = 1.0 / (double)N;
     const int nseg = (st->nsteps + st->every - 1) / st->every;
+    int rc;
     for (int seg = nseg - 1; seg >= 0; --seg) {
-        const int s0 = seg * st->every;
-        const int s1 = std::min(st->nsteps, s0 + st->every);
-        // recompute c_{s0} .. c_{s1}
-        int rc;
-        if ((rc = gopf_real_to_state(ctx, (char *)st->d_ckpt + (size_t)seg * rb))) return rc;
-        ACK(cudaMemcpyAsync(st->d_seg, (char *)st->d_ckpt + (size_t)seg * rb, rb, cudaMemcpyDeviceToDevice, ctx->stream));
-        for (int n = s0; n < s1; ++n) {
-            if ((rc = gopf_step_device(ctx, 1))) return rc;
-            if ((rc = gopf_state_to_real(ctx, (char *)st->d_seg + (size_t)(n + 1 - s0) * rb))) return rc;
+        const int len = std::min(st->nsteps, (seg + 1) * st->every) - seg * st->every;
+        ACK(cudaMemcpyAsync(st->d_stage, (char *)st->d_ckpt + (size_t)seg * rb, rb, cudaMemcpyDeviceToDevice,
+                            ctx->stream));
+        cudaGraphExec_t *ge = (len == st->every) ? &st->g_full : &st->g_tail;
+        int *glen = (len == st->every) ? &st->g_full_len : &st->g_tail_len;
+        if (!*ge || *glen != len) {
+            if (*ge) cudaGraphExecDestroy(*ge);
+            *ge = nullptr;
+            if ((rc = adj_capture<R>(ctx, st, len, ge))) return rc;
+            *glen = len;
         }
-        for (int n = s1 - 1; n >= s0; --n) {
-            const R *cn = (const R *)((char *)st->d_seg + (size_t)(n - s0) * rb);
-            const R *cn1 = (const R *)((char *)st->d_seg + (size_t)(n + 1 - s0) * rb);
-            k_fpoly<R><<<ew(N), 256, 0, ctx->stream>>>(cn, f, N);
-            ACK(cudaGetLastError());
-            ACK(r2c<R>(ctx, f, Sf));
-            ACK(r2c<R>(ctx, cn1, Sc));
-            ACK(r2c<R>(ctx, lam, Sl));
-            k_adj_kspace<R><<<ew(ctx->g.C), 256, 0, ctx->stream>>>(ctx->g, Sl, Sf, Sc, dtMg, invN, st->d_sums);
-            ACK(cudaGetLastError());
-            ACK(c2r<R>(ctx, Sl, mu));
-            ACK(c2r<R>(ctx, Sf, nu));
-            k_adj_real<R><<<ew(N), 256, 0, ctx->stream>>>(mu, nu, cn, lam, (R)dtM, N);
-            ACK(cudaGetLastError());
-        }
+        ACK(cudaGraphLaunch(*ge, ctx->stream));
+        ctx->step += len;
     }
     double sums[2];
     ACK(cudaMemcpyAsync(sums, st->d_sums, sizeof(sums), cudaMemcpyDeviceToHost, ctx->stream));
@@ -253,6 +312,14 @@ template <typename R> static int adj_backward(gopf_ctx *ctx, gopf_adjoint_state 
     if (dM) *dM = -st->dt * st->gamma * S1 - st->dt * S2;
     if (dc0_host)
         for (long long i = 0; i < N; ++i) dc0_host[i] = (double)h[i];
+    if (ctx->d_status) { // a bounded tile wait that ran out inside the sweep
+        unsigned stv = 0;
+        ACK(cudaMemcpy(&stv, ctx->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+        if (stv) {
+            ACK(cudaMemset(ctx->d_status, 0, sizeof(unsigned)));
+            return gopf_fail(ctx, GOPF_ERR_TIMEOUT, "a device copy did not complete in time");
+        }
+    }
     return GOPF_OK;
 }
 
@@ -291,12 +358,17 @@ extern "C" int gopf_adjoint_forward(gopf_ctx *ctx, double gamma, double M, doubl
     const size_t sb = (ctx->prec == GOPF_FP32 ? sizeof(float2) : sizeof(double2)) * ctx->g.C;
     const int nck = (nsteps + every - 1) / every + 1;
     if (st->nckpt < nck || st->every != every) {
+        adj_drop_graphs(st); // they point into the buffers replaced here
         if (st->d_ckpt) cudaFree(st->d_ckpt);
         if (st->d_seg) cudaFree(st->d_seg);
+        if (st->d_segs) cudaFree(st->d_segs);
+        st->d_ckpt = st->d_seg = st->d_segs = nullptr;
         ACK(gopf_malloc(&st->d_ckpt, rb * nck));
         ACK(gopf_malloc(&st->d_seg, rb * (every + 1)));
+        ACK(gopf_malloc(&st->d_segs, sb * (every + 1)));
         st->nckpt = nck;
     }
+    if (!st->d_stage) ACK(gopf_malloc(&st->d_stage, rb));
     for (int i = 0; i < 4; ++i)
         if (!st->d_r[i]) ACK(gopf_malloc(&st->d_r[i], rb));
     for (int i = 0; i < 3; ++i)
@@ -308,9 +380,10 @@ extern "C" int gopf_adjoint_forward(gopf_ctx *ctx, double gamma, double M, doubl
     st->M = M;
     st->dt = dt;
     if ((rc = gopf_field_upload_real(ctx, 0, c0, (size_t)N))) return rc;
-    for (int n = 0; n < nsteps; ++n) {
-        if (n % every == 0 && (rc = gopf_state_to_real(ctx, (char *)st->d_ckpt + (size_t)(n / every) * rb))) return rc;
-        if ((rc = gopf_step_device(ctx, 1))) return rc;
+    // one checkpoint per segment, the segment's steps replayed from the context's step graphs
+    for (int s0 = 0; s0 < nsteps; s0 += every) {
+        if ((rc = gopf_state_to_real(ctx, (char *)st->d_ckpt + (size_t)(s0 / every) * rb))) return rc;
+        if ((rc = gopf_step(ctx, std::min(every, nsteps - s0)))) return rc;
     }
     if (cT) return gopf_field_download_real(ctx, 0, cT, (size_t)N);
     ACK(cudaStreamSynchronize(ctx->stream));
@@ -350,8 +423,9 @@ extern "C" int gopf_adjoint_release(gopf_ctx *ctx)
     if (it == g_adj.end()) return GOPF_OK;
     gopf_adjoint_state *s = it->second;
     cudaSetDevice(ctx->device);
-    void *ptrs[] = {s->d_ckpt, s->d_seg, s->d_r[0], s->d_r[1], s->d_r[2], s->d_r[3], s->d_s[0], s->d_s[1], s->d_s[2],
-                    s->d_sums};
+    adj_drop_graphs(s);
+    void *ptrs[] = {s->d_ckpt, s->d_seg, s->d_segs, s->d_stage, s->d_r[0], s->d_r[1], s->d_r[2], s->d_r[3],
+                    s->d_s[0],  s->d_s[1], s->d_s[2], s->d_sums};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete s;

@@ -21,17 +21,21 @@ namespace gopf {
 template <int LB> struct Log2 { static constexpr int v = (LB == 1) ? 0 : 1 + Log2<LB / 2>::v; };
 template <> struct Log2<1> { static constexpr int v = 0; };
 
-// Asynchronous global -> shared copy of one spectral element (8 or 16 bytes), or zeros when
-// `valid` is false; the copies of a tile are issued back to back and completed together by
-// ga_wait() before the barrier that publishes the tile.
+// Asynchronous global -> shared copy of one element (a 4-byte or 8-byte real, or an 8-byte or
+// 16-byte complex value), or zeros when `valid` is false; the copy size is the element's own, so
+// both addresses need only the element's alignment.  The copies of a tile are issued back to back
+// and completed together by ga_wait() before the barrier that publishes the tile.
 template <typename V> __device__ __forceinline__ void ga_copy(V *dst, const V *src, bool valid)
 {
+    static_assert(sizeof(V) == 4 || sizeof(V) == 8 || sizeof(V) == 16, "cp.async copies 4, 8 or 16 bytes");
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
     const int n = valid ? (int)sizeof(V) : 0;
     if constexpr (sizeof(V) == 16)
         asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(n) : "memory");
-    else
+    else if constexpr (sizeof(V) == 8)
         asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(src), "r"(n) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(n) : "memory");
 }
 __device__ __forceinline__ void ga_wait()
 {
@@ -378,7 +382,7 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
         __syncthreads();
     }
 
-    if (a.rout) {
+    if (a.rout && a.program != XP_ADJ) {
         if (odd) {
             R *base = a.rout + ((long long)z * Y + y0) * g.X;
             for (int e = tid; e < npos; e += nt) {
@@ -418,6 +422,45 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
         }
         __shared__ double shred[32 * RED_SLOTS];
         block_reduce_store(vals, a.red, shred);
+    }
+
+    if (a.program == XP_ADJ) {
+        // A = mu (from in, above), B = nu = c2r(in2); c from the real rows of rin; lambda into rout
+        // and into B, then r2c(lambda) into out[0]
+        xload_c2r<R, LB, PERB, NCT>(B, a.in2, sbase, nl, g, a.planH, twX, stage);
+        const R dtM = (R)a.adj_dtM;
+        for (int e = tid; e < npos; e += nt) {
+            R cx, cy;
+            int r0, r1;
+            tile_rows<LB>(odd, e, r0, r1);
+            if (odd) {
+                const int x = e / (LB / 2);
+                const R *base = a.rin + ((long long)z * Y + y0) * g.X + x;
+                cx = (r0 < nl) ? base[(long long)r0 * g.X] : (R)0;
+                cy = (r1 < nl) ? base[(long long)r1 * g.X] : (R)0;
+            } else {
+                const int m = e >> LBSH;
+                const V c2 = (r0 < nl) ? reinterpret_cast<const V *>(a.rin)[((long long)z * Y + y0 + r0) * H + m] : zero;
+                cx = c2.x;
+                cy = c2.y;
+            }
+            const V mu = A[e], nu = B[e];
+            const V lam = cmk<V>(mu.x - dtM * ((R)3 * cx * cx - (R)1) * nu.x, mu.y - dtM * ((R)3 * cy * cy - (R)1) * nu.y);
+            B[e] = lam;
+            if (a.rout) {
+                if (odd) {
+                    const int x = e / (LB / 2);
+                    R *base = a.rout + ((long long)z * Y + y0) * g.X + x;
+                    if (r0 < nl) base[(long long)r0 * g.X] = lam.x;
+                    if (r1 < nl) base[(long long)r1 * g.X] = lam.y;
+                } else if (r0 < nl) {
+                    reinterpret_cast<V *>(a.rout)[((long long)z * Y + y0 + r0) * H + (e >> LBSH)] = lam;
+                }
+            }
+        }
+        __syncthreads();
+        xr2c_store<R, LB, PERB, NCT>(B, a.out[0], sbase, nl, g, a.planH, twX);
+        return;
     }
 
     if (a.program == XP_ELASTIC_Q) {

@@ -197,9 +197,12 @@ template <typename R> struct XPassArgs {
     MonoTable mono;
     int redfield; // XP_MULTI with red: the field whose real-space values are summed into red
     const R *rinF[GOPF_MAX_FIELDS]; // XP_MULTI with XIN_REAL: the real rows of field f
+    double adj_dtM; // XP_ADJ: dt M
 };
 
-enum XProgram { XP_POLY = 0, XP_ELASTIC_Q = 1, XP_MULTI = 2 };
+// XP_ADJ (the adjoint step): mu = c2r(in), nu = c2r(in2), c = rin; lambda = mu - adj_dtM (3c^2 - 1) nu
+// into rout and r2c(lambda) into out[0]
+enum XProgram { XP_POLY = 0, XP_ELASTIC_Q = 1, XP_MULTI = 2, XP_ADJ = 3 };
 
 // PM_ELASTIC_K: forward transform buf[0], multiply by bsym(k)/N, inverse transform in place
 enum PassMode { PM_FWD = 0, PM_INV = 1, PM_FUSED = 2, PM_INIT = 3, PM_ELASTIC_K = 4 };
