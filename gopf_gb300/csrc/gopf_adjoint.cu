@@ -151,6 +151,10 @@ template <typename R> static int adj_segment(gopf_ctx *ctx, gopf_adjoint_state *
     R *lam = (R *)st->d_r[0];
     V *S0 = (V *)st->d_s[0], *S1 = (V *)st->d_s[1];
     const double dtM = st->dt * st->M, dtMg = st->dt * st->M * st->gamma, invN = 1.0 / (double)g.N;
+    // narrow tiles on grids too small to fill the GPU with the context's tile widths (512^2: 32
+    // x-pass blocks at 16 rows per tile, 128 at 4)
+    const int lbx = ((long long)(g.Y / ctx->LBx) * g.Z < 2 * 152) ? 4 : ctx->LBx;
+    const int lby = ((long long)(g.KX / ctx->LBy) * g.Z < 2 * 152) ? 4 : ctx->LBy;
     int rc;
     if ((rc = gopf_real_to_state(ctx, st->d_stage))) return rc;
     ACK(cudaMemcpyAsync(st->d_seg, st->d_stage, rb, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -181,7 +185,7 @@ template <typename R> static int adj_segment(gopf_ctx *ctx, gopf_adjoint_state *
         xa.pw.pw[0][1] = 1;
         xa.pw.coef[0][1] = -1.0;
         pw_densify(xa.pw);
-        ACK(launch_xpass<R>(xa, ctx->LBx, ctx->stream));
+        ACK(launch_xpass<R>(xa, lbx, ctx->stream));
         PassArgs<R> pa;
         memset(&pa, 0, sizeof(pa));
         pa.g = g;
@@ -193,7 +197,7 @@ template <typename R> static int adj_segment(gopf_ctx *ctx, gopf_adjoint_state *
         pa.nbuf = 2;
         pa.allow_fast = ctx->use_fast;
         pa.status = ctx->d_status;
-        ACK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+        ACK(launch_cpass<R>(pa, lby, ctx->stream));
         if (g.Z > 1) {
             PassArgs<R> za = pa;
             za.plan = ctx->planZ;
@@ -211,7 +215,7 @@ template <typename R> static int adj_segment(gopf_ctx *ctx, gopf_adjoint_state *
             za.tw = (const V *)ctx->d_twZ;
             ACK(launch_spass<R>(za, ctx->LBz, ctx->stream));
         }
-        ACK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
+        ACK(launch_cpass<R>(pa, lby, ctx->stream));
         XPassArgs<R> xj;
         memset(&xj, 0, sizeof(xj));
         xj.g = g;
@@ -228,7 +232,7 @@ template <typename R> static int adj_segment(gopf_ctx *ctx, gopf_adjoint_state *
         xj.out[0] = S0;
         xj.ngrp_out = 1;
         xj.adj_dtM = dtM;
-        ACK(launch_xpass<R>(xj, ctx->LBx, ctx->stream));
+        ACK(launch_xpass<R>(xj, lbx, ctx->stream));
     }
     return GOPF_OK;
 }
