@@ -1183,10 +1183,11 @@ template <typename R> static PassArgs<R> pargs(gopf_ctx *ctx, bool zaxis)
     return a;
 }
 
+// External records: inside a stream capture they become event-record nodes that the host can time
 static void prof_mark(gopf_ctx *ctx)
 {
     if (ctx->prof_events && ctx->prof_next < ctx->prof_events->size())
-        cudaEventRecord((*ctx->prof_events)[ctx->prof_next++], ctx->stream);
+        cudaEventRecordWithFlags((*ctx->prof_events)[ctx->prof_next++], ctx->stream, cudaEventRecordExternal);
 }
 
 #define LK(call)                                                                                                       \
@@ -2586,27 +2587,39 @@ extern "C" int gopf_profile_step(gopf_ctx *ctx, int nsteps, double *avg_ms, doub
     step_slots(ctx, names, bytes);
     const size_t ns = names.size();
     *nslots = (int)ns;
-    std::vector<cudaEvent_t> ev(1 + ns * nsteps);
+    // One step with an event between its launches, captured as a graph (as the step runs when it
+    // is replayed from the context's graphs, without host launch gaps), replayed once untimed and
+    // then nsteps times, each replay's event intervals read back and summed.
+    std::vector<cudaEvent_t> ev(1 + ns);
     for (auto &e : ev) CK(cudaEventCreate(&e));
     std::vector<double> acc(ns, 0.0);
-    cudaError_t e = cudaSuccess;
-    CK(cudaEventRecord(ev[0], ctx->stream));
-    ctx->prof_events = &ev;
-    ctx->prof_next = 1;
-    for (int s = 0; s < nsteps && e == cudaSuccess; ++s)
-        e = (ctx->prec == GOPF_FP32) ? enqueue_euler<float>(ctx) : enqueue_euler<double>(ctx);
-    ctx->prof_events = nullptr;
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    if (e == cudaSuccess && ctx->prof_next != ev.size()) e = cudaErrorInvalidValue;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        for (int s = 0; s < nsteps; ++s)
+        e = cudaEventRecordWithFlags(ev[0], ctx->stream, cudaEventRecordExternal);
+        ctx->prof_events = &ev;
+        ctx->prof_next = 1;
+        if (e == cudaSuccess) e = (ctx->prec == GOPF_FP32) ? enqueue_euler<float>(ctx) : enqueue_euler<double>(ctx);
+        ctx->prof_events = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &graph);
+        if (e == cudaSuccess) e = e2;
+    }
+    if (e == cudaSuccess && ctx->prof_next != ev.size()) e = cudaErrorInvalidValue;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    for (int s = -1; s < nsteps && e == cudaSuccess; ++s) {
+        e = cudaGraphLaunch(exec, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e == cudaSuccess && s >= 0)
             for (size_t k = 0; k < ns; ++k) {
                 float ms = 0.f;
-                cudaEventElapsedTime(&ms, ev[s * ns + k], ev[s * ns + k + 1]);
+                cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
                 acc[k] += ms;
             }
-        ctx->step += nsteps;
     }
+    if (e == cudaSuccess) ctx->step += nsteps + 1;
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
     for (auto &x : ev) cudaEventDestroy(x);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "profile");
     for (size_t k = 0; k < ns && (int)k < capacity; ++k) {

@@ -393,9 +393,11 @@ int gopf_device_bytes(gopf_ctx *ctx, size_t *bytes);
  * graphs exist, i.e. after a gopf_step of at least 16 steps).  No counterpart in the reference. */
 int gopf_kernel_launches(gopf_ctx *ctx, long long nsteps, long long *count);
 int gopf_kernels_per_step(gopf_ctx *ctx, int *n);
-/* Run nsteps Euler steps launch by launch with CUDA events between kernels on the
- * context's stream; per kernel slot of one step write the average device time (ms)
- * and the algorithmic HBM bytes (each array read and written once).  Advances the state. */
+/* Per-kernel device time of the Euler step: one step with a CUDA event between its launches is
+ * captured as a graph (so the kernels run back to back as in the context's own step graphs) and
+ * replayed once untimed and then nsteps times; per kernel slot of one step write the average time
+ * (ms) and the algorithmic HBM bytes (each array read and written once).  Advances the state by
+ * nsteps + 1 steps.  No counterpart in the reference. */
 int gopf_profile_step(gopf_ctx *ctx, int nsteps, double *avg_ms, double *alg_bytes, int capacity, int *nslots);
 int gopf_profile_slot_name(gopf_ctx *ctx, int slot, char *buf, int buflen);
 
