@@ -106,6 +106,8 @@ struct gopf_adjoint_state {
     cudaGraphExec_t g_full = nullptr, g_tail = nullptr;
     int g_full_len = 0, g_tail_len = 0;
     double g_key[3] = {0.0, 0.0, 0.0}; // gamma, M, dt the graphs were captured with
+    double model_key[3] = {0.0, 0.0, 0.0}; // gamma, M, dt of the model installed on the context
+    bool model_set = false;
 };
 
 static void adj_drop_graphs(gopf_adjoint_state *st)
@@ -353,10 +355,18 @@ extern "C" int gopf_adjoint_forward(gopf_ctx *ctx, double gamma, double M, doubl
     t[1].implicit = 1;
     t[1].coef = -M * gamma;
     t[1].lap = 2;
-    int rc = gopf_set_terms(ctx, 1, &mu, 1, t, 2);
-    if (rc) return rc;
-    if ((rc = gopf_set_stepper(ctx, GOPF_STEPPER_EULER, dt))) return rc;
     gopf_adjoint_state *st = adj_state(ctx);
+    int rc;
+    // the model and stepper are installed again only when gamma, M or dt change: installing them
+    // drops the context's captured step graphs, which repeated evaluations (a fit) can reuse
+    const double mkey[3] = {gamma, M, dt};
+    if (!st->model_set || memcmp(mkey, st->model_key, sizeof(mkey)) != 0 || !ctx->initialised ||
+        ctx->stepper != GOPF_STEPPER_EULER || ctx->dt != dt) {
+        if ((rc = gopf_set_terms(ctx, 1, &mu, 1, t, 2))) return rc;
+        if ((rc = gopf_set_stepper(ctx, GOPF_STEPPER_EULER, dt))) return rc;
+        memcpy(st->model_key, mkey, sizeof(mkey));
+        st->model_set = true;
+    }
     const long long N = ctx->g.N;
     const size_t rb = (ctx->prec == GOPF_FP32 ? sizeof(float) : sizeof(double)) * N;
     const size_t sb = (ctx->prec == GOPF_FP32 ? sizeof(float2) : sizeof(double2)) * ctx->g.C;
