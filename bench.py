@@ -214,6 +214,8 @@ def run_gpu(args):
     m = ch3d_model(G, "fp32", c0, local, stream)
     if args.tma is not None:
         m.set_option(G._lib.OPT_TMA, args.tma)
+    if args.x_rows is not None:
+        m.set_option(G._lib.OPT_X_ROWS, args.x_rows)
     mass0 = m.mass(0)
     m.prepare_graphs(args.steps)  # capture the graphs the timed steps replay (no stepping)
     m.step(warmup_steps(args))
@@ -849,6 +851,8 @@ def main():
                     help="steps of the FP32-vs-FP64 device comparison in the default line")
     ap.add_argument("--grid", type=int, default=256, help="cube side (256 is the benchmark workload)")
     ap.add_argument("--workload", default="ch3d", choices=["ch3d", "sweep", "adjoint", "elastic", "precision", "c1"])
+    ap.add_argument("--x-rows", type=int, default=None, choices=[16, 32],
+                    help="rows per tile of the 256-column x pass (the library's default when omitted)")
     ap.add_argument("--tma", type=int, default=None, choices=[0, 1],
                     help="tile movement of the 256-point kernels: 0 plain loads, 1 TMA")
     ap.add_argument("--no-tune", action="store_true", help="sweep: keep the built-in kernel choices")

@@ -854,5 +854,104 @@ static __global__ void __launch_bounds__(NT, 4) k_x256_tl(const XPassArgs<float>
     x_fwd_store(v, a.out[0], r, j, s_tw, at, s_x, (long long)z * a.g.S + y0, a.g.KX, a.g.Y);
 }
 
+// ---------------------------------------------------------------------------
+// One output group on half-height tiles: 16 rows (8 packed row pairs) per block, 128 threads,
+// about 19.5 KB of shared memory, so eight blocks share an SM (four with k_x256_tl) and more tile
+// loads overlap other blocks' transforms.  A thread t = 8 r + j owns radix position r of row
+// pair j.  The exchange slots of the 8 lines are padded to 132 per radix row so that both
+// directions of the exchange are conflict free.  The tile arrives by one 3D TMA copy
+// ({16 y, 129 kx, 1 z}); the separated spectra leave as 16-byte stores of a row pair.
+// ---------------------------------------------------------------------------
+constexpr int XH_ROWS = 16, XH_NT = 128, XH_LINES = 8, XH_PITCH = 16 * XH_LINES + 4;
+constexpr int XH_TILE_BYTES = 129 * XH_ROWS * 8;       // 16,512
+constexpr int XH_XCH_FLOATS2 = 16 * XH_PITCH;          // 2,112 float2 = 16,896 B >= the tile
+
+__host__ __device__ constexpr int x256_th_smem_bytes()
+{
+    return 128 + XH_XCH_FLOATS2 * 8 + N * 8 + GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1) * 4 + 16;
+}
+
+static __global__ void __launch_bounds__(XH_NT, 8) k_x256_th(const XPassArgs<float> a, const __grid_constant__ CUtensorMap mIn)
+{
+    extern __shared__ unsigned char xh_dsm[];
+    unsigned char *base = xh_dsm + ((128u - (smem_u32(xh_dsm) & 127u)) & 127u);
+    float2 *s_x = reinterpret_cast<float2 *>(base); // input tile, then exchange slots
+    float2 *s_tw = reinterpret_cast<float2 *>(base + XH_XCH_FLOATS2 * 8);
+    float *s_poly = reinterpret_cast<float *>(s_tw + N);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(s_poly + GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1));
+    int *s_ok = reinterpret_cast<int *>(bar + 1);
+
+    const int tid = threadIdx.x;
+    const int j = tid & 7, r = tid >> 3;
+    const int y0 = blockIdx.x * XH_ROWS;
+    const int z = blockIdx.y;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        mbar_arrive_expect_tx(bar, (uint32_t)XH_TILE_BYTES);
+        tma_load_3d(s_x, &mIn, y0, 0, z, bar);
+    }
+    for (int t = tid; t < GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1); t += XH_NT)
+        s_poly[t] = (float)a.pw.dense[t / (GOPF_MAX_DEG + 1)][t % (GOPF_MAX_DEG + 1)];
+    for (int t = tid; t < N; t += XH_NT) s_tw[t] = a.twX[(t & 15) * (t >> 4)];
+    if (tid == 0) *s_ok = tma_wait_or_flag(bar, 0, a.status) ? 1 : 0;
+    __syncthreads();
+    if (!*s_ok) return;
+
+    // Hermitian extension of rows (2j, 2j+1) packed as a + i b: the tile is [129 kx][16 y]
+    float2 v[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int k = r + 16 * i;
+        if (i < 8) {
+            const float4 ab = *reinterpret_cast<const float4 *>(&s_x[k * XH_ROWS + 2 * j]);
+            v[i] = make_float2(ab.x - ab.w, ab.y + ab.z);
+        } else if (i > 8) {
+            const float4 ab = *reinterpret_cast<const float4 *>(&s_x[(N - k) * XH_ROWS + 2 * j]);
+            v[i] = make_float2(ab.x + ab.w, -ab.y + ab.z);
+        } else {
+            const bool lo = (r == 0);
+            const float4 ab = *reinterpret_cast<const float4 *>(&s_x[(lo ? 128 : N - k) * XH_ROWS + 2 * j]);
+            v[i] = lo ? make_float2(ab.x - ab.w, ab.y + ab.z) : make_float2(ab.x + ab.w, -ab.y + ab.z);
+        }
+    }
+    __syncthreads(); // the tile becomes the exchange slots
+    auto at = [&](int x, int y) -> float2 & { return s_x[x * XH_PITCH + y * XH_LINES + j]; };
+    fft256<true>(v, r, s_tw, at);
+    switch (a.identity ? -1 : a.pw.deg[0]) { // the launch guarantees a dense degree <= 6
+    case 0: poly_regs<0>(v, s_poly); break;
+    case 1: poly_regs<1>(v, s_poly); break;
+    case 2: poly_regs<2>(v, s_poly); break;
+    case 3: poly_regs<3>(v, s_poly); break;
+    case 4: poly_regs<4>(v, s_poly); break;
+    case 5: poly_regs<5>(v, s_poly); break;
+    case 6: poly_regs<6>(v, s_poly); break;
+    default: break;
+    }
+    fft256<false>(v, r, s_tw, at);
+    // spectrum Z(k) of line j at slot [k][j] (pitch 8 per k), then the row pairs' half spectra
+#pragma unroll
+    for (int i = 0; i < 16; ++i) s_x[(r + 16 * i) * XH_LINES + j] = v[i];
+    __syncthreads();
+    const int p = tid & 7, k0 = tid >> 3; // 16 kx per pass
+    float2 *o = a.out[0] + (long long)z * a.g.S + y0 + (long long)k0 * a.g.Y + 2 * p;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int kx = k0 + 16 * q;
+        const float2 P = s_x[kx * XH_LINES + p];
+        const float2 Q = s_x[((N - kx) & (N - 1)) * XH_LINES + p];
+        *reinterpret_cast<float4 *>(o + (long long)(16 * q) * a.g.Y) =
+            make_float4(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y), 0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
+    }
+    if (k0 == 0) { // kx = 128
+        const float2 P = s_x[128 * XH_LINES + p];
+        *reinterpret_cast<float4 *>(a.out[0] + (long long)z * a.g.S + y0 + 128LL * a.g.Y + 2 * p) =
+            make_float4(P.x, 0.f, P.y, 0.f);
+    }
+}
+
 } // namespace f256
 } // namespace gopf

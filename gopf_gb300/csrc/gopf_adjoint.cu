@@ -16,7 +16,7 @@
 // checkpoint and walks it backwards.  A segment's recompute and backward
 // walk are one captured CUDA graph (replayed for every segment of that
 // length); a backward step is five launches in 2D: the x pass forming
-// r2c_x(c^3 - c), one y pass forward-transforming that and lambda, the k-space
+// r2c_x(c^3 - c) from the step's x-spectral field, one y pass forward-transforming that and lambda, the k-space
 // product and gradient sums, one inverse y pass, and an x pass that forms
 // lambda_n = mu - dt M (3c^2 - 1) nu and its r2c_x for the next step.
 #include <algorithm>
@@ -31,31 +31,35 @@
 namespace gopf {
 
 // k space: mu = D lam / N, nu = k^2 D lam / N (in place of lam-hat and f-hat),
-// plus the two gradient sums (FP64, atomically accumulated per block).
+// plus the two gradient sums (FP64, atomically accumulated per block).  The per-mode
+// arithmetic runs in the state's precision (FP64 is a small fraction of the FP32 rate on this
+// GPU); only the accumulation is FP64.  Indices are 32-bit (C < 2^31).
 template <typename R>
 __global__ void k_adj_kspace(Geom g, typename VecOf<R>::type *__restrict__ lamh, typename VecOf<R>::type *__restrict__ fh,
                              const typename VecOf<R>::type *__restrict__ ch, double dtMg, double invN, double *__restrict__ sums)
 {
     typedef typename VecOf<R>::type V;
     double s1 = 0.0, s2 = 0.0;
-    const double fourpi2 = 39.478417604357434475337963999504;
-    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < g.C;
-         idx += (long long)gridDim.x * blockDim.x) {
-        const long long z = idx / g.S;
-        const long long rem = idx - z * g.S;
-        const long long kx = rem / g.Y;
-        const long long y = rem - kx * g.Y;
-        const long long jy = (2 * y > g.Y) ? g.Y - y : y;
-        const long long jz = (2 * z > g.Z) ? g.Z - z : z;
-        const double fx = (double)kx / g.X, fy = (double)jy / g.Y, fz = (double)jz / g.Z;
-        const double k2 = fourpi2 * (fx * fx + fy * fy + fz * fz);
-        const double D = 1.0 / (1.0 + dtMg * k2 * k2);
-        const double w = (kx == 0 || 2 * kx == g.X) ? 1.0 : 2.0;
+    const R fourpi2 = (R)39.478417604357434475337963999504;
+    const R a_dt = (R)dtMg, a_inv = (R)invN;
+    const unsigned C = (unsigned)g.C, S = (unsigned)g.S, Y = (unsigned)g.Y;
+    const R rX = (R)1 / (R)g.X, rY = (R)1 / (R)g.Y, rZ = (R)1 / (R)g.Z;
+    for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < C; idx += gridDim.x * blockDim.x) {
+        const unsigned z = idx / S;
+        const unsigned rem = idx - z * S;
+        const unsigned kx = rem / Y;
+        const unsigned y = rem - kx * Y;
+        const unsigned jy = (2 * y > Y) ? Y - y : y;
+        const unsigned jz = (2 * z > (unsigned)g.Z) ? (unsigned)g.Z - z : z;
+        const R fx = (R)kx * rX, fy = (R)jy * rY, fz = (R)jz * rZ;
+        const R k2 = fourpi2 * (fx * fx + fy * fy + fz * fz);
+        const R D = (R)1 / ((R)1 + a_dt * k2 * k2);
+        const R w = (kx == 0 || 2 * kx == (unsigned)g.X) ? (R)1 : (R)2;
         const V l = lamh[idx], c = ch[idx], f = fh[idx];
         // Re(conj(l) * c) and Re(conj(l) * f)
-        s1 += w * k2 * k2 * D * ((double)l.x * (double)c.x + (double)l.y * (double)c.y);
-        s2 += w * k2 * D * ((double)l.x * (double)f.x + (double)l.y * (double)f.y);
-        const R a = (R)(D * invN), b = (R)(D * k2 * invN);
+        s1 += (double)(w * k2 * k2 * D * (l.x * c.x + l.y * c.y));
+        s2 += (double)(w * k2 * D * (l.x * f.x + l.y * f.y));
+        const R a = D * a_inv, b = D * k2 * a_inv;
         V mu, nu;
         mu.x = l.x * a;
         mu.y = l.y * a;
@@ -97,6 +101,7 @@ struct gopf_adjoint_state {
     void *d_ckpt = nullptr;  // (nsteps/every + 1) real fields
     void *d_seg = nullptr;   // every + 1 real fields
     void *d_segs = nullptr;  // every + 1 spectra (c-hat of the recomputed steps)
+    void *d_segT = nullptr;  // every + 1 x-spectral fields (T of the recomputed steps)
     void *d_stage = nullptr; // the checkpoint a segment graph starts from
     void *d_r[4] = {nullptr, nullptr, nullptr, nullptr}; // real work: lambda (the others unused)
     void *d_s[3] = {nullptr, nullptr, nullptr};           // spectral work
@@ -140,7 +145,7 @@ int gopf_step_device(gopf_ctx *ctx, long long n);
 // One segment's sweep, stream-ordered (captured into a graph by the caller): recompute c_{s0+1} ..
 // c_{s0+len} from the checkpoint in d_stage, keeping each step's real field and c-hat, then walk
 // the steps backwards.  Per backward step n, with Lx = the x-transformed lambda_{n+1} in S[0]:
-//   x pass   : f(c_n) = c_n^3 - c_n from the real rows, r2c along x          -> S[1]
+//   x pass   : f(c_n) = c_n^3 - c_n from T_n (c2r, polynomial, r2c along x)  -> S[1]
 //   y (z)    : forward of S[1] and S[0] in one launch                        -> F, Lambda
 //   k space  : the two gradient sums; mu-hat = D Lambda / N -> S[0], nu-hat = k^2 D Lambda / N -> S[1]
 //   (z) y    : inverse of S[0] and S[1] in one launch
@@ -160,15 +165,20 @@ template <typename R> static int adj_segment(gopf_ctx *ctx, gopf_adjoint_state *
     int rc;
     if ((rc = gopf_real_to_state(ctx, st->d_stage))) return rc;
     ACK(cudaMemcpyAsync(st->d_seg, st->d_stage, rb, cudaMemcpyDeviceToDevice, ctx->stream));
+    ACK(cudaMemcpyAsync(st->d_segT, ctx->d_T, sb, cudaMemcpyDeviceToDevice, ctx->stream));
     for (int n = 0; n < len; ++n) {
         if ((rc = gopf_step_device(ctx, 1))) return rc;
         if ((rc = gopf_state_to_real(ctx, (char *)st->d_seg + (size_t)(n + 1) * rb))) return rc;
         ACK(cudaMemcpyAsync((char *)st->d_segs + (size_t)(n + 1) * sb, ctx->d_state, sb, cudaMemcpyDeviceToDevice,
                             ctx->stream));
+        ACK(cudaMemcpyAsync((char *)st->d_segT + (size_t)(n + 1) * sb, ctx->d_T, sb, cudaMemcpyDeviceToDevice,
+                            ctx->stream));
     }
     for (int n = len - 1; n >= 0; --n) {
         const R *cn = (const R *)((char *)st->d_seg + (size_t)n * rb);
         const V *chat1 = (const V *)((char *)st->d_segs + (size_t)(n + 1) * sb);
+        // f(c_n) from the step's own x-spectral field T_n: the c2r, the polynomial and the r2c of
+        // one x pass (the register line engine where it serves the length)
         XPassArgs<R> xa;
         memset(&xa, 0, sizeof(xa));
         xa.g = g;
@@ -176,8 +186,8 @@ template <typename R> static int adj_segment(gopf_ctx *ctx, gopf_adjoint_state *
         xa.twX = (const V *)ctx->d_twX;
         xa.allow_fast = ctx->use_fast;
         xa.status = ctx->d_status;
-        xa.in_mode = XIN_REAL;
-        xa.rin = cn;
+        xa.in_mode = XIN_SPECTRAL;
+        xa.in = (const V *)((char *)st->d_segT + (size_t)n * sb);
         xa.out[0] = S1;
         xa.ngrp_out = 1;
         xa.pw.ngrp = 1;
@@ -376,10 +386,12 @@ extern "C" int gopf_adjoint_forward(gopf_ctx *ctx, double gamma, double M, doubl
         if (st->d_ckpt) cudaFree(st->d_ckpt);
         if (st->d_seg) cudaFree(st->d_seg);
         if (st->d_segs) cudaFree(st->d_segs);
-        st->d_ckpt = st->d_seg = st->d_segs = nullptr;
+        if (st->d_segT) cudaFree(st->d_segT);
+        st->d_ckpt = st->d_seg = st->d_segs = st->d_segT = nullptr;
         ACK(gopf_malloc(&st->d_ckpt, rb * nck));
         ACK(gopf_malloc(&st->d_seg, rb * (every + 1)));
         ACK(gopf_malloc(&st->d_segs, sb * (every + 1)));
+        ACK(gopf_malloc(&st->d_segT, sb * (every + 1)));
         st->nckpt = nck;
     }
     if (!st->d_stage) ACK(gopf_malloc(&st->d_stage, rb));
@@ -438,8 +450,8 @@ extern "C" int gopf_adjoint_release(gopf_ctx *ctx)
     gopf_adjoint_state *s = it->second;
     cudaSetDevice(ctx->device);
     adj_drop_graphs(s);
-    void *ptrs[] = {s->d_ckpt, s->d_seg, s->d_segs, s->d_stage, s->d_r[0], s->d_r[1], s->d_r[2], s->d_r[3],
-                    s->d_s[0],  s->d_s[1], s->d_s[2], s->d_sums};
+    void *ptrs[] = {s->d_ckpt, s->d_seg,  s->d_segs, s->d_segT, s->d_stage, s->d_r[0], s->d_r[1],
+                    s->d_r[2], s->d_r[3], s->d_s[0], s->d_s[1],  s->d_s[2],  s->d_sums};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete s;

@@ -421,6 +421,10 @@ extern "C" int gopf_set_option(gopf_ctx *ctx, int opt, long long v)
     else if (opt == GOPF_OPT_FAST_KERNELS) ctx->use_fast = (int)(v != 0);
     else if (opt == GOPF_OPT_DIRECT_HOST) ctx->use_direct_host = (int)(v != 0);
     else if (opt == GOPF_OPT_TMA) ctx->use_tma = (int)(v != 0);
+    else if (opt == GOPF_OPT_X_ROWS) {
+        if (v != 16 && v != 32) return gopf_fail(ctx, GOPF_ERR_ARG, "the x tile height is 16 or 32 rows");
+        ctx->x_rows = (int)v;
+    }
     else if (opt == GOPF_OPT_WAIT_LIMIT_NS) {
         if (v < 0) return gopf_fail(ctx, GOPF_ERR_ARG, "negative wait limit");
         if (!ctx->d_status) return gopf_fail(ctx, GOPF_ERR_STATE, "context has no device");
@@ -1165,7 +1169,7 @@ template <typename R> static XPassArgs<R> xargs(gopf_ctx *ctx)
     a.g = ctx->g;
     a.planH = ctx->planH;
     a.twX = (const V *)ctx->d_twX;
-    a.allow_fast = ctx->use_fast ? (ctx->use_tma ? 3 : 1) : 0;
+    a.allow_fast = ctx->use_fast ? ((ctx->use_tma ? 3 : 1) | (ctx->x_rows == 16 ? 8 : 0)) : 0;
     a.status = ctx->d_status;
     return a;
 }
@@ -1178,7 +1182,7 @@ template <typename R> static PassArgs<R> pargs(gopf_ctx *ctx, bool zaxis)
     a.g = ctx->g;
     a.plan = zaxis ? ctx->planZ : ctx->planY;
     a.tw = (const V *)(zaxis ? ctx->d_twZ : ctx->d_twY);
-    a.allow_fast = ctx->use_fast ? (ctx->use_tma ? 3 : 1) : 0;
+    a.allow_fast = ctx->use_fast ? ((ctx->use_tma ? 3 : 1) | (ctx->x_rows == 16 ? 8 : 0)) : 0;
     a.status = ctx->d_status;
     return a;
 }

@@ -20,13 +20,13 @@ static bool z_map(CUtensorMap *m, const float2 *p, const Geom &g)
     return encode_map_8b(m, p, 2, dims, strides, box);
 }
 
-// [Z][KX][Y] view of an x-pass array with {32, KX, 1} boxes
-static bool x_map(CUtensorMap *m, const float2 *p, const Geom &g)
+// [Z][KX][Y] view of an x-pass array with {rows, KX, 1} boxes
+static bool x_map(CUtensorMap *m, const float2 *p, const Geom &g, int rows = f256::XROWS)
 {
     const unsigned long long dims[3] = {(unsigned long long)g.Y, (unsigned long long)g.KX, (unsigned long long)g.Z};
     const unsigned long long strides[2] = {(unsigned long long)g.Y * sizeof(float2),
                                            (unsigned long long)g.S * sizeof(float2)};
-    const unsigned box[3] = {(unsigned)f256::XROWS, (unsigned)g.KX, 1};
+    const unsigned box[3] = {(unsigned)rows, (unsigned)g.KX, 1};
     return encode_map_8b(m, p, 3, dims, strides, box);
 }
 
@@ -43,8 +43,22 @@ static bool launch_x_tma(const XPassArgs<float> &a, cudaStream_t st, cudaError_t
     });
     if (attr_err != cudaSuccess || a.g.KX != 129 || a.ngrp_out > GOPF_MAX_GROUPS) return false;
     CUtensorMap mi, mo[GOPF_MAX_GROUPS];
+    const bool one = (a.ngrp_out == 1 && (a.identity || (a.pw.deg[0] >= 0 && a.pw.deg[0] <= 6)));
+    if (one && (a.allow_fast & 8) && a.g.Y % f256::XH_ROWS == 0) {
+        // one dense polynomial group on half-height tiles: eight blocks per SM
+        static std::once_flag once_h;
+        static cudaError_t attr_h = cudaSuccess;
+        std::call_once(once_h, [] {
+            attr_h = cudaFuncSetAttribute(f256::k_x256_th, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          f256::x256_th_smem_bytes());
+        });
+        if (attr_h != cudaSuccess || !x_map(&mi, a.in, a.g, f256::XH_ROWS)) return false;
+        f256::k_x256_th<<<dim3(a.g.Y / f256::XH_ROWS, a.g.Z), f256::XH_NT, f256::x256_th_smem_bytes(), st>>>(a, mi);
+        *err = cudaGetLastError();
+        return true;
+    }
     if (!x_map(&mi, a.in, a.g)) return false;
-    if (a.ngrp_out == 1 && (a.identity || (a.pw.deg[0] >= 0 && a.pw.deg[0] <= 6))) {
+    if (one) {
         // one dense polynomial group: four blocks per SM, direct stores
         f256::k_x256_tl<<<dim3(a.g.Y / f256::XROWS, a.g.Z), f256::NT, f256::x256_tl_smem_bytes(), st>>>(a, mi);
         *err = cudaGetLastError();

@@ -100,11 +100,14 @@ enum {
                                   0: plain loads (value 4 is unused) */
     GOPF_OPT_DIRECT_HOST = 5,  /* 1 (default): pinned host buffers given to upload/download are read and
                                   written by kernels in place; pageable buffers are staged */
-    GOPF_OPT_WAIT_LIMIT_NS = 6 /* limit (ns) of a kernel's first wait for a tile copy; 0 (default) = 2 s.
+    GOPF_OPT_WAIT_LIMIT_NS = 6, /* limit (ns) of a kernel's first wait for a tile copy; 0 (default) = 2 s.
                                   A wait that runs out flags the step (GOPF_ERR_TIMEOUT from gopf_step or
                                   gopf_synchronize), waits up to 2 s more for the copy still in flight and
                                   leaves the tile alone, so the field must be uploaded again.  Meant for
                                   testing that error path; the reference has no counterpart. */
+    GOPF_OPT_X_ROWS = 7         /* rows per tile of the 256-column x pass with one dense polynomial group:
+                                  32 (default: 256 threads, four blocks per SM) or 16 (128 threads,
+                                  eight blocks per SM); both compute the same values */
 };
 
 #define GOPF_MAX_FACTORS 8

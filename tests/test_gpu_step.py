@@ -334,6 +334,24 @@ def test_tma_tiles_match_plain_loads(two_groups):
     assert np.array_equal(models[0], models[1])
 
 
+def test_half_height_x_tiles_match():
+    """The one-group 256-column x pass on 16-row tiles (128 threads, eight blocks per SM) computes
+    exactly what the 32-row tiles do: bitwise equal after 10 steps, 256^3 and 256^2 FP32."""
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+
+    for dims in ([256, 256, 256], [256, 256]):
+        c0 = uniform_field(8, int(np.prod(dims)), 0.0, 0.1)
+        out = []
+        for rows in (16, 32):
+            m = ch_gpu(dims, "fp32", 0.5, 0.05, c0)
+            m.set_option(G._lib.OPT_X_ROWS, rows)
+            m.step(10)
+            out.append(m.download(0).real)
+            m.close()
+        assert np.array_equal(out[0], out[1])
+
+
 def test_real_space_x_kernels_match_generic():
     """Upload (real -> spectrum), download (spectrum -> real) and the FP64 reductions through the
     256-column real-space kernels agree with the generic x pass to FP32 round-off."""
