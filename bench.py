@@ -216,6 +216,8 @@ def run_gpu(args):
         m.set_option(G._lib.OPT_TMA, args.tma)
     if args.x_rows is not None:
         m.set_option(G._lib.OPT_X_ROWS, args.x_rows)
+    if args.z_lines is not None:
+        m.set_option(G._lib.OPT_Z_LINES, args.z_lines)
     mass0 = m.mass(0)
     m.prepare_graphs(args.steps)  # capture the graphs the timed steps replay (no stepping)
     m.step(warmup_steps(args))
@@ -853,6 +855,8 @@ def main():
     ap.add_argument("--workload", default="ch3d", choices=["ch3d", "sweep", "adjoint", "elastic", "precision", "c1"])
     ap.add_argument("--x-rows", type=int, default=None, choices=[16, 32],
                     help="rows per tile of the 256-column x pass (the library's default when omitted)")
+    ap.add_argument("--z-lines", type=int, default=None, choices=[8, 16],
+                    help="lines per tile of the 256-point z pass (the library's default when omitted)")
     ap.add_argument("--tma", type=int, default=None, choices=[0, 1],
                     help="tile movement of the 256-point kernels: 0 plain loads, 1 TMA")
     ap.add_argument("--no-tune", action="store_true", help="sweep: keep the built-in kernel choices")

@@ -855,6 +855,120 @@ static __global__ void __launch_bounds__(NT, 4) k_x256_tl(const XPassArgs<float>
 }
 
 // ---------------------------------------------------------------------------
+// z axis on half-width tiles: 8 lines per block, 128 threads, the group and c-hat tiles
+// 16 KB each, so six blocks share an SM (three with k_z256_tma) and more tile loads overlap
+// other blocks' transforms.  One explicit group.  A thread t = 8 r + l owns radix position r of
+// line l; the exchange slots of the 8 lines are padded to 132 per radix row (both exchange
+// directions conflict free).  TMA boxes {8 lines, 256 z}.
+// ---------------------------------------------------------------------------
+constexpr int ZH_LINES = 8, ZH_NT = 128, ZH_PITCH = 16 * ZH_LINES + 4;
+constexpr int ZH_TILE_BYTES = ZH_LINES * N * 8;         // 16,384
+constexpr int ZH_XCH_BYTES = 16 * ZH_PITCH * 8;         // 16,896: the group tile, then the exchange
+
+__host__ __device__ constexpr int z256_th_smem_bytes()
+{
+    return 128 + ZH_XCH_BYTES + ZH_TILE_BYTES + N * 8 + N * 4 + ZH_LINES * 4 + 16;
+}
+
+template <bool NZ>
+__global__ void __launch_bounds__(ZH_NT, 6)
+    k_z256_th(const PassArgs<float> a, const __grid_constant__ CUtensorMap mU0, const __grid_constant__ CUtensorMap mS,
+              const __grid_constant__ CUtensorMap mT)
+{
+    extern __shared__ unsigned char zh_dsm[];
+    unsigned char *base = zh_dsm + ((128u - (smem_u32(zh_dsm) & 127u)) & 127u);
+    float2 *tU0 = reinterpret_cast<float2 *>(base);
+    float2 *tS = reinterpret_cast<float2 *>(base + ZH_XCH_BYTES);
+    float2 *s_tw = reinterpret_cast<float2 *>(base + ZH_XCH_BYTES + ZH_TILE_BYTES);
+    float *s_fz = reinterpret_cast<float *>(s_tw + N);
+    float *s_fl = s_fz + N;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(s_fl + ZH_LINES);
+    int *s_ok = reinterpret_cast<int *>(bar + 1);
+
+    const Geom &g = a.g;
+    const int tid = threadIdx.x;
+    const int l = tid & 7, r = tid >> 3;
+    const int i0 = blockIdx.x * ZH_LINES;
+    const bool init = (a.mode == PM_INIT);
+    const int ngrp = (a.upd.ngrp > 0 ? 1 : 0);
+
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        const uint32_t bytes = (uint32_t)ZH_TILE_BYTES * (1u + (init ? 0u : 1u));
+        mbar_arrive_expect_tx(bar, bytes);
+        tma_load_2d(tU0, &mU0, i0, 0, bar);
+        if (!init) tma_load_2d(tS, &mS, i0, 0, bar);
+    }
+    for (int t = tid; t < N; t += ZH_NT) {
+        s_tw[t] = a.tw[(t & 15) * (t >> 4)];
+        s_fz[t] = fsqf(t, g.Z);
+    }
+    if (tid < ZH_LINES) {
+        const int q = i0 + tid;
+        const int kx = q / g.Y, y = q - kx * g.Y;
+        const float fx = (float)kx / (float)g.X;
+        s_fl[tid] = fx * fx + fsqf(y, g.Y);
+    }
+    if (tid == 0) *s_ok = tma_wait_or_flag(bar, 0, a.status) ? 1 : 0;
+    __syncthreads();
+    if (!*s_ok) return;
+
+    float2 v[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = tU0[(r + 16 * i) * ZH_LINES + l];
+    __syncthreads(); // the group tile becomes the exchange slots
+    auto at = [&](int x, int y) -> float2 & { return tU0[x * ZH_PITCH + y * ZH_LINES + l]; };
+    fft256<false>(v, r, s_tw, at);
+
+    const UpdTable &u = a.upd;
+    const UpdRegs R = load_upd(u, ngrp);
+    const float fourpi2 = 39.478417604357434f;
+    const float fl = s_fl[l];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int k = r + 16 * i;
+        float2 cn;
+        if (init) {
+            cn = v[i];
+        } else {
+            const float mk = -fourpi2 * (fl + s_fz[k]);
+            float2 c0 = tS[k * ZH_LINES + l];
+            if (NZ && u.noise.kind) {
+                const long long q = i0 + l, kx = q / g.Y, yy = q - kx * g.Y;
+                double nr, ni;
+                noise_term(u.noise, g.X, g.Y, g.Z, kx, yy, k, (double)mk, nr, ni);
+                c0.x += R.dt * (float)nr;
+                c0.y += R.dt * (float)ni;
+            }
+            cn = euler_update<1>(R, c0, v[i], v[i], mk);
+            if (NZ && u.filt) cn = modal_filter(u, cn, fl + s_fz[k]);
+        }
+        tS[k * ZH_LINES + l] = cn; // each thread rewrites exactly the elements it read
+        v[i] = make_float2(cn.x * R.invN, cn.y * R.invN);
+    }
+    fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+        tma_store_2d(&mS, i0, 0, tS);
+        bulk_commit();
+    }
+    fft256<true>(v, r, s_tw, at);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) tU0[(r + 16 * i) * ZH_LINES + l] = v[i];
+    fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+        tma_store_2d(&mT, i0, 0, tU0);
+        bulk_commit();
+        bulk_wait_read_all(); // the tiles stay allocated until both stores have read them
+    }
+}
+
+// ---------------------------------------------------------------------------
 // One output group on half-height tiles: 16 rows (8 packed row pairs) per block, 128 threads,
 // about 19.5 KB of shared memory, so eight blocks share an SM (four with k_x256_tl) and more tile
 // loads overlap other blocks' transforms.  A thread t = 8 r + j owns radix position r of row

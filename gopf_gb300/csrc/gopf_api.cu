@@ -421,7 +421,10 @@ extern "C" int gopf_set_option(gopf_ctx *ctx, int opt, long long v)
     else if (opt == GOPF_OPT_FAST_KERNELS) ctx->use_fast = (int)(v != 0);
     else if (opt == GOPF_OPT_DIRECT_HOST) ctx->use_direct_host = (int)(v != 0);
     else if (opt == GOPF_OPT_TMA) ctx->use_tma = (int)(v != 0);
-    else if (opt == GOPF_OPT_X_ROWS) {
+    else if (opt == GOPF_OPT_Z_LINES) {
+        if (v != 8 && v != 16) return gopf_fail(ctx, GOPF_ERR_ARG, "the z tile width is 8 or 16 lines");
+        ctx->z_lines = (int)v;
+    } else if (opt == GOPF_OPT_X_ROWS) {
         if (v != 16 && v != 32) return gopf_fail(ctx, GOPF_ERR_ARG, "the x tile height is 16 or 32 rows");
         ctx->x_rows = (int)v;
     }
@@ -1169,7 +1172,8 @@ template <typename R> static XPassArgs<R> xargs(gopf_ctx *ctx)
     a.g = ctx->g;
     a.planH = ctx->planH;
     a.twX = (const V *)ctx->d_twX;
-    a.allow_fast = ctx->use_fast ? ((ctx->use_tma ? 3 : 1) | (ctx->x_rows == 16 ? 8 : 0)) : 0;
+    a.allow_fast = ctx->use_fast ? ((ctx->use_tma ? 3 : 1) | (ctx->x_rows == 16 ? 8 : 0) | (ctx->z_lines == 8 ? 16 : 0))
+                                 : 0;
     a.status = ctx->d_status;
     return a;
 }
@@ -1182,7 +1186,8 @@ template <typename R> static PassArgs<R> pargs(gopf_ctx *ctx, bool zaxis)
     a.g = ctx->g;
     a.plan = zaxis ? ctx->planZ : ctx->planY;
     a.tw = (const V *)(zaxis ? ctx->d_twZ : ctx->d_twY);
-    a.allow_fast = ctx->use_fast ? ((ctx->use_tma ? 3 : 1) | (ctx->x_rows == 16 ? 8 : 0)) : 0;
+    a.allow_fast = ctx->use_fast ? ((ctx->use_tma ? 3 : 1) | (ctx->x_rows == 16 ? 8 : 0) | (ctx->z_lines == 8 ? 16 : 0))
+                                 : 0;
     a.status = ctx->d_status;
     return a;
 }
@@ -2591,39 +2596,28 @@ extern "C" int gopf_profile_step(gopf_ctx *ctx, int nsteps, double *avg_ms, doub
     step_slots(ctx, names, bytes);
     const size_t ns = names.size();
     *nslots = (int)ns;
-    // One step with an event between its launches, captured as a graph (as the step runs when it
-    // is replayed from the context's graphs, without host launch gaps), replayed once untimed and
-    // then nsteps times, each replay's event intervals read back and summed.
-    std::vector<cudaEvent_t> ev(1 + ns);
+    // The step's launches with a CUDA event between consecutive kernels, nsteps times.
+    std::vector<cudaEvent_t> ev(1 + ns * nsteps);
     for (auto &e : ev) CK(cudaEventCreate(&e));
     std::vector<double> acc(ns, 0.0);
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
-    if (e == cudaSuccess) {
-        e = cudaEventRecordWithFlags(ev[0], ctx->stream, cudaEventRecordExternal);
-        ctx->prof_events = &ev;
-        ctx->prof_next = 1;
-        if (e == cudaSuccess) e = (ctx->prec == GOPF_FP32) ? enqueue_euler<float>(ctx) : enqueue_euler<double>(ctx);
-        ctx->prof_events = nullptr;
-        const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &graph);
-        if (e == cudaSuccess) e = e2;
-    }
+    cudaError_t e = cudaSuccess;
+    CK(cudaEventRecord(ev[0], ctx->stream));
+    ctx->prof_events = &ev;
+    ctx->prof_next = 1;
+    for (int s = 0; s < nsteps && e == cudaSuccess; ++s)
+        e = (ctx->prec == GOPF_FP32) ? enqueue_euler<float>(ctx) : enqueue_euler<double>(ctx);
+    ctx->prof_events = nullptr;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e == cudaSuccess && ctx->prof_next != ev.size()) e = cudaErrorInvalidValue;
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
-    for (int s = -1; s < nsteps && e == cudaSuccess; ++s) {
-        e = cudaGraphLaunch(exec, ctx->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-        if (e == cudaSuccess && s >= 0)
+    if (e == cudaSuccess) {
+        for (int s = 0; s < nsteps; ++s)
             for (size_t k = 0; k < ns; ++k) {
                 float ms = 0.f;
-                cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+                cudaEventElapsedTime(&ms, ev[s * ns + k], ev[s * ns + k + 1]);
                 acc[k] += ms;
             }
+        ctx->step += nsteps;
     }
-    if (e == cudaSuccess) ctx->step += nsteps + 1;
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
     for (auto &x : ev) cudaEventDestroy(x);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "profile");
     for (size_t k = 0; k < ns && (int)k < capacity; ++k) {

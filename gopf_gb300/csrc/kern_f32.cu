@@ -11,12 +11,12 @@
 
 namespace gopf {
 
-// [Z][S] view of a z-pass array with 16 x 256 boxes
-static bool z_map(CUtensorMap *m, const float2 *p, const Geom &g)
+// [Z][S] view of a z-pass array with lines x 256 boxes
+static bool z_map(CUtensorMap *m, const float2 *p, const Geom &g, int lines = 16)
 {
     const unsigned long long dims[2] = {(unsigned long long)g.S, (unsigned long long)g.Z};
     const unsigned long long strides[1] = {(unsigned long long)g.S * sizeof(float2)};
-    const unsigned box[2] = {16, (unsigned)f256::N};
+    const unsigned box[2] = {(unsigned)lines, (unsigned)f256::N};
     return encode_map_8b(m, p, 2, dims, strides, box);
 }
 
@@ -95,6 +95,27 @@ static bool launch_z_tma(const PassArgs<float> &a, cudaStream_t st, cudaError_t 
     });
     if (attr_err != cudaSuccess) return false;
     CUtensorMap mU0, mU1, mS, mT;
+    const bool nz = (a.upd.noise.kind != 0 || a.upd.filt != nullptr);
+    if (a.nbuf == 1 && (a.allow_fast & 16) && a.g.S % f256::ZH_LINES == 0) {
+        // one group on half-width tiles: six blocks per SM
+        static std::once_flag once_h;
+        static cudaError_t attr_h = cudaSuccess;
+        std::call_once(once_h, [] {
+            attr_h = cudaFuncSetAttribute(f256::k_z256_th<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          f256::z256_th_smem_bytes());
+            if (attr_h == cudaSuccess)
+                attr_h = cudaFuncSetAttribute(f256::k_z256_th<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              f256::z256_th_smem_bytes());
+        });
+        if (attr_h != cudaSuccess || !z_map(&mU0, a.buf[0], a.g, f256::ZH_LINES) ||
+            !z_map(&mT, a.tout, a.g, f256::ZH_LINES) || !z_map(&mS, a.state, a.g, f256::ZH_LINES))
+            return false;
+        const unsigned gh = (unsigned)(a.g.S / f256::ZH_LINES);
+        if (nz) f256::k_z256_th<true><<<gh, f256::ZH_NT, f256::z256_th_smem_bytes(), st>>>(a, mU0, mS, mT);
+        else f256::k_z256_th<false><<<gh, f256::ZH_NT, f256::z256_th_smem_bytes(), st>>>(a, mU0, mS, mT);
+        *err = cudaGetLastError();
+        return true;
+    }
     if (!z_map(&mU0, a.buf[0], a.g) || !z_map(&mT, a.tout, a.g) || !z_map(&mS, a.state, a.g)) return false;
     if (a.nbuf > 1) {
         if (!z_map(&mU1, a.buf[1], a.g)) return false;
@@ -102,7 +123,6 @@ static bool launch_z_tma(const PassArgs<float> &a, cudaStream_t st, cudaError_t 
         mU1 = mU0;
     }
     const unsigned grid = (unsigned)(a.g.S / 16);
-    const bool nz = (a.upd.noise.kind != 0 || a.upd.filt != nullptr);
     const int sm1 = f256::z256_tma_smem_bytes(1), sm2 = f256::z256_tma_smem_bytes(2);
     if (a.nbuf > 1) {
         if (nz) f256::k_z256_tma<2, true><<<grid, f256::NT, sm2, st>>>(a, mU0, mU1, mS, mT);

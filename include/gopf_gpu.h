@@ -105,9 +105,12 @@ enum {
                                   gopf_synchronize), waits up to 2 s more for the copy still in flight and
                                   leaves the tile alone, so the field must be uploaded again.  Meant for
                                   testing that error path; the reference has no counterpart. */
-    GOPF_OPT_X_ROWS = 7         /* rows per tile of the 256-column x pass with one dense polynomial group:
+    GOPF_OPT_X_ROWS = 7,        /* rows per tile of the 256-column x pass with one dense polynomial group:
                                   32 (default: 256 threads, four blocks per SM) or 16 (128 threads,
                                   eight blocks per SM); both compute the same values */
+    GOPF_OPT_Z_LINES = 8        /* lines per tile of the 256-point z pass with one explicit group: 16
+                                  (default: 256 threads, three blocks per SM) or 8 (128 threads, six
+                                  blocks per SM); both compute the same values */
 };
 
 #define GOPF_MAX_FACTORS 8
@@ -396,11 +399,11 @@ int gopf_device_bytes(gopf_ctx *ctx, size_t *bytes);
  * graphs exist, i.e. after a gopf_step of at least 16 steps).  No counterpart in the reference. */
 int gopf_kernel_launches(gopf_ctx *ctx, long long nsteps, long long *count);
 int gopf_kernels_per_step(gopf_ctx *ctx, int *n);
-/* Per-kernel device time of the Euler step: one step with a CUDA event between its launches is
- * captured as a graph (so the kernels run back to back as in the context's own step graphs) and
- * replayed once untimed and then nsteps times; per kernel slot of one step write the average time
- * (ms) and the algorithmic HBM bytes (each array read and written once).  Advances the state by
- * nsteps + 1 steps.  No counterpart in the reference. */
+/* Run nsteps Euler steps launch by launch with CUDA events between kernels on the
+ * context's stream; per kernel slot of one step write the average device time (ms)
+ * and the algorithmic HBM bytes (each array read and written once).  Advances the state.
+ * (Timing the same step captured as a graph with event nodes gave slightly longer times: the
+ * event nodes themselves separate the kernels.)  No counterpart in the reference. */
 int gopf_profile_step(gopf_ctx *ctx, int nsteps, double *avg_ms, double *alg_bytes, int capacity, int *nslots);
 int gopf_profile_slot_name(gopf_ctx *ctx, int slot, char *buf, int buflen);
 

@@ -352,6 +352,23 @@ def test_half_height_x_tiles_match():
         assert np.array_equal(out[0], out[1])
 
 
+def test_half_width_z_tiles_match():
+    """The one-group 256-point z pass on 8-line tiles (128 threads, six blocks per SM) computes
+    exactly what the 16-line tiles do: bitwise equal after 10 steps, 256^3 FP32."""
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+
+    c0 = uniform_field(9, 256 ** 3, 0.0, 0.1)
+    out = []
+    for lines in (8, 16):
+        m = ch_gpu([256, 256, 256], "fp32", 0.5, 0.05, c0)
+        m.set_option(G._lib.OPT_Z_LINES, lines)
+        m.step(10)
+        out.append(m.download(0).real)
+        m.close()
+    assert np.array_equal(out[0], out[1])
+
+
 def test_real_space_x_kernels_match_generic():
     """Upload (real -> spectrum), download (spectrum -> real) and the FP64 reductions through the
     256-column real-space kernels agree with the generic x pass to FP32 round-off."""
