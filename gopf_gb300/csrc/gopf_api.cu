@@ -1192,11 +1192,10 @@ template <typename R> static PassArgs<R> pargs(gopf_ctx *ctx, bool zaxis)
     return a;
 }
 
-// External records: inside a stream capture they become event-record nodes that the host can time
 static void prof_mark(gopf_ctx *ctx)
 {
     if (ctx->prof_events && ctx->prof_next < ctx->prof_events->size())
-        cudaEventRecordWithFlags((*ctx->prof_events)[ctx->prof_next++], ctx->stream, cudaEventRecordExternal);
+        cudaEventRecord((*ctx->prof_events)[ctx->prof_next++], ctx->stream);
 }
 
 #define LK(call)                                                                                                       \
