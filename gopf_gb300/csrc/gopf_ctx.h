@@ -197,8 +197,8 @@ struct gopf_ctx {
     int use_graphs = 1;
     int use_fast = 1;
     int use_tma = 1;
-    int x_rows = 32; // tile height of the one-group 256-point x pass (GOPF_OPT_X_ROWS)
-    int z_lines = 16; // tile width of the one-group 256-point z pass (GOPF_OPT_Z_LINES)
+    int x_rows = 16; // tile height of the one-group 256-point x pass (GOPF_OPT_X_ROWS)
+    int z_lines = 8;  // tile width of the one-group 256-point z pass (GOPF_OPT_Z_LINES)
     int use_direct_host = 1;
 
     // ImplicitEuler's Newton-Krylov controls (DefaultNonLinSolver, pf/implicitEuler.go:221-228) and

@@ -106,10 +106,10 @@ enum {
                                   leaves the tile alone, so the field must be uploaded again.  Meant for
                                   testing that error path; the reference has no counterpart. */
     GOPF_OPT_X_ROWS = 7,        /* rows per tile of the 256-column x pass with one dense polynomial group:
-                                  32 (default: 256 threads, four blocks per SM) or 16 (128 threads,
-                                  eight blocks per SM); both compute the same values */
-    GOPF_OPT_Z_LINES = 8        /* lines per tile of the 256-point z pass with one explicit group: 16
-                                  (default: 256 threads, three blocks per SM) or 8 (128 threads, six
+                                  16 (default: 128 threads, eight blocks per SM) or 32 (256 threads,
+                                  four blocks per SM); both compute the same values */
+    GOPF_OPT_Z_LINES = 8        /* lines per tile of the 256-point z pass with one explicit group: 8
+                                  (default: 128 threads, six blocks per SM) or 16 (256 threads, three
                                   blocks per SM); both compute the same values */
 };
 
