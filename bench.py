@@ -41,8 +41,8 @@ UNIT = "steps/s"
 # one ncu capture on a GB300 of `python bench.py --steps 20 --warmup 17 --no-cpu-baseline --no-e2e
 # --no-precision` (the kernels' summaries under profiles/).  Bytes that a launch leaves in L2 are not
 # in these counts.
-NCU_TRAFFIC = {"zpass_update": 207.4e6, "xpass_pointwise": 72.8e6, "ypass_forward": 72.7e6,
-               "ypass_inverse": 72.7e6}
+NCU_TRAFFIC = {"zpass_update": 211.8e6, "xpass_pointwise": 72.6e6, "ypass_forward": 72.6e6,
+               "ypass_inverse": 72.6e6}
 DIMS = [256, 256, 256]
 GAMMA, M, DT, SEED = 0.5, 1.0, 0.05, 1
 CH_EQ = "dconc/dt = M*LAP conc^3 + m1*LAP conc + m1*gamma*LAP^2 conc"
