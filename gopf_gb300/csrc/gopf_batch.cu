@@ -7,10 +7,13 @@
 // present gets one x-pass launch and one fused y-pass launch over its
 // (instance, tile) items, ordered largest first, so small instances no longer
 // leave the GPU idle and the launch overhead is paid once per class instead of
-// once per instance.  The classes run as parallel branches of the step's CUDA
-// graph (a class's y pass follows its own x pass when the classes of both
-// passes cover the same instances), followed by one Hermitian-projection
-// launch over every instance: 2 x (classes) + 1 launches per step.
+// once per instance.  When the classes of both passes cover the same instances,
+// each class is a chain on its own branch of the captured graph: x pass, y pass
+// and the Hermitian projection of its own instances, for every step of the
+// graph, with one fork and one join per graph (3 launches per class and step),
+// so a class never waits for another between steps.  Otherwise the classes of
+// a pass run as parallel branches and one projection of every instance ends
+// each step (2 x classes + 1 launches).
 #include <algorithm>
 #include <cstring>
 #include <map>
@@ -29,7 +32,6 @@ template <typename R> struct BatchInst {
     XPassArgs<R> xa;
     PassArgs<R> pa;
     int lbx, lby;
-    long long herm_off; // first element of this instance in the projection index space
 };
 
 template <typename R, int LB> __device__ __forceinline__ void batch_x_item(const XPassArgs<R> &a, int ty)
@@ -212,22 +214,25 @@ template <typename R> static const void *y_kernel(int cls)
     return (const void *)k_batch_ypass<R>;
 }
 
-// Hermitian projection of the kx = 0 and kx = X/2 lines of every instance (2D)
+// Hermitian projection of the kx = 0 and kx = X/2 lines of the instances hinst[0 .. n): element
+// idx < total of the projection index space belongs to listed instance j, the last with
+// hoff[j] <= idx (hoff: prefix sums of the instances' line lengths, 1 or 2 lines of Y each)
 template <typename R>
-__global__ void k_batch_herm(const BatchInst<R> *__restrict__ inst, int ninst, long long total)
+__global__ void k_batch_herm(const BatchInst<R> *__restrict__ inst, const int *__restrict__ hinst,
+                             const long long *__restrict__ hoff, int n, long long total)
 {
     typedef typename VecOf<R>::type V;
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
-        int lo = 0, hi = ninst - 1;
-        while (lo < hi) { // last instance with herm_off <= idx
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
-            if (inst[mid].herm_off <= idx) lo = mid;
+            if (hoff[mid] <= idx) lo = mid;
             else hi = mid - 1;
         }
-        const BatchInst<R> &b = inst[lo];
+        const BatchInst<R> &b = inst[hinst[lo]];
         const Geom &g = b.pa.g;
-        const long long r = idx - b.herm_off;
+        const long long r = idx - hoff[lo];
         const int plane = (int)(r / g.Y);
         const long long y = r - (long long)plane * g.Y;
         const long long yp = (g.Y - y) % g.Y;
@@ -248,6 +253,14 @@ __global__ void k_batch_herm(const BatchInst<R> *__restrict__ inst, int ninst, l
 } // namespace gopf
 
 using namespace gopf;
+
+// one projection launch: the instances it covers and their offsets in its index space
+struct BatchHerm {
+    int *d_inst = nullptr;
+    long long *d_off = nullptr;
+    int n = 0;
+    long long total = 0;
+};
 
 // one launch of a pass: the items of one size class
 struct BatchLaunch {
@@ -280,10 +293,14 @@ struct gopf_batch {
     // When the x and y classes cover the same instance sets (square instances), class i's y pass
     // depends only on class i's x pass: each class runs x then y on its own branch (chain[i] =
     // indices into xl, yl), with no pass-wide join.  Empty: two pass-wide phases.
+    // Every step of a chain ends with the projection of its own instances (hchain[i]), so the
+    // chains need no join between steps: a captured graph of n steps forks once, runs each chain's
+    // n steps on its branch and joins once.  Without chains every step ends with hall.
     std::vector<std::pair<int, int>> chain;
+    std::vector<BatchHerm> hchain;
+    BatchHerm hall;
     std::vector<cudaStream_t> side;  // branch streams of a pass's launches
     std::vector<cudaEvent_t> ev;     // [0] fork, [1 ..] joins
-    long long herm_total = 0;
     cudaGraphExec_t g1 = nullptr, gK = nullptr;
     int K = 16;
     std::string err;
@@ -312,7 +329,6 @@ template <typename R> static int batch_build(gopf_batch *b)
     std::vector<std::pair<int, int2>> xs[NCLASS], ys[NCLASS]; // (cost, item) per size class
     int smem_x[NCLASS] = {0}, smem_y[NCLASS] = {0}, thr_x[NCLASS], thr_y[NCLASS];
     for (int k = 0; k < NCLASS; ++k) thr_x[k] = thr_y[k] = 256;
-    long long hoff = 0;
     const int vb = sizeof(V);
     for (size_t i = 0; i < b->ctx.size(); ++i) {
         gopf_ctx *c = b->ctx[i];
@@ -345,8 +361,6 @@ template <typename R> static int batch_build(gopf_batch *b)
         pa.upd.invN = 1.0 / (double)g.N;
         bi.lbx = c->LBx;
         bi.lby = c->LBy;
-        bi.herm_off = hoff;
-        hoff += ((g.X & 1) ? 1LL : 2LL) * g.Y; // the kx = 0 line, and kx = X/2 for even X
         int xc = 0, yc = 0, fx = -1, fy = -1;
         if (sizeof(R) == 4) {
             for (int k = 1; k < 7; ++k) {
@@ -412,7 +426,6 @@ template <typename R> static int batch_build(gopf_batch *b)
             smem_y[yc] = std::max(smem_y[yc], cpass_smem_bytes(g, g.Y, lb, nb, vb) + (lb + g.Y) * (int)sizeof(R));
         }
     }
-    b->herm_total = hoff;
     BCK(gopf_malloc(&b->d_inst, sizeof(BatchInst<R>) * inst.size()));
     BCK(cudaMemcpy(b->d_inst, inst.data(), sizeof(BatchInst<R>) * inst.size(), cudaMemcpyHostToDevice));
     int nsm = 0;
@@ -463,6 +476,31 @@ template <typename R> static int batch_build(gopf_batch *b)
                 if (b->xl[i].inst == b->yl[j].inst) b->chain.push_back({(int)i, (int)j});
         if (b->chain.size() != b->xl.size()) b->chain.clear();
     }
+    // projection launches: all instances, and each chain's own
+    auto make_herm = [&](const std::vector<int> &ids, BatchHerm &h) -> int {
+        std::vector<long long> off;
+        long long t = 0;
+        for (int i : ids) {
+            off.push_back(t);
+            const Geom &g = b->ctx[i]->g;
+            t += ((g.X & 1) ? 1LL : 2LL) * g.Y;
+        }
+        h.n = (int)ids.size();
+        h.total = t;
+        BCK(gopf_malloc(&h.d_inst, sizeof(int) * ids.size()));
+        BCK(gopf_malloc(&h.d_off, sizeof(long long) * off.size()));
+        BCK(cudaMemcpy(h.d_inst, ids.data(), sizeof(int) * ids.size(), cudaMemcpyHostToDevice));
+        BCK(cudaMemcpy(h.d_off, off.data(), sizeof(long long) * off.size(), cudaMemcpyHostToDevice));
+        return GOPF_OK;
+    };
+    {
+        std::vector<int> all(b->ctx.size());
+        for (size_t i = 0; i < all.size(); ++i) all[i] = (int)i;
+        if ((rc = make_herm(all, b->hall))) return rc;
+        b->hchain.assign(b->chain.size(), BatchHerm());
+        for (size_t i = 0; i < b->chain.size(); ++i)
+            if ((rc = make_herm(b->xl[b->chain[i].first].inst, b->hchain[i]))) return rc;
+    }
     const size_t nbranch = std::max(b->xl.size(), b->yl.size());
     while (b->side.size() + 1 < nbranch) {
         cudaStream_t st;
@@ -512,8 +550,15 @@ template <typename R> static cudaError_t launch_one(gopf_batch *b, const BatchLa
     return cudaLaunchKernel(L.fn, dim3(L.grid), dim3(L.threads), args, (size_t)L.smem, st);
 }
 
-// class chains: x then y of each class on its own branch
-template <typename R> static cudaError_t batch_chains(gopf_batch *b)
+template <typename R> static cudaError_t launch_herm(gopf_batch *b, const BatchHerm &h, cudaStream_t st)
+{
+    const unsigned hb = (unsigned)std::max<long long>(1, std::min<long long>((h.total + 255) / 256, 152 * 4));
+    k_batch_herm<R><<<hb, 256, 0, st>>>((const BatchInst<R> *)b->d_inst, h.d_inst, h.d_off, h.n, h.total);
+    return cudaGetLastError();
+}
+
+// n steps of the class chains: each class runs x, y and its projection n times on its own branch
+template <typename R> static cudaError_t batch_chains(gopf_batch *b, int nsteps)
 {
     cudaError_t e;
     const size_t n = b->chain.size();
@@ -524,8 +569,11 @@ template <typename R> static cudaError_t batch_chains(gopf_batch *b)
     }
     for (size_t i = 0; i < n; ++i) {
         cudaStream_t st = (i == 0) ? b->stream : b->side[i - 1];
-        if ((e = launch_one<R>(b, b->xl[b->chain[i].first], st)) != cudaSuccess) return e;
-        if ((e = launch_one<R>(b, b->yl[b->chain[i].second], st)) != cudaSuccess) return e;
+        for (int s = 0; s < nsteps; ++s) {
+            if ((e = launch_one<R>(b, b->xl[b->chain[i].first], st)) != cudaSuccess) return e;
+            if ((e = launch_one<R>(b, b->yl[b->chain[i].second], st)) != cudaSuccess) return e;
+            if ((e = launch_herm<R>(b, b->hchain[i], st)) != cudaSuccess) return e;
+        }
         if (i > 0 && (e = cudaEventRecord(b->ev[i], st)) != cudaSuccess) return e;
     }
     for (size_t i = 1; i < n; ++i)
@@ -533,28 +581,21 @@ template <typename R> static cudaError_t batch_chains(gopf_batch *b)
     return cudaSuccess;
 }
 
-template <typename R> static cudaError_t batch_enqueue(gopf_batch *b)
+template <typename R> static cudaError_t batch_enqueue(gopf_batch *b, int nsteps)
 {
-    const BatchInst<R> *inst = (const BatchInst<R> *)b->d_inst;
+    if (!b->chain.empty()) return batch_chains<R>(b, nsteps);
     cudaError_t e;
-    if (!b->chain.empty()) {
-        if ((e = batch_chains<R>(b)) != cudaSuccess) return e;
-    } else {
+    for (int s = 0; s < nsteps; ++s) {
         if ((e = batch_pass<R>(b, b->xl)) != cudaSuccess) return e;
         if ((e = batch_pass<R>(b, b->yl)) != cudaSuccess) return e;
+        if ((e = launch_herm<R>(b, b->hall, b->stream)) != cudaSuccess) return e;
     }
-    const unsigned hb = (unsigned)std::min<long long>((b->herm_total + 255) / 256, 152 * 4);
-    k_batch_herm<R><<<hb, 256, 0, b->stream>>>(inst, (int)b->ctx.size(), b->herm_total);
-    return cudaGetLastError();
+    return cudaSuccess;
 }
 
 static cudaError_t batch_enqueue_any(gopf_batch *b, int n)
 {
-    for (int i = 0; i < n; ++i) {
-        cudaError_t e = (b->prec == GOPF_FP32) ? batch_enqueue<float>(b) : batch_enqueue<double>(b);
-        if (e != cudaSuccess) return e;
-    }
-    return cudaSuccess;
+    return (b->prec == GOPF_FP32) ? batch_enqueue<float>(b, n) : batch_enqueue<double>(b, n);
 }
 
 static int batch_capture(gopf_batch *b, int n, cudaGraphExec_t *exec)
@@ -620,6 +661,16 @@ static void batch_release(gopf_batch *b)
         ls->clear();
     }
     b->chain.clear();
+    for (BatchHerm *h : {&b->hall}) {
+        if (h->d_inst) cudaFree(h->d_inst);
+        if (h->d_off) cudaFree(h->d_off);
+        *h = BatchHerm();
+    }
+    for (BatchHerm &h : b->hchain) {
+        if (h.d_inst) cudaFree(h.d_inst);
+        if (h.d_off) cudaFree(h.d_off);
+    }
+    b->hchain.clear();
 }
 
 static int batch_rebuild(gopf_batch *b)
@@ -876,6 +927,6 @@ extern "C" int gopf_batch_step(gopf_batch *b, long long nsteps)
 extern "C" int gopf_batch_kernels_per_step(gopf_batch *b, int *n)
 {
     if (!b || !n) return GOPF_ERR_ARG;
-    *n = (int)(b->xl.size() + b->yl.size()) + 1;
+    *n = b->chain.empty() ? (int)(b->xl.size() + b->yl.size()) + 1 : 3 * (int)b->chain.size();
     return GOPF_OK;
 }

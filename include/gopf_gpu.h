@@ -327,8 +327,12 @@ int gopf_adjoint_release(gopf_ctx *ctx);
  * single counterpart in the reference.  Every context keeps its own model,
  * dt and device state; gopf_batch_step(nsteps) advances all of them by
  * nsteps Euler steps: per step one x-pass and one y-pass launch for each size
- * class present plus one projection launch (gopf_batch_kernels_per_step),
- * captured in a CUDA graph.
+ * class present and the projection of the self-conjugate lines, captured in a
+ * CUDA graph.  When the x and y classes cover the same instances each class
+ * runs its x, y and projection launches on its own branch for all steps of a
+ * graph (3 launches per class and step); otherwise the classes of a pass run
+ * side by side and one projection of every instance ends each step
+ * (2 x classes + 1).  gopf_batch_kernels_per_step reports the count.
  * Contexts must be 2D, single-field, Euler, without user-defined terms, on one
  * device and precision, and stay alive while the batch exists. */
 typedef struct gopf_batch gopf_batch;

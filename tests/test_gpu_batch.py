@@ -105,8 +105,11 @@ def test_batch_with_large_instances_runs_and_stays_finite():
 
 def test_batch_size_classes_equal_generic_contexts():
     """The sweep's sides go through one kernel per size class (the register line engine for FP32 sides
-    256 ... 1024, compile-time Stockham plans for 128), run as parallel graph branches; they compute
-    what the runtime-plan kernels of single contexts compute, to FP32 rounding."""
+    256 ... 1024, compile-time Stockham plans for 128).  Each class is a chain of x pass, y pass and
+    the projection of its own instances on its own graph branch (3 launches per class and step,
+    no join between steps).  They compute what the runtime-plan kernels of single contexts compute,
+    to FP32 rounding, after 12 steps (a 1-step graph and a 16-step graph replay both appear when
+    stepping 12 then 20)."""
     import gopf_gb300 as G
     from gopf_gb300.synthetic import uniform_field
 
@@ -117,13 +120,14 @@ def test_batch_size_classes_equal_generic_contexts():
         a_models.append(ch_ctx(side, "fp32", 0.4 + 0.1 * i, 1.0, 0.05, c0, fast=False))
         b_models.append(ch_ctx(side, "fp32", 0.4 + 0.1 * i, 1.0, 0.05, c0, fast=False))
     batch = G.Batch(a_models)
-    assert batch.kernels_per_step() == 6 + 6 + 1
-    batch.step(12)
-    for m in b_models:
-        m.step(12)
-    for a, b in zip(a_models, b_models):
-        x, y = a.download_real(0), b.download_real(0)
-        assert np.max(np.abs(x - y)) <= 1e-6 * np.max(np.abs(y))
+    assert batch.kernels_per_step() == 3 * 6
+    for n in (12, 20):
+        batch.step(n)
+        for m in b_models:
+            m.step(n)
+        for a, b in zip(a_models, b_models):
+            x, y = a.download_real(0), b.download_real(0)
+            assert np.max(np.abs(x - y)) <= 1e-6 * np.max(np.abs(y))
 
 
 def test_sweep_draw_fp32_batch_matches_fp64_per_instance():
