@@ -508,6 +508,8 @@ def run_sweep(args):
     sweep_bytes = float(sum(6 * (s // 2 + 1) * s * 8 for s, _, _ in params))
     models = sweep_models("fp32", params, indices=mine, device=local)
     batch = G.Batch(models)
+    if args.batch_mode != "auto":
+        batch.set_mode(G._lib.BATCH_MODE_PERSISTENT if args.batch_mode == "persistent" else G._lib.BATCH_MODE_CHAINS)
     tuned, tune_s = None, None
     if not args.no_tune:
         # the autotuner: kernel family, tile width and plan variant per kind of instance, timed on
@@ -558,7 +560,7 @@ def run_sweep(args):
         seq = kseq / (e0.elapsed_time(e1) / 1000.0)
         for m in seq_models:
             m.close()
-    launches = batch.kernels_per_step() * args.steps
+    launches = batch.launches(args.steps)
     check = None
     if args.check_steps != 0:
         # per-instance rel-L2 of the FP32 batch against sequential FP64 runs, each rank checking its
@@ -590,6 +592,7 @@ def run_sweep(args):
                           "parallelism": f"instances sharded over {world} GPU(s), no collective"
                                          if world > 1 else "single GPU",
                           "rank_cells": rank_cells,
+                          "mode": "persistent" if batch.mode() == G._lib.BATCH_MODE_PERSISTENT else "chains",
                           "tuned": tuned, "tune_seconds": tune_s,
                           "families": "0 line engine, 1 compile-time Stockham, 2 runtime Stockham"},
                "sequential_value": seq, "speedup_vs_sequential": (batched / seq) if seq else None,
@@ -860,6 +863,8 @@ def main():
     ap.add_argument("--tma", type=int, default=None, choices=[0, 1],
                     help="tile movement of the 256-point kernels: 0 plain loads, 1 TMA")
     ap.add_argument("--no-tune", action="store_true", help="sweep: keep the built-in kernel choices")
+    ap.add_argument("--batch-mode", default="auto", choices=["auto", "persistent", "chains"],
+                    help="sweep: one persistent kernel per captured graph, or a launch per class and pass")
     ap.add_argument("--check-steps", type=int, default=-1,
                     help="sweep: per-instance rel-L2 against FP64 after this many steps (-1: the configuration's "
                          "2000; 0: no check)")

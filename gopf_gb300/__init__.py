@@ -467,6 +467,28 @@ class Batch:
         self._ck(self._L.gopf_batch_choice(self._h, int(inst), out))
         return dict(zip(("xfam", "yfam", "lbx", "lby", "xplan", "yplan"), list(out)))
 
+    def set_mode(self, mode: int) -> None:
+        """BATCH_MODE_PERSISTENT (one persistent kernel per captured graph), BATCH_MODE_CHAINS (a launch
+        per class and pass) or BATCH_MODE_AUTO (persistent when every instance allows it)."""
+        self._ck(self._L.gopf_batch_set_mode(self._h, int(mode)))
+
+    def mode(self) -> int:
+        """The mode in effect: BATCH_MODE_PERSISTENT or BATCH_MODE_CHAINS."""
+        m = ctypes.c_int()
+        self._ck(self._L.gopf_batch_mode(self._h, ctypes.byref(m)))
+        return m.value
+
+    def set_wait_limit_ns(self, ns: int) -> None:
+        """Limit of the persistent kernel's dependency waits (0: the built-in 2 s)."""
+        self._ck(self._L.gopf_batch_set_wait_limit(self._h, int(ns)))
+
+    def launches(self, nsteps: int) -> int:
+        """Kernel launches gopf_batch_step(nsteps) makes: one per captured graph replay (16-step
+        graphs, then 1-step graphs) in the persistent mode, kernels_per_step() per step otherwise."""
+        if self.mode() == _lib.BATCH_MODE_PERSISTENT:
+            return nsteps // 16 + nsteps % 16
+        return self.kernels_per_step() * nsteps
+
     @staticmethod
     def tune_reset() -> None:
         _lib.load().gopf_batch_tune_reset()

@@ -31,6 +31,7 @@ OPT_X_ROWS = 7
 OPT_Z_LINES = 8
 MAX_FACTORS = 8
 BATCH_AUTO, BATCH_LINE, BATCH_STOCKHAM_CT, BATCH_STOCKHAM = -1, 0, 1, 2
+BATCH_MODE_AUTO, BATCH_MODE_CHAINS, BATCH_MODE_PERSISTENT = -1, 0, 1
 
 
 class GopfDerived(ctypes.Structure):
@@ -137,6 +138,9 @@ SIGNATURES = {
     "gopf_batch_tune_reset": ([], _i),
     "gopf_batch_force": ([_vp, _i, _i, _i, _i, _i, _i], _i),
     "gopf_batch_choice": ([_vp, _i, _ip], _i),
+    "gopf_batch_set_mode": ([_vp, _i], _i),
+    "gopf_batch_mode": ([_vp, _ip], _i),
+    "gopf_batch_set_wait_limit": ([_vp, ctypes.c_longlong], _i),
     "gopf_sweep_partition": ([ctypes.POINTER(_ll), _i, _i, _ip, ctypes.POINTER(_ll)], _i),
 }
 

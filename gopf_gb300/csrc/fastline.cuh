@@ -47,6 +47,15 @@ template <int L> struct Geo {
     static_assert(L == 256 || L == 384 || L == 512 || L == 768 || L == 1024, "line length");
 };
 
+// Barrier over the Geo<L>::NT threads of a tile: __syncthreads when the tile takes a whole 256-thread
+// block, else named barrier 1 over its NT threads, so that a larger block (the persistent batch
+// kernel's) can leave its other threads out of the tile.
+template <int L> __device__ __forceinline__ void lsync()
+{
+    if constexpr (Geo<L>::NT == 256) __syncthreads();
+    else asm volatile("bar.sync 1, %0;" ::"n"(Geo<L>::NT) : "memory");
+}
+
 // First-stage twiddles W_L^(r k1) (r < T, k1 < 16) laid out [k1][r]: the T threads of a line read
 // consecutive slots (conflict free) instead of the strided W_L table entries r k1.
 template <int L> __device__ __forceinline__ void load_twr(float2 *twr, const float2 *__restrict__ tw, int nt)
@@ -186,7 +195,7 @@ __device__ __forceinline__ void line_fwd(float2 (&v)[16], int r, const Role<L> &
     for (int k1 = 1; k1 < 16; ++k1) v[k1] = cm(v[k1], twr[k1 * G::T + r]);
 #pragma unroll
     for (int k1 = 0; k1 < 16; ++k1) z[slot(r, k1)] = v[k1];
-    __syncthreads();
+    lsync<L>();
     if constexpr (G::U == 3) {
         // T = 3 P: r = s + P t, k2 = 3 c + d.  The thread's output d: radix-3 over t (reading the
         // three rows of each s), twiddle W_T^(s d) = W_L^(16 s d), radix-P over s.
@@ -198,7 +207,7 @@ __device__ __forceinline__ void line_fwd(float2 (&v)[16], int r, const Role<L> &
                 const int col = ro.k1 + 8 * h;
                 v[P * h + s] = dft3_out<false>(z[slot(s, col)], z[slot(s + P, col)], z[slot(s + 2 * P, col)], ro.d);
             }
-        __syncthreads();
+        lsync<L>();
         if (ro.d)
 #pragma unroll
             for (int j = 0; j < 16; ++j)
@@ -212,7 +221,7 @@ __device__ __forceinline__ void line_fwd(float2 (&v)[16], int r, const Role<L> &
     } else {
 #pragma unroll
         for (int s = 0; s < 16; ++s) v[s] = z[slot(G::U * s + ro.u, ro.k1)];
-        __syncthreads();
+        lsync<L>();
         pdft16<false>(v);
         if (G::U > 1 && ro.u)
 #pragma unroll
@@ -245,12 +254,12 @@ __device__ __forceinline__ void line_inv(float2 (&v)[16], int r, const Role<L> &
         for (int h = 0; h < 16 / P; ++h)
 #pragma unroll
             for (int s = 0; s < P; ++s) z[slot(ro.d * P + s, ro.k1 + 8 * h)] = v[P * h + s];
-        __syncthreads();
+        lsync<L>();
         const int s0 = r % P, t0 = r / P;
 #pragma unroll
         for (int k1 = 0; k1 < 16; ++k1)
             v[k1] = dft3_out<true>(z[slot(s0, k1)], z[slot(P + s0, k1)], z[slot(2 * P + s0, k1)], t0);
-        __syncthreads();
+        lsync<L>();
     } else {
         if constexpr (G::U == 2 || G::U == 4) xdft_inv<G::U, true>(v, ro.u);
         if (G::U > 1 && ro.u)
@@ -259,10 +268,10 @@ __device__ __forceinline__ void line_inv(float2 (&v)[16], int r, const Role<L> &
         pdft16<true>(v);
 #pragma unroll
         for (int s = 0; s < 16; ++s) z[slot(G::U * s + ro.u, ro.k1)] = v[s];
-        __syncthreads();
+        lsync<L>();
 #pragma unroll
         for (int k1 = 0; k1 < 16; ++k1) v[k1] = z[slot(r, k1)];
-        __syncthreads();
+        lsync<L>();
     }
 #pragma unroll
     for (int k1 = 1; k1 < 16; ++k1) v[k1] = cmc(v[k1], twr[k1 * G::T + r]);
@@ -303,7 +312,7 @@ template <int L, int NG> __device__ __forceinline__ void yline_tile(const PassAr
     // latency overlaps the forward FFT
 #pragma unroll
     for (int j = 0; j < 16; ++j) cs[j] = valid ? state[q * L + ro.elem(j)] : zero;
-    __syncthreads();
+    lsync<L>();
     line_fwd<L>(v, r, ro, z, s_tw, s_twr);
     const UpdTable &u = a.upd;
     const int ngrp = (NG == 1) ? (u.ngrp > 0 ? 1 : 0) : u.ngrp;
@@ -411,7 +420,7 @@ __device__ __forceinline__ void xline_separate(float2 (&v)[16], float2 *s_sep, i
     constexpr int KX = G::KX;
 #pragma unroll
     for (int i = 0; i < 16; ++i) s_sep[l * G::SEP + r + G::T * i] = make_float2(v[i].x, -v[i].y);
-    __syncthreads();
+    lsync<L>();
     for (int e = threadIdx.x; e < KX * G::LPB; e += G::NT) {
         const int kx = e / G::LPB, p = e - kx * G::LPB;
         const float2 P = s_sep[p * G::SEP + kx];
@@ -420,7 +429,7 @@ __device__ __forceinline__ void xline_separate(float2 (&v)[16], float2 *s_sep, i
             *reinterpret_cast<float4 *>(&out[sbase + (long long)kx * Y + 2 * p]) =
                 make_float4(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y), 0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
     }
-    __syncthreads();
+    lsync<L>();
 }
 
 // One x tile from its spectral tile in area (which then serves as exchange and separation
@@ -446,7 +455,7 @@ __device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float
     const Role<L> ro(r);
     float2 v[16];
     xline_gather_conj<L>(s_a, l, r, v);
-    __syncthreads(); // the tile becomes the exchange slots
+    lsync<L>(); // the tile becomes the exchange slots
     float2 *z = s_a + l * G::LREG;
     line_fwd<L>(v, r, ro, z, s_tw, s_twr);
     // conj(v[j]) = c(row 2l, col elem(j)) + i c(row 2l + 1, col elem(j)) (times L)
@@ -508,7 +517,7 @@ template <int L, bool ONE = false> __device__ __forceinline__ void xline_tile(co
     xline_request<L>(s_a, a, ty, zp);
     load_xconsts<L>(a, s_tw, s_twr, s_poly);
     cp_async_wait<0>();
-    __syncthreads();
+    lsync<L>();
     xline_compute<L, ONE>(s_a, a, ty, zp, s_tw, s_twr, s_poly);
 }
 

@@ -6,14 +6,18 @@
 // together.  Instances are grouped into size classes; per step each class
 // present gets one x-pass launch and one fused y-pass launch over its
 // (instance, tile) items, ordered largest first, so small instances no longer
-// leave the GPU idle and the launch overhead is paid once per class instead of
-// once per instance.  When the classes of both passes cover the same instances,
-// each class is a chain on its own branch of the captured graph: x pass, y pass
-// and the Hermitian projection of its own instances, for every step of the
-// graph, with one fork and one join per graph (3 launches per class and step),
-// so a class never waits for another between steps.  Otherwise the classes of
-// a pass run as parallel branches and one projection of every instance ends
-// each step (2 x classes + 1 launches).
+// leave the GPU idle.  Two ways to step them, both captured in CUDA graphs of 1
+// and 16 steps:
+// - persistent (the default where every instance allows it): one kernel launch
+//   per graph.  Its blocks take the x and y tiles of every instance and step
+//   from one queue; per-instance counters order each instance's tiles
+//   (k_batch_persist);
+// - chains: when the classes of both passes cover the same instances, each
+//   class is a chain on its own branch of the graph: x pass, y pass and the
+//   Hermitian projection of its own instances, for every step of the graph,
+//   with one fork and one join per graph (3 launches per class and step).
+//   Otherwise the classes of a pass run as parallel branches and one projection
+//   of every instance ends each step (2 x classes + 1 launches).
 #include <algorithm>
 #include <cstring>
 #include <map>
@@ -250,6 +254,179 @@ __global__ void k_batch_herm(const BatchInst<R> *__restrict__ inst, const int *_
     }
 }
 
+// ---- the persistent sweep kernel ----
+// One launch steps every instance nsteps times.  The items of one step (x tiles, then y tiles, each
+// class largest first) are handed out in order from a queue counter; item g of the launch is item
+// g % nper of step g / nper.  An x item of step s needs every y item of its instance's step s - 1
+// done (it overwrites the rows of T they wrote), a y item every x item of its instance's step s (it
+// reads the lines they wrote): per-instance completion counters, incremented after an item's last
+// write, carry that.  An item's dependencies always come earlier in the queue, so they were taken by
+// running blocks and complete: no wait can deadlock, and every wait is bounded all the same.
+// An item {instance, first tile, kind, tiles} covers `tiles` consecutive tiles of one instance and pass;
+// the counters count tiles.
+// Item kinds: PK_X + c (x pass) and PK_Y + c (y pass) of size class c: 0 .. 4 the line engine's sides
+// 256, 384, 512, 768, 1024 (x: one dense polynomial group, y: one group), PK_CT the side 128 on
+// compile-time Stockham tiles (x: 16-row tiles of the 64-point half transform, y: 16-line tiles).  A y
+// item also projects the self-conjugate lines it owns (kx = 0 and X/2), as k_batch_herm does after a
+// pass.  The 192-thread tiles (384, 768) run on the block's first 192 threads under a named barrier.
+constexpr int PK_X = 0, PK_Y = 8, PK_CT = 5, PK_TILES = 2;
+// lines per y tile of class c
+__host__ __device__ constexpr int pk_lpb(int c)
+{
+    return c == 0 ? fl::Geo<256>::LPB : c == 1 ? fl::Geo<384>::LPB : c == 2 ? fl::Geo<512>::LPB
+         : c == 3 ? fl::Geo<768>::LPB : c == 4 ? fl::Geo<1024>::LPB : 16;
+}
+
+// The counters' ordering: a block's writes, a barrier, then a release add by one of its threads; the
+// waiting block's thread sees the count with an acquire load, then a barrier, then the block reads.
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void red_release_add(unsigned *p, unsigned v)
+{
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Wait until *c >= need, for at most the limit at status + 2 (u64 ns; 0: 2 s).  On timeout flag
+// DS_DEP_TIMEOUT in status[0] and return false.
+__device__ __noinline__ bool pk_wait(const unsigned *c, unsigned need, unsigned *status)
+{
+    if (ld_acquire_u32(c) >= need) return true;
+    unsigned long long lim = *reinterpret_cast<const volatile unsigned long long *>(status + 2);
+    if (!lim) lim = 2000000000ull;
+    const unsigned long long t0 = global_ns();
+    while (true) {
+        __nanosleep(128);
+        if (ld_acquire_u32(c) >= need) return true;
+        if (global_ns() - t0 > lim) {
+            atomicOr(status, (unsigned)DS_DEP_TIMEOUT);
+            return false;
+        }
+    }
+}
+
+// The tile kinds are separate (not inlined) functions, so that each gets its own register
+// allocation instead of the kernel holding the union of all of them.
+template <int L> __device__ __noinline__ void pk_x(const BatchInst<float> *bi, int tile, XPassArgs<float> *s_a)
+{
+    stage_args(s_a, &bi->xa);
+    __syncthreads();
+    if (threadIdx.x < fl::Geo<L>::NT) fl::xline_tile<L, true>(*s_a, tile, 0);
+}
+
+template <int L> __device__ __noinline__ void pk_y(const BatchInst<float> *bi, int tile)
+{
+    if (threadIdx.x < fl::Geo<L>::NT) fl::yline_tile<L, 1>(bi->pa, tile);
+}
+
+__device__ __noinline__ void pk_x_ct(const BatchInst<float> *bi, int tile, XPassArgs<float> *s_a)
+{
+    stage_args(s_a, &bi->xa);
+    __syncthreads();
+    if (s_a->ngrp_out) xpass_tile<float, 16, 16, false, 64>(*s_a, tile, 0);
+}
+
+__device__ __noinline__ void pk_y_ct(const BatchInst<float> *bi, int tile, PassArgs<float> *s_a)
+{
+    stage_args(s_a, &bi->pa);
+    __syncthreads();
+    pass_tile<float, 16, 16, true, false, 128>(*s_a, tile, 0);
+}
+
+// the projection of line kx of a 2D instance's c-hat (the formula of k_batch_herm)
+__device__ __forceinline__ void pk_herm_line(float2 *__restrict__ c, long long base, int Y)
+{
+    for (int y = threadIdx.x; y < Y; y += blockDim.x) {
+        const int yp = (Y - y) % Y;
+        if (y > yp) continue;
+        const float2 a = c[base + y], b = c[base + yp];
+        float2 m;
+        m.x = (a.x + b.x) * 0.5f;
+        m.y = (a.y - b.y) * 0.5f;
+        c[base + y] = m;
+        m.y = -m.y;
+        c[base + yp] = m;
+    }
+}
+
+__global__ void __launch_bounds__(256, 3)
+    k_batch_persist(const BatchInst<float> *__restrict__ inst, const int4 *__restrict__ items, int nper, int nsteps,
+                    const int2 *__restrict__ nxy, unsigned *__restrict__ ctr, unsigned *status)
+{
+    // an item's pass arguments, staged in shared memory (x: XPassArgs, y on Stockham tiles: PassArgs)
+    __shared__ __align__(16) unsigned char s_args[sizeof(XPassArgs<float>) > sizeof(PassArgs<float>)
+                                                      ? sizeof(XPassArgs<float>)
+                                                      : sizeof(PassArgs<float>)];
+    XPassArgs<float> *s_xa = reinterpret_cast<XPassArgs<float> *>(s_args);
+    __shared__ int s_g;
+    __shared__ int4 s_it;
+    const int total = nper * nsteps;
+    // Thread 0 takes the tickets and waits for the dependencies; the next ticket is taken while the
+    // current item runs (its latency hides there).  A block holding a ticket it has not started
+    // cannot deadlock the queue: it took that ticket after the one it is running, and every item's
+    // dependencies have smaller tickets.
+    auto prepare = [&](int g) {
+        int4 it = make_int4(0, 0, -1, 0);
+        if (g < total) {
+            const int s = g / nper;
+            it = items[g - s * nper];
+            const bool yp = it.z >= PK_Y;
+            const unsigned need = yp ? (unsigned)((s + 1) * nxy[it.x].x) : (unsigned)(s * nxy[it.x].y);
+            // a wait that ran out skips the item (the step is flagged) but still counts it done
+            if (!pk_wait(&ctr[1 + 2 * it.x + (yp ? 0 : 1)], need, status)) g = -1 - g;
+        } else {
+            g = total;
+        }
+        s_g = g;
+        s_it = it;
+    };
+    if (threadIdx.x == 0) prepare((int)atomicAdd(ctr, 1u));
+    __syncthreads();
+    for (;;) {
+        const int g = s_g;
+        if (g >= total) return;
+        const int4 it = s_it;
+        int gnext = total;
+        if (threadIdx.x == 0) gnext = (int)atomicAdd(ctr, 1u);
+        const BatchInst<float> *bi = inst + it.x;
+        for (int k = 0; g >= 0 && k < it.w; ++k) {
+            const int tile = it.y + k;
+            if (k) __syncthreads(); // the previous tile is done with the shared memory
+            switch (it.z) {
+            case PK_X + 0: pk_x<256>(bi, tile, s_xa); break;
+            case PK_X + 1: pk_x<384>(bi, tile, s_xa); break;
+            case PK_X + 2: pk_x<512>(bi, tile, s_xa); break;
+            case PK_X + 3: pk_x<768>(bi, tile, s_xa); break;
+            case PK_X + 4: pk_x<1024>(bi, tile, s_xa); break;
+            case PK_X + PK_CT: pk_x_ct(bi, tile, s_xa); break;
+            case PK_Y + 0: pk_y<256>(bi, tile); break;
+            case PK_Y + 1: pk_y<384>(bi, tile); break;
+            case PK_Y + 2: pk_y<512>(bi, tile); break;
+            case PK_Y + 3: pk_y<768>(bi, tile); break;
+            case PK_Y + 4: pk_y<1024>(bi, tile); break;
+            case PK_Y + PK_CT: pk_y_ct(bi, tile, reinterpret_cast<PassArgs<float> *>(s_args)); break;
+            default: break;
+            }
+            if (it.z >= PK_Y) {
+                __syncthreads(); // the tile's c-hat writes are done
+                const int Y = bi->pa.g.Y, H = bi->pa.g.H;
+                const long long q0 = (long long)tile * pk_lpb(it.z - PK_Y);
+                const long long q1 = q0 + pk_lpb(it.z - PK_Y);
+                if (q0 == 0) pk_herm_line(bi->pa.state, 0, Y);
+                if (H >= q0 && H < q1) pk_herm_line(bi->pa.state, (long long)H * Y, Y);
+            }
+        }
+        __syncthreads(); // every write of the item is done, and s_g, s_it are free again
+        if (threadIdx.x == 32) // the completion, while thread 0 prepares the next item
+            red_release_add(&ctr[1 + 2 * it.x + (it.z >= PK_Y ? 1 : 0)], (unsigned)it.w);
+        if (threadIdx.x == 0) prepare(gnext);
+        __syncthreads();
+    }
+}
+
 } // namespace gopf
 
 using namespace gopf;
@@ -299,6 +476,15 @@ struct gopf_batch {
     std::vector<std::pair<int, int>> chain;
     std::vector<BatchHerm> hchain;
     BatchHerm hall;
+    // the persistent mode (k_batch_persist): requested mode, mode in effect (1: persistent), the items
+    // of one step, per-instance item counts, the queue and completion counters, the launch shape
+    int mode = GOPF_BATCH_MODE_AUTO, pmode = 0;
+    int4 *d_pitems = nullptr;
+    int2 *d_pnxy = nullptr;
+    unsigned *d_pctr = nullptr;
+    int pnper = 0, pgrid = 0, psmem = 0;
+    size_t pctr_bytes = 0;
+    unsigned *d_pstatus = nullptr; // [0] flags, [2..3] wait limit (u64 ns, 0: 2 s)
     std::vector<cudaStream_t> side;  // branch streams of a pass's launches
     std::vector<cudaEvent_t> ev;     // [0] fork, [1 ..] joins
     cudaGraphExec_t g1 = nullptr, gK = nullptr;
@@ -501,6 +687,81 @@ template <typename R> static int batch_build(gopf_batch *b)
         for (size_t i = 0; i < b->chain.size(); ++i)
             if ((rc = make_herm(b->xl[b->chain[i].first].inst, b->hchain[i]))) return rc;
     }
+    // the persistent mode: every instance on a kind k_batch_persist runs (FP32)
+    b->pmode = 0;
+    if (b->mode != GOPF_BATCH_MODE_CHAINS) {
+        bool ok = (sizeof(R) == 4);
+        std::vector<int> xkind(b->ctx.size(), -1), ykind(b->ctx.size(), -1);
+        for (int k = 0; k < NCLASS && ok; ++k) {
+            int xk = -1, yk = -1;
+            if (k >= 31 && k <= 35) xk = PK_X + (k - 31);
+            if (k == 1) xk = PK_X + PK_CT;
+            if (k >= 11 && k <= 15) yk = PK_Y + (k - 11);
+            if (k == 1) yk = PK_Y + PK_CT;
+            for (auto &p : xs[k]) {
+                if (xk < 0) ok = false;
+                xkind[p.second.x] = xk;
+            }
+            for (auto &p : ys[k]) {
+                if (yk < 0) ok = false;
+                ykind[p.second.x] = yk;
+            }
+        }
+        for (size_t i = 0; i < b->ctx.size() && ok; ++i)
+            if (xkind[i] < 0 || ykind[i] < 0 || (b->ctx[i]->g.X & 1)) ok = false;
+        if (!ok && b->mode == GOPF_BATCH_MODE_PERSISTENT)
+            return bfail(b, GOPF_ERR_UNSUPPORTED,
+                         "the persistent mode takes FP32 instances of sides 128 ... 1024 on the line engine "
+                         "(256 ... 1024, one dense polynomial group) or compile-time Stockham tiles (128)");
+        if (ok) {
+            // one step's items: the x tiles of every class, largest class first, then the y tiles
+            std::vector<int4> items;
+            std::vector<int2> nxy(b->ctx.size(), make_int2(0, 0));
+            int smem = 0;
+            for (int pass = 0; pass < 2; ++pass) {
+                std::vector<std::pair<long long, int>> order;
+                for (int k = 0; k < NCLASS; ++k) {
+                    auto &lst = pass ? ys[k] : xs[k];
+                    if (lst.empty()) continue;
+                    long long cost = 0;
+                    for (auto &p : lst) cost += p.first;
+                    order.push_back({cost, k});
+                    smem = std::max(smem, pass ? smem_y[k] : smem_x[k]);
+                }
+                std::sort(order.begin(), order.end(), [](auto &a, auto &c) { return a.first > c.first; });
+                for (auto &o : order) {
+                    // consecutive tiles of an instance, PK_TILES to an item (the class's list holds
+                    // each instance's tiles in order, instances largest first)
+                    const auto &lst = pass ? ys[o.second] : xs[o.second];
+                    for (size_t a = 0; a < lst.size();) {
+                        const int i = lst[a].second.x, t0 = lst[a].second.y;
+                        int w = 1;
+                        while (w < PK_TILES && a + w < lst.size() && lst[a + w].second.x == i &&
+                               lst[a + w].second.y == t0 + w)
+                            ++w;
+                        items.push_back(make_int4(i, t0, pass ? ykind[i] : xkind[i], w));
+                        if (pass) nxy[i].y += w;
+                        else nxy[i].x += w;
+                        a += w;
+                    }
+                }
+            }
+            b->pnper = (int)items.size();
+            b->psmem = smem;
+            b->pctr_bytes = sizeof(unsigned) * (1 + 2 * b->ctx.size());
+            BCK(gopf_malloc(&b->d_pitems, sizeof(int4) * items.size()));
+            BCK(gopf_malloc(&b->d_pnxy, sizeof(int2) * nxy.size()));
+            BCK(gopf_malloc(&b->d_pctr, b->pctr_bytes));
+            BCK(cudaMemcpy(b->d_pitems, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
+            BCK(cudaMemcpy(b->d_pnxy, nxy.data(), sizeof(int2) * nxy.size(), cudaMemcpyHostToDevice));
+            BCK(cudaFuncSetAttribute(k_batch_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+            int occ = 0;
+            BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch_persist, 256, smem));
+            if (occ < 1) return bfail(b, GOPF_ERR_UNSUPPORTED, "the persistent batch kernel does not fit an SM");
+            b->pgrid = nsm * occ;
+            b->pmode = 1;
+        }
+    }
     const size_t nbranch = std::max(b->xl.size(), b->yl.size());
     while (b->side.size() + 1 < nbranch) {
         cudaStream_t st;
@@ -583,6 +844,17 @@ template <typename R> static cudaError_t batch_chains(gopf_batch *b, int nsteps)
 
 template <typename R> static cudaError_t batch_enqueue(gopf_batch *b, int nsteps)
 {
+    if (b->pmode) {
+        if constexpr (sizeof(R) == 4) {
+            cudaError_t e = cudaMemsetAsync(b->d_pctr, 0, b->pctr_bytes, b->stream);
+            if (e != cudaSuccess) return e;
+            k_batch_persist<<<b->pgrid, 256, b->psmem, b->stream>>>((const BatchInst<float> *)b->d_inst, b->d_pitems,
+                                                                   b->pnper, nsteps, b->d_pnxy, b->d_pctr,
+                                                                   b->d_pstatus);
+            return cudaGetLastError();
+        }
+        return cudaErrorNotSupported;
+    }
     if (!b->chain.empty()) return batch_chains<R>(b, nsteps);
     cudaError_t e;
     for (int s = 0; s < nsteps; ++s) {
@@ -641,6 +913,9 @@ static int batch_init(gopf_batch *b, gopf_ctx *const *ctxs, int n)
     e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return bfail(b, GOPF_ERR_CUDA, cudaGetErrorString(e));
     b->stream = b->own_stream;
+    e = cudaMalloc(&b->d_pstatus, 4 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(b->d_pstatus, 0, 4 * sizeof(unsigned));
+    if (e != cudaSuccess) return bfail(b, GOPF_ERR_CUDA, cudaGetErrorString(e));
     // the contexts' own streams may still hold work
     for (gopf_ctx *c : b->ctx) cudaStreamSynchronize(c->stream);
     return GOPF_OK;
@@ -671,6 +946,13 @@ static void batch_release(gopf_batch *b)
         if (h.d_off) cudaFree(h.d_off);
     }
     b->hchain.clear();
+    if (b->d_pitems) cudaFree(b->d_pitems);
+    if (b->d_pnxy) cudaFree(b->d_pnxy);
+    if (b->d_pctr) cudaFree(b->d_pctr);
+    b->d_pitems = nullptr;
+    b->d_pnxy = nullptr;
+    b->d_pctr = nullptr;
+    b->pmode = 0;
 }
 
 static int batch_rebuild(gopf_batch *b)
@@ -698,6 +980,7 @@ extern "C" int gopf_batch_destroy(gopf_batch *b)
     for (cudaStream_t st : b->side) cudaStreamDestroy(st);
     for (cudaEvent_t e : b->ev) cudaEventDestroy(e);
     if (b->own_stream) cudaStreamDestroy(b->own_stream);
+    if (b->d_pstatus) cudaFree(b->d_pstatus);
     delete b;
     return GOPF_OK;
 }
@@ -753,6 +1036,7 @@ int time_choice(gopf_batch *parent, const std::vector<gopf_ctx *> &cs, const Bat
     for (cudaStream_t st : t.side) cudaStreamDestroy(st);
     for (cudaEvent_t e : t.ev) cudaEventDestroy(e);
     if (t.own_stream) cudaStreamDestroy(t.own_stream);
+    if (t.d_pstatus) cudaFree(t.d_pstatus);
     return rc;
 }
 
@@ -797,6 +1081,8 @@ extern "C" int gopf_batch_tune(gopf_batch *b, int reps)
     if (reps < 1) reps = 5;
     BCK(cudaSetDevice(b->device));
     BCK(cudaStreamSynchronize(b->stream));
+    // the persistent kernel's kinds are fixed (line engine 256 ... 1024, compile-time Stockham 128)
+    if (b->pmode) return GOPF_OK;
     std::map<TuneKey, std::vector<int>> groups;
     for (size_t i = 0; i < b->ctx.size(); ++i) groups[tune_key(b->ctx[i])].push_back((int)i);
     for (auto &kv : groups) {
@@ -921,12 +1207,56 @@ extern "C" int gopf_batch_step(gopf_batch *b, long long nsteps)
     for (gopf_ctx *c : b->ctx) c->step += nsteps;
     // later calls on the contexts' own streams must see the batch's work
     BCK(cudaStreamSynchronize(b->stream));
+    if (b->pmode) {
+        unsigned flags = 0;
+        BCK(cudaMemcpy(&flags, b->d_pstatus, sizeof(unsigned), cudaMemcpyDeviceToHost));
+        if (flags) {
+            BCK(cudaMemset(b->d_pstatus, 0, sizeof(unsigned)));
+            return bfail(b, GOPF_ERR_TIMEOUT, "a persistent batch item's wait for the items it depends on ran out; "
+                                              "the fields are not valid (upload them again)");
+        }
+    }
     return GOPF_OK;
 }
 
 extern "C" int gopf_batch_kernels_per_step(gopf_batch *b, int *n)
 {
     if (!b || !n) return GOPF_ERR_ARG;
-    *n = b->chain.empty() ? (int)(b->xl.size() + b->yl.size()) + 1 : 3 * (int)b->chain.size();
+    *n = b->pmode ? 1 : b->chain.empty() ? (int)(b->xl.size() + b->yl.size()) + 1 : 3 * (int)b->chain.size();
+    return GOPF_OK;
+}
+
+extern "C" int gopf_batch_set_mode(gopf_batch *b, int mode)
+{
+    if (!b) return GOPF_ERR_ARG;
+    if (mode < GOPF_BATCH_MODE_AUTO || mode > GOPF_BATCH_MODE_PERSISTENT)
+        return bfail(b, GOPF_ERR_ARG, "unknown batch mode");
+    BCK(cudaSetDevice(b->device));
+    const int old = b->mode;
+    b->mode = mode;
+    const int rc = batch_rebuild(b);
+    if (rc && mode == GOPF_BATCH_MODE_PERSISTENT) {
+        // keep the batch usable in the mode it had
+        const std::string msg = b->err;
+        b->mode = old;
+        if (batch_rebuild(b) == GOPF_OK) b->err = msg;
+    }
+    return rc;
+}
+
+extern "C" int gopf_batch_mode(gopf_batch *b, int *mode)
+{
+    if (!b || !mode) return GOPF_ERR_ARG;
+    *mode = b->pmode ? GOPF_BATCH_MODE_PERSISTENT : GOPF_BATCH_MODE_CHAINS;
+    return GOPF_OK;
+}
+
+extern "C" int gopf_batch_set_wait_limit(gopf_batch *b, long long ns)
+{
+    if (!b || ns < 0) return GOPF_ERR_ARG;
+    BCK(cudaSetDevice(b->device));
+    BCK(cudaStreamSynchronize(b->stream));
+    const unsigned long long v = (unsigned long long)ns;
+    BCK(cudaMemcpy(b->d_pstatus + 2, &v, sizeof(v), cudaMemcpyHostToDevice));
     return GOPF_OK;
 }

@@ -12,7 +12,9 @@
 
 namespace gopf {
 
-enum DeviceStatusBits : unsigned { DS_TMA_TIMEOUT = 1u };
+// DS_TMA_TIMEOUT: a tile copy's wait ran out; DS_DEP_TIMEOUT: a persistent kernel's wait for the
+// items an item depends on ran out
+enum DeviceStatusBits : unsigned { DS_TMA_TIMEOUT = 1u, DS_DEP_TIMEOUT = 2u };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 

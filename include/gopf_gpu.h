@@ -326,13 +326,16 @@ int gopf_adjoint_release(gopf_ctx *ctx);
  * sweep database serves, README.md:21-33, pf/database.go:67-80); it has no
  * single counterpart in the reference.  Every context keeps its own model,
  * dt and device state; gopf_batch_step(nsteps) advances all of them by
- * nsteps Euler steps: per step one x-pass and one y-pass launch for each size
- * class present and the projection of the self-conjugate lines, captured in a
- * CUDA graph.  When the x and y classes cover the same instances each class
- * runs its x, y and projection launches on its own branch for all steps of a
- * graph (3 launches per class and step); otherwise the classes of a pass run
- * side by side and one projection of every instance ends each step
- * (2 x classes + 1).  gopf_batch_kernels_per_step reports the count.
+ * nsteps Euler steps, captured in CUDA graphs of 1 and 16 steps.  By default
+ * one persistent kernel per graph steps every instance (gopf_batch_set_mode
+ * below).  Otherwise each size class gets an x-pass and a y-pass launch per
+ * step, plus the projection of the self-conjugate lines.  When the x and y
+ * classes cover the same instances each class runs its x, y and projection
+ * launches on its own branch for all steps of a graph (3 launches per class
+ * and step).  Otherwise the classes of a pass run side by side and one
+ * projection of every instance ends each step (2 x classes + 1).
+ * gopf_batch_kernels_per_step reports the launches per step (1 when
+ * persistent).
  * Contexts must be 2D, single-field, Euler, without user-defined terms, on one
  * device and precision, and stay alive while the batch exists. */
 typedef struct gopf_batch gopf_batch;
@@ -363,6 +366,23 @@ int gopf_batch_tune_reset(void);
 int gopf_batch_force(gopf_batch *batch, int xfam, int yfam, int lbx, int lby, int xplan, int yplan);
 /* The choice in effect for instance inst: {xfam, yfam, lbx, lby, xplan, yplan}. */
 int gopf_batch_choice(gopf_batch *batch, int inst, int *out6);
+/* How a batch steps (no counterpart in the reference).
+ * GOPF_BATCH_MODE_PERSISTENT: one persistent kernel steps every instance for all the steps of a
+ * captured graph (1 or 16 steps per launch). Its blocks take x and y tiles of all instances from
+ * one queue; per-instance completion counters order an instance's y tiles after its x tiles and its
+ * next x tiles after its y tiles. Each wait is bounded, and one that runs out makes
+ * gopf_batch_step return GOPF_ERR_TIMEOUT. It takes FP32 instances of sides 256 ... 1024 with one
+ * dense polynomial group (line engine) and of side 128 (compile-time Stockham tiles). The kernel
+ * families are then fixed, so gopf_batch_tune keeps them.
+ * GOPF_BATCH_MODE_CHAINS: a launch per class and pass, with the classes as graph branches.
+ * GOPF_BATCH_MODE_AUTO (default): persistent when every instance allows it, else chains. */
+enum { GOPF_BATCH_MODE_AUTO = -1, GOPF_BATCH_MODE_CHAINS = 0, GOPF_BATCH_MODE_PERSISTENT = 1 };
+int gopf_batch_set_mode(gopf_batch *batch, int mode);
+/* The mode in effect: GOPF_BATCH_MODE_CHAINS or GOPF_BATCH_MODE_PERSISTENT. */
+int gopf_batch_mode(gopf_batch *batch, int *mode);
+/* Limit (ns) of the persistent kernel's waits for an item's dependencies; 0 (default) = 2 s. Meant for
+ * testing the timeout path. */
+int gopf_batch_set_wait_limit(gopf_batch *batch, long long ns);
 
 /* ---- sweeps over several GPUs, one process each ----
  * The sweep workflow (README.md:21-33) runs one pf.Solver per parameter set; its instances are

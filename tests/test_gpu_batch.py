@@ -120,6 +120,7 @@ def test_batch_size_classes_equal_generic_contexts():
         a_models.append(ch_ctx(side, "fp32", 0.4 + 0.1 * i, 1.0, 0.05, c0, fast=False))
         b_models.append(ch_ctx(side, "fp32", 0.4 + 0.1 * i, 1.0, 0.05, c0, fast=False))
     batch = G.Batch(a_models)
+    batch.set_mode(G._lib.BATCH_MODE_CHAINS)
     assert batch.kernels_per_step() == 3 * 6
     for n in (12, 20):
         batch.step(n)
@@ -223,6 +224,7 @@ def test_autotuner_picks_valid_choices_and_keeps_fields():
     ms = _tune_models("fp32", sides)
     before = [m.download_real(0) for m in ms]
     b = G.Batch(ms)
+    b.set_mode(L.BATCH_MODE_CHAINS)  # the persistent kernel's families are fixed
     b.tune(3)
     for m, x in zip(ms, before):
         assert np.array_equal(m.download_real(0), x)  # tuning left the fields alone
@@ -242,6 +244,7 @@ def test_autotuner_picks_valid_choices_and_keeps_fields():
     for i, s in enumerate(sides):
         m2 = ch_ctx(s, "fp32", 0.4 + 0.1 * i, 1.0 + 0.05 * i, 0.05, uniform_field(4000 + i, s * s, 0.5, 0.05))
         b2 = G.Batch([m2])
+        b2.set_mode(L.BATCH_MODE_CHAINS)
         c = choices[i]
         b2.force(c["xfam"], c["yfam"], c["lbx"], c["lby"], c["xplan"], c["yplan"])
         b2.step(10)
@@ -249,5 +252,85 @@ def test_autotuner_picks_valid_choices_and_keeps_fields():
     # cached: a new batch of the same kinds gets the same choices
     ms3 = _tune_models("fp32", sides)
     b3 = G.Batch(ms3)
+    b3.set_mode(L.BATCH_MODE_CHAINS)
     b3.tune(3)
     assert [b3.choice(i) for i in range(len(sides))] == choices
+    # the persistent mode keeps its fixed families: line engine for 256 ... 1024, compile-time
+    # Stockham for 128
+    ms4 = _tune_models("fp32", sides)
+    b4 = G.Batch(ms4)
+    assert b4.mode() == L.BATCH_MODE_PERSISTENT
+    b4.tune(3)
+    for s, i in zip(sides, range(len(sides))):
+        fam = L.BATCH_STOCKHAM_CT if s == 128 else L.BATCH_LINE
+        assert b4.choice(i)["xfam"] == fam and b4.choice(i)["yfam"] == fam
+
+
+# ---------------------------------------------------------------- the persistent mode
+
+def test_persistent_mode_equals_chains():
+    """The persistent kernel (one launch per captured graph; x and y tiles of every instance from one
+    queue; per-instance completion counters; the projection of the self-conjugate lines inside the y
+    tiles) steps exactly what the per-class chains step: bitwise after 1, 17 and 38 steps (1-step and
+    16-step graphs), sides 128 ... 1024 (256-thread tiles and the 192-thread tiles of 384 and 768)."""
+    import gopf_gb300 as G
+    from gopf_gb300 import _lib as L
+
+    sides = [1024, 768, 512, 384, 256, 128, 256, 768]
+    a = _tune_models("fp32", sides, seed0=5000)
+    b = _tune_models("fp32", sides, seed0=5000)
+    ba, bb = G.Batch(a), G.Batch(b)
+    bb.set_mode(L.BATCH_MODE_CHAINS)
+    assert ba.mode() == L.BATCH_MODE_PERSISTENT and bb.mode() == L.BATCH_MODE_CHAINS
+    assert ba.kernels_per_step() == 1 and ba.launches(38) == 2 + 6
+    for n in (1, 16, 21):
+        ba.step(n)
+        bb.step(n)
+        for x, y in zip(a, b):
+            assert np.array_equal(x.download(0), y.download(0))
+
+
+def test_persistent_mode_rejects_what_it_cannot_step():
+    """FP64 instances and sides outside 128 ... 1024 stay on the chains: AUTO falls back, PERSISTENT
+    is refused with GOPF_ERR_UNSUPPORTED and leaves the batch stepping in its previous mode."""
+    import gopf_gb300 as G
+    from gopf_gb300 import _lib as L
+
+    for prec, sides in (("fp64", [256]), ("fp32", [256, 96])):
+        ms = _tune_models(prec, sides)
+        b = G.Batch(ms)
+        assert b.mode() == L.BATCH_MODE_CHAINS
+        with pytest.raises(G.GopfError) as e:
+            b.set_mode(L.BATCH_MODE_PERSISTENT)
+        assert e.value.status == 6
+        assert b.mode() == L.BATCH_MODE_CHAINS
+        b.step(2)
+        ref = _tune_models(prec, sides)
+        G.Batch(ref).step(2)
+        for x, y in zip(ms, ref):
+            assert np.array_equal(x.download(0), y.download(0))
+
+
+def test_persistent_wait_timeout_is_reported():
+    """A dependency-wait limit of 1 ns makes the y tiles of a lone 256^2 instance give up waiting for
+    its x tiles: gopf_batch_step reports GOPF_ERR_TIMEOUT.  With the limit restored and the field
+    uploaded again the batch steps like a fresh one."""
+    import gopf_gb300 as G
+    from gopf_gb300 import _lib as L
+    from gopf_gb300.synthetic import uniform_field
+
+    c0 = uniform_field(77, 256 * 256, 0.5, 0.05)
+    m = ch_ctx(256, "fp32", 0.5, 1.0, 0.05, c0)
+    b = G.Batch([m])
+    assert b.mode() == L.BATCH_MODE_PERSISTENT
+    b.set_wait_limit_ns(1)
+    with pytest.raises(G.GopfError) as e:
+        b.step(1)
+    assert e.value.status == 5
+    b.set_wait_limit_ns(0)
+    m.upload(0, c0)
+    b.step(3)
+    f = ch_ctx(256, "fp32", 0.5, 1.0, 0.05, c0)
+    fb = G.Batch([f])
+    fb.step(3)
+    assert np.array_equal(m.download(0), f.download(0))
