@@ -218,6 +218,8 @@ def run_gpu(args):
         m.set_option(G._lib.OPT_X_ROWS, args.x_rows)
     if args.z_lines is not None:
         m.set_option(G._lib.OPT_Z_LINES, args.z_lines)
+    if args.pdl is not None:
+        m.set_option(G._lib.OPT_PDL, args.pdl)
     mass0 = m.mass(0)
     m.prepare_graphs(args.steps)  # capture the graphs the timed steps replay (no stepping)
     m.step(warmup_steps(args))
@@ -862,6 +864,8 @@ def main():
                     help="lines per tile of the 256-point z pass (the library's default when omitted)")
     ap.add_argument("--tma", type=int, default=None, choices=[0, 1],
                     help="tile movement of the 256-point kernels: 0 plain loads, 1 TMA")
+    ap.add_argument("--pdl", type=int, default=None, choices=[0, 1],
+                    help="programmatic dependent launches in the 3D step (the library's default when omitted)")
     ap.add_argument("--no-tune", action="store_true", help="sweep: keep the built-in kernel choices")
     ap.add_argument("--batch-mode", default="auto", choices=["auto", "persistent", "chains"],
                     help="sweep: one persistent kernel per captured graph, or a launch per class and pass")

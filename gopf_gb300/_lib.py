@@ -28,6 +28,7 @@ RED_SUM, RED_SUMSQ, RED_MIN, RED_MAX, RED_NONFINITE = range(5)
 OPT_CHECK_FINITE, OPT_USE_GRAPHS, OPT_FAST_KERNELS, OPT_TMA, OPT_DIRECT_HOST = 0, 1, 2, 3, 5
 OPT_WAIT_LIMIT_NS = 6
 OPT_X_ROWS = 7
+OPT_PDL = 9
 OPT_Z_LINES = 8
 MAX_FACTORS = 8
 BATCH_AUTO, BATCH_LINE, BATCH_STOCKHAM_CT, BATCH_STOCKHAM = -1, 0, 1, 2

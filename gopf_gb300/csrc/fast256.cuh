@@ -79,6 +79,12 @@ template <bool INV> __device__ __forceinline__ void pdft16(float2 (&v)[16])
 // at(a, b) is the shared-memory slot of element (a, b) of this thread's line.
 // WARP: the 16 threads of every line are one half-warp and its slots are its
 // own, so the exchange only has to be ordered within the warp.
+// Programmatic dependent launch.  pdl_trigger lets the next kernel of the stream be scheduled once
+// every block of this one has started; pdl_wait (before a thread's first access to data an earlier
+// kernel produced or still reads) returns once the previous kernel has completed and its writes are
+// visible.  Both do nothing in a kernel that was not launched as a programmatic dependent.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void xsync(bool warp)
 {
     if (warp) __syncwarp();
@@ -419,10 +425,15 @@ __global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_y256(const PassArgs<flo
     const bool fused = (a.mode == PM_FUSED || a.mode == PM_INIT);
     float2 *__restrict__ buf = fused ? a.buf[0] : a.buf[blockIdx.y];
     const float2 zero = make_float2(0.f, 0.f);
+    const bool pdl = (a.allow_fast & ALLOW_PDL) != 0;
+    pdl_trigger();
 
+    // a programmatic dependent sets up its tables while the previous kernel finishes, then waits
+    // for its data; otherwise the line is requested first, so that its latency hides behind the tables
     float2 v[16];
+    if (!pdl)
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = valid ? buf[q * N + r + 16 * i] : zero;
+        for (int i = 0; i < 16; ++i) v[i] = valid ? buf[q * N + r + 16 * i] : zero;
     load_twiddles(s_tw, a.tw);
     if (fused) {
         if (threadIdx.x < 16) {
@@ -436,6 +447,11 @@ __global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2) k_y256(const PassArgs<flo
             s_fl[threadIdx.x] = f2;
         }
         s_fy[threadIdx.x] = fsqf(threadIdx.x, g.Y);
+    }
+    if (pdl) {
+        pdl_wait();
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = valid ? buf[q * N + r + 16 * i] : zero;
     }
     __syncthreads();
     auto at = [&](int x, int y) -> float2 & { return s_x[l * N + x * 16 + ((x + y) & 15)]; };
@@ -891,18 +907,25 @@ __global__ void __launch_bounds__(ZH_NT, 6)
     const int i0 = blockIdx.x * ZH_LINES;
     const bool init = (a.mode == PM_INIT);
     const int ngrp = (a.upd.ngrp > 0 ? 1 : 0);
+    const bool pdl = (a.allow_fast & ALLOW_PDL) != 0;
+    pdl_trigger();
 
     if (tid == 0) {
         mbar_init(bar, 1);
         fence_mbar_init();
     }
     __syncthreads();
-    if (tid == 0) {
-        const uint32_t bytes = (uint32_t)ZH_TILE_BYTES * (1u + (init ? 0u : 1u));
-        mbar_arrive_expect_tx(bar, bytes);
-        tma_load_2d(tU0, &mU0, i0, 0, bar);
-        if (!init) tma_load_2d(tS, &mS, i0, 0, bar);
-    }
+    // the tiles are requested first, unless the launch is a programmatic dependent: then the
+    // tables are set up while the previous kernel finishes, and the tiles requested after its end
+    auto request = [&]() {
+        if (tid == 0) {
+            const uint32_t bytes = (uint32_t)ZH_TILE_BYTES * (1u + (init ? 0u : 1u));
+            mbar_arrive_expect_tx(bar, bytes);
+            tma_load_2d(tU0, &mU0, i0, 0, bar);
+            if (!init) tma_load_2d(tS, &mS, i0, 0, bar);
+        }
+    };
+    if (!pdl) request();
     for (int t = tid; t < N; t += ZH_NT) {
         s_tw[t] = a.tw[(t & 15) * (t >> 4)];
         s_fz[t] = fsqf(t, g.Z);
@@ -912,6 +935,10 @@ __global__ void __launch_bounds__(ZH_NT, 6)
         const int kx = q / g.Y, y = q - kx * g.Y;
         const float fx = (float)kx / (float)g.X;
         s_fl[tid] = fx * fx + fsqf(y, g.Y);
+    }
+    if (pdl) {
+        pdl_wait(); // every thread: the stores below touch T and c-hat
+        request();
     }
     if (tid == 0) *s_ok = tma_wait_or_flag(bar, 0, a.status) ? 1 : 0;
     __syncthreads();
@@ -999,6 +1026,7 @@ static __global__ void __launch_bounds__(XH_NT, 8) k_x256_th(const XPassArgs<flo
     const int j = tid & 7, r = tid >> 3;
     const int y0 = blockIdx.x * XH_ROWS;
     const int z = blockIdx.y;
+    pdl_trigger(); // the y pass may be scheduled as soon as every x block runs
     if (tid == 0) {
         mbar_init(bar, 1);
         fence_mbar_init();

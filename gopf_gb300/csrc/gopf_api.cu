@@ -424,6 +424,8 @@ extern "C" int gopf_set_option(gopf_ctx *ctx, int opt, long long v)
     else if (opt == GOPF_OPT_Z_LINES) {
         if (v != 8 && v != 16) return gopf_fail(ctx, GOPF_ERR_ARG, "the z tile width is 8 or 16 lines");
         ctx->z_lines = (int)v;
+    } else if (opt == GOPF_OPT_PDL) {
+        ctx->use_pdl = (int)(v != 0);
     } else if (opt == GOPF_OPT_X_ROWS) {
         if (v != 16 && v != 32) return gopf_fail(ctx, GOPF_ERR_ARG, "the x tile height is 16 or 32 rows");
         ctx->x_rows = (int)v;
@@ -1317,6 +1319,9 @@ template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx)
         u.gscale[G] = nullptr;
     }
     const bool is3d = ctx->g.Z > 1;
+    // the y, z and y launches of the plain 3D step as programmatic dependents of the kernel before
+    // them (not under per-kernel profiling, which records events between the kernels)
+    const int pdl = (ctx->use_pdl && !ctx->prof_events) ? ALLOW_PDL : 0;
     if (GE > 0) {
         XPassArgs<R> xa = xargs<R>(ctx);
         xa.in_mode = XIN_SPECTRAL;
@@ -1376,11 +1381,13 @@ template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx)
         pa.mode = PM_FWD;
         for (int b = 0; b < GE; ++b) pa.buf[b] = U[b];
         pa.nbuf = GE;
+        pa.allow_fast |= pdl;
         LK(launch_cpass<R>(pa, ctx->LBy, ctx->stream));
     }
     // with no explicit term the last pass reads c-hat only (identity contribution when ngrp == 0)
     const int nb = std::max(GE, 1);
     PassArgs<R> fa = pargs<R>(ctx, is3d);
+    if (is3d && !el && GE > 0) fa.allow_fast |= pdl; // after the forward y pass
     fa.mode = PM_FUSED;
     for (int b = 0; b < nb; ++b) fa.buf[b] = U[b];
     fa.nbuf = nb;
@@ -1404,6 +1411,7 @@ template <typename R> static cudaError_t enqueue_euler(gopf_ctx *ctx)
         ia.mode = PM_INV;
         ia.buf[0] = T;
         ia.nbuf = 1;
+        ia.allow_fast |= pdl;
         LK(launch_cpass<R>(ia, ctx->LBy, ctx->stream));
     }
     if (fork) LK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));

@@ -199,6 +199,7 @@ struct gopf_ctx {
     int use_tma = 1;
     int x_rows = 16; // tile height of the one-group 256-point x pass (GOPF_OPT_X_ROWS)
     int z_lines = 8;  // tile width of the one-group 256-point z pass (GOPF_OPT_Z_LINES)
+    int use_pdl = 1;  // the step's y, z and y passes as programmatic dependents (GOPF_OPT_PDL)
     int use_direct_host = 1;
 
     // ImplicitEuler's Newton-Krylov controls (DefaultNonLinSolver, pf/implicitEuler.go:221-228) and

@@ -207,6 +207,10 @@ enum XProgram { XP_POLY = 0, XP_ELASTIC_Q = 1, XP_MULTI = 2, XP_ADJ = 3 };
 // PM_ELASTIC_K: forward transform buf[0], multiply by bsym(k)/N, inverse transform in place
 enum PassMode { PM_FWD = 0, PM_INV = 1, PM_FUSED = 2, PM_INIT = 3, PM_ELASTIC_K = 4 };
 
+// bit of PassArgs::allow_fast: the launch is a programmatic dependent of the stream's previous
+// kernel (the 256-point y and z kernels then set up their tables before waiting for its data)
+constexpr int ALLOW_PDL = 64;
+
 template <typename R> struct PassArgs {
     typedef typename VecOf<R>::type V;
     Geom g;

@@ -2,6 +2,7 @@
 // register-resident 256-point kernels serving the launches they cover.
 #include <algorithm>
 #include <mutex>
+#include <utility>
 
 #include "fast256.cuh"
 #include "fastline.cuh"
@@ -10,6 +11,25 @@
 #include "x256_io.cuh"
 
 namespace gopf {
+
+// Launch k with the programmatic-serialization attribute when pdl is set: the kernel may start while
+// the stream's previous kernel finishes (it waits for that kernel's data with griddepcontrol.wait).
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_k(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool pdl,
+                            Args &&...args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
 
 // [Z][S] view of a z-pass array with lines x 256 boxes
 static bool z_map(CUtensorMap *m, const float2 *p, const Geom &g, int lines = 16)
@@ -111,9 +131,9 @@ static bool launch_z_tma(const PassArgs<float> &a, cudaStream_t st, cudaError_t 
             !z_map(&mT, a.tout, a.g, f256::ZH_LINES) || !z_map(&mS, a.state, a.g, f256::ZH_LINES))
             return false;
         const unsigned gh = (unsigned)(a.g.S / f256::ZH_LINES);
-        if (nz) f256::k_z256_th<true><<<gh, f256::ZH_NT, f256::z256_th_smem_bytes(), st>>>(a, mU0, mS, mT);
-        else f256::k_z256_th<false><<<gh, f256::ZH_NT, f256::z256_th_smem_bytes(), st>>>(a, mU0, mS, mT);
-        *err = cudaGetLastError();
+        const bool pdl = (a.allow_fast & ALLOW_PDL) != 0;
+        *err = launch_k(nz ? f256::k_z256_th<true> : f256::k_z256_th<false>, dim3(gh), dim3(f256::ZH_NT),
+                        f256::z256_th_smem_bytes(), st, pdl, a, mU0, mS, mT);
         return true;
     }
     if (!z_map(&mU0, a.buf[0], a.g) || !z_map(&mT, a.tout, a.g) || !z_map(&mS, a.state, a.g)) return false;
@@ -360,14 +380,10 @@ template <> cudaError_t launch_cpass<float>(const PassArgs<float> &a, int LB, cu
         const bool fused = (a.mode == PM_FUSED || a.mode == PM_INIT);
         dim3 grid((unsigned)((nlines + 15) / 16), fused ? 1 : a.nbuf);
         const bool nz = fused && (a.upd.noise.kind != 0 || a.upd.filt != nullptr);
-        if (fused && a.nbuf > 1) {
-            if (nz) f256::k_y256<2, true><<<grid, f256::NT, 0, st>>>(a);
-            else f256::k_y256<2, false><<<grid, f256::NT, 0, st>>>(a);
-        } else {
-            if (nz) f256::k_y256<1, true><<<grid, f256::NT, 0, st>>>(a);
-            else f256::k_y256<1, false><<<grid, f256::NT, 0, st>>>(a);
-        }
-        return cudaGetLastError();
+        const bool pdl = (a.allow_fast & ALLOW_PDL) != 0;
+        if (fused && a.nbuf > 1)
+            return launch_k(nz ? f256::k_y256<2, true> : f256::k_y256<2, false>, grid, dim3(f256::NT), 0, st, pdl, a);
+        return launch_k(nz ? f256::k_y256<1, true> : f256::k_y256<1, false>, grid, dim3(f256::NT), 0, st, pdl, a);
     }
     {
         cudaError_t e;

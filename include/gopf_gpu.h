@@ -108,9 +108,13 @@ enum {
     GOPF_OPT_X_ROWS = 7,        /* rows per tile of the 256-column x pass with one dense polynomial group:
                                   16 (default: 128 threads, eight blocks per SM) or 32 (256 threads,
                                   four blocks per SM); both compute the same values */
-    GOPF_OPT_Z_LINES = 8        /* lines per tile of the 256-point z pass with one explicit group: 8
+    GOPF_OPT_Z_LINES = 8,       /* lines per tile of the 256-point z pass with one explicit group: 8
                                   (default: 128 threads, six blocks per SM) or 16 (256 threads, three
                                   blocks per SM); both compute the same values */
+    GOPF_OPT_PDL = 9            /* 1 (default): in the 3D Euler step the forward y, fused z and inverse y
+                                  256-point kernels launch as programmatic dependents of the kernel
+                                  before them, setting up their tables while it finishes; 0: plain
+                                  stream order.  The same values either way */
 };
 
 #define GOPF_MAX_FACTORS 8

@@ -352,6 +352,31 @@ def test_half_height_x_tiles_match():
         assert np.array_equal(out[0], out[1])
 
 
+def test_programmatic_dependent_launches_match():
+    """The 3D step with its forward y, fused z and inverse y kernels launched as programmatic
+    dependents (tables set up while the previous kernel finishes, data read after griddepcontrol.wait)
+    steps exactly what plain stream order steps: bitwise after 1 and 21 steps (the 1-step and 16-step
+    graphs), 256^3 FP32; and eagerly (no graphs) after 3 steps."""
+    import gopf_gb300 as G
+    from gopf_gb300.synthetic import uniform_field
+
+    c0 = uniform_field(10, 256 ** 3, 0.0, 0.1)
+    a = ch_gpu([256, 256, 256], "fp32", 0.5, 0.05, c0)
+    b = ch_gpu([256, 256, 256], "fp32", 0.5, 0.05, c0)
+    b.set_option(G._lib.OPT_PDL, 0)
+    for n in (1, 20):
+        a.step(n)
+        b.step(n)
+        assert np.array_equal(a.download_real(0), b.download_real(0))
+    a.set_option(G._lib.OPT_USE_GRAPHS, 0)
+    b.set_option(G._lib.OPT_USE_GRAPHS, 0)
+    a.step(3)
+    b.step(3)
+    assert np.array_equal(a.download_real(0), b.download_real(0))
+    a.close()
+    b.close()
+
+
 def test_half_width_z_tiles_match():
     """The one-group 256-point z pass on 8-line tiles (128 threads, six blocks per SM) computes
     exactly what the 16-line tiles do: bitwise equal after 10 steps, 256^3 FP32."""
