@@ -365,6 +365,21 @@ extern "C" int gopf_ctx_create(int ndim, const int *domain_size, int precision, 
     ctx->LBz = lb_for(g.Z, vb);
     if ((long long)ctx->LBx * g.H > 4096 || (long long)ctx->LBy * g.Y > 4096 || (long long)ctx->LBz * g.Z > 4096)
         return gopf_fail(ctx, GOPF_ERR_UNSUPPORTED, "axis longer than 1024 (2048 columns) is not supported");
+    // Small grids: narrower tiles (down to 4 lines), so that each pass of the generic kernels has
+    // about two tiles per SM; a pass of a few tiles otherwise takes as long as one block's
+    // transforms (FP64 arithmetic runs at a small fraction of the FP32 rate).  The tile width does
+    // not change a line's arithmetic.
+    {
+        int nsm = 152;
+        if (device >= 0) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+        auto narrow = [&](int lb, long long lines) {
+            while (lb > 4 && (lines + lb - 1) / lb < 2LL * nsm) lb /= 2;
+            return lb;
+        };
+        ctx->LBx = narrow(ctx->LBx, (long long)g.Y * g.Z);
+        ctx->LBy = narrow(ctx->LBy, (long long)g.KX * g.Z);
+        if (g.Z > 1) ctx->LBz = narrow(ctx->LBz, g.S);
+    }
     if (oddx) gopf_make_plan(g.X, 1, 0, ctx->planH); // the x transform of the row pairs
     else gopf_make_plan(g.H, 2, 0, ctx->planH);
     gopf_make_plan(g.Y, 1, 0, ctx->planY);

@@ -545,13 +545,16 @@ template <typename R> static int batch_build(gopf_batch *b)
         pa.upd = c->upd;
         pa.upd.dt = c->dt;
         pa.upd.invN = 1.0 / (double)g.N;
-        bi.lbx = c->LBx;
-        bi.lby = c->LBy;
+        // the batch's own default tile widths (a context narrows its tiles for its own small passes,
+        // a batch's passes are wide)
+        const bool oddx = (g.X & 1) != 0;
+        bi.lbx = lb_for(oddx ? g.KX : g.H, vb);
+        bi.lby = lb_for(g.Y, vb);
         int xc = 0, yc = 0, fx = -1, fy = -1;
         if (sizeof(R) == 4) {
             for (int k = 1; k < 7; ++k) {
-                if (g.H == XCLS_H[k] && c->LBx == XCLS_LB[k] && !(g.X & 1)) xc = k;
-                if (g.Y == YCLS_N[k] && c->LBy == YCLS_LB[k]) yc = k;
+                if (g.H == XCLS_H[k] && bi.lbx == XCLS_LB[k] && !(g.X & 1)) xc = k;
+                if (g.Y == YCLS_N[k] && bi.lby == YCLS_LB[k]) yc = k;
             }
             for (int k = 0; k < 5; ++k) {
                 if (g.X == FL_L[k] && g.Y % (2 * FL_LPB[k]) == 0) fx = k;
