@@ -141,7 +141,8 @@ def test_cahn_hilliard_fp32_parity(oracle, dims, steps, gamma, dt, center, hw):
 
 
 def test_explicit_linear_splitting_matches_oracle(oracle):
-    """The spec splitting mu = c^3 - c explicit, -gamma k^4 implicit, via a registered polynomial."""
+    """The splitting mu = c^3 - c explicit, -gamma k^4 implicit (c_k <- (c_k - dt M k^2 mu_k) /
+    (1 + dt M gamma k^4)), via a registered polynomial."""
     import gopf_gb300 as G
     from gopf_gb300.synthetic import uniform_field
 
