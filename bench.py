@@ -687,6 +687,8 @@ def run_elastic(args):
     c0 = uniform_field(3, n, 0.3, 0.02)
     m = G.Model([256] * 3, "fp32", device=0)
     m.set_option(G._lib.OPT_CHECK_FINITE, 0)
+    if args.pdl is not None:
+        m.set_option(G._lib.OPT_PDL, args.pdl)
     m.add_field("conc")
     m.add_scalar("gamma", 1.0)
     m.add_scalar("m1", -1.0)

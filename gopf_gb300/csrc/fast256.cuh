@@ -306,6 +306,7 @@ __global__ void __launch_bounds__(NT, NG == 1 ? 3 : 2)
     k_z256_tma(const PassArgs<float> a, const __grid_constant__ CUtensorMap mU0, const __grid_constant__ CUtensorMap mU1,
                const __grid_constant__ CUtensorMap mS, const __grid_constant__ CUtensorMap mT)
 {
+    pdl_trigger(); // the inverse y pass may be scheduled as soon as every block runs
     extern __shared__ unsigned char z_dsm[];
     unsigned char *base = z_dsm + ((128u - (smem_u32(z_dsm) & 127u)) & 127u);
     float2 *tU0 = reinterpret_cast<float2 *>(base);
@@ -752,6 +753,7 @@ __global__ void __launch_bounds__(NT, 3)
                const __grid_constant__ CUtensorMap mO1, const __grid_constant__ CUtensorMap mO2,
                const __grid_constant__ CUtensorMap mO3)
 {
+    pdl_trigger(); // the forward y pass may be scheduled as soon as every block runs
     extern __shared__ unsigned char x_dsm[];
     unsigned char *base = x_dsm + ((128u - (smem_u32(x_dsm) & 127u)) & 127u);
     float2 *s_x = reinterpret_cast<float2 *>(base);                        // input tile, then exchange slots
