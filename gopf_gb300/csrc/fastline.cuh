@@ -120,24 +120,26 @@ __device__ __forceinline__ float2 shfl2(float2 v, int m)
 // multiply by -i (forward) or +i (inverse)
 template <bool INV> __device__ __forceinline__ float2 mi(float2 a) { return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x); }
 
-// radix-U DFT across the U threads of a column, U = 2 or 4 (forward keeps d, inverse ends in u)
+// a + s b on both lanes with one packed FFMA2: for s = +1 or -1 it rounds exactly as a + b or a - b
+__device__ __forceinline__ float2 addsub(float2 b, float2 s, float2 a) { return __ffma2_rn(b, s, a); }
+__device__ __forceinline__ float2 sign2(bool neg) { return neg ? make_float2(-1.f, -1.f) : make_float2(1.f, 1.f); }
+
+// radix-U DFT across the U threads of a column, U = 2 or 4 (forward keeps d, inverse ends in u).  The
+// thread holding the difference of a butterfly takes o - v, the other v + o, both as v * s + o.
 template <int U, bool INV> __device__ __forceinline__ void xdft_fwd(float2 (&v)[16], int u)
 {
     if constexpr (U == 2) {
+        const float2 s = sign2(u != 0);
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {
-            const float2 o = shfl2(v[c], 8);
-            v[c] = u ? sub2(o, v[c]) : add2(v[c], o);
-        }
+        for (int c = 0; c < 16; ++c) v[c] = addsub(v[c], s, shfl2(v[c], 8));
     } else { // U = 4, u = 2 u1 + u0: first across u1 (lane bit 4), then across u0 (lane bit 3)
         const int u0 = u & 1, u1 = u >> 1;
+        const float2 s0 = sign2(u0 != 0), s1 = sign2(u1 != 0);
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
-            const float2 o = shfl2(v[c], 16);
-            float2 e = u1 ? sub2(o, v[c]) : add2(v[c], o); // E[u0][d0 = u1]
-            if (u0 && u1) e = mi<INV>(e);                   // W_4^(u0 d0)
-            const float2 o2 = shfl2(e, 8);
-            v[c] = u0 ? sub2(o2, e) : add2(e, o2);         // X[d0 + 2 d1], d1 = u0
+            float2 e = addsub(v[c], s1, shfl2(v[c], 16)); // E[u0][d0 = u1]
+            if (u0 && u1) e = mi<INV>(e);                // W_4^(u0 d0)
+            v[c] = addsub(e, s0, shfl2(e, 8));           // X[d0 + 2 d1], d1 = u0
         }
     }
 }
@@ -145,20 +147,17 @@ template <int U, bool INV> __device__ __forceinline__ void xdft_fwd(float2 (&v)[
 template <int U, bool INV> __device__ __forceinline__ void xdft_inv(float2 (&v)[16], int u)
 {
     if constexpr (U == 2) {
+        const float2 s = sign2(u != 0);
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {
-            const float2 o = shfl2(v[c], 8);
-            v[c] = u ? sub2(o, v[c]) : add2(v[c], o);
-        }
+        for (int c = 0; c < 16; ++c) v[c] = addsub(v[c], s, shfl2(v[c], 8));
     } else {
         const int u0 = u & 1, u1 = u >> 1;
+        const float2 s0 = sign2(u0 != 0), s1 = sign2(u1 != 0);
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
-            const float2 o = shfl2(v[c], 8);
-            float2 g = u0 ? sub2(o, v[c]) : add2(v[c], o); // G[d0 = u1][u0]
-            if (u0 && u1) g = mi<INV>(g);                   // conj(W_4^(u0 d0)) on the inverse
-            const float2 o2 = shfl2(g, 16);
-            v[c] = u1 ? sub2(o2, g) : add2(g, o2);
+            float2 g = addsub(v[c], s0, shfl2(v[c], 8)); // G[d0 = u1][u0]
+            if (u0 && u1) g = mi<INV>(g);               // conj(W_4^(u0 d0)) on the inverse
+            v[c] = addsub(g, s1, shfl2(g, 16));
         }
     }
 }
