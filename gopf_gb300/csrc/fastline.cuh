@@ -347,6 +347,50 @@ template <int L, int NG> __device__ __forceinline__ void yline_tile(const PassAr
         if (valid) T[q * L + r + G::T * i] = v[i];
 }
 
+// Forward or inverse (unnormalised) transforms of LPB lines of buf, in place, with no update: the
+// y passes of PM_FWD and PM_INV (L = g.Y, lines q = z KX + kx).  The forward transform leaves a line in
+// the B layout, stored at its natural positions elem(j); the inverse reads those and ends in the A
+// layout.  Shared memory as yline_tile (the frequency table unused).
+template <int L> __device__ __forceinline__ void yline_pass_tile(const PassArgs<float> &a, long long tile, int b, bool inv)
+{
+    typedef Geo<L> G;
+    extern __shared__ __align__(16) unsigned char fl_dsm[];
+    float2 *s_x = reinterpret_cast<float2 *>(fl_dsm);
+    float2 *s_tw = s_x + G::LPB * G::LREG;
+    float2 *s_twr = s_tw + L;
+    const Geom &g = a.g;
+    const int l = threadIdx.x / G::T, r = threadIdx.x - l * G::T;
+    const long long nlines = (long long)g.Z * g.KX;
+    const long long q = tile * G::LPB + l;
+    const bool valid = q < nlines;
+    float2 *z = s_x + l * G::LREG;
+    const float2 zero = make_float2(0.f, 0.f);
+    float2 *__restrict__ buf = a.buf[b];
+    const Role<L> ro(r);
+    float2 v[16];
+    if (!inv) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = valid ? buf[q * L + r + G::T * i] : zero;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = valid ? buf[q * L + ro.elem(j)] : zero;
+    }
+    for (int t = threadIdx.x; t < L; t += G::NT) s_tw[t] = a.tw[t];
+    load_twr<L>(s_twr, a.tw, G::NT);
+    lsync<L>();
+    if (!inv) {
+        line_fwd<L>(v, r, ro, z, s_tw, s_twr);
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            if (valid) buf[q * L + ro.elem(j)] = v[j];
+    } else {
+        line_inv<L>(v, r, ro, z, s_tw, s_twr);
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+            if (valid) buf[q * L + r + G::T * i] = v[i];
+    }
+}
+
 // one shared array holds, in turn, the spectral tile [2 LPB rows][PX], the exchange slots of the
 // LPB lines and the separation slots [LPB][SEP]; then two twiddle tables and the polynomial
 // coefficients

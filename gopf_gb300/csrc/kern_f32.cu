@@ -257,6 +257,10 @@ template <int L, int NG> __global__ void __launch_bounds__(fl::Geo<L>::NT, 3) k_
 {
     fl::yline_tile<L, NG>(a, blockIdx.x);
 }
+template <int L> __global__ void __launch_bounds__(fl::Geo<L>::NT, 3) k_yline_pass(const PassArgs<float> a)
+{
+    fl::yline_pass_tile<L>(a, blockIdx.x, blockIdx.y, a.mode == PM_INV);
+}
 template <int L> __global__ void __launch_bounds__(fl::Geo<L>::NT, 3) k_xline(const XPassArgs<float> a)
 {
     fl::xline_tile<L>(a, blockIdx.x, blockIdx.y);
@@ -304,6 +308,24 @@ template <int L> static cudaError_t launch_xline(const XPassArgs<float> &a, cuda
     static const cudaError_t attr = line_smem(k_xline<L>, fl::xline_smem_bytes<L>());
     if (attr != cudaSuccess) return attr;
     k_xline<L><<<grid, G::NT, fl::xline_smem_bytes<L>(), st>>>(a);
+    return cudaGetLastError();
+}
+
+// plain forward / inverse y transforms of every buffer on the line engine (sides 384 ... 1024)
+static bool fast_y_line_pass(const PassArgs<float> &a)
+{
+    return a.allow_fast && (a.mode == PM_FWD || a.mode == PM_INV) && line_len(a.plan.n) && a.g.Y == a.plan.n &&
+           a.nbuf >= 1;
+}
+
+template <int L> static cudaError_t launch_yline_pass(const PassArgs<float> &a, cudaStream_t st)
+{
+    typedef fl::Geo<L> G;
+    static const cudaError_t attr = line_smem(k_yline_pass<L>, fl::yline_smem_bytes<L>());
+    if (attr != cudaSuccess) return attr;
+    const long long nlines = (long long)a.g.Z * a.g.KX;
+    k_yline_pass<L><<<dim3((unsigned)((nlines + G::LPB - 1) / G::LPB), (unsigned)a.nbuf), G::NT,
+                      fl::yline_smem_bytes<L>(), st>>>(a);
     return cudaGetLastError();
 }
 
@@ -388,6 +410,14 @@ template <> cudaError_t launch_cpass<float>(const PassArgs<float> &a, int LB, cu
     {
         cudaError_t e;
         if (launch_y_line(a, st, &e)) return e;
+    }
+    if (fast_y_line_pass(a)) {
+        switch (a.plan.n) {
+        case 384: return launch_yline_pass<384>(a, st);
+        case 512: return launch_yline_pass<512>(a, st);
+        case 768: return launch_yline_pass<768>(a, st);
+        default: return launch_yline_pass<1024>(a, st);
+        }
     }
     return launch_cpass_generic<float>(a, LB, st);
 }
