@@ -752,17 +752,23 @@ template <typename R> static int batch_build(gopf_batch *b)
             b->pnper = (int)items.size();
             b->psmem = smem;
             b->pctr_bytes = sizeof(unsigned) * (1 + 2 * b->ctx.size());
-            BCK(gopf_malloc(&b->d_pitems, sizeof(int4) * items.size()));
-            BCK(gopf_malloc(&b->d_pnxy, sizeof(int2) * nxy.size()));
-            BCK(gopf_malloc(&b->d_pctr, b->pctr_bytes));
-            BCK(cudaMemcpy(b->d_pitems, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
-            BCK(cudaMemcpy(b->d_pnxy, nxy.data(), sizeof(int2) * nxy.size(), cudaMemcpyHostToDevice));
-            BCK(cudaFuncSetAttribute(k_batch_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
             int occ = 0;
-            BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch_persist, 256, smem));
-            if (occ < 1) return bfail(b, GOPF_ERR_UNSUPPORTED, "the persistent batch kernel does not fit an SM");
-            b->pgrid = nsm * occ;
-            b->pmode = 1;
+            cudaError_t fe = cudaFuncSetAttribute(k_batch_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (fe == cudaSuccess) fe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch_persist, 256, smem);
+            if (fe != cudaSuccess || occ < 1) {
+                // the kernel does not fit: AUTO steps by the chains, PERSISTENT is refused
+                cudaGetLastError();
+                if (b->mode == GOPF_BATCH_MODE_PERSISTENT)
+                    return bfail(b, GOPF_ERR_UNSUPPORTED, "the persistent batch kernel does not fit an SM");
+            } else {
+                BCK(gopf_malloc(&b->d_pitems, sizeof(int4) * items.size()));
+                BCK(gopf_malloc(&b->d_pnxy, sizeof(int2) * nxy.size()));
+                BCK(gopf_malloc(&b->d_pctr, b->pctr_bytes));
+                BCK(cudaMemcpy(b->d_pitems, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
+                BCK(cudaMemcpy(b->d_pnxy, nxy.data(), sizeof(int2) * nxy.size(), cudaMemcpyHostToDevice));
+                b->pgrid = nsm * occ;
+                b->pmode = 1;
+            }
         }
     }
     const size_t nbranch = std::max(b->xl.size(), b->yl.size());
