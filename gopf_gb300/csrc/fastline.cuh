@@ -27,40 +27,43 @@ namespace fl {
 
 using f256::pdft16;
 
-template <int L> struct Geo {
+template <int L, int NB = 0> struct Geo {
     static constexpr int T = L / 16;                 // threads per line
     static constexpr bool P8 = (T == 24);            // second stage: two radix-8 DFTs per thread
     static constexpr int P = P8 ? 8 : 16;            // radix of the in-register second stage
     static constexpr int U = T / P;                  // threads sharing one column DFT (1, 2, 3, 4)
-    static constexpr int NT = (U == 3) ? 192 : 256;  // threads per block
+    // threads per block: 256 (192 when U = 3), or NB (a multiple of T) for smaller blocks
+    static constexpr int NT = NB ? NB : (U == 3) ? 192 : 256;
     static constexpr int LPB = NT / T;               // lines per block
     static constexpr int PAD = (T == 24) ? 4 : 0;    // slot offset between lines (bank spread)
     static constexpr int LREG = 16 * T + PAD;        // shared slots per line
     // separation pitch: the readers take (line p, column kx) with p fastest over LPB lines, so a
     // pitch of 32 / LPB (mod 16) float2 spreads a warp's 32 reads over all 16 bank pairs
     static constexpr int SEP = L + 32 / LPB;
-    // the x pass's input tile is [2 LPB rows][PX] (kx contiguous): with 8 rows (L = 768, 1024) a
-    // pitch of 4 (mod 16) float2 spreads the copies of (row, kx), row fastest, over all 16 bank
-    // pairs; with 16 or 32 rows the odd KX itself does
+    // the x pass's input tile is [2 LPB rows][PX] (kx contiguous): with 4 or 8 rows a pitch of
+    // 32 / rows (mod 16) float2 spreads the copies of (row, kx), row fastest, over all 16 bank pairs;
+    // with 2 rows, or 16 or 32 rows, the odd KX itself does
     static constexpr int KX = L / 2 + 1;
-    static constexpr int PX = (2 * LPB == 8) ? KX + ((4 - KX % 16) + 16) % 16 : KX;
+    static constexpr int PXM = (2 * LPB == 4 || 2 * LPB == 8) ? 32 / (2 * LPB) : 0;
+    static constexpr int PX = PXM ? KX + ((PXM - KX % 16) + 16) % 16 : KX;
     static_assert(L == 256 || L == 384 || L == 512 || L == 768 || L == 1024, "line length");
+    static_assert(NT % T == 0 && NT % 32 == 0 && LPB >= 1, "whole lines and warps per block");
 };
 
-// Barrier over the Geo<L>::NT threads of a tile: __syncthreads when the tile takes a whole 256-thread
+// Barrier over the Geo<L, NB>::NT threads of a tile: __syncthreads when the tile takes a whole 256-thread
 // block, else named barrier 1 over its NT threads, so that a larger block (the persistent batch
 // kernel's) can leave its other threads out of the tile.
-template <int L> __device__ __forceinline__ void lsync()
+template <int L, int NB = 0> __device__ __forceinline__ void lsync()
 {
-    if constexpr (Geo<L>::NT == 256) __syncthreads();
-    else asm volatile("bar.sync 1, %0;" ::"n"(Geo<L>::NT) : "memory");
+    if constexpr (Geo<L, NB>::NT == 256) __syncthreads();
+    else asm volatile("bar.sync 1, %0;" ::"n"(Geo<L, NB>::NT) : "memory");
 }
 
 // First-stage twiddles W_L^(r k1) (r < T, k1 < 16) laid out [k1][r]: the T threads of a line read
 // consecutive slots (conflict free) instead of the strided W_L table entries r k1.
-template <int L> __device__ __forceinline__ void load_twr(float2 *twr, const float2 *__restrict__ tw, int nt)
+template <int L, int NB = 0> __device__ __forceinline__ void load_twr(float2 *twr, const float2 *__restrict__ tw, int nt)
 {
-    constexpr int T = Geo<L>::T;
+    constexpr int T = Geo<L, NB>::T;
     for (int t = threadIdx.x; t < L; t += nt) {
         const int k1 = t / T, r = t - k1 * T;
         twr[t] = tw[r * k1];
@@ -77,7 +80,7 @@ template <int L> struct Role {
     int k1, u, d;
     __device__ __forceinline__ Role(int r)
     {
-        typedef Geo<L> G;
+        typedef Geo<L> G; // the role depends on T only
         if constexpr (G::U == 1) {
             k1 = r;
             u = 0;
@@ -99,7 +102,7 @@ template <int L> struct Role {
     // index along the line of the thread's value j in the B layout
     __device__ __forceinline__ int elem(int j) const
     {
-        typedef Geo<L> G;
+        typedef Geo<L> G; // the role depends on T only
         if constexpr (G::U == 3) { // k2 = 3 c + d
             if constexpr (G::P8) return k1 + ((j >> 3) << 3) + 48 * (j & 7) + 16 * d;
             else return k1 + 48 * j + 16 * d;
@@ -184,17 +187,17 @@ template <bool INV> __device__ __forceinline__ void dft8at(float2 (&v)[16], int 
 
 // Forward transform of the thread's line: in v[i] = x[r + T i]; out v[j] = X[ro.elem(j)].
 // z: the line's slot region; tw: W_L^t (t < L).  Leaves the slots free (ends with a barrier).
-template <int L>
+template <int L, int NB = 0>
 __device__ __forceinline__ void line_fwd(float2 (&v)[16], int r, const Role<L> &ro, float2 *z, const float2 *tw,
                                          const float2 *twr)
 {
-    typedef Geo<L> G;
+    typedef Geo<L, NB> G;
     pdft16<false>(v);
 #pragma unroll
     for (int k1 = 1; k1 < 16; ++k1) v[k1] = cm(v[k1], twr[k1 * G::T + r]);
 #pragma unroll
     for (int k1 = 0; k1 < 16; ++k1) z[slot(r, k1)] = v[k1];
-    lsync<L>();
+    lsync<L, NB>();
     if constexpr (G::U == 3) {
         // T = 3 P: r = s + P t, k2 = 3 c + d.  The thread's output d: radix-3 over t (reading the
         // three rows of each s), twiddle W_T^(s d) = W_L^(16 s d), radix-P over s.
@@ -206,7 +209,7 @@ __device__ __forceinline__ void line_fwd(float2 (&v)[16], int r, const Role<L> &
                 const int col = ro.k1 + 8 * h;
                 v[P * h + s] = dft3_out<false>(z[slot(s, col)], z[slot(s + P, col)], z[slot(s + 2 * P, col)], ro.d);
             }
-        lsync<L>();
+        lsync<L, NB>();
         if (ro.d)
 #pragma unroll
             for (int j = 0; j < 16; ++j)
@@ -220,7 +223,7 @@ __device__ __forceinline__ void line_fwd(float2 (&v)[16], int r, const Role<L> &
     } else {
 #pragma unroll
         for (int s = 0; s < 16; ++s) v[s] = z[slot(G::U * s + ro.u, ro.k1)];
-        lsync<L>();
+        lsync<L, NB>();
         pdft16<false>(v);
         if (G::U > 1 && ro.u)
 #pragma unroll
@@ -230,11 +233,11 @@ __device__ __forceinline__ void line_fwd(float2 (&v)[16], int r, const Role<L> &
 }
 
 // Inverse (unnormalised) transform: in v[j] = X[ro.elem(j)]; out v[i] = x[r + T i] * L.
-template <int L>
+template <int L, int NB = 0>
 __device__ __forceinline__ void line_inv(float2 (&v)[16], int r, const Role<L> &ro, float2 *z, const float2 *tw,
                                          const float2 *twr)
 {
-    typedef Geo<L> G;
+    typedef Geo<L, NB> G;
     if constexpr (G::U == 3) {
         // reverse of the forward: radix-P over c, conjugate twiddle, then the radix-3 over d is
         // formed by the reading thread r = s + P t from the three d slots of (s, column)
@@ -253,12 +256,12 @@ __device__ __forceinline__ void line_inv(float2 (&v)[16], int r, const Role<L> &
         for (int h = 0; h < 16 / P; ++h)
 #pragma unroll
             for (int s = 0; s < P; ++s) z[slot(ro.d * P + s, ro.k1 + 8 * h)] = v[P * h + s];
-        lsync<L>();
+        lsync<L, NB>();
         const int s0 = r % P, t0 = r / P;
 #pragma unroll
         for (int k1 = 0; k1 < 16; ++k1)
             v[k1] = dft3_out<true>(z[slot(s0, k1)], z[slot(P + s0, k1)], z[slot(2 * P + s0, k1)], t0);
-        lsync<L>();
+        lsync<L, NB>();
     } else {
         if constexpr (G::U == 2 || G::U == 4) xdft_inv<G::U, true>(v, ro.u);
         if (G::U > 1 && ro.u)
@@ -267,23 +270,23 @@ __device__ __forceinline__ void line_inv(float2 (&v)[16], int r, const Role<L> &
         pdft16<true>(v);
 #pragma unroll
         for (int s = 0; s < 16; ++s) z[slot(G::U * s + ro.u, ro.k1)] = v[s];
-        lsync<L>();
+        lsync<L, NB>();
 #pragma unroll
         for (int k1 = 0; k1 < 16; ++k1) v[k1] = z[slot(r, k1)];
-        lsync<L>();
+        lsync<L, NB>();
     }
 #pragma unroll
     for (int k1 = 1; k1 < 16; ++k1) v[k1] = cmc(v[k1], twr[k1 * G::T + r]);
     pdft16<true>(v);
 }
 
-template <int L> constexpr int yline_smem_bytes() { return (Geo<L>::LPB * Geo<L>::LREG + L + L + L) * 8; }
+template <int L, int NB = 0> constexpr int yline_smem_bytes() { return (Geo<L, NB>::LPB * Geo<L, NB>::LREG + L + L + L) * 8; }
 
 // One y tile of the 2D fused Euler update (pf/euler.go:16-47; plain form, no noise or filter):
 // LPB lines q0 .. of length L = g.Y, groups a.buf[0 .. ng), c-hat a.state, T <- inverse(c_new/N).
-template <int L, int NG> __device__ __forceinline__ void yline_tile(const PassArgs<float> &a, long long tile)
+template <int L, int NG, int NB = 0> __device__ __forceinline__ void yline_tile(const PassArgs<float> &a, long long tile)
 {
-    typedef Geo<L> G;
+    typedef Geo<L, NB> G;
     extern __shared__ __align__(16) unsigned char fl_dsm[];
     float2 *s_x = reinterpret_cast<float2 *>(fl_dsm);
     float2 *s_tw = s_x + G::LPB * G::LREG;
@@ -300,7 +303,7 @@ template <int L, int NG> __device__ __forceinline__ void yline_tile(const PassAr
         s_tw[t] = a.tw[t];
         s_fy[t] = f256::fsqf(t, g.Y);
     }
-    load_twr<L>(s_twr, a.tw, G::NT);
+    load_twr<L, NB>(s_twr, a.tw, G::NT);
     const Role<L> ro(r);
     const float2 *__restrict__ U0 = a.buf[0];
     float2 *__restrict__ state = a.state;
@@ -311,8 +314,8 @@ template <int L, int NG> __device__ __forceinline__ void yline_tile(const PassAr
     // latency overlaps the forward FFT
 #pragma unroll
     for (int j = 0; j < 16; ++j) cs[j] = valid ? state[q * L + ro.elem(j)] : zero;
-    lsync<L>();
-    line_fwd<L>(v, r, ro, z, s_tw, s_twr);
+    lsync<L, NB>();
+    line_fwd<L, NB>(v, r, ro, z, s_tw, s_twr);
     const UpdTable &u = a.upd;
     const int ngrp = (NG == 1) ? (u.ngrp > 0 ? 1 : 0) : u.ngrp;
     float2 w[NG == 1 ? 1 : 16];
@@ -320,7 +323,7 @@ template <int L, int NG> __device__ __forceinline__ void yline_tile(const PassAr
         const float2 *__restrict__ U1 = a.buf[1];
 #pragma unroll
         for (int i = 0; i < 16; ++i) w[i] = valid ? U1[q * L + r + G::T * i] : zero;
-        line_fwd<L>(reinterpret_cast<float2(&)[16]>(w), r, ro, z, s_tw, s_twr);
+        line_fwd<L, NB>(reinterpret_cast<float2(&)[16]>(w), r, ro, z, s_tw, s_twr);
     }
     const f256::UpdRegs R = f256::load_upd(u, ngrp);
     float fl = 0.f;
@@ -340,7 +343,7 @@ template <int L, int NG> __device__ __forceinline__ void yline_tile(const PassAr
         }
         v[j] = make_float2(cn.x * R.invN, cn.y * R.invN);
     }
-    line_inv<L>(v, r, ro, z, s_tw, s_twr);
+    line_inv<L, NB>(v, r, ro, z, s_tw, s_twr);
     float2 *__restrict__ T = a.tout;
 #pragma unroll
     for (int i = 0; i < 16; ++i)
@@ -351,9 +354,9 @@ template <int L, int NG> __device__ __forceinline__ void yline_tile(const PassAr
 // y passes of PM_FWD and PM_INV (L = g.Y, lines q = z KX + kx).  The forward transform leaves a line in
 // the B layout, stored at its natural positions elem(j); the inverse reads those and ends in the A
 // layout.  Shared memory as yline_tile (the frequency table unused).
-template <int L> __device__ __forceinline__ void yline_pass_tile(const PassArgs<float> &a, long long tile, int b, bool inv)
+template <int L, int NB = 0> __device__ __forceinline__ void yline_pass_tile(const PassArgs<float> &a, long long tile, int b, bool inv)
 {
-    typedef Geo<L> G;
+    typedef Geo<L, NB> G;
     extern __shared__ __align__(16) unsigned char fl_dsm[];
     float2 *s_x = reinterpret_cast<float2 *>(fl_dsm);
     float2 *s_tw = s_x + G::LPB * G::LREG;
@@ -376,15 +379,15 @@ template <int L> __device__ __forceinline__ void yline_pass_tile(const PassArgs<
         for (int j = 0; j < 16; ++j) v[j] = valid ? buf[q * L + ro.elem(j)] : zero;
     }
     for (int t = threadIdx.x; t < L; t += G::NT) s_tw[t] = a.tw[t];
-    load_twr<L>(s_twr, a.tw, G::NT);
-    lsync<L>();
+    load_twr<L, NB>(s_twr, a.tw, G::NT);
+    lsync<L, NB>();
     if (!inv) {
-        line_fwd<L>(v, r, ro, z, s_tw, s_twr);
+        line_fwd<L, NB>(v, r, ro, z, s_tw, s_twr);
 #pragma unroll
         for (int j = 0; j < 16; ++j)
             if (valid) buf[q * L + ro.elem(j)] = v[j];
     } else {
-        line_inv<L>(v, r, ro, z, s_tw, s_twr);
+        line_inv<L, NB>(v, r, ro, z, s_tw, s_twr);
 #pragma unroll
         for (int i = 0; i < 16; ++i)
             if (valid) buf[q * L + r + G::T * i] = v[i];
@@ -394,14 +397,14 @@ template <int L> __device__ __forceinline__ void yline_pass_tile(const PassArgs<
 // one shared array holds, in turn, the spectral tile [2 LPB rows][PX], the exchange slots of the
 // LPB lines and the separation slots [LPB][SEP]; then two twiddle tables and the polynomial
 // coefficients
-template <int L> __host__ __device__ constexpr int xline_area()
+template <int L, int NB = 0> __host__ __device__ constexpr int xline_area()
 {
-    constexpr int a = 2 * Geo<L>::LPB * Geo<L>::PX, b = Geo<L>::LPB * Geo<L>::LREG, c = Geo<L>::LPB * Geo<L>::SEP;
+    constexpr int a = 2 * Geo<L, NB>::LPB * Geo<L, NB>::PX, b = Geo<L, NB>::LPB * Geo<L, NB>::LREG, c = Geo<L, NB>::LPB * Geo<L, NB>::SEP;
     return (a > b ? (a > c ? a : c) : (b > c ? b : c));
 }
-template <int L> constexpr int xline_smem_bytes()
+template <int L, int NB = 0> constexpr int xline_smem_bytes()
 {
-    return (xline_area<L>() + 2 * L) * 8 + GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1) * 4;
+    return (xline_area<L, NB>() + 2 * L) * 8 + GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1) * 4;
 }
 
 // 16-byte asynchronous global -> shared copy (no register staging), completed by cp_async_wait
@@ -419,9 +422,9 @@ template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile(
 
 // Request the spectral tile of x tile ty (kx = 0 .. L/2, rows y0 .. y0 + 2 LPB) into area[row][kx]
 // (pitch PX) with 8-byte asynchronous copies, row fastest (g.Y must be a multiple of 2 LPB).
-template <int L> __device__ __forceinline__ void xline_request(float2 *area, const XPassArgs<float> &a, int ty, int zp)
+template <int L, int NB = 0> __device__ __forceinline__ void xline_request(float2 *area, const XPassArgs<float> &a, int ty, int zp)
 {
-    typedef Geo<L> G;
+    typedef Geo<L, NB> G;
     constexpr int KX = G::KX, RB = 2 * G::LPB;
     const long long sbase = (long long)zp * a.g.S + (long long)ty * RB;
     const float2 *__restrict__ in = a.in;
@@ -435,9 +438,9 @@ template <int L> __device__ __forceinline__ void xline_request(float2 *area, con
 // Rows (2l, 2l + 1) of the tile as one complex line a + i b of L columns, Hermitian-extended, in
 // the A layout (v[i] = column r + T i), conjugated: conj(A(k) + i B(k)) for k <= L/2 and
 // conj(conj A(L - k) + i conj B(L - k)) above.  Consecutive r read consecutive slots.
-template <int L> __device__ __forceinline__ void xline_gather_conj(const float2 *s_a, int l, int r, float2 (&v)[16])
+template <int L, int NB = 0> __device__ __forceinline__ void xline_gather_conj(const float2 *s_a, int l, int r, float2 (&v)[16])
 {
-    typedef Geo<L> G;
+    typedef Geo<L, NB> G;
     constexpr int H = L / 2;
     const float2 *ra = s_a + (2 * l) * G::PX, *rb = ra + G::PX;
 #pragma unroll
@@ -455,15 +458,15 @@ template <int L> __device__ __forceinline__ void xline_gather_conj(const float2 
 // The separation slots of the line's forward spectrum Z (A layout, v holding conj Z) and the
 // coalesced stores of the two rows' half spectra X_a(k) = (Z(k) + conj Z(-k))/2 (row 2p) and
 // X_b(k) = (Z(k) - conj Z(-k))/(2i) (row 2p + 1).
-template <int L>
+template <int L, int NB = 0>
 __device__ __forceinline__ void xline_separate(float2 (&v)[16], float2 *s_sep, int l, int r, float2 *__restrict__ out,
                                                long long sbase, int y0, int Y)
 {
-    typedef Geo<L> G;
+    typedef Geo<L, NB> G;
     constexpr int KX = G::KX;
 #pragma unroll
     for (int i = 0; i < 16; ++i) s_sep[l * G::SEP + r + G::T * i] = make_float2(v[i].x, -v[i].y);
-    lsync<L>();
+    lsync<L, NB>();
     for (int e = threadIdx.x; e < KX * G::LPB; e += G::NT) {
         const int kx = e / G::LPB, p = e - kx * G::LPB;
         const float2 P = s_sep[p * G::SEP + kx];
@@ -472,7 +475,7 @@ __device__ __forceinline__ void xline_separate(float2 (&v)[16], float2 *s_sep, i
             *reinterpret_cast<float4 *>(&out[sbase + (long long)kx * Y + 2 * p]) =
                 make_float4(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y), 0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
     }
-    lsync<L>();
+    lsync<L, NB>();
 }
 
 // One x tile from its spectral tile in area (which then serves as exchange and separation
@@ -483,11 +486,11 @@ __device__ __forceinline__ void xline_separate(float2 (&v)[16], float2 *s_sep, i
 // consecutive slots.  s_poly: this instance's dense polynomial coefficients.  Ends with a barrier.
 // ONE: exactly one output group, a dense polynomial of degree <= 6 (the caller checks), so only one
 // line is held in registers and the polynomial is unrolled for its degree
-template <int L, bool ONE = false>
+template <int L, bool ONE = false, int NB = 0>
 __device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float> &a, int ty, int zp,
                                               const float2 *s_tw, const float2 *s_twr, const float *s_poly)
 {
-    typedef Geo<L> G;
+    typedef Geo<L, NB> G;
     constexpr int RB = 2 * G::LPB;
     float2 *s_sep = s_a; // [LPB][SEP], once the exchange is done
     const Geom &g = a.g;
@@ -497,10 +500,10 @@ __device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float
     const int Y = g.Y;
     const Role<L> ro(r);
     float2 v[16];
-    xline_gather_conj<L>(s_a, l, r, v);
-    lsync<L>(); // the tile becomes the exchange slots
+    xline_gather_conj<L, NB>(s_a, l, r, v);
+    lsync<L, NB>(); // the tile becomes the exchange slots
     float2 *z = s_a + l * G::LREG;
-    line_fwd<L>(v, r, ro, z, s_tw, s_twr);
+    line_fwd<L, NB>(v, r, ro, z, s_tw, s_twr);
     // conj(v[j]) = c(row 2l, col elem(j)) + i c(row 2l + 1, col elem(j)) (times L)
 #pragma unroll
     for (int j = 0; j < 16; ++j) v[j].y = -v[j].y;
@@ -509,8 +512,8 @@ __device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float
         if (!a.identity) f256::apply_poly(w, a, grp, s_poly + grp * (GOPF_MAX_DEG + 1));
 #pragma unroll
         for (int j = 0; j < 16; ++j) w[j].y = -w[j].y;
-        line_inv<L>(w, r, ro, z, s_tw, s_twr);
-        xline_separate<L>(w, s_sep, l, r, a.out[grp], sbase, y0, Y);
+        line_inv<L, NB>(w, r, ro, z, s_tw, s_twr);
+        xline_separate<L, NB>(w, s_sep, l, r, a.out[grp], sbase, y0, Y);
     };
     if constexpr (ONE) {
         switch (a.pw.deg[0]) {
@@ -524,8 +527,8 @@ __device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float
         }
 #pragma unroll
         for (int j = 0; j < 16; ++j) v[j].y = -v[j].y;
-        line_inv<L>(v, r, ro, z, s_tw, s_twr);
-        xline_separate<L>(v, s_sep, l, r, a.out[0], sbase, y0, Y);
+        line_inv<L, NB>(v, r, ro, z, s_tw, s_twr);
+        xline_separate<L, NB>(v, s_sep, l, r, a.out[0], sbase, y0, Y);
         return;
     }
     // every group but the last works on a copy; the last one on v itself, so that a single group
@@ -540,28 +543,28 @@ __device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float
     if (ng > 0) emit(v, ng - 1);
 }
 
-template <int L>
+template <int L, int NB = 0>
 __device__ __forceinline__ void load_xconsts(const XPassArgs<float> &a, float2 *s_tw, float2 *s_twr, float *s_poly)
 {
-    for (int t = threadIdx.x; t < L; t += Geo<L>::NT) s_tw[t] = a.twX[t];
-    load_twr<L>(s_twr, a.twX, Geo<L>::NT);
-    for (int t = threadIdx.x; t < GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1); t += Geo<L>::NT)
+    for (int t = threadIdx.x; t < L; t += Geo<L, NB>::NT) s_tw[t] = a.twX[t];
+    load_twr<L, NB>(s_twr, a.twX, Geo<L, NB>::NT);
+    for (int t = threadIdx.x; t < GOPF_MAX_GROUPS * (GOPF_MAX_DEG + 1); t += Geo<L, NB>::NT)
         s_poly[t] = (float)a.pw.dense[t / (GOPF_MAX_DEG + 1)][t % (GOPF_MAX_DEG + 1)];
 }
 
 // One x tile: 2 LPB rows from row ty * 2 LPB of depth plane zp (g.Y a multiple of 2 LPB).
-template <int L, bool ONE = false> __device__ __forceinline__ void xline_tile(const XPassArgs<float> &a, int ty, int zp)
+template <int L, bool ONE = false, int NB = 0> __device__ __forceinline__ void xline_tile(const XPassArgs<float> &a, int ty, int zp)
 {
     extern __shared__ __align__(16) unsigned char fl_dsm[];
     float2 *s_a = reinterpret_cast<float2 *>(fl_dsm);
-    float2 *s_tw = s_a + xline_area<L>();
+    float2 *s_tw = s_a + xline_area<L, NB>();
     float2 *s_twr = s_tw + L;
     float *s_poly = reinterpret_cast<float *>(s_twr + L);
-    xline_request<L>(s_a, a, ty, zp);
-    load_xconsts<L>(a, s_tw, s_twr, s_poly);
+    xline_request<L, NB>(s_a, a, ty, zp);
+    load_xconsts<L, NB>(a, s_tw, s_twr, s_poly);
     cp_async_wait<0>();
-    lsync<L>();
-    xline_compute<L, ONE>(s_a, a, ty, zp, s_tw, s_twr, s_poly);
+    lsync<L, NB>();
+    xline_compute<L, ONE, NB>(s_a, a, ty, zp, s_tw, s_twr, s_poly);
 }
 
 } // namespace fl

@@ -253,22 +253,42 @@ template <> int xpass_red_blocks<float>(const XPassArgs<float> &a, int LB)
 
 // ---- the register-resident line engine for 2D lines of 384 ... 1024 (fastline.cuh) ----
 
-template <int L, int NG> __global__ void __launch_bounds__(fl::Geo<L>::NT, 3) k_yline(const PassArgs<float> a)
+// NB: threads per block; 0 is the engine's default (256, or 192 for 384 and 768), half of that serves
+// grids too small to give every SM two blocks of the default size (twice the blocks per SM, each with
+// half the lines, so the launch bounds double the blocks per SM at the same registers per thread)
+template <int L, int NG, int NB>
+__global__ void __launch_bounds__(fl::Geo<L, NB>::NT, NB ? 6 : 3) k_yline(const PassArgs<float> a)
 {
-    fl::yline_tile<L, NG>(a, blockIdx.x);
+    fl::yline_tile<L, NG, NB>(a, blockIdx.x);
 }
-template <int L> __global__ void __launch_bounds__(fl::Geo<L>::NT, 3) k_yline_pass(const PassArgs<float> a)
+template <int L, int NB>
+__global__ void __launch_bounds__(fl::Geo<L, NB>::NT, NB ? 6 : 3) k_yline_pass(const PassArgs<float> a)
 {
-    fl::yline_pass_tile<L>(a, blockIdx.x, blockIdx.y, a.mode == PM_INV);
+    fl::yline_pass_tile<L, NB>(a, blockIdx.x, blockIdx.y, a.mode == PM_INV);
 }
-template <int L> __global__ void __launch_bounds__(fl::Geo<L>::NT, 3) k_xline(const XPassArgs<float> a)
+template <int L, int NB> __global__ void __launch_bounds__(fl::Geo<L, NB>::NT, NB ? 6 : 3) k_xline(const XPassArgs<float> a)
 {
-    fl::xline_tile<L>(a, blockIdx.x, blockIdx.y);
+    fl::xline_tile<L, false, NB>(a, blockIdx.x, blockIdx.y);
 }
 // one dense polynomial group of degree <= 6: one line in registers, four blocks per SM
-template <int L> __global__ void __launch_bounds__(fl::Geo<L>::NT, 4) k_xline1(const XPassArgs<float> a)
+template <int L, int NB> __global__ void __launch_bounds__(fl::Geo<L, NB>::NT, NB ? 8 : 4) k_xline1(const XPassArgs<float> a)
 {
-    fl::xline_tile<L, true>(a, blockIdx.x, blockIdx.y);
+    fl::xline_tile<L, true, NB>(a, blockIdx.x, blockIdx.y);
+}
+
+// half of the engine's default block (a multiple of the line's T threads and of a warp)
+template <int L> constexpr int half_nb() { return fl::Geo<L>::NT / 2; }
+
+// blocks a grid of `blocks` default-size blocks leaves per SM: fewer than two asks for half-size blocks
+static bool small_grid(long long blocks)
+{
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1)
+            nsm = 152;
+    }
+    return blocks < 2LL * nsm;
 }
 
 static bool line_len(int n) { return n == 384 || n == 512 || n == 768 || n == 1024; }
@@ -294,21 +314,28 @@ template <typename K> static cudaError_t line_smem(K kern, int bytes)
                              : cudaSuccess;
 }
 
-template <int L> static cudaError_t launch_xline(const XPassArgs<float> &a, cudaStream_t st)
+template <int L, int NB> static cudaError_t launch_xline_nb(const XPassArgs<float> &a, cudaStream_t st)
 {
-    typedef fl::Geo<L> G;
+    typedef fl::Geo<L, NB> G;
     if (a.g.Y % (2 * G::LPB)) return cudaErrorNotSupported;
     const dim3 grid(a.g.Y / (2 * G::LPB), a.g.Z);
     if (a.ngrp_out == 1 && a.pw.deg[0] >= 0 && a.pw.deg[0] <= 6) {
-        static const cudaError_t attr1 = line_smem(k_xline1<L>, fl::xline_smem_bytes<L>());
+        static const cudaError_t attr1 = line_smem(k_xline1<L, NB>, fl::xline_smem_bytes<L, NB>());
         if (attr1 != cudaSuccess) return attr1;
-        k_xline1<L><<<grid, G::NT, fl::xline_smem_bytes<L>(), st>>>(a);
+        k_xline1<L, NB><<<grid, G::NT, fl::xline_smem_bytes<L, NB>(), st>>>(a);
         return cudaGetLastError();
     }
-    static const cudaError_t attr = line_smem(k_xline<L>, fl::xline_smem_bytes<L>());
+    static const cudaError_t attr = line_smem(k_xline<L, NB>, fl::xline_smem_bytes<L, NB>());
     if (attr != cudaSuccess) return attr;
-    k_xline<L><<<grid, G::NT, fl::xline_smem_bytes<L>(), st>>>(a);
+    k_xline<L, NB><<<grid, G::NT, fl::xline_smem_bytes<L, NB>(), st>>>(a);
     return cudaGetLastError();
+}
+
+template <int L> static cudaError_t launch_xline(const XPassArgs<float> &a, cudaStream_t st)
+{
+    typedef fl::Geo<L> G;
+    if (small_grid((long long)(a.g.Y / (2 * G::LPB)) * a.g.Z)) return launch_xline_nb<L, half_nb<L>()>(a, st);
+    return launch_xline_nb<L, 0>(a, st);
 }
 
 // plain forward / inverse y transforms of every buffer on the line engine (sides 384 ... 1024)
@@ -318,24 +345,39 @@ static bool fast_y_line_pass(const PassArgs<float> &a)
            a.nbuf >= 1;
 }
 
+template <int L, int NB> static cudaError_t launch_yline_pass_nb(const PassArgs<float> &a, cudaStream_t st)
+{
+    typedef fl::Geo<L, NB> G;
+    static const cudaError_t attr = line_smem(k_yline_pass<L, NB>, fl::yline_smem_bytes<L, NB>());
+    if (attr != cudaSuccess) return attr;
+    const long long nlines = (long long)a.g.Z * a.g.KX;
+    k_yline_pass<L, NB><<<dim3((unsigned)((nlines + G::LPB - 1) / G::LPB), (unsigned)a.nbuf), G::NT,
+                          fl::yline_smem_bytes<L, NB>(), st>>>(a);
+    return cudaGetLastError();
+}
+
 template <int L> static cudaError_t launch_yline_pass(const PassArgs<float> &a, cudaStream_t st)
 {
     typedef fl::Geo<L> G;
-    static const cudaError_t attr = line_smem(k_yline_pass<L>, fl::yline_smem_bytes<L>());
+    const long long blocks = ((long long)a.g.Z * a.g.KX + G::LPB - 1) / G::LPB * a.nbuf;
+    if (small_grid(blocks)) return launch_yline_pass_nb<L, half_nb<L>()>(a, st);
+    return launch_yline_pass_nb<L, 0>(a, st);
+}
+
+template <int L, int NG, int NB> static cudaError_t launch_yline_nb(const PassArgs<float> &a, cudaStream_t st)
+{
+    typedef fl::Geo<L, NB> G;
+    static const cudaError_t attr = line_smem(k_yline<L, NG, NB>, fl::yline_smem_bytes<L, NB>());
     if (attr != cudaSuccess) return attr;
-    const long long nlines = (long long)a.g.Z * a.g.KX;
-    k_yline_pass<L><<<dim3((unsigned)((nlines + G::LPB - 1) / G::LPB), (unsigned)a.nbuf), G::NT,
-                      fl::yline_smem_bytes<L>(), st>>>(a);
+    k_yline<L, NG, NB><<<(unsigned)((a.g.KX + G::LPB - 1) / G::LPB), G::NT, fl::yline_smem_bytes<L, NB>(), st>>>(a);
     return cudaGetLastError();
 }
 
 template <int L, int NG> static cudaError_t launch_yline(const PassArgs<float> &a, cudaStream_t st)
 {
     typedef fl::Geo<L> G;
-    static const cudaError_t attr = line_smem(k_yline<L, NG>, fl::yline_smem_bytes<L>());
-    if (attr != cudaSuccess) return attr;
-    k_yline<L, NG><<<(unsigned)((a.g.KX + G::LPB - 1) / G::LPB), G::NT, fl::yline_smem_bytes<L>(), st>>>(a);
-    return cudaGetLastError();
+    if (small_grid((a.g.KX + G::LPB - 1) / G::LPB)) return launch_yline_nb<L, NG, half_nb<L>()>(a, st);
+    return launch_yline_nb<L, NG, 0>(a, st);
 }
 
 static bool launch_x_line(const XPassArgs<float> &a, cudaStream_t st, cudaError_t *e)

@@ -334,3 +334,23 @@ def test_persistent_wait_timeout_is_reported():
     fb = G.Batch([f])
     fb.step(3)
     assert np.array_equal(m.download(0), f.download(0))
+
+
+@pytest.mark.parametrize("side", [384, 512, 768, 1024])
+def test_line_engine_block_sizes_match(side):
+    """A single 2D context on the line engine takes half-size blocks where the default ones would
+    leave SMs without two blocks (every side here); a one-instance batch in the chains mode takes the
+    default blocks.  The per-line arithmetic is the same, so both step the same field bitwise (FP32,
+    25 steps)."""
+    import gopf_gb300 as G
+    from gopf_gb300 import _lib as L
+    from gopf_gb300.synthetic import uniform_field
+
+    c0 = uniform_field(6000 + side, side * side, 0.5, 0.05)
+    a = ch_ctx(side, "fp32", 0.6, 1.2, 0.05, c0)
+    b = ch_ctx(side, "fp32", 0.6, 1.2, 0.05, c0)
+    a.step(25)
+    bb = G.Batch([b])
+    bb.set_mode(L.BATCH_MODE_CHAINS)
+    bb.step(25)
+    assert np.array_equal(a.download(0), b.download(0))
