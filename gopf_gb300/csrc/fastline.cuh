@@ -422,17 +422,21 @@ template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile(
 
 // Request the spectral tile of x tile ty (kx = 0 .. L/2, rows y0 .. y0 + 2 LPB) into area[row][kx]
 // (pitch PX) with 8-byte asynchronous copies, row fastest (g.Y must be a multiple of 2 LPB).
-template <int L, int NB = 0> __device__ __forceinline__ void xline_request(float2 *area, const XPassArgs<float> &a, int ty, int zp)
+template <int L, int NB = 0>
+__device__ __forceinline__ void xline_request_from(float2 *area, const float2 *__restrict__ in, const Geom &g, int ty, int zp)
 {
     typedef Geo<L, NB> G;
     constexpr int KX = G::KX, RB = 2 * G::LPB;
-    const long long sbase = (long long)zp * a.g.S + (long long)ty * RB;
-    const float2 *__restrict__ in = a.in;
+    const long long sbase = (long long)zp * g.S + (long long)ty * RB;
     for (int e = threadIdx.x; e < KX * RB; e += G::NT) {
         const int kx = e / RB, row = e - kx * RB;
-        cp_async8(&area[row * G::PX + kx], &in[sbase + (long long)kx * a.g.Y + row]);
+        cp_async8(&area[row * G::PX + kx], &in[sbase + (long long)kx * g.Y + row]);
     }
     cp_async_commit();
+}
+template <int L, int NB = 0> __device__ __forceinline__ void xline_request(float2 *area, const XPassArgs<float> &a, int ty, int zp)
+{
+    xline_request_from<L, NB>(area, a.in, a.g, ty, zp);
 }
 
 // Rows (2l, 2l + 1) of the tile as one complex line a + i b of L columns, Hermitian-extended, in
@@ -553,6 +557,56 @@ __device__ __forceinline__ void load_xconsts(const XPassArgs<float> &a, float2 *
 }
 
 // One x tile: 2 LPB rows from row ty * 2 LPB of depth plane zp (g.Y a multiple of 2 LPB).
+// The adjoint step's x pass (program XP_ADJ) on one x tile: mu = c2r(in) and nu = c2r(in2) along x,
+// c from the real rows rin, lambda = mu - dtM (3 c^2 - 1) nu into the real rows rout and, forward
+// transformed and separated, into out[0] (in place of in when out[0] == in: the tile is read first).
+template <int L, int NB = 0> __device__ __forceinline__ void xline_adj_tile(const XPassArgs<float> &a, int ty, int zp)
+{
+    typedef Geo<L, NB> G;
+    extern __shared__ __align__(16) unsigned char fl_dsm[];
+    float2 *s_a = reinterpret_cast<float2 *>(fl_dsm);
+    float2 *s_tw = s_a + xline_area<L, NB>();
+    float2 *s_twr = s_tw + L;
+    float *s_poly = reinterpret_cast<float *>(s_twr + L);
+    constexpr int RB = 2 * G::LPB;
+    const Geom &g = a.g;
+    const int l = threadIdx.x / G::T, r = threadIdx.x - l * G::T;
+    const int y0 = ty * RB;
+    const Role<L> ro(r);
+    float2 *z = s_a + l * G::LREG;
+    float2 mu[16], nu[16];
+    xline_request_from<L, NB>(s_a, a.in, g, ty, zp);
+    load_xconsts<L, NB>(a, s_tw, s_twr, s_poly);
+    cp_async_wait<0>();
+    lsync<L, NB>();
+    xline_gather_conj<L, NB>(s_a, l, r, mu);
+    lsync<L, NB>(); // the tile becomes the exchange slots
+    line_fwd<L, NB>(mu, r, ro, z, s_tw, s_twr);
+    xline_request_from<L, NB>(s_a, a.in2, g, ty, zp);
+    cp_async_wait<0>();
+    lsync<L, NB>();
+    xline_gather_conj<L, NB>(s_a, l, r, nu);
+    lsync<L, NB>();
+    line_fwd<L, NB>(nu, r, ro, z, s_tw, s_twr);
+    // conj(mu[j]) = mu(row 2l, col elem(j)) + i mu(row 2l + 1, col elem(j)); nu likewise
+    const float dtM = (float)a.adj_dtM;
+    const long long row0 = ((long long)zp * g.Y + y0 + 2 * l) * g.X;
+    const float *__restrict__ rin = a.rin + row0;
+    float *__restrict__ rout = a.rout + row0;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        const int col = ro.elem(j);
+        const float cx = rin[col], cy = rin[g.X + col];
+        const float lx = mu[j].x - dtM * (3.f * cx * cx - 1.f) * nu[j].x;
+        const float ly = -mu[j].y - dtM * (3.f * cy * cy - 1.f) * (-nu[j].y);
+        rout[col] = lx;
+        rout[g.X + col] = ly;
+        mu[j] = make_float2(lx, -ly); // conjugated again for the forward transform
+    }
+    line_inv<L, NB>(mu, r, ro, z, s_tw, s_twr);
+    xline_separate<L, NB>(mu, s_a, l, r, a.out[0], (long long)zp * g.S + y0, y0, g.Y);
+}
+
 template <int L, bool ONE = false, int NB = 0> __device__ __forceinline__ void xline_tile(const XPassArgs<float> &a, int ty, int zp)
 {
     extern __shared__ __align__(16) unsigned char fl_dsm[];

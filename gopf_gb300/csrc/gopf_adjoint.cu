@@ -18,7 +18,8 @@
 // length); a backward step is five launches in 2D: the x pass forming
 // r2c_x(c^3 - c) from the step's x-spectral field, one y pass forward-transforming that and lambda, the k-space
 // product and gradient sums, one inverse y pass, and an x pass that forms
-// lambda_n = mu - dt M (3c^2 - 1) nu and its r2c_x for the next step.
+// lambda_n = mu - dt M (3c^2 - 1) nu and its r2c_x for the next step (the register line engine's
+// passes where they serve the length).
 #include <algorithm>
 #include <cmath>
 #include <cstring>

@@ -276,6 +276,13 @@ template <int L, int NB> __global__ void __launch_bounds__(fl::Geo<L, NB>::NT, N
     fl::xline_tile<L, true, NB>(a, blockIdx.x, blockIdx.y);
 }
 
+// the adjoint step's x pass (XP_ADJ): two lines in registers, so half the default blocks per SM
+template <int L, int NB>
+__global__ void __launch_bounds__(fl::Geo<L, NB>::NT, NB ? 4 : 2) k_xline_adj(const XPassArgs<float> a)
+{
+    fl::xline_adj_tile<L, NB>(a, blockIdx.x, blockIdx.y);
+}
+
 // half of the engine's default block (a multiple of the line's T threads and of a warp)
 template <int L> constexpr int half_nb() { return fl::Geo<L>::NT / 2; }
 
@@ -338,6 +345,30 @@ template <int L> static cudaError_t launch_xline(const XPassArgs<float> &a, cuda
     return launch_xline_nb<L, 0>(a, st);
 }
 
+template <int L, int NB> static cudaError_t launch_xline_adj_nb(const XPassArgs<float> &a, cudaStream_t st)
+{
+    typedef fl::Geo<L, NB> G;
+    if (a.g.Y % (2 * G::LPB)) return cudaErrorNotSupported;
+    static const cudaError_t attr = line_smem(k_xline_adj<L, NB>, fl::xline_smem_bytes<L, NB>());
+    if (attr != cudaSuccess) return attr;
+    k_xline_adj<L, NB><<<dim3(a.g.Y / (2 * G::LPB), a.g.Z), G::NT, fl::xline_smem_bytes<L, NB>(), st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int L> static cudaError_t launch_xline_adj(const XPassArgs<float> &a, cudaStream_t st)
+{
+    typedef fl::Geo<L> G;
+    if (small_grid((long long)(a.g.Y / (2 * G::LPB)) * a.g.Z)) return launch_xline_adj_nb<L, half_nb<L>()>(a, st);
+    return launch_xline_adj_nb<L, 0>(a, st);
+}
+
+// the adjoint's x pass on the line engine: spectral inputs, the real rows in and out, one output
+static bool fast_x_line_adj(const XPassArgs<float> &a)
+{
+    return a.allow_fast && line_len(a.g.X) && a.in_mode == XIN_SPECTRAL && a.program == XP_ADJ && a.in && a.in2 &&
+           a.rin && a.rout && a.ngrp_out == 1 && !a.red && !a.red2;
+}
+
 // plain forward / inverse y transforms of every buffer on the line engine (sides 384 ... 1024)
 static bool fast_y_line_pass(const PassArgs<float> &a)
 {
@@ -382,6 +413,15 @@ template <int L, int NG> static cudaError_t launch_yline(const PassArgs<float> &
 
 static bool launch_x_line(const XPassArgs<float> &a, cudaStream_t st, cudaError_t *e)
 {
+    if (fast_x_line_adj(a)) {
+        switch (a.g.X) {
+        case 384: *e = launch_xline_adj<384>(a, st); break;
+        case 512: *e = launch_xline_adj<512>(a, st); break;
+        case 768: *e = launch_xline_adj<768>(a, st); break;
+        default: *e = launch_xline_adj<1024>(a, st); break;
+        }
+        return *e != cudaErrorNotSupported;
+    }
     if (!fast_x_line(a)) return false;
     switch (a.g.X) {
     case 384: *e = launch_xline<384>(a, st); break;
