@@ -354,3 +354,23 @@ def test_line_engine_block_sizes_match(side):
     bb.set_mode(L.BATCH_MODE_CHAINS)
     bb.step(25)
     assert np.array_equal(a.download(0), b.download(0))
+
+
+def test_persistent_mode_small_instances_equal_chains():
+    """Only small instances (four 128² on the compile-time Stockham tiles, two 256²): few tiles per
+    instance, so the persistent kernel's y tiles often wait for their x tiles.  Bitwise equal to the
+    chains after 1, 16 and 23 steps."""
+    import gopf_gb300 as G
+    from gopf_gb300 import _lib as L
+
+    sides = [128, 256, 128, 128, 256, 128]
+    a = _tune_models("fp32", sides, seed0=7000)
+    b = _tune_models("fp32", sides, seed0=7000)
+    ba, bb = G.Batch(a), G.Batch(b)
+    bb.set_mode(L.BATCH_MODE_CHAINS)
+    assert ba.mode() == L.BATCH_MODE_PERSISTENT
+    for n in (1, 15, 7):
+        ba.step(n)
+        bb.step(n)
+    for x, y in zip(a, b):
+        assert np.array_equal(x.download(0), y.download(0))
