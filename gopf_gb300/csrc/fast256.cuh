@@ -91,7 +91,11 @@ __device__ __forceinline__ void xsync(bool warp)
     else __syncthreads();
 }
 
-template <bool INV, bool WARP = false, typename AT>
+// TR: the exchange stores thread r's values in column r (at(k1, r)) and reads row r, the transpose
+// of the default; the arithmetic is the same.  A transform in the transposed form writes exactly the
+// slots the same thread read in a default-form transform just before it, so that transform may end
+// without its trailing barrier (TAIL = false) when the transposed one follows.
+template <bool INV, bool WARP = false, bool TAIL = true, bool TR = false, typename AT>
 __device__ __forceinline__ void fft256(float2 (&v)[16], int r, const float2 *__restrict__ tw, AT &&at)
 {
     pdft16<INV>(v);
@@ -101,12 +105,15 @@ __device__ __forceinline__ void fft256(float2 (&v)[16], int r, const float2 *__r
         v[k1] = INV ? cmulc(v[k1], w) : cmul(v[k1], w);
     }
 #pragma unroll
-    for (int k1 = 0; k1 < 16; ++k1) at(r, k1) = v[k1];
+    for (int k1 = 0; k1 < 16; ++k1) {
+        if (TR) at(k1, r) = v[k1];
+        else at(r, k1) = v[k1];
+    }
     xsync(WARP);
 #pragma unroll
-    for (int n2 = 0; n2 < 16; ++n2) v[n2] = at(n2, r);
+    for (int n2 = 0; n2 < 16; ++n2) v[n2] = TR ? at(r, n2) : at(n2, r);
     pdft16<INV>(v);
-    xsync(WARP); // slots may be reused after return
+    if (TAIL) xsync(WARP); // slots may be reused after return
 }
 
 // s_tw[k1*16 + r] = W256^(r*k1)
@@ -951,7 +958,8 @@ __global__ void __launch_bounds__(ZH_NT, 6)
     for (int i = 0; i < 16; ++i) v[i] = tU0[(r + 16 * i) * ZH_LINES + l];
     __syncthreads(); // the group tile becomes the exchange slots
     auto at = [&](int x, int y) -> float2 & { return tU0[x * ZH_PITCH + y * ZH_LINES + l]; };
-    fft256<false>(v, r, s_tw, at);
+    // no trailing barrier: the one before the c-hat store orders these reads before the inverse's writes
+    fft256<false, false, false>(v, r, s_tw, at);
 
     const UpdTable &u = a.upd;
     const UpdRegs R = load_upd(u, ngrp);
@@ -1064,7 +1072,9 @@ static __global__ void __launch_bounds__(XH_NT, 8) k_x256_th(const XPassArgs<flo
     }
     __syncthreads(); // the tile becomes the exchange slots
     auto at = [&](int x, int y) -> float2 & { return s_x[x * XH_PITCH + y * XH_LINES + j]; };
-    fft256<true>(v, r, s_tw, at);
+    // the forward transform stores in the transposed form, into the slots each thread read at the
+    // end of the inverse one: no barrier between the two
+    fft256<true, false, false>(v, r, s_tw, at);
     switch (a.identity ? -1 : a.pw.deg[0]) { // the launch guarantees a dense degree <= 6
     case 0: poly_regs<0>(v, s_poly); break;
     case 1: poly_regs<1>(v, s_poly); break;
@@ -1075,7 +1085,7 @@ static __global__ void __launch_bounds__(XH_NT, 8) k_x256_th(const XPassArgs<flo
     case 6: poly_regs<6>(v, s_poly); break;
     default: break;
     }
-    fft256<false>(v, r, s_tw, at);
+    fft256<false, false, true, true>(v, r, s_tw, at);
     // spectrum Z(k) of line j at slot [k][j] (pitch 8 per k), then the row pairs' half spectra
 #pragma unroll
     for (int i = 0; i < 16; ++i) s_x[(r + 16 * i) * XH_LINES + j] = v[i];

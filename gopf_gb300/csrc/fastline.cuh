@@ -187,9 +187,11 @@ template <bool INV> __device__ __forceinline__ void dft8at(float2 (&v)[16], int 
 
 // Forward transform of the thread's line: in v[i] = x[r + T i]; out v[j] = X[ro.elem(j)].
 // z: the line's slot region; tw: W_L^t (t < L).  Leaves the slots free (ends with a barrier).
+// tail = false (U = 1, 2, 4) leaves out that last barrier: allowed when the next access to the slots
+// is line_inv's first store, which writes exactly the slots each thread read here last.
 template <int L, int NB = 0>
 __device__ __forceinline__ void line_fwd(float2 (&v)[16], int r, const Role<L> &ro, float2 *z, const float2 *tw,
-                                         const float2 *twr)
+                                         const float2 *twr, bool tail = true)
 {
     typedef Geo<L, NB> G;
     pdft16<false>(v);
@@ -223,7 +225,7 @@ __device__ __forceinline__ void line_fwd(float2 (&v)[16], int r, const Role<L> &
     } else {
 #pragma unroll
         for (int s = 0; s < 16; ++s) v[s] = z[slot(G::U * s + ro.u, ro.k1)];
-        lsync<L, NB>();
+        if (tail) lsync<L, NB>();
         pdft16<false>(v);
         if (G::U > 1 && ro.u)
 #pragma unroll
@@ -233,9 +235,11 @@ __device__ __forceinline__ void line_fwd(float2 (&v)[16], int r, const Role<L> &
 }
 
 // Inverse (unnormalised) transform: in v[j] = X[ro.elem(j)]; out v[i] = x[r + T i] * L.
+// tail = false leaves out the last barrier (after the final slot reads): allowed when the slots are
+// not touched again before a barrier of the caller.
 template <int L, int NB = 0>
 __device__ __forceinline__ void line_inv(float2 (&v)[16], int r, const Role<L> &ro, float2 *z, const float2 *tw,
-                                         const float2 *twr)
+                                         const float2 *twr, bool tail = true)
 {
     typedef Geo<L, NB> G;
     if constexpr (G::U == 3) {
@@ -261,7 +265,7 @@ __device__ __forceinline__ void line_inv(float2 (&v)[16], int r, const Role<L> &
 #pragma unroll
         for (int k1 = 0; k1 < 16; ++k1)
             v[k1] = dft3_out<true>(z[slot(s0, k1)], z[slot(P + s0, k1)], z[slot(2 * P + s0, k1)], t0);
-        lsync<L, NB>();
+        if (tail) lsync<L, NB>();
     } else {
         if constexpr (G::U == 2 || G::U == 4) xdft_inv<G::U, true>(v, ro.u);
         if (G::U > 1 && ro.u)
@@ -273,7 +277,7 @@ __device__ __forceinline__ void line_inv(float2 (&v)[16], int r, const Role<L> &
         lsync<L, NB>();
 #pragma unroll
         for (int k1 = 0; k1 < 16; ++k1) v[k1] = z[slot(r, k1)];
-        lsync<L, NB>();
+        if (tail) lsync<L, NB>();
     }
 #pragma unroll
     for (int k1 = 1; k1 < 16; ++k1) v[k1] = cmc(v[k1], twr[k1 * G::T + r]);
@@ -315,15 +319,16 @@ template <int L, int NG, int NB = 0> __device__ __forceinline__ void yline_tile(
 #pragma unroll
     for (int j = 0; j < 16; ++j) cs[j] = valid ? state[q * L + ro.elem(j)] : zero;
     lsync<L, NB>();
-    line_fwd<L, NB>(v, r, ro, z, s_tw, s_twr);
     const UpdTable &u = a.upd;
     const int ngrp = (NG == 1) ? (u.ngrp > 0 ? 1 : 0) : u.ngrp;
+    // the last forward transform before line_inv needs no trailing barrier
+    line_fwd<L, NB>(v, r, ro, z, s_tw, s_twr, NG > 1 && ngrp > 1);
     float2 w[NG == 1 ? 1 : 16];
     if (NG > 1 && ngrp > 1) {
         const float2 *__restrict__ U1 = a.buf[1];
 #pragma unroll
         for (int i = 0; i < 16; ++i) w[i] = valid ? U1[q * L + r + G::T * i] : zero;
-        line_fwd<L, NB>(reinterpret_cast<float2(&)[16]>(w), r, ro, z, s_tw, s_twr);
+        line_fwd<L, NB>(reinterpret_cast<float2(&)[16]>(w), r, ro, z, s_tw, s_twr, false);
     }
     const f256::UpdRegs R = f256::load_upd(u, ngrp);
     float fl = 0.f;
@@ -343,7 +348,8 @@ template <int L, int NG, int NB = 0> __device__ __forceinline__ void yline_tile(
         }
         v[j] = make_float2(cn.x * R.invN, cn.y * R.invN);
     }
-    line_inv<L, NB>(v, r, ro, z, s_tw, s_twr);
+    // the tile ends here: the block exits, or its caller passes a barrier before the next tile
+    line_inv<L, NB>(v, r, ro, z, s_tw, s_twr, false);
     float2 *__restrict__ T = a.tout;
 #pragma unroll
     for (int i = 0; i < 16; ++i)
@@ -507,7 +513,7 @@ __device__ __forceinline__ void xline_compute(float2 *s_a, const XPassArgs<float
     xline_gather_conj<L, NB>(s_a, l, r, v);
     lsync<L, NB>(); // the tile becomes the exchange slots
     float2 *z = s_a + l * G::LREG;
-    line_fwd<L, NB>(v, r, ro, z, s_tw, s_twr);
+    line_fwd<L, NB>(v, r, ro, z, s_tw, s_twr, false); // line_inv comes next
     // conj(v[j]) = c(row 2l, col elem(j)) + i c(row 2l + 1, col elem(j)) (times L)
 #pragma unroll
     for (int j = 0; j < 16; ++j) v[j].y = -v[j].y;
