@@ -13,6 +13,8 @@ One step = one Euler step of the whole grid (pf/euler.go:16-47).
   roofline : dominant kernel's algorithmic bytes / its average duration
   cpu_baseline : the FP64 CPU oracle (a restatement of the reference's Euler
                  step, OpenMP over all host cores) on a bounded sample
+  config.monitors : the mass and free-energy monitors on the stepped field
+                    (time per synchronous call, algorithmic bytes, GB/s)
 
 --impl reference times the CPU oracle alone (the reference itself is Go +
 FFTW and cannot be built on these machines).
@@ -247,6 +249,7 @@ def run_gpu(args):
     value = world * args.steps / (ms / 1000.0)
     mass1 = m.mass(0)
     finite = m.reduce(0, G.RED_NONFINITE) == 0
+    monitors = time_monitors(m, n)
 
     # ---- per-kernel roofline (launch by launch, events on the same stream) ----
     prof = m.profile_step(20)
@@ -273,11 +276,35 @@ def run_gpu(args):
     if rank == 0 and not args.no_precision:
         precision = measure_precision(args, G, torch, c0, n, stream, value / world, oracle_run)
     out = emit(args, world, rank, value, per_step_ms, mass0, mass1, finite, prof, dom, hbm, peak_kind, achieved,
-               step_bytes, e2e, clocks, n, cpu, precision, gpu_launches)
+               step_bytes, e2e, clocks, n, cpu, precision, gpu_launches, monitors)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
     return 0
+
+
+def time_monitors(m, n, reps=20):
+    """The device monitors on the stepped field, each call synchronous (the result is on the host when
+    it returns): median wall time per call over `reps` calls, and the algorithmic bytes over that time.
+    Mass (gopf_reduce): the inverse x pass of T with FP64 block sums, C bytes.  Free energy
+    (gopf_free_energy): the inverse x pass to real rows, the bulk sum over the cells and the gradient
+    sum over the spectrum, 2C + 2R bytes (C = the half spectrum, R = the real field, FP32)."""
+    C = (DIMS[0] // 2 + 1) * DIMS[1] * DIMS[2] * 8
+    R = n * 4
+    out = {}
+    for name, call, nbytes in (("mass", lambda: m.mass(0), C),
+                               ("free_energy", lambda: m.free_energy(0, kappa=GAMMA), 2 * C + 2 * R)):
+        call()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            call()
+            ts.append(time.perf_counter() - t0)
+        t = sorted(ts)[len(ts) // 2]
+        out[name] = {"us_per_call": t * 1e6, "bytes_algorithmic": nbytes, "GBps": nbytes / t / 1e9,
+                     "includes": "launches, FP64 partial sums and the host synchronisation"}
+    out["free_energy_value"] = m.free_energy(0, kappa=GAMMA)[2]
+    return out
 
 
 def warmup_steps(args) -> int:
@@ -416,7 +443,7 @@ def host_link(torch, host, stream, reps=5):
 
 
 def emit(args, world, rank, value, per_step_ms, mass0, mass1, finite, prof, dom, hbm, peak_kind, achieved,
-         step_bytes, e2e, clocks, n, cpu, precision, gpu_launches):
+         step_bytes, e2e, clocks, n, cpu, precision, gpu_launches, monitors=None):
     out = None
     if rank == 0:
         out = {
@@ -429,6 +456,7 @@ def emit(args, world, rank, value, per_step_ms, mass0, mass1, finite, prof, dom,
                               "step_fraction_of_hbm": (step_bytes * value / world / 1e9) / hbm,
                               "mass_drift_per_cell": abs(mass1 - mass0) / n, "finite": bool(finite),
                               "precision": precision,
+                              "monitors": monitors,
                               "per_pass_gbs": {p["name"]: p["bytes"] / p["ms"] / 1e6 for p in prof if p["ms"] > 0},
                               "per_pass_frac_of_hbm": {p["name"]: p["bytes"] / p["ms"] / 1e6 / hbm
                                                        for p in prof if p["ms"] > 0}}),
@@ -722,9 +750,25 @@ def run_elastic(args):
            "step_bytes_algorithmic": step_bytes, "step_fraction_of_hbm": step_bytes * value / 1e9 / hbm,
            "mass_drift_per_cell": abs(m.mass(0) - mass0) / n,
            "per_kernel": [{"name": p["name"], "ms": p["ms"], "GBps": p["bytes"] / p["ms"] / 1e6 if p["ms"] > 0 else 0}
-                          for p in prof], "clocks": clk.summary(), "gpu_launches": m.kernel_launches(args.steps)}
+                          for p in prof], "clocks": clk.summary(), "gpu_launches": m.kernel_launches(args.steps),
+           "elastic_energy_monitor": time_elastic_energy(m)}
     print(json.dumps(out))
     return 0
+
+
+def time_elastic_energy(m, reps=5):
+    """HomogeneousModulusEnergy of the stepped field's indicator (the elastic monitor): median wall time
+    of a synchronous call over `reps` calls (the first call, which allocates its work buffers, untimed)."""
+    C, mis = _cubic(1.0, 0.6, 0.5), np.eye(3) * 0.01
+    e = m.elastic_energy(C, mis, indicator=True)
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        m.elastic_energy(C, mis, indicator=True)
+        ts.append(time.perf_counter() - t0)
+    return {"value": e, "ms_per_call": sorted(ts)[len(ts) // 2] * 1e3,
+            "passes": "x-hat (3 forward passes), the six strain spectra in one kernel, 6 x 3 inverse passes, "
+                      "the energy density with FP64 sums"}
 
 
 def run_c1(args):

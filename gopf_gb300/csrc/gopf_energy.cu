@@ -28,9 +28,12 @@
 //   Hermitian, i.e. of x-hat (s(k) + s(-k))/2: the symbol is symmetrised here so
 //   the strains can use the real-to-complex passes.
 //
-// All sums are FP64 with Neumaier compensation; the fields and transforms are
-// in the context's precision.  Work buffers are allocated on the first call
-// and kept with the context.
+// All sums are FP64: each thread adds its cells' terms (FP32 terms 16 at a
+// time in FP32 first, CellSum), and the threads' and blocks' partial sums are
+// combined with Neumaier compensation.  The fields, transforms and per-cell
+// terms are in the context's precision.  Work buffers are allocated on the
+// first call and kept with the context.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -63,6 +66,30 @@ __device__ __forceinline__ void nadd(double &s, double &c, double v)
     c += (fabs(s) >= fabs(v)) ? (s - t) + v : (v - t) + s;
     s = t;
 }
+
+// A thread's running sum of per-cell terms in FP64.  FP32 terms are added 16 at a time in FP32 and
+// each such partial once into the FP64 total (FP64 arithmetic runs at a small fraction of the FP32
+// rate on this GPU); FP64 terms go straight into the total.
+template <typename T> struct CellSum {
+    double s = 0.0;
+    __device__ __forceinline__ void add(T v) { s += (double)v; }
+    __device__ __forceinline__ double total() const { return s; }
+};
+template <> struct CellSum<float> {
+    double s = 0.0;
+    float a = 0.f;
+    int n = 0;
+    __device__ __forceinline__ void add(float v)
+    {
+        a += v;
+        if (++n == 16) {
+            s += (double)a;
+            a = 0.f;
+            n = 0;
+        }
+    }
+    __device__ __forceinline__ double total() const { return s + (double)a; }
+};
 
 // Block-wide compensated sum of (s, c) per slot; thread 0 writes part[blockIdx.x][slot].
 template <int NS> __device__ void block_store(double (&s)[NS], double (&c)[NS], double *part)
@@ -98,57 +125,92 @@ struct BulkPoly {
     double a[EN_MAX_DEG + 1];
 };
 
-// slot 0: sum of the polynomial, slot 1: sum of x, slot 2: non-finite cells
+// slot 0: sum of the polynomial, slot 2: non-finite cells (slot 1 unused).  A thread adds its cells'
+// values with CellSum (at most ceil(n / (EN_BLOCKS EN_THREADS)) of them, 54 at 256^3); the threads'
+// and blocks' partial sums are combined with Neumaier compensation.  An FP32 field's polynomial is
+// evaluated in FP32 (the cell value itself is FP32), an FP64 field's in FP64.
 template <typename R> __global__ void k_bulk(const R *__restrict__ x, long long n, BulkPoly p, double *__restrict__ part)
 {
+    __shared__ R s_a[EN_MAX_DEG + 1];
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int q = 0; q <= EN_MAX_DEG; ++q) s_a[q] = (R)p.a[q];
+    __syncthreads();
     double s[3] = {0.0, 0.0, 0.0}, c[3] = {0.0, 0.0, 0.0};
+    CellSum<R> acc;
+    unsigned bad = 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const double v = (double)x[i];
-        double h = p.a[p.deg];
-        for (int q = p.deg - 1; q >= 0; --q) h = fma(h, v, p.a[q]);
-        nadd(s[0], c[0], h);
-        nadd(s[1], c[1], v);
-        s[2] += isfinite(v) ? 0.0 : 1.0;
+        const R v = x[i];
+        R h = s_a[p.deg];
+        for (int q = p.deg - 1; q >= 0; --q) h = h * v + s_a[q];
+        acc.add(h);
+        bad += isfinite(v) ? 0u : 1u;
     }
+    s[0] = acc.total();
+    s[2] = (double)bad;
     block_store<3>(s, c, part);
 }
 
+// index i on an axis of n points as a frequency in cycles per sample, Nyquist at +1/2
 __device__ __forceinline__ double fold(long long i, long long n)
 {
     const double f = (double)i / (double)n;
     return (f > 0.5) ? f - 1.0 : f;
 }
 
-// slot 0: sum over the full spectrum of |f|^2 |c-hat|^2 (f in cycles per sample)
+// fold(i, n)^2, from the reciprocal of n
+template <typename T> __device__ __forceinline__ T fold2(int i, int n, T inv_n)
+{
+    const T f = (T)(2 * i > n ? i - n : i) * inv_n;
+    return f * f;
+}
+
+// slot 0: sum over the full spectrum of |f|^2 |c-hat|^2 (f in cycles per sample).  A block takes
+// whole lines (z, kx) of the half spectrum, its threads the y positions; per-thread partial sums by
+// CellSum, combined with Neumaier compensation.  An FP32 spectrum's terms are formed in FP32.
 template <typename V> __global__ void k_grad(const V *__restrict__ st, Geom g, double *__restrict__ part)
 {
+    typedef decltype(V().x) T;
     double s[1] = {0.0}, c[1] = {0.0};
-    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < g.C;
-         idx += (long long)gridDim.x * blockDim.x) {
-        const long long z = idx / g.S, rem = idx - z * g.S;
-        const long long kx = rem / g.Y, y = rem - kx * g.Y;
-        const double fr = fold(y, g.Y), fc = fold(kx, g.X), fd = fold(z, g.Z);
-        const double w = (kx == 0 || 2 * kx == g.X) ? 1.0 : 2.0;
-        const V v = st[idx];
-        const double a = (double)v.x, b = (double)v.y;
-        nadd(s[0], c[0], w * (fr * fr + fc * fc + fd * fd) * (a * a + b * b));
+    CellSum<T> acc;
+    const T iy = (T)1 / (T)g.Y, ix = (T)1 / (T)g.X, iz = (T)1 / (T)g.Z;
+    const long long nlines = (long long)g.Z * g.KX;
+    for (long long line = blockIdx.x; line < nlines; line += gridDim.x) {
+        const int z = (int)(line / g.KX), kx = (int)(line - (long long)z * g.KX);
+        const T fl = fold2<T>(kx, g.X, ix) + fold2<T>(z, g.Z, iz);
+        const T w = (kx == 0 || 2 * kx == g.X) ? (T)1 : (T)2;
+        const V *row = st + line * g.Y;
+        for (int y = threadIdx.x; y < g.Y; y += blockDim.x) {
+            const V v = row[y];
+            acc.add(w * (fold2<T>(y, g.Y, iy) + fl) * (v.x * v.x + v.y * v.y));
+        }
     }
+    s[0] = acc.total();
     block_store<1>(s, c, part);
 }
 
-// one block: compensated sums of the block partials, slot by slot
+// one block: compensated sums of the block partials, slot by slot (each thread over its partials,
+// then a shuffle tree and the warps' results, all with Neumaier compensation)
 __global__ void k_finish(const double *__restrict__ part, int nblocks, double *__restrict__ out)
 {
-    __shared__ double sh_s[EN_THREADS], sh_c[EN_THREADS];
+    __shared__ double sh_s[EN_THREADS / 32], sh_c[EN_THREADS / 32];
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
     for (int k = 0; k < EN_SLOTS; ++k) {
         double s = 0.0, c = 0.0;
         for (int b = threadIdx.x; b < nblocks; b += blockDim.x) nadd(s, c, part[(long long)b * EN_SLOTS + k]);
-        sh_s[threadIdx.x] = s;
-        sh_c[threadIdx.x] = c;
+        for (int o = 16; o > 0; o >>= 1) {
+            const double so = __shfl_xor_sync(0xffffffffu, s, o), co = __shfl_xor_sync(0xffffffffu, c, o);
+            c += co;
+            nadd(s, c, so);
+        }
+        if (lane == 0) {
+            sh_s[wp] = s;
+            sh_c[wp] = c;
+        }
         __syncthreads();
         if (threadIdx.x == 0) {
             double ss = 0.0, cc = 0.0;
-            for (int q = 0; q < (int)blockDim.x; ++q) {
+            for (int q = 0; q < (int)blockDim.x / 32; ++q) {
                 cc += sh_c[q];
                 nadd(ss, cc, sh_s[q]);
             }
@@ -170,110 +232,183 @@ struct StrainParams {
     double C[81];
     double A[9];     // C : misfit
     double mis[9];   // misfit strain
-    int m, n;        // strain component of k_strain
     double scale;    // 1/N
 };
 
-// v = Gamma'(f)^-1 A f (0 at f = 0, as Displacements leaves the zero mode), Gaussian elimination
-// with partial pivoting
-__device__ void disp_dir(const StrainParams &p, const double f[3], double v[3])
+// The same constants in the precision the per-cell terms are formed in (the context's)
+template <typename T> struct StrainConsts {
+    T C[81];
+    T A[9];
+    T mis[9];
+    T scale;
+};
+
+template <typename T> StrainConsts<T> consts_of(const StrainParams &p)
 {
-    const double tol = 1e-10;
-    v[0] = v[1] = v[2] = 0.0;
-    if (fabs(f[0]) < tol && fabs(f[1]) < tol && fabs(f[2]) < tol) return;
-    double G[3][3], b[3];
+    StrainConsts<T> q;
+    for (int i = 0; i < 81; ++i) q.C[i] = (T)p.C[i];
+    for (int i = 0; i < 9; ++i) {
+        q.A[i] = (T)p.A[i];
+        q.mis[i] = (T)p.mis[i];
+    }
+    q.scale = (T)p.scale;
+    return q;
+}
+
+// v = Gamma'(f)^-1 A f (0 at f = 0, as Displacements leaves the zero mode), Gaussian elimination
+// with partial pivoting.  zero: f is the zero mode (the reference tests |f_i| < 1e-10; the indices
+// decide it here)
+template <typename T> __device__ __forceinline__ void disp_dir(const StrainConsts<T> &p, const T f[3], bool zero, T v[3])
+{
+    v[0] = v[1] = v[2] = (T)0;
+    if (zero) return;
+    T G[3][3], b[3];
+#pragma unroll
     for (int m = 0; m < 3; ++m) {
+#pragma unroll
         for (int n = 0; n < 3; ++n) {
-            double e = 0.0;
+            T e = (T)0;
+#pragma unroll
             for (int j = 0; j < 3; ++j)
+#pragma unroll
                 for (int l = 0; l < 3; ++l) e += p.C[m * 27 + j * 9 + n * 3 + l] * f[j] * f[l];
             G[m][n] = e;
         }
         b[m] = p.A[m * 3 + 0] * f[0] + p.A[m * 3 + 1] * f[1] + p.A[m * 3 + 2] * f[2];
     }
+#pragma unroll
     for (int c = 0; c < 3; ++c) {
         int best = c;
+        T bv = fabs(G[c][c]);
+#pragma unroll
         for (int r = c + 1; r < 3; ++r)
-            if (fabs(G[r][c]) > fabs(G[best][c])) best = r;
-        if (best != c) {
-            for (int k = 0; k < 3; ++k) {
-                const double t = G[c][k];
-                G[c][k] = G[best][k];
-                G[best][k] = t;
+            if (fabs(G[r][c]) > bv) {
+                bv = fabs(G[r][c]);
+                best = r;
             }
-            const double t = b[c];
-            b[c] = b[best];
-            b[best] = t;
-        }
+        // swap rows c and best (selects keep the arrays in registers)
+#pragma unroll
+        for (int r = c + 1; r < 3; ++r)
+            if (best == r) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const T t = G[c][k];
+                    G[c][k] = G[r][k];
+                    G[r][k] = t;
+                }
+                const T t = b[c];
+                b[c] = b[r];
+                b[r] = t;
+            }
+#pragma unroll
         for (int r = c + 1; r < 3; ++r) {
-            const double fct = G[r][c] / G[c][c];
+            const T fct = G[r][c] / G[c][c];
+#pragma unroll
             for (int k = c; k < 3; ++k) G[r][k] -= fct * G[c][k];
             b[r] -= fct * b[c];
         }
     }
+#pragma unroll
     for (int r = 2; r >= 0; --r) {
-        double s = b[r];
-        for (int q = r + 1; q < 3; ++q) s -= G[r][q] * v[q];
-        v[r] = s / G[r][r];
+        T t = b[r];
+#pragma unroll
+        for (int q = r + 1; q < 3; ++q) t -= G[r][q] * v[q];
+        v[r] = t / G[r][r];
     }
 }
 
-__device__ double strain_symbol(const StrainParams &p, const double f[3])
+// strain symbol s_mn(f) = (f~_n v_m + f~_m v_n)/2, f~ with its Nyquist components zeroed (Strain;
+// the reference tests ||f_i| - 1/2| < 1e-10, ny[i] is that test on the index)
+template <typename T> __device__ __forceinline__ T strain_symbol(const T f[3], const bool ny[3], const T v[3], int m, int n)
 {
-    double v[3];
-    disp_dir(p, f, v);
-    const double tol = 1e-10;
-    const double fm = (fabs(fabs(f[p.m]) - 0.5) < tol) ? 0.0 : f[p.m];
-    const double fn = (fabs(fabs(f[p.n]) - 0.5) < tol) ? 0.0 : f[p.n];
-    return 0.5 * (fn * v[p.m] + fm * v[p.n]);
+    const T fm = ny[m] ? (T)0 : f[m];
+    const T fn = ny[n] ? (T)0 : f[n];
+    return (T)0.5 * (fn * v[m] + fm * v[n]);
 }
 
-// out = x-hat * (s_mn(k) + s_mn(-k)) / 2 / N
-template <typename V> __global__ void k_strain(const V *__restrict__ xh, Geom g, int ndim, StrainParams p, V *__restrict__ out)
+// index i on an axis of n points in cycles per sample (Nyquist at +1/2), from the reciprocal of n
+template <typename T> __device__ __forceinline__ T fold_t(int i, int n, T inv_n) { return (T)(2 * i > n ? i - n : i) * inv_n; }
+
+// strain component q = 00 01 02 11 12 22 -> (m, n)
+__host__ __device__ constexpr int strain_m(int q) { return q < 3 ? 0 : q < 5 ? 1 : 2; }
+__host__ __device__ constexpr int strain_n(int q) { return q < 3 ? q : q < 5 ? q - 2 : 2; }
+
+// out[q] = x-hat * (s_mn(k) + s_mn(-k)) / 2 / N for the six components q = 00 01 02 11 12 22 (out[q] at
+// out + q C).  v(f) and v(-f) are solved once per mode for all six.  A block takes whole lines (z, kx)
+// of the half spectrum, its threads the y positions.
+template <typename V> __global__ void k_strain6(const V *__restrict__ xh, Geom g, int ndim, StrainConsts<decltype(V().x)> p,
+                                               V *__restrict__ out)
 {
-    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < g.C;
-         idx += (long long)gridDim.x * blockDim.x) {
-        const long long z = idx / g.S, rem = idx - z * g.S;
-        const long long kx = rem / g.Y, y = rem - kx * g.Y;
+    typedef decltype(V().x) T;
+    const T iy = (T)1 / (T)g.Y, ix = (T)1 / (T)g.X, iz = (T)1 / (T)g.Z;
+    const long long nlines = (long long)g.Z * g.KX;
+    for (long long line = blockIdx.x; line < nlines; line += gridDim.x) {
+        const int z = (int)(line / g.KX), kx = (int)(line - (long long)z * g.KX);
         // the reference's order: f[0] row, f[1] col, f[2] depth (0 in 2D: its 3-vector wrapper)
-        const double f[3] = {fold(y, g.Y), fold(kx, g.X), ndim == 3 ? fold(z, g.Z) : 0.0};
-        const double fmk[3] = {fold((g.Y - y) % g.Y, g.Y), fold((g.X - kx) % g.X, g.X),
-                               ndim == 3 ? fold((g.Z - z) % g.Z, g.Z) : 0.0};
-        const double s = 0.5 * (strain_symbol(p, f) + strain_symbol(p, fmk)) * p.scale;
-        V v = xh[idx];
-        v.x = (decltype(v.x))((double)v.x * s);
-        v.y = (decltype(v.y))((double)v.y * s);
-        out[idx] = v;
+        const T fx = fold_t<T>(kx, g.X, ix), fxm = fold_t<T>((g.X - kx) % g.X, g.X, ix);
+        const T fz = ndim == 3 ? fold_t<T>(z, g.Z, iz) : (T)0, fzm = ndim == 3 ? fold_t<T>((g.Z - z) % g.Z, g.Z, iz) : (T)0;
+        const bool nyx = 2 * kx == g.X, nyz = ndim == 3 && 2 * z == g.Z; // a mode and its partner alike
+        const bool zxz = kx == 0 && (ndim != 3 || z == 0);
+        for (int y = threadIdx.x; y < g.Y; y += blockDim.x) {
+            const T f[3] = {fold_t<T>(y, g.Y, iy), fx, fz};
+            const T fm[3] = {fold_t<T>((g.Y - y) % g.Y, g.Y, iy), fxm, fzm};
+            const bool ny[3] = {2 * y == g.Y, nyx, nyz};
+            T v[3], vm[3];
+            disp_dir<T>(p, f, zxz && y == 0, v);
+            disp_dir<T>(p, fm, zxz && y == 0, vm);
+            const long long idx = line * g.Y + y;
+            const V xv = xh[idx];
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                const T sq = (T)0.5 * (strain_symbol<T>(f, ny, v, strain_m(q), strain_n(q)) +
+                                      strain_symbol<T>(fm, ny, vm, strain_m(q), strain_n(q))) * p.scale;
+                V o;
+                o.x = xv.x * sq;
+                o.y = xv.y * sq;
+                out[(long long)q * g.C + idx] = o;
+            }
+        }
     }
 }
 
-// slot 0: sum of the energy density, slot 1: sum of x; components in the order 00 01 02 11 12 22
+// slot 0: sum of the energy density, slot 1: sum of x; components in the order 00 01 02 11 12 22.
+// The density is formed in the field's precision; per-thread sums by CellSum, combined with
+// Neumaier compensation.
 template <typename R>
-__global__ void k_elastic_density(const R *__restrict__ x, const R *__restrict__ strain, long long n, StrainParams p,
+__global__ void k_elastic_density(const R *__restrict__ x, const R *__restrict__ strain, long long n, StrainConsts<R> p,
                                   double *__restrict__ part)
 {
     double s[2] = {0.0, 0.0}, c[2] = {0.0, 0.0};
+    CellSum<R> ad, ax;
     const int ci[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const double xv = (double)x[i];
-        const bool inside = xv > 0.5;
-        double e[6];
+        const R xv = x[i];
+        const bool inside = xv > (R)0.5;
+        R e[6];
 #pragma unroll
-        for (int q = 0; q < 6; ++q) e[q] = (double)strain[q * n + i];
-        double E[3][3];
+        for (int q = 0; q < 6; ++q) e[q] = strain[q * n + i];
+        R E[3][3];
+#pragma unroll
         for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) E[a][b] = e[ci[a][b]] - (inside ? p.mis[a * 3 + b] : 0.0);
-        double d = 0.0;
+#pragma unroll
+            for (int b = 0; b < 3; ++b) E[a][b] = e[ci[a][b]] - (inside ? p.mis[a * 3 + b] : (R)0);
+        R d = (R)0;
+#pragma unroll
         for (int a = 0; a < 3; ++a)
+#pragma unroll
             for (int b = 0; b < 3; ++b) {
-                double t = 0.0;
+                R t = (R)0;
+#pragma unroll
                 for (int k = 0; k < 3; ++k)
+#pragma unroll
                     for (int l = 0; l < 3; ++l) t += p.C[a * 27 + b * 9 + k * 3 + l] * E[k][l];
                 d += E[a][b] * t;
             }
-        nadd(s[0], c[0], 0.5 * d);
-        nadd(s[1], c[1], xv);
+        ad.add((R)0.5 * d);
+        ax.add(xv);
     }
+    s[0] = ad.total();
+    s[1] = ax.total();
     block_store<2>(s, c, part);
 }
 
@@ -378,10 +513,10 @@ template <typename R> int elastic_energy_impl(gopf_ctx *ctx, int field, int indi
     int rc;
     if (!w->xh) {
         if ((rc = ck(ctx, gopf_malloc(&w->xh, sizeof(V) * g.C), "gopf_malloc"))) return rc;
-        if ((rc = ck(ctx, gopf_malloc(&w->bh, sizeof(V) * g.C), "gopf_malloc"))) return rc;
+        if ((rc = ck(ctx, gopf_malloc(&w->bh, sizeof(V) * 6 * g.C), "gopf_malloc"))) return rc;
         if ((rc = ck(ctx, gopf_malloc(&w->ind, sizeof(R) * g.N), "gopf_malloc"))) return rc;
         if ((rc = ck(ctx, gopf_malloc(&w->strain, sizeof(R) * 6 * g.N), "gopf_malloc"))) return rc;
-        ctx->dev_bytes += 2 * sizeof(V) * g.C + 7 * sizeof(R) * g.N;
+        ctx->dev_bytes += 7 * sizeof(V) * g.C + 7 * sizeof(R) * g.N;
     }
     // the indicator x in real space
     if ((rc = gopf_field_to_real(ctx, field, w->ind))) return rc;
@@ -401,26 +536,30 @@ template <typename R> int elastic_energy_impl(gopf_ctx *ctx, int field, int indi
     if (g.Z > 1 &&
         (rc = ck(ctx, launch_spass<R>(pbase<R>(ctx, true, PM_FWD, w->xh), ctx->LBz, ctx->stream), "z pass")))
         return rc;
-    // the six strains: symbol times x-hat / N, then the inverse transform to real rows
-    const int comps[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
+    // the six strains: symbols times x-hat / N (one kernel for all six), then each inverse
+    // transformed to real rows
     p.scale = 1.0 / (double)g.N;
+    const StrainConsts<R> pc = consts_of<R>(p);
+    {
+        const long long nl = (long long)g.Z * g.KX;
+        const unsigned nb = (unsigned)std::min<long long>(nl, (long long)EN_BLOCKS * 4);
+        k_strain6<V><<<nb, EN_THREADS, 0, ctx->stream>>>((const V *)w->xh, g, ctx->ndim, pc, (V *)w->bh);
+        if ((rc = ck(ctx, cudaGetLastError(), "strain symbols"))) return rc;
+    }
     for (int q = 0; q < 6; ++q) {
-        p.m = comps[q][0];
-        p.n = comps[q][1];
-        k_strain<V><<<grid_for(g.C), EN_THREADS, 0, ctx->stream>>>((const V *)w->xh, g, ctx->ndim, p, (V *)w->bh);
-        if ((rc = ck(ctx, cudaGetLastError(), "strain symbol"))) return rc;
+        V *bq = (V *)w->bh + (long long)q * g.C;
         if (g.Z > 1 &&
-            (rc = ck(ctx, launch_spass<R>(pbase<R>(ctx, true, PM_INV, w->bh), ctx->LBz, ctx->stream), "z pass")))
+            (rc = ck(ctx, launch_spass<R>(pbase<R>(ctx, true, PM_INV, bq), ctx->LBz, ctx->stream), "z pass")))
             return rc;
-        if ((rc = ck(ctx, launch_cpass<R>(pbase<R>(ctx, false, PM_INV, w->bh), ctx->LBy, ctx->stream), "y pass")))
+        if ((rc = ck(ctx, launch_cpass<R>(pbase<R>(ctx, false, PM_INV, bq), ctx->LBy, ctx->stream), "y pass")))
             return rc;
         XPassArgs<R> xo = xbase<R>(ctx);
         xo.in_mode = XIN_SPECTRAL;
-        xo.in = (const V *)w->bh;
+        xo.in = (const V *)bq;
         xo.rout = (R *)w->strain + (long long)q * g.N;
         if ((rc = ck(ctx, launch_xpass<R>(xo, ctx->LBx, ctx->stream), "x pass"))) return rc;
     }
-    k_elastic_density<R><<<EN_BLOCKS, EN_THREADS, 0, ctx->stream>>>((const R *)w->ind, (const R *)w->strain, g.N, p,
+    k_elastic_density<R><<<EN_BLOCKS, EN_THREADS, 0, ctx->stream>>>((const R *)w->ind, (const R *)w->strain, g.N, pc,
                                                                      w->part);
     if ((rc = ck(ctx, cudaGetLastError(), "energy density"))) return rc;
     double sums[EN_SLOTS];
