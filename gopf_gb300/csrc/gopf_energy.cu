@@ -36,6 +36,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
 #include "gopf_ctx.h"
 #include "gopf_kernels.cuh"
@@ -46,7 +47,7 @@ struct gopf_energy_work {
     double *part = nullptr; // block partials [EN_BLOCKS][EN_SLOTS]
     double *out = nullptr;  // finished sums [EN_SLOTS]
     void *xh = nullptr;     // half spectrum of the indicator
-    void *bh = nullptr;     // half spectrum of one strain component
+    void *bh = nullptr;     // half spectra of the six strain components (6 C)
     void *ind = nullptr;    // real indicator (N)
     void *strain = nullptr; // six real strain fields (6 N)
 };
@@ -56,6 +57,10 @@ int gopf_field_to_real(gopf_ctx *ctx, int f, void *dst);
 namespace {
 
 constexpr int EN_BLOCKS = 152 * 8;
+// k_bulk's grid: one wave of four blocks per SM on 152 SMs (four 16-byte loads in flight per
+// thread), so that its FP64 block epilogue (block_store) runs as few times as possible: FP64
+// instructions are expensive on this GPU
+constexpr int EN_BULK_BLOCKS = 152 * 4;
 constexpr int EN_SLOTS = 4;
 constexpr int EN_THREADS = 256;
 constexpr int EN_MAX_DEG = 12;
@@ -136,26 +141,52 @@ template <typename R> __global__ void k_bulk(const R *__restrict__ x, long long 
 #pragma unroll
         for (int q = 0; q <= EN_MAX_DEG; ++q) s_a[q] = (R)p.a[q];
     __syncthreads();
-    double s[3] = {0.0, 0.0, 0.0}, c[3] = {0.0, 0.0, 0.0};
+    double s[1] = {0.0}, c[1] = {0.0};
     CellSum<R> acc;
     unsigned bad = 0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const R v = x[i];
+    auto cell = [&](R v) {
         R h = s_a[p.deg];
         for (int q = p.deg - 1; q >= 0; --q) h = h * v + s_a[q];
         acc.add(h);
         bad += isfinite(v) ? 0u : 1u;
+    };
+    // 16-byte loads, four per thread in flight (the field is a cudaMalloc'd array: 16-byte aligned)
+    typedef typename std::conditional<sizeof(R) == 4, float4, double2>::type Q;
+    constexpr int PER = 16 / (int)sizeof(R), U = 4;
+    const Q *xq = reinterpret_cast<const Q *>(x);
+    const long long nq = n / PER, stride = (long long)gridDim.x * blockDim.x;
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (; i + (U - 1) * stride < nq; i += U * stride) {
+        Q w[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) w[u] = xq[i + u * stride];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const R *e = reinterpret_cast<const R *>(&w[u]);
+#pragma unroll
+            for (int k = 0; k < PER; ++k) cell(e[k]);
+        }
     }
+    for (; i < nq; i += stride) {
+        const Q w = xq[i];
+        const R *e = reinterpret_cast<const R *>(&w);
+#pragma unroll
+        for (int k = 0; k < PER; ++k) cell(e[k]);
+    }
+    for (long long j = nq * PER + blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += stride) cell(x[j]);
+    // the non-finite count as an integer, the polynomial sum compensated (slot 0)
+    __shared__ unsigned s_bad;
+    if (threadIdx.x == 0) s_bad = 0;
+    __syncthreads();
+    const unsigned wbad = __reduce_add_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0 && wbad) atomicAdd(&s_bad, wbad);
     s[0] = acc.total();
-    s[2] = (double)bad;
-    block_store<3>(s, c, part);
-}
-
-// index i on an axis of n points as a frequency in cycles per sample, Nyquist at +1/2
-__device__ __forceinline__ double fold(long long i, long long n)
-{
-    const double f = (double)i / (double)n;
-    return (f > 0.5) ? f - 1.0 : f;
+    block_store<1>(s, c, part); // its barrier orders the count above
+    if (threadIdx.x == 0) {
+        part[(long long)blockIdx.x * EN_SLOTS + 1] = 0.0;
+        part[(long long)blockIdx.x * EN_SLOTS + 2] = (double)s_bad;
+        part[(long long)blockIdx.x * EN_SLOTS + 3] = 0.0;
+    }
 }
 
 // fold(i, n)^2, from the reciprocal of n
@@ -175,48 +206,69 @@ template <typename V> __global__ void k_grad(const V *__restrict__ st, Geom g, d
     CellSum<T> acc;
     const T iy = (T)1 / (T)g.Y, ix = (T)1 / (T)g.X, iz = (T)1 / (T)g.Z;
     const long long nlines = (long long)g.Z * g.KX;
-    for (long long line = blockIdx.x; line < nlines; line += gridDim.x) {
-        const int z = (int)(line / g.KX), kx = (int)(line - (long long)z * g.KX);
-        const T fl = fold2<T>(kx, g.X, ix) + fold2<T>(z, g.Z, iz);
-        const T w = (kx == 0 || 2 * kx == g.X) ? (T)1 : (T)2;
-        const V *row = st + line * g.Y;
+    // four lines per round, so that each thread has four loads in flight
+    constexpr int U = 4;
+    for (long long l0 = blockIdx.x; l0 < nlines; l0 += U * (long long)gridDim.x) {
+        T fl[U], wt[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) { // a line's x and z frequencies and its Hermitian weight (0: no line)
+            const long long line = l0 + u * (long long)gridDim.x;
+            const int li = (int)line, z = li / g.KX, kx = li - z * g.KX; // Z KX < 2^31 lines
+            fl[u] = fold2<T>(kx, g.X, ix) + fold2<T>(z, g.Z, iz);
+            wt[u] = line >= nlines ? (T)0 : (kx == 0 || 2 * kx == g.X) ? (T)1 : (T)2;
+        }
         for (int y = threadIdx.x; y < g.Y; y += blockDim.x) {
-            const V v = row[y];
-            acc.add(w * (fold2<T>(y, g.Y, iy) + fl) * (v.x * v.x + v.y * v.y));
+            V v[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const long long line = l0 + u * (long long)gridDim.x;
+                v[u] = line < nlines ? st[line * g.Y + y] : V();
+            }
+            const T fy = fold2<T>(y, g.Y, iy);
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (wt[u] != (T)0) acc.add(wt[u] * (fy + fl[u]) * (v[u].x * v[u].x + v[u].y * v[u].y));
         }
     }
     s[0] = acc.total();
     block_store<1>(s, c, part);
 }
 
-// one block: compensated sums of the block partials, slot by slot (each thread over its partials,
-// then a shuffle tree and the warps' results, all with Neumaier compensation)
+// one block: compensated sums of the block partials, all slots at once (each thread over its
+// partials, then a shuffle tree and the warps' results, all with Neumaier compensation)
 __global__ void k_finish(const double *__restrict__ part, int nblocks, double *__restrict__ out)
 {
-    __shared__ double sh_s[EN_THREADS / 32], sh_c[EN_THREADS / 32];
+    __shared__ double sh_s[EN_THREADS / 32][EN_SLOTS], sh_c[EN_THREADS / 32][EN_SLOTS];
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-    for (int k = 0; k < EN_SLOTS; ++k) {
-        double s = 0.0, c = 0.0;
-        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) nadd(s, c, part[(long long)b * EN_SLOTS + k]);
-        for (int o = 16; o > 0; o >>= 1) {
-            const double so = __shfl_xor_sync(0xffffffffu, s, o), co = __shfl_xor_sync(0xffffffffu, c, o);
-            c += co;
-            nadd(s, c, so);
+    double s[EN_SLOTS], c[EN_SLOTS];
+#pragma unroll
+    for (int k = 0; k < EN_SLOTS; ++k) s[k] = c[k] = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
+#pragma unroll
+        for (int k = 0; k < EN_SLOTS; ++k) nadd(s[k], c[k], part[(long long)b * EN_SLOTS + k]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < EN_SLOTS; ++k) {
+            const double so = __shfl_xor_sync(0xffffffffu, s[k], o), co = __shfl_xor_sync(0xffffffffu, c[k], o);
+            c[k] += co;
+            nadd(s[k], c[k], so);
         }
-        if (lane == 0) {
-            sh_s[wp] = s;
-            sh_c[wp] = c;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < EN_SLOTS; ++k) {
+            sh_s[wp][k] = s[k];
+            sh_c[wp][k] = c[k];
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double ss = 0.0, cc = 0.0;
-            for (int q = 0; q < (int)blockDim.x / 32; ++q) {
-                cc += sh_c[q];
-                nadd(ss, cc, sh_s[q]);
-            }
-            out[k] = ss + cc;
+    __syncthreads();
+    if (threadIdx.x < EN_SLOTS) {
+        const int k = threadIdx.x;
+        double ss = 0.0, cc = 0.0;
+        for (int q = 0; q < (int)blockDim.x / 32; ++q) {
+            cc += sh_c[q][k];
+            nadd(ss, cc, sh_s[q][k]);
         }
-        __syncthreads();
+        out[k] = ss + cc;
     }
 }
 
@@ -343,7 +395,7 @@ template <typename V> __global__ void k_strain6(const V *__restrict__ xh, Geom g
     const T iy = (T)1 / (T)g.Y, ix = (T)1 / (T)g.X, iz = (T)1 / (T)g.Z;
     const long long nlines = (long long)g.Z * g.KX;
     for (long long line = blockIdx.x; line < nlines; line += gridDim.x) {
-        const int z = (int)(line / g.KX), kx = (int)(line - (long long)z * g.KX);
+        const int li = (int)line, z = li / g.KX, kx = li - z * g.KX; // Z KX < 2^31 lines
         // the reference's order: f[0] row, f[1] col, f[2] depth (0 in 2D: its 3-vector wrapper)
         const T fx = fold_t<T>(kx, g.X, ix), fxm = fold_t<T>((g.X - kx) % g.X, g.X, ix);
         const T fz = ndim == 3 ? fold_t<T>(z, g.Z, iz) : (T)0, fzm = ndim == 3 ? fold_t<T>((g.Z - z) % g.Z, g.Z, iz) : (T)0;
@@ -441,10 +493,10 @@ int prepare(gopf_ctx *ctx, int field)
 unsigned grid_for(long long n) { return (unsigned)std::min<long long>((n + EN_THREADS - 1) / EN_THREADS, EN_BLOCKS); }
 
 // finish the partials of the last kernel and copy the sums to the host (stream-synchronising)
-int finish(gopf_ctx *ctx, double *host)
+int finish(gopf_ctx *ctx, double *host, int nblocks = EN_BLOCKS)
 {
     gopf_energy_work *w = ctx->energy;
-    k_finish<<<1, EN_THREADS, 0, ctx->stream>>>(w->part, EN_BLOCKS, w->out);
+    k_finish<<<1, EN_THREADS, 0, ctx->stream>>>(w->part, nblocks, w->out);
     int rc;
     if ((rc = ck(ctx, cudaGetLastError(), "finish"))) return rc;
     if ((rc = ck(ctx, cudaMemcpyAsync(host, w->out, sizeof(double) * EN_SLOTS, cudaMemcpyDeviceToHost, ctx->stream),
@@ -489,10 +541,10 @@ template <typename R> int free_energy_impl(gopf_ctx *ctx, int field, const BulkP
     gopf_energy_work *w = ctx->energy;
     int rc;
     if ((rc = gopf_field_to_real(ctx, field, ctx->d_real))) return rc;
-    k_bulk<R><<<EN_BLOCKS, EN_THREADS, 0, ctx->stream>>>((const R *)ctx->d_real, g.N, p, w->part);
+    k_bulk<R><<<EN_BULK_BLOCKS, EN_THREADS, 0, ctx->stream>>>((const R *)ctx->d_real, g.N, p, w->part);
     if ((rc = ck(ctx, cudaGetLastError(), "bulk sums"))) return rc;
     double bulk[EN_SLOTS];
-    if ((rc = finish(ctx, bulk))) return rc;
+    if ((rc = finish(ctx, bulk, EN_BULK_BLOCKS))) return rc;
     k_grad<V><<<EN_BLOCKS, EN_THREADS, 0, ctx->stream>>>((const V *)field_state(ctx, field), g, w->part);
     if ((rc = ck(ctx, cudaGetLastError(), "gradient sums"))) return rc;
     double grad[EN_SLOTS];
