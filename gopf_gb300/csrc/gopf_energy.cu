@@ -57,9 +57,9 @@ int gopf_field_to_real(gopf_ctx *ctx, int f, void *dst);
 namespace {
 
 constexpr int EN_BLOCKS = 152 * 8;
-// k_bulk's grid: one wave of four blocks per SM on 152 SMs (four 16-byte loads in flight per
-// thread), so that its FP64 block epilogue (block_store) runs as few times as possible: FP64
-// instructions are expensive on this GPU
+// The summing kernels' grid: one wave of four blocks per SM on 152 SMs (with several loads in
+// flight per thread), so that their FP64 block epilogue (block_store) runs as few times as
+// possible: FP64 instructions are expensive on this GPU
 constexpr int EN_BULK_BLOCKS = 152 * 4;
 constexpr int EN_SLOTS = 4;
 constexpr int EN_THREADS = 256;
@@ -433,6 +433,7 @@ __global__ void k_elastic_density(const R *__restrict__ x, const R *__restrict__
     double s[2] = {0.0, 0.0}, c[2] = {0.0, 0.0};
     CellSum<R> ad, ax;
     const int ci[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+#pragma unroll 2 // two cells' seven loads in flight
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const R xv = x[i];
         const bool inside = xv > (R)0.5;
@@ -545,10 +546,10 @@ template <typename R> int free_energy_impl(gopf_ctx *ctx, int field, const BulkP
     if ((rc = ck(ctx, cudaGetLastError(), "bulk sums"))) return rc;
     double bulk[EN_SLOTS];
     if ((rc = finish(ctx, bulk, EN_BULK_BLOCKS))) return rc;
-    k_grad<V><<<EN_BLOCKS, EN_THREADS, 0, ctx->stream>>>((const V *)field_state(ctx, field), g, w->part);
+    k_grad<V><<<EN_BULK_BLOCKS, EN_THREADS, 0, ctx->stream>>>((const V *)field_state(ctx, field), g, w->part);
     if ((rc = ck(ctx, cudaGetLastError(), "gradient sums"))) return rc;
     double grad[EN_SLOTS];
-    if ((rc = finish(ctx, grad))) return rc;
+    if ((rc = finish(ctx, grad, EN_BULK_BLOCKS))) return rc;
     const double fourpi2 = 39.47841760435743;
     out3[0] = bulk[0];
     out3[1] = 0.5 * kappa * fourpi2 * grad[0] / (double)g.N;
@@ -611,11 +612,11 @@ template <typename R> int elastic_energy_impl(gopf_ctx *ctx, int field, int indi
         xo.rout = (R *)w->strain + (long long)q * g.N;
         if ((rc = ck(ctx, launch_xpass<R>(xo, ctx->LBx, ctx->stream), "x pass"))) return rc;
     }
-    k_elastic_density<R><<<EN_BLOCKS, EN_THREADS, 0, ctx->stream>>>((const R *)w->ind, (const R *)w->strain, g.N, pc,
+    k_elastic_density<R><<<EN_BULK_BLOCKS, EN_THREADS, 0, ctx->stream>>>((const R *)w->ind, (const R *)w->strain, g.N, pc,
                                                                      w->part);
     if ((rc = ck(ctx, cudaGetLastError(), "energy density"))) return rc;
     double sums[EN_SLOTS];
-    if ((rc = finish(ctx, sums))) return rc;
+    if ((rc = finish(ctx, sums, EN_BULK_BLOCKS))) return rc;
     if (!(sums[1] != 0.0)) return gopf_fail(ctx, GOPF_ERR_ARG, "the indicator sums to zero (no volume)");
     *out = sums[0] / sums[1];
     return GOPF_OK;
