@@ -143,62 +143,53 @@ __global__ void k_real_to_double(const R *__restrict__ in, double *__restrict__ 
         out[i] = (double)in[i];
 }
 
-// Final cross-block reduction (one block of 256 threads, a power of two).
-// Each thread folds a strided share of the block partials with Neumaier
-// compensation; a fixed-order tree then combines the 256 (sum, error) pairs,
-// adding each combination's rounding error to the error terms.  The result
-// is deterministic and the FP64 dependency chain is short (GB300 runs FP64
-// at a small fraction of its FP32 rate).
+// Final cross-block reduction: one block per slot (launched with RED_NONFINITE + 1 blocks of a
+// multiple of 32 threads).  Each thread folds a strided share of the block partials (the sums with
+// Neumaier compensation); a fixed-order shuffle tree and the warps' results in order then combine
+// the (sum, error) pairs, adding each combination's rounding error to the error terms.  The result
+// is deterministic, and the slots' FP64 dependency chains run on separate SMs (GB300 runs FP64 at a
+// small fraction of its FP32 rate).
 __global__ void k_finish_reduce(const double *__restrict__ part, int nblocks, double *__restrict__ out)
 {
-    __shared__ double s_sum[256], s_c[256], s_min[256], s_max[256], s_sq[256], s_sqc[256], s_nf[256];
-    double sum = 0, c = 0, sq = 0, sqc = 0, mn = INFINITY, mx = -INFINITY, nf = 0;
-    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
-        const double *p = part + (long long)b * RED_SLOTS;
-        double v = p[RED_SUM];
-        double t = sum + v;
-        c += (fabs(sum) >= fabs(v)) ? (sum - t) + v : (v - t) + sum;
-        sum = t;
-        v = p[RED_SUMSQ];
-        t = sq + v;
-        sqc += (fabs(sq) >= fabs(v)) ? (sq - t) + v : (v - t) + sq;
-        sq = t;
-        mn = fmin(mn, p[RED_MIN]);
-        mx = fmax(mx, p[RED_MAX]);
-        nf += p[RED_NONFINITE];
-    }
-    const int t = threadIdx.x;
-    s_sum[t] = sum;
-    s_c[t] = c;
-    s_sq[t] = sq;
-    s_sqc[t] = sqc;
-    s_min[t] = mn;
-    s_max[t] = mx;
-    s_nf[t] = nf;
-    __syncthreads();
-    for (int w = (int)blockDim.x / 2; w > 0; w >>= 1) {
-        if (t < w) {
-            const int o = t + w;
-            double a = s_sum[t], b = s_sum[o], r = a + b;
-            s_c[t] += s_c[o] + ((fabs(a) >= fabs(b)) ? (a - r) + b : (b - r) + a);
-            s_sum[t] = r;
-            a = s_sq[t];
-            b = s_sq[o];
-            r = a + b;
-            s_sqc[t] += s_sqc[o] + ((fabs(a) >= fabs(b)) ? (a - r) + b : (b - r) + a);
-            s_sq[t] = r;
-            s_min[t] = fmin(s_min[t], s_min[o]);
-            s_max[t] = fmax(s_max[t], s_max[o]);
-            s_nf[t] += s_nf[o];
+    // one block per slot (RED_SUM, RED_SUMSQ: Neumaier; RED_MIN, RED_MAX; RED_NONFINITE: a count), so
+    // that the slots' FP64 chains run on separate SMs
+    const int slot = blockIdx.x;
+    const bool comp = (slot == RED_SUM || slot == RED_SUMSQ);
+    double v = (slot == RED_MIN) ? INFINITY : (slot == RED_MAX) ? -INFINITY : 0.0, c = 0.0;
+    auto nsum = [](double &s, double &cc, double x) {
+        const double t = s + x;
+        cc += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
+        s = t;
+    };
+    auto combine = [&](double x, double xc) {
+        if (comp) {
+            c += xc;
+            nsum(v, c, x);
+        } else if (slot == RED_MIN) {
+            v = fmin(v, x);
+        } else if (slot == RED_MAX) {
+            v = fmax(v, x);
+        } else {
+            v += x;
         }
-        __syncthreads();
+    };
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) combine(part[(long long)b * RED_SLOTS + slot], 0.0);
+    for (int o = 16; o > 0; o >>= 1) {
+        const double x = __shfl_xor_sync(0xffffffffu, v, o), xc = __shfl_xor_sync(0xffffffffu, c, o);
+        combine(x, xc);
     }
-    if (t == 0) {
-        out[RED_SUM] = s_sum[0] + s_c[0];
-        out[RED_SUMSQ] = s_sq[0] + s_sqc[0];
-        out[RED_MIN] = s_min[0];
-        out[RED_MAX] = s_max[0];
-        out[RED_NONFINITE] = s_nf[0];
+    __shared__ double s_v[32], s_c[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        s_v[w] = v;
+        s_c[w] = c;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        v = (slot == RED_MIN) ? INFINITY : (slot == RED_MAX) ? -INFINITY : 0.0;
+        c = 0.0;
+        for (int q = 0; q < (int)blockDim.x / 32; ++q) combine(s_v[q], s_c[q]);
+        out[slot] = comp ? v + c : v;
     }
 }
 
@@ -1866,7 +1857,7 @@ static int reduce_all(gopf_ctx *ctx, double *host5, int f = 0)
                        ? xpass_red_blocks<float>(xargs_out<float>(ctx, nullptr, ctx->d_red, f), ctx->LBx)
                        : xpass_red_blocks<double>(xargs_out<double>(ctx, nullptr, ctx->d_red, f), ctx->LBx);
     if (nb > ctx->nred_blocks) return gopf_fail(ctx, GOPF_ERR_STATE, "reduction partials exceed their buffer");
-    k_finish_reduce<<<1, 256, 0, ctx->stream>>>(ctx->d_red, nb, ctx->d_redout);
+    k_finish_reduce<<<RED_NONFINITE + 1, 128, 0, ctx->stream>>>(ctx->d_red, nb, ctx->d_redout);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(host5, ctx->d_redout, sizeof(double) * 5, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));

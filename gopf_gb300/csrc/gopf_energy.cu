@@ -234,39 +234,31 @@ template <typename V> __global__ void k_grad(const V *__restrict__ st, Geom g, d
     block_store<1>(s, c, part);
 }
 
-// one block: compensated sums of the block partials, all slots at once (each thread over its
-// partials, then a shuffle tree and the warps' results, all with Neumaier compensation)
+// one block per slot (EN_SLOTS blocks, so that the FP64 chains run on separate SMs): compensated
+// sum of the block partials of that slot (each thread over its partials, then a shuffle tree and
+// the warps' results in order, all with Neumaier compensation)
 __global__ void k_finish(const double *__restrict__ part, int nblocks, double *__restrict__ out)
 {
-    __shared__ double sh_s[EN_THREADS / 32][EN_SLOTS], sh_c[EN_THREADS / 32][EN_SLOTS];
-    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-    double s[EN_SLOTS], c[EN_SLOTS];
+    __shared__ double sh_s[32], sh_c[32];
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, k = blockIdx.x;
+    double s = 0.0, c = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) nadd(s, c, part[(long long)b * EN_SLOTS + k]);
 #pragma unroll
-    for (int k = 0; k < EN_SLOTS; ++k) s[k] = c[k] = 0.0;
-    for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
-#pragma unroll
-        for (int k = 0; k < EN_SLOTS; ++k) nadd(s[k], c[k], part[(long long)b * EN_SLOTS + k]);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-        for (int k = 0; k < EN_SLOTS; ++k) {
-            const double so = __shfl_xor_sync(0xffffffffu, s[k], o), co = __shfl_xor_sync(0xffffffffu, c[k], o);
-            c[k] += co;
-            nadd(s[k], c[k], so);
-        }
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < EN_SLOTS; ++k) {
-            sh_s[wp][k] = s[k];
-            sh_c[wp][k] = c[k];
-        }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double so = __shfl_xor_sync(0xffffffffu, s, o), co = __shfl_xor_sync(0xffffffffu, c, o);
+        c += co;
+        nadd(s, c, so);
+    }
+    if (lane == 0) {
+        sh_s[wp] = s;
+        sh_c[wp] = c;
+    }
     __syncthreads();
-    if (threadIdx.x < EN_SLOTS) {
-        const int k = threadIdx.x;
+    if (threadIdx.x == 0) {
         double ss = 0.0, cc = 0.0;
         for (int q = 0; q < (int)blockDim.x / 32; ++q) {
-            cc += sh_c[q][k];
-            nadd(ss, cc, sh_s[q][k]);
+            cc += sh_c[q];
+            nadd(ss, cc, sh_s[q]);
         }
         out[k] = ss + cc;
     }
@@ -497,7 +489,7 @@ unsigned grid_for(long long n) { return (unsigned)std::min<long long>((n + EN_TH
 int finish(gopf_ctx *ctx, double *host, int nblocks = EN_BLOCKS)
 {
     gopf_energy_work *w = ctx->energy;
-    k_finish<<<1, EN_THREADS, 0, ctx->stream>>>(w->part, nblocks, w->out);
+    k_finish<<<EN_SLOTS, 128, 0, ctx->stream>>>(w->part, nblocks, w->out);
     int rc;
     if ((rc = ck(ctx, cudaGetLastError(), "finish"))) return rc;
     if ((rc = ck(ctx, cudaMemcpyAsync(host, w->out, sizeof(double) * EN_SLOTS, cudaMemcpyDeviceToHost, ctx->stream),
