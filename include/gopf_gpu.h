@@ -295,14 +295,16 @@ int gopf_point_values(gopf_ctx *ctx, int field_id, const long long *sites, int n
  *   F = sum_cells sum_p coefs[p] c^p + (kappa/2) sum_cells |grad c|^2
  * (0 <= ncoefs <= 13), the gradient part from the spectrum with |k|^2 = 4 pi^2 |Freq|^2, the symbol
  * the model's LAP uses.  coefs = {0, 0, -1/2, 0, 1/4} and kappa = gamma give the free energy of the
- * Cahn-Hilliard string of examples/cahnHilliard/main.go:33.  FP64 compensated sums; GOPF_ERR_NAN
- * when the field holds non-finite values.  No counterpart in the reference (its monitors are user
- * code). */
+ * Cahn-Hilliard string of examples/cahnHilliard/main.go:33.  Per-cell terms in the context's
+ * precision (an FP32 context adds them 16 at a time in FP32), FP64 sums with Neumaier compensation
+ * of the thread and block partials; GOPF_ERR_NAN when the field holds non-finite values.  No
+ * counterpart in the reference (its monitors are user code). */
 int gopf_free_energy(gopf_ctx *ctx, int field, const double *coefs, int ncoefs, double kappa, double *out3);
 /* elasticity.HomogeneousModulusEnergy (elasticity/linearElasticity.go:101-165) of the indicator x =
  * the field (indicator == 0) or its Indicator 3c^2 - 2c^3 (indicator != 0, pf/homoLinElast.go:10-12):
  * elastic energy over sum x, the misfit subtracted where x > 1/2.  C81 and misfit9 as in
- * gopf_register_elastic.  FP64 sums; the transforms run in the context's precision. */
+ * gopf_register_elastic.  The transforms and per-cell terms run in the context's precision, the
+ * sums in FP64 as for gopf_free_energy. */
 int gopf_elastic_energy(gopf_ctx *ctx, int field, int indicator, const double *C81, const double *misfit9,
                         double *out);
 
