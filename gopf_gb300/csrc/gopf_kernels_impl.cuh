@@ -62,12 +62,69 @@ template <typename R> __device__ __forceinline__ R poly_eval(const PwTable &pw, 
     return acc;
 }
 
-// block-wide reduction of RED_SLOTS doubles into red[block]
+// A thread's share of a real-space block reduction (sum, sum of squares, min, max, non-finite count).
+// FP32 values are summed in FP32 with Kahan compensation (the exact square's rounding residual
+// included), their extremes and count kept in FP32 and integers, and converted once; FP64 values
+// are summed plainly in FP64.  FP64 arithmetic runs at a small fraction of the FP32 rate on this GPU.
+template <typename R> struct RedAcc {
+    double s = 0.0, q = 0.0, mn = INFINITY, mx = -INFINITY, nf = 0.0;
+    __device__ __forceinline__ void add(R v)
+    {
+        s += v;
+        q += v * v;
+        mn = fmin(mn, v);
+        mx = fmax(mx, v);
+        nf += isfinite(v) ? 0.0 : 1.0;
+    }
+    __device__ __forceinline__ void add_sum(R v) { s += v; }
+    __device__ __forceinline__ void store(double *vals) const
+    {
+        vals[RED_SUM] = s;
+        vals[RED_SUMSQ] = q;
+        vals[RED_MIN] = mn;
+        vals[RED_MAX] = mx;
+        vals[RED_NONFINITE] = nf;
+    }
+};
+template <> struct RedAcc<float> {
+    float s = 0.f, sc = 0.f, q = 0.f, qc = 0.f, mn = INFINITY, mx = -INFINITY;
+    int nf = 0;
+    __device__ __forceinline__ static void kahan(float &acc, float &comp, float x)
+    {
+        const float y = x - comp;
+        const float t = acc + y;
+        comp = (t - acc) - y;
+        acc = t;
+    }
+    __device__ __forceinline__ void add(float v)
+    {
+        kahan(s, sc, v);
+        const float p = v * v;
+        kahan(q, qc, p);
+        qc -= fmaf(v, v, -p); // the square's rounding residual
+        mn = fminf(mn, v);
+        mx = fmaxf(mx, v);
+        nf += isfinite(v) ? 0 : 1;
+    }
+    __device__ __forceinline__ void add_sum(float v) { kahan(s, sc, v); }
+    __device__ __forceinline__ void store(double *vals) const
+    {
+        vals[RED_SUM] = (double)s - (double)sc;
+        vals[RED_SUMSQ] = (double)q - (double)qc;
+        vals[RED_MIN] = (double)mn;
+        vals[RED_MAX] = (double)mx;
+        vals[RED_NONFINITE] = (double)nf;
+    }
+};
+
+// block-wide reduction of the first NS of the RED_SLOTS doubles into red[block] (the others are
+// not written: nothing reads them)
+template <int NS = RED_NONFINITE + 1>
 __device__ __forceinline__ void block_reduce_store(double *vals, double *red, double *sh)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
-    for (int s = 0; s < RED_SLOTS; ++s) {
+    for (int s = 0; s < NS; ++s) {
         double v = vals[s];
         for (int o = 16; o > 0; o >>= 1) {
             double w = __shfl_xor_sync(0xffffffffu, v, o);
@@ -78,7 +135,7 @@ __device__ __forceinline__ void block_reduce_store(double *vals, double *red, do
         if (lane == 0) sh[warp * RED_SLOTS + s] = v;
     }
     __syncthreads();
-    if (threadIdx.x < RED_SLOTS) {
+    if (threadIdx.x < NS) {
         const int s = threadIdx.x;
         double v = sh[s];
         for (int w = 1; w < nw; ++w) {
@@ -326,16 +383,21 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
             vals[RED_MIN] = INFINITY;
             vals[RED_MAX] = -INFINITY;
             const V *F = A + a.redfield * tsz;
+            RedAcc<R> acc;
             for (int e = tid; e < npos; e += nt) {
                 int r0, r1;
                 tile_rows<LB>(odd, e, r0, r1);
-                vals[RED_SUM] += (r0 < nl ? (double)F[e].x : 0.0) + (r1 < nl ? (double)F[e].y : 0.0);
+                if (r0 < nl) acc.add_sum(F[e].x);
+                if (r1 < nl) acc.add_sum(F[e].y);
             }
+            double tmp[RED_SLOTS];
+            acc.store(tmp);
+            vals[RED_SUM] = tmp[RED_SUM];
             __shared__ double shredm[32 * RED_SLOTS];
-            block_reduce_store(vals, a.red, shredm);
+            block_reduce_store<1>(vals, a.red, shredm); // the volume integral: the sum only
         }
         for (int grp = 0; grp < mt.ngrp; ++grp) {
-            double gsum = 0.0;
+            RedAcc<R> gacc;
             for (int e = tid; e < npos; e += nt) {
                 R vx = (R)0, vy = (R)0;
                 for (int m = 0; m < mt.nmono[grp]; ++m) {
@@ -354,18 +416,15 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
                 if (a.red2 && grp == a.redgrp) {
                     int r0, r1;
                     tile_rows<LB>(odd, e, r0, r1);
-                    gsum += (r0 < nl ? (double)vx : 0.0) + (r1 < nl ? (double)vy : 0.0);
+                    if (r0 < nl) gacc.add_sum(vx);
+                    if (r1 < nl) gacc.add_sum(vy);
                 }
             }
             if (a.red2 && grp == a.redgrp) {
                 double vals[RED_SLOTS];
-#pragma unroll
-                for (int s = 0; s < RED_SLOTS; ++s) vals[s] = 0.0;
-                vals[RED_SUM] = gsum;
-                vals[RED_MIN] = INFINITY;
-                vals[RED_MAX] = -INFINITY;
+                gacc.store(vals);
                 __shared__ double shredm2[32 * RED_SLOTS];
-                block_reduce_store(vals, a.red2, shredm2);
+                block_reduce_store<1>(vals, a.red2, shredm2); // the indicator integral: the sum only
             }
             __syncthreads();
             xr2c_store<R, LB, PERB, NCT>(Bm, a.out[grp], sbase, nl, g, a.planH, twX);
@@ -399,27 +458,16 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
         }
     }
     if (a.red) {
-        double vals[RED_SLOTS];
-#pragma unroll
-        for (int s = 0; s < RED_SLOTS; ++s) vals[s] = 0.0;
-        vals[RED_MIN] = INFINITY;
-        vals[RED_MAX] = -INFINITY;
+        RedAcc<R> acc;
         for (int e = tid; e < npos; e += nt) {
             int r0, r1;
             tile_rows<LB>(odd, e, r0, r1);
             const V c = A[e];
-            const double cv[2] = {(double)c.x, (double)c.y};
-            const bool ok[2] = {r0 < nl, r1 < nl};
-#pragma unroll
-            for (int q = 0; q < 2; ++q)
-                if (ok[q]) {
-                    vals[RED_SUM] += cv[q];
-                    vals[RED_SUMSQ] += cv[q] * cv[q];
-                    vals[RED_MIN] = fmin(vals[RED_MIN], cv[q]);
-                    vals[RED_MAX] = fmax(vals[RED_MAX], cv[q]);
-                    vals[RED_NONFINITE] += isfinite(cv[q]) ? 0.0 : 1.0;
-                }
+            if (r0 < nl) acc.add(c.x);
+            if (r1 < nl) acc.add(c.y);
         }
+        double vals[RED_SLOTS];
+        acc.store(vals);
         __shared__ double shred[32 * RED_SLOTS];
         block_reduce_store(vals, a.red, shred);
     }
@@ -477,7 +525,7 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
     }
 
     for (int grp = 0; grp < a.ngrp_out; ++grp) {
-        double gsum = 0.0;
+        RedAcc<R> gacc;
         for (int e = tid; e < npos; e += nt) {
             const V c = A[e];
             const V r = a.identity ? c : cmk<V>(poly_eval<R>(a.pw, grp, c.x), poly_eval<R>(a.pw, grp, c.y));
@@ -485,18 +533,15 @@ __device__ __forceinline__ void xpass_tile(const XPassArgs<R> &a, int ty, int z)
             if (a.red2 && grp == a.redgrp) {
                 int r0, r1;
                 tile_rows<LB>(odd, e, r0, r1);
-                gsum += (r0 < nl ? (double)r.x : 0.0) + (r1 < nl ? (double)r.y : 0.0);
+                if (r0 < nl) gacc.add_sum(r.x);
+                if (r1 < nl) gacc.add_sum(r.y);
             }
         }
         if (a.red2 && grp == a.redgrp) {
             double vals[RED_SLOTS];
-#pragma unroll
-            for (int s2 = 0; s2 < RED_SLOTS; ++s2) vals[s2] = 0.0;
-            vals[RED_SUM] = gsum;
-            vals[RED_MIN] = INFINITY;
-            vals[RED_MAX] = -INFINITY;
+            gacc.store(vals);
             __shared__ double shred2[32 * RED_SLOTS];
-            block_reduce_store(vals, a.red2, shred2);
+            block_reduce_store<1>(vals, a.red2, shred2); // the indicator integral: the sum only
         }
         __syncthreads();
         xr2c_store<R, LB, PERB, NCT>(B, a.out[grp], sbase, nl, g, a.planH, twX);

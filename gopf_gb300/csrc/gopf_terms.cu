@@ -105,26 +105,55 @@ template <typename R> __global__ void k_elastic_symbol(Geom g, ElasticParams p, 
     }
 }
 
-// Neumaier sum of slot `slot` over the block partials (single thread).
-__device__ double sum_partials(const double *part, int nblocks, int slot)
+__device__ __forceinline__ void vc_nadd(double &s, double &c, double v)
 {
-    double s = 0.0, c = 0.0;
-    for (int b = 0; b < nblocks; ++b) {
-        const double v = part[(long long)b * RED_SLOTS + slot];
-        const double t = s + v;
-        c += (fabs(s) >= fabs(v)) ? (s - t) + v : (v - t) + s;
-        s = t;
-    }
-    return s + c;
+    const double t = s + v;
+    c += (fabs(s) >= fabs(v)) ? (s - t) + v : (v - t) + s;
+    s = t;
 }
 
-// vc = [lambda, current_integral, indicator_integral_prev, count, coef*lambda]
-__global__ void k_volcons_finalize(const double *__restrict__ red_field, const double *__restrict__ red_ind, int nblocks,
-                                   double dt, double coef, double *__restrict__ vc)
+// vc = [lambda, current_integral, indicator_integral_prev, count, coef*lambda].  One block of
+// VC_THREADS threads: each thread folds a strided share of both arrays' RED_SUM partials with
+// Neumaier compensation, a fixed-order shuffle tree and the warps' results in order combine them
+// (deterministic), and thread 0 updates the multiplier.  The FP64 dependency chain per thread stays
+// short however many x-pass blocks there are (FP64 runs at a small fraction of the FP32 rate here).
+constexpr int VC_THREADS = 256;
+__global__ void __launch_bounds__(VC_THREADS)
+    k_volcons_finalize(const double *__restrict__ red_field, const double *__restrict__ red_ind, int nblocks, double dt,
+                       double coef, double *__restrict__ vc)
 {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    const double I = sum_partials(red_field, nblocks, RED_SUM);
-    const double S = sum_partials(red_ind, nblocks, RED_SUM);
+    double si = 0.0, ci = 0.0, ss = 0.0, cs = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+        vc_nadd(si, ci, red_field[(long long)b * RED_SLOTS + RED_SUM]);
+        vc_nadd(ss, cs, red_ind[(long long)b * RED_SLOTS + RED_SUM]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double xi = __shfl_xor_sync(0xffffffffu, si, o), xci = __shfl_xor_sync(0xffffffffu, ci, o);
+        const double xs = __shfl_xor_sync(0xffffffffu, ss, o), xcs = __shfl_xor_sync(0xffffffffu, cs, o);
+        ci += xci;
+        vc_nadd(si, ci, xi);
+        cs += xcs;
+        vc_nadd(ss, cs, xs);
+    }
+    __shared__ double sh[4][VC_THREADS / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        sh[0][w] = si;
+        sh[1][w] = ci;
+        sh[2][w] = ss;
+        sh[3][w] = cs;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    double I = 0.0, Ic = 0.0, S = 0.0, Sc = 0.0;
+    for (int q = 0; q < (int)blockDim.x / 32; ++q) {
+        Ic += sh[1][q];
+        vc_nadd(I, Ic, sh[0][q]);
+        Sc += sh[3][q];
+        vc_nadd(S, Sc, sh[2][q]);
+    }
+    I += Ic;
+    S += Sc;
     const double count = vc[3];
     if (count == 1.0) {
         vc[1] = I; // IsFirstUpdate: remember the integral, keep the multiplier
@@ -205,6 +234,7 @@ int gopf_elastic_table(gopf_ctx *ctx)
 
 cudaError_t gopf_launch_volcons_finalize(gopf_ctx *ctx, const double *red_field, int nblocks)
 {
-    k_volcons_finalize<<<1, 32, 0, ctx->stream>>>(red_field, ctx->d_red2, nblocks, ctx->vc_dt, ctx->vc_coef, ctx->d_vc);
+    k_volcons_finalize<<<1, VC_THREADS, 0, ctx->stream>>>(red_field, ctx->d_red2, nblocks, ctx->vc_dt, ctx->vc_coef,
+                                                        ctx->d_vc);
     return cudaGetLastError();
 }
