@@ -72,7 +72,9 @@ def ellipsoid(N, a, b, c):
 
 
 @pytest.mark.parametrize("dims,prec,tol", [([32, 32, 32], "fp64", 1e-11), ([128, 128], "fp64", 1e-11),
-                                           ([32, 32, 32], "fp32", 1e-5), ([256, 256], "fp32", 1e-5)])
+                                           ([32, 32, 32], "fp32", 1e-5), ([256, 256], "fp32", 1e-5),
+                                           # an odd axis (no Nyquist mode) and an even one of 2^2 3 5
+                                           ([60, 45], "fp64", 1e-11), ([60, 45], "fp32", 1e-5)])
 def test_free_energy_matches_oracle(oracle, dims, prec, tol):
     from gopf_gb300.synthetic import uniform_field
 
@@ -145,7 +147,10 @@ def test_elastic_energy_eshelby(oracle, abc):
 
 
 @pytest.mark.parametrize("dims,prec,tol", [([32, 32, 32], "fp64", 1e-10), ([64, 64], "fp64", 1e-10),
-                                           ([32, 32, 32], "fp32", 1e-4)])
+                                           ([32, 32, 32], "fp32", 1e-4),
+                                           # Nyquist modes of a 2^3 3 axis; an odd axis
+                                           ([24, 24, 24], "fp64", 1e-10), ([30, 45], "fp64", 1e-10),
+                                           ([24, 24, 24], "fp32", 1e-4)])
 @pytest.mark.parametrize("indicator", [False, True])
 def test_elastic_energy_matches_oracle(oracle, dims, prec, tol, indicator):
     """A smooth random field (and its Indicator) under the cubic stiffness of the CH + elasticity
