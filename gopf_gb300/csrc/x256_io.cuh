@@ -91,11 +91,34 @@ __global__ void __launch_bounds__(NT, 3) k_x256_c2r(const XPassArgs<float> a, co
         for (int k = 0; k < RED_SLOTS; ++k) vals[k] = 0.0;
         vals[RED_SUM] = (double)s - (double)sc;
         vals[RED_SUMSQ] = (double)q - (double)qc;
-        vals[RED_MIN] = (double)mn;
-        vals[RED_MAX] = (double)mx;
-        vals[RED_NONFINITE] = (double)nf;
         __shared__ double shred[8 * RED_SLOTS];
-        block_reduce_store(vals, a.red, shred);
+        block_reduce_store<RED_SUMSQ + 1>(vals, a.red, shred); // the two sums in FP64
+        // the extremes in FP32 and the count in integers (exact), converted once per block
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            nf += __shfl_xor_sync(0xffffffffu, nf, o);
+        }
+        __shared__ float shmm[2][NT / 32];
+        __shared__ int shnf[NT / 32];
+        if ((tid & 31) == 0) {
+            shmm[0][tid >> 5] = mn;
+            shmm[1][tid >> 5] = mx;
+            shnf[tid >> 5] = nf;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            for (int w = 1; w < NT / 32; ++w) {
+                shmm[0][0] = fminf(shmm[0][0], shmm[0][w]);
+                shmm[1][0] = fmaxf(shmm[1][0], shmm[1][w]);
+                shnf[0] += shnf[w];
+            }
+            double *row = a.red + (long long)(blockIdx.y * gridDim.x + blockIdx.x) * RED_SLOTS;
+            row[RED_MIN] = (double)shmm[0][0];
+            row[RED_MAX] = (double)shmm[1][0];
+            row[RED_NONFINITE] = (double)shnf[0];
+        }
     }
     if (a.rout) {
 #pragma unroll
