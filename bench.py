@@ -41,7 +41,7 @@ METRIC = ("CH steps/s at 256³ FP32 vs GPU FP64 (rel-L2≤1e-4); FFT % of HBM pe
 UNIT = "steps/s"
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of each step kernel, from
 # one ncu capture on a GB300 of `python bench.py --steps 20 --warmup 17 --no-cpu-baseline --no-e2e
-# --no-precision` (the kernels' summaries under profiles/).  Bytes that a launch leaves in L2 are not
+# --no-precision --no-monitors` (the kernels' summaries under profiles/).  Bytes that a launch leaves in L2 are not
 # in these counts.
 NCU_TRAFFIC = {"zpass_update": 211.8e6, "xpass_pointwise": 72.6e6, "ypass_forward": 72.6e6,
                "ypass_inverse": 72.6e6}
@@ -252,7 +252,7 @@ def run_gpu(args):
     value = world * args.steps / (ms / 1000.0)
     mass1 = m.mass(0)
     finite = m.reduce(0, G.RED_NONFINITE) == 0
-    monitors = time_monitors(m, n)
+    monitors = None if args.no_monitors else time_monitors(m, n)
 
     # ---- per-kernel roofline (launch by launch, events on the same stream) ----
     prof = m.profile_step(20)
@@ -901,6 +901,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-monitors", action="store_true", help="skip the monitor timings (config.monitors)")
     ap.add_argument("--no-precision", action="store_true",
                     help="skip the FP64 rate and the FP32-vs-FP64 / FP64-vs-oracle checks of the default line")
     ap.add_argument("--precision-steps", type=int, default=1000,
